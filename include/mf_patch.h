@@ -1,0 +1,217 @@
+/*
+ * mf_patch.h - C ABI of the GB300 multi-fluid MHD patch integrator.
+ *
+ * The entry points replace the per-patch Godunov update of MHDAM / MS-FLUKSS
+ * (MHDAM-3.2.4).  Every pointer that names state (mf_fab::data, face fluxes,
+ * divB) is a DEVICE pointer unless the function name ends in _host.  No
+ * function aborts; every call returns an mf_status.  There are no globals:
+ * all physical and numerical parameters travel in mf_params, so runs with
+ * different parameters can share one GPU.
+ *
+ * Reference interfaces replaced (paths inside the MHDAM-3.2.4 tree):
+ *   mf_create / mf_destroy     the PatchMHDMF object set up by the driver
+ *                              (main/MHDAM.cpp:771-1046) and cloned per level
+ *                              (srcIdeal/PatchMHDMF.cpp:43-62).  The Fortran
+ *                              COMMON blocks /eos/ (srcIdeal/EosCommon.fh:39-40),
+ *                              /RiemSol/ (src/RSCommon.fh:6), /chargeexcm/
+ *                              (srcIdeal/ChargeExchange.fh:8-10) and /Dedner/
+ *                              become fields of mf_params.
+ *   mf_num_ghost               PatchMHDAM::numGhostCells (src/PatchMHDAM.cpp:280-286)
+ *   mf_set_current_time        PatchMHDAM::setCurrentTime (src/PatchMHDAM.cpp:272-276)
+ *   mf_set_dedner              EqSysMHDMF::setCorrectionPotential -> SETDEDNERCONST
+ *                              (src/DednerF.ChF:4-13)
+ *   mf_patch_update            PatchMHDAM::updateState (src/PatchMHDAM.H:252-260,
+ *                              src/PatchMHDAM.cpp:1192-1317)
+ *   mf_compute_dt              PatchMHDMF::computeDt (srcIdeal/PatchMHDMF.cpp:66-146)
+ *   mf_level_*                 AMRLevelIdealMHD::advance/step over all patches of a
+ *                              level: ghost exchange (srcIdeal/AMRLevelIdealMHD.cpp:772),
+ *                              the patch loop (:1203-1309) and the dt MIN
+ *                              reduction (:1517-1529) with the GLM Ch/Cp update
+ *                              (:1531-1548).
+ *
+ * Data layout (Chombo FArrayBox): one contiguous FP64 array per patch covering
+ * the valid box grown by mf_num_ghost() cells on every side, component-major,
+ * x fastest: data[((c*nz + (k-lo2))*ny + (j-lo1))*nx + (i-lo0)].  In 2D the
+ * third index range is lo[2] = hi[2] = 0.
+ */
+#ifndef MF_PATCH_H
+#define MF_PATCH_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum mf_status {
+  MF_OK = 0,
+  MF_ERR_BAD_ARG = 1,      /* invalid argument (sizes, boxes, null pointers) */
+  MF_ERR_OOM = 2,          /* device or host allocation failed */
+  MF_ERR_NONFINITE = 3,    /* a non-finite value appeared in the updated state */
+  MF_ERR_NEG_STATE = 4,    /* density or pressure <= 0 after the positivity fix, or dt <= 0 */
+  MF_ERR_TIMEOUT = 5,      /* a bounded wait on the device gave up */
+  MF_ERR_CUDA = 6,         /* a CUDA runtime call failed */
+  MF_ERR_UNSUPPORTED = 7   /* option combination not implemented */
+} mf_status;
+
+/* time_approximation (PatchMHDAM::eTimeApproximation) */
+enum { MF_TA_FIRST_ORDER = 0, MF_TA_HANCOCK = 1, MF_TA_RK2 = 2 };
+/* precision of reconstruction + Riemann fluxes; state, accumulation, pressure
+   recovery, positivity and charge exchange are always FP64 */
+enum { MF_PREC_FP64 = 0, MF_PREC_MIXED = 1 };
+/* physical (non-periodic) boundary treatment of primitive ghost cells */
+enum { MF_BC_NONE = 0, MF_BC_FARFIELD = 1 };
+/* limiter1D::eLimiters (src/limiter1D.H:17-28) */
+enum {
+  MF_LIM_CD = 0, MF_LIM_MINMOD = 1, MF_LIM_SUPERBEE = 2, MF_LIM_VANALBADA = 3,
+  MF_LIM_MC = 4, MF_LIM_HARMONIC = 5, MF_LIM_VANLEER = 9
+};
+
+#define MF_MAX_FLUIDS 5
+/* plasma (8) + psi (1) + 4 neutral fluids x 5 */
+#define MF_MAX_COMP 29
+
+typedef struct mf_box {
+  int lo[3];
+  int hi[3];   /* inclusive, cell-centred */
+} mf_box;
+
+typedef struct mf_fab {
+  double* data;  /* component-major, x fastest */
+  mf_box box;    /* box of the stored data (valid box + ghosts) */
+  int ncomp;
+} mf_fab;
+
+typedef struct mf_params {
+  int space_dim;           /* 2 or 3 */
+  int n_fluids;            /* 1 = MHD plasma only; 2..5 = plasma + (n_fluids-1) neutral H fluids */
+  int time_approximation;  /* MF_TA_FIRST_ORDER or MF_TA_RK2 */
+  int flux;                /* mhdam.flux: 0/1 Roe 8-wave arithmetic avg, 3 Roe 8-wave Roe avg,
+                              2/4 Rusanov (arith/Roe avg), 11/13 Roe 7-wave (arith/Roe avg) */
+  int divb_cleaning;       /* 0: none; 5: GLM/Dedner (Roe 7-wave + 2x2 (Bn,psi) flux) */
+  int use_8wave;           /* Powell 8-wave source (mhdam.8wave_use) */
+  int divb_method;         /* 0: none; 1: Bn = average of face states; 2: central */
+  int limiter[8];          /* limiter per plasma primitive rho,u,v,w,p,bx,by,bz */
+  int check_positivity;    /* first-order fallback where rho or p face values <= 0 */
+  int precision;           /* MF_PREC_FP64 or MF_PREC_MIXED */
+  double gamma;
+  double smallr, smallp;   /* EOS floors */
+  double entropy_fix;      /* del2 of the Roe solvers (mhdam.entropy_fix_coeff, default 0.3) */
+  double small_b;          /* smallB of the Roe solvers (1e-9) */
+  double dx;               /* uniform cell size */
+  double dedner_ch, dedner_cp;   /* current GLM speeds (SETDEDNERCONST) */
+  double factor_ch, factor_cp;   /* Ch = factor_ch*dx/dt, Cp = sqrt(Ch*dx/factor_cp) */
+  /* charge exchange between the plasma and each neutral fluid */
+  int charge_exchange;
+  double ce_scale_vel;     /* velocity scale applied before the cross-section */
+  double ce_sigma_scale;   /* cross-section scale (length x number density units) */
+  double ce_sigma_a, ce_sigma_b;   /* sigma(v) = scale*(a - b ln(v*scale_vel))^2 * damping */
+  double ce_damp_c, ce_damp_pow;   /* damping (1-exp(-c/(v*scale_vel)))^pow when c > 0 */
+  /* region classification (DEFINE_REGIONS_2F) */
+  double sun_center[3];    /* x = (i+1/2)dx - sun_center[0], ... */
+  double sun_r;            /* sunR */
+  double sun_v;            /* sunV; LIMSUN = 0.6 sunV */
+  double region_t_coeff;   /* TEMP = region_t_coeff * p / rho */
+  double region_tmlim;     /* TMLIM */
+  double region_zbot, region_ztop;  /* RegSafeZBot / RegSafeZTop (3D) */
+  /* inner solar-wind sphere reset after each stage (HELIOREINIT_DEFAULT, monopolar field) */
+  int reinit_sphere;
+  double reinit_r0;        /* Rinit */
+  double sun_int_bc_radius;
+  double sun_rho, sun_p, sun_b, sun_beta, dir_br;
+  /* problem domain (index space) */
+  int domain_lo[3], domain_hi[3];
+  int periodic[3];
+  int bc_kind;             /* MF_BC_NONE or MF_BC_FARFIELD */
+  double bc_plasma[8];     /* far-field plasma primitives rho,u,v,w,p,bx,by,bz */
+  double bc_neutral1[5];   /* far-field primitives of neutral fluid 1 */
+} mf_params;
+
+struct mf_ctx;
+struct mf_level;
+typedef struct mf_ctx mf_ctx;
+typedef struct mf_level mf_level;
+
+/* Defaults of the reference driver (main/MHDAM.cpp:647-666, 913-1046):
+   flux 1, minmod for all variables, first-order time, divB method 1, 8-wave on,
+   entropy fix 0.3, smallB 1e-9, gamma 5/3, periodic unit domain of 64 cells. */
+void mf_params_default(mf_params* p, int space_dim, int n_fluids);
+
+/* Number of conserved components for the parameter set (EqSysMHDMF ctor,
+   srcIdeal/EqSysMHDMF.cpp:11-48). */
+int mf_params_num_cons(const mf_params* p);
+
+mf_status mf_create(const mf_params* p, mf_ctx** out);
+void mf_destroy(mf_ctx* ctx);
+int mf_num_ghost(const mf_ctx* ctx);
+int mf_num_cons(const mf_ctx* ctx);
+mf_status mf_set_current_time(mf_ctx* ctx, double t);
+mf_status mf_set_dedner(mf_ctx* ctx, double ch, double cp);
+const char* mf_status_string(mf_status s);
+/* Upper bound (seconds) of every host wait on the device; a wait that runs
+   out returns MF_ERR_TIMEOUT and leaves the work queued.  Default 600 s or
+   the MF_WAIT_TIMEOUT_S environment variable.  No reference counterpart (the
+   reference has no device). */
+mf_status mf_set_wait_timeout(mf_ctx* ctx, double seconds);
+
+/* One time step of one patch, in place on U's valid box (same semantics as
+   PatchMHDAM::updateState).  U: device fab holding valid + mf_num_ghost()
+   ghost layers with the ghosts already filled by the caller.  F: NULL or an
+   array of space_dim device fabs sized on the faces of `valid` in each
+   direction (node-centred box), receiving the fluxes used for the update
+   (RK2: average of both stages).  divB: NULL or a device fab on `valid`.
+   new_dt / min_cell: patch minimum of dx / (max wave speed) and its cell
+   (first minimum in Fortran order).  stream: cudaStream_t or NULL.
+   The call returns after the stream has finished. */
+mf_status mf_patch_update(mf_ctx* ctx, mf_fab* U, const mf_box* valid, double dt,
+                          mf_fab* F, mf_fab* divB, double* new_dt, int min_cell[3],
+                          void* stream);
+
+/* dx / max wave speed minimum over `box` (PatchMHDMF::computeDt). */
+mf_status mf_compute_dt(mf_ctx* ctx, const mf_fab* U, const mf_box* box, double* dt,
+                        int min_cell[3], void* stream);
+
+/* A level: all patches of one refinement level resident on the device, one
+   contiguous allocation, patch p at offset mf_level_patch_offset(p) doubles. */
+mf_status mf_level_create(mf_ctx* ctx, int npatch, const mf_box* valid, mf_level** out);
+void mf_level_destroy(mf_level* lev);
+long long mf_level_num_doubles(const mf_level* lev);
+long long mf_level_patch_offset(const mf_level* lev, int patch);
+mf_status mf_level_patch_fab(const mf_level* lev, int patch, mf_fab* out);
+long long mf_level_num_cells(const mf_level* lev);
+/* Copy the whole level state host -> device / device -> host (layout as on the device). */
+mf_status mf_level_upload(mf_level* lev, const double* host, void* stream);
+mf_status mf_level_download(const mf_level* lev, double* host, void* stream);
+/* Fill ghost cells of every patch from the valid cells of its neighbours
+   (periodic images included); LevelData::exchange. */
+mf_status mf_level_exchange(mf_level* lev, void* stream);
+/* Level minimum of dx / max wave speed over the valid cells (the initial dt of
+   AMRLevelIdealMHD::computeInitialDt, srcIdeal/AMRLevelIdealMHD.cpp:2140-2200). */
+mf_status mf_level_compute_dt(mf_level* lev, double* dt, int* min_patch, int min_cell[3],
+                              void* stream);
+/* One time step of every patch of the level: exchange, both RK2 stages (or the
+   first-order stage), and the level minimum of the new dt.  The step is
+   replayed from a CUDA graph after its first call.  new_dt: level minimum of
+   dx/cmax (before cfl); min_patch/min_cell: where it was attained. */
+mf_status mf_level_step(mf_level* lev, double dt, double* new_dt, int* min_patch,
+                        int min_cell[3], void* stream);
+/* Enqueue one step without waiting: dt and the GLM speeds are read from the
+   device copy written by the previous step (dt = cfl * previous minimum;
+   Ch = factor_ch*dx/min, Cp = sqrt(Ch*dx/factor_cp)).  Call
+   mf_level_seed_dt first, mf_level_result to read the outcome. */
+mf_status mf_level_seed_dt(mf_level* lev, double dt, double cfl, void* stream);
+mf_status mf_level_step_async(mf_level* lev, void* stream);
+mf_status mf_level_result(mf_level* lev, double* new_dt, int* min_patch, int min_cell[3],
+                          void* stream);
+/* Kernel launches enqueued by one mf_level_step (for accounting). */
+int mf_level_launches_per_step(const mf_level* lev);
+
+/* Problem set-up on host fabs (PhysProblem::initialize):
+   Orszag-Tang vortex (problems/OrszagF.ChF:27-79) and the synthetic
+   heliosphere (uniform inflow + inner solar-wind sphere). */
+mf_status mf_init_orszag_host(const mf_params* p, mf_fab* U, const mf_box* box);
+mf_status mf_init_helio_host(const mf_params* p, const double* inflow_plasma,
+                             const double* inflow_neutrals, mf_fab* U, const mf_box* box);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,1170 @@
+// mf_capi.cu - C ABI of the GB300 patch integrator (include/mf_patch.h).
+//
+// mf_patch_update follows PatchMHDAM::updateState (src/PatchMHDAM.cpp:1192-1317)
+// on one device fab: RK2 stage 1 on box.grow(2), stage 2 on box, AVERAGESTATE,
+// computeDt.  mf_level_* keep every patch of a level resident in one device
+// allocation and replace the redundant stage-1 ghost computation by a
+// device-side exchange of the stage-1 state between the two stages; both give
+// the same results because every stage-1 ghost value equals the value its
+// owner patch computes for that cell.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <new>
+#include <thread>
+#include <vector>
+
+#include "mf_kernels.cuh"
+
+using mf::CopyReg;
+using mf::DevParams;
+using mf::DtPartial;
+using mf::StageBuffers;
+using mf::StageDesc;
+using mf::StepState;
+
+namespace {
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  cudaError_t ensure(size_t n) {
+    if (n <= bytes && p) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+    cudaError_t e = cudaMalloc(&p, n > 0 ? n : 16);
+    if (e == cudaSuccess) bytes = n;
+    return e;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+};
+
+struct PinnedBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  cudaError_t ensure(size_t n) {
+    if (n <= bytes && p) return cudaSuccess;
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    bytes = 0;
+    cudaError_t e = cudaMallocHost(&p, n > 0 ? n : 16);
+    if (e == cudaSuccess) bytes = n;
+    return e;
+  }
+  void release() {
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    bytes = 0;
+  }
+};
+
+int space_dim_ok(int sd) { return sd == 2 || sd == 3; }
+
+long long box_cells(const mf_box& b) {
+  long long n = 1;
+  for (int d = 0; d < 3; ++d) n *= (long long)(b.hi[d] - b.lo[d] + 1);
+  return n;
+}
+
+bool box_empty(const mf_box& b) {
+  for (int d = 0; d < 3; ++d)
+    if (b.hi[d] < b.lo[d]) return true;
+  return false;
+}
+
+mf_box box_grow(mf_box b, int n, int sd) {
+  for (int d = 0; d < sd; ++d) {
+    b.lo[d] -= n;
+    b.hi[d] += n;
+  }
+  return b;
+}
+
+mf_box box_isect(const mf_box& a, const mf_box& b) {
+  mf_box r;
+  for (int d = 0; d < 3; ++d) {
+    r.lo[d] = std::max(a.lo[d], b.lo[d]);
+    r.hi[d] = std::min(a.hi[d], b.hi[d]);
+  }
+  return r;
+}
+
+mf_box box_nodes(mf_box b, int d) {
+  b.hi[d] += 1;
+  return b;
+}
+
+bool box_contains(const mf_box& outer, const mf_box& inner) {
+  for (int d = 0; d < 3; ++d)
+    if (inner.lo[d] < outer.lo[d] || inner.hi[d] > outer.hi[d]) return false;
+  return true;
+}
+
+// Box & ProblemDomain: only the non-periodic directions are clipped.
+mf_box box_and_domain(mf_box b, const mf_params& p) {
+  for (int d = 0; d < p.space_dim; ++d) {
+    if (p.periodic[d]) continue;
+    b.lo[d] = std::max(b.lo[d], p.domain_lo[d]);
+    b.hi[d] = std::min(b.hi[d], p.domain_hi[d]);
+  }
+  return b;
+}
+
+void ext3(const mf_box& b, int n[3]) {
+  for (int d = 0; d < 3; ++d) n[d] = b.hi[d] - b.lo[d] + 1;
+}
+
+int num_cons(const mf_params& p) {
+  return 8 + (p.divb_cleaning == 5 ? 1 : 0) + (p.n_fluids - 1) * 5;
+}
+
+int num_ghost_of(const mf_params& p) {
+  if (p.time_approximation == MF_TA_RK2) return 4;
+  if (p.time_approximation == MF_TA_HANCOCK) return 3;
+  return 2;
+}
+
+mf_status validate_params(const mf_params& p) {
+  if (!space_dim_ok(p.space_dim)) return MF_ERR_BAD_ARG;
+  if (p.n_fluids < 1 || p.n_fluids > MF_MAX_FLUIDS) return MF_ERR_BAD_ARG;
+  if (!(p.gamma > 1.0) || !(p.dx > 0.0)) return MF_ERR_BAD_ARG;
+  if (p.time_approximation != MF_TA_RK2 && p.time_approximation != MF_TA_FIRST_ORDER)
+    return MF_ERR_UNSUPPORTED;
+  if (p.precision != MF_PREC_FP64 && p.precision != MF_PREC_MIXED) return MF_ERR_BAD_ARG;
+  if (p.divb_cleaning != 0 && p.divb_cleaning != 5) return MF_ERR_UNSUPPORTED;
+  if (p.divb_cleaning == 5) {
+    // main/MHDAM.cpp:1042-1046
+    if (p.use_8wave) return MF_ERR_UNSUPPORTED;
+    if (!(p.flux == 1 || p.flux == 3)) return MF_ERR_UNSUPPORTED;
+  }
+  if (p.flux == 5) return MF_ERR_UNSUPPORTED;
+  for (int v = 0; v < 8; ++v) {
+    int l = p.limiter[v];
+    if (!(l == MF_LIM_CD || l == MF_LIM_MINMOD || l == MF_LIM_SUPERBEE || l == MF_LIM_VANALBADA ||
+          l == MF_LIM_MC || l == MF_LIM_HARMONIC || l == MF_LIM_VANLEER))
+      return MF_ERR_UNSUPPORTED;
+  }
+  if (p.divb_method < 0 || p.divb_method > 2) return MF_ERR_BAD_ARG;
+  for (int d = 0; d < p.space_dim; ++d)
+    if (p.domain_hi[d] < p.domain_lo[d]) return MF_ERR_BAD_ARG;
+  for (int d = p.space_dim; d < 3; ++d)
+    if (p.domain_lo[d] != 0 || p.domain_hi[d] != 0) return MF_ERR_BAD_ARG;
+  return MF_OK;
+}
+
+DevParams make_dev(const mf_params& p) {
+  DevParams P;
+  std::memset(&P, 0, sizeof(P));
+  P.sd = p.space_dim;
+  P.nf = p.n_fluids;
+  P.glm = (p.divb_cleaning == 5) ? 1 : 0;
+  P.nc = num_cons(p);
+  P.irhon = 8 + P.glm;
+  // RiemannSolver::make (src/RiemannSolver.cpp:13-112)
+  if (P.glm) {
+    P.rs = mf::kRoe7;
+    P.aver = (p.flux == 3);
+  } else {
+    switch (p.flux) {
+      case 2: P.rs = mf::kRusanov; P.aver = 0; break;
+      case 3: P.rs = mf::kRoe8; P.aver = 1; break;
+      case 4: P.rs = mf::kRusanov; P.aver = 1; break;
+      case 11: P.rs = mf::kRoe7; P.aver = 0; break;
+      case 13: P.rs = mf::kRoe7; P.aver = 1; break;
+      default: P.rs = mf::kRoe8; P.aver = 0; break;
+    }
+  }
+  P.use8 = p.use_8wave ? 1 : 0;
+  P.divb_method = p.divb_method;
+  P.check_pos = p.check_positivity ? 1 : 0;
+  P.ce = (p.charge_exchange && p.n_fluids >= 2) ? 1 : 0;
+  P.reinit = p.reinit_sphere ? 1 : 0;
+  P.bc_kind = p.bc_kind;
+  for (int v = 0; v < 8; ++v) P.lim[v] = p.limiter[v];
+  for (int d = 0; d < 3; ++d) {
+    P.periodic[d] = (d < p.space_dim) ? (p.periodic[d] ? 1 : 0) : 1;
+    P.dlo[d] = p.domain_lo[d];
+    P.dhi[d] = p.domain_hi[d];
+  }
+  P.gamma = p.gamma;
+  P.hgamma = p.gamma - 1.0;
+  P.invhgamma = 1.0 / P.hgamma;
+  P.smallr = p.smallr;
+  P.smallp = p.smallp;
+  P.del2 = p.entropy_fix;
+  P.smallB = p.small_b;
+  P.dx = p.dx;
+  P.invdx = 1.0 / p.dx;
+  P.factor_ch = p.factor_ch;
+  P.factor_cp = p.factor_cp;
+  P.ce_scale_vel = p.ce_scale_vel;
+  P.ce_sigma_scale = p.ce_sigma_scale;
+  P.ce_a = p.ce_sigma_a;
+  P.ce_b = p.ce_sigma_b;
+  P.ce_damp_c = p.ce_damp_c;
+  P.ce_damp_pow = p.ce_damp_pow;
+  for (int d = 0; d < 3; ++d) P.sun_c[d] = p.sun_center[d];
+  P.sun_r = p.sun_r;
+  P.sun_v = p.sun_v;
+  P.t_coeff = p.region_t_coeff;
+  P.tmlim = p.region_tmlim;
+  P.zbot = p.region_zbot;
+  P.ztop = p.region_ztop;
+  P.r0 = p.reinit_r0;
+  P.rint = p.sun_int_bc_radius;
+  P.sun_rho = p.sun_rho;
+  P.sun_p = p.sun_p;
+  P.sun_b = p.sun_b;
+  P.sun_beta = p.sun_beta;
+  P.dir_br = p.dir_br;
+  for (int q = 0; q < 8; ++q) P.bc_plasma[q] = p.bc_plasma[q];
+  for (int q = 0; q < 5; ++q) P.bc_n1[q] = p.bc_neutral1[q];
+  return P;
+}
+
+double default_timeout() {
+  const char* e = std::getenv("MF_WAIT_TIMEOUT_S");
+  if (e) {
+    double v = std::atof(e);
+    if (v > 0) return v;
+  }
+  return 600.0;
+}
+
+// Bounded host wait: polls an event recorded on s; gives up after timeout_s.
+mf_status wait_stream(cudaStream_t s, double timeout_s) {
+  cudaEvent_t ev;
+  if (cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess) return MF_ERR_CUDA;
+  if (cudaEventRecord(ev, s) != cudaSuccess) {
+    cudaEventDestroy(ev);
+    return MF_ERR_CUDA;
+  }
+  auto t0 = std::chrono::steady_clock::now();
+  mf_status st = MF_OK;
+  for (;;) {
+    cudaError_t e = cudaEventQuery(ev);
+    if (e == cudaSuccess) break;
+    if (e != cudaErrorNotReady) {
+      st = MF_ERR_CUDA;
+      break;
+    }
+    double el = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    if (el >= timeout_s) {
+      st = MF_ERR_TIMEOUT;
+      break;
+    }
+    std::this_thread::sleep_for(std::chrono::microseconds(20));
+  }
+  cudaEventDestroy(ev);
+  return st;
+}
+
+mf_status flags_status(unsigned flags) {
+  if (flags & mf::kFlagNonFinite) return MF_ERR_NONFINITE;
+  if (flags & mf::kFlagBadDt) return MF_ERR_NEG_STATE;
+  return MF_OK;
+}
+
+#define MF_CHECK_CUDA(x)                 \
+  do {                                   \
+    cudaError_t e_ = (x);                \
+    if (e_ != cudaSuccess) {             \
+      if (e_ == cudaErrorMemoryAllocation) return MF_ERR_OOM; \
+      return MF_ERR_CUDA;                \
+    }                                    \
+  } while (0)
+
+}  // namespace
+
+struct mf_ctx {
+  mf_params p;
+  DevParams dp;
+  int ng = 0, nc = 0;
+  double time = 0.0;
+  double timeout = 600.0;
+  DevBuf pred, w, f1[3], bn1[3], f2[3], bn2[3], desc, partials, state;
+  PinnedBuf hdesc, hstate;
+};
+
+struct mf_level {
+  mf_ctx* ctx = nullptr;
+  int np = 0;
+  std::vector<mf_box> valid, fab;
+  std::vector<long long> off;
+  long long total = 0;
+  long long cells = 0;
+  DevBuf U, U1, W, F[3], Bn[3], desc, exfull, extwo, partials, state, state2;
+  int nfull = 0, ntwo = 0;
+  long long max_w = 0, max_f[3] = {0, 0, 0}, max_v = 0;
+  int nparts = 0;
+  PinnedBuf hstate;
+  cudaStream_t s = nullptr;
+  cudaGraphExec_t gsync = nullptr, gasync = nullptr;
+  int launches = 0;
+};
+
+extern "C" {
+
+void mf_params_default(mf_params* p, int space_dim, int n_fluids) {
+  if (!p) return;
+  std::memset(p, 0, sizeof(*p));
+  p->space_dim = space_dim;
+  p->n_fluids = n_fluids;
+  p->time_approximation = MF_TA_FIRST_ORDER;
+  p->flux = 1;
+  p->divb_cleaning = 0;
+  p->use_8wave = 1;
+  p->divb_method = 1;
+  for (int v = 0; v < 8; ++v) p->limiter[v] = MF_LIM_MINMOD;
+  p->check_positivity = 0;
+  p->precision = MF_PREC_FP64;
+  p->gamma = 5.0 / 3.0;
+  p->smallr = 1.0e-12;
+  p->smallp = 1.0e-12;
+  p->entropy_fix = 0.3;
+  p->small_b = 1.0e-9;
+  p->dx = 1.0 / 64.0;
+  p->dedner_ch = 1.0;
+  p->dedner_cp = 1.0;
+  p->factor_ch = 0.0;
+  p->factor_cp = 1.0;
+  p->ce_scale_vel = 1.0;
+  p->ce_sigma_scale = 1.0;
+  p->ce_sigma_a = 2.1;
+  p->ce_sigma_b = 0.092;
+  p->ce_damp_c = 0.0;
+  p->ce_damp_pow = 4.5;
+  p->region_zbot = -1.0e300;
+  p->region_ztop = 1.0e300;
+  p->region_tmlim = 1.0e300;
+  p->sun_int_bc_radius = 1.0;
+  p->dir_br = 1.0;
+  for (int d = 0; d < 3; ++d) {
+    p->domain_lo[d] = 0;
+    p->domain_hi[d] = (d < space_dim) ? 63 : 0;
+    p->periodic[d] = 1;
+  }
+  p->bc_kind = MF_BC_NONE;
+}
+
+int mf_params_num_cons(const mf_params* p) { return p ? num_cons(*p) : 0; }
+
+const char* mf_status_string(mf_status s) {
+  switch (s) {
+    case MF_OK: return "ok";
+    case MF_ERR_BAD_ARG: return "bad argument";
+    case MF_ERR_OOM: return "out of memory";
+    case MF_ERR_NONFINITE: return "non-finite state";
+    case MF_ERR_NEG_STATE: return "non-positive state or time step";
+    case MF_ERR_TIMEOUT: return "device wait timed out";
+    case MF_ERR_CUDA: return "CUDA error";
+    case MF_ERR_UNSUPPORTED: return "unsupported option";
+  }
+  return "unknown status";
+}
+
+mf_status mf_create(const mf_params* p, mf_ctx** out) {
+  if (!p || !out) return MF_ERR_BAD_ARG;
+  *out = nullptr;
+  mf_status st = validate_params(*p);
+  if (st != MF_OK) return st;
+  mf_ctx* c = new (std::nothrow) mf_ctx();
+  if (!c) return MF_ERR_OOM;
+  c->p = *p;
+  c->dp = make_dev(*p);
+  c->ng = num_ghost_of(*p);
+  c->nc = num_cons(*p);
+  c->timeout = default_timeout();
+  *out = c;
+  return MF_OK;
+}
+
+void mf_destroy(mf_ctx* c) {
+  if (!c) return;
+  c->pred.release();
+  c->w.release();
+  for (int d = 0; d < 3; ++d) {
+    c->f1[d].release();
+    c->bn1[d].release();
+    c->f2[d].release();
+    c->bn2[d].release();
+  }
+  c->desc.release();
+  c->partials.release();
+  c->state.release();
+  c->hdesc.release();
+  c->hstate.release();
+  delete c;
+}
+
+int mf_num_ghost(const mf_ctx* c) { return c ? c->ng : -1; }
+int mf_num_cons(const mf_ctx* c) { return c ? c->nc : -1; }
+
+mf_status mf_set_current_time(mf_ctx* c, double t) {
+  if (!c) return MF_ERR_BAD_ARG;
+  c->time = t;
+  return MF_OK;
+}
+
+mf_status mf_set_dedner(mf_ctx* c, double ch, double cp) {
+  if (!c || !(ch > 0.0) || !(cp > 0.0)) return MF_ERR_BAD_ARG;
+  c->p.dedner_ch = ch;
+  c->p.dedner_cp = cp;
+  return MF_OK;
+}
+
+mf_status mf_set_wait_timeout(mf_ctx* c, double seconds) {
+  if (!c || !(seconds >= 0.0)) return MF_ERR_BAD_ARG;
+  c->timeout = seconds;
+  return MF_OK;
+}
+
+static mf_status check_fab(const mf_ctx* c, const mf_fab* U, const mf_box* valid) {
+  if (!U || !U->data || !valid) return MF_ERR_BAD_ARG;
+  if (U->ncomp != c->nc) return MF_ERR_BAD_ARG;
+  for (int d = c->p.space_dim; d < 3; ++d)
+    if (valid->lo[d] != 0 || valid->hi[d] != 0 || U->box.lo[d] != 0 || U->box.hi[d] != 0)
+      return MF_ERR_BAD_ARG;
+  if (box_empty(*valid)) return MF_ERR_BAD_ARG;
+  // the patch lies inside the problem domain in every non-periodic direction
+  for (int d = 0; d < c->p.space_dim; ++d)
+    if (!c->p.periodic[d] &&
+        (valid->lo[d] < c->p.domain_lo[d] || valid->hi[d] > c->p.domain_hi[d]))
+      return MF_ERR_BAD_ARG;
+  mf_box need = box_grow(*valid, c->ng, c->p.space_dim);
+  if (!box_contains(U->box, need)) return MF_ERR_BAD_ARG;
+  if (box_cells(U->box) * c->nc >= (1LL << 31)) return MF_ERR_BAD_ARG;
+  return MF_OK;
+}
+
+static void fill_desc(StageDesc& D, const mf_box& fab, const mf_box& vbox, const mf_box& wbox) {
+  std::memset(&D, 0, sizeof(D));
+  for (int d = 0; d < 3; ++d) {
+    D.flo[d] = fab.lo[d];
+    D.fn[d] = fab.hi[d] - fab.lo[d] + 1;
+    D.vlo[d] = vbox.lo[d];
+    D.vn[d] = vbox.hi[d] - vbox.lo[d] + 1;
+    D.wlo[d] = wbox.lo[d];
+    D.wn[d] = wbox.hi[d] - wbox.lo[d] + 1;
+  }
+}
+
+mf_status mf_patch_update(mf_ctx* c, mf_fab* U, const mf_box* valid, double dt, mf_fab* F,
+                          mf_fab* divB, double* new_dt, int min_cell[3], void* stream) {
+  if (!c) return MF_ERR_BAD_ARG;
+  mf_status st = check_fab(c, U, valid);
+  if (st != MF_OK) return st;
+  if (!(dt > 0.0) || !std::isfinite(dt)) return MF_ERR_BAD_ARG;
+  const mf_params& p = c->p;
+  const int sd = p.space_dim, nc = c->nc;
+  const int mixed = (p.precision == MF_PREC_MIXED);
+  const size_t rs = mixed ? sizeof(float) : sizeof(double);
+  const bool rk2 = (p.time_approximation == MF_TA_RK2);
+  cudaStream_t s = (cudaStream_t)stream;
+  const long long fabn = box_cells(U->box);
+
+  mf_box v2 = box_and_domain(*valid, p);
+  mf_box v1 = rk2 ? box_and_domain(box_grow(*valid, 2, sd), p) : v2;
+  mf_box w1 = box_isect(box_grow(v1, 2, sd), U->box);
+  mf_box w2 = box_isect(box_grow(v2, 2, sd), U->box);
+  if (divB && divB->data && !box_contains(divB->box, v2)) return MF_ERR_BAD_ARG;
+  if (F) {
+    for (int d = 0; d < sd; ++d)
+      if (!F[d].data || F[d].ncomp != nc || !box_contains(F[d].box, box_nodes(v2, d)))
+        return MF_ERR_BAD_ARG;
+  }
+
+  MF_CHECK_CUDA(c->w.ensure(sizeof(double) * fabn * nc));
+  if (rk2) MF_CHECK_CUDA(c->pred.ensure(sizeof(double) * fabn * nc));
+  for (int d = 0; d < sd; ++d) {
+    MF_CHECK_CUDA(c->f1[d].ensure(rs * box_cells(box_nodes(v1, d)) * nc));
+    MF_CHECK_CUDA(c->bn1[d].ensure(rs * box_cells(box_nodes(v1, d))));
+    if (rk2) {
+      MF_CHECK_CUDA(c->f2[d].ensure(rs * box_cells(box_nodes(v2, d)) * nc));
+      MF_CHECK_CUDA(c->bn2[d].ensure(rs * box_cells(box_nodes(v2, d))));
+    }
+  }
+  MF_CHECK_CUDA(c->desc.ensure(sizeof(StageDesc) * 2));
+  MF_CHECK_CUDA(c->hdesc.ensure(sizeof(StageDesc) * 2));
+  MF_CHECK_CUDA(c->state.ensure(sizeof(StepState)));
+  MF_CHECK_CUDA(c->hstate.ensure(sizeof(StepState)));
+  const long long vmax = box_cells(v2);
+  const long long nparts = (vmax + 127) / 128 + 1;
+  MF_CHECK_CUDA(c->partials.ensure(sizeof(DtPartial) * nparts));
+
+  StageDesc* hd = (StageDesc*)c->hdesc.p;
+  fill_desc(hd[0], U->box, v1, w1);
+  fill_desc(hd[1], U->box, v2, w2);
+  StepState* hs = (StepState*)c->hstate.p;
+  std::memset(hs, 0, sizeof(*hs));
+  hs->dt = dt;
+  hs->ch = p.dedner_ch;
+  hs->cp = p.dedner_cp;
+  hs->cfl = 0.0;
+  StageDesc* dd = (StageDesc*)c->desc.p;
+  StepState* ds = (StepState*)c->state.p;
+  MF_CHECK_CUDA(cudaMemcpyAsync(dd, hd, sizeof(StageDesc) * 2, cudaMemcpyHostToDevice, s));
+  MF_CHECK_CUDA(cudaMemcpyAsync(ds, hs, sizeof(StepState), cudaMemcpyHostToDevice, s));
+
+  long long mf1[3] = {0, 0, 0}, mf2[3] = {0, 0, 0};
+  for (int d = 0; d < sd; ++d) {
+    mf1[d] = box_cells(box_nodes(v1, d));
+    mf2[d] = box_cells(box_nodes(v2, d));
+  }
+  int nb = 0;
+  DtPartial* parts = (DtPartial*)c->partials.p;
+  StageBuffers B;
+  std::memset(&B, 0, sizeof(B));
+  B.w = (double*)c->w.p;
+  if (rk2) {
+    MF_CHECK_CUDA(cudaMemcpyAsync(c->pred.p, U->data, sizeof(double) * fabn * nc,
+                                  cudaMemcpyDeviceToDevice, s));
+    B.uin = U->data;
+    B.uout = (double*)c->pred.p;
+    for (int d = 0; d < 3; ++d) {
+      B.f[d] = c->f1[d].p;
+      B.bn[d] = c->bn1[d].p;
+    }
+    MF_CHECK_CUDA(mf::launch_stage(c->dp, mixed, B, dd, 1, box_cells(w1), mf1, box_cells(v1), 0,
+                                   1.0, ds, parts, &nb, s));
+    B.uin = (double*)c->pred.p;
+    B.uout = U->data;
+    B.uold = U->data;
+    for (int d = 0; d < 3; ++d) {
+      B.f[d] = c->f2[d].p;
+      B.bn[d] = c->bn2[d].p;
+    }
+    if (divB && divB->data) {
+      B.divb = divB->data;
+      for (int d = 0; d < 3; ++d) {
+        B.divb_lo[d] = divB->box.lo[d];
+        B.divb_n[d] = divB->box.hi[d] - divB->box.lo[d] + 1;
+      }
+    }
+    MF_CHECK_CUDA(mf::launch_stage(c->dp, mixed, B, dd + 1, 1, box_cells(w2), mf2, box_cells(v2),
+                                   mf::kStageAverage | mf::kStageDt, 0.5, ds, parts, &nb, s));
+  } else {
+    B.uin = U->data;
+    B.uout = U->data;
+    for (int d = 0; d < 3; ++d) {
+      B.f[d] = c->f1[d].p;
+      B.bn[d] = c->bn1[d].p;
+    }
+    if (divB && divB->data) {
+      B.divb = divB->data;
+      for (int d = 0; d < 3; ++d) {
+        B.divb_lo[d] = divB->box.lo[d];
+        B.divb_n[d] = divB->box.hi[d] - divB->box.lo[d] + 1;
+      }
+    }
+    MF_CHECK_CUDA(mf::launch_stage(c->dp, mixed, B, dd + 1, 1, box_cells(w2), mf2, box_cells(v2),
+                                   mf::kStageDt, 1.0, ds, parts, &nb, s));
+  }
+  MF_CHECK_CUDA(mf::launch_finalize(c->dp, parts, nb, ds, 0, s));
+  if (F) {
+    const void* f2p[3] = {nullptr, nullptr, nullptr};
+    const void* f1p[3] = {nullptr, nullptr, nullptr};
+    double* fo[3] = {nullptr, nullptr, nullptr};
+    int f2lo[3][3], f2n[3][3], f1lo[3][3], f1n[3][3], olo[3][3], on[3][3];
+    std::memset(f2lo, 0, sizeof(f2lo));
+    std::memset(f2n, 0, sizeof(f2n));
+    std::memset(f1lo, 0, sizeof(f1lo));
+    std::memset(f1n, 0, sizeof(f1n));
+    std::memset(olo, 0, sizeof(olo));
+    std::memset(on, 0, sizeof(on));
+    for (int d = 0; d < sd; ++d) {
+      mf_box b2 = box_nodes(v2, d), b1 = box_nodes(v1, d);
+      f2p[d] = rk2 ? c->f2[d].p : c->f1[d].p;
+      f1p[d] = rk2 ? c->f1[d].p : nullptr;
+      fo[d] = F[d].data;
+      for (int e = 0; e < 3; ++e) {
+        f2lo[d][e] = b2.lo[e];
+        f2n[d][e] = b2.hi[e] - b2.lo[e] + 1;
+        f1lo[d][e] = b1.lo[e];
+        f1n[d][e] = b1.hi[e] - b1.lo[e] + 1;
+        olo[d][e] = b2.lo[e];
+        on[d][e] = b2.hi[e] - b2.lo[e] + 1;
+      }
+      // the output fab may be larger than the faces of the valid box
+      if (!(F[d].box.lo[0] == b2.lo[0] && F[d].box.lo[1] == b2.lo[1] &&
+            F[d].box.lo[2] == b2.lo[2] && F[d].box.hi[0] == b2.hi[0] &&
+            F[d].box.hi[1] == b2.hi[1] && F[d].box.hi[2] == b2.hi[2]))
+        return MF_ERR_BAD_ARG;
+    }
+    MF_CHECK_CUDA(mf::launch_flux_out(mixed, sd, nc, f2p, f2lo, f2n, f1p, f1lo, f1n, fo, olo, on,
+                                      s));
+  }
+  MF_CHECK_CUDA(cudaMemcpyAsync(hs, ds, sizeof(StepState), cudaMemcpyDeviceToHost, s));
+  st = wait_stream(s, c->timeout);
+  if (st != MF_OK) return st;
+  if (new_dt) *new_dt = hs->dt_min;
+  if (min_cell) {
+    int n[3];
+    ext3(*valid, n);
+    int idx = hs->min_idx;
+    if (idx < 0 || idx == 0x7fffffff) idx = 0;
+    min_cell[0] = valid->lo[0] + idx % n[0];
+    min_cell[1] = valid->lo[1] + (idx / n[0]) % n[1];
+    min_cell[2] = valid->lo[2] + idx / (n[0] * n[1]);
+  }
+  return flags_status(hs->flags);
+}
+
+mf_status mf_compute_dt(mf_ctx* c, const mf_fab* U, const mf_box* box, double* dt,
+                        int min_cell[3], void* stream) {
+  if (!c || !U || !U->data || !box || box_empty(*box) || !box_contains(U->box, *box))
+    return MF_ERR_BAD_ARG;
+  if (U->ncomp != c->nc) return MF_ERR_BAD_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  const long long nv = box_cells(*box);
+  MF_CHECK_CUDA(c->desc.ensure(sizeof(StageDesc) * 2));
+  MF_CHECK_CUDA(c->hdesc.ensure(sizeof(StageDesc) * 2));
+  MF_CHECK_CUDA(c->state.ensure(sizeof(StepState)));
+  MF_CHECK_CUDA(c->hstate.ensure(sizeof(StepState)));
+  MF_CHECK_CUDA(c->partials.ensure(sizeof(DtPartial) * ((nv + 127) / 128 + 1)));
+  StageDesc* hd = (StageDesc*)c->hdesc.p;
+  fill_desc(hd[0], U->box, *box, *box);
+  StepState* hs = (StepState*)c->hstate.p;
+  std::memset(hs, 0, sizeof(*hs));
+  StageDesc* dd = (StageDesc*)c->desc.p;
+  StepState* ds = (StepState*)c->state.p;
+  DtPartial* parts = (DtPartial*)c->partials.p;
+  MF_CHECK_CUDA(cudaMemcpyAsync(dd, hd, sizeof(StageDesc), cudaMemcpyHostToDevice, s));
+  MF_CHECK_CUDA(cudaMemcpyAsync(ds, hs, sizeof(StepState), cudaMemcpyHostToDevice, s));
+  int nb = 0;
+  MF_CHECK_CUDA(mf::launch_dt(c->dp, U->data, dd, 1, nv, parts, &nb, s));
+  MF_CHECK_CUDA(mf::launch_finalize(c->dp, parts, nb, ds, 0, s));
+  MF_CHECK_CUDA(cudaMemcpyAsync(hs, ds, sizeof(StepState), cudaMemcpyDeviceToHost, s));
+  mf_status st = wait_stream(s, c->timeout);
+  if (st != MF_OK) return st;
+  if (dt) *dt = hs->dt_min;
+  if (min_cell) {
+    int n[3];
+    ext3(*box, n);
+    int idx = hs->min_idx;
+    if (idx < 0 || idx == 0x7fffffff) idx = 0;
+    min_cell[0] = box->lo[0] + idx % n[0];
+    min_cell[1] = box->lo[1] + (idx / n[0]) % n[1];
+    min_cell[2] = box->lo[2] + idx / (n[0] * n[1]);
+  }
+  return flags_status(hs->flags);
+}
+
+// ---------------------------------------------------------------------------
+// level
+// ---------------------------------------------------------------------------
+
+static void add_regions(const mf_level* L, const mf_params& p, int depth, std::vector<CopyReg>& out) {
+  const int sd = p.space_dim;
+  int Lp[3] = {0, 0, 0};
+  for (int d = 0; d < sd; ++d) Lp[d] = p.domain_hi[d] - p.domain_lo[d] + 1;
+  int rng[3];
+  for (int d = 0; d < 3; ++d) rng[d] = (d < sd && p.periodic[d]) ? 1 : 0;
+  for (int dp = 0; dp < L->np; ++dp) {
+    mf_box dst = box_grow(L->valid[dp], depth, sd);
+    int dfn[3];
+    ext3(L->fab[dp], dfn);
+    for (int sp = 0; sp < L->np; ++sp) {
+      int sfn[3];
+      ext3(L->fab[sp], sfn);
+      for (int a = -rng[0]; a <= rng[0]; ++a)
+        for (int b = -rng[1]; b <= rng[1]; ++b)
+          for (int e = -rng[2]; e <= rng[2]; ++e) {
+            if (sp == dp && a == 0 && b == 0 && e == 0) continue;
+            int sh[3] = {a * Lp[0], b * Lp[1], e * Lp[2]};
+            mf_box src = L->valid[sp];
+            for (int d = 0; d < 3; ++d) {
+              src.lo[d] += sh[d];
+              src.hi[d] += sh[d];
+            }
+            mf_box r = box_isect(src, dst);
+            if (box_empty(r)) continue;
+            CopyReg R;
+            R.src_off = L->off[sp];
+            R.dst_off = L->off[dp];
+            for (int d = 0; d < 3; ++d) {
+              R.sfn[d] = sfn[d];
+              R.dfn[d] = dfn[d];
+              R.s0[d] = r.lo[d] - sh[d] - L->fab[sp].lo[d];
+              R.d0[d] = r.lo[d] - L->fab[dp].lo[d];
+              R.ext[d] = r.hi[d] - r.lo[d] + 1;
+            }
+            out.push_back(R);
+          }
+    }
+  }
+}
+
+static mf_status enqueue_level_step(mf_level* L, int advance) {
+  mf_ctx* c = L->ctx;
+  const mf_params& p = c->p;
+  const int mixed = (p.precision == MF_PREC_MIXED);
+  cudaStream_t s = L->s;
+  StageDesc* dd = (StageDesc*)L->desc.p;
+  StepState* ds = (StepState*)L->state.p;
+  DtPartial* parts = (DtPartial*)L->partials.p;
+  StageBuffers B;
+  std::memset(&B, 0, sizeof(B));
+  B.w = (double*)L->W.p;
+  for (int d = 0; d < 3; ++d) {
+    B.f[d] = L->F[d].p;
+    B.bn[d] = L->Bn[d].p;
+  }
+  int nb = 0;
+  const int nc = c->nc;
+  MF_CHECK_CUDA(mf::launch_exchange((double*)L->U.p, (const CopyReg*)L->exfull.p, L->nfull, nc, s));
+  if (p.time_approximation == MF_TA_RK2) {
+    B.uin = (const double*)L->U.p;
+    B.uout = (double*)L->U1.p;
+    MF_CHECK_CUDA(mf::launch_stage(c->dp, mixed, B, dd, L->np, L->max_w, L->max_f, L->max_v, 0,
+                                   1.0, ds, parts, &nb, s));
+    MF_CHECK_CUDA(
+        mf::launch_exchange((double*)L->U1.p, (const CopyReg*)L->extwo.p, L->ntwo, nc, s));
+    B.uin = (const double*)L->U1.p;
+    B.uout = (double*)L->U.p;
+    B.uold = (const double*)L->U.p;
+    MF_CHECK_CUDA(mf::launch_stage(c->dp, mixed, B, dd, L->np, L->max_w, L->max_f, L->max_v,
+                                   mf::kStageAverage | mf::kStageDt, 0.5, ds, parts, &nb, s));
+  } else {
+    B.uin = (const double*)L->U.p;
+    B.uout = (double*)L->U.p;
+    MF_CHECK_CUDA(mf::launch_stage(c->dp, mixed, B, dd, L->np, L->max_w, L->max_f, L->max_v,
+                                   mf::kStageDt, 1.0, ds, parts, &nb, s));
+  }
+  MF_CHECK_CUDA(mf::launch_finalize(c->dp, parts, nb, ds, advance, s));
+  return MF_OK;
+}
+
+static mf_status level_graph(mf_level* L, int advance, cudaGraphExec_t* out) {
+  if (*out) return MF_OK;
+  cudaGraph_t g = nullptr;
+  MF_CHECK_CUDA(cudaStreamBeginCapture(L->s, cudaStreamCaptureModeThreadLocal));
+  mf_status st = enqueue_level_step(L, advance);
+  cudaError_t e = cudaStreamEndCapture(L->s, &g);
+  if (st != MF_OK) {
+    if (g) cudaGraphDestroy(g);
+    return st;
+  }
+  if (e != cudaSuccess) return MF_ERR_CUDA;
+  e = cudaGraphInstantiate(out, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) {
+    *out = nullptr;
+    return MF_ERR_CUDA;
+  }
+  return MF_OK;
+}
+
+// The user stream (if any) and the level's own stream are ordered with events.
+static mf_status join_streams(cudaStream_t from, cudaStream_t to) {
+  if (from == to) return MF_OK;
+  cudaEvent_t ev;
+  MF_CHECK_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+  cudaError_t e = cudaEventRecord(ev, from);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(to, ev, 0);
+  cudaEventDestroy(ev);
+  return e == cudaSuccess ? MF_OK : MF_ERR_CUDA;
+}
+
+mf_status mf_level_create(mf_ctx* c, int npatch, const mf_box* valid, mf_level** out) {
+  if (!c || !valid || !out || npatch <= 0) return MF_ERR_BAD_ARG;
+  *out = nullptr;
+  const mf_params& p = c->p;
+  const int sd = p.space_dim, nc = c->nc;
+  for (int d = 0; d < sd; ++d)
+    if (!p.periodic[d] && p.bc_kind != MF_BC_FARFIELD) return MF_ERR_UNSUPPORTED;
+  mf_level* L = new (std::nothrow) mf_level();
+  if (!L) return MF_ERR_OOM;
+  L->ctx = c;
+  L->np = npatch;
+  L->valid.assign(valid, valid + npatch);
+  L->fab.resize(npatch);
+  L->off.resize(npatch);
+  mf_box dom;
+  for (int d = 0; d < 3; ++d) {
+    dom.lo[d] = p.domain_lo[d];
+    dom.hi[d] = p.domain_hi[d];
+  }
+  long long off = 0;
+  for (int i = 0; i < npatch; ++i) {
+    const mf_box& v = valid[i];
+    bool bad = box_empty(v) || !box_contains(dom, v);
+    for (int d = sd; d < 3; ++d)
+      if (v.lo[d] != 0 || v.hi[d] != 0) bad = true;
+    if (bad) {
+      delete L;
+      return MF_ERR_BAD_ARG;
+    }
+    L->fab[i] = box_grow(v, c->ng, sd);
+    L->off[i] = off;
+    off += ((box_cells(L->fab[i]) * nc + 31) / 32) * 32;  // 256-byte aligned fabs
+    L->cells += box_cells(v);
+  }
+  // valid boxes must not overlap
+  for (int i = 0; i < npatch; ++i)
+    for (int j = i + 1; j < npatch; ++j)
+      if (!box_empty(box_isect(valid[i], valid[j]))) {
+        delete L;
+        return MF_ERR_BAD_ARG;
+      }
+  L->total = off;
+  const int mixed = (p.precision == MF_PREC_MIXED);
+  const size_t rs = mixed ? sizeof(float) : sizeof(double);
+  std::vector<StageDesc> hd(npatch);
+  long long foff[3] = {0, 0, 0}, boff[3] = {0, 0, 0};
+  for (int i = 0; i < npatch; ++i) {
+    mf_box wb = box_grow(valid[i], 2, sd);
+    fill_desc(hd[i], L->fab[i], valid[i], wb);
+    hd[i].u_off = L->off[i];
+    for (int d = 0; d < sd; ++d) {
+      long long nf = box_cells(box_nodes(valid[i], d));
+      hd[i].f_off[d] = foff[d];
+      hd[i].bn_off[d] = boff[d];
+      foff[d] += ((nf * nc + 63) / 64) * 64;
+      boff[d] += ((nf + 63) / 64) * 64;
+      L->max_f[d] = std::max(L->max_f[d], nf);
+    }
+    L->max_w = std::max(L->max_w, box_cells(wb));
+    L->max_v = std::max(L->max_v, box_cells(valid[i]));
+  }
+  std::vector<CopyReg> full, two;
+  add_regions(L, p, c->ng, full);
+  if (p.time_approximation == MF_TA_RK2) add_regions(L, p, 2, two);
+  L->nfull = (int)full.size();
+  L->ntwo = (int)two.size();
+  L->nparts = (int)(((L->max_v + 127) / 128) * npatch);
+  mf_status st = MF_OK;
+  auto fail = [&](cudaError_t e) {
+    st = (e == cudaErrorMemoryAllocation) ? MF_ERR_OOM : MF_ERR_CUDA;
+  };
+  cudaError_t e = cudaSuccess;
+  do {
+    if ((e = L->U.ensure(sizeof(double) * L->total)) != cudaSuccess) break;
+    if ((e = cudaMemset(L->U.p, 0, sizeof(double) * L->total)) != cudaSuccess) break;
+    if (p.time_approximation == MF_TA_RK2) {
+      if ((e = L->U1.ensure(sizeof(double) * L->total)) != cudaSuccess) break;
+      if ((e = cudaMemset(L->U1.p, 0, sizeof(double) * L->total)) != cudaSuccess) break;
+    }
+    if ((e = L->W.ensure(sizeof(double) * L->total)) != cudaSuccess) break;
+    for (int d = 0; d < sd && e == cudaSuccess; ++d) {
+      e = L->F[d].ensure(rs * foff[d]);
+      if (e == cudaSuccess) e = L->Bn[d].ensure(rs * boff[d]);
+    }
+    if (e != cudaSuccess) break;
+    if ((e = L->desc.ensure(sizeof(StageDesc) * npatch)) != cudaSuccess) break;
+    if ((e = cudaMemcpy(L->desc.p, hd.data(), sizeof(StageDesc) * npatch,
+                        cudaMemcpyHostToDevice)) != cudaSuccess)
+      break;
+    if ((e = L->exfull.ensure(sizeof(CopyReg) * std::max<size_t>(1, full.size()))) != cudaSuccess)
+      break;
+    if (!full.empty() &&
+        (e = cudaMemcpy(L->exfull.p, full.data(), sizeof(CopyReg) * full.size(),
+                        cudaMemcpyHostToDevice)) != cudaSuccess)
+      break;
+    if ((e = L->extwo.ensure(sizeof(CopyReg) * std::max<size_t>(1, two.size()))) != cudaSuccess)
+      break;
+    if (!two.empty() && (e = cudaMemcpy(L->extwo.p, two.data(), sizeof(CopyReg) * two.size(),
+                                        cudaMemcpyHostToDevice)) != cudaSuccess)
+      break;
+    if ((e = L->partials.ensure(sizeof(DtPartial) * (L->nparts + 1))) != cudaSuccess) break;
+    if ((e = L->state.ensure(sizeof(StepState))) != cudaSuccess) break;
+    if ((e = L->state2.ensure(sizeof(StepState))) != cudaSuccess) break;
+    if ((e = L->hstate.ensure(sizeof(StepState))) != cudaSuccess) break;
+    std::memset(L->hstate.p, 0, sizeof(StepState));
+    if ((e = cudaMemcpy(L->state.p, L->hstate.p, sizeof(StepState), cudaMemcpyHostToDevice)) !=
+        cudaSuccess)
+      break;
+    if ((e = cudaStreamCreateWithFlags(&L->s, cudaStreamNonBlocking)) != cudaSuccess) break;
+  } while (0);
+  if (e != cudaSuccess) fail(e);
+  if (st != MF_OK) {
+    mf_level_destroy(L);
+    return st;
+  }
+  const int per_stage = mf::stage_launches(sd);
+  L->launches = (p.time_approximation == MF_TA_RK2) ? (2 * per_stage + 2 + 1) : (per_stage + 1 + 1);
+  if (L->nfull == 0) L->launches -= 1;
+  if (p.time_approximation == MF_TA_RK2 && L->ntwo == 0) L->launches -= 1;
+  *out = L;
+  return MF_OK;
+}
+
+void mf_level_destroy(mf_level* L) {
+  if (!L) return;
+  if (L->gsync) cudaGraphExecDestroy(L->gsync);
+  if (L->gasync) cudaGraphExecDestroy(L->gasync);
+  if (L->s) cudaStreamDestroy(L->s);
+  L->U.release();
+  L->U1.release();
+  L->W.release();
+  for (int d = 0; d < 3; ++d) {
+    L->F[d].release();
+    L->Bn[d].release();
+  }
+  L->desc.release();
+  L->exfull.release();
+  L->extwo.release();
+  L->partials.release();
+  L->state.release();
+  L->state2.release();
+  L->hstate.release();
+  delete L;
+}
+
+long long mf_level_num_doubles(const mf_level* L) { return L ? L->total : -1; }
+long long mf_level_num_cells(const mf_level* L) { return L ? L->cells : -1; }
+
+long long mf_level_patch_offset(const mf_level* L, int p) {
+  if (!L || p < 0 || p >= L->np) return -1;
+  return L->off[p];
+}
+
+mf_status mf_level_patch_fab(const mf_level* L, int p, mf_fab* out) {
+  if (!L || !out || p < 0 || p >= L->np) return MF_ERR_BAD_ARG;
+  out->data = (double*)L->U.p + L->off[p];
+  out->box = L->fab[p];
+  out->ncomp = L->ctx->nc;
+  return MF_OK;
+}
+
+mf_status mf_level_upload(mf_level* L, const double* host, void* stream) {
+  if (!L || !host) return MF_ERR_BAD_ARG;
+  cudaStream_t us = (cudaStream_t)stream;
+  mf_status st = join_streams(us, L->s);
+  if (st != MF_OK) return st;
+  MF_CHECK_CUDA(
+      cudaMemcpyAsync(L->U.p, host, sizeof(double) * L->total, cudaMemcpyHostToDevice, L->s));
+  st = join_streams(L->s, us);
+  if (st != MF_OK) return st;
+  return wait_stream(L->s, L->ctx->timeout);
+}
+
+mf_status mf_level_download(const mf_level* L, double* host, void* stream) {
+  if (!L || !host) return MF_ERR_BAD_ARG;
+  cudaStream_t us = (cudaStream_t)stream;
+  mf_status st = join_streams(us, L->s);
+  if (st != MF_OK) return st;
+  MF_CHECK_CUDA(
+      cudaMemcpyAsync(host, L->U.p, sizeof(double) * L->total, cudaMemcpyDeviceToHost, L->s));
+  return wait_stream(L->s, L->ctx->timeout);
+}
+
+mf_status mf_level_exchange(mf_level* L, void* stream) {
+  if (!L) return MF_ERR_BAD_ARG;
+  cudaStream_t us = (cudaStream_t)stream;
+  mf_status st = join_streams(us, L->s);
+  if (st != MF_OK) return st;
+  MF_CHECK_CUDA(mf::launch_exchange((double*)L->U.p, (const CopyReg*)L->exfull.p, L->nfull,
+                                    L->ctx->nc, L->s));
+  st = join_streams(L->s, us);
+  if (st != MF_OK) return st;
+  return wait_stream(L->s, L->ctx->timeout);
+}
+
+static void decode_result(const mf_level* L, const StepState* hs, double* new_dt, int* min_patch,
+                          int min_cell[3]) {
+  if (new_dt) *new_dt = hs->dt_min;
+  int pi = hs->min_desc;
+  if (pi < 0 || pi >= L->np) pi = 0;
+  if (min_patch) *min_patch = pi;
+  if (min_cell) {
+    int n[3];
+    ext3(L->valid[pi], n);
+    int idx = hs->min_idx;
+    if (idx < 0 || idx == 0x7fffffff) idx = 0;
+    min_cell[0] = L->valid[pi].lo[0] + idx % n[0];
+    min_cell[1] = L->valid[pi].lo[1] + (idx / n[0]) % n[1];
+    min_cell[2] = L->valid[pi].lo[2] + idx / (n[0] * n[1]);
+  }
+}
+
+mf_status mf_level_step(mf_level* L, double dt, double* new_dt, int* min_patch, int min_cell[3],
+                        void* stream) {
+  if (!L || !(dt > 0.0) || !std::isfinite(dt)) return MF_ERR_BAD_ARG;
+  mf_ctx* c = L->ctx;
+  mf_status st = level_graph(L, 0, &L->gsync);
+  if (st != MF_OK) return st;
+  cudaStream_t us = (cudaStream_t)stream;
+  st = join_streams(us, L->s);
+  if (st != MF_OK) return st;
+  StepState* hs = (StepState*)L->hstate.p;
+  std::memset(hs, 0, sizeof(*hs));
+  hs->dt = dt;
+  hs->ch = c->p.dedner_ch;
+  hs->cp = c->p.dedner_cp;
+  MF_CHECK_CUDA(cudaMemcpyAsync(L->state.p, hs, sizeof(StepState), cudaMemcpyHostToDevice, L->s));
+  MF_CHECK_CUDA(cudaGraphLaunch(L->gsync, L->s));
+  MF_CHECK_CUDA(cudaMemcpyAsync(hs, L->state.p, sizeof(StepState), cudaMemcpyDeviceToHost, L->s));
+  st = join_streams(L->s, us);
+  if (st != MF_OK) return st;
+  st = wait_stream(L->s, c->timeout);
+  if (st != MF_OK) return st;
+  decode_result(L, hs, new_dt, min_patch, min_cell);
+  return flags_status(hs->flags);
+}
+
+mf_status mf_level_compute_dt(mf_level* L, double* dt, int* min_patch, int min_cell[3],
+                              void* stream) {
+  if (!L) return MF_ERR_BAD_ARG;
+  mf_ctx* c = L->ctx;
+  cudaStream_t us = (cudaStream_t)stream;
+  mf_status st = join_streams(us, L->s);
+  if (st != MF_OK) return st;
+  StepState* hs = (StepState*)L->hstate.p;
+  std::memset(hs, 0, sizeof(*hs));
+  MF_CHECK_CUDA(cudaMemcpyAsync(L->state2.p, hs, sizeof(StepState), cudaMemcpyHostToDevice, L->s));
+  int nb = 0;
+  MF_CHECK_CUDA(mf::launch_dt(c->dp, (const double*)L->U.p, (const StageDesc*)L->desc.p, L->np,
+                              L->max_v, (DtPartial*)L->partials.p, &nb, L->s));
+  MF_CHECK_CUDA(mf::launch_finalize(c->dp, (const DtPartial*)L->partials.p, nb,
+                                    (StepState*)L->state2.p, 0, L->s));
+  MF_CHECK_CUDA(
+      cudaMemcpyAsync(hs, L->state2.p, sizeof(StepState), cudaMemcpyDeviceToHost, L->s));
+  st = wait_stream(L->s, c->timeout);
+  if (st != MF_OK) return st;
+  decode_result(L, hs, dt, min_patch, min_cell);
+  return flags_status(hs->flags);
+}
+
+mf_status mf_level_seed_dt(mf_level* L, double dt, double cfl, void* stream) {
+  if (!L || !(dt > 0.0) || !(cfl > 0.0)) return MF_ERR_BAD_ARG;
+  mf_ctx* c = L->ctx;
+  cudaStream_t us = (cudaStream_t)stream;
+  mf_status st = join_streams(us, L->s);
+  if (st != MF_OK) return st;
+  StepState* hs = (StepState*)L->hstate.p;
+  std::memset(hs, 0, sizeof(*hs));
+  hs->dt = dt;
+  hs->cfl = cfl;
+  hs->ch = c->p.dedner_ch;
+  hs->cp = c->p.dedner_cp;
+  MF_CHECK_CUDA(cudaMemcpyAsync(L->state.p, hs, sizeof(StepState), cudaMemcpyHostToDevice, L->s));
+  return wait_stream(L->s, c->timeout);
+}
+
+mf_status mf_level_step_async(mf_level* L, void* stream) {
+  if (!L) return MF_ERR_BAD_ARG;
+  mf_status st = level_graph(L, 1, &L->gasync);
+  if (st != MF_OK) return st;
+  cudaStream_t us = (cudaStream_t)stream;
+  st = join_streams(us, L->s);
+  if (st != MF_OK) return st;
+  MF_CHECK_CUDA(cudaGraphLaunch(L->gasync, L->s));
+  return join_streams(L->s, us);
+}
+
+mf_status mf_level_result(mf_level* L, double* new_dt, int* min_patch, int min_cell[3],
+                          void* stream) {
+  if (!L) return MF_ERR_BAD_ARG;
+  cudaStream_t us = (cudaStream_t)stream;
+  mf_status st = join_streams(us, L->s);
+  if (st != MF_OK) return st;
+  StepState* hs = (StepState*)L->hstate.p;
+  MF_CHECK_CUDA(cudaMemcpyAsync(hs, L->state.p, sizeof(StepState), cudaMemcpyDeviceToHost, L->s));
+  st = wait_stream(L->s, L->ctx->timeout);
+  if (st != MF_OK) return st;
+  decode_result(L, hs, new_dt, min_patch, min_cell);
+  return flags_status(hs->flags);
+}
+
+int mf_level_launches_per_step(const mf_level* L) { return L ? L->launches : -1; }
+
+// ---------------------------------------------------------------------------
+// problem set-up on host fabs
+// ---------------------------------------------------------------------------
+
+static inline long long hidx(const mf_fab* U, int i, int j, int k, int q) {
+  int n[3];
+  ext3(U->box, n);
+  return (long long)(i - U->box.lo[0]) +
+         (long long)n[0] * ((long long)(j - U->box.lo[1]) +
+                            (long long)n[1] * ((long long)(k - U->box.lo[2]) + (long long)n[2] * q));
+}
+
+mf_status mf_init_orszag_host(const mf_params* p, mf_fab* U, const mf_box* box) {
+  // ORSZAGINIT (problems/OrszagF.ChF:27-79)
+  if (!p || !U || !U->data || !box || !box_contains(U->box, *box)) return MF_ERR_BAD_ARG;
+  if (U->ncomp != num_cons(*p)) return MF_ERR_BAD_ARG;
+  const double gamma = p->gamma, hgamma = gamma - 1.0, dx = p->dx;
+  const double p0 = mf::kInv4Pi * gamma;
+  const double r0 = p0 * gamma;
+  const int glm = (p->divb_cleaning == 5);
+  for (int k = box->lo[2]; k <= box->hi[2]; ++k)
+    for (int j = box->lo[1]; j <= box->hi[1]; ++j)
+      for (int i = box->lo[0]; i <= box->hi[0]; ++i) {
+        double x = (i + 0.5) * dx, y = (j + 0.5) * dx;
+        double Ux = -std::sin(mf::k2Pi * y);
+        double Uy = std::sin(mf::k2Pi * x);
+        double Bx = -std::sin(mf::k2Pi * y);
+        double By = std::sin((mf::k2Pi + mf::k2Pi) * x);
+        double b = mf::kInv4Pi * (Bx * Bx + By * By);
+        double ke = Ux * Ux + Uy * Uy;
+        double e0 = p0 / hgamma + 0.5 * (r0 * ke + b);
+        double* d = U->data;
+        d[hidx(U, i, j, k, 0)] = r0;
+        d[hidx(U, i, j, k, 1)] = r0 * Ux;
+        d[hidx(U, i, j, k, 2)] = r0 * Uy;
+        d[hidx(U, i, j, k, 3)] = 0.0;
+        d[hidx(U, i, j, k, 4)] = e0;
+        d[hidx(U, i, j, k, 5)] = Bx;
+        d[hidx(U, i, j, k, 6)] = By;
+        d[hidx(U, i, j, k, 7)] = 0.0;
+        if (glm) d[hidx(U, i, j, k, 8)] = 0.0;
+        for (int q = 8 + glm; q < U->ncomp; ++q) d[hidx(U, i, j, k, q)] = 0.0;
+      }
+  return MF_OK;
+}
+
+mf_status mf_init_helio_host(const mf_params* p, const double* wp, const double* wn, mf_fab* U,
+                             const mf_box* box) {
+  // uniform inflow from primitive states (PRIMTOCONS_MF, srcIdeal/PatchMHDMFF.ChF:82-149)
+  // plus the inner solar-wind sphere (HELIOREINIT_DEFAULT)
+  if (!p || !wp || !U || !U->data || !box || !box_contains(U->box, *box)) return MF_ERR_BAD_ARG;
+  if (U->ncomp != num_cons(*p)) return MF_ERR_BAD_ARG;
+  if (p->n_fluids > 1 && !wn) return MF_ERR_BAD_ARG;
+  const DevParams P = make_dev(*p);
+  const double hg = p->gamma - 1.0, invhg = 1.0 / hg;
+  const int glm = P.glm, irhon = 8 + glm;
+  double u[MF_MAX_COMP];
+  for (int k = box->lo[2]; k <= box->hi[2]; ++k)
+    for (int j = box->lo[1]; j <= box->hi[1]; ++j)
+      for (int i = box->lo[0]; i <= box->hi[0]; ++i) {
+        double rho = std::max(wp[0], p->smallr);
+        double uu = wp[1], vv = wp[2], ww = wp[3], pr = wp[4];
+        double bx = wp[5], by = wp[6], bz = wp[7];
+        double b = mf::kInv4Pi * (bx * bx + by * by + bz * bz);
+        double ke = uu * uu + vv * vv + ww * ww;
+        u[0] = rho;
+        u[1] = rho * uu;
+        u[2] = rho * vv;
+        u[3] = rho * ww;
+        u[4] = pr * invhg + 0.5 * (rho * ke + b);
+        u[5] = bx;
+        u[6] = by;
+        u[7] = bz;
+        if (glm) u[8] = 0.0;
+        for (int f = 1; f < p->n_fluids; ++f) {
+          const double* w = wn + 5 * (f - 1);
+          int s = irhon + 5 * (f - 1);
+          double r = std::max(w[0], p->smallr);
+          double ke2 = w[1] * w[1] + w[2] * w[2] + w[3] * w[3];
+          u[s] = r;
+          u[s + 1] = r * w[1];
+          u[s + 2] = r * w[2];
+          u[s + 3] = r * w[3];
+          u[s + 4] = w[4] * invhg + 0.5 * r * ke2;
+        }
+        if (p->reinit_sphere) mf::reinit_cell(P, i, j, k, u);
+        for (int q = 0; q < U->ncomp; ++q) U->data[hidx(U, i, j, k, q)] = u[q];
+      }
+  return MF_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,538 @@
+"""ctypes binding of libmfgpu.so (include/mf_patch.h) and problem presets.
+
+The shared library is the product: hand-written sm_103a CUDA kernels behind a
+C ABI.  This module only declares the C structs, loads the library (failing
+loudly when it is absent: there is no CPU fallback) and builds parameter sets
+for the two reference problems used by the tests and the benchmark:
+
+* Orszag-Tang vortex, 2D periodic single-fluid MHD (problems/OrszagF.ChF);
+* a synthetic 3D heliosphere: plasma + 3 neutral H fluids, GLM cleaning,
+  charge exchange, a supersonic radial wind from an inner sphere.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libmfgpu.so")
+
+MF_OK = 0
+MF_ERR_BAD_ARG = 1
+MF_ERR_OOM = 2
+MF_ERR_NONFINITE = 3
+MF_ERR_NEG_STATE = 4
+MF_ERR_TIMEOUT = 5
+MF_ERR_CUDA = 6
+MF_ERR_UNSUPPORTED = 7
+
+TA_FIRST_ORDER, TA_HANCOCK, TA_RK2 = 0, 1, 2
+PREC_FP64, PREC_MIXED = 0, 1
+BC_NONE, BC_FARFIELD = 0, 1
+LIM_CD, LIM_MINMOD, LIM_SUPERBEE, LIM_VANALBADA, LIM_MC, LIM_HARMONIC, LIM_VANLEER = (
+    0, 1, 2, 3, 4, 5, 9)
+MAX_COMP = 29
+
+c_int3 = ctypes.c_int * 3
+c_double3 = ctypes.c_double * 3
+
+
+class MfBox(ctypes.Structure):
+    _fields_ = [("lo", c_int3), ("hi", c_int3)]
+
+
+class MfFab(ctypes.Structure):
+    _fields_ = [("data", ctypes.c_void_p), ("box", MfBox), ("ncomp", ctypes.c_int)]
+
+
+class MfParams(ctypes.Structure):
+    _fields_ = [
+        ("space_dim", ctypes.c_int),
+        ("n_fluids", ctypes.c_int),
+        ("time_approximation", ctypes.c_int),
+        ("flux", ctypes.c_int),
+        ("divb_cleaning", ctypes.c_int),
+        ("use_8wave", ctypes.c_int),
+        ("divb_method", ctypes.c_int),
+        ("limiter", ctypes.c_int * 8),
+        ("check_positivity", ctypes.c_int),
+        ("precision", ctypes.c_int),
+        ("gamma", ctypes.c_double),
+        ("smallr", ctypes.c_double),
+        ("smallp", ctypes.c_double),
+        ("entropy_fix", ctypes.c_double),
+        ("small_b", ctypes.c_double),
+        ("dx", ctypes.c_double),
+        ("dedner_ch", ctypes.c_double),
+        ("dedner_cp", ctypes.c_double),
+        ("factor_ch", ctypes.c_double),
+        ("factor_cp", ctypes.c_double),
+        ("charge_exchange", ctypes.c_int),
+        ("ce_scale_vel", ctypes.c_double),
+        ("ce_sigma_scale", ctypes.c_double),
+        ("ce_sigma_a", ctypes.c_double),
+        ("ce_sigma_b", ctypes.c_double),
+        ("ce_damp_c", ctypes.c_double),
+        ("ce_damp_pow", ctypes.c_double),
+        ("sun_center", c_double3),
+        ("sun_r", ctypes.c_double),
+        ("sun_v", ctypes.c_double),
+        ("region_t_coeff", ctypes.c_double),
+        ("region_tmlim", ctypes.c_double),
+        ("region_zbot", ctypes.c_double),
+        ("region_ztop", ctypes.c_double),
+        ("reinit_sphere", ctypes.c_int),
+        ("reinit_r0", ctypes.c_double),
+        ("sun_int_bc_radius", ctypes.c_double),
+        ("sun_rho", ctypes.c_double),
+        ("sun_p", ctypes.c_double),
+        ("sun_b", ctypes.c_double),
+        ("sun_beta", ctypes.c_double),
+        ("dir_br", ctypes.c_double),
+        ("domain_lo", c_int3),
+        ("domain_hi", c_int3),
+        ("periodic", c_int3),
+        ("bc_kind", ctypes.c_int),
+        ("bc_plasma", ctypes.c_double * 8),
+        ("bc_neutral1", ctypes.c_double * 5),
+    ]
+
+
+def num_cons(p: MfParams) -> int:
+    """EqSysMHDMF component count (srcIdeal/EqSysMHDMF.cpp:11-48)."""
+    return 8 + (1 if p.divb_cleaning == 5 else 0) + (p.n_fluids - 1) * 5
+
+
+def num_ghost(p: MfParams) -> int:
+    """PatchMHDAM::numGhostCells (src/PatchMHDAM.cpp:280-286)."""
+    if p.time_approximation == TA_RK2:
+        return 4
+    if p.time_approximation == TA_HANCOCK:
+        return 3
+    return 2
+
+
+_P = ctypes.POINTER
+_SIGS = {
+    "mf_params_default": (None, [_P(MfParams), ctypes.c_int, ctypes.c_int]),
+    "mf_params_num_cons": (ctypes.c_int, [_P(MfParams)]),
+    "mf_create": (ctypes.c_int, [_P(MfParams), _P(ctypes.c_void_p)]),
+    "mf_destroy": (None, [ctypes.c_void_p]),
+    "mf_num_ghost": (ctypes.c_int, [ctypes.c_void_p]),
+    "mf_num_cons": (ctypes.c_int, [ctypes.c_void_p]),
+    "mf_set_current_time": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double]),
+    "mf_set_dedner": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double, ctypes.c_double]),
+    "mf_set_wait_timeout": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double]),
+    "mf_status_string": (ctypes.c_char_p, [ctypes.c_int]),
+    "mf_patch_update": (ctypes.c_int, [ctypes.c_void_p, _P(MfFab), _P(MfBox), ctypes.c_double,
+                                       ctypes.c_void_p, ctypes.c_void_p,
+                                       _P(ctypes.c_double), c_int3, ctypes.c_void_p]),
+    "mf_compute_dt": (ctypes.c_int, [ctypes.c_void_p, _P(MfFab), _P(MfBox),
+                                     _P(ctypes.c_double), c_int3, ctypes.c_void_p]),
+    "mf_level_create": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _P(MfBox),
+                                       _P(ctypes.c_void_p)]),
+    "mf_level_destroy": (None, [ctypes.c_void_p]),
+    "mf_level_num_doubles": (ctypes.c_longlong, [ctypes.c_void_p]),
+    "mf_level_num_cells": (ctypes.c_longlong, [ctypes.c_void_p]),
+    "mf_level_patch_offset": (ctypes.c_longlong, [ctypes.c_void_p, ctypes.c_int]),
+    "mf_level_patch_fab": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _P(MfFab)]),
+    "mf_level_upload": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "mf_level_download": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "mf_level_exchange": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "mf_level_compute_dt": (ctypes.c_int, [ctypes.c_void_p, _P(ctypes.c_double),
+                                           _P(ctypes.c_int), c_int3, ctypes.c_void_p]),
+    "mf_level_step": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double, _P(ctypes.c_double),
+                                     _P(ctypes.c_int), c_int3, ctypes.c_void_p]),
+    "mf_level_seed_dt": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double, ctypes.c_double,
+                                        ctypes.c_void_p]),
+    "mf_level_step_async": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "mf_level_result": (ctypes.c_int, [ctypes.c_void_p, _P(ctypes.c_double), _P(ctypes.c_int),
+                                       c_int3, ctypes.c_void_p]),
+    "mf_level_launches_per_step": (ctypes.c_int, [ctypes.c_void_p]),
+    "mf_init_orszag_host": (ctypes.c_int, [_P(MfParams), _P(MfFab), _P(MfBox)]),
+    "mf_init_helio_host": (ctypes.c_int, [_P(MfParams), _P(ctypes.c_double), _P(ctypes.c_double),
+                                          _P(MfFab), _P(MfBox)]),
+}
+
+_lib = None
+
+
+def header_symbols() -> list[str]:
+    """Names of the functions declared in the public headers."""
+    return sorted(_SIGS)
+
+
+def load(path: str | None = None):
+    """Load libmfgpu.so.  Raises RuntimeError when the library was not built:
+    the product has no CPU fallback."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise RuntimeError(f"libmfgpu.so not built ({p}); run __graft_entry__.build()")
+    lib = ctypes.CDLL(p)
+    for name, (res, args) in _SIGS.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    if path is None:
+        _lib = lib
+    return lib
+
+
+def status_string(code: int) -> str:
+    return load().mf_status_string(code).decode()
+
+
+class MfError(RuntimeError):
+    def __init__(self, code: int, what: str):
+        super().__init__(f"{what}: {status_string(code)} ({code})")
+        self.code = code
+
+
+def check(code: int, what: str) -> None:
+    if code != MF_OK:
+        raise MfError(code, what)
+
+
+def make_box(lo, hi) -> MfBox:
+    b = MfBox()
+    for d in range(3):
+        b.lo[d] = int(lo[d]) if d < len(lo) else 0
+        b.hi[d] = int(hi[d]) if d < len(hi) else 0
+    return b
+
+
+def box_tuple(b: MfBox):
+    return tuple(b.lo), tuple(b.hi)
+
+
+def grow(lo, hi, n, sd):
+    lo = list(lo) + [0] * (3 - len(lo))
+    hi = list(hi) + [0] * (3 - len(hi))
+    return ([lo[d] - n if d < sd else 0 for d in range(3)],
+            [hi[d] + n if d < sd else 0 for d in range(3)])
+
+
+def fab_shape(lo, hi, nc):
+    """numpy shape (nc, nz, ny, nx) of an FArrayBox on [lo, hi]."""
+    return (nc, hi[2] - lo[2] + 1, hi[1] - lo[1] + 1, hi[0] - lo[0] + 1)
+
+
+def default_params(space_dim: int, n_fluids: int) -> MfParams:
+    p = MfParams()
+    load().mf_params_default(ctypes.byref(p), space_dim, n_fluids)
+    return p
+
+
+def _base_params(space_dim: int, n_fluids: int) -> MfParams:
+    """Same defaults as mf_params_default, without needing the library."""
+    p = MfParams()
+    p.space_dim = space_dim
+    p.n_fluids = n_fluids
+    p.time_approximation = TA_FIRST_ORDER
+    p.flux = 1
+    p.divb_cleaning = 0
+    p.use_8wave = 1
+    p.divb_method = 1
+    for v in range(8):
+        p.limiter[v] = LIM_MINMOD
+    p.check_positivity = 0
+    p.precision = PREC_FP64
+    p.gamma = 5.0 / 3.0
+    p.smallr = 1e-12
+    p.smallp = 1e-12
+    p.entropy_fix = 0.3
+    p.small_b = 1e-9
+    p.dx = 1.0 / 64.0
+    p.dedner_ch = 1.0
+    p.dedner_cp = 1.0
+    p.factor_ch = 0.0
+    p.factor_cp = 1.0
+    p.ce_scale_vel = 1.0
+    p.ce_sigma_scale = 1.0
+    p.ce_sigma_a = 2.1
+    p.ce_sigma_b = 0.092
+    p.ce_damp_c = 0.0
+    p.ce_damp_pow = 4.5
+    p.region_zbot = -1e300
+    p.region_ztop = 1e300
+    p.region_tmlim = 1e300
+    p.sun_int_bc_radius = 1.0
+    p.dir_br = 1.0
+    for d in range(3):
+        p.domain_lo[d] = 0
+        p.domain_hi[d] = 63 if d < space_dim else 0
+        p.periodic[d] = 1
+    p.bc_kind = BC_NONE
+    return p
+
+
+def orszag_params(n: int = 256, time_approximation: int = TA_RK2,
+                  precision: int = PREC_FP64) -> MfParams:
+    """Orszag-Tang vortex on an n x n periodic unit square (problems/OrszagF.ChF,
+    SETORSZAG :4-25): gamma 5/3, Roe 8-wave flux with arithmetic averaging,
+    minmod, 8-wave source, Bn from the face average."""
+    p = _base_params(2, 1)
+    p.time_approximation = time_approximation
+    p.precision = precision
+    g = 5.0 / 3.0
+    p.gamma = g
+    r0 = g * g
+    umag = np.sqrt(g * g / r0)
+    p.smallr = 1e-8 * r0
+    p.smallp = 1e-8 * r0 * 0.5 * umag * umag
+    p.dx = 1.0 / n
+    for d in range(2):
+        p.domain_lo[d] = 0
+        p.domain_hi[d] = n - 1
+        p.periodic[d] = 1
+    return p
+
+
+HELIO_T_INFLOW = 0.5
+
+
+def helio_params(n: int = 128, seed: int = 20240601, time_approximation: int = TA_RK2,
+                 precision: int = PREC_FP64) -> MfParams:
+    """Synthetic heliosphere on [-1,1]^3 with n^3 cells (index space 0..n-1):
+    MHD plasma + 3 neutral H fluids, gamma 5/3, GLM cleaning (Roe 7-wave +
+    Dedner), van Leer neutral fluxes, charge exchange with a seeded cross-section
+    sigma(v) = (a - b ln v)^2, regions after DEFINE_REGIONS_2F, an inner
+    solar-wind sphere of radius 0.1 reset after every stage, far-field
+    boundaries holding the inflow state."""
+    p = _base_params(3, 4)
+    p.time_approximation = time_approximation
+    p.precision = precision
+    p.gamma = 5.0 / 3.0
+    p.smallr = 1e-8
+    p.smallp = 1e-10
+    p.dx = 2.0 / n
+    p.divb_cleaning = 5
+    p.flux = 1
+    p.use_8wave = 0
+    p.divb_method = 1
+    p.factor_ch = 1.0
+    p.factor_cp = 1.0
+    rng = np.random.default_rng(seed)
+    p.charge_exchange = 1
+    p.ce_scale_vel = 1.0
+    p.ce_sigma_scale = 1.0
+    p.ce_sigma_a = float(rng.uniform(1.5, 2.5))
+    p.ce_sigma_b = float(rng.uniform(0.05, 0.15))
+    p.ce_damp_c = 0.0
+    for d in range(3):
+        p.sun_center[d] = 1.0
+        p.domain_lo[d] = 0
+        p.domain_hi[d] = n - 1
+        p.periodic[d] = 0
+    p.sun_r = 0.1
+    p.sun_v = 10.0
+    p.region_t_coeff = 1.0e4
+    p.region_tmlim = 1.0e5
+    p.reinit_sphere = 1
+    p.reinit_r0 = 0.1
+    p.sun_int_bc_radius = 0.1
+    p.sun_rho = 1.0
+    p.sun_p = 1.0
+    p.sun_b = 0.1
+    p.sun_beta = 2.0
+    p.dir_br = 1.0
+    p.bc_kind = BC_FARFIELD
+    wp, wn = helio_inflow()
+    for q in range(8):
+        p.bc_plasma[q] = wp[q]
+    for q in range(5):
+        p.bc_neutral1[q] = wn[q]
+    # initial GLM speeds; the level step replaces them from its dt
+    p.dedner_ch = 10.0
+    p.dedner_cp = float(np.sqrt(10.0 * p.dx))
+    return p
+
+
+def helio_inflow():
+    """Inflow primitive states: plasma rho 0.1, v = (-1,0,0), p = rho T,
+    |B| = 0.05 at 60 degrees to the flow in the x-y plane; neutral fluids
+    rho 0.1 / 0.05 / 0.05 (0.2 in total), same velocity and temperature."""
+    T = HELIO_T_INFLOW
+    b = 0.05
+    ang = np.deg2rad(60.0)
+    wp = np.array([0.1, -1.0, 0.0, 0.0, 0.1 * T,
+                   -b * np.cos(ang), b * np.sin(ang), 0.0], dtype=np.float64)
+    rhos = [0.1, 0.05, 0.05]
+    wn = np.concatenate([[r, -1.0, 0.0, 0.0, r * T] for r in rhos]).astype(np.float64)
+    return wp, wn
+
+
+def tile_boxes(n, patch, space_dim):
+    """Valid boxes of patch^d tiles covering 0..n-1 in each direction
+    (x fastest)."""
+    boxes = []
+    nz = n // patch if space_dim == 3 else 1
+    for kb in range(nz):
+        for jb in range(n // patch):
+            for ib in range(n // patch):
+                lo = [ib * patch, jb * patch, kb * patch if space_dim == 3 else 0]
+                hi = [lo[0] + patch - 1, lo[1] + patch - 1,
+                      lo[2] + patch - 1 if space_dim == 3 else 0]
+                boxes.append((lo, hi))
+    return boxes
+
+
+def init_host_fab(p: MfParams, lo, hi, problem: str) -> np.ndarray:
+    """Host FArrayBox on [lo, hi] filled by the library's problem set-up."""
+    lib = load()
+    nc = num_cons(p)
+    arr = np.zeros(fab_shape(lo, hi, nc), dtype=np.float64)
+    fab = MfFab(arr.ctypes.data, make_box(lo, hi), nc)
+    box = make_box(lo, hi)
+    if problem == "orszag":
+        check(lib.mf_init_orszag_host(ctypes.byref(p), ctypes.byref(fab), ctypes.byref(box)),
+              "mf_init_orszag_host")
+    elif problem == "helio":
+        wp, wn = helio_inflow()
+        wn = wn[:5 * (p.n_fluids - 1)].copy() if p.n_fluids > 1 else np.zeros(5)
+        check(lib.mf_init_helio_host(ctypes.byref(p),
+                                     wp.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                     wn.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                     ctypes.byref(fab), ctypes.byref(box)), "mf_init_helio_host")
+    else:
+        raise ValueError(problem)
+    return arr
+
+
+class Context:
+    """Owner of an mf_ctx."""
+
+    def __init__(self, p: MfParams):
+        self.lib = load()
+        self.p = p
+        h = ctypes.c_void_p()
+        check(self.lib.mf_create(ctypes.byref(p), ctypes.byref(h)), "mf_create")
+        self.h = h
+        self.nc = self.lib.mf_num_cons(h)
+        self.ng = self.lib.mf_num_ghost(h)
+
+    def close(self):
+        if self.h:
+            self.lib.mf_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_dedner(self, ch, cp):
+        check(self.lib.mf_set_dedner(self.h, ch, cp), "mf_set_dedner")
+
+    def patch_update(self, U_ptr, fab_lo, fab_hi, valid_lo, valid_hi, dt, F=None, divB=None,
+                     stream=None, allow_error=False):
+        """mf_patch_update on a device fab; returns (status, new_dt, min_cell)."""
+        fab = MfFab(U_ptr, make_box(fab_lo, fab_hi), self.nc)
+        valid = make_box(valid_lo, valid_hi)
+        ndt = ctypes.c_double()
+        cell = c_int3()
+        fptr = None
+        if F is not None:
+            arr = (MfFab * 3)()
+            for d, (ptr, lo, hi) in enumerate(F):
+                arr[d] = MfFab(ptr, make_box(lo, hi), self.nc)
+            fptr = ctypes.cast(arr, ctypes.c_void_p)
+            self._keep = arr
+        dptr = None
+        if divB is not None:
+            ptr, lo, hi = divB
+            dfab = MfFab(ptr, make_box(lo, hi), 1)
+            self._keep_d = dfab
+            dptr = ctypes.cast(ctypes.pointer(dfab), ctypes.c_void_p)
+        st = self.lib.mf_patch_update(self.h, ctypes.byref(fab), ctypes.byref(valid), dt, fptr,
+                                      dptr, ctypes.byref(ndt), cell, stream)
+        if not allow_error:
+            check(st, "mf_patch_update")
+        return st, ndt.value, tuple(cell)
+
+
+class Level:
+    """Owner of an mf_level: every patch of a level resident on the device."""
+
+    def __init__(self, ctx: Context, boxes):
+        self.ctx = ctx
+        self.lib = ctx.lib
+        self.boxes = boxes
+        arr = (MfBox * len(boxes))()
+        for i, (lo, hi) in enumerate(boxes):
+            arr[i] = make_box(lo, hi)
+        h = ctypes.c_void_p()
+        check(self.lib.mf_level_create(ctx.h, len(boxes), arr, ctypes.byref(h)),
+              "mf_level_create")
+        self.h = h
+        self.ndoubles = self.lib.mf_level_num_doubles(h)
+        self.ncells = self.lib.mf_level_num_cells(h)
+        self.offsets = [self.lib.mf_level_patch_offset(h, i) for i in range(len(boxes))]
+
+    def close(self):
+        if self.h:
+            self.lib.mf_level_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def fab_box(self, i):
+        lo, hi = self.boxes[i]
+        return grow(lo, hi, self.ctx.ng, self.ctx.p.space_dim)
+
+    def patch_view(self, flat: np.ndarray, i: int) -> np.ndarray:
+        """numpy view (nc, nz, ny, nx) of patch i inside a level-layout buffer."""
+        lo, hi = self.fab_box(i)
+        shp = fab_shape(lo, hi, self.ctx.nc)
+        n = int(np.prod(shp))
+        o = self.offsets[i]
+        return flat[o:o + n].reshape(shp)
+
+    def upload(self, host_ptr, stream=None):
+        check(self.lib.mf_level_upload(self.h, host_ptr, stream), "mf_level_upload")
+
+    def download(self, host_ptr, stream=None):
+        check(self.lib.mf_level_download(self.h, host_ptr, stream), "mf_level_download")
+
+    def compute_dt(self):
+        dt = ctypes.c_double()
+        ip = ctypes.c_int()
+        cell = c_int3()
+        check(self.lib.mf_level_compute_dt(self.h, ctypes.byref(dt), ctypes.byref(ip), cell, None),
+              "mf_level_compute_dt")
+        return dt.value, ip.value, tuple(cell)
+
+    def step(self, dt, stream=None, allow_error=False):
+        ndt = ctypes.c_double()
+        ip = ctypes.c_int()
+        cell = c_int3()
+        st = self.lib.mf_level_step(self.h, dt, ctypes.byref(ndt), ctypes.byref(ip), cell, stream)
+        if not allow_error:
+            check(st, "mf_level_step")
+        return st, ndt.value, ip.value, tuple(cell)
+
+    def seed_dt(self, dt, cfl, stream=None):
+        check(self.lib.mf_level_seed_dt(self.h, dt, cfl, stream), "mf_level_seed_dt")
+
+    def step_async(self, stream=None):
+        check(self.lib.mf_level_step_async(self.h, stream), "mf_level_step_async")
+
+    def result(self, stream=None):
+        ndt = ctypes.c_double()
+        ip = ctypes.c_int()
+        cell = c_int3()
+        st = self.lib.mf_level_result(self.h, ctypes.byref(ndt), ctypes.byref(ip), cell, stream)
+        return st, ndt.value, ip.value, tuple(cell)
+
+    def launches_per_step(self):
+        return self.lib.mf_level_launches_per_step(self.h)

@@ -1,0 +1,2033 @@
+/*
+ * mf_oracle.c - CPU restatement of the MHDAM / MS-FLUKSS per-patch Godunov
+ * update (PatchMHDAM::updateState for the multi-fluid MHD model).
+ *
+ * TEST INFRASTRUCTURE ONLY: the parity checker of the GPU path and the timed
+ * CPU baseline.  Nothing in the product links or calls this file.
+ *
+ * Parity status: "parity unpinned".  The reference ships no tests, golden
+ * vectors or benchmark outputs, and it cannot be compiled here (no Fortran
+ * compiler, Chombo 3.2.4 not vendored).  Every routine below restates the
+ * cited Fortran/C++ literally, including the order in which each expression is
+ * evaluated (Fortran evaluates a+b+c left to right; x**2 is x*x), and it is
+ * pinned by the known-answer and invariant tests under tests/.
+ *
+ * Citations are paths inside the MHDAM-3.2.4 tree.
+ * Compile with -ffp-contract=off so that no multiply-add is fused.
+ */
+#include "mf_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+/* srcIdeal/EosCommon.fh:13-27 */
+#define D_1_4PI 0.079577471545947667884441881686257181
+#define D_1_8PI 0.039788735772973833942220940843128591
+#define D_SQRT_2 0.707106781186547524400844362104849039
+#define D_PI 3.14159265358979323846264338327950288
+#define D_2PI 6.28318530717958647692528676655900576
+/* srcIdeal/EosCommon.fh:31-37 */
+#define NETF2_DENS 1.0e-6
+#define NETF2_PRES 1.0e-8
+#define NETF3_DENS 1.0e-7
+#define NETF3_PRES 1.0e-9
+
+/* ------------------------------------------------------------------------ */
+/* boxes and FArrayBox-like arrays                                           */
+/* ------------------------------------------------------------------------ */
+
+typedef struct {
+  double* p;
+  mf_box b;
+  int nc;
+  long n0, n1, n2, csz;
+  int owned;
+} Fab;
+
+static Fab fab_wrap(double* p, mf_box b, int nc) {
+  Fab f;
+  f.p = p;
+  f.b = b;
+  f.nc = nc;
+  f.n0 = b.hi[0] - b.lo[0] + 1;
+  f.n1 = b.hi[1] - b.lo[1] + 1;
+  f.n2 = b.hi[2] - b.lo[2] + 1;
+  f.csz = f.n0 * f.n1 * f.n2;
+  f.owned = 0;
+  return f;
+}
+
+static Fab fab_alloc(mf_box b, int nc) {
+  Fab f = fab_wrap(NULL, b, nc);
+  long n = f.csz * (long)nc;
+  f.p = (double*)malloc(sizeof(double) * (size_t)(n > 0 ? n : 1));
+  /* FArrayBox storage is uninitialised; NaN makes any read of an unset
+     entry visible in the results. */
+  for (long q = 0; q < n; ++q) f.p[q] = NAN;
+  f.owned = 1;
+  return f;
+}
+
+static void fab_free(Fab* f) {
+  if (f->owned && f->p) free(f->p);
+  f->p = NULL;
+}
+
+static inline long fab_off(const Fab* f, int i, int j, int k) {
+  return (i - f->b.lo[0]) + f->n0 * ((j - f->b.lo[1]) + f->n1 * (long)(k - f->b.lo[2]));
+}
+#define AT(f, i, j, k, c) ((f)->p[fab_off((f), (i), (j), (k)) + (long)(c) * (f)->csz])
+
+static mf_box box_grow(mf_box b, int n, int sd) {
+  for (int d = 0; d < sd; ++d) {
+    b.lo[d] -= n;
+    b.hi[d] += n;
+  }
+  return b;
+}
+
+/* Box & ProblemDomain: clip the non-periodic directions only. */
+static mf_box box_and_domain(mf_box b, const mf_params* p) {
+  for (int d = 0; d < p->space_dim; ++d) {
+    if (p->periodic[d]) continue;
+    if (b.lo[d] < p->domain_lo[d]) b.lo[d] = p->domain_lo[d];
+    if (b.hi[d] > p->domain_hi[d]) b.hi[d] = p->domain_hi[d];
+  }
+  return b;
+}
+
+static mf_box box_nodes(mf_box b, int d) {
+  b.hi[d] += 1;
+  return b;
+}
+
+static int box_in(const mf_box* b, int i, int j, int k) {
+  return i >= b->lo[0] && i <= b->hi[0] && j >= b->lo[1] && j <= b->hi[1] && k >= b->lo[2] &&
+         k <= b->hi[2];
+}
+
+static int box_contains(const mf_box* outer, const mf_box* inner) {
+  for (int d = 0; d < 3; ++d)
+    if (inner->lo[d] < outer->lo[d] || inner->hi[d] > outer->hi[d]) return 0;
+  return 1;
+}
+
+#define FOR_BOX(bx, i, j, k)                               \
+  for (int k = (bx).lo[2]; k <= (bx).hi[2]; ++k)           \
+    for (int j = (bx).lo[1]; j <= (bx).hi[1]; ++j)         \
+      for (int i = (bx).lo[0]; i <= (bx).hi[0]; ++i)
+
+/* ------------------------------------------------------------------------ */
+/* model constants                                                           */
+/* ------------------------------------------------------------------------ */
+
+enum { RS_ROE8 = 0, RS_ROE7 = 1, RS_RUSANOV = 2 };
+
+typedef struct {
+  const mf_params* p;
+  int sd, nf, glm, nc, nprim, irhon, ipsi;
+  int rs, aver;
+  double gamma, hgamma, invhgamma, smallr, smallp, del2, smallB;
+  double dCh, dCp;
+} Ctx;
+
+/* EqSysMHDMF ctor (srcIdeal/EqSysMHDMF.cpp:11-48) and RiemannSolver::make
+   (src/RiemannSolver.cpp:13-112). */
+static int ctx_init(Ctx* c, const mf_params* p) {
+  if (p->space_dim < 2 || p->space_dim > 3) return MF_ERR_BAD_ARG;
+  if (p->n_fluids < 1 || p->n_fluids > MF_MAX_FLUIDS) return MF_ERR_BAD_ARG;
+  c->p = p;
+  c->sd = p->space_dim;
+  c->nf = p->n_fluids;
+  c->glm = (p->divb_cleaning == 5) ? 1 : 0;
+  c->nc = 8 + c->glm + (c->nf - 1) * 5;
+  c->nprim = c->nc;
+  c->irhon = 8 + c->glm;
+  c->ipsi = c->glm ? 8 : -1;
+  c->gamma = p->gamma;
+  c->hgamma = p->gamma - 1.0;
+  c->invhgamma = 1.0 / c->hgamma;
+  c->smallr = p->smallr;
+  c->smallp = p->smallp;
+  c->del2 = p->entropy_fix;
+  c->smallB = p->small_b;
+  c->dCh = p->dedner_ch;
+  c->dCp = p->dedner_cp;
+  int f = p->flux;
+  if (c->glm) {
+    if (!(f == 1 || f == 3)) return MF_ERR_UNSUPPORTED;
+    if (p->use_8wave) return MF_ERR_UNSUPPORTED;
+    c->rs = RS_ROE7;
+    c->aver = (f == 3);
+  } else {
+    switch (f) {
+      case 2: c->rs = RS_RUSANOV; c->aver = 0; break;
+      case 3: c->rs = RS_ROE8; c->aver = 1; break;
+      case 4: c->rs = RS_RUSANOV; c->aver = 1; break;
+      case 5: return MF_ERR_UNSUPPORTED;
+      case 11: c->rs = RS_ROE7; c->aver = 0; break;
+      case 13: c->rs = RS_ROE7; c->aver = 1; break;
+      default: c->rs = RS_ROE8; c->aver = 0; break;
+    }
+  }
+  if (p->time_approximation != MF_TA_FIRST_ORDER && p->time_approximation != MF_TA_RK2)
+    return MF_ERR_UNSUPPORTED;
+  return MF_OK;
+}
+
+static int num_ghost(const mf_params* p) {
+  if (p->time_approximation == MF_TA_RK2) return 4;
+  if (p->time_approximation == MF_TA_HANCOCK) return 3;
+  return 2;
+}
+
+/* ------------------------------------------------------------------------ */
+/* conserved -> primitive                                                    */
+/* ------------------------------------------------------------------------ */
+
+/* CONSTOPRIM (srcIdeal/PatchIdealMHDF.ChF:143-189) and CONSTOPRIM_MF
+   (srcIdeal/PatchMHDMFF.ChF:5-80), then the psi copy of
+   EqSysMHDMF::stateToPrim (srcIdeal/EqSysMHDMF.cpp:169-212). */
+static void cons_to_prim_cell(const Ctx* c, const double* U, double* W) {
+  double rho, ru, rv, rw, invrho, uu, vv, ww, ke, bx, by, bz, b, p;
+  if (c->nf == 1)
+    rho = U[0];
+  else
+    rho = fmax(U[0], c->smallr);
+  ru = U[1];
+  rv = U[2];
+  rw = U[3];
+  invrho = 1.0 / rho;
+  uu = ru * invrho;
+  vv = rv * invrho;
+  ww = rw * invrho;
+  ke = ru * uu + rv * vv + rw * ww;
+  bx = U[5];
+  by = U[6];
+  bz = U[7];
+  b = D_1_4PI * (bx * bx + by * by + bz * bz);
+  p = c->hgamma * (U[4] - 0.5 * (ke + b));
+  p = fmax(p, c->smallp);
+  W[1] = uu;
+  W[2] = vv;
+  W[3] = ww;
+  W[0] = rho;
+  W[4] = p;
+  W[5] = bx;
+  W[6] = by;
+  W[7] = bz;
+  for (int f = 1; f < c->nf; ++f) {
+    int s = c->irhon + (f - 1) * 5;
+    rho = fmax(U[s], c->smallr);
+    ru = U[s + 1];
+    rv = U[s + 2];
+    rw = U[s + 3];
+    invrho = 1.0 / rho;
+    uu = ru * invrho;
+    vv = rv * invrho;
+    ww = rw * invrho;
+    ke = ru * uu + rv * vv + rw * ww;
+    p = c->hgamma * (U[s + 4] - 0.5 * ke);
+    p = fmax(p, c->smallp);
+    W[s + 1] = uu;
+    W[s + 2] = vv;
+    W[s + 3] = ww;
+    W[s] = rho;
+    W[s + 4] = p;
+  }
+  if (c->glm) W[8] = U[8];
+}
+
+/* ------------------------------------------------------------------------ */
+/* limited face values                                                       */
+/* ------------------------------------------------------------------------ */
+
+/* minmod (src/reconstructionF.ChF:5-13); sign(one,A) is copysign. */
+static double minmod(double A, double B) {
+  double signA = copysign(1.0, A);
+  return signA * fmax(0.0, fmin(fabs(A), signA * B));
+}
+
+/* One cell, one variable: returns Wleft (value on the low face) and Wright
+   (value on the high face) from W(i-1), W(i), W(i+1).
+   MINMODFACEVALUES :126-155, SUPERBEEFACEVALUES :258-301,
+   VANALBADAFACEVALUES :550-589, MCFACEVALUES :622-661,
+   HARMONICFACEVALUES :492-524, VANLEERFACEVALUES :794-841,
+   CDFACEVALUES :1056-1079. */
+static void face_values(int lim, double Wm1, double WP, double Wp1, double* WL, double* WR) {
+  double dWR = Wp1 - WP;
+  double dWL = WP - Wm1;
+  double SLOPE;
+  switch (lim) {
+    case MF_LIM_CD:
+      *WL = 0.5 * (WP + Wp1);
+      *WR = 0.5 * (WP + Wm1);
+      return;
+    case MF_LIM_SUPERBEE:
+      if (dWL * dWR <= 0.0) {
+        *WL = WP;
+        *WR = WP;
+        return;
+      } else {
+        double AR = fabs(dWR), AL = fabs(dWL);
+        if (AL <= 0.5 * AR)
+          SLOPE = dWL;
+        else if (AL <= AR)
+          SLOPE = 0.5 * dWR;
+        else if (AL <= AR + AR)
+          SLOPE = 0.5 * dWL;
+        else
+          SLOPE = dWR;
+      }
+      break;
+    case MF_LIM_VANALBADA: {
+      const double dSave = 1.0e-6, dSaveS = dSave + dSave;
+      if (dWL * dWR <= 0.0) {
+        *WL = WP;
+        *WR = WP;
+        return;
+      }
+      SLOPE = 0.5 * (dWR * dWL + dSave) * (dWR + dWL) / (dWR * dWR + dWL * dWL + dSaveS);
+      break;
+    }
+    case MF_LIM_MC:
+      if (dWL * dWR <= 0.0) {
+        *WL = WP;
+        *WR = WP;
+        return;
+      } else {
+        double AR = fabs(dWR), AL = fabs(dWL);
+        if (3.0 * AL <= AR)
+          SLOPE = dWL;
+        else if (AL <= 3.0 * AR)
+          SLOPE = 0.25 * (dWR + dWL);
+        else
+          SLOPE = dWR;
+      }
+      break;
+    case MF_LIM_HARMONIC:
+      if (dWL * dWR <= 0.0) {
+        *WL = WP;
+        *WR = WP;
+        return;
+      }
+      SLOPE = dWR / (1.0 + dWR / dWL);
+      break;
+    case MF_LIM_VANLEER: {
+      const double dSLim = 1.0 / 3.0;
+      const double BT = (3.0 - dSLim) / (1.0 - dSLim);
+      const double SL1 = 0.25 * (1.0 - dSLim);
+      const double SL2 = 0.25 * (1.0 + dSLim);
+      if (dWL * dWR <= 0.0) {
+        *WL = WP;
+        *WR = WP;
+        return;
+      } else {
+        double SL = fmin(fabs(dWR), fabs(BT * dWL));
+        double SR = fmin(fabs(dWL), fabs(BT * dWR));
+        double SLOPL = SL1 * SL + SL2 * SR;
+        double SLOPR = SL1 * SR + SL2 * SL;
+        if (dWR < 0.0) {
+          SLOPL = -SLOPL;
+          SLOPR = -SLOPR;
+        }
+        *WL = WP - SLOPL;
+        *WR = WP + SLOPR;
+        return;
+      }
+    }
+    case MF_LIM_MINMOD:
+    default:
+      SLOPE = 0.5 * minmod(dWR, dWL);
+      break;
+  }
+  *WL = WP - SLOPE;
+  *WR = WP + SLOPE;
+}
+
+/* Limiter of primitive variable v: the driver sets minmod for every slope and
+   then the per-variable limiters of the plasma variables
+   (main/MHDAM.cpp:927-1009). */
+static int limiter_of(const Ctx* c, int v) {
+  if (v < 8) return c->p->limiter[v];
+  return MF_LIM_MINMOD;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Riemann solvers                                                           */
+/* ------------------------------------------------------------------------ */
+
+/* RIEMANNF, Roe 8-wave (src/Roe8WaveF.ChF:5-601), one face.  wl, wr are the
+   left and right primitive states; g receives the fluxes at the prim indices
+   (iRho = 0). */
+static void roe8_face(const Ctx* c, int idir, const double* wl, const double* wr, double* g) {
+  const double gamma = c->gamma, hgamma = c->hgamma, smallp = c->smallp, smallr = c->smallr;
+  const double del2 = c->del2, smallB = c->smallB;
+  const int inorm = 1 + idir, itan1 = 1 + (idir + 1) % 3, itan2 = 1 + (idir + 2) % 3;
+  const int inormB = 5 + idir, itanB1 = 5 + (idir + 1) % 3, itanB2 = 5 + (idir + 2) % 3;
+  double PGasL, RhoL, UL, VL, WL, RUL, RVL, RWL, BXL, BYL, BZL;
+  double PGasR, RhoR, UR, VR, WR, RUR, RVR, RWR, BXR, BYR, BZR;
+  double PGas, Rho, U, V, W, BX, BY, BZ;
+  double BxBL, RUxUL, PL, EL, AL2, HL, coefRL, BxBR, RUxUR, PR, ER, AR2, HR, coefRR;
+  double BxBH, P, HAV, BXAV, DBX, DBY, DBZ;
+  double aas, as, aaf, af, alf, als, cc, c_, ccmi, ccma, dfs, X;
+  double hyy = 0, hyz, hzz = 0, szb, h, kk, sih, z, del, dell2;
+  double b, bb, BX2, BY2, BZ2, BYZ2, sqPiRho, sq2PiRho;
+  double Ae[9], eig[9], eigmax;
+  double fl[9], fr[9], du[9], lu[9], ra[9];
+  double sp[9][9], so[9][9];
+
+  PGasL = fmax(smallp, wl[4]);
+  RhoL = fmax(smallr, wl[0]);
+  UL = wl[inorm];
+  VL = wl[itan1];
+  WL = wl[itan2];
+  BXL = wl[inormB];
+  BYL = wl[itanB1];
+  BZL = wl[itanB2];
+  PGasR = fmax(smallp, wr[4]);
+  RhoR = fmax(smallr, wr[0]);
+  UR = wr[inorm];
+  VR = wr[itan1];
+  WR = wr[itan2];
+  BXR = wr[inormB];
+  BYR = wr[itanB1];
+  BZR = wr[itanB2];
+
+  RUL = RhoL * UL;
+  RVL = RhoL * VL;
+  RWL = RhoL * WL;
+  BxBL = D_1_8PI * (BXL * BXL + BYL * BYL + BZL * BZL);
+  RUxUL = 0.5 * (RUL * UL + RVL * VL + RWL * WL);
+  PL = PGasL + BxBL;
+  EL = PGasL / hgamma + RUxUL + BxBL;
+  AL2 = gamma * PGasL / RhoL;
+
+  RUR = RhoR * UR;
+  RVR = RhoR * VR;
+  RWR = RhoR * WR;
+  BxBR = D_1_8PI * (BXR * BXR + BYR * BYR + BZR * BZR);
+  RUxUR = 0.5 * (RUR * UR + RVR * VR + RWR * WR);
+  PR = PGasR + BxBR;
+  ER = PGasR / hgamma + RUxUR + BxBR;
+  AR2 = gamma * PGasR / RhoR;
+
+  if (AL2 > AR2) {
+    ccmi = AR2;
+    ccma = AL2;
+  } else {
+    ccmi = AL2;
+    ccma = AR2;
+  }
+
+  if (c->aver == 1) {
+    HL = (EL + PL) / RhoL;
+    HR = (ER + PR) / RhoR;
+    coefRL = 1.0 / (1.0 + sqrt(RhoR / RhoL));
+    coefRR = 1.0 - coefRL;
+    Rho = RhoR * coefRL + RhoL * coefRR;
+    U = UL * coefRL + UR * coefRR;
+    V = VL * coefRL + VR * coefRR;
+    W = WL * coefRL + WR * coefRR;
+    HAV = HL * coefRL + HR * coefRR;
+    BX = BXR * coefRL + BXL * coefRR;
+    BY = BYR * coefRL + BYL * coefRR;
+    BZ = BZR * coefRL + BZL * coefRR;
+    BXAV = 0.5 * (BXL + BXR);
+    BX2 = BXAV * BXAV;
+    BY2 = BY * BY;
+    BZ2 = BZ * BZ;
+    BYZ2 = BY2 + BZ2;
+    BxBH = D_1_8PI * (BX2 + BYZ2);
+    kk = 0.5 * (U * U + V * V + W * W);
+    DBX = BXR - BXL;
+    DBY = BYR - BYL;
+    DBZ = BZR - BZL;
+    X = D_1_8PI * (DBX * DBX + DBY * DBY + DBZ * DBZ) * coefRL * coefRL / RhoL;
+    cc = hgamma * (HAV - kk - D_1_4PI * (BX * BXAV + BYZ2) / Rho) + (2.0 - gamma) * X;
+  } else {
+    Rho = 0.5 * (RhoL + RhoR);
+    U = 0.5 * (UL + UR);
+    V = 0.5 * (VL + VR);
+    W = 0.5 * (WL + WR);
+    BX = 0.5 * (BXL + BXR);
+    BY = 0.5 * (BYL + BYR);
+    BZ = 0.5 * (BZL + BZR);
+    P = 0.5 * (PL + PR);
+    BX2 = BX * BX;
+    BY2 = BY * BY;
+    BZ2 = BZ * BZ;
+    BYZ2 = BY2 + BZ2;
+    BxBH = D_1_8PI * (BX2 + BYZ2);
+    kk = 0.5 * (U * U + V * V + W * W);
+    PGas = P - BxBH;
+    cc = gamma * PGas / Rho;
+  }
+
+  bb = D_1_4PI * BX2 / Rho;
+  b = sqrt(bb);
+  if (cc < ccmi) cc = ccmi;
+  if (cc > ccma) cc = ccma;
+  c_ = sqrt(cc);
+
+  if (BYZ2 < smallB * smallB) {
+    hyy = D_SQRT_2;
+    hzz = D_SQRT_2;
+    if (bb > cc) {
+      aaf = bb;
+      aas = cc;
+      af = b;
+      as = c_;
+    } else {
+      aaf = cc;
+      aas = bb;
+      af = c_;
+      as = b;
+    }
+  } else {
+    hyz = sqrt(BYZ2);
+    hyy = BY / hyz;
+    hzz = BZ / hyz;
+    szb = cc + (BxBH + BxBH) / Rho;
+    h = sqrt(szb * szb - 4.0 * cc * bb);
+    aas = 0.5 * (szb - h);
+    if (aas <= 0.0) {
+      aas = 0.0;
+      as = 0.0;
+    } else if (aas >= cc) {
+      aas = cc;
+      as = c_;
+    } else {
+      as = sqrt(aas);
+    }
+    aaf = 0.5 * (szb + h);
+    if (aaf <= cc) {
+      aaf = cc;
+      af = c_;
+    } else {
+      af = sqrt(aaf);
+    }
+  }
+
+  eig[1] = U;
+  eig[2] = U;
+  eig[3] = U + b;
+  eig[4] = U - b;
+  eig[5] = U + af;
+  eig[6] = U - af;
+  eig[7] = U + as;
+  eig[8] = U - as;
+  eigmax = fabs(U) + fabs(V) + fabs(W) + af;
+  del = del2 * eigmax;
+  dell2 = del * del;
+  for (int q = 1; q <= 8; ++q) {
+    z = fabs(eig[q]);
+    if (z >= del)
+      Ae[q] = z;
+    else
+      Ae[q] = 0.5 * (z * z + dell2) / del;
+  }
+
+  dfs = aaf - aas;
+  if (dfs < 1.0e-8) {
+    alf = 1.0;
+    als = 0.0;
+  } else if ((cc - aas) <= 0.0) {
+    alf = 0.0;
+    als = 1.0;
+  } else if ((aaf - cc) <= 0.0) {
+    alf = 1.0;
+    als = 0.0;
+  } else {
+    alf = sqrt((cc - aas) / dfs);
+    als = sqrt((aaf - cc) / dfs);
+  }
+
+  sih = -1.0;
+  if (BX >= 0.0) sih = 1.0;
+
+  fl[1] = RUL;
+  fl[2] = UL * RUL - BXL * BXL * D_1_4PI + PL;
+  fl[3] = UL * RVL - BXL * BYL * D_1_4PI;
+  fl[4] = UL * RWL - BXL * BZL * D_1_4PI;
+  fl[5] = UL * (EL + PL) - BXL * (UL * BXL + VL * BYL + WL * BZL) * D_1_4PI;
+  fl[6] = 0.0;
+  fl[7] = UL * BYL - BXL * VL;
+  fl[8] = UL * BZL - BXL * WL;
+
+  fr[1] = RUR;
+  fr[2] = UR * RUR - BXR * BXR * D_1_4PI + PR;
+  fr[3] = UR * RVR - BXR * BYR * D_1_4PI;
+  fr[4] = UR * RWR - BXR * BZR * D_1_4PI;
+  fr[5] = UR * (ER + PR) - BXR * (UR * BXR + VR * BYR + WR * BZR) * D_1_4PI;
+  fr[6] = 0.0;
+  fr[7] = UR * BYR - BXR * VR;
+  fr[8] = UR * BZR - BXR * WR;
+
+  du[1] = RhoL - RhoR;
+  du[2] = RUL - RUR;
+  du[3] = RVL - RVR;
+  du[4] = RWL - RWR;
+  du[5] = EL - ER;
+  du[6] = BXL - BXR;
+  du[7] = BYL - BYR;
+  du[8] = BZL - BZR;
+
+  du[5] = -hgamma * (-kk * du[1] + U * du[2] + V * du[3] + W * du[4] - du[5] +
+                     (BX * du[6] + BY * du[7] + BZ * du[8]) * D_1_4PI);
+  du[2] = (-U * du[1] + du[2]) / Rho;
+  du[3] = (-V * du[1] + du[3]) / Rho;
+  du[4] = (-W * du[1] + du[4]) / Rho;
+
+  sqPiRho = sqrt(D_PI * Rho);
+  sq2PiRho = sqrt(D_2PI * Rho);
+
+  sp[1][1] = 1.0; sp[1][2] = 0.0; sp[1][3] = 0.0; sp[1][4] = 0.0;
+  sp[1][5] = Rho * alf; sp[1][6] = Rho * alf; sp[1][7] = Rho * als; sp[1][8] = Rho * als;
+
+  sp[2][1] = 0.0; sp[2][2] = 0.0; sp[2][3] = 0.0; sp[2][4] = 0.0;
+  sp[2][5] = alf * af; sp[2][6] = -alf * af; sp[2][7] = als * as; sp[2][8] = -als * as;
+
+  sp[3][1] = 0.0; sp[3][2] = 0.0;
+  sp[3][3] = -hzz * D_SQRT_2; sp[3][4] = -hzz * D_SQRT_2;
+  sp[3][5] = -als * as * hyy * sih; sp[3][6] = als * as * hyy * sih;
+  sp[3][7] = alf * af * hyy * sih; sp[3][8] = -alf * af * hyy * sih;
+
+  sp[4][1] = 0.0; sp[4][2] = 0.0;
+  sp[4][3] = hyy * D_SQRT_2; sp[4][4] = hyy * D_SQRT_2;
+  sp[4][5] = -als * as * hzz * sih; sp[4][6] = als * as * hzz * sih;
+  sp[4][7] = alf * af * hzz * sih; sp[4][8] = -alf * af * hzz * sih;
+
+  sp[5][1] = 0.0; sp[5][2] = 0.0; sp[5][3] = 0.0; sp[5][4] = 0.0;
+  sp[5][5] = alf * Rho * cc; sp[5][6] = alf * Rho * cc;
+  sp[5][7] = als * Rho * cc; sp[5][8] = als * Rho * cc;
+
+  sp[6][1] = 0.0; sp[6][2] = 1.0; sp[6][3] = 0.0; sp[6][4] = 0.0;
+  sp[6][5] = 0.0; sp[6][6] = 0.0; sp[6][7] = 0.0; sp[6][8] = 0.0;
+
+  sp[7][1] = 0.0; sp[7][2] = 0.0;
+  sp[7][3] = hzz * sq2PiRho * sih; sp[7][4] = -hzz * sq2PiRho * sih;
+  sp[7][5] = 2.0 * als * sqPiRho * c_ * hyy; sp[7][6] = 2.0 * als * sqPiRho * c_ * hyy;
+  sp[7][7] = -2.0 * alf * sqPiRho * c_ * hyy; sp[7][8] = -2.0 * alf * sqPiRho * c_ * hyy;
+
+  sp[8][1] = 0.0; sp[8][2] = 0.0;
+  sp[8][3] = -hyy * sq2PiRho * sih; sp[8][4] = hyy * sq2PiRho * sih;
+  sp[8][5] = 2.0 * als * sqPiRho * c_ * hzz; sp[8][6] = 2.0 * als * sqPiRho * c_ * hzz;
+  sp[8][7] = -2.0 * alf * sqPiRho * c_ * hzz; sp[8][8] = -2.0 * alf * sqPiRho * c_ * hzz;
+
+  so[1][1] = 1.0; so[1][2] = 0.0; so[1][3] = 0.0; so[1][4] = 0.0;
+  so[1][5] = -1.0 / cc; so[1][6] = 0.0; so[1][7] = 0.0; so[1][8] = 0.0;
+
+  so[2][1] = 0.0; so[2][2] = 0.0; so[2][3] = 0.0; so[2][4] = 0.0;
+  so[2][5] = 0.0; so[2][6] = 1.0; so[2][7] = 0.0; so[2][8] = 0.0;
+
+  so[3][1] = 0.0; so[3][2] = 0.0;
+  so[3][3] = -hzz * D_SQRT_2; so[3][4] = hyy * D_SQRT_2;
+  so[3][5] = 0.0; so[3][6] = 0.0;
+  so[3][7] = 0.5 * hzz * sih / sq2PiRho; so[3][8] = -0.5 * hyy * sih / sq2PiRho;
+
+  so[4][1] = 0.0; so[4][2] = 0.0;
+  so[4][3] = -hzz * D_SQRT_2; so[4][4] = hyy * D_SQRT_2;
+  so[4][5] = 0.0; so[4][6] = 0.0;
+  so[4][7] = -0.5 * hzz * sih / sq2PiRho; so[4][8] = 0.5 * hyy * sih / sq2PiRho;
+
+  so[5][1] = 0.0;
+  so[5][2] = 0.5 * alf * af / cc;
+  so[5][3] = -0.5 * als * as * hyy * sih / cc;
+  so[5][4] = -0.5 * als * as * hzz * sih / cc;
+  so[5][5] = 0.5 * alf / (cc * Rho);
+  so[5][6] = 0.0;
+  so[5][7] = 0.25 * als * hyy / (c_ * sqPiRho);
+  so[5][8] = 0.25 * als * hzz / (c_ * sqPiRho);
+
+  so[6][1] = 0.0;
+  so[6][2] = -0.5 * alf * af / cc;
+  so[6][3] = 0.5 * als * as * hyy * sih / cc;
+  so[6][4] = 0.5 * als * as * hzz * sih / cc;
+  so[6][5] = 0.5 * alf / (cc * Rho);
+  so[6][6] = 0.0;
+  so[6][7] = 0.25 * als * hyy / (c_ * sqPiRho);
+  so[6][8] = 0.25 * als * hzz / (c_ * sqPiRho);
+
+  so[7][1] = 0.0;
+  so[7][2] = 0.5 * als * as / cc;
+  so[7][3] = 0.5 * alf * af * hyy * sih / cc;
+  so[7][4] = 0.5 * alf * af * hzz * sih / cc;
+  so[7][5] = 0.5 * als / (Rho * cc);
+  so[7][6] = 0.0;
+  so[7][7] = -0.25 * alf * hyy / (c_ * sqPiRho);
+  so[7][8] = -0.25 * alf * hzz / (c_ * sqPiRho);
+
+  so[8][1] = 0.0;
+  so[8][2] = -0.5 * als * as / cc;
+  so[8][3] = -0.5 * alf * af * hyy * sih / cc;
+  so[8][4] = -0.5 * alf * af * hzz * sih / cc;
+  so[8][5] = 0.5 * als / (Rho * cc);
+  so[8][6] = 0.0;
+  so[8][7] = -0.25 * alf * hyy / (c_ * sqPiRho);
+  so[8][8] = -0.25 * alf * hzz / (c_ * sqPiRho);
+
+  for (int r = 1; r <= 8; ++r) {
+    double s = so[r][1] * du[1];
+    for (int q = 2; q <= 8; ++q) s = s + so[r][q] * du[q];
+    lu[r] = Ae[r] * s;
+  }
+  for (int r = 1; r <= 8; ++r) {
+    double s = sp[r][1] * lu[1];
+    for (int q = 2; q <= 8; ++q) s = s + sp[r][q] * lu[q];
+    ra[r] = s;
+  }
+  ra[5] = ra[1] * kk + Rho * (U * ra[2] + V * ra[3] + W * ra[4]) + ra[5] / hgamma +
+          D_1_4PI * (BX * ra[6] + BY * ra[7] + BZ * ra[8]);
+  ra[2] = U * ra[1] + Rho * ra[2];
+  ra[3] = V * ra[1] + Rho * ra[3];
+  ra[4] = W * ra[1] + Rho * ra[4];
+
+  g[0] = 0.5 * (fl[1] + fr[1] + ra[1]);
+  g[inorm] = 0.5 * (fl[2] + fr[2] + ra[2]);
+  g[itan1] = 0.5 * (fl[3] + fr[3] + ra[3]);
+  g[itan2] = 0.5 * (fl[4] + fr[4] + ra[4]);
+  g[4] = 0.5 * (fl[5] + fr[5] + ra[5]);
+  g[inormB] = 0.5 * (fl[6] + fr[6] + ra[6]);
+  g[itanB1] = 0.5 * (fl[7] + fr[7] + ra[7]);
+  g[itanB2] = 0.5 * (fl[8] + fr[8] + ra[8]);
+}
+
+/* RIEMANN7F, Roe 7-wave (src/Roe7WaveF.ChF:5-558), one face.  Identical to
+   RIEMANNF up to the speeds; the normal-B wave is removed and the normal-B
+   flux is zero (:522). */
+static void roe7_face(const Ctx* c, int idir, const double* wl, const double* wr, double* g) {
+  const double gamma = c->gamma, hgamma = c->hgamma, smallp = c->smallp, smallr = c->smallr;
+  const double del2 = c->del2, smallB = c->smallB;
+  const int inorm = 1 + idir, itan1 = 1 + (idir + 1) % 3, itan2 = 1 + (idir + 2) % 3;
+  const int inormB = 5 + idir, itanB1 = 5 + (idir + 1) % 3, itanB2 = 5 + (idir + 2) % 3;
+  double PGasL, RhoL, UL, VL, WL, RUL, RVL, RWL, BXL, BYL, BZL;
+  double PGasR, RhoR, UR, VR, WR, RUR, RVR, RWR, BXR, BYR, BZR;
+  double PGas, Rho, U, V, W, BX, BY, BZ;
+  double BxBL, RUxUL, PL, EL, AL2, HL, coefRL, BxBR, RUxUR, PR, ER, AR2, HR, coefRR;
+  double BxBH, P, HAV, BXAV, DBX, DBY, DBZ;
+  double aas, as, aaf, af, alf, als, cc, c_, ccmi, ccma, dfs, X;
+  double hyy = 0, hyz, hzz = 0, szb, h, kk, sih, z, del, dell2;
+  double b, bb, BX2, BY2, BZ2, BYZ2, sqPiRho, sq2PiRho;
+  double Ae[8], eig[8], eigmax;
+  double fl[8], fr[8], du[8], lu[8], ra[8];
+  double sp[8][8], so[8][8];
+
+  PGasL = fmax(smallp, wl[4]);
+  RhoL = fmax(smallr, wl[0]);
+  UL = wl[inorm];
+  VL = wl[itan1];
+  WL = wl[itan2];
+  BXL = wl[inormB];
+  BYL = wl[itanB1];
+  BZL = wl[itanB2];
+  PGasR = fmax(smallp, wr[4]);
+  RhoR = fmax(smallr, wr[0]);
+  UR = wr[inorm];
+  VR = wr[itan1];
+  WR = wr[itan2];
+  BXR = wr[inormB];
+  BYR = wr[itanB1];
+  BZR = wr[itanB2];
+
+  RUL = RhoL * UL;
+  RVL = RhoL * VL;
+  RWL = RhoL * WL;
+  BxBL = D_1_8PI * (BXL * BXL + BYL * BYL + BZL * BZL);
+  RUxUL = 0.5 * (RUL * UL + RVL * VL + RWL * WL);
+  PL = PGasL + BxBL;
+  EL = PGasL / hgamma + RUxUL + BxBL;
+  AL2 = gamma * PGasL / RhoL;
+
+  RUR = RhoR * UR;
+  RVR = RhoR * VR;
+  RWR = RhoR * WR;
+  BxBR = D_1_8PI * (BXR * BXR + BYR * BYR + BZR * BZR);
+  RUxUR = 0.5 * (RUR * UR + RVR * VR + RWR * WR);
+  PR = PGasR + BxBR;
+  ER = PGasR / hgamma + RUxUR + BxBR;
+  AR2 = gamma * PGasR / RhoR;
+
+  if (AL2 > AR2) {
+    ccmi = AR2;
+    ccma = AL2;
+  } else {
+    ccmi = AL2;
+    ccma = AR2;
+  }
+
+  if (c->aver == 1) {
+    HL = (EL + PL) / RhoL;
+    HR = (ER + PR) / RhoR;
+    coefRL = 1.0 / (1.0 + sqrt(RhoR / RhoL));
+    coefRR = 1.0 - coefRL;
+    Rho = RhoR * coefRL + RhoL * coefRR;
+    U = UL * coefRL + UR * coefRR;
+    V = VL * coefRL + VR * coefRR;
+    W = WL * coefRL + WR * coefRR;
+    HAV = HL * coefRL + HR * coefRR;
+    BX = BXR * coefRL + BXL * coefRR;
+    BY = BYR * coefRL + BYL * coefRR;
+    BZ = BZR * coefRL + BZL * coefRR;
+    BXAV = 0.5 * (BXL + BXR);
+    BX2 = BXAV * BXAV;
+    BY2 = BY * BY;
+    BZ2 = BZ * BZ;
+    BYZ2 = BY2 + BZ2;
+    BxBH = D_1_8PI * (BX2 + BYZ2);
+    kk = 0.5 * (U * U + V * V + W * W);
+    DBX = BXR - BXL;
+    DBY = BYR - BYL;
+    DBZ = BZR - BZL;
+    X = D_1_8PI * (DBX * DBX + DBY * DBY + DBZ * DBZ) * coefRL * coefRL / RhoL;
+    cc = hgamma * (HAV - kk - D_1_4PI * (BX * BXAV + BYZ2) / Rho) + (2.0 - gamma) * X;
+  } else {
+    Rho = 0.5 * (RhoL + RhoR);
+    U = 0.5 * (UL + UR);
+    V = 0.5 * (VL + VR);
+    W = 0.5 * (WL + WR);
+    BX = 0.5 * (BXL + BXR);
+    BY = 0.5 * (BYL + BYR);
+    BZ = 0.5 * (BZL + BZR);
+    P = 0.5 * (PL + PR);
+    BX2 = BX * BX;
+    BY2 = BY * BY;
+    BZ2 = BZ * BZ;
+    BYZ2 = BY2 + BZ2;
+    BxBH = D_1_8PI * (BX2 + BYZ2);
+    kk = 0.5 * (U * U + V * V + W * W);
+    PGas = P - BxBH;
+    cc = gamma * PGas / Rho;
+  }
+
+  bb = D_1_4PI * BX2 / Rho;
+  b = sqrt(bb);
+  if (cc < ccmi) cc = ccmi;
+  if (cc > ccma) cc = ccma;
+  c_ = sqrt(cc);
+
+  if (BYZ2 < smallB * smallB) {
+    hyy = D_SQRT_2;
+    hzz = D_SQRT_2;
+    if (bb > cc) {
+      aaf = bb;
+      aas = cc;
+      af = b;
+      as = c_;
+    } else {
+      aaf = cc;
+      aas = bb;
+      af = c_;
+      as = b;
+    }
+  } else {
+    hyz = sqrt(BYZ2);
+    hyy = BY / hyz;
+    hzz = BZ / hyz;
+    szb = cc + (BxBH + BxBH) / Rho;
+    h = sqrt(szb * szb - 4.0 * cc * bb);
+    aas = 0.5 * (szb - h);
+    if (aas <= 0.0) {
+      aas = 0.0;
+      as = 0.0;
+    } else if (aas >= cc) {
+      aas = cc;
+      as = c_;
+    } else {
+      as = sqrt(aas);
+    }
+    aaf = 0.5 * (szb + h);
+    if (aaf <= cc) {
+      aaf = cc;
+      af = c_;
+    } else {
+      af = sqrt(aaf);
+    }
+  }
+
+  eig[1] = U;
+  eig[2] = U + b;
+  eig[3] = U - b;
+  eig[4] = U + af;
+  eig[5] = U - af;
+  eig[6] = U + as;
+  eig[7] = U - as;
+  eigmax = fabs(U) + fabs(V) + fabs(W) + af;
+  del = del2 * eigmax;
+  dell2 = del * del;
+  for (int q = 1; q <= 7; ++q) {
+    z = fabs(eig[q]);
+    if (z >= del)
+      Ae[q] = z;
+    else
+      Ae[q] = 0.5 * (z * z + dell2) / del;
+  }
+
+  dfs = aaf - aas;
+  if (dfs < 1.0e-8) {
+    alf = 1.0;
+    als = 0.0;
+  } else if ((cc - aas) <= 0.0) {
+    alf = 0.0;
+    als = 1.0;
+  } else if ((aaf - cc) <= 0.0) {
+    alf = 1.0;
+    als = 0.0;
+  } else {
+    alf = sqrt((cc - aas) / dfs);
+    als = sqrt((aaf - cc) / dfs);
+  }
+
+  sih = -1.0;
+  if (BX >= 0.0) sih = 1.0;
+
+  fl[1] = RUL;
+  fl[2] = UL * RUL - BXL * BXL * D_1_4PI + PL;
+  fl[3] = UL * RVL - BXL * BYL * D_1_4PI;
+  fl[4] = UL * RWL - BXL * BZL * D_1_4PI;
+  fl[5] = UL * (EL + PL) - BXL * (UL * BXL + VL * BYL + WL * BZL) * D_1_4PI;
+  fl[6] = UL * BYL - BXL * VL;
+  fl[7] = UL * BZL - BXL * WL;
+
+  fr[1] = RUR;
+  fr[2] = UR * RUR - BXR * BXR * D_1_4PI + PR;
+  fr[3] = UR * RVR - BXR * BYR * D_1_4PI;
+  fr[4] = UR * RWR - BXR * BZR * D_1_4PI;
+  fr[5] = UR * (ER + PR) - BXR * (UR * BXR + VR * BYR + WR * BZR) * D_1_4PI;
+  fr[6] = UR * BYR - BXR * VR;
+  fr[7] = UR * BZR - BXR * WR;
+
+  du[1] = RhoL - RhoR;
+  du[2] = RUL - RUR;
+  du[3] = RVL - RVR;
+  du[4] = RWL - RWR;
+  du[5] = EL - ER;
+  du[6] = BYL - BYR;
+  du[7] = BZL - BZR;
+
+  du[5] = -hgamma * (-kk * du[1] + U * du[2] + V * du[3] + W * du[4] - du[5] +
+                     (BY * du[6] + BZ * du[7]) * D_1_4PI);
+  du[2] = (-U * du[1] + du[2]) / Rho;
+  du[3] = (-V * du[1] + du[3]) / Rho;
+  du[4] = (-W * du[1] + du[4]) / Rho;
+
+  sqPiRho = sqrt(D_PI * Rho);
+  sq2PiRho = sqrt(D_2PI * Rho);
+
+  sp[1][1] = 1.0; sp[1][2] = 0.0; sp[1][3] = 0.0;
+  sp[1][4] = Rho * alf; sp[1][5] = Rho * alf; sp[1][6] = Rho * als; sp[1][7] = Rho * als;
+
+  sp[2][1] = 0.0; sp[2][2] = 0.0; sp[2][3] = 0.0;
+  sp[2][4] = alf * af; sp[2][5] = -alf * af; sp[2][6] = als * as; sp[2][7] = -als * as;
+
+  sp[3][1] = 0.0;
+  sp[3][2] = -hzz * D_SQRT_2; sp[3][3] = -hzz * D_SQRT_2;
+  sp[3][4] = -als * as * hyy * sih; sp[3][5] = als * as * hyy * sih;
+  sp[3][6] = alf * af * hyy * sih; sp[3][7] = -alf * af * hyy * sih;
+
+  sp[4][1] = 0.0;
+  sp[4][2] = hyy * D_SQRT_2; sp[4][3] = hyy * D_SQRT_2;
+  sp[4][4] = -als * as * hzz * sih; sp[4][5] = als * as * hzz * sih;
+  sp[4][6] = alf * af * hzz * sih; sp[4][7] = -alf * af * hzz * sih;
+
+  sp[5][1] = 0.0; sp[5][2] = 0.0; sp[5][3] = 0.0;
+  sp[5][4] = alf * Rho * cc; sp[5][5] = alf * Rho * cc;
+  sp[5][6] = als * Rho * cc; sp[5][7] = als * Rho * cc;
+
+  sp[6][1] = 0.0;
+  sp[6][2] = hzz * sq2PiRho * sih; sp[6][3] = -hzz * sq2PiRho * sih;
+  sp[6][4] = 2.0 * als * sqPiRho * c_ * hyy; sp[6][5] = 2.0 * als * sqPiRho * c_ * hyy;
+  sp[6][6] = -2.0 * alf * sqPiRho * c_ * hyy; sp[6][7] = -2.0 * alf * sqPiRho * c_ * hyy;
+
+  sp[7][1] = 0.0;
+  sp[7][2] = -hyy * sq2PiRho * sih; sp[7][3] = hyy * sq2PiRho * sih;
+  sp[7][4] = 2.0 * als * sqPiRho * c_ * hzz; sp[7][5] = 2.0 * als * sqPiRho * c_ * hzz;
+  sp[7][6] = -2.0 * alf * sqPiRho * c_ * hzz; sp[7][7] = -2.0 * alf * sqPiRho * c_ * hzz;
+
+  so[1][1] = 1.0; so[1][2] = 0.0; so[1][3] = 0.0; so[1][4] = 0.0;
+  so[1][5] = -1.0 / cc; so[1][6] = 0.0; so[1][7] = 0.0;
+
+  so[2][1] = 0.0; so[2][2] = 0.0;
+  so[2][3] = -hzz * D_SQRT_2; so[2][4] = hyy * D_SQRT_2; so[2][5] = 0.0;
+  so[2][6] = 0.5 * hzz * sih / sq2PiRho; so[2][7] = -0.5 * hyy * sih / sq2PiRho;
+
+  so[3][1] = 0.0; so[3][2] = 0.0;
+  so[3][3] = -hzz * D_SQRT_2; so[3][4] = hyy * D_SQRT_2; so[3][5] = 0.0;
+  so[3][6] = -0.5 * hzz * sih / sq2PiRho; so[3][7] = 0.5 * hyy * sih / sq2PiRho;
+
+  so[4][1] = 0.0;
+  so[4][2] = 0.5 * alf * af / cc;
+  so[4][3] = -0.5 * als * as * hyy * sih / cc;
+  so[4][4] = -0.5 * als * as * hzz * sih / cc;
+  so[4][5] = 0.5 * alf / (cc * Rho);
+  so[4][6] = 0.25 * als * hyy / (c_ * sqPiRho);
+  so[4][7] = 0.25 * als * hzz / (c_ * sqPiRho);
+
+  so[5][1] = 0.0;
+  so[5][2] = -0.5 * alf * af / cc;
+  so[5][3] = 0.5 * als * as * hyy * sih / cc;
+  so[5][4] = 0.5 * als * as * hzz * sih / cc;
+  so[5][5] = 0.5 * alf / (cc * Rho);
+  so[5][6] = 0.25 * als * hyy / (c_ * sqPiRho);
+  so[5][7] = 0.25 * als * hzz / (c_ * sqPiRho);
+
+  so[6][1] = 0.0;
+  so[6][2] = 0.5 * als * as / cc;
+  so[6][3] = 0.5 * alf * af * hyy * sih / cc;
+  so[6][4] = 0.5 * alf * af * hzz * sih / cc;
+  so[6][5] = 0.5 * als / (Rho * cc);
+  so[6][6] = -0.25 * alf * hyy / (c_ * sqPiRho);
+  so[6][7] = -0.25 * alf * hzz / (c_ * sqPiRho);
+
+  so[7][1] = 0.0;
+  so[7][2] = -0.5 * als * as / cc;
+  so[7][3] = -0.5 * alf * af * hyy * sih / cc;
+  so[7][4] = -0.5 * alf * af * hzz * sih / cc;
+  so[7][5] = 0.5 * als / (Rho * cc);
+  so[7][6] = -0.25 * alf * hyy / (c_ * sqPiRho);
+  so[7][7] = -0.25 * alf * hzz / (c_ * sqPiRho);
+
+  for (int r = 1; r <= 7; ++r) {
+    double s = so[r][1] * du[1];
+    for (int q = 2; q <= 7; ++q) s = s + so[r][q] * du[q];
+    lu[r] = Ae[r] * s;
+  }
+  for (int r = 1; r <= 7; ++r) {
+    double s = sp[r][1] * lu[1];
+    for (int q = 2; q <= 7; ++q) s = s + sp[r][q] * lu[q];
+    ra[r] = s;
+  }
+  ra[5] = ra[1] * kk + Rho * (U * ra[2] + V * ra[3] + W * ra[4]) + ra[5] / hgamma +
+          D_1_4PI * (BY * ra[6] + BZ * ra[7]);
+  ra[2] = U * ra[1] + Rho * ra[2];
+  ra[3] = V * ra[1] + Rho * ra[3];
+  ra[4] = W * ra[1] + Rho * ra[4];
+
+  g[0] = 0.5 * (fl[1] + fr[1] + ra[1]);
+  g[inorm] = 0.5 * (fl[2] + fr[2] + ra[2]);
+  g[itan1] = 0.5 * (fl[3] + fr[3] + ra[3]);
+  g[itan2] = 0.5 * (fl[4] + fr[4] + ra[4]);
+  g[4] = 0.5 * (fl[5] + fr[5] + ra[5]);
+  g[itanB1] = 0.5 * (fl[6] + fr[6] + ra[6]);
+  g[itanB2] = 0.5 * (fl[7] + fr[7] + ra[7]);
+  g[inormB] = 0.0;
+}
+
+/* RUSANOVF (src/RusanovF.ChF:4-197), one face. */
+static void rusanov_face(const Ctx* c, int idir, const double* wl, const double* wr, double* g) {
+  const double gamma = c->gamma, hgamma = c->hgamma, smallp = c->smallp, smallr = c->smallr;
+  const int inorm = 1 + idir, itan1 = 1 + (idir + 1) % 3, itan2 = 1 + (idir + 2) % 3;
+  const int inormB = 5 + idir, itanB1 = 5 + (idir + 1) % 3, itanB2 = 5 + (idir + 2) % 3;
+  double PGasL = fmax(smallp, wl[4]), RhoL = fmax(smallr, wl[0]);
+  double UL = wl[inorm], VL = wl[itan1], WL = wl[itan2];
+  double BXL = wl[inormB], BYL = wl[itanB1], BZL = wl[itanB2];
+  double PGasR = fmax(smallp, wr[4]), RhoR = fmax(smallr, wr[0]);
+  double UR = wr[inorm], VR = wr[itan1], WR = wr[itan2];
+  double BXR = wr[inormB], BYR = wr[itanB1], BZR = wr[itanB2];
+  double RUL = RhoL * UL, RVL = RhoL * VL, RWL = RhoL * WL;
+  double BxBL = D_1_8PI * (BXL * BXL + BYL * BYL + BZL * BZL);
+  double RUxUL = 0.5 * (RUL * UL + RVL * VL + RWL * WL);
+  double PL = PGasL + BxBL;
+  double EL = PGasL / hgamma + RUxUL + BxBL;
+  double BXL_4PI = BXL * D_1_4PI;
+  double RUR = RhoR * UR, RVR = RhoR * VR, RWR = RhoR * WR;
+  double BxBR = D_1_8PI * (BXR * BXR + BYR * BYR + BZR * BZR);
+  double RUxUR = 0.5 * (RUR * UR + RVR * VR + RWR * WR);
+  double PR = PGasR + BxBR;
+  double ER = PGasR / hgamma + RUxUR + BxBR;
+  double BXR_4PI = BXR * D_1_4PI;
+  double Rho, U, BX2, BxBH, A2;
+  if (c->aver == 1) {
+    double HL = (EL + PL) / RhoL, HR = (ER + PR) / RhoR;
+    double coefRL = 1.0 / (1.0 + sqrt(RhoR / RhoL));
+    double coefRR = 1.0 - coefRL;
+    Rho = RhoR * coefRL + RhoL * coefRR;
+    U = UL * coefRL + UR * coefRR;
+    double V = VL * coefRL + VR * coefRR;
+    double W = WL * coefRL + WR * coefRR;
+    double HAV = HL * coefRL + HR * coefRR;
+    double BX = BXR * coefRL + BXL * coefRR;
+    double BY = BYR * coefRL + BYL * coefRR;
+    double BZ = BZR * coefRL + BZL * coefRR;
+    double BXAV = 0.5 * (BXL + BXR);
+    BX2 = BXAV * BXAV;
+    double BY2 = BY * BY, BZ2 = BZ * BZ;
+    double BYZ2 = BY2 + BZ2;
+    BxBH = D_1_8PI * (BX2 + BYZ2);
+    double kk = 0.5 * (U * U + V * V + W * W);
+    double DBX = BXR - BXL, DBY = BYR - BYL, DBZ = BZR - BZL;
+    double X = D_1_8PI * (DBX * DBX + DBY * DBY + DBZ * DBZ) * coefRL * coefRL / RhoL;
+    A2 = hgamma * (HAV - kk - D_1_4PI * (BX * BXAV + BYZ2) / Rho) + (2.0 - gamma) * X;
+  } else {
+    Rho = 0.5 * (RhoL + RhoR);
+    U = 0.5 * (UL + UR);
+    double BX = 0.5 * (BXL + BXR), BY = 0.5 * (BYL + BYR), BZ = 0.5 * (BZL + BZR);
+    double PGas = 0.5 * (PGasL + PGasR);
+    BX2 = BX * BX;
+    double BY2 = BY * BY, BZ2 = BZ * BZ;
+    BxBH = D_1_8PI * (BX2 + BY2 + BZ2);
+    A2 = gamma * PGas / Rho;
+  }
+  double bb = D_1_4PI * BX2 / Rho;
+  double szb = A2 + (BxBH + BxBH) / Rho;
+  double h = sqrt(szb * szb - 4.0 * A2 * bb);
+  double aaf = 0.5 * (szb + h);
+  double af = sqrt(aaf);
+  double eigmax = fabs(U) + af;
+  double fl[9], fr[9], du[9];
+  fl[1] = RUL;
+  fl[2] = UL * RUL - BXL_4PI * BXL + PL;
+  fl[3] = UL * RVL - BXL_4PI * BYL;
+  fl[4] = UL * RWL - BXL_4PI * BZL;
+  fl[5] = UL * (EL + PL) - BXL_4PI * (UL * BXL + VL * BYL + WL * BZL);
+  fl[6] = 0.0;
+  fl[7] = UL * BYL - BXL * VL;
+  fl[8] = UL * BZL - BXL * WL;
+  fr[1] = RUR;
+  fr[2] = UR * RUR - BXR_4PI * BXR + PR;
+  fr[3] = UR * RVR - BXR_4PI * BYR;
+  fr[4] = UR * RWR - BXR_4PI * BZR;
+  fr[5] = UR * (ER + PR) - BXR_4PI * (UR * BXR + VR * BYR + WR * BZR);
+  fr[6] = 0.0;
+  fr[7] = UR * BYR - BXR * VR;
+  fr[8] = UR * BZR - BXR * WR;
+  du[1] = RhoL - RhoR;
+  du[2] = RUL - RUR;
+  du[3] = RVL - RVR;
+  du[4] = RWL - RWR;
+  du[5] = EL - ER;
+  du[6] = BXL - BXR;
+  du[7] = BYL - BYR;
+  du[8] = BZL - BZR;
+  g[0] = 0.5 * (fl[1] + fr[1] + eigmax * du[1]);
+  g[inorm] = 0.5 * (fl[2] + fr[2] + eigmax * du[2]);
+  g[itan1] = 0.5 * (fl[3] + fr[3] + eigmax * du[3]);
+  g[itan2] = 0.5 * (fl[4] + fr[4] + eigmax * du[4]);
+  g[4] = 0.5 * (fl[5] + fr[5] + eigmax * du[5]);
+  g[inormB] = 0.5 * (fl[6] + fr[6] + eigmax * du[6]);
+  g[itanB1] = 0.5 * (fl[7] + fr[7] + eigmax * du[7]);
+  g[itanB2] = 0.5 * (fl[8] + fr[8] + eigmax * du[8]);
+}
+
+/* DEDNER2X2F (src/DednerF.ChF:89-170): (Bn, psi) flux with speed Ch. */
+static void dedner_face(const Ctx* c, int idir, const double* wl, const double* wr, double* g) {
+  const int inormB = 5 + idir, iPsi = 8;
+  double dCh = c->dCh, dCh2 = dCh * dCh;
+  double sp11 = 1.0, sp12 = 1.0, sp21 = -dCh, sp22 = dCh;
+  double so11 = 0.5, so12 = -0.5 / dCh, so21 = 0.5, so22 = 0.5 / dCh;
+  double BXL = wl[inormB], PsiL = wl[iPsi], BXR = wr[inormB], PsiR = wr[iPsi];
+  double Aeigen1 = dCh, Aeigen2 = dCh;
+  double fl1 = PsiL, fl2 = dCh2 * BXL, fr1 = PsiR, fr2 = dCh2 * BXR;
+  double du1 = BXL - BXR, du2 = PsiL - PsiR;
+  double lu1 = Aeigen1 * (so11 * du1 + so12 * du2);
+  double lu2 = Aeigen2 * (so21 * du1 + so22 * du2);
+  double ra1 = sp11 * lu1 + sp12 * lu2;
+  double ra2 = sp21 * lu1 + sp22 * lu2;
+  g[inormB] = 0.5 * (fl1 + fr1 + ra1);
+  g[iPsi] = 0.5 * (fl2 + fr2 + ra2);
+}
+
+/* VANLEERF (src/VanLeerRSF.ChF:4-130): van Leer flux-vector splitting of one
+   Euler fluid whose density sits at index irho. */
+static void vanleer_face(const Ctx* c, int idir, int irho, const double* wl, const double* wr,
+                         double* g) {
+  const double gamma = c->gamma, hgamma = c->hgamma, smallp = c->smallp, smallr = c->smallr;
+  const int iPres = irho + 4;
+  const int inorm = irho + 1 + idir, itan1 = irho + 1 + (idir + 1) % 3,
+            itan2 = irho + 1 + (idir + 2) % 3;
+  double fl1, fl2, fl3, fl4, fl5, fr1, fr2, fr3, fr4, fr5;
+  double PGasL = fmax(smallp, wl[iPres]), RhoL = fmax(smallr, wl[irho]);
+  double UL = wl[inorm], VL = wl[itan1], WL = wl[itan2];
+  double RUL = RhoL * UL, RVL = RhoL * VL, RWL = RhoL * WL;
+  double RUxUL = 0.5 * (RUL * UL + RVL * VL + RWL * WL);
+  double EL = PGasL / hgamma + RUxUL;
+  double AL2 = gamma * PGasL / RhoL;
+  double AL = sqrt(AL2);
+  if (UL <= -AL) {
+    fr1 = fr2 = fr3 = fr4 = fr5 = 0.0;
+  } else if (UL >= AL) {
+    fr1 = RhoL * UL;
+    fr2 = fr1 * UL + PGasL;
+    fr3 = fr1 * VL;
+    fr4 = fr1 * WL;
+    fr5 = UL * (EL + PGasL);
+  } else {
+    double UA = (-UL + (AL + AL)) / gamma;
+    double H = (EL + PGasL) / RhoL;
+    double HU = UL + AL;
+    fr1 = 0.25 * RhoL * HU * HU / AL;
+    fr2 = fr1 * (UL + UA);
+    fr3 = fr1 * (VL);
+    fr4 = fr1 * (WL);
+    fr5 = fr1 * (H);
+  }
+  double PGasR = fmax(smallp, wr[iPres]), RhoR = fmax(smallr, wr[irho]);
+  double UR = wr[inorm], VR = wr[itan1], WR = wr[itan2];
+  double RUR = RhoR * UR, RVR = RhoR * VR, RWR = RhoR * WR;
+  double RUxUR = 0.5 * (RUR * UR + RVR * VR + RWR * WR);
+  double ER = PGasR / hgamma + RUxUR;
+  double AR2 = gamma * PGasR / RhoR;
+  double AR = sqrt(AR2);
+  if (UR >= AR) {
+    fl1 = fl2 = fl3 = fl4 = fl5 = 0.0;
+  } else if (UR <= -AR) {
+    fl1 = RhoR * UR;
+    fl2 = fl1 * UR + PGasR;
+    fl3 = fl1 * VR;
+    fl4 = fl1 * WR;
+    fl5 = UR * (ER + PGasR);
+  } else {
+    double UA = (-UR - (AR + AR)) / gamma;
+    double H = (ER + PGasR) / RhoR;
+    double HU = UR - AR;
+    fl1 = -0.25 * RhoR * HU * HU / AR;
+    fl2 = fl1 * (UR + UA);
+    fl3 = fl1 * (VR);
+    fl4 = fl1 * (WR);
+    fl5 = fl1 * (H);
+  }
+  g[irho] = fl1 + fr1;
+  g[inorm] = fl2 + fr2;
+  g[itan1] = fl3 + fr3;
+  g[itan2] = fl4 + fr4;
+  g[iPres] = fl5 + fr5;
+}
+
+/* PatchMHDMF::fluxesRP (srcIdeal/PatchMHDMF.cpp:408-440) on one face. */
+static void face_flux(const Ctx* c, int dir, const double* wl, const double* wr, double* g) {
+  if (c->rs == RS_ROE8)
+    roe8_face(c, dir, wl, wr, g);
+  else if (c->rs == RS_ROE7)
+    roe7_face(c, dir, wl, wr, g);
+  else
+    rusanov_face(c, dir, wl, wr, g);
+  if (c->glm) dedner_face(c, dir, wl, wr, g);
+  for (int f = 1; f < c->nf; ++f) vanleer_face(c, dir, c->irhon + (f - 1) * 5, wl, wr, g);
+}
+
+/* ------------------------------------------------------------------------ */
+/* sources                                                                   */
+/* ------------------------------------------------------------------------ */
+
+/* DEFINE_REGIONS_2F (swlism/SWLISMF.ChF:654-742), Cartesian branch. */
+static int region_cell(const Ctx* c, int i, int j, int k, const double* W) {
+  const mf_params* p = c->p;
+  double dx = p->dx;
+  double LIMSUN = 0.6 * p->sun_v;
+  double coeff = p->region_t_coeff;
+  double sunR2 = p->sun_r * p->sun_r;
+  double x = (i + 0.5) * dx - p->sun_center[0];
+  double y = (j + 0.5) * dx - p->sun_center[1];
+  double z = 0.0, r2, invr, ur;
+  if (c->sd == 3) {
+    z = (k + 0.5) * dx - p->sun_center[2];
+    r2 = x * x + y * y + z * z;
+    invr = 1.0 / sqrt(r2);
+    ur = W[1] * (x * invr) + W[2] * (y * invr) + W[3] * (z * invr);
+  } else {
+    r2 = x * x + y * y;
+    invr = 1.0 / sqrt(r2);
+    ur = W[1] * (x * invr) + W[2] * (y * invr);
+  }
+  double TEMP = coeff * W[4] / W[0];
+  int reg;
+  if (fabs(ur) >= LIMSUN) {
+    if ((TEMP >= 1.0e6) && (r2 > sunR2))
+      reg = 2;
+    else
+      reg = 3;
+    if (c->sd == 3 && ((z < p->region_zbot) || (z > p->region_ztop))) reg = 1;
+  } else {
+    if (TEMP >= p->region_tmlim) {
+      reg = 2;
+      if (c->sd == 3 && ((z < p->region_zbot) || (z > p->region_ztop))) reg = 1;
+    } else {
+      reg = 1;
+    }
+  }
+  return reg;
+}
+
+/* Neutral fluid that receives the newly created neutrals in region REG:
+   CHARGE_EXCHANGE_2F/3F/4F/MF (swlism/ChargeExchange2F.ChF:294-432,
+   434-671, 673-993, 995-1149). 0 = none. */
+static int ce_recipient(int nN, int reg) {
+  if (nN == 1) return (reg == 1 || reg == 4) ? 1 : 0;
+  if (nN == 2) return (reg == 1) ? 1 : (reg == 2) ? 2 : 0;
+  if (nN == 3) return (reg == 1 || reg == 4) ? 1 : (reg == 2) ? 2 : (reg == 3) ? 3 : 0;
+  return (reg >= 1 && reg <= nN) ? reg : 0;
+}
+
+/* Charge-exchange source of one cell (Pauls & Zank rates), S = -dt*H.  The
+   cross-section is parametric: sigma(v) = scale*(a - b ln(v*scaleVel))^2,
+   optionally damped by (1-exp(-c/(v*scaleVel)))^pow (the reference's Lindsay &
+   Stebbings form is a=13.493, b=0.531, c=2.946e9, pow=4.5).  S[0] and the
+   magnetic (and psi) entries are zero. */
+static void charge_exchange_cell(const Ctx* c, const double* W, int reg, double dt, double* S) {
+  const mf_params* p = c->p;
+  const int nN = c->nf - 1;
+  double rho = W[0], ux = W[1], uy = W[2], uz = W[3], pp = W[4];
+  double U2 = ux * ux + uy * uy + uz * uz;
+  double VVTP = pp / rho;
+  double h2 = 0, h3 = 0, h4 = 0, h5 = 0, PPLUX = 0, PPLUY = 0, PPLUZ = 0, ENPLU = 0;
+  double DENPLU[MF_MAX_FLUIDS], PMIX[MF_MAX_FLUIDS], PMIY[MF_MAX_FLUIDS], PMIZ[MF_MAX_FLUIDS],
+      ENMI[MF_MAX_FLUIDS];
+  for (int f = 1; f <= nN; ++f) {
+    int s = c->irhon + (f - 1) * 5;
+    double rhoN = W[s], uxN = W[s + 1], uyN = W[s + 2], uzN = W[s + 3], pN = W[s + 4];
+    double UH2 = uxN * uxN + uyN * uyN + uzN * uzN;
+    double DU2 = (ux - uxN) * (ux - uxN) + (uy - uyN) * (uy - uyN) + (uz - uzN) * (uz - uzN);
+    double VPHH = (ux - uxN) * uxN + (uy - uyN) * uyN + (uz - uzN) * uzN;
+    double VPHP = (ux - uxN) * ux + (uy - uyN) * uy + (uz - uzN) * uz;
+    double VVTH = 2.0 * pN / rhoN;
+    double UD = sqrt(4.0 * (VVTP + VVTH) / D_PI + DU2);
+    double UPM = sqrt(16.0 * VVTP / D_PI + 2.25 * D_PI * VVTH + 4.0 * DU2);
+    double UHM = sqrt(2.25 * D_PI * VVTP + 16.0 * VVTH / D_PI + 4.0 * DU2);
+    double UPE = sqrt((4.0 * VVTP + 64.0 * VVTH / 9.0) / D_PI + DU2);
+    double UHE = sqrt((64.0 * VVTP / 9.0 + 4.0 * VVTH) / D_PI + DU2);
+    double UDS = p->ce_scale_vel * UD;
+    double t = p->ce_sigma_a - p->ce_sigma_b * log(UDS);
+    double SIGMAL = t * t;
+    if (p->ce_damp_c > 0.0) SIGMAL = SIGMAL * pow(1.0 - exp(-p->ce_damp_c / UDS), p->ce_damp_pow);
+    SIGMAL = p->ce_sigma_scale * SIGMAL;
+    double ARR = SIGMAL * rhoN * rho;
+    double VVTHU = VVTH / UPM;
+    h2 = h2 + ARR * (ux - uxN) * (UD + VVTHU + VVTP / UHM);
+    h3 = h3 + ARR * (uy - uyN) * (UD + VVTHU + VVTP / UHM);
+    h4 = h4 + ARR * (uz - uzN) * (UD + VVTHU + VVTP / UHM);
+    h5 = h5 + 0.5 * ARR *
+                  (1.5 * (UHE * VVTP - UPE * VVTH) + UD * (U2 - UH2) +
+                   2.0 * (VVTHU * VPHH + VVTP * VPHP / UHM));
+    DENPLU[f] = -ARR * UD;
+    PPLUX = PPLUX - ARR * (ux * UD - (uxN - ux) * VVTP / UHM);
+    PPLUY = PPLUY - ARR * (uy * UD - (uyN - uy) * VVTP / UHM);
+    PPLUZ = PPLUZ - ARR * (uz * UD - (uzN - uz) * VVTP / UHM);
+    ENPLU = ENPLU - ARR * (0.5 * U2 * UD + VVTP * (VPHP / UHM + 0.75 * UHE));
+    PMIX[f] = ARR * (uxN * UD + (uxN - ux) * VVTHU);
+    PMIY[f] = ARR * (uyN * UD + (uyN - uy) * VVTHU);
+    PMIZ[f] = ARR * (uzN * UD + (uzN - uz) * VVTHU);
+    ENMI[f] = ARR * (0.5 * UH2 * UD - VPHH * VVTHU + 0.75 * VVTH * UPE);
+  }
+  for (int q = 0; q < c->nc; ++q) S[q] = 0.0;
+  S[1] = -dt * h2;
+  S[2] = -dt * h3;
+  S[3] = -dt * h4;
+  S[4] = -dt * h5;
+  int rk = ce_recipient(nN, reg);
+  for (int f = 1; f <= nN; ++f) {
+    double H1, H2, H3, H4, H5;
+    if (f == rk) {
+      if (nN <= 3) {
+        /* 2F/3F/4F: sum of the other populations in index order */
+        int first = 1;
+        H1 = 0.0;
+        for (int q = 1; q <= nN; ++q) {
+          if (q == f) continue;
+          if (first) {
+            H1 = DENPLU[q];
+            first = 0;
+          } else {
+            H1 = H1 + DENPLU[q];
+          }
+        }
+      } else {
+        /* MF: sum(DENPLU) - DENPLU(iFluid) */
+        double sum = DENPLU[1];
+        for (int q = 2; q <= nN; ++q) sum = sum + DENPLU[q];
+        H1 = sum - DENPLU[f];
+      }
+      H2 = PPLUX + PMIX[f];
+      H3 = PPLUY + PMIY[f];
+      H4 = PPLUZ + PMIZ[f];
+      H5 = ENPLU + ENMI[f];
+    } else {
+      H1 = -DENPLU[f];
+      H2 = PMIX[f];
+      H3 = PMIY[f];
+      H4 = PMIZ[f];
+      H5 = ENMI[f];
+    }
+    int s = c->irhon + (f - 1) * 5;
+    S[s] = -dt * H1;
+    S[s + 1] = -dt * H2;
+    S[s + 2] = -dt * H3;
+    S[s + 3] = -dt * H4;
+    S[s + 4] = -dt * H5;
+  }
+}
+
+/* HELIOREINIT_DEFAULT (swlism/HeliosphericPlasmaBCF.ChF:1435-1555) with a
+   monopolar field: the plasma inside r <= Rinit is reset to the radial wind. */
+static void reinit_cell(const Ctx* c, int i, int j, int k, double* U) {
+  const mf_params* p = c->p;
+  double dx = p->dx;
+  double x = (i + 0.5) * dx - p->sun_center[0];
+  double y = (j + 0.5) * dx - p->sun_center[1];
+  double z = 0.0;
+  if (c->sd == 3) z = (k + 0.5) * dx - p->sun_center[2];
+  double r2 = (c->sd == 3) ? (x * x + y * y + z * z) : (x * x + y * y);
+  double sunR2 = p->reinit_r0 * p->reinit_r0;
+  if (!(r2 <= sunR2)) return;
+  double r = sqrt(r2);
+  double rr = r / p->sun_int_bc_radius;
+  double xy = sqrt(x * x + y * y);
+  double cosT = z / r;
+  double sinT = sqrt(1.0 - cosT * cosT);
+  double cosF = x / xy;
+  double sinF = y / xy;
+  double rho = p->sun_rho / (rr * rr);
+  double ux = p->sun_v * sinT * cosF;
+  double uy = p->sun_v * sinT * sinF;
+  double uz = p->sun_v * cosT;
+  double pr = p->sun_p / pow(rr, 2.0 * c->gamma);
+  double br = p->dir_br * p->sun_b / (rr * rr);
+  double bp = -p->sun_beta * br * r * sinT;
+  double bx = br * sinT * cosF - bp * sinF;
+  double by = br * sinT * sinF + bp * cosF;
+  double bz = br * cosT;
+  double b = bx * bx + by * by + bz * bz;
+  double e0 = pr / c->hgamma + 0.5 * (rho * p->sun_v * p->sun_v + D_1_4PI * b);
+  U[0] = rho;
+  U[1] = rho * ux;
+  U[2] = rho * uy;
+  U[3] = rho * uz;
+  U[4] = e0;
+  U[5] = bx;
+  U[6] = by;
+  U[7] = bz;
+}
+
+/* POSTPROCESSING (srcIdeal/PatchIdealMHDF.ChF:1019-1070) and
+   POSTPROCESSING_MF (srcIdeal/PatchMHDMFF.ChF:301-511). */
+static void positivity_cell(const Ctx* c, double* U) {
+  const double hgamma = c->hgamma, smallR = c->smallr, smallP = c->smallp;
+  if (c->nf == 1) {
+    double Rho = U[0];
+    int iWas = 0;
+    if (Rho < smallR) {
+      Rho = smallR;
+      iWas = 1;
+    }
+    double invRho = 1.0 / Rho;
+    double Ux = U[1] * invRho, Uy = U[2] * invRho, Uz = U[3] * invRho;
+    double E = U[4];
+    double Bx = U[5], By = U[6], Bz = U[7];
+    double BxB = D_1_8PI * (Bx * Bx + By * By + Bz * Bz);
+    double UxU = 0.5 * (Ux * Ux + Uy * Uy + Uz * Uz);
+    double P = hgamma * (E - BxB - Rho * UxU);
+    if (P < smallP) {
+      P = smallP;
+      iWas = 1;
+    }
+    if (iWas == 1) {
+      U[0] = Rho;
+      U[4] = P / hgamma + Rho * UxU + BxB;
+    }
+    return;
+  }
+  {
+    double Rho = U[0];
+    double invRho = 1.0 / Rho;
+    double Ux = U[1] * invRho, Uy = U[2] * invRho, Uz = U[3] * invRho;
+    double E = U[4];
+    double Bx = U[5], By = U[6], Bz = U[7];
+    double BxB = D_1_8PI * (Bx * Bx + By * By + Bz * Bz);
+    double UxU = 0.5 * (Ux * Ux + Uy * Uy + Uz * Uz);
+    double P = hgamma * (E - BxB - Rho * UxU);
+    int iWas = 0;
+    if (Rho < smallR) {
+      Rho = smallR;
+      iWas = 1;
+    }
+    if (P < smallP) {
+      P = smallP;
+      iWas = 1;
+    }
+    if (iWas == 1) {
+      U[0] = Rho;
+      U[1] = Rho * Ux;
+      U[2] = Rho * Uy;
+      U[3] = Rho * Uz;
+      U[4] = P / hgamma + Rho * UxU + BxB;
+    }
+  }
+  for (int f = 1; f < c->nf; ++f) {
+    double fd, fp;
+    if (f == 1) {
+      fd = smallR;
+      fp = smallP;
+    } else if (f == 3) {
+      fd = NETF3_DENS;
+      fp = NETF3_PRES;
+    } else {
+      fd = NETF2_DENS;
+      fp = NETF2_PRES;
+    }
+    int s = c->irhon + (f - 1) * 5;
+    double Rho = U[s];
+    double invRho = 1.0 / Rho;
+    double Ux = U[s + 1] * invRho, Uy = U[s + 2] * invRho, Uz = U[s + 3] * invRho;
+    double E = U[s + 4];
+    double UxU = 0.5 * (Ux * Ux + Uy * Uy + Uz * Uz);
+    double P = hgamma * (E - Rho * UxU);
+    int iWas = 0;
+    if (Rho < fd) {
+      Rho = fd;
+      iWas = 1;
+    }
+    if (P < fp) {
+      P = fp;
+      iWas = 1;
+    }
+    if (iWas == 1) {
+      U[s] = Rho;
+      U[s + 1] = Rho * Ux;
+      U[s + 2] = Rho * Uy;
+      U[s + 3] = Rho * Uz;
+      U[s + 4] = P / hgamma + Rho * UxU;
+    }
+  }
+}
+
+/* ------------------------------------------------------------------------ */
+/* physical boundary: primitive ghost cells outside the domain               */
+/* ------------------------------------------------------------------------ */
+
+/* Far-field ghost fill after HELIOGS (swlism/HeliosphericF.ChF:978-1140): the
+   plasma and neutral fluid 1 take the far-field state, the other neutral
+   fluids copy the nearest cell inside the domain along the boundary normal.
+   Applied per direction in order 0,1,2 over the part of W's box outside the
+   domain in that direction (HeliosphericProblem::fillGhostCells,
+   swlism/HeliosphericProblem.cpp:1663-1760). */
+static void fill_ghost_cells(const Ctx* c, Fab* W) {
+  const mf_params* p = c->p;
+  if (p->bc_kind != MF_BC_FARFIELD) return;
+  for (int d = 0; d < c->sd; ++d) {
+    if (p->periodic[d]) continue;
+    for (int side = 0; side < 2; ++side) {
+      mf_box bb = W->b;
+      int edge;
+      if (side == 0) {
+        if (bb.lo[d] >= p->domain_lo[d]) continue;
+        bb.hi[d] = p->domain_lo[d] - 1;
+        edge = p->domain_lo[d];
+      } else {
+        if (bb.hi[d] <= p->domain_hi[d]) continue;
+        bb.lo[d] = p->domain_hi[d] + 1;
+        edge = p->domain_hi[d];
+      }
+      FOR_BOX(bb, i, j, k) {
+        for (int q = 0; q < 8; ++q) AT(W, i, j, k, q) = p->bc_plasma[q];
+        if (c->glm) AT(W, i, j, k, 8) = 0.0;
+        if (c->nf > 1)
+          for (int q = 0; q < 5; ++q) AT(W, i, j, k, c->irhon + q) = p->bc_neutral1[q];
+        for (int f = 2; f < c->nf; ++f) {
+          int ii = i, jj = j, kk = k;
+          if (d == 0) ii = edge;
+          if (d == 1) jj = edge;
+          if (d == 2) kk = edge;
+          int s = c->irhon + (f - 1) * 5;
+          for (int q = 0; q < 5; ++q) AT(W, i, j, k, s + q) = AT(W, ii, jj, kk, s + q);
+        }
+      }
+    }
+  }
+}
+
+/* ------------------------------------------------------------------------ */
+/* EulerStep                                                                 */
+/* ------------------------------------------------------------------------ */
+
+/* PatchMHDAM::EulerStep (src/PatchMHDAM.cpp:495-709) for PatchMHDMF. */
+static int euler_step(const Ctx* c, double time, Fab* U, Fab* F /* [sd] or NULL */, Fab* divBout,
+                      double dt, mf_box a_box) {
+  const mf_params* p = c->p;
+  const int sd = c->sd, nc = c->nc, np = c->nprim;
+  (void)time;
+  mf_box UBox = U->b;
+  /* With a far-field boundary the primitive ghosts outside the domain come
+     from the boundary state; otherwise the caller filled U's ghosts. */
+  mf_box WBoxB = (p->bc_kind == MF_BC_FARFIELD) ? box_and_domain(UBox, p) : UBox;
+  Fab Uold = fab_alloc(UBox, nc);
+  memcpy(Uold.p, U->p, sizeof(double) * (size_t)(Uold.csz * nc));
+  Fab W = fab_alloc(UBox, np);
+  double u[MF_MAX_COMP], w[MF_MAX_COMP];
+
+  /* stateToPrim on UBox & domain, then fillGhostCells */
+  FOR_BOX(WBoxB, i, j, k) {
+    for (int q = 0; q < nc; ++q) u[q] = AT(U, i, j, k, q);
+    cons_to_prim_cell(c, u, w);
+    for (int q = 0; q < np; ++q) AT(&W, i, j, k, q) = w[q];
+  }
+  fill_ghost_cells(c, &W);
+
+  mf_box valueBox = box_and_domain(a_box, p);
+  mf_box slopeBox = box_grow(valueBox, 1, sd);
+
+  /* reconstruction: WMinus = value on the low face, WPlus on the high face */
+  Fab Wm[3], Wp[3];
+  for (int d = 0; d < sd; ++d) {
+    Wm[d] = fab_alloc(slopeBox, np);
+    Wp[d] = fab_alloc(slopeBox, np);
+    int o[3] = {0, 0, 0};
+    o[d] = 1;
+    FOR_BOX(slopeBox, i, j, k) {
+      for (int v = 0; v < np; ++v) {
+        double lo, hi;
+        face_values(limiter_of(c, v), AT(&W, i - o[0], j - o[1], k - o[2], v), AT(&W, i, j, k, v),
+                    AT(&W, i + o[0], j + o[1], k + o[2], v), &lo, &hi);
+        AT(&Wm[d], i, j, k, v) = lo;
+        AT(&Wp[d], i, j, k, v) = hi;
+      }
+    }
+    if (p->check_positivity) {
+      /* CHECKPOSITIVITY on rho and p, REDUCEORDER on every variable
+         (src/Reconstruction.cpp:209-234) */
+      FOR_BOX(slopeBox, i, j, k) {
+        int neg = 0;
+        if (AT(&Wm[d], i, j, k, 0) <= 0.0) neg = 1;
+        if (AT(&Wp[d], i, j, k, 0) <= 0.0) neg = 1;
+        if (AT(&Wm[d], i, j, k, 4) <= 0.0) neg = 1;
+        if (AT(&Wp[d], i, j, k, 4) <= 0.0) neg = 1;
+        if (neg)
+          for (int v = 0; v < np; ++v) {
+            AT(&Wm[d], i, j, k, v) = AT(&W, i, j, k, v);
+            AT(&Wp[d], i, j, k, v) = AT(&W, i, j, k, v);
+          }
+      }
+    }
+  }
+
+  /* fluxes on fluxBox = surroundingNodes(valueBox): interior faces by the
+     Riemann solvers, domain-boundary faces (fluxBC) by the same solvers on
+     the ghost-filled states; Bn = average of the two face states, one-sided
+     on non-periodic domain faces (PatchMHDMF::computeBn :509-620). */
+  Fab Fl[3], Bn[3];
+  for (int d = 0; d < sd; ++d) {
+    mf_box fb = box_nodes(valueBox, d);
+    Fl[d] = fab_alloc(fb, nc);
+    Bn[d] = fab_alloc(fb, 1);
+    int o[3] = {0, 0, 0};
+    o[d] = 1;
+    double wl[MF_MAX_COMP], wr[MF_MAX_COMP], g[MF_MAX_COMP];
+    FOR_BOX(fb, i, j, k) {
+      for (int v = 0; v < np; ++v) {
+        wl[v] = AT(&Wp[d], i - o[0], j - o[1], k - o[2], v);
+        wr[v] = AT(&Wm[d], i, j, k, v);
+      }
+      for (int q = 0; q < nc; ++q) g[q] = NAN;
+      face_flux(c, d, wl, wr, g);
+      for (int q = 0; q < nc; ++q) AT(&Fl[d], i, j, k, q) = g[q];
+      int f = (d == 0) ? i : (d == 1) ? j : k;
+      double bn;
+      if (p->divb_method == 2) {
+        bn = 0.5 * (AT(&W, i - o[0], j - o[1], k - o[2], 5 + d) + AT(&W, i, j, k, 5 + d));
+      } else {
+        bn = 0.5 * (wl[5 + d] + wr[5 + d]);
+        if (!p->periodic[d]) {
+          if (f == p->domain_lo[d]) bn = wr[5 + d];
+          if (f == p->domain_hi[d] + 1) bn = wl[5 + d];
+        }
+      }
+      if (p->divb_method == 0) bn = 0.0;
+      AT(&Bn[d], i, j, k, 0) = bn;
+    }
+  }
+
+  /* finalUpdate -> UPDATECONS (src/PatchMHDAMF.ChF:542-587) */
+  double invvol = 1.0 / p->dx;
+  for (int d = 0; d < sd; ++d) {
+    int o[3] = {0, 0, 0};
+    o[d] = 1;
+    for (int q = 0; q < nc; ++q) {
+      FOR_BOX(valueBox, i, j, k) {
+        AT(U, i, j, k, q) = AT(U, i, j, k, q) - dt * invvol *
+                                                    (AT(&Fl[d], i + o[0], j + o[1], k + o[2], q) -
+                                                     AT(&Fl[d], i, j, k, q));
+      }
+    }
+  }
+
+  /* addExplicitSources (srcIdeal/PatchMHDMF.cpp:1149-1389) */
+  double psicoef = 0.0;
+  if (c->glm) psicoef = exp(-dt * c->dCh * c->dCh / (c->dCp * c->dCp));
+  double dtbydx = dt / p->dx;
+  double S[MF_MAX_COMP];
+  FOR_BOX(valueBox, i, j, k) {
+    double divB = 0.0;
+    for (int d = 0; d < sd; ++d) {
+      int o[3] = {0, 0, 0};
+      o[d] = 1;
+      divB = divB + AT(&Bn[d], i + o[0], j + o[1], k + o[2], 0) - AT(&Bn[d], i, j, k, 0);
+    }
+    for (int q = 0; q < np; ++q) w[q] = AT(&W, i, j, k, q);
+    if (p->use_8wave) {
+      /* SOURCE8WAVES (srcIdeal/PatchIdealMHDF.ChF:681-722) + ADDSOURCES */
+      double dB = -divB * dtbydx;
+      double Ux = w[1], Uy = w[2], Uz = w[3];
+      double Bx = D_1_4PI * w[5], By = D_1_4PI * w[6], Bz = D_1_4PI * w[7];
+      S[1] = dB * Bx;
+      S[2] = dB * By;
+      S[3] = dB * Bz;
+      S[4] = dB * (Bx * Ux + By * Uy + Bz * Uz);
+      S[5] = dB * Ux;
+      S[6] = dB * Uy;
+      S[7] = dB * Uz;
+      for (int q = 1; q <= 7; ++q) AT(U, i, j, k, q) = AT(U, i, j, k, q) + S[q];
+      if (divBout) AT(divBout, i, j, k, 0) = divB;
+    }
+    if (c->glm) AT(U, i, j, k, 8) = psicoef * AT(U, i, j, k, 8); /* PSIPARABOLIC */
+    if (p->charge_exchange && c->nf >= 2) {
+      /* HeliosphericProblem::explicitSource (swlism/HeliosphericProblem.cpp:1394-1539) */
+      int reg = region_cell(c, i, j, k, w);
+      charge_exchange_cell(c, w, reg, dt, S);
+      int iEND = c->irhon + (c->nf - 2) * 5 + 4;
+      for (int q = 1; q <= iEND; ++q) AT(U, i, j, k, q) = AT(U, i, j, k, q) + S[q];
+    }
+  }
+
+  /* problem postprocessing, then positivity (src/PatchMHDAM.cpp:705-707) */
+  FOR_BOX(valueBox, i, j, k) {
+    for (int q = 0; q < nc; ++q) u[q] = AT(U, i, j, k, q);
+    if (p->reinit_sphere) reinit_cell(c, i, j, k, u);
+    positivity_cell(c, u);
+    for (int q = 0; q < nc; ++q) AT(U, i, j, k, q) = u[q];
+  }
+
+  if (F) {
+    for (int d = 0; d < sd; ++d) {
+      mf_box fb = box_nodes(valueBox, d);
+      if (!box_contains(&F[d].b, &fb)) continue;
+      for (int q = 0; q < nc; ++q) FOR_BOX(fb, i, j, k) AT(&F[d], i, j, k, q) = AT(&Fl[d], i, j, k, q);
+    }
+  }
+
+  for (int d = 0; d < sd; ++d) {
+    fab_free(&Wm[d]);
+    fab_free(&Wp[d]);
+    fab_free(&Fl[d]);
+    fab_free(&Bn[d]);
+  }
+  fab_free(&W);
+  fab_free(&Uold);
+  return MF_OK;
+}
+
+/* ------------------------------------------------------------------------ */
+/* dt                                                                        */
+/* ------------------------------------------------------------------------ */
+
+/* MAXWAVESPEED (srcIdeal/PatchIdealMHDF.ChF:5-63) + MAXWAVESPEED_E
+   (srcIdeal/PatchEulerF.ChF:5-50) of one cell. */
+static double max_wave_speed_cell(const Ctx* c, const double* cons) {
+  const double gamma = c->gamma, hgamma = c->hgamma;
+  double cmax = 0.0;
+  {
+    double rho = cons[0];
+    double invrho = 1.0 / rho;
+    double ru = cons[1], rv = cons[2], rw = cons[3];
+    double u = ru * invrho, v = rv * invrho, w = rw * invrho;
+    double ke = ru * u + rv * v + rw * w;
+    double bx = cons[5], by = cons[6], bz = cons[7];
+    double b = D_1_4PI * (bx * bx + by * by + bz * bz);
+    double p = hgamma * (cons[4] - 0.5 * (ke + b));
+    p = fmax(p, c->smallp);
+    double a2 = gamma * p * invrho;
+    double as2 = 0.5 * (a2 + invrho * b);
+    double as4 = as2 * as2;
+    double bn2 = D_1_4PI * bx * bx * invrho;
+    double cf2 = as2 + sqrt(as4 - a2 * bn2);
+    double umax = fabs(u) + sqrt(cf2);
+    bn2 = D_1_4PI * by * by * invrho;
+    cf2 = as2 + sqrt(as4 - a2 * bn2);
+    umax = fmax(fabs(v) + sqrt(cf2), umax);
+    bn2 = D_1_4PI * bz * bz * invrho;
+    cf2 = as2 + sqrt(as4 - a2 * bn2);
+    umax = fmax(fabs(w) + sqrt(cf2), umax);
+    cmax = fmax(umax, cmax);
+  }
+  for (int f = 1; f < c->nf; ++f) {
+    int s = c->irhon + (f - 1) * 5;
+    double rho = cons[s];
+    rho = fmax(rho, c->smallr);
+    double invrho = 1.0 / rho;
+    double ru = cons[s + 1], rv = cons[s + 2], rw = cons[s + 3];
+    double u = ru * invrho, v = rv * invrho, w = rw * invrho;
+    double ke = ru * u + rv * v + rw * w;
+    double p = hgamma * (cons[s + 4] - 0.5 * ke);
+    p = fmax(p, c->smallp);
+    double a = sqrt(gamma * p * invrho);
+    double umax = fmax(fmax(fabs(u), fabs(v)), fabs(w)) + a;
+    cmax = fmax(umax, cmax);
+  }
+  return cmax;
+}
+
+/* PatchMHDMF::computeDt + PhysProblem::computeDt (src/PhysProblem.cpp:298-319):
+   dt = dx / cmax, first minimum in box order (FArrayBox::minIndex). */
+static void compute_dt_fab(const Ctx* c, const Fab* U, mf_box box, double* dt, int cell[3]) {
+  double u[MF_MAX_COMP];
+  int first = 1;
+  double best = 0.0;
+  FOR_BOX(box, i, j, k) {
+    for (int q = 0; q < c->nc; ++q) u[q] = AT(U, i, j, k, q);
+    double cm = max_wave_speed_cell(c, u);
+    double v = c->p->dx / cm;
+    if (first || v < best) {
+      best = v;
+      cell[0] = i;
+      cell[1] = j;
+      cell[2] = k;
+      first = 0;
+    }
+  }
+  *dt = best;
+}
+
+/* ------------------------------------------------------------------------ */
+/* updateState                                                               */
+/* ------------------------------------------------------------------------ */
+
+static int check_fab(const Ctx* c, const mf_fab* U, const mf_box* valid) {
+  if (!U || !U->data || !valid) return MF_ERR_BAD_ARG;
+  if (U->ncomp != c->nc) return MF_ERR_BAD_ARG;
+  mf_box need = box_grow(*valid, num_ghost(c->p), c->sd);
+  if (!box_contains(&U->box, &need)) return MF_ERR_BAD_ARG;
+  return MF_OK;
+}
+
+int mf_oracle_patch_update(const mf_params* p, double time, mf_fab* Uf, const mf_box* valid,
+                           double dt, mf_fab* Fout, mf_fab* divBf, double* new_dt,
+                           int min_cell[3]) {
+  Ctx c;
+  int st = ctx_init(&c, p);
+  if (st) return st;
+  st = check_fab(&c, Uf, valid);
+  if (st) return st;
+  Fab U = fab_wrap(Uf->data, Uf->box, Uf->ncomp);
+  Fab divB, *pdivB = NULL;
+  if (divBf && divBf->data) {
+    divB = fab_wrap(divBf->data, divBf->box, 1);
+    pdivB = &divB;
+  }
+  Fab F[3], *pF = NULL;
+  if (Fout) {
+    for (int d = 0; d < c.sd; ++d) F[d] = fab_wrap(Fout[d].data, Fout[d].box, Fout[d].ncomp);
+    pF = F;
+  }
+  long n = U.csz * c.nc;
+  if (p->time_approximation == MF_TA_RK2) {
+    /* src/PatchMHDAM.cpp:1239-1286 */
+    Fab Uold = fab_alloc(U.b, c.nc);
+    Fab Upred = fab_alloc(U.b, c.nc);
+    memcpy(Uold.p, U.p, sizeof(double) * (size_t)n);
+    memcpy(Upred.p, U.p, sizeof(double) * (size_t)n);
+    Fab Fp[3];
+    mf_box bp = box_grow(*valid, 2, c.sd);
+    mf_box vbp = box_and_domain(bp, p);
+    for (int d = 0; d < c.sd; ++d) Fp[d] = fab_alloc(box_nodes(vbp, d), c.nc);
+    euler_step(&c, time, &Upred, pF ? Fp : NULL, pdivB, dt, bp);
+    memcpy(U.p, Upred.p, sizeof(double) * (size_t)n);
+    euler_step(&c, time, &U, pF, pdivB, 0.5 * dt, *valid);
+    if (pF) {
+      mf_box vb = box_and_domain(*valid, p);
+      for (int d = 0; d < c.sd; ++d) {
+        mf_box fb = box_nodes(vb, d);
+        for (int q = 0; q < c.nc; ++q) FOR_BOX(fb, i, j, k) {
+            AT(&F[d], i, j, k, q) = AT(&F[d], i, j, k, q) + AT(&Fp[d], i, j, k, q);
+            AT(&F[d], i, j, k, q) = AT(&F[d], i, j, k, q) * 0.5;
+          }
+      }
+    }
+    /* AVERAGESTATE (src/PatchMHDAMF.ChF:289-316) */
+    for (int q = 0; q < c.nc; ++q) FOR_BOX((*valid), i, j, k) {
+        AT(&U, i, j, k, q) =
+            AT(&U, i, j, k, q) + 0.5 * (AT(&Uold, i, j, k, q) - AT(&Upred, i, j, k, q));
+      }
+    for (int d = 0; d < c.sd; ++d) fab_free(&Fp[d]);
+    fab_free(&Uold);
+    fab_free(&Upred);
+  } else {
+    euler_step(&c, time, &U, pF, pdivB, dt, *valid);
+  }
+  double ndt;
+  int cell[3] = {0, 0, 0};
+  compute_dt_fab(&c, &U, *valid, &ndt, cell);
+  if (new_dt) *new_dt = ndt;
+  if (min_cell) {
+    min_cell[0] = cell[0];
+    min_cell[1] = cell[1];
+    min_cell[2] = cell[2];
+  }
+  return MF_OK;
+}
+
+int mf_oracle_compute_dt(const mf_params* p, const mf_fab* Uf, const mf_box* box, double* dt,
+                         int min_cell[3]) {
+  Ctx c;
+  int st = ctx_init(&c, p);
+  if (st) return st;
+  if (!Uf || !box || !box_contains(&Uf->box, box)) return MF_ERR_BAD_ARG;
+  Fab U = fab_wrap(Uf->data, Uf->box, Uf->ncomp);
+  int cell[3] = {0, 0, 0};
+  compute_dt_fab(&c, &U, *box, dt, cell);
+  if (min_cell) memcpy(min_cell, cell, sizeof(cell));
+  return MF_OK;
+}
+
+/* ------------------------------------------------------------------------ */
+/* level                                                                     */
+/* ------------------------------------------------------------------------ */
+
+int mf_oracle_level_exchange(const mf_params* p, int npatch, mf_fab* Uf, const mf_box* valid) {
+  int sd = p->space_dim;
+  int L[3] = {0, 0, 0};
+  for (int d = 0; d < sd; ++d) L[d] = p->domain_hi[d] - p->domain_lo[d] + 1;
+  int rng[3][2];
+  for (int d = 0; d < 3; ++d) {
+    int r = (d < sd && p->periodic[d]) ? 1 : 0;
+    rng[d][0] = -r;
+    rng[d][1] = r;
+  }
+  for (int dp = 0; dp < npatch; ++dp) {
+    Fab D = fab_wrap(Uf[dp].data, Uf[dp].box, Uf[dp].ncomp);
+    for (int sp_ = 0; sp_ < npatch; ++sp_) {
+      Fab S = fab_wrap(Uf[sp_].data, Uf[sp_].box, Uf[sp_].ncomp);
+      for (int a = rng[0][0]; a <= rng[0][1]; ++a)
+        for (int b = rng[1][0]; b <= rng[1][1]; ++b)
+          for (int e = rng[2][0]; e <= rng[2][1]; ++e) {
+            if (sp_ == dp && a == 0 && b == 0 && e == 0) continue;
+            int sh[3] = {a * L[0], b * L[1], e * L[2]};
+            mf_box r;
+            int empty = 0;
+            for (int d = 0; d < 3; ++d) {
+              r.lo[d] = valid[sp_].lo[d] + sh[d];
+              r.hi[d] = valid[sp_].hi[d] + sh[d];
+              if (r.lo[d] < D.b.lo[d]) r.lo[d] = D.b.lo[d];
+              if (r.hi[d] > D.b.hi[d]) r.hi[d] = D.b.hi[d];
+              if (r.lo[d] > r.hi[d]) empty = 1;
+            }
+            if (empty) continue;
+            for (int q = 0; q < D.nc; ++q) FOR_BOX(r, i, j, k) {
+                if (box_in(&valid[dp], i, j, k)) continue;
+                AT(&D, i, j, k, q) = AT(&S, i - sh[0], j - sh[1], k - sh[2], q);
+              }
+          }
+    }
+  }
+  return MF_OK;
+}
+
+int mf_oracle_level_step(const mf_params* p, double time, int npatch, mf_fab* Uf,
+                         const mf_box* valid, double dt, int nthreads, double* new_dt,
+                         int* min_patch, int min_cell[3]) {
+  int st = mf_oracle_level_exchange(p, npatch, Uf, valid);
+  if (st) return st;
+  double* dts = (double*)malloc(sizeof(double) * (size_t)npatch);
+  int* cells = (int*)malloc(sizeof(int) * 3 * (size_t)npatch);
+  int* sts = (int*)malloc(sizeof(int) * (size_t)npatch);
+#ifdef _OPENMP
+  if (nthreads <= 0) nthreads = omp_get_max_threads();
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nthreads)
+#else
+  (void)nthreads;
+#endif
+  for (int ip = 0; ip < npatch; ++ip)
+    sts[ip] = mf_oracle_patch_update(p, time, &Uf[ip], &valid[ip], dt, NULL, NULL, &dts[ip],
+                                     &cells[3 * ip]);
+  int best = -1;
+  for (int ip = 0; ip < npatch; ++ip) {
+    if (sts[ip]) st = sts[ip];
+    if (best < 0 || dts[ip] < dts[best]) best = ip;
+  }
+  if (best >= 0) {
+    if (new_dt) *new_dt = dts[best];
+    if (min_patch) *min_patch = best;
+    if (min_cell) memcpy(min_cell, &cells[3 * best], sizeof(int) * 3);
+  }
+  free(dts);
+  free(cells);
+  free(sts);
+  return st;
+}
+
+/* ------------------------------------------------------------------------ */
+/* single-point entry points for known-answer tests                          */
+/* ------------------------------------------------------------------------ */
+
+int mf_oracle_face_flux(const mf_params* p, int dir, const double* wl, const double* wr,
+                        double* f) {
+  Ctx c;
+  int st = ctx_init(&c, p);
+  if (st) return st;
+  face_flux(&c, dir, wl, wr, f);
+  return MF_OK;
+}
+
+int mf_oracle_cons_to_prim(const mf_params* p, const double* u, double* w) {
+  Ctx c;
+  int st = ctx_init(&c, p);
+  if (st) return st;
+  cons_to_prim_cell(&c, u, w);
+  return MF_OK;
+}
+
+int mf_oracle_charge_exchange(const mf_params* p, const double* w, int reg, double dt,
+                              double* s) {
+  Ctx c;
+  int st = ctx_init(&c, p);
+  if (st) return st;
+  if (c.nf < 2) return MF_ERR_BAD_ARG;
+  charge_exchange_cell(&c, w, reg, dt, s);
+  return MF_OK;
+}
+
+int mf_oracle_region(const mf_params* p, int i, int j, int k, const double* w) {
+  Ctx c;
+  if (ctx_init(&c, p)) return -1;
+  return region_cell(&c, i, j, k, w);
+}
+
+/* ORSZAGINIT (problems/OrszagF.ChF:27-79). */
+int mf_oracle_init_orszag(const mf_params* p, mf_fab* Uf, const mf_box* box) {
+  Ctx c;
+  int st = ctx_init(&c, p);
+  if (st) return st;
+  Fab U = fab_wrap(Uf->data, Uf->box, Uf->ncomp);
+  double gamma = p->gamma, hgamma = gamma - 1.0, dx = p->dx;
+  double p0 = D_1_4PI * gamma;
+  double r0 = p0 * gamma;
+  FOR_BOX((*box), i, j, k) {
+    double x = (i + 0.5) * dx;
+    double y = (j + 0.5) * dx;
+    double Ux = -sin(D_2PI * y);
+    double Uy = sin(D_2PI * x);
+    double Bx = -sin(D_2PI * y);
+    double By = sin((D_2PI + D_2PI) * x);
+    double b = D_1_4PI * (Bx * Bx + By * By);
+    double ke = Ux * Ux + Uy * Uy;
+    double e0 = p0 / hgamma + 0.5 * (r0 * ke + b);
+    AT(&U, i, j, k, 0) = r0;
+    AT(&U, i, j, k, 1) = r0 * Ux;
+    AT(&U, i, j, k, 2) = r0 * Uy;
+    AT(&U, i, j, k, 3) = 0.0;
+    AT(&U, i, j, k, 4) = e0;
+    AT(&U, i, j, k, 5) = Bx;
+    AT(&U, i, j, k, 6) = By;
+    AT(&U, i, j, k, 7) = 0.0;
+    if (c.glm) AT(&U, i, j, k, 8) = 0.0;
+  }
+  return MF_OK;
+}
+
+int mf_oracle_max_threads(void) {
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
+}

@@ -1,0 +1,193 @@
+"""ctypes binding of the CPU restatement (oracle/libmforacle.so).
+
+TEST INFRASTRUCTURE ONLY: used by tests/, __graft_entry__.smoke() and the
+CPU-baseline leg of bench.py as the checker; the product never imports it.
+Parity status: unpinned by reference outputs (see mf_oracle.c).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "libmforacle.so")
+_PKG = os.path.join(os.path.dirname(HERE), "ms-flukss-multifluid_gb300")
+if _PKG not in sys.path:
+    sys.path.insert(0, _PKG)
+import mfgpu  # noqa: E402  (struct layouts of include/mf_patch.h only)
+from mfgpu import MfBox, MfFab, MfParams, make_box  # noqa: E402
+
+_lib = None
+_P = ctypes.POINTER
+_DP = ctypes.POINTER(ctypes.c_double)
+
+
+def build(force: bool = False) -> str:
+    srcs = [os.path.join(HERE, f) for f in ("mf_oracle.c", "mf_oracle.h", "Makefile")]
+    hdr = os.path.join(os.path.dirname(HERE), "include", "mf_patch.h")
+    if (not force and os.path.exists(LIB)
+            and all(os.path.getmtime(s) <= os.path.getmtime(LIB) for s in srcs + [hdr])):
+        return LIB
+    r = subprocess.run(["make", "-B" if force else "-s", "-C", HERE], capture_output=True,
+                       text=True)
+    if r.returncode != 0 or not os.path.exists(LIB):
+        raise RuntimeError(f"oracle build failed:\n{r.stdout}\n{r.stderr}")
+    return LIB
+
+
+def load():
+    global _lib
+    if _lib is not None:
+        return _lib
+    build()
+    lib = ctypes.CDLL(LIB)
+    sig = {
+        "mf_oracle_patch_update": (ctypes.c_int, [_P(MfParams), ctypes.c_double, _P(MfFab),
+                                                  _P(MfBox), ctypes.c_double, ctypes.c_void_p,
+                                                  ctypes.c_void_p, _DP, ctypes.c_int * 3]),
+        "mf_oracle_compute_dt": (ctypes.c_int, [_P(MfParams), _P(MfFab), _P(MfBox), _DP,
+                                                ctypes.c_int * 3]),
+        "mf_oracle_level_exchange": (ctypes.c_int, [_P(MfParams), ctypes.c_int, _P(MfFab),
+                                                    _P(MfBox)]),
+        "mf_oracle_level_step": (ctypes.c_int, [_P(MfParams), ctypes.c_double, ctypes.c_int,
+                                                _P(MfFab), _P(MfBox), ctypes.c_double,
+                                                ctypes.c_int, _DP, _P(ctypes.c_int),
+                                                ctypes.c_int * 3]),
+        "mf_oracle_face_flux": (ctypes.c_int, [_P(MfParams), ctypes.c_int, _DP, _DP, _DP]),
+        "mf_oracle_cons_to_prim": (ctypes.c_int, [_P(MfParams), _DP, _DP]),
+        "mf_oracle_charge_exchange": (ctypes.c_int, [_P(MfParams), _DP, ctypes.c_int,
+                                                     ctypes.c_double, _DP]),
+        "mf_oracle_region": (ctypes.c_int, [_P(MfParams), ctypes.c_int, ctypes.c_int,
+                                            ctypes.c_int, _DP]),
+        "mf_oracle_init_orszag": (ctypes.c_int, [_P(MfParams), _P(MfFab), _P(MfBox)]),
+        "mf_oracle_max_threads": (ctypes.c_int, []),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def _dp(a: np.ndarray):
+    return a.ctypes.data_as(_DP)
+
+
+def patch_update(p: MfParams, U: np.ndarray, fab_lo, fab_hi, valid_lo, valid_hi, dt,
+                 F=None, divB=None, time=0.0):
+    """updateState on a host fab (modified in place). F: list of
+    (array, lo, hi) per direction; divB: (array, lo, hi)."""
+    lib = load()
+    assert U.dtype == np.float64 and U.flags.c_contiguous
+    nc = U.shape[0]
+    fab = MfFab(U.ctypes.data, make_box(fab_lo, fab_hi), nc)
+    valid = make_box(valid_lo, valid_hi)
+    fptr = None
+    keep = []
+    if F is not None:
+        arr = (MfFab * 3)()
+        for d, (a, lo, hi) in enumerate(F):
+            arr[d] = MfFab(a.ctypes.data, make_box(lo, hi), nc)
+        keep.append(arr)
+        fptr = ctypes.cast(arr, ctypes.c_void_p)
+    dptr = None
+    if divB is not None:
+        a, lo, hi = divB
+        dfab = MfFab(a.ctypes.data, make_box(lo, hi), 1)
+        keep.append(dfab)
+        dptr = ctypes.cast(ctypes.pointer(dfab), ctypes.c_void_p)
+    ndt = ctypes.c_double()
+    cell = (ctypes.c_int * 3)()
+    st = lib.mf_oracle_patch_update(ctypes.byref(p), time, ctypes.byref(fab),
+                                    ctypes.byref(valid), dt, fptr, dptr, ctypes.byref(ndt), cell)
+    return st, ndt.value, tuple(cell)
+
+
+def compute_dt(p: MfParams, U: np.ndarray, fab_lo, fab_hi, lo, hi):
+    lib = load()
+    fab = MfFab(U.ctypes.data, make_box(fab_lo, fab_hi), U.shape[0])
+    box = make_box(lo, hi)
+    dt = ctypes.c_double()
+    cell = (ctypes.c_int * 3)()
+    st = lib.mf_oracle_compute_dt(ctypes.byref(p), ctypes.byref(fab), ctypes.byref(box),
+                                  ctypes.byref(dt), cell)
+    return st, dt.value, tuple(cell)
+
+
+def _fab_array(arrays, fab_boxes):
+    n = len(arrays)
+    fabs = (MfFab * n)()
+    for i, (a, (lo, hi)) in enumerate(zip(arrays, fab_boxes)):
+        fabs[i] = MfFab(a.ctypes.data, make_box(lo, hi), a.shape[0])
+    return fabs
+
+
+def level_exchange(p: MfParams, arrays, fab_boxes, valid_boxes):
+    lib = load()
+    fabs = _fab_array(arrays, fab_boxes)
+    vb = (MfBox * len(valid_boxes))(*[make_box(lo, hi) for lo, hi in valid_boxes])
+    return lib.mf_oracle_level_exchange(ctypes.byref(p), len(arrays), fabs, vb)
+
+
+def level_step(p: MfParams, arrays, fab_boxes, valid_boxes, dt, nthreads=0, time=0.0):
+    """exchange + updateState on every patch (arrays modified in place)."""
+    lib = load()
+    fabs = _fab_array(arrays, fab_boxes)
+    vb = (MfBox * len(valid_boxes))(*[make_box(lo, hi) for lo, hi in valid_boxes])
+    ndt = ctypes.c_double()
+    ip = ctypes.c_int()
+    cell = (ctypes.c_int * 3)()
+    st = lib.mf_oracle_level_step(ctypes.byref(p), time, len(arrays), fabs, vb, dt, nthreads,
+                                  ctypes.byref(ndt), ctypes.byref(ip), cell)
+    return st, ndt.value, ip.value, tuple(cell)
+
+
+def face_flux(p: MfParams, direction: int, wl, wr):
+    lib = load()
+    nc = mfgpu.num_cons(p)
+    wl = np.ascontiguousarray(wl, dtype=np.float64)
+    wr = np.ascontiguousarray(wr, dtype=np.float64)
+    f = np.full(nc, np.nan)
+    st = lib.mf_oracle_face_flux(ctypes.byref(p), direction, _dp(wl), _dp(wr), _dp(f))
+    assert st == 0, st
+    return f
+
+
+def cons_to_prim(p: MfParams, u):
+    lib = load()
+    u = np.ascontiguousarray(u, dtype=np.float64)
+    w = np.full(mfgpu.num_cons(p), np.nan)
+    st = lib.mf_oracle_cons_to_prim(ctypes.byref(p), _dp(u), _dp(w))
+    assert st == 0, st
+    return w
+
+
+def charge_exchange(p: MfParams, w, reg, dt):
+    lib = load()
+    w = np.ascontiguousarray(w, dtype=np.float64)
+    s = np.full(mfgpu.num_cons(p), np.nan)
+    st = lib.mf_oracle_charge_exchange(ctypes.byref(p), _dp(w), reg, dt, _dp(s))
+    assert st == 0, st
+    return s
+
+
+def region(p: MfParams, i, j, k, w):
+    lib = load()
+    w = np.ascontiguousarray(w, dtype=np.float64)
+    return lib.mf_oracle_region(ctypes.byref(p), i, j, k, _dp(w))
+
+
+def init_orszag(p: MfParams, U: np.ndarray, fab_lo, fab_hi, lo, hi):
+    lib = load()
+    fab = MfFab(U.ctypes.data, make_box(fab_lo, fab_hi), U.shape[0])
+    box = make_box(lo, hi)
+    return lib.mf_oracle_init_orszag(ctypes.byref(p), ctypes.byref(fab), ctypes.byref(box))
+
+
+def max_threads() -> int:
+    return load().mf_oracle_max_threads()

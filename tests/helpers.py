@@ -1,0 +1,57 @@
+"""Shared helpers of the tests: fab construction, periodic ghost fill on the
+host, device round trips through torch, and the parity comparison."""
+from __future__ import annotations
+
+import numpy as np
+
+import mfgpu
+
+
+def periodic_fill(U: np.ndarray, ng: int, sd: int) -> np.ndarray:
+    """Fill the ghost cells of a single-patch fab that covers a periodic
+    domain exactly (valid = fab shrunk by ng)."""
+    if sd == 2:
+        v = U[:, :, ng:-ng, ng:-ng]
+        U[:] = np.pad(v, ((0, 0), (0, 0), (ng, ng), (ng, ng)), mode="wrap")
+    else:
+        v = U[:, ng:-ng, ng:-ng, ng:-ng]
+        U[:] = np.pad(v, ((0, 0), (ng, ng), (ng, ng), (ng, ng)), mode="wrap")
+    return U
+
+
+def valid_view(U: np.ndarray, ng: int, sd: int) -> np.ndarray:
+    if sd == 2:
+        return U[:, :, ng:-ng, ng:-ng]
+    return U[:, ng:-ng, ng:-ng, ng:-ng]
+
+
+def rel_err(a: np.ndarray, b: np.ndarray, floor_frac: float = 1e-3) -> np.ndarray:
+    """Per-component maximum of |a-b| / max(|b|, floor_frac * max|b_c|):
+    pointwise relative error, with components that pass through zero measured
+    against their own scale."""
+    out = []
+    for c in range(b.shape[0]):
+        bc = b[c]
+        sc = float(np.max(np.abs(bc))) if bc.size else 0.0
+        den = np.maximum(np.abs(bc), floor_frac * sc)
+        den = np.where(den == 0.0, 1.0, den)
+        out.append(float(np.max(np.abs(a[c] - bc) / den)) if bc.size else 0.0)
+    return np.array(out)
+
+
+def to_device(arr: np.ndarray):
+    import torch
+    return torch.from_numpy(np.ascontiguousarray(arr)).to("cuda")
+
+
+def to_host(t) -> np.ndarray:
+    import torch
+    torch.cuda.synchronize()
+    return t.cpu().numpy()
+
+
+def orszag_patch(n: int, ng: int, p) -> np.ndarray:
+    """Single periodic patch [0,n-1]^2 + ghosts holding the Orszag-Tang state."""
+    lo, hi = mfgpu.grow([0, 0, 0], [n - 1, n - 1, 0], ng, 2)
+    U = mfgpu.init_host_fab(p, lo, hi, "orszag")
+    return periodic_fill(U, ng, 2)

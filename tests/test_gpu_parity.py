@@ -1,0 +1,313 @@
+"""GPU parity: the CUDA path through the C ABI against the CPU restatement on
+identical inputs.
+
+Tolerance (FP64 path): 1e-12 relative per step in every conserved variable
+(rel_err: pointwise relative error, components that pass through zero measured
+against 1e-3 of their largest magnitude).  The new dt: 1e-12 relative.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+import mfgpu
+from helpers import orszag_patch, periodic_fill, rel_err, to_device, to_host, valid_view
+
+RTOL = 1e-12
+
+pytestmark = pytest.mark.gpu
+
+
+def _gpu_patch_step(ctx, U, lo, hi, vlo, vhi, dt, F=None, divB=None):
+    t = to_device(U)
+    tF = None
+    if F is not None:
+        tF = [(to_device(a), flo, fhi) for a, flo, fhi in F]
+        Fspec = [(x.data_ptr(), flo, fhi) for x, flo, fhi in tF]
+    tD = None
+    if divB is not None:
+        a, dlo, dhi = divB
+        tD = to_device(a)
+    st, ndt, cell = ctx.patch_update(t.data_ptr(), lo, hi, vlo, vhi, dt,
+                                     F=Fspec if F is not None else None,
+                                     divB=(tD.data_ptr(), divB[1], divB[2]) if divB is not None
+                                     else None)
+    out = to_host(t)
+    Fo = [to_host(x) for x, _, _ in tF] if tF is not None else None
+    Do = to_host(tD) if tD is not None else None
+    return out, ndt, cell, Fo, Do
+
+
+def _orszag_case(n, ta, prec=mfgpu.PREC_FP64, **kw):
+    p = mfgpu.orszag_params(n, ta, prec)
+    for k, v in kw.items():
+        if k == "limiter":
+            for q in range(8):
+                p.limiter[q] = v
+        else:
+            setattr(p, k, v)
+    return p
+
+
+@pytest.mark.parametrize("ta", [mfgpu.TA_RK2, mfgpu.TA_FIRST_ORDER])
+def test_orszag_single_patch_steps(gpulib, oracle, ta):
+    n = 64
+    p = _orszag_case(n, ta)
+    ctx = mfgpu.Context(p)
+    ng = ctx.ng
+    U = orszag_patch(n, ng, p)
+    lo, hi = mfgpu.grow([0, 0, 0], [n - 1, n - 1, 0], ng, 2)
+    vlo, vhi = [0, 0, 0], [n - 1, n - 1, 0]
+    st, dt0, _ = oracle.compute_dt(p, U, lo, hi, vlo, vhi)
+    assert st == 0
+    dt = 0.4 * dt0
+    for step in range(4):
+        Uo = U.copy()
+        st, ndt_o, cell_o = oracle.patch_update(p, Uo, lo, hi, vlo, vhi, dt)
+        assert st == 0
+        Ug, ndt_g, cell_g, _, _ = _gpu_patch_step(ctx, U, lo, hi, vlo, vhi, dt)
+        e = rel_err(valid_view(Ug, ng, 2), valid_view(Uo, ng, 2))
+        assert np.all(e <= RTOL), (step, e)
+        assert abs(ndt_g - ndt_o) <= RTOL * ndt_o
+        assert cell_g == cell_o
+        # next step from the oracle's state, ghosts refilled
+        U = periodic_fill(Uo.copy(), ng, 2)
+        dt = 0.4 * ndt_o
+    ctx.close()
+
+
+@pytest.mark.parametrize("lim", [mfgpu.LIM_CD, mfgpu.LIM_SUPERBEE, mfgpu.LIM_VANALBADA,
+                                 mfgpu.LIM_MC, mfgpu.LIM_HARMONIC, mfgpu.LIM_VANLEER])
+def test_limiters(gpulib, oracle, lim):
+    n = 32
+    p = _orszag_case(n, mfgpu.TA_RK2, limiter=lim)
+    ctx = mfgpu.Context(p)
+    ng = ctx.ng
+    U = orszag_patch(n, ng, p)
+    lo, hi = mfgpu.grow([0, 0, 0], [n - 1, n - 1, 0], ng, 2)
+    vlo, vhi = [0, 0, 0], [n - 1, n - 1, 0]
+    dt = 0.4 * oracle.compute_dt(p, U, lo, hi, vlo, vhi)[1]
+    Uo = U.copy()
+    assert oracle.patch_update(p, Uo, lo, hi, vlo, vhi, dt)[0] == 0
+    Ug = _gpu_patch_step(ctx, U, lo, hi, vlo, vhi, dt)[0]
+    e = rel_err(valid_view(Ug, ng, 2), valid_view(Uo, ng, 2))
+    assert np.all(e <= RTOL), e
+
+
+@pytest.mark.parametrize("flux,chk", [(3, 0), (2, 0), (4, 0), (11, 0), (13, 0), (1, 1)])
+def test_solvers(gpulib, oracle, flux, chk):
+    n = 32
+    p = _orszag_case(n, mfgpu.TA_RK2, flux=flux, check_positivity=chk)
+    ctx = mfgpu.Context(p)
+    ng = ctx.ng
+    U = orszag_patch(n, ng, p)
+    lo, hi = mfgpu.grow([0, 0, 0], [n - 1, n - 1, 0], ng, 2)
+    vlo, vhi = [0, 0, 0], [n - 1, n - 1, 0]
+    dt = 0.4 * oracle.compute_dt(p, U, lo, hi, vlo, vhi)[1]
+    Uo = U.copy()
+    assert oracle.patch_update(p, Uo, lo, hi, vlo, vhi, dt)[0] == 0
+    Ug = _gpu_patch_step(ctx, U, lo, hi, vlo, vhi, dt)[0]
+    e = rel_err(valid_view(Ug, ng, 2), valid_view(Uo, ng, 2))
+    assert np.all(e <= RTOL), e
+
+
+def test_flux_and_divb_outputs(gpulib, oracle):
+    n = 32
+    p = _orszag_case(n, mfgpu.TA_RK2)
+    ctx = mfgpu.Context(p)
+    ng, nc = ctx.ng, ctx.nc
+    U = orszag_patch(n, ng, p)
+    lo, hi = mfgpu.grow([0, 0, 0], [n - 1, n - 1, 0], ng, 2)
+    vlo, vhi = [0, 0, 0], [n - 1, n - 1, 0]
+    dt = 0.4 * oracle.compute_dt(p, U, lo, hi, vlo, vhi)[1]
+    F, Fg = [], []
+    for d in range(2):
+        fhi = list(vhi)
+        fhi[d] += 1
+        F.append((np.zeros(mfgpu.fab_shape(vlo, fhi, nc)), vlo, fhi))
+        Fg.append((np.zeros(mfgpu.fab_shape(vlo, fhi, nc)), vlo, fhi))
+    D = (np.zeros(mfgpu.fab_shape(vlo, vhi, 1)), vlo, vhi)
+    Uo = U.copy()
+    assert oracle.patch_update(p, Uo, lo, hi, vlo, vhi, dt, F=F, divB=D)[0] == 0
+    Ug, _, _, Fo, Do = _gpu_patch_step(ctx, U, lo, hi, vlo, vhi, dt, F=Fg,
+                                       divB=(np.zeros(mfgpu.fab_shape(vlo, vhi, 1)), vlo, vhi))
+    for d in range(2):
+        e = rel_err(Fo[d], F[d][0])
+        assert np.all(e <= 1e-11), (d, e)
+    scale = np.max(np.abs(D[0]))
+    assert np.max(np.abs(Do - D[0])) <= 1e-11 * max(scale, 1e-300)
+
+
+def _helio_single(n):
+    p = mfgpu.helio_params(n)
+    ctx = mfgpu.Context(p)
+    ng = ctx.ng
+    lo, hi = mfgpu.grow([0, 0, 0], [n - 1] * 3, ng, 3)
+    U = mfgpu.init_host_fab(p, lo, hi, "helio")
+    return p, ctx, U, lo, hi
+
+
+def test_helio_single_patch_steps(gpulib, oracle):
+    n = 24
+    p, ctx, U, lo, hi = _helio_single(n)
+    ng = ctx.ng
+    vlo, vhi = [0, 0, 0], [n - 1] * 3
+    dt0 = oracle.compute_dt(p, U, lo, hi, vlo, vhi)[1]
+    ch = p.factor_ch * p.dx / dt0
+    cp = np.sqrt(ch * p.dx / p.factor_cp)
+    p.dedner_ch, p.dedner_cp = ch, cp
+    ctx.set_dedner(ch, cp)
+    dt = 0.4 * dt0
+    for step in range(3):
+        Uo = U.copy()
+        st, ndt_o, cell_o = oracle.patch_update(p, Uo, lo, hi, vlo, vhi, dt)
+        assert st == 0
+        Ug, ndt_g, cell_g, _, _ = _gpu_patch_step(ctx, U, lo, hi, vlo, vhi, dt)
+        e = rel_err(valid_view(Ug, ng, 3), valid_view(Uo, ng, 3))
+        assert np.all(e <= RTOL), (step, e)
+        assert abs(ndt_g - ndt_o) <= RTOL * ndt_o
+        assert cell_g == cell_o
+        U = Uo
+        dt = 0.4 * ndt_o
+    ctx.close()
+
+
+def test_helio_level_vs_oracle(gpulib, oracle):
+    n, patch = 32, 16
+    p = mfgpu.helio_params(n)
+    ctx = mfgpu.Context(p)
+    ng, nc = ctx.ng, ctx.nc
+    boxes = mfgpu.tile_boxes(n, patch, 3)
+    lev = mfgpu.Level(ctx, boxes)
+    flat = np.zeros(lev.ndoubles)
+    arrays, fboxes = [], []
+    for i, (blo, bhi) in enumerate(boxes):
+        flo, fhi = lev.fab_box(i)
+        a = mfgpu.init_host_fab(p, flo, fhi, "helio")
+        lev.patch_view(flat, i)[:] = a
+        arrays.append(a)
+        fboxes.append((flo, fhi))
+    lev.upload(flat.ctypes.data)
+    dt0, _, _ = lev.compute_dt()
+    odt = min(oracle.compute_dt(p, a, fb[0], fb[1], b[0], b[1])[1]
+              for a, fb, b in zip(arrays, fboxes, boxes))
+    assert abs(dt0 - odt) <= RTOL * odt
+    ch = p.factor_ch * p.dx / dt0
+    cp = float(np.sqrt(ch * p.dx / p.factor_cp))
+    p.dedner_ch, p.dedner_cp = ch, cp
+    ctx.set_dedner(ch, cp)
+    dt = 0.4 * dt0
+    for step in range(2):
+        st, ndt_o, ip_o, cell_o = oracle.level_step(p, arrays, fboxes, boxes, dt)
+        assert st == 0
+        st, ndt_g, ip_g, cell_g = lev.step(dt)
+        out = np.zeros(lev.ndoubles)
+        lev.download(out.ctypes.data)
+        for i in range(len(boxes)):
+            g = valid_view(lev.patch_view(out, i), ng, 3)
+            o = valid_view(arrays[i], ng, 3)
+            e = rel_err(g, o)
+            assert np.all(e <= RTOL), (step, i, e)
+        assert abs(ndt_g - ndt_o) <= RTOL * ndt_o
+        assert (ip_g, cell_g) == (ip_o, cell_o)
+        # continue both from the oracle's state
+        for i in range(len(boxes)):
+            lev.patch_view(flat, i)[:] = arrays[i]
+        lev.upload(flat.ctypes.data)
+        dt = 0.4 * ndt_o
+    lev.close()
+    ctx.close()
+
+
+def test_orszag_level_equals_patch(gpulib, oracle):
+    """Batched level (device exchange between the RK2 stages) gives the same
+    numbers as the single-patch path (redundant stage-1 ghosts) and as the
+    oracle."""
+    n, patch = 64, 16
+    p = mfgpu.orszag_params(n)
+    ctx = mfgpu.Context(p)
+    ng = ctx.ng
+    boxes = mfgpu.tile_boxes(n, patch, 2)
+    lev = mfgpu.Level(ctx, boxes)
+    flat = np.zeros(lev.ndoubles)
+    for i in range(len(boxes)):
+        flo, fhi = lev.fab_box(i)
+        lev.patch_view(flat, i)[:] = mfgpu.init_host_fab(p, flo, fhi, "orszag")
+    lev.upload(flat.ctypes.data)
+    dt = 0.4 * lev.compute_dt()[0]
+    st, ndt, ip, cell = lev.step(dt)
+    out = np.zeros(lev.ndoubles)
+    lev.download(out.ctypes.data)
+    # single patch covering the whole domain
+    U = orszag_patch(n, ng, p)
+    lo, hi = mfgpu.grow([0, 0, 0], [n - 1, n - 1, 0], ng, 2)
+    Ug, ndt1, cell1, _, _ = _gpu_patch_step(ctx, U, lo, hi, [0, 0, 0], [n - 1, n - 1, 0], dt)
+    whole = valid_view(Ug, ng, 2)
+    for i, (blo, bhi) in enumerate(boxes):
+        g = valid_view(lev.patch_view(out, i), ng, 2)
+        ref = whole[:, :, blo[1]:bhi[1] + 1, blo[0]:bhi[0] + 1]
+        assert np.array_equal(g, ref), i
+    assert ndt == ndt1
+    lev.close()
+    ctx.close()
+
+
+def test_mixed_precision_error(gpulib, oracle):
+    n = 64
+    res = {}
+    for prec in (mfgpu.PREC_FP64, mfgpu.PREC_MIXED):
+        p = mfgpu.orszag_params(n, mfgpu.TA_RK2, prec)
+        ctx = mfgpu.Context(p)
+        ng = ctx.ng
+        U = orszag_patch(n, ng, p)
+        lo, hi = mfgpu.grow([0, 0, 0], [n - 1, n - 1, 0], ng, 2)
+        dt = 0.4 * oracle.compute_dt(p, U, lo, hi, [0, 0, 0], [n - 1, n - 1, 0])[1]
+        for _ in range(10):
+            U, ndt, _, _, _ = _gpu_patch_step(ctx, U, lo, hi, [0, 0, 0], [n - 1, n - 1, 0], dt)
+            U = periodic_fill(U, ng, 2)
+            dt = 0.4 * ndt
+        res[prec] = valid_view(U, ng, 2)
+        ctx.close()
+    a, b = res[mfgpu.PREC_MIXED], res[mfgpu.PREC_FP64]
+    l1 = np.sum(np.abs(a[0] - b[0])) / np.sum(np.abs(b[0]))
+    assert l1 <= 1e-5, l1
+    assert l1 > 0.0
+
+
+def test_bad_arguments(gpulib):
+    p = mfgpu.orszag_params(16)
+    ctx = mfgpu.Context(p)
+    ng = ctx.ng
+    U = orszag_patch(16, ng, p)
+    t = to_device(U)
+    lo, hi = mfgpu.grow([0, 0, 0], [15, 15, 0], ng, 2)
+    # fab too small for the ghost width
+    st, _, _ = ctx.patch_update(t.data_ptr(), [lo[0] + 1, lo[1], 0], hi, [0, 0, 0], [15, 15, 0],
+                                1e-3, allow_error=True)
+    assert st == mfgpu.MF_ERR_BAD_ARG
+    st, _, _ = ctx.patch_update(t.data_ptr(), lo, hi, [0, 0, 0], [15, 15, 0], -1.0,
+                                allow_error=True)
+    assert st == mfgpu.MF_ERR_BAD_ARG
+    q = mfgpu.orszag_params(16)
+    q.flux = 5
+    with pytest.raises(mfgpu.MfError) as ei:
+        mfgpu.Context(q)
+    assert ei.value.code == mfgpu.MF_ERR_UNSUPPORTED
+
+
+def test_nonfinite_input_reported(gpulib):
+    p = mfgpu.orszag_params(16)
+    ctx = mfgpu.Context(p)
+    ng = ctx.ng
+    U = orszag_patch(16, ng, p)
+    U[4, 0, ng + 3, ng + 5] = np.nan
+    t = to_device(U)
+    lo, hi = mfgpu.grow([0, 0, 0], [15, 15, 0], ng, 2)
+    st, _, _ = ctx.patch_update(t.data_ptr(), lo, hi, [0, 0, 0], [15, 15, 0], 1e-4,
+                                allow_error=True)
+    assert st == mfgpu.MF_ERR_NONFINITE
+    # the context stays usable
+    U = orszag_patch(16, ng, p)
+    t = to_device(U)
+    st, ndt, _ = ctx.patch_update(t.data_ptr(), lo, hi, [0, 0, 0], [15, 15, 0], 1e-4)
+    assert st == 0 and ndt > 0
