@@ -29,11 +29,27 @@ enum StageFlags : int { kStageAverage = 1, kStageDt = 2 };
 
 // Enqueue one stage (prim, fluxes in every direction, update) for ndesc
 // patches.  max_w / max_f[d] / max_v: largest region sizes over the descs.
-cudaError_t launch_stage(const DevParams& P, int mixed, const StageBuffers& B,
-                         const StageDesc* d_desc, int ndesc, long long max_w,
-                         const long long max_f[3], long long max_v, int flags,
-                         double dt_scale, StepState* state, DtPartial* partials,
-                         int* nblocks_v, cudaStream_t s);
+cudaError_t launch_stage_fp64(const DevParams& P, const StageBuffers& B, const StageDesc* d_desc,
+                              int ndesc, long long max_w, const long long max_f[3],
+                              long long max_v, int flags, double dt_scale, StepState* state,
+                              DtPartial* partials, int* nblocks_v, cudaStream_t s);
+cudaError_t launch_stage_mixed(const DevParams& P, const StageBuffers& B,
+                               const StageDesc* d_desc, int ndesc, long long max_w,
+                               const long long max_f[3], long long max_v, int flags,
+                               double dt_scale, StepState* state, DtPartial* partials,
+                               int* nblocks_v, cudaStream_t s);
+
+inline cudaError_t launch_stage(const DevParams& P, int mixed, const StageBuffers& B,
+                                const StageDesc* d_desc, int ndesc, long long max_w,
+                                const long long max_f[3], long long max_v, int flags,
+                                double dt_scale, StepState* state, DtPartial* partials,
+                                int* nblocks_v, cudaStream_t s) {
+  if (mixed)
+    return launch_stage_mixed(P, B, d_desc, ndesc, max_w, max_f, max_v, flags, dt_scale, state,
+                              partials, nblocks_v, s);
+  return launch_stage_fp64(P, B, d_desc, ndesc, max_w, max_f, max_v, flags, dt_scale, state,
+                           partials, nblocks_v, s);
+}
 
 // dx / max wave speed over each desc's valueBox into per-block partials.
 cudaError_t launch_dt(const DevParams& P, const double* u, const StageDesc* d_desc, int ndesc,

@@ -1,4 +1,4 @@
-// mf_kernels.cu - the stage kernels of the GB300 patch integrator.
+// mf_stage_impl.cuh - the stage kernels of the GB300 patch integrator.
 //
 // One explicit stage of PatchMHDAM::EulerStep (src/PatchMHDAM.cpp:495-709) is
 // three kernels over every patch of a batch (blockIdx.y = patch):
@@ -9,6 +9,15 @@
 //             inner-sphere reset, positivity, RK2 averaging and the per-cell dt
 // Threads map to consecutive x cells/faces, so every load and store of the
 // component-major FArrayBox data is coalesced.
+//
+// This file is included by two translation units: mf_stage_fp64.cu (FP64
+// reconstruction and fluxes, compiled without multiply-add contraction so that
+// every operation rounds as in the CPU restatement) and mf_stage_mixed.cu
+// (FP32 reconstruction and fluxes, contraction allowed).  MF_STAGE_REAL selects
+// the flux precision; MF_STAGE_COMMON marks the unit that also defines the
+// precision-independent kernels.
+#pragma once
+
 #include "mf_kernels.cuh"
 
 #include <cfloat>
@@ -542,18 +551,26 @@ cudaError_t stage_impl(const DevParams& P, const StageBuffers& B, const StageDes
 
 }  // namespace
 
-cudaError_t launch_stage(const DevParams& P, int mixed, const StageBuffers& B,
-                         const StageDesc* d_desc, int ndesc, long long max_w,
-                         const long long max_f[3], long long max_v, int flags,
-                         double dt_scale, StepState* state, DtPartial* partials,
-                         int* nblocks_v, cudaStream_t s) {
-  if (mixed)
-    return stage_impl<float>(P, B, d_desc, ndesc, max_w, max_f, max_v, flags, dt_scale, state,
-                             partials, nblocks_v, s);
+#ifdef MF_STAGE_COMMON
+cudaError_t launch_stage_fp64(const DevParams& P, const StageBuffers& B, const StageDesc* d_desc,
+                              int ndesc, long long max_w, const long long max_f[3],
+                              long long max_v, int flags, double dt_scale, StepState* state,
+                              DtPartial* partials, int* nblocks_v, cudaStream_t s) {
   return stage_impl<double>(P, B, d_desc, ndesc, max_w, max_f, max_v, flags, dt_scale, state,
                             partials, nblocks_v, s);
 }
+#else
+cudaError_t launch_stage_mixed(const DevParams& P, const StageBuffers& B,
+                               const StageDesc* d_desc, int ndesc, long long max_w,
+                               const long long max_f[3], long long max_v, int flags,
+                               double dt_scale, StepState* state, DtPartial* partials,
+                               int* nblocks_v, cudaStream_t s) {
+  return stage_impl<float>(P, B, d_desc, ndesc, max_w, max_f, max_v, flags, dt_scale, state,
+                           partials, nblocks_v, s);
+}
+#endif
 
+#ifdef MF_STAGE_COMMON
 cudaError_t launch_dt(const DevParams& P, const double* u, const StageDesc* d_desc, int ndesc,
                       long long max_v, DtPartial* partials, int* nblocks, cudaStream_t s) {
   const dim3 gv((unsigned)((max_v + kBlock - 1) / kBlock), (unsigned)ndesc);
@@ -601,5 +618,7 @@ cudaError_t launch_flux_out(int mixed, int sd, int nc, const void* const f2[3],
   }
   return cudaGetLastError();
 }
+
+#endif  // MF_STAGE_COMMON
 
 }  // namespace mf

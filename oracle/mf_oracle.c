@@ -1678,7 +1678,7 @@ static int euler_step(const Ctx* c, double time, Fab* U, Fab* F /* [sd] or NULL 
       S[6] = dB * Uy;
       S[7] = dB * Uz;
       for (int q = 1; q <= 7; ++q) AT(U, i, j, k, q) = AT(U, i, j, k, q) + S[q];
-      if (divBout) AT(divBout, i, j, k, 0) = divB;
+      if (divBout && box_in(&divBout->b, i, j, k)) AT(divBout, i, j, k, 0) = divB;
     }
     if (c->glm) AT(U, i, j, k, 8) = psicoef * AT(U, i, j, k, 8); /* PSIPARABOLIC */
     if (p->charge_exchange && c->nf >= 2) {

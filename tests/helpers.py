@@ -25,15 +25,36 @@ def valid_view(U: np.ndarray, ng: int, sd: int) -> np.ndarray:
     return U[:, ng:-ng, ng:-ng, ng:-ng]
 
 
+def component_groups(nc: int) -> list[list[int]]:
+    """Physical groups of the conserved components: density, momentum vector,
+    energy, magnetic field vector, psi, then density / momentum / energy of
+    each neutral fluid."""
+    glm = 1 if (nc - 8) % 5 == 1 else 0
+    groups = [[0], [1, 2, 3], [4], [5, 6, 7]]
+    if glm:
+        groups.append([8])
+    s = 8 + glm
+    while s + 5 <= nc:
+        groups += [[s], [s + 1, s + 2, s + 3], [s + 4]]
+        s += 5
+    return groups
+
+
 def rel_err(a: np.ndarray, b: np.ndarray, floor_frac: float = 1e-3) -> np.ndarray:
-    """Per-component maximum of |a-b| / max(|b|, floor_frac * max|b_c|):
-    pointwise relative error, with components that pass through zero measured
-    against their own scale."""
+    """Per-component maximum of |a-b| / max(|b|, floor_frac * S): pointwise
+    relative error, where S is the largest magnitude of the component's
+    physical group (a vector component that is zero, e.g. the z-momentum of a
+    2D run, is measured against the magnitude of its vector)."""
+    nc = b.shape[0]
+    scale = np.zeros(nc)
+    for g in component_groups(nc):
+        s = max(float(np.max(np.abs(b[c]))) if b[c].size else 0.0 for c in g)
+        for c in g:
+            scale[c] = s
     out = []
-    for c in range(b.shape[0]):
+    for c in range(nc):
         bc = b[c]
-        sc = float(np.max(np.abs(bc))) if bc.size else 0.0
-        den = np.maximum(np.abs(bc), floor_frac * sc)
+        den = np.maximum(np.abs(bc), floor_frac * scale[c])
         den = np.where(den == 0.0, 1.0, den)
         out.append(float(np.max(np.abs(a[c] - bc) / den)) if bc.size else 0.0)
     return np.array(out)

@@ -18,6 +18,14 @@ RTOL = 1e-12
 pytestmark = pytest.mark.gpu
 
 
+def _assert_argmin(oracle, p, U, lo, hi, cell, dt_min):
+    """The reported cell attains the minimum dt (ties between cells whose dt
+    agree to round-off may resolve either way)."""
+    st, dtc, _ = oracle.compute_dt(p, U, lo, hi, list(cell), list(cell))
+    assert st == 0
+    assert dtc <= dt_min * (1.0 + RTOL), (cell, dtc, dt_min)
+
+
 def _gpu_patch_step(ctx, U, lo, hi, vlo, vhi, dt, F=None, divB=None):
     t = to_device(U)
     tF = None
@@ -69,7 +77,7 @@ def test_orszag_single_patch_steps(gpulib, oracle, ta):
         e = rel_err(valid_view(Ug, ng, 2), valid_view(Uo, ng, 2))
         assert np.all(e <= RTOL), (step, e)
         assert abs(ndt_g - ndt_o) <= RTOL * ndt_o
-        assert cell_g == cell_o
+        _assert_argmin(oracle, p, Uo, lo, hi, cell_g, ndt_o)
         # next step from the oracle's state, ghosts refilled
         U = periodic_fill(Uo.copy(), ng, 2)
         dt = 0.4 * ndt_o
@@ -166,7 +174,7 @@ def test_helio_single_patch_steps(gpulib, oracle):
         e = rel_err(valid_view(Ug, ng, 3), valid_view(Uo, ng, 3))
         assert np.all(e <= RTOL), (step, e)
         assert abs(ndt_g - ndt_o) <= RTOL * ndt_o
-        assert cell_g == cell_o
+        _assert_argmin(oracle, p, Uo, lo, hi, cell_g, ndt_o)
         U = Uo
         dt = 0.4 * ndt_o
     ctx.close()
@@ -209,7 +217,7 @@ def test_helio_level_vs_oracle(gpulib, oracle):
             e = rel_err(g, o)
             assert np.all(e <= RTOL), (step, i, e)
         assert abs(ndt_g - ndt_o) <= RTOL * ndt_o
-        assert (ip_g, cell_g) == (ip_o, cell_o)
+        _assert_argmin(oracle, p, arrays[ip_g], fboxes[ip_g][0], fboxes[ip_g][1], cell_g, ndt_o)
         # continue both from the oracle's state
         for i in range(len(boxes)):
             lev.patch_view(flat, i)[:] = arrays[i]
