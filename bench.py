@@ -1,0 +1,511 @@
+#!/usr/bin/env python
+"""Zone-updates/s of the multi-fluid MHD level step on one GB300.
+
+Workload (the single-GPU configuration the metric is quoted on): 3D
+multi-fluid heliosphere on a 128^3 box over [-1,1]^3 split into 512 patches of
+16^3 (4 ghost layers each), plasma MHD + 3 neutral H fluids (24 conserved
+components), GLM cleaning, charge exchange with a seeded cross-section, an
+inner solar-wind sphere, RK2, CFL 0.4.  A step advances every patch of the
+level by one time step; zone-updates per step = 128^3.
+
+Arms:
+  default            this repository's CUDA path (FP64 headline, FP32-mixed beside it)
+  --impl reference   the CPU restatement of the reference patch update on the
+                     host cores (a bounded sample of the same workload)
+
+Timing: warm-up steps, then exactly K steps bracketed by a barrier and
+torch.cuda.synchronize(); device time from CUDA events recorded on the stream
+the steps are launched on; max over ranks.  The state (>1.3 GB per array) is
+larger than L2, so no flush is needed between steps.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "ms-flukss-multifluid_gb300")
+if PKG not in sys.path:
+    sys.path.insert(0, PKG)
+
+METRIC = "zone-updates/s on 1 GB300 (FP64 vs FP32-mixed), % HBM peak, p50/p99 latency"
+UNIT = "zone-updates/s"
+N_DEFAULT = 128
+PATCH_DEFAULT = 16
+CFL = 0.4
+
+
+def _args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=40)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=N_DEFAULT)
+    ap.add_argument("--patch", type=int, default=PATCH_DEFAULT)
+    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-mixed", action="store_true")
+    return ap.parse_args()
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples every 200 ms while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.rows = []
+        self.proc = None
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200", "-i", str(self.device)],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+        time.sleep(0.3)
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 9:
+                self.rows.append(parts)
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=5)
+        sm, mx, pw = [], [], []
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            try:
+                sm.append(float(r[1]))
+                mx.append(float(r[2]))
+                pw.append(float(r[3]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, r[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        loaded = [s for s, p in zip(sm, pw) if p > 200.0] or sm
+        return {"sm_mhz": statistics.median(loaded) if loaded else None,
+                "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm),
+                "power_w_max": max(pw) if pw else None}
+
+
+def _peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def _traffic_table():
+    """Per-launch DRAM bytes of each kernel kind from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "ncu_traffic_helio.json")
+    try:
+        with open(path) as f:
+            return json.load(f)
+    except Exception:
+        return {}
+
+
+def _build_level(mfgpu, p, boxes, torch):
+    ctx = mfgpu.Context(p)
+    lev = mfgpu.Level(ctx, boxes)
+    host = torch.empty(lev.ndoubles, dtype=torch.float64, pin_memory=True)
+    flat = host.numpy()
+    flat[:] = 0.0
+    for i in range(len(boxes)):
+        flo, fhi = lev.fab_box(i)
+        lev.patch_view(flat, i)[:] = mfgpu.init_host_fab(p, flo, fhi, "helio")
+    lev.upload(host.data_ptr())
+    dt0, _, _ = lev.compute_dt()
+    ch = p.factor_ch * p.dx / dt0
+    cp = (ch * p.dx / p.factor_cp) ** 0.5
+    ctx.set_dedner(ch, cp)
+    return ctx, lev, host, dt0
+
+
+def _algorithmic_bytes(kind, p, boxes, nc, rsize):
+    """Minimum bytes one launch of a kernel kind must move (each value once)."""
+    sd = p.space_dim
+    cells = sum((hi[0] - lo[0] + 1) * (hi[1] - lo[1] + 1) * (hi[2] - lo[2] + 1) for lo, hi in boxes)
+    faces = 0
+    for lo, hi in boxes:
+        n = [hi[d] - lo[d] + 1 for d in range(3)]
+        faces += (n[0] + 1) * n[1] * n[2]  # one direction
+    wcells = sum((hi[0] - lo[0] + 5) * (hi[1] - lo[1] + 5) * (hi[2] - lo[2] + 5) for lo, hi in boxes)
+    if kind == "flux":
+        return wcells * 8 * nc + faces * (nc + 1) * rsize
+    if kind == "update":
+        return cells * 8 * nc * 4 + sd * faces * (nc + 1) * rsize
+    if kind == "prim":
+        return wcells * 8 * nc * 2
+    if kind == "exchange":
+        ghost = sum(((hi[0] - lo[0] + 9) * (hi[1] - lo[1] + 9) * (hi[2] - lo[2] + 9))
+                    - (hi[0] - lo[0] + 1) * (hi[1] - lo[1] + 1) * (hi[2] - lo[2] + 1)
+                    for lo, hi in boxes)
+        return ghost * nc * 16
+    return 0
+
+
+def _time_steps(lev, torch, stream, steps):
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(steps):
+        lev.step_async(stream.cuda_stream)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    return ev0.elapsed_time(ev1)
+
+
+def run_ours(a):
+    import numpy as np
+    import torch
+
+    import build as mfbuild
+    mfbuild.build()
+    import mfgpu
+
+    ws, rank, local = _dist()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    def barrier():
+        if ws > 1:
+            import torch.distributed as dist
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    n, patch = a.n, a.patch
+    boxes = mfgpu.tile_boxes(n, patch, 3)
+    zones = n ** 3
+    stream = torch.cuda.Stream()
+    p64 = mfgpu.helio_params(n, precision=mfgpu.PREC_FP64)
+    ctx, lev, host, dt0 = _build_level(mfgpu, p64, boxes, torch)
+    lev.seed_dt(CFL * dt0, CFL, stream.cuda_stream)
+    for _ in range(a.warmup):
+        lev.step_async(stream.cuda_stream)
+    torch.cuda.synchronize()
+    st, _, _, _ = lev.result(stream.cuda_stream)
+    mfgpu.check(st, "warm-up steps")
+
+    sampler = ClockSampler(local)
+    sampler.start()
+    barrier()
+    ms = _time_steps(lev, torch, stream, a.steps)
+    barrier()
+    clocks = sampler.stop()
+    st, dt_min, _, _ = lev.result(stream.cuda_stream)
+    mfgpu.check(st, "timed steps")
+    ms_all = ms
+    if ws > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_all = float(t.item())
+    value = ws * zones * a.steps / (ms_all * 1e-3)
+    launches = lev.launches_per_step()
+
+    # per-launch device times of one step (CUDA events on the launching stream)
+    prof = lev.profile_step(CFL * dt_min)
+    by_kind = {}
+    for kind, t in prof:
+        tot, cnt = by_kind.get(kind, (0.0, 0))
+        by_kind[kind] = (tot + t, cnt + 1)
+    step_ms_prof = sum(t for _, t in prof)
+    dom = max(by_kind, key=lambda k: by_kind[k][0])
+    dom_avg_ms = by_kind[dom][0] / by_kind[dom][1]
+    nc = ctx.nc
+    alg = _algorithmic_bytes(dom, p64, boxes, nc, 8)
+    peak, peak_kind = _peaks()
+    achieved = alg / (dom_avg_ms * 1e-3) / 1e9
+    traffic = _traffic_table().get(f"fp64_{dom}")
+
+    # end to end through the C ABI with host buffers: H2D of the level state,
+    # one step (mf_level_step returns the new dt on the host), D2H of the state
+    e2e_steps = max(1, a.e2e_steps)
+    nbytes = lev.ndoubles * 8
+    dt_e = CFL * dt_min
+    lev.upload(host.data_ptr(), stream.cuda_stream)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    t0 = time.perf_counter()
+    e0.record(stream)
+    for _ in range(e2e_steps):
+        lev.upload(host.data_ptr(), stream.cuda_stream)
+        st, ndt, _, _ = lev.step(dt_e, stream.cuda_stream)
+        mfgpu.check(st, "e2e step")
+        lev.download(host.data_ptr(), stream.cuda_stream)
+        dt_e = CFL * ndt
+    e1.record(stream)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    e2e_ms = e0.elapsed_time(e1)
+    e2e_value = ws * zones * e2e_steps / (max(e2e_ms * 1e-3, wall))
+
+    fast = None
+    if not a.no_mixed:
+        pf = mfgpu.helio_params(n, precision=mfgpu.PREC_FP64_FAST)
+        ctxf, levf, hostf, dtf = _build_level(mfgpu, pf, boxes, torch)
+        levf.seed_dt(CFL * dtf, CFL, stream.cuda_stream)
+        for _ in range(a.warmup):
+            levf.step_async(stream.cuda_stream)
+        torch.cuda.synchronize()
+        barrier()
+        msf = _time_steps(levf, torch, stream, a.steps)
+        barrier()
+        stf, _, _, _ = levf.result(stream.cuda_stream)
+        mfgpu.check(stf, "fast fp64 steps")
+        proff = levf.profile_step(CFL * dtf)
+        fast = {"value": ws * zones * a.steps / (msf * 1e-3), "ms_per_step": msf / a.steps,
+                "speedup_vs_fp64": (ws * zones * a.steps / (msf * 1e-3)) / value,
+                "per_kind_ms": {}, "dtype": "f64 with fused multiply-adds and reused reciprocals"}
+        for kind, t in proff:
+            fast["per_kind_ms"][kind] = fast["per_kind_ms"].get(kind, 0.0) + t
+        levf.close()
+        ctxf.close()
+        del hostf
+
+    mixed = None
+    if not a.no_mixed:
+        pm = mfgpu.helio_params(n, precision=mfgpu.PREC_MIXED)
+        ctxm, levm, hostm, dtm = _build_level(mfgpu, pm, boxes, torch)
+        levm.seed_dt(CFL * dtm, CFL, stream.cuda_stream)
+        for _ in range(a.warmup):
+            levm.step_async(stream.cuda_stream)
+        torch.cuda.synchronize()
+        barrier()
+        msm = _time_steps(levm, torch, stream, a.steps)
+        barrier()
+        stm, _, _, _ = levm.result(stream.cuda_stream)
+        mfgpu.check(stm, "mixed steps")
+        # accuracy: same initial state, same dt sequence, both forms
+        nsteps_acc = min(a.steps, 20)
+        flat0 = np.zeros(lev.ndoubles)
+        for i in range(len(boxes)):
+            flo, fhi = lev.fab_box(i)
+            lev.patch_view(flat0, i)[:] = mfgpu.init_host_fab(p64, flo, fhi, "helio")
+        lev.upload(flat0.ctypes.data)
+        levm.upload(flat0.ctypes.data)
+        ctxm.set_dedner(p64.factor_ch * p64.dx / dt0,
+                        (p64.factor_ch * p64.dx / dt0 * p64.dx / p64.factor_cp) ** 0.5)
+        ctx.set_dedner(p64.factor_ch * p64.dx / dt0,
+                       (p64.factor_ch * p64.dx / dt0 * p64.dx / p64.factor_cp) ** 0.5)
+        dt = CFL * dt0
+        for _ in range(nsteps_acc):
+            mfgpu.check(levm.step(dt)[0], "mixed accuracy step")
+            st, ndt, _, _ = lev.step(dt)
+            mfgpu.check(st, "fp64 accuracy step")
+            ch = p64.factor_ch * p64.dx / ndt
+            cp = (ch * p64.dx / p64.factor_cp) ** 0.5
+            ctx.set_dedner(ch, cp)
+            ctxm.set_dedner(ch, cp)
+            dt = CFL * ndt
+        a64 = np.zeros(lev.ndoubles)
+        amx = np.zeros(lev.ndoubles)
+        lev.download(a64.ctypes.data)
+        levm.download(amx.ctypes.data)
+        ng = ctx.ng
+        num = {}
+        den = {}
+        for i in range(len(boxes)):
+            g64 = lev.patch_view(a64, i)[:, ng:-ng, ng:-ng, ng:-ng]
+            gmx = lev.patch_view(amx, i)[:, ng:-ng, ng:-ng, ng:-ng]
+            qs = {"rho": (g64[0], gmx[0]),
+                  "rho_n1": (g64[9], gmx[9]), "rho_n2": (g64[14], gmx[14]),
+                  "rho_n3": (g64[19], gmx[19]),
+                  "absB": (np.sqrt(g64[5] ** 2 + g64[6] ** 2 + g64[7] ** 2),
+                           np.sqrt(gmx[5] ** 2 + gmx[6] ** 2 + gmx[7] ** 2))}
+            ke64 = 0.5 * (g64[1] ** 2 + g64[2] ** 2 + g64[3] ** 2) / g64[0]
+            kemx = 0.5 * (gmx[1] ** 2 + gmx[2] ** 2 + gmx[3] ** 2) / gmx[0]
+            b64 = (g64[5] ** 2 + g64[6] ** 2 + g64[7] ** 2) / (8 * np.pi)
+            bmx = (gmx[5] ** 2 + gmx[6] ** 2 + gmx[7] ** 2) / (8 * np.pi)
+            qs["p"] = ((2.0 / 3.0) * (g64[4] - ke64 - b64), (2.0 / 3.0) * (gmx[4] - kemx - bmx))
+            for k, (x, y) in qs.items():
+                num[k] = num.get(k, 0.0) + float(np.sum(np.abs(y - x)))
+                den[k] = den.get(k, 0.0) + float(np.sum(np.abs(x)))
+        l1 = {k: num[k] / den[k] for k in num}
+        profm = levm.profile_step(CFL * dt0)
+        mixed = {"value": ws * zones * a.steps / (msm * 1e-3),
+                 "ms_per_step": msm / a.steps,
+                 "speedup_vs_fp64": (ws * zones * a.steps / (msm * 1e-3)) / value,
+                 "step_hbm_frac": (ws * zones * a.steps / (msm * 1e-3) * 16 * nc / 1e9) / peak,
+                 "per_kind_ms": {},
+                 "l1_rel_vs_fp64": l1, "l1_steps": nsteps_acc,
+                 "dtype": "f32 reconstruction+fluxes, f64 state/accumulation/sources"}
+        for kind, t in profm:
+            mixed["per_kind_ms"][kind] = mixed["per_kind_ms"].get(kind, 0.0) + t
+        levm.close()
+        ctxm.close()
+
+    cpu = None
+    if not a.no_cpu_baseline and rank == 0 and ws == 1:
+        cpu = cpu_baseline(n, patch, min_seconds=10.0, max_steps=30)
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": a.steps,
+        "warmup": a.warmup, "ms_per_step": ms_all / a.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"3D multi-fluid heliosphere {n}^3 on [-1,1]^3, "
+                               f"{len(boxes)} patches of {patch}^3 + 4 ghosts, plasma MHD + "
+                               "3 neutral H fluids (24 comps), GLM, charge exchange, RK2, CFL 0.4",
+                   "zones_per_step": zones, "patches": len(boxes), "patch": patch,
+                   "l2": "inputs larger than L2 (state arrays > 1.3 GB); no flush",
+                   "parallelism": f"{ws} independent replica(s), one per GPU"},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": nbytes,
+                "d2h_bytes_per_step": nbytes, "steps": e2e_steps,
+                "path": "mf_level_upload (pinned host) + mf_level_step + mf_level_download"},
+        "gpu_launches": launches * a.steps,
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
+                     "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
+                     "peak_source": peak_kind,
+                     "algorithmic_bytes_per_launch": alg, "avg_launch_ms": dom_avg_ms,
+                     "step_hbm_frac": (value * 16 * nc / 1e9) / peak,
+                     "per_kind_ms": {k: v[0] for k, v in by_kind.items()},
+                     "profiled_step_ms": step_ms_prof},
+        "clocks": clocks,
+    }
+    if fast is not None:
+        line["fp64_fast"] = fast
+    if mixed is not None:
+        line["mixed"] = mixed
+    if cpu is not None:
+        line["cpu_baseline"] = cpu
+    if rank == 0:
+        print(json.dumps(line))
+    lev.close()
+    ctx.close()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def _cpu_sample(n, patch):
+    """64 patches (a 4x4x4 block at the centre of the domain, containing the
+    inner sphere) of the full workload."""
+    import mfgpu
+    boxes = mfgpu.tile_boxes(n, patch, 3)
+    npb = n // patch
+    c0 = max(0, npb // 2 - 2)
+    sel = []
+    for lo, hi in boxes:
+        ib, jb, kb = lo[0] // patch, lo[1] // patch, lo[2] // patch
+        if c0 <= ib < c0 + 4 and c0 <= jb < c0 + 4 and c0 <= kb < c0 + 4:
+            sel.append((lo, hi))
+    return sel
+
+
+def cpu_baseline(n, patch, min_seconds=10.0, max_steps=30, warmup=1, fixed_steps=None):
+    """The oracle (C restatement of the reference patch update, OpenMP over
+    patches as AMRLevelIdealMHD::stepOMP) on a bounded sample of the workload."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import numpy as np
+    import mfgpu
+    import pyoracle
+    p = mfgpu.helio_params(n, precision=mfgpu.PREC_FP64)
+    sel = _cpu_sample(n, patch)
+    ng = mfgpu.num_ghost(p)
+    arrays, fboxes = [], []
+    for lo, hi in sel:
+        flo, fhi = mfgpu.grow(lo, hi, ng, 3)
+        arrays.append(np.ascontiguousarray(mfgpu.init_host_fab(p, flo, fhi, "helio")))
+        fboxes.append((flo, fhi))
+    threads = os.cpu_count() or 1
+    dt0 = min(pyoracle.compute_dt(p, a, fb[0], fb[1], b[0], b[1])[1]
+              for a, fb, b in zip(arrays, fboxes, sel))
+    ch = p.factor_ch * p.dx / dt0
+    p.dedner_ch, p.dedner_cp = ch, (ch * p.dx / p.factor_cp) ** 0.5
+    dt = CFL * dt0
+    for _ in range(warmup):
+        st, ndt, _, _ = pyoracle.level_step(p, arrays, fboxes, sel, dt, threads)
+        dt = CFL * ndt
+    steps = 0
+    t0 = time.perf_counter()
+    while True:
+        st, ndt, _, _ = pyoracle.level_step(p, arrays, fboxes, sel, dt, threads)
+        assert st == 0, st
+        dt = CFL * ndt
+        steps += 1
+        el = time.perf_counter() - t0
+        if fixed_steps is not None:
+            if steps >= fixed_steps:
+                break
+        elif el >= min_seconds or steps >= max_steps:
+            break
+    el = time.perf_counter() - t0
+    zones = sum((hi[0] - lo[0] + 1) * (hi[1] - lo[1] + 1) * (hi[2] - lo[2] + 1) for lo, hi in sel)
+    return {"value": zones * steps / el, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{len(sel)} of the {(n // patch) ** 3} patches ({zones} zones, the "
+                      f"central 4x4x4 block), {steps} level steps after {warmup} warm-up, "
+                      f"{el:.1f} s", "threads": pyoracle.max_threads()}
+
+
+def run_reference(a):
+    ws, rank, _ = _dist()
+    if rank != 0:
+        return
+    cb = cpu_baseline(a.n, a.patch, warmup=max(1, a.warmup), fixed_steps=max(1, a.steps))
+    line = {
+        "metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": ws, "steps": a.steps,
+        "warmup": a.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic", "impl": "reference",
+        "config": {"workload": f"3D multi-fluid heliosphere {a.n}^3, patches of {a.patch}^3 "
+                               "(bounded sample, see cpu_baseline.sample)"},
+        "cpu_baseline": cb,
+        "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def main():
+    a = _args()
+    if a.impl == "reference":
+        run_reference(a)
+    else:
+        run_ours(a)
+
+
+if __name__ == "__main__":
+    main()

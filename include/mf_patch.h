@@ -54,9 +54,17 @@ typedef enum mf_status {
 
 /* time_approximation (PatchMHDAM::eTimeApproximation) */
 enum { MF_TA_FIRST_ORDER = 0, MF_TA_HANCOCK = 1, MF_TA_RK2 = 2 };
-/* precision of reconstruction + Riemann fluxes; state, accumulation, pressure
-   recovery, positivity and charge exchange are always FP64 */
-enum { MF_PREC_FP64 = 0, MF_PREC_MIXED = 1 };
+/* Precision modes.
+   MF_PREC_FP64       FP64 everywhere, every operation in the reference's order
+                      and rounding (no fused multiply-add): the parity path.
+   MF_PREC_MIXED      FP32 reconstruction + Riemann fluxes; state, flux
+                      accumulation, pressure recovery, positivity and charge
+                      exchange FP64.
+   MF_PREC_FP64_FAST  FP64 everywhere with fused multiply-adds and reused
+                      reciprocals (results differ from MF_PREC_FP64 at the
+                      rounding level; limiter and region decisions identical
+                      for identical input states). */
+enum { MF_PREC_FP64 = 0, MF_PREC_MIXED = 1, MF_PREC_FP64_FAST = 2 };
 /* physical (non-periodic) boundary treatment of primitive ghost cells */
 enum { MF_BC_NONE = 0, MF_BC_FARFIELD = 1 };
 /* limiter1D::eLimiters (src/limiter1D.H:17-28) */
@@ -203,6 +211,13 @@ mf_status mf_level_result(mf_level* lev, double* new_dt, int* min_patch, int min
                           void* stream);
 /* Kernel launches enqueued by one mf_level_step (for accounting). */
 int mf_level_launches_per_step(const mf_level* lev);
+/* Diagnostic (no reference counterpart): one step enqueued launch by launch
+   (no graph) with a CUDA event after every launch on the launching stream;
+   ms[i] is the device time of launch i, kinds[i] its kernel kind (0 ghost
+   exchange, 1 primitive variables, 2 face fluxes, 3 update + sources,
+   4 dt reduction).  The state advances by one step with time step dt. */
+mf_status mf_level_profile_step(mf_level* lev, double dt, float* ms, int* kinds, int* nlaunch,
+                                int max_launch);
 
 /* Problem set-up on host fabs (PhysProblem::initialize):
    Orszag-Tang vortex (problems/OrszagF.ChF:27-79) and the synthetic

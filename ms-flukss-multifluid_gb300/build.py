@@ -45,8 +45,8 @@ def _headers() -> list[str]:
 def _compile(src: str, verbose: bool) -> str:
     obj = os.path.join(BUILD_DIR, os.path.basename(src) + ".o")
     cmd = [_nvcc()] + ARCH + NVCC_FLAGS
-    if "_fp64" in os.path.basename(src):
-        # FP64 kernels: no fused multiply-add, every operation rounds as in
+    if "_exact" in os.path.basename(src):
+        # no fused multiply-add: every operation rounds as in
         # the CPU restatement of the reference
         cmd += ["-fmad=false"]
     if src.endswith(".cpp"):

@@ -17,6 +17,7 @@
 #include <vector>
 
 #include "mf_kernels.cuh"
+#include "mf_sources_exact.cuh"
 
 using mf::CopyReg;
 using mf::DevParams;
@@ -137,7 +138,9 @@ mf_status validate_params(const mf_params& p) {
   if (!(p.gamma > 1.0) || !(p.dx > 0.0)) return MF_ERR_BAD_ARG;
   if (p.time_approximation != MF_TA_RK2 && p.time_approximation != MF_TA_FIRST_ORDER)
     return MF_ERR_UNSUPPORTED;
-  if (p.precision != MF_PREC_FP64 && p.precision != MF_PREC_MIXED) return MF_ERR_BAD_ARG;
+  if (p.precision != MF_PREC_FP64 && p.precision != MF_PREC_MIXED &&
+      p.precision != MF_PREC_FP64_FAST)
+    return MF_ERR_BAD_ARG;
   if (p.divb_cleaning != 0 && p.divb_cleaning != 5) return MF_ERR_UNSUPPORTED;
   if (p.divb_cleaning == 5) {
     // main/MHDAM.cpp:1042-1046
@@ -196,6 +199,7 @@ DevParams make_dev(const mf_params& p) {
   P.gamma = p.gamma;
   P.hgamma = p.gamma - 1.0;
   P.invhgamma = 1.0 / P.hgamma;
+  P.invgamma = 1.0 / p.gamma;
   P.smallr = p.smallr;
   P.smallp = p.smallp;
   P.del2 = p.entropy_fix;
@@ -532,7 +536,7 @@ mf_status mf_patch_update(mf_ctx* c, mf_fab* U, const mf_box* valid, double dt, 
       B.f[d] = c->f1[d].p;
       B.bn[d] = c->bn1[d].p;
     }
-    MF_CHECK_CUDA(mf::launch_stage(c->dp, mixed, B, dd, 1, box_cells(w1), mf1, box_cells(v1), 0,
+    MF_CHECK_CUDA(mf::launch_stage(c->dp, p.precision,B, dd, 1, box_cells(w1), mf1, box_cells(v1), 0,
                                    1.0, ds, parts, &nb, s));
     B.uin = (double*)c->pred.p;
     B.uout = U->data;
@@ -548,7 +552,7 @@ mf_status mf_patch_update(mf_ctx* c, mf_fab* U, const mf_box* valid, double dt, 
         B.divb_n[d] = divB->box.hi[d] - divB->box.lo[d] + 1;
       }
     }
-    MF_CHECK_CUDA(mf::launch_stage(c->dp, mixed, B, dd + 1, 1, box_cells(w2), mf2, box_cells(v2),
+    MF_CHECK_CUDA(mf::launch_stage(c->dp, p.precision,B, dd + 1, 1, box_cells(w2), mf2, box_cells(v2),
                                    mf::kStageAverage | mf::kStageDt, 0.5, ds, parts, &nb, s));
   } else {
     B.uin = U->data;
@@ -564,7 +568,7 @@ mf_status mf_patch_update(mf_ctx* c, mf_fab* U, const mf_box* valid, double dt, 
         B.divb_n[d] = divB->box.hi[d] - divB->box.lo[d] + 1;
       }
     }
-    MF_CHECK_CUDA(mf::launch_stage(c->dp, mixed, B, dd + 1, 1, box_cells(w2), mf2, box_cells(v2),
+    MF_CHECK_CUDA(mf::launch_stage(c->dp, p.precision,B, dd + 1, 1, box_cells(w2), mf2, box_cells(v2),
                                    mf::kStageDt, 1.0, ds, parts, &nb, s));
   }
   MF_CHECK_CUDA(mf::launch_finalize(c->dp, parts, nb, ds, 0, s));
@@ -702,7 +706,10 @@ static void add_regions(const mf_level* L, const mf_params& p, int depth, std::v
   }
 }
 
-static mf_status enqueue_level_step(mf_level* L, int advance) {
+// ev (nullable): events recorded after every launch, in launch order, with
+// kinds[] receiving 0 exchange, 1 prim, 2 flux, 3 update, 4 finalize.
+static mf_status enqueue_level_step(mf_level* L, int advance, cudaEvent_t* ev = nullptr,
+                                    int* kinds = nullptr, int* nev = nullptr) {
   mf_ctx* c = L->ctx;
   const mf_params& p = c->p;
   const int mixed = (p.precision == MF_PREC_MIXED);
@@ -719,26 +726,51 @@ static mf_status enqueue_level_step(mf_level* L, int advance) {
   }
   int nb = 0;
   const int nc = c->nc;
+  const int sd = p.space_dim;
+  int ne = 0;
+  auto mark = [&](int kind) {
+    if (!ev) return;
+    cudaEventRecord(ev[ne], s);
+    kinds[ne] = kind;
+    ++ne;
+  };
+  auto stage_marks = [&](int n0) {
+    if (!ev) return;
+    kinds[n0] = 1;
+    for (int d = 0; d < sd; ++d) kinds[n0 + 1 + d] = 2;
+    kinds[n0 + 1 + sd] = 3;
+    ne = n0 + 2 + sd;
+  };
   MF_CHECK_CUDA(mf::launch_exchange((double*)L->U.p, (const CopyReg*)L->exfull.p, L->nfull, nc, s));
+  if (L->nfull) mark(0);
   if (p.time_approximation == MF_TA_RK2) {
     B.uin = (const double*)L->U.p;
     B.uout = (double*)L->U1.p;
-    MF_CHECK_CUDA(mf::launch_stage(c->dp, mixed, B, dd, L->np, L->max_w, L->max_f, L->max_v, 0,
+    B.ev = ev ? ev + ne : nullptr;
+    MF_CHECK_CUDA(mf::launch_stage(c->dp, p.precision,B, dd, L->np, L->max_w, L->max_f, L->max_v, 0,
                                    1.0, ds, parts, &nb, s));
+    stage_marks(ne);
     MF_CHECK_CUDA(
         mf::launch_exchange((double*)L->U1.p, (const CopyReg*)L->extwo.p, L->ntwo, nc, s));
+    if (L->ntwo) mark(0);
     B.uin = (const double*)L->U1.p;
     B.uout = (double*)L->U.p;
     B.uold = (const double*)L->U.p;
-    MF_CHECK_CUDA(mf::launch_stage(c->dp, mixed, B, dd, L->np, L->max_w, L->max_f, L->max_v,
+    B.ev = ev ? ev + ne : nullptr;
+    MF_CHECK_CUDA(mf::launch_stage(c->dp, p.precision,B, dd, L->np, L->max_w, L->max_f, L->max_v,
                                    mf::kStageAverage | mf::kStageDt, 0.5, ds, parts, &nb, s));
+    stage_marks(ne);
   } else {
     B.uin = (const double*)L->U.p;
     B.uout = (double*)L->U.p;
-    MF_CHECK_CUDA(mf::launch_stage(c->dp, mixed, B, dd, L->np, L->max_w, L->max_f, L->max_v,
+    B.ev = ev ? ev + ne : nullptr;
+    MF_CHECK_CUDA(mf::launch_stage(c->dp, p.precision,B, dd, L->np, L->max_w, L->max_f, L->max_v,
                                    mf::kStageDt, 1.0, ds, parts, &nb, s));
+    stage_marks(ne);
   }
   MF_CHECK_CUDA(mf::launch_finalize(c->dp, parts, nb, ds, advance, s));
+  mark(4);
+  if (nev) *nev = ne;
   return MF_OK;
 }
 
@@ -1076,6 +1108,42 @@ mf_status mf_level_result(mf_level* L, double* new_dt, int* min_patch, int min_c
 
 int mf_level_launches_per_step(const mf_level* L) { return L ? L->launches : -1; }
 
+mf_status mf_level_profile_step(mf_level* L, double dt, float* ms, int* kinds, int* nlaunch,
+                                int max_launch) {
+  if (!L || !ms || !kinds || !nlaunch || !(dt > 0.0)) return MF_ERR_BAD_ARG;
+  if (max_launch < L->launches) return MF_ERR_BAD_ARG;
+  mf_ctx* c = L->ctx;
+  std::vector<cudaEvent_t> ev(L->launches + 1);
+  for (auto& e : ev) MF_CHECK_CUDA(cudaEventCreate(&e));
+  StepState* hs = (StepState*)L->hstate.p;
+  std::memset(hs, 0, sizeof(*hs));
+  hs->dt = dt;
+  hs->ch = c->p.dedner_ch;
+  hs->cp = c->p.dedner_cp;
+  mf_status st = MF_OK;
+  int ne = 0;
+  do {
+    if (cudaMemcpyAsync(L->state.p, hs, sizeof(StepState), cudaMemcpyHostToDevice, L->s) !=
+        cudaSuccess) {
+      st = MF_ERR_CUDA;
+      break;
+    }
+    cudaEventRecord(ev[0], L->s);
+    st = enqueue_level_step(L, 0, ev.data() + 1, kinds, &ne);
+    if (st != MF_OK) break;
+    st = wait_stream(L->s, c->timeout);
+    if (st != MF_OK) break;
+    for (int q = 0; q < ne; ++q) {
+      float t = 0.f;
+      cudaEventElapsedTime(&t, ev[q], ev[q + 1]);
+      ms[q] = t;
+    }
+    *nlaunch = ne;
+  } while (0);
+  for (auto& e : ev) cudaEventDestroy(e);
+  return st;
+}
+
 // ---------------------------------------------------------------------------
 // problem set-up on host fabs
 // ---------------------------------------------------------------------------
@@ -1161,7 +1229,7 @@ mf_status mf_init_helio_host(const mf_params* p, const double* wp, const double*
           u[s + 3] = r * w[3];
           u[s + 4] = w[4] * invhg + 0.5 * r * ke2;
         }
-        if (p->reinit_sphere) mf::reinit_cell(P, i, j, k, u);
+        if (p->reinit_sphere) mf::exact::reinit_cell(P, i, j, k, u);
         for (int q = 0; q < U->ncomp; ++q) U->data[hidx(U, i, j, k, q)] = u[q];
       }
   return MF_OK;

@@ -1,0 +1,126 @@
+// mf_flux_kernel.cuh - the face-flux kernel.  Included by mf_flux.cu (fast
+// physics, contraction allowed) and mf_flux_exact.cu (parity physics, no
+// contraction); MF_PHYS names the physics namespace of the including unit.
+#pragma once
+
+#include "mf_kernels.cuh"
+
+namespace mf {
+namespace {
+using namespace MF_PHYS;
+
+template <typename R, int DIR>
+__global__ void __launch_bounds__(kBlock)
+    k_flux(const DevParams P, const double* __restrict__ W, R* __restrict__ F,
+           R* __restrict__ Bn, const StageDesc* __restrict__ descs,
+           const StepState* __restrict__ ss) {
+  const StageDesc& D = descs[blockIdx.y];
+  int fnb[3] = {D.vn[0], D.vn[1], D.vn[2]};
+  fnb[DIR] += 1;
+  const int n = fnb[0] * fnb[1] * fnb[2];
+  const int lin = blockIdx.x * blockDim.x + threadIdx.x;
+  if (lin >= n) return;
+  int i, j, k;
+  decode(lin, D.vlo, fnb, i, j, k);
+  const long long cs = (long long)D.fn[0] * D.fn[1] * D.fn[2];
+  const long long st = (DIR == 0) ? 1 : (DIR == 1) ? (long long)D.fn[0]
+                                                   : (long long)D.fn[0] * D.fn[1];
+  // cell on the high side of face (i,j,k) has the same index
+  const double* __restrict__ w0 = W + D.u_off + loc(D.flo, D.fn, i, j, k);
+  const long long fcs = (long long)fnb[0] * fnb[1] * fnb[2];
+  const long long fo = loc(D.vlo, fnb, i, j, k);
+  R* __restrict__ Fo = F + D.f_off[DIR] + fo;
+
+  // positivity check of rho and p face values (CHECKPOSITIVITY / REDUCEORDER,
+  // src/reconstructionF.ChF:1023-1054): first order for the whole cell
+  bool negL = false, negR = false;
+  if (P.check_pos) {
+#pragma unroll
+    for (int t = 0; t < 2; ++t) {
+      const int v = t ? 4 : 0;
+      const double* wv = w0 + v * cs;
+      R a = R(wv[-2 * st]), b = R(wv[-st]), c = R(wv[0]), d = R(wv[st]);
+      R lo, hi;
+      face_values<R>(P.lim[v], a, b, c, lo, hi);
+      if (lo <= R(0) || hi <= R(0)) negL = true;
+      face_values<R>(P.lim[v], b, c, d, lo, hi);
+      if (lo <= R(0) || hi <= R(0)) negR = true;
+    }
+  }
+
+  // plasma (+ psi) face states: left = high-face value of the low cell,
+  // right = low-face value of the high cell (Roe8WavesRS::fluxes,
+  // src/Roe8WavesRS.cpp:38-78)
+  R wl[9], wr[9];
+#pragma unroll
+  for (int v = 0; v < 9; ++v) {
+    if (v < 8 || P.glm) {
+      const int lim = (v < 8) ? P.lim[v] : (int)MF_LIM_MINMOD;
+      const double* wv = w0 + v * cs;
+      R a = R(wv[-2 * st]), b = R(wv[-st]), c = R(wv[0]), d = R(wv[st]);
+      R lo, hi;
+      face_values<R>(lim, a, b, c, lo, hi);
+      wl[v] = negL ? b : hi;
+      face_values<R>(lim, b, c, d, lo, hi);
+      wr[v] = negR ? c : lo;
+    } else {
+      wl[v] = R(0);
+      wr[v] = R(0);
+    }
+  }
+  R g[9];
+  if (P.rs == kRoe8)
+    roe_mhd<R, DIR, false>(P, wl, wr, g);
+  else if (P.rs == kRoe7)
+    roe_mhd<R, DIR, true>(P, wl, wr, g);
+  else
+    rusanov_mhd<R, DIR>(P, wl, wr, g);
+  if (P.glm) {
+    R fbn, fpsi;
+    dedner_2x2<R>(R(ss->ch), wl[5 + DIR], wl[8], wr[5 + DIR], wr[8], fbn, fpsi);
+    g[5 + DIR] = fbn;
+    g[8] = fpsi;
+  }
+#pragma unroll
+  for (int q = 0; q < 8; ++q) Fo[q * fcs] = g[q];
+  if (P.glm) Fo[8 * fcs] = g[8];
+
+  // face-normal B (PatchMHDMF::computeBn, srcIdeal/PatchMHDMF.cpp:509-620)
+  R bn = R(0);
+  if (P.divb_method == 1) {
+    bn = R(0.5) * (wl[5 + DIR] + wr[5 + DIR]);
+    if (!P.periodic[DIR]) {
+      const int f = (DIR == 0) ? i : (DIR == 1) ? j : k;
+      if (f == P.dlo[DIR]) bn = wr[5 + DIR];
+      if (f == P.dhi[DIR] + 1) bn = wl[5 + DIR];
+    }
+  } else if (P.divb_method == 2) {
+    const double* wv = w0 + (5 + DIR) * cs;
+    bn = R(0.5 * (wv[-st] + wv[0]));
+  }
+  Bn[D.bn_off[DIR] + fo] = bn;
+
+  // neutral fluids: minmod face states, van Leer splitting (VANLEERF)
+  for (int fl = 1; fl < P.nf; ++fl) {
+    const int s = P.irhon + (fl - 1) * 5;
+    R nl[5], nr[5], gn[5];
+#pragma unroll
+    for (int m = 0; m < 5; ++m) {
+      const double* wv = w0 + (s + m) * cs;
+      R a = R(wv[-2 * st]), b = R(wv[-st]), c = R(wv[0]), d = R(wv[st]);
+      R lo, hi;
+      face_values<R>(MF_LIM_MINMOD, a, b, c, lo, hi);
+      nl[m] = negL ? b : hi;
+      face_values<R>(MF_LIM_MINMOD, b, c, d, lo, hi);
+      nr[m] = negR ? c : lo;
+    }
+    vanleer_euler<R, DIR>(P, nl, nr, gn);
+#pragma unroll
+    for (int m = 0; m < 5; ++m) Fo[(s + m) * fcs] = gn[m];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// update + sources + positivity (+ RK2 average, + dt)
+}  // namespace
+}  // namespace mf

@@ -1,9 +1,34 @@
-// mf_kernels.cuh - launch interface of the stage kernels (see mf_kernels.cu).
+// mf_kernels.cuh - launch interface of the stage kernels.
+//
+// One explicit stage of PatchMHDAM::EulerStep (src/PatchMHDAM.cpp:495-709) is
+// three kinds of kernel over every patch of a batch (blockIdx.y = patch):
+//   k_prim    (mf_prim_exact.cu) conserved -> primitive on valueBox.grow(2)
+//   k_flux<D> (mf_flux.cu)       face states + Riemann fluxes in direction D
+//   k_update  (mf_update.cu)     flux divergence, sources, positivity, RK2
+//                                averaging and the per-cell dt
 #pragma once
+
+#include <cfloat>
+#include <climits>
 
 #include "mf_device.cuh"
 
 namespace mf {
+
+constexpr int kBlock = 128;
+
+__device__ __forceinline__ long long loc(const int* lo, const int* n, int i, int j, int k) {
+  return (long long)(i - lo[0]) +
+         (long long)n[0] * ((long long)(j - lo[1]) + (long long)n[1] * (long long)(k - lo[2]));
+}
+
+__device__ __forceinline__ void decode(int lin, const int* lo, const int* n, int& i, int& j,
+                                       int& k) {
+  i = lo[0] + lin % n[0];
+  int t = lin / n[0];
+  j = lo[1] + t % n[1];
+  k = lo[2] + t / n[1];
+}
 
 // One block copies one box of cells (all components) from a source fab to a
 // destination fab inside the same buffer: a ghost region of LevelData::exchange.
@@ -23,33 +48,44 @@ struct StageBuffers {
   void* bn[3];         // face-normal B (double or float), per direction
   double* divb;        // optional divB output (single patch: fab on the valid box)
   int divb_lo[3], divb_n[3];
+  cudaEvent_t* ev;     // optional: an event recorded after each launch (profiling)
 };
 
 enum StageFlags : int { kStageAverage = 1, kStageDt = 2 };
 
+cudaError_t launch_prim(const DevParams& P, const double* uin, double* w, const StageDesc* d_desc,
+                        int ndesc, long long max_w, cudaStream_t s);
+
+// FP64 parity path (reference evaluation order, no contraction)
+cudaError_t launch_flux_exact(const DevParams& P, int dir, const double* w, void* f, void* bn,
+                              const StageDesc* d_desc, int ndesc, long long max_f,
+                              const StepState* state, cudaStream_t s);
+cudaError_t launch_update_exact(const DevParams& P, const StageBuffers& B,
+                                const StageDesc* d_desc, int ndesc, long long max_v, int flags,
+                                double dt_scale, StepState* state, DtPartial* partials,
+                                int* nblocks_v, cudaStream_t s);
+// fast physics: R = float (mixed precision) or double (fast FP64)
+template <typename R>
+cudaError_t launch_flux_fast(const DevParams& P, int dir, const double* w, void* f, void* bn,
+                             const StageDesc* d_desc, int ndesc, long long max_f,
+                             const StepState* state, cudaStream_t s);
+template <typename R>
+cudaError_t launch_update_fast(const DevParams& P, const StageBuffers& B, const StageDesc* d_desc,
+                               int ndesc, long long max_v, int flags, double dt_scale,
+                               StepState* state, DtPartial* partials, int* nblocks_v,
+                               cudaStream_t s);
+
+// Bytes of one face-flux value for a precision mode (MF_PREC_*).
+inline size_t flux_bytes(int precision) { return precision == MF_PREC_MIXED ? 4 : 8; }
+
 // Enqueue one stage (prim, fluxes in every direction, update) for ndesc
 // patches.  max_w / max_f[d] / max_v: largest region sizes over the descs.
-cudaError_t launch_stage_fp64(const DevParams& P, const StageBuffers& B, const StageDesc* d_desc,
-                              int ndesc, long long max_w, const long long max_f[3],
-                              long long max_v, int flags, double dt_scale, StepState* state,
-                              DtPartial* partials, int* nblocks_v, cudaStream_t s);
-cudaError_t launch_stage_mixed(const DevParams& P, const StageBuffers& B,
-                               const StageDesc* d_desc, int ndesc, long long max_w,
-                               const long long max_f[3], long long max_v, int flags,
-                               double dt_scale, StepState* state, DtPartial* partials,
-                               int* nblocks_v, cudaStream_t s);
-
-inline cudaError_t launch_stage(const DevParams& P, int mixed, const StageBuffers& B,
-                                const StageDesc* d_desc, int ndesc, long long max_w,
-                                const long long max_f[3], long long max_v, int flags,
-                                double dt_scale, StepState* state, DtPartial* partials,
-                                int* nblocks_v, cudaStream_t s) {
-  if (mixed)
-    return launch_stage_mixed(P, B, d_desc, ndesc, max_w, max_f, max_v, flags, dt_scale, state,
-                              partials, nblocks_v, s);
-  return launch_stage_fp64(P, B, d_desc, ndesc, max_w, max_f, max_v, flags, dt_scale, state,
-                           partials, nblocks_v, s);
-}
+// precision: MF_PREC_FP64 (parity), MF_PREC_FP64_FAST or MF_PREC_MIXED.
+cudaError_t launch_stage(const DevParams& P, int precision, const StageBuffers& B,
+                         const StageDesc* d_desc, int ndesc, long long max_w,
+                         const long long max_f[3], long long max_v, int flags,
+                         double dt_scale, StepState* state, DtPartial* partials,
+                         int* nblocks_v, cudaStream_t s);
 
 // dx / max wave speed over each desc's valueBox into per-block partials.
 cudaError_t launch_dt(const DevParams& P, const double* u, const StageDesc* d_desc, int ndesc,

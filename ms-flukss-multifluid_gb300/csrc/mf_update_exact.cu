@@ -1,0 +1,237 @@
+// mf_update_exact.cu - update kernel of the FP64 parity path, the stand-alone
+// dt kernel, the level dt finalisation, the device ghost exchange and the
+// face-flux output of the single-patch call.  Built with -fmad=false.
+#include <cfloat>
+#include <climits>
+
+#define MF_PHYS exact
+#include "mf_sources_exact.cuh"
+#include "mf_update_kernel.cuh"
+
+namespace mf {
+namespace {
+using namespace MF_PHYS;
+
+template <int GLM>
+__global__ void __launch_bounds__(kBlock)
+    k_dt(const DevParams P, const double* __restrict__ U, const StageDesc* __restrict__ descs,
+         DtPartial* __restrict__ partials) {
+  constexpr int IRHON = 8 + GLM;
+  const StageDesc& D = descs[blockIdx.y];
+  const int n = D.vn[0] * D.vn[1] * D.vn[2];
+  const int lin = blockIdx.x * blockDim.x + threadIdx.x;
+  double dtc = DBL_MAX;
+  int myidx = INT_MAX;
+  if (lin < n) {
+    int i, j, k;
+    decode(lin, D.vlo, D.vn, i, j, k);
+    const long long cs = (long long)D.fn[0] * D.fn[1] * D.fn[2];
+    const long long base = D.u_off + loc(D.flo, D.fn, i, j, k);
+    double u[MF_MAX_COMP];
+#pragma unroll
+    for (int q = 0; q < MF_MAX_COMP; ++q)
+      if (q < P.nc) u[q] = U[base + q * cs];
+    dtc = P.dx / max_wave_speed<IRHON>(P, u);
+    myidx = lin;
+  }
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    double od = __shfl_down_sync(0xffffffffu, dtc, off);
+    int oi = __shfl_down_sync(0xffffffffu, myidx, off);
+    if (dt_less(od, oi, dtc, myidx)) {
+      dtc = od;
+      myidx = oi;
+    }
+  }
+  __shared__ double sdt[kBlock / 32];
+  __shared__ int sidx[kBlock / 32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) {
+    sdt[wid] = dtc;
+    sidx[wid] = myidx;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double bd = sdt[0];
+    int bi = sidx[0];
+    for (int q = 1; q < kBlock / 32; ++q)
+      if (dt_less(sdt[q], sidx[q], bd, bi)) {
+        bd = sdt[q];
+        bi = sidx[q];
+      }
+    DtPartial pr;
+    pr.dt = bd;
+    pr.desc = blockIdx.y;
+    pr.idx = bi;
+    partials[(long long)blockIdx.y * gridDim.x + blockIdx.x] = pr;
+  }
+}
+
+__device__ __forceinline__ bool part_less(const DtPartial& a, const DtPartial& b) {
+  if (a.dt < b.dt) return true;
+  if (a.dt > b.dt) return false;
+  if (a.desc != b.desc) return a.desc < b.desc;
+  return a.idx < b.idx;
+}
+
+__global__ void __launch_bounds__(256)
+    k_finalize(const DevParams P, const DtPartial* __restrict__ parts, int np,
+               StepState* __restrict__ ss, int advance) {
+  DtPartial best;
+  best.dt = DBL_MAX;
+  best.desc = INT_MAX;
+  best.idx = INT_MAX;
+  for (int q = threadIdx.x; q < np; q += blockDim.x) {
+    DtPartial c = parts[q];
+    if (part_less(c, best)) best = c;
+  }
+  __shared__ DtPartial sb[256];
+  sb[threadIdx.x] = best;
+  __syncthreads();
+  for (int s = 128; s > 0; s >>= 1) {
+    if (threadIdx.x < s && part_less(sb[threadIdx.x + s], sb[threadIdx.x]))
+      sb[threadIdx.x] = sb[threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    best = sb[0];
+    ss->dt_min = best.dt;
+    ss->min_desc = best.desc;
+    ss->min_idx = best.idx;
+    if (!(best.dt > 0.0) || best.dt >= DBL_MAX) atomicOr(&ss->flags, kFlagBadDt);
+    if (advance) {
+      // AMRLevelIdealMHD::advance (srcIdeal/AMRLevelIdealMHD.cpp:1531-1548, 1588)
+      const double dtn = best.dt;
+      ss->dt = ss->cfl * dtn;
+      if (P.glm && P.factor_ch > 0.0) {
+        const double ch = P.factor_ch * P.dx / dtn;
+        ss->ch = ch;
+        ss->cp = sqrt(ch * P.dx / P.factor_cp);
+      }
+    }
+  }
+}
+
+__global__ void __launch_bounds__(256)
+    k_exchange(double* __restrict__ U, const CopyReg* __restrict__ regs, int nc) {
+  const CopyReg R = regs[blockIdx.x];
+  const int n = R.ext[0] * R.ext[1] * R.ext[2];
+  const long long scs = (long long)R.sfn[0] * R.sfn[1] * R.sfn[2];
+  const long long dcs = (long long)R.dfn[0] * R.dfn[1] * R.dfn[2];
+  const long long tot = (long long)n * nc;
+  for (long long t = threadIdx.x; t < tot; t += blockDim.x) {
+    const int q = (int)(t / n);
+    const int c = (int)(t - (long long)q * n);
+    const int a = c % R.ext[0];
+    const int r = c / R.ext[0];
+    const int b = r % R.ext[1];
+    const int e = r / R.ext[1];
+    const long long so = R.src_off + q * scs + (R.s0[0] + a) +
+                         (long long)R.sfn[0] * ((R.s0[1] + b) + (long long)R.sfn[1] * (R.s0[2] + e));
+    const long long dof = R.dst_off + q * dcs + (R.d0[0] + a) +
+                          (long long)R.dfn[0] * ((R.d0[1] + b) + (long long)R.dfn[1] * (R.d0[2] + e));
+    U[dof] = U[so];
+  }
+}
+
+template <typename R>
+__global__ void k_flux_out(int nc, const R* __restrict__ f2, int l20, int l21, int l22, int n20,
+                           int n21, int n22, const R* __restrict__ f1, int l10, int l11, int l12,
+                           int n10, int n11, int n12, double* __restrict__ out, int lo0, int lo1,
+                           int lo2, int on0, int on1, int on2) {
+  const long long n = (long long)on0 * on1 * on2;
+  const long long cs2 = (long long)n20 * n21 * n22, cs1 = (long long)n10 * n11 * n12;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n * nc;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int q = (int)(t / n);
+    const long long c = t - (long long)q * n;
+    const int a = (int)(c % on0);
+    const long long r = c / on0;
+    const int b = (int)(r % on1);
+    const int e = (int)(r / on1);
+    const int i = lo0 + a, j = lo1 + b, k = lo2 + e;
+    const long long i2 = q * cs2 + (i - l20) + (long long)n20 * ((j - l21) + (long long)n21 * (k - l22));
+    double v = (double)f2[i2];
+    if (f1) {
+      const long long i1 =
+          q * cs1 + (i - l10) + (long long)n10 * ((j - l11) + (long long)n11 * (k - l12));
+      v = v + (double)f1[i1];
+      v = v * 0.5;
+    }
+    out[t] = v;
+  }
+}
+
+}  // namespace
+
+cudaError_t launch_update_exact(const DevParams& P, const StageBuffers& B,
+                                const StageDesc* d_desc, int ndesc, long long max_v, int flags,
+                                double dt_scale, StepState* state, DtPartial* partials,
+                                int* nblocks_v, cudaStream_t s) {
+  const dim3 gv((unsigned)((max_v + kBlock - 1) / kBlock), (unsigned)ndesc);
+  if (nblocks_v) *nblocks_v = (int)(gv.x * gv.y);
+#define MF_UPD(G, FL) \
+  k_update<double, G, FL><<<gv, kBlock, 0, s>>>(P, B, d_desc, state, dt_scale, partials)
+  if (P.glm) {
+    if (flags == 0) MF_UPD(1, 0);
+    else if (flags == kStageDt) MF_UPD(1, kStageDt);
+    else MF_UPD(1, kStageAverage | kStageDt);
+  } else {
+    if (flags == 0) MF_UPD(0, 0);
+    else if (flags == kStageDt) MF_UPD(0, kStageDt);
+    else MF_UPD(0, kStageAverage | kStageDt);
+  }
+#undef MF_UPD
+  return cudaGetLastError();
+}
+
+cudaError_t launch_dt(const DevParams& P, const double* u, const StageDesc* d_desc, int ndesc,
+                      long long max_v, DtPartial* partials, int* nblocks, cudaStream_t s) {
+  const dim3 gv((unsigned)((max_v + kBlock - 1) / kBlock), (unsigned)ndesc);
+  if (nblocks) *nblocks = (int)(gv.x * gv.y);
+  if (P.glm)
+    k_dt<1><<<gv, kBlock, 0, s>>>(P, u, d_desc, partials);
+  else
+    k_dt<0><<<gv, kBlock, 0, s>>>(P, u, d_desc, partials);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_finalize(const DevParams& P, const DtPartial* partials, int npart,
+                            StepState* state, int advance, cudaStream_t s) {
+  k_finalize<<<1, 256, 0, s>>>(P, partials, npart, state, advance);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_exchange(double* u, const CopyReg* regs, int nreg, int nc, cudaStream_t s) {
+  if (nreg <= 0) return cudaSuccess;
+  k_exchange<<<nreg, 256, 0, s>>>(u, regs, nc);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_flux_out(int mixed, int sd, int nc, const void* const f2[3],
+                            const int f2lo[3][3], const int f2n[3][3], const void* const f1[3],
+                            const int f1lo[3][3], const int f1n[3][3], double* const fout[3],
+                            const int olo[3][3], const int on[3][3], cudaStream_t s) {
+  for (int d = 0; d < sd; ++d) {
+    long long n = (long long)on[d][0] * on[d][1] * on[d][2] * nc;
+    int blocks = (int)((n + 255) / 256);
+    if (blocks > 4096) blocks = 4096;
+    if (blocks < 1) blocks = 1;
+    if (mixed)
+      k_flux_out<float><<<blocks, 256, 0, s>>>(
+          nc, (const float*)f2[d], f2lo[d][0], f2lo[d][1], f2lo[d][2], f2n[d][0], f2n[d][1],
+          f2n[d][2], (const float*)f1[d], f1lo[d][0], f1lo[d][1], f1lo[d][2], f1n[d][0],
+          f1n[d][1], f1n[d][2], fout[d], olo[d][0], olo[d][1], olo[d][2], on[d][0], on[d][1],
+          on[d][2]);
+    else
+      k_flux_out<double><<<blocks, 256, 0, s>>>(
+          nc, (const double*)f2[d], f2lo[d][0], f2lo[d][1], f2lo[d][2], f2n[d][0], f2n[d][1],
+          f2n[d][2], (const double*)f1[d], f1lo[d][0], f1lo[d][1], f1lo[d][2], f1n[d][0],
+          f1n[d][1], f1n[d][2], fout[d], olo[d][0], olo[d][1], olo[d][2], on[d][0], on[d][1],
+          on[d][2]);
+  }
+  return cudaGetLastError();
+}
+
+
+}  // namespace mf

@@ -1,0 +1,158 @@
+// mf_update_kernel.cuh - the update kernel (flux divergence, sources,
+// positivity, RK2 averaging, per-cell dt).  Included by mf_update.cu (fast
+// physics) and mf_update_exact.cu (parity physics); MF_PHYS names the physics
+// namespace of the including unit.
+#pragma once
+
+#include "mf_kernels.cuh"
+
+namespace mf {
+namespace {
+using namespace MF_PHYS;
+
+__device__ __forceinline__ bool dt_less(double a, int ia, double b, int ib) {
+  return (a < b) || (a == b && ia < ib);
+}
+
+template <typename R, int GLM, int FLAGS>
+__global__ void __launch_bounds__(kBlock)
+    k_update(const DevParams P, const StageBuffers B, const StageDesc* __restrict__ descs,
+             StepState* __restrict__ ss, const double dt_scale, DtPartial* __restrict__ partials) {
+  constexpr int IRHON = 8 + GLM;
+  const StageDesc& D = descs[blockIdx.y];
+  const int n = D.vn[0] * D.vn[1] * D.vn[2];
+  const int lin = blockIdx.x * blockDim.x + threadIdx.x;
+  double dtc = DBL_MAX;
+  int myidx = INT_MAX;
+  if (lin < n) {
+    int i, j, k;
+    decode(lin, D.vlo, D.vn, i, j, k);
+    const long long cs = (long long)D.fn[0] * D.fn[1] * D.fn[2];
+    const long long base = D.u_off + loc(D.flo, D.fn, i, j, k);
+    const double dt = ss->dt * dt_scale;
+    double u[MF_MAX_COMP];
+#pragma unroll
+    for (int q = 0; q < MF_MAX_COMP; ++q)
+      if (q < P.nc) u[q] = B.uin[base + q * cs];
+
+    // UPDATECONS (src/PatchMHDAMF.ChF:542-587), one direction after another
+    const double dtinv = dt * P.invdx;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      if (d < P.sd) {
+        int fnb[3] = {D.vn[0], D.vn[1], D.vn[2]};
+        fnb[d] += 1;
+        const long long fcs = (long long)fnb[0] * fnb[1] * fnb[2];
+        const long long sf = (d == 0) ? 1 : (d == 1) ? (long long)fnb[0]
+                                                     : (long long)fnb[0] * fnb[1];
+        const R* __restrict__ Fd = (const R*)B.f[d] + D.f_off[d] + loc(D.vlo, fnb, i, j, k);
+#pragma unroll
+        for (int q = 0; q < MF_MAX_COMP; ++q)
+          if (q < P.nc)
+            u[q] = u[q] - dtinv * ((double)Fd[q * fcs + sf] - (double)Fd[q * fcs]);
+      }
+    }
+
+    // addExplicitSources (srcIdeal/PatchMHDMF.cpp:1149-1389) with the
+    // stage-start primitive state
+    double w[MF_MAX_COMP];
+    const bool need_w = P.use8 || (P.ce && P.nf >= 2);
+    if (need_w) {
+#pragma unroll
+      for (int q = 0; q < MF_MAX_COMP; ++q)
+        if (q < P.nc) w[q] = B.w[base + q * cs];
+    }
+    double divB = 0.0;
+    if (P.use8) {
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        if (d < P.sd) {
+          int fnb[3] = {D.vn[0], D.vn[1], D.vn[2]};
+          fnb[d] += 1;
+          const long long sf = (d == 0) ? 1 : (d == 1) ? (long long)fnb[0]
+                                                       : (long long)fnb[0] * fnb[1];
+          const R* __restrict__ Bd = (const R*)B.bn[d] + D.bn_off[d] + loc(D.vlo, fnb, i, j, k);
+          divB = divB + (double)Bd[sf] - (double)Bd[0];  // COMPUTEDIVB
+        }
+      }
+      // SOURCE8WAVES (srcIdeal/PatchIdealMHDF.ChF:681-722) + ADDSOURCES
+      const double dtbydx = dt / P.dx;
+      const double dB = -divB * dtbydx;
+      const double Ux = w[1], Uy = w[2], Uz = w[3];
+      const double Bx = kInv4Pi * w[5], By = kInv4Pi * w[6], Bz = kInv4Pi * w[7];
+      u[1] = u[1] + dB * Bx;
+      u[2] = u[2] + dB * By;
+      u[3] = u[3] + dB * Bz;
+      u[4] = u[4] + dB * (Bx * Ux + By * Uy + Bz * Uz);
+      u[5] = u[5] + dB * Ux;
+      u[6] = u[6] + dB * Uy;
+      u[7] = u[7] + dB * Uz;
+    }
+    if (GLM) {  // PSIPARABOLIC (src/DednerF.ChF:65-87)
+      const double ch = ss->ch, cp = ss->cp;
+      u[8] = exp(-dt * ch * ch / (cp * cp)) * u[8];
+    }
+    if (P.ce && P.nf >= 2) {
+      const int reg = region_cell(P, i, j, k, w);
+      charge_exchange_add<IRHON>(P, w, reg, dt, u);
+    }
+    if (P.reinit) reinit_cell(P, i, j, k, u);
+    positivity_cell<IRHON>(P, u);
+
+    if (FLAGS & kStageAverage) {  // AVERAGESTATE (src/PatchMHDAMF.ChF:289-316)
+#pragma unroll
+      for (int q = 0; q < MF_MAX_COMP; ++q)
+        if (q < P.nc) u[q] = u[q] + 0.5 * (B.uold[base + q * cs] - B.uin[base + q * cs]);
+    }
+    bool finite = true;
+#pragma unroll
+    for (int q = 0; q < MF_MAX_COMP; ++q)
+      if (q < P.nc) {
+        finite = finite && isfinite(u[q]);
+        B.uout[base + q * cs] = u[q];
+      }
+    if (!finite) atomicOr(&ss->flags, kFlagNonFinite);
+    if (FLAGS & kStageDt) {
+      dtc = P.dx / max_wave_speed<IRHON>(P, u);
+      myidx = lin;
+      if (B.divb && P.use8) B.divb[loc(B.divb_lo, B.divb_n, i, j, k)] = divB;
+    }
+  }
+  if (FLAGS & kStageDt) {
+    // block minimum of (dt, index): warp shuffles, then one warp
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      double od = __shfl_down_sync(0xffffffffu, dtc, off);
+      int oi = __shfl_down_sync(0xffffffffu, myidx, off);
+      if (dt_less(od, oi, dtc, myidx)) {
+        dtc = od;
+        myidx = oi;
+      }
+    }
+    __shared__ double sdt[kBlock / 32];
+    __shared__ int sidx[kBlock / 32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) {
+      sdt[wid] = dtc;
+      sidx[wid] = myidx;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double bd = sdt[0];
+      int bi = sidx[0];
+      for (int q = 1; q < kBlock / 32; ++q)
+        if (dt_less(sdt[q], sidx[q], bd, bi)) {
+          bd = sdt[q];
+          bi = sidx[q];
+        }
+      DtPartial pr;
+      pr.dt = bd;
+      pr.desc = blockIdx.y;
+      pr.idx = bi;
+      partials[(long long)blockIdx.y * gridDim.x + blockIdx.x] = pr;
+    }
+  }
+}
+
+}  // namespace
+}  // namespace mf

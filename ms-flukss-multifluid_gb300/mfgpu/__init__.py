@@ -29,7 +29,7 @@ MF_ERR_CUDA = 6
 MF_ERR_UNSUPPORTED = 7
 
 TA_FIRST_ORDER, TA_HANCOCK, TA_RK2 = 0, 1, 2
-PREC_FP64, PREC_MIXED = 0, 1
+PREC_FP64, PREC_MIXED, PREC_FP64_FAST = 0, 1, 2
 BC_NONE, BC_FARFIELD = 0, 1
 LIM_CD, LIM_MINMOD, LIM_SUPERBEE, LIM_VANALBADA, LIM_MC, LIM_HARMONIC, LIM_VANLEER = (
     0, 1, 2, 3, 4, 5, 9)
@@ -151,6 +151,9 @@ _SIGS = {
     "mf_level_result": (ctypes.c_int, [ctypes.c_void_p, _P(ctypes.c_double), _P(ctypes.c_int),
                                        c_int3, ctypes.c_void_p]),
     "mf_level_launches_per_step": (ctypes.c_int, [ctypes.c_void_p]),
+    "mf_level_profile_step": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double,
+                                             _P(ctypes.c_float), _P(ctypes.c_int),
+                                             _P(ctypes.c_int), ctypes.c_int]),
     "mf_init_orszag_host": (ctypes.c_int, [_P(MfParams), _P(MfFab), _P(MfBox)]),
     "mf_init_helio_host": (ctypes.c_int, [_P(MfParams), _P(ctypes.c_double), _P(ctypes.c_double),
                                           _P(MfFab), _P(MfBox)]),
@@ -536,3 +539,16 @@ class Level:
 
     def launches_per_step(self):
         return self.lib.mf_level_launches_per_step(self.h)
+
+    KIND_NAMES = {0: "exchange", 1: "prim", 2: "flux", 3: "update", 4: "finalize"}
+
+    def profile_step(self, dt):
+        """One step launch by launch with CUDA events between the launches;
+        returns [(kind_name, ms), ...] in launch order."""
+        n = self.launches_per_step() + 4
+        ms = (ctypes.c_float * n)()
+        kinds = (ctypes.c_int * n)()
+        cnt = ctypes.c_int()
+        check(self.lib.mf_level_profile_step(self.h, dt, ms, kinds, ctypes.byref(cnt), n),
+              "mf_level_profile_step")
+        return [(self.KIND_NAMES[kinds[i]], float(ms[i])) for i in range(cnt.value)]
