@@ -1,0 +1,316 @@
+"""Known-answer and invariant tests of the CPU restatement (the parity
+checker).  The reference ships no test vectors and cannot be built here, so
+these pin the restatement: flux consistency, upwinding, cons<->prim, uniform
+states, conservation, mirror symmetry, charge-exchange mass balance, region
+logic and the Sod problem against its exact solution."""
+import numpy as np
+import pytest
+
+import mfgpu
+from helpers import periodic_fill, valid_view
+
+pyoracle = pytest.importorskip("pyoracle")
+
+I4PI = 1.0 / (4.0 * np.pi)
+I8PI = 1.0 / (8.0 * np.pi)
+
+
+def _mhd_flux(w, d, gamma):
+    """Physical ideal-MHD flux (Gaussian units) of primitive state w in
+    direction d: rho,u,v,w,p,bx,by,bz."""
+    rho, u, p, b = w[0], np.array(w[1:4]), w[4], np.array(w[5:8])
+    un, bn = u[d], b[d]
+    pb = p + I8PI * b.dot(b)
+    e = p / (gamma - 1.0) + 0.5 * rho * u.dot(u) + I8PI * b.dot(b)
+    f = np.zeros(8)
+    f[0] = rho * un
+    f[1:4] = rho * un * u - bn * b * I4PI
+    f[1 + d] += pb
+    f[4] = un * (e + pb) - bn * u.dot(b) * I4PI
+    f[5:8] = un * b - bn * u
+    return f
+
+
+def _euler_flux(w, d, gamma):
+    rho, u, p = w[0], np.array(w[1:4]), w[4]
+    e = p / (gamma - 1.0) + 0.5 * rho * u.dot(u)
+    f = np.zeros(5)
+    f[0] = rho * u[d]
+    f[1:4] = rho * u[d] * u
+    f[1 + d] += p
+    f[4] = u[d] * (e + p)
+    return f
+
+
+def _rand_state(rng, nc, glm, nf):
+    w = np.zeros(nc)
+    w[0] = rng.uniform(0.2, 2.0)
+    w[1:4] = rng.uniform(-1.5, 1.5, 3)
+    w[4] = rng.uniform(0.1, 2.0)
+    w[5:8] = rng.uniform(-1.0, 1.0, 3)
+    if glm:
+        w[8] = rng.uniform(-0.1, 0.1)
+    s = 8 + glm
+    for _ in range(nf - 1):
+        w[s] = rng.uniform(0.05, 1.0)
+        w[s + 1:s + 4] = rng.uniform(-1.5, 1.5, 3)
+        w[s + 4] = rng.uniform(0.01, 1.0)
+        s += 5
+    return w
+
+
+SOLVERS = [(1, 0), (3, 0), (2, 0), (4, 0), (11, 0), (13, 0), (1, 5), (3, 5)]
+
+
+@pytest.mark.parametrize("flux,cleaning", SOLVERS)
+def test_flux_consistency(oracle, flux, cleaning):
+    """F(W, W) equals the physical flux for every solver and direction."""
+    rng = np.random.default_rng(7 + flux + cleaning)
+    p = mfgpu.helio_params(16) if cleaning == 5 else mfgpu.orszag_params(16)
+    if cleaning != 5:
+        p.n_fluids = 3
+    p.space_dim = 3
+    for d in range(3):
+        p.domain_lo[d], p.domain_hi[d] = 0, 15
+    p.flux, p.divb_cleaning = flux, cleaning
+    p.use_8wave = 0 if cleaning == 5 else 1
+    p.dedner_ch = 2.5
+    nc = mfgpu.num_cons(p)
+    glm = 1 if cleaning == 5 else 0
+    for _ in range(20):
+        w = _rand_state(rng, nc, glm, p.n_fluids)
+        for d in range(3):
+            f = oracle.face_flux(p, d, w, w)
+            ref = _mhd_flux(w[:8], d, p.gamma)
+            if glm:
+                ref[5 + d] = w[8]                     # Dedner: psi
+                assert f[8] == pytest.approx(2.5 ** 2 * w[5 + d], rel=1e-14)
+            elif flux in (11, 13):
+                ref[5 + d] = 0.0                      # Roe 7-wave: no normal-B flux
+            np.testing.assert_allclose(f[:8], ref, rtol=1e-12, atol=1e-12)
+            s = 8 + glm
+            for _k in range(p.n_fluids - 1):
+                np.testing.assert_allclose(f[s:s + 5], _euler_flux(w[s:s + 5], d, p.gamma),
+                                           rtol=1e-12, atol=1e-13)
+                s += 5
+
+
+def test_vanleer_supersonic_upwind(oracle):
+    """Van Leer splitting returns the upwind flux exactly for supersonic flow."""
+    p = mfgpu.helio_params(16)
+    nc = mfgpu.num_cons(p)
+    rng = np.random.default_rng(3)
+    for _ in range(20):
+        wl = _rand_state(rng, nc, 1, 4)
+        wr = _rand_state(rng, nc, 1, 4)
+        for d in range(3):
+            for s in (9, 14, 19):
+                for w in (wl, wr):
+                    a = np.sqrt(p.gamma * w[s + 4] / w[s])
+                    w[s + 1 + d] = 2.0 * a + 0.1        # supersonic to +x_d
+            f = oracle.face_flux(p, d, wl, wr)
+            for s in (9, 14, 19):
+                np.testing.assert_allclose(f[s:s + 5], _euler_flux(wl[s:s + 5], d, p.gamma),
+                                           rtol=1e-13, atol=1e-14)
+
+
+def test_cons_to_prim_roundtrip(oracle):
+    p = mfgpu.helio_params(16)
+    nc = mfgpu.num_cons(p)
+    rng = np.random.default_rng(11)
+    g = p.gamma
+    for _ in range(50):
+        w = _rand_state(rng, nc, 1, 4)
+        u = np.zeros(nc)
+        u[0] = w[0]
+        u[1:4] = w[0] * w[1:4]
+        u[4] = w[4] / (g - 1) + 0.5 * w[0] * w[1:4].dot(w[1:4]) + I8PI * w[5:8].dot(w[5:8])
+        u[5:9] = w[5:9]
+        for s in (9, 14, 19):
+            u[s] = w[s]
+            u[s + 1:s + 4] = w[s] * w[s + 1:s + 4]
+            u[s + 4] = w[s + 4] / (g - 1) + 0.5 * w[s] * w[s + 1:s + 4].dot(w[s + 1:s + 4])
+        np.testing.assert_allclose(oracle.cons_to_prim(p, u), w, rtol=1e-12, atol=1e-14)
+
+
+def _uniform_patch(p, n, ng, w):
+    sd = p.space_dim
+    lo, hi = mfgpu.grow([0, 0, 0], [n - 1, n - 1, n - 1 if sd == 3 else 0], ng, sd)
+    nc = mfgpu.num_cons(p)
+    U = np.zeros(mfgpu.fab_shape(lo, hi, nc))
+    g = p.gamma
+    U[0] = w[0]
+    U[1:4] = (w[0] * np.array(w[1:4]))[:, None, None, None]
+    U[4] = w[4] / (g - 1) + 0.5 * w[0] * np.dot(w[1:4], w[1:4]) + I8PI * np.dot(w[5:8], w[5:8])
+    U[5:8] = np.array(w[5:8])[:, None, None, None]
+    return U, lo, hi
+
+
+@pytest.mark.parametrize("ta", [mfgpu.TA_FIRST_ORDER, mfgpu.TA_RK2])
+def test_uniform_state_is_invariant(oracle, ta):
+    n = 12
+    p = mfgpu.orszag_params(n, ta)
+    ng = mfgpu.num_ghost(p)
+    U, lo, hi = _uniform_patch(p, n, ng, [1.3, 0.4, -0.2, 0.1, 0.7, 0.3, -0.5, 0.2])
+    U0 = U.copy()
+    st, dt, _ = oracle.patch_update(p, U, lo, hi, [0, 0, 0], [n - 1, n - 1, 0], 1e-3)
+    assert st == 0 and dt > 0
+    assert np.array_equal(valid_view(U, ng, 2), valid_view(U0, ng, 2))
+
+
+@pytest.mark.parametrize("ta", [mfgpu.TA_FIRST_ORDER, mfgpu.TA_RK2])
+def test_periodic_conservation(oracle, ta):
+    """Without the 8-wave source every conserved sum is unchanged on a periodic
+    box (the flux differences telescope)."""
+    n = 32
+    p = mfgpu.orszag_params(n, ta)
+    p.use_8wave = 0
+    ng = mfgpu.num_ghost(p)
+    lo, hi = mfgpu.grow([0, 0, 0], [n - 1, n - 1, 0], ng, 2)
+    U = periodic_fill(mfgpu.init_host_fab(p, lo, hi, "orszag"), ng, 2)
+    s0 = valid_view(U, ng, 2).sum(axis=(1, 2, 3))
+    scale = np.abs(valid_view(U, ng, 2)).sum(axis=(1, 2, 3)) + 1.0
+    st, dt, _ = oracle.compute_dt(p, U, lo, hi, [0, 0, 0], [n - 1, n - 1, 0])
+    for _ in range(3):
+        st, ndt, _ = oracle.patch_update(p, U, lo, hi, [0, 0, 0], [n - 1, n - 1, 0], 0.4 * dt)
+        U = periodic_fill(U, ng, 2)
+        dt = ndt
+    s1 = valid_view(U, ng, 2).sum(axis=(1, 2, 3))
+    assert np.all(np.abs(s1 - s0) <= 1e-13 * scale), (s1 - s0) / scale
+
+
+def test_mirror_symmetry(oracle):
+    """A 1D problem symmetric about the box centre stays symmetric."""
+    n = 64
+    p = mfgpu.orszag_params(n)
+    ng = mfgpu.num_ghost(p)
+    lo, hi = mfgpu.grow([0, 0, 0], [n - 1, 3, 0], ng, 2)
+    p.domain_hi[1] = 3
+    nc = mfgpu.num_cons(p)
+    x = (np.arange(lo[0], hi[0] + 1) + 0.5) / n
+    rho = 1.0 + 0.5 * np.exp(-((x - 0.5) / 0.1) ** 2)
+    pr = 0.6 + 0.3 * np.exp(-((x - 0.5) / 0.15) ** 2)
+    by = 0.3
+    U = np.zeros(mfgpu.fab_shape(lo, hi, nc))
+    U[0] = rho[None, None, :]
+    U[4] = (pr / (p.gamma - 1) + I8PI * by * by)[None, None, :]
+    U[6] = by
+    U = periodic_fill(U, ng, 2)
+    st, _, _ = oracle.patch_update(p, U, lo, hi, [0, 0, 0], [n - 1, 3, 0], 2e-3)
+    assert st == 0
+    v = valid_view(U, ng, 2)
+    np.testing.assert_allclose(v[0], v[0][:, :, ::-1], rtol=1e-13)
+    np.testing.assert_allclose(v[4], v[4][:, :, ::-1], rtol=1e-13)
+    np.testing.assert_allclose(v[1], -v[1][:, :, ::-1], atol=1e-13)
+
+
+@pytest.mark.parametrize("reg", [1, 2, 3, 4])
+def test_charge_exchange_mass_balance(oracle, reg):
+    """Plasma density is untouched; the neutral populations exchange mass
+    without loss whenever the region has a recipient population."""
+    p = mfgpu.helio_params(16)
+    nc = mfgpu.num_cons(p)
+    rng = np.random.default_rng(reg)
+    for _ in range(20):
+        w = _rand_state(rng, nc, 1, 4)
+        s = oracle.charge_exchange(p, w, reg, 0.01)
+        assert s[0] == 0.0
+        assert np.all(s[5:9] == 0.0)
+        dens = s[[9, 14, 19]]
+        assert abs(dens.sum()) <= 1e-14 * np.abs(dens).sum()
+
+
+def test_regions(oracle):
+    """DEFINE_REGIONS_2F: supersonic radial wind -> 3, hot shocked wind -> 2,
+    interstellar medium -> 1."""
+    p = mfgpu.helio_params(64)
+    nc = mfgpu.num_cons(p)
+    w = np.zeros(nc)
+    i, j, k = 50, 32, 32   # x = (i+0.5)dx - 1 > 0, on the +x axis
+    w[0], w[4] = 1.0, 1.0
+    w[1] = 8.0             # radial speed > 0.6 sunV, cool
+    assert oracle.region(p, i, j, k, w) == 3
+    w[4] = 200.0           # TEMP = 1e4 * 200 >= 1e6, r > sunR
+    assert oracle.region(p, i, j, k, w) == 2
+    w[1] = 1.0             # slow and hot (TEMP >= TMLIM)
+    assert oracle.region(p, i, j, k, w) == 2
+    w[4] = 1.0             # slow and cool
+    assert oracle.region(p, i, j, k, w) == 1
+
+
+def _sod_exact(x, t, g=1.4, wl=(1.0, 0.0, 1.0), wr=(0.125, 0.0, 0.1), x0=0.5):
+    """Exact Riemann solution (Toro, ch. 4) of the Sod problem."""
+    rl, ul, pl = wl
+    rr, ur, pr = wr
+    cl, cr = np.sqrt(g * pl / rl), np.sqrt(g * pr / rr)
+
+    def fk(pp, rk, pk, ck):
+        if pp > pk:
+            a, b = 2.0 / ((g + 1) * rk), (g - 1) / (g + 1) * pk
+            return (pp - pk) * np.sqrt(a / (pp + b))
+        return 2 * ck / (g - 1) * ((pp / pk) ** ((g - 1) / (2 * g)) - 1)
+
+    lo_, hi_ = 1e-8, 10.0
+    for _ in range(200):
+        mid = 0.5 * (lo_ + hi_)
+        if fk(mid, rl, pl, cl) + fk(mid, rr, pr, cr) + (ur - ul) > 0:
+            hi_ = mid
+        else:
+            lo_ = mid
+    ps = 0.5 * (lo_ + hi_)
+    us = 0.5 * (ul + ur) + 0.5 * (fk(ps, rr, pr, cr) - fk(ps, rl, pl, cl))
+    rsl = rl * (ps / pl) ** (1 / g)
+    csl = cl * (ps / pl) ** ((g - 1) / (2 * g))
+    rsr = rr * ((ps / pr + (g - 1) / (g + 1)) / ((g - 1) / (g + 1) * ps / pr + 1))
+    sshock = ur + cr * np.sqrt((g + 1) / (2 * g) * ps / pr + (g - 1) / (2 * g))
+    rho = np.empty_like(x)
+    for q, xx in enumerate(x):
+        s = (xx - x0) / t
+        if s < ul - cl:
+            rho[q] = rl
+        elif s < us - csl:
+            c = 2 / (g + 1) * (cl + (g - 1) / 2 * (ul - s))
+            rho[q] = rl * (c / cl) ** (2 / (g - 1))
+        elif s < us:
+            rho[q] = rsl
+        elif s < sshock:
+            rho[q] = rsr
+        else:
+            rho[q] = rr
+    return rho
+
+
+def test_sod_against_exact_solution(oracle):
+    """B = 0 reduces the MHD solver to the Euler equations: the Sod problem
+    converges to its exact solution."""
+    n = 400
+    p = mfgpu.orszag_params(n)
+    p.gamma = 1.4
+    p.smallr, p.smallp = 1e-10, 1e-10
+    p.domain_hi[1] = 3
+    ng = mfgpu.num_ghost(p)
+    lo, hi = mfgpu.grow([0, 0, 0], [n - 1, 3, 0], ng, 2)
+    nc = mfgpu.num_cons(p)
+    x = (np.arange(lo[0], hi[0] + 1) + 0.5) / n
+    rho = np.where(x < 0.5, 1.0, 0.125)
+    pr = np.where(x < 0.5, 1.0, 0.1)
+    U = np.zeros(mfgpu.fab_shape(lo, hi, nc))
+    U[0] = rho[None, None, :]
+    U[4] = (pr / 0.4)[None, None, :]
+    # periodic in x: the far edges of the box carry a second (mirrored) jump,
+    # whose waves stay outside the compared window (0.2, 0.78) until t = 0.1
+    U = periodic_fill(U, ng, 2)
+    t, tend = 0.0, 0.1
+    st, dt, _ = oracle.compute_dt(p, U, lo, hi, [0, 0, 0], [n - 1, 3, 0])
+    while t < tend - 1e-12:
+        step = min(0.4 * dt, tend - t)
+        st, dt, _ = oracle.patch_update(p, U, lo, hi, [0, 0, 0], [n - 1, 3, 0], step)
+        assert st == 0
+        U = periodic_fill(U, ng, 2)
+        t += step
+    xs = (np.arange(n) + 0.5) / n
+    num = valid_view(U, ng, 2)[0, 0, 0, :]
+    ref = _sod_exact(xs, tend)
+    sel = (xs > 0.2) & (xs < 0.78)
+    l1 = np.mean(np.abs(num[sel] - ref[sel]))
+    assert l1 < 6e-3, l1
