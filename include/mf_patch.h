@@ -49,7 +49,9 @@ typedef enum mf_status {
   MF_ERR_NEG_STATE = 4,    /* density or pressure <= 0 after the positivity fix, or dt <= 0 */
   MF_ERR_TIMEOUT = 5,      /* a bounded wait on the device gave up */
   MF_ERR_CUDA = 6,         /* a CUDA runtime call failed */
-  MF_ERR_UNSUPPORTED = 7   /* option combination not implemented */
+  MF_ERR_UNSUPPORTED = 7,  /* option combination not implemented */
+  MF_ERR_SCRATCH_LIMIT = 8 /* mf_patch_update_noalloc: the patch needs more scratch than
+                              MF_NOALLOC_SCRATCH_BYTES */
 } mf_status;
 
 /* time_approximation (PatchMHDAM::eTimeApproximation) */
@@ -172,6 +174,28 @@ mf_status mf_set_wait_timeout(mf_ctx* ctx, double seconds);
 mf_status mf_patch_update(mf_ctx* ctx, mf_fab* U, const mf_box* valid, double dt,
                           mf_fab* F, mf_fab* divB, double* new_dt, int min_cell[3],
                           void* stream);
+
+/* Size of the device scratch array of mf_patch_update_noalloc: 16 MiB, enough
+   for a 16^3 patch of the 24-component multi-fluid model with 4 ghost layers
+   (about 12.7 MiB) or a 2D single-fluid patch of about 200^2 cells. */
+#define MF_NOALLOC_SCRATCH_BYTES (16u << 20)
+
+/* mf_patch_update for callers that cannot allocate device memory: code that
+   runs inside another framework's stream capture (where cudaMalloc is not
+   allowed), processes whose device memory belongs to a pool allocator that
+   must not be bypassed, and loops that forbid allocation after start-up.
+   Same arguments, kernels and results as mf_patch_update; it calls no
+   cudaMalloc, cudaFree or other allocating routine.  Its scratch is one
+   file-scope device array of MF_NOALLOC_SCRATCH_BYTES that every GPU loading
+   the library holds until the process exits; a patch that needs more returns
+   MF_ERR_SCRATCH_LIMIT.  The first call on a device looks the array's device
+   address up (cudaGetSymbolAddress) and should come before any stream
+   capture.  All calls share the array and it keeps the last call's contents;
+   calls that overlap on the GPU race and must be serialised by the caller.
+   No counterpart in the reference (its patch update allocates per call). */
+mf_status mf_patch_update_noalloc(mf_ctx* ctx, mf_fab* U, const mf_box* valid, double dt,
+                                  mf_fab* F, mf_fab* divB, double* new_dt, int min_cell[3],
+                                  void* stream);
 
 /* dx / max wave speed minimum over `box` (PatchMHDMF::computeDt). */
 mf_status mf_compute_dt(mf_ctx* ctx, const mf_fab* U, const mf_box* box, double* dt,

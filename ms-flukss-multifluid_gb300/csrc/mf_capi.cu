@@ -16,6 +16,7 @@
 #include <thread>
 #include <vector>
 
+#include "mf_internal.h"
 #include "mf_kernels.cuh"
 #include "mf_sources_exact.cuh"
 
@@ -370,6 +371,7 @@ const char* mf_status_string(mf_status s) {
     case MF_ERR_TIMEOUT: return "device wait timed out";
     case MF_ERR_CUDA: return "CUDA error";
     case MF_ERR_UNSUPPORTED: return "unsupported option";
+    case MF_ERR_SCRATCH_LIMIT: return "patch exceeds the static scratch of the no-allocation update";
   }
   return "unknown status";
 }
@@ -1236,3 +1238,15 @@ mf_status mf_init_helio_host(const mf_params* p, const double* wp, const double*
 }
 
 }  // extern "C"
+
+// Read-only view of a context for the other translation units of the library.
+namespace mf {
+CtxView ctx_view(const mf_ctx* c) {
+  CtxView v;
+  v.p = &c->p;
+  v.dp = &c->dp;
+  v.ng = c->ng;
+  v.nc = c->nc;
+  return v;
+}
+}  // namespace mf

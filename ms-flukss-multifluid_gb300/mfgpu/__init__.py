@@ -27,6 +27,8 @@ MF_ERR_NEG_STATE = 4
 MF_ERR_TIMEOUT = 5
 MF_ERR_CUDA = 6
 MF_ERR_UNSUPPORTED = 7
+MF_ERR_SCRATCH_LIMIT = 8
+NOALLOC_SCRATCH_BYTES = 16 << 20
 
 TA_FIRST_ORDER, TA_HANCOCK, TA_RK2 = 0, 1, 2
 PREC_FP64, PREC_MIXED, PREC_FP64_FAST = 0, 1, 2
@@ -129,6 +131,9 @@ _SIGS = {
     "mf_patch_update": (ctypes.c_int, [ctypes.c_void_p, _P(MfFab), _P(MfBox), ctypes.c_double,
                                        ctypes.c_void_p, ctypes.c_void_p,
                                        _P(ctypes.c_double), c_int3, ctypes.c_void_p]),
+    "mf_patch_update_noalloc": (ctypes.c_int, [ctypes.c_void_p, _P(MfFab), _P(MfBox),
+                                               ctypes.c_double, ctypes.c_void_p, ctypes.c_void_p,
+                                               _P(ctypes.c_double), c_int3, ctypes.c_void_p]),
     "mf_compute_dt": (ctypes.c_int, [ctypes.c_void_p, _P(MfFab), _P(MfBox),
                                      _P(ctypes.c_double), c_int3, ctypes.c_void_p]),
     "mf_level_create": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _P(MfBox),
