@@ -181,25 +181,26 @@ __device__ __forceinline__ void roe_mhd(const DevParams& P, const R* wl, const R
   R so15 = -R(1) / cc;
   R so33 = -hzz * sq2, so34 = hyy * sq2;
   R so37 = R(0.5) * hzz * sih / sq2PiRho, so38 = -R(0.5) * hyy * sih / sq2PiRho;
-  R so47 = -R(0.5) * hzz * sih / sq2PiRho, so48 = R(0.5) * hyy * sih / sq2PiRho;
+  // (-a)/b == -(a/b) exactly: the mirrored coefficients are negations
+  R so47 = -so37, so48 = -so38;
   R so52 = R(0.5) * alf * af / cc;
   R so53 = -R(0.5) * als * as * hyy * sih / cc;
   R so54 = -R(0.5) * als * as * hzz * sih / cc;
   R so55 = R(0.5) * alf / (cc * Rho);
   R so57 = R(0.25) * als * hyy / (c * sqPiRho);
   R so58 = R(0.25) * als * hzz / (c * sqPiRho);
-  R so62 = -R(0.5) * alf * af / cc;
-  R so63 = R(0.5) * als * as * hyy * sih / cc;
-  R so64 = R(0.5) * als * as * hzz * sih / cc;
+  R so62 = -so52;
+  R so63 = -so53;
+  R so64 = -so54;
   R so72 = R(0.5) * als * as / cc;
   R so73 = R(0.5) * alf * af * hyy * sih / cc;
   R so74 = R(0.5) * alf * af * hzz * sih / cc;
   R so75 = R(0.5) * als / (Rho * cc);
   R so77 = -R(0.25) * alf * hyy / (c * sqPiRho);
   R so78 = -R(0.25) * alf * hzz / (c * sqPiRho);
-  R so82 = -R(0.5) * als * as / cc;
-  R so83 = -R(0.5) * alf * af * hyy * sih / cc;
-  R so84 = -R(0.5) * alf * af * hzz * sih / cc;
+  R so82 = -so72;
+  R so83 = -so73;
+  R so84 = -so74;
 
   R lu1 = A1 * (du1 + so15 * du5);
   R lu2 = A2 * du6;

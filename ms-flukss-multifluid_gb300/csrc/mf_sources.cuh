@@ -80,17 +80,21 @@ __device__ __forceinline__ void charge_exchange_add(const DevParams& P, const do
     const double VPHH = dx_ * uxN + dy_ * uyN + dz_ * uzN;
     const double VPHP = dx_ * ux + dy_ * uy + dz_ * uz;
     const double VVTH = 2.0 * wn[4] / rhoN;
-    const double UD = sqrt((4.0 * kInvPi) * (VVTP + VVTH) + DU2);
-    const double UPM = sqrt((16.0 * kInvPi) * VVTP + (2.25 * kPi) * VVTH + 4.0 * DU2);
+    // thermal + relative speeds; every argument is > 0, so sqrt(a) = a*rsqrt(a)
+    const double aUD = (4.0 * kInvPi) * (VVTP + VVTH) + DU2;
+    const double UD = aUD * rsqrt(aUD);
+    const double iUPM = rsqrt((16.0 * kInvPi) * VVTP + (2.25 * kPi) * VVTH + 4.0 * DU2);
     const double iUHM = rsqrt((2.25 * kPi) * VVTP + (16.0 * kInvPi) * VVTH + 4.0 * DU2);
-    const double UPE = sqrt(kInvPi * (4.0 * VVTP + (64.0 / 9.0) * VVTH) + DU2);
-    const double UHE = sqrt(kInvPi * ((64.0 / 9.0) * VVTP + 4.0 * VVTH) + DU2);
+    const double aPE = kInvPi * (4.0 * VVTP + (64.0 / 9.0) * VVTH) + DU2;
+    const double UPE = aPE * rsqrt(aPE);
+    const double aHE = kInvPi * ((64.0 / 9.0) * VVTP + 4.0 * VVTH) + DU2;
+    const double UHE = aHE * rsqrt(aHE);
     const double UDS = P.ce_scale_vel * UD;
     const double t = P.ce_a - P.ce_b * log(UDS);
     double SIG = t * t;
     if (P.ce_damp_c > 0.0) SIG = SIG * pow(1.0 - exp(-P.ce_damp_c / UDS), P.ce_damp_pow);
     const double ARR = P.ce_sigma_scale * SIG * rhoN * rho;
-    const double VVTHU = VVTH / UPM;
+    const double VVTHU = VVTH * iUPM;
     const double VP_UHM = VVTP * iUHM;
     const double hv = ARR * (UD + VVTHU + VP_UHM);
     h2 = h2 + hv * dx_;

@@ -10,6 +10,13 @@ namespace mf {
 namespace {
 using namespace MF_PHYS;
 
+// Difference of the fluxes on the two faces of a cell.  FP64 fluxes: in
+// FP64.  FP32 fluxes (mixed precision): in FP32, whose rounding is below the
+// FP32 error the fluxes already carry; the accumulation into the state stays
+// FP64.
+__device__ __forceinline__ double flux_diff(double hi, double lo) { return hi - lo; }
+__device__ __forceinline__ double flux_diff(float hi, float lo) { return (double)(hi - lo); }
+
 __device__ __forceinline__ bool dt_less(double a, int ia, double b, int ib) {
   return (a < b) || (a == b && ia < ib);
 }
@@ -49,7 +56,7 @@ __global__ void __launch_bounds__(kBlock)
 #pragma unroll
         for (int q = 0; q < MF_MAX_COMP; ++q)
           if (q < P.nc)
-            u[q] = u[q] - dtinv * ((double)Fd[q * fcs + sf] - (double)Fd[q * fcs]);
+            u[q] = u[q] - dtinv * flux_diff(Fd[q * fcs + sf], Fd[q * fcs]);
       }
     }
 
