@@ -243,6 +243,15 @@ int mf_level_launches_per_step(const mf_level* lev);
 mf_status mf_level_profile_step(mf_level* lev, double dt, float* ms, int* kinds, int* nlaunch,
                                 int max_launch);
 
+/* Autotuner (no reference counterpart: the reference runs one Fortran call
+   per patch).  Times the prim, flux and update kernels of the level's batch
+   at 64, 128 and 256 threads per block (reps launches each, stage-1 form, so
+   the level's state is not changed) and keeps the fastest shape of each
+   kind for later steps; previously captured step graphs are rebuilt.
+   threads (nullable) receives the chosen {prim, flux, update} shapes.
+   Results of a step do not depend on the shapes. */
+mf_status mf_level_autotune(mf_level* lev, int reps, int threads[3]);
+
 /* Problem set-up on host fabs (PhysProblem::initialize):
    Orszag-Tang vortex (problems/OrszagF.ChF:27-79) and the synthetic
    heliosphere (uniform inflow + inner solar-wind sphere). */

@@ -14,6 +14,7 @@
 #include <cstring>
 #include <new>
 #include <thread>
+#include <array>
 #include <vector>
 
 #include "mf_internal.h"
@@ -307,7 +308,10 @@ struct mf_level {
   long long cells = 0;
   DevBuf U, U1, W, F[3], Bn[3], desc, exfull, extwo, partials, state, state2;
   int nfull = 0, ntwo = 0;
-  long long max_w = 0, max_f[3] = {0, 0, 0}, max_v = 0;
+  // b1: RK2 stage 1 (valid boxes grown on uncovered sides); b2: the stage
+  // on the valid boxes (RK2 stage 2, first order).  Descs at desc.p: b1's
+  // np entries, then b2's.
+  mf::Batch b1, b2;
   int nparts = 0;
   PinnedBuf hstate;
   cudaStream_t s = nullptr;
@@ -462,6 +466,17 @@ static void fill_desc(StageDesc& D, const mf_box& fab, const mf_box& vbox, const
   }
 }
 
+// A batch of one patch: g0 = 0 in the host desc, device desc at dd.  The
+// fab-size check of check_fab keeps every count inside a 32-bit index.
+static mf::Batch single_batch(StageDesc& hd, const StageDesc* dd, int sd) {
+  mf::Batch b;
+  std::memset(&b, 0, sizeof(b));
+  mf::batch_offsets(&hd, 1, sd, b);
+  b.desc = dd;
+  mf::batch_default_threads(b);
+  return b;
+}
+
 mf_status mf_patch_update(mf_ctx* c, mf_fab* U, const mf_box* valid, double dt, mf_fab* F,
                           mf_fab* divB, double* new_dt, int min_cell[3], void* stream) {
   if (!c) return MF_ERR_BAD_ARG;
@@ -508,22 +523,18 @@ mf_status mf_patch_update(mf_ctx* c, mf_fab* U, const mf_box* valid, double dt, 
   StageDesc* hd = (StageDesc*)c->hdesc.p;
   fill_desc(hd[0], U->box, v1, w1);
   fill_desc(hd[1], U->box, v2, w2);
+  StageDesc* dd = (StageDesc*)c->desc.p;
+  mf::Batch b1 = single_batch(hd[0], dd, sd), b2 = single_batch(hd[1], dd + 1, sd);
   StepState* hs = (StepState*)c->hstate.p;
   std::memset(hs, 0, sizeof(*hs));
   hs->dt = dt;
   hs->ch = p.dedner_ch;
   hs->cp = p.dedner_cp;
   hs->cfl = 0.0;
-  StageDesc* dd = (StageDesc*)c->desc.p;
   StepState* ds = (StepState*)c->state.p;
   MF_CHECK_CUDA(cudaMemcpyAsync(dd, hd, sizeof(StageDesc) * 2, cudaMemcpyHostToDevice, s));
   MF_CHECK_CUDA(cudaMemcpyAsync(ds, hs, sizeof(StepState), cudaMemcpyHostToDevice, s));
 
-  long long mf1[3] = {0, 0, 0}, mf2[3] = {0, 0, 0};
-  for (int d = 0; d < sd; ++d) {
-    mf1[d] = box_cells(box_nodes(v1, d));
-    mf2[d] = box_cells(box_nodes(v2, d));
-  }
   int nb = 0;
   DtPartial* parts = (DtPartial*)c->partials.p;
   StageBuffers B;
@@ -538,8 +549,7 @@ mf_status mf_patch_update(mf_ctx* c, mf_fab* U, const mf_box* valid, double dt, 
       B.f[d] = c->f1[d].p;
       B.bn[d] = c->bn1[d].p;
     }
-    MF_CHECK_CUDA(mf::launch_stage(c->dp, p.precision,B, dd, 1, box_cells(w1), mf1, box_cells(v1), 0,
-                                   1.0, ds, parts, &nb, s));
+    MF_CHECK_CUDA(mf::launch_stage(c->dp, p.precision, B, b1, 0, 1.0, ds, parts, &nb, s));
     B.uin = (double*)c->pred.p;
     B.uout = U->data;
     B.uold = U->data;
@@ -554,8 +564,8 @@ mf_status mf_patch_update(mf_ctx* c, mf_fab* U, const mf_box* valid, double dt, 
         B.divb_n[d] = divB->box.hi[d] - divB->box.lo[d] + 1;
       }
     }
-    MF_CHECK_CUDA(mf::launch_stage(c->dp, p.precision,B, dd + 1, 1, box_cells(w2), mf2, box_cells(v2),
-                                   mf::kStageAverage | mf::kStageDt, 0.5, ds, parts, &nb, s));
+    MF_CHECK_CUDA(mf::launch_stage(c->dp, p.precision, B, b2, mf::kStageAverage | mf::kStageDt,
+                                   0.5, ds, parts, &nb, s));
   } else {
     B.uin = U->data;
     B.uout = U->data;
@@ -570,8 +580,8 @@ mf_status mf_patch_update(mf_ctx* c, mf_fab* U, const mf_box* valid, double dt, 
         B.divb_n[d] = divB->box.hi[d] - divB->box.lo[d] + 1;
       }
     }
-    MF_CHECK_CUDA(mf::launch_stage(c->dp, p.precision,B, dd + 1, 1, box_cells(w2), mf2, box_cells(v2),
-                                   mf::kStageDt, 1.0, ds, parts, &nb, s));
+    MF_CHECK_CUDA(
+        mf::launch_stage(c->dp, p.precision, B, b2, mf::kStageDt, 1.0, ds, parts, &nb, s));
   }
   MF_CHECK_CUDA(mf::launch_finalize(c->dp, parts, nb, ds, 0, s));
   if (F) {
@@ -630,6 +640,7 @@ mf_status mf_compute_dt(mf_ctx* c, const mf_fab* U, const mf_box* box, double* d
   if (U->ncomp != c->nc) return MF_ERR_BAD_ARG;
   cudaStream_t s = (cudaStream_t)stream;
   const long long nv = box_cells(*box);
+  if (nv >= (1LL << 31) - 1024) return MF_ERR_BAD_ARG;
   MF_CHECK_CUDA(c->desc.ensure(sizeof(StageDesc) * 2));
   MF_CHECK_CUDA(c->hdesc.ensure(sizeof(StageDesc) * 2));
   MF_CHECK_CUDA(c->state.ensure(sizeof(StepState)));
@@ -637,15 +648,16 @@ mf_status mf_compute_dt(mf_ctx* c, const mf_fab* U, const mf_box* box, double* d
   MF_CHECK_CUDA(c->partials.ensure(sizeof(DtPartial) * ((nv + 127) / 128 + 1)));
   StageDesc* hd = (StageDesc*)c->hdesc.p;
   fill_desc(hd[0], U->box, *box, *box);
+  StageDesc* dd = (StageDesc*)c->desc.p;
+  mf::Batch b = single_batch(hd[0], dd, c->p.space_dim);
   StepState* hs = (StepState*)c->hstate.p;
   std::memset(hs, 0, sizeof(*hs));
-  StageDesc* dd = (StageDesc*)c->desc.p;
   StepState* ds = (StepState*)c->state.p;
   DtPartial* parts = (DtPartial*)c->partials.p;
   MF_CHECK_CUDA(cudaMemcpyAsync(dd, hd, sizeof(StageDesc), cudaMemcpyHostToDevice, s));
   MF_CHECK_CUDA(cudaMemcpyAsync(ds, hs, sizeof(StepState), cudaMemcpyHostToDevice, s));
   int nb = 0;
-  MF_CHECK_CUDA(mf::launch_dt(c->dp, U->data, dd, 1, nv, parts, &nb, s));
+  MF_CHECK_CUDA(mf::launch_dt(c->dp, U->data, b, parts, &nb, s));
   MF_CHECK_CUDA(mf::launch_finalize(c->dp, parts, nb, ds, 0, s));
   MF_CHECK_CUDA(cudaMemcpyAsync(hs, ds, sizeof(StepState), cudaMemcpyDeviceToHost, s));
   mf_status st = wait_stream(s, c->timeout);
@@ -667,46 +679,171 @@ mf_status mf_compute_dt(mf_ctx* c, const mf_fab* U, const mf_box* box, double* d
 // level
 // ---------------------------------------------------------------------------
 
-static void add_regions(const mf_level* L, const mf_params& p, int depth, std::vector<CopyReg>& out) {
+}  // extern "C"
+
+// Uniform bucket grid over the valid boxes of a level, so that finding the
+// patches that meet a box costs the buckets it spans instead of a pass over
+// every patch (a level can hold thousands of patches).
+struct PatchIndex {
+  int nb[3] = {1, 1, 1}, bs[3] = {1, 1, 1}, lo[3] = {0, 0, 0};
+  std::vector<std::vector<int>> bucket;
+  std::vector<int> stamp;
+  int tick = 0;
+
+  void build(const std::vector<mf_box>& v, const mf_params& p) {
+    const int sd = p.space_dim;
+    for (int d = 0; d < 3; ++d) {
+      lo[d] = (d < sd) ? p.domain_lo[d] : 0;
+      bs[d] = 1;
+      nb[d] = 1;
+    }
+    for (const mf_box& b : v)
+      for (int d = 0; d < sd; ++d) bs[d] = std::max(bs[d], b.hi[d] - b.lo[d] + 1);
+    for (int d = 0; d < sd; ++d)
+      nb[d] = std::max(1, (p.domain_hi[d] - p.domain_lo[d] + bs[d]) / bs[d]);
+    bucket.assign((size_t)nb[0] * nb[1] * nb[2], std::vector<int>());
+    stamp.assign(v.size(), 0);
+    for (int i = 0; i < (int)v.size(); ++i) {
+      int b0[3], b1[3];
+      if (!range(v[i], b0, b1)) continue;
+      for (int z = b0[2]; z <= b1[2]; ++z)
+        for (int y = b0[1]; y <= b1[1]; ++y)
+          for (int x = b0[0]; x <= b1[0]; ++x)
+            bucket[((size_t)z * nb[1] + y) * nb[0] + x].push_back(i);
+    }
+  }
+  bool range(const mf_box& q, int b0[3], int b1[3]) const {
+    for (int d = 0; d < 3; ++d) {
+      b0[d] = std::max(0, floordiv(q.lo[d] - lo[d], bs[d]));
+      b1[d] = std::min(nb[d] - 1, floordiv(q.hi[d] - lo[d], bs[d]));
+      if (b0[d] > b1[d]) return false;
+    }
+    return true;
+  }
+  static int floordiv(int a, int b) { return (a >= 0) ? a / b : -((-a + b - 1) / b); }
+  // f(i) once for every patch i whose buckets meet q (a superset of the
+  // patches whose valid box meets q).
+  template <class Fn>
+  void query(const mf_box& q, Fn&& f) {
+    int b0[3], b1[3];
+    if (!range(q, b0, b1)) return;
+    ++tick;
+    for (int z = b0[2]; z <= b1[2]; ++z)
+      for (int y = b0[1]; y <= b1[1]; ++y)
+        for (int x = b0[0]; x <= b1[0]; ++x)
+          for (int i : bucket[((size_t)z * nb[1] + y) * nb[0] + x])
+            if (stamp[i] != tick) {
+              stamp[i] = tick;
+              f(i);
+            }
+  }
+};
+
+// Periodic image shifts (in cells) of a level's domain: 3^np vectors, np the
+// number of periodic directions; the zero shift first.
+static std::vector<std::array<int, 3>> periodic_shifts(const mf_params& p) {
   const int sd = p.space_dim;
-  int Lp[3] = {0, 0, 0};
-  for (int d = 0; d < sd; ++d) Lp[d] = p.domain_hi[d] - p.domain_lo[d] + 1;
-  int rng[3];
-  for (int d = 0; d < 3; ++d) rng[d] = (d < sd && p.periodic[d]) ? 1 : 0;
+  int Lp[3] = {0, 0, 0}, rng[3] = {0, 0, 0};
+  for (int d = 0; d < sd; ++d) {
+    Lp[d] = p.domain_hi[d] - p.domain_lo[d] + 1;
+    rng[d] = p.periodic[d] ? 1 : 0;
+  }
+  std::vector<std::array<int, 3>> out;
+  out.push_back({0, 0, 0});
+  for (int a = -rng[0]; a <= rng[0]; ++a)
+    for (int b = -rng[1]; b <= rng[1]; ++b)
+      for (int e = -rng[2]; e <= rng[2]; ++e)
+        if (a || b || e) out.push_back({a * Lp[0], b * Lp[1], e * Lp[2]});
+  return out;
+}
+
+static mf_box box_shift(mf_box b, const std::array<int, 3>& sh) {
+  for (int d = 0; d < 3; ++d) {
+    b.lo[d] += sh[d];
+    b.hi[d] += sh[d];
+  }
+  return b;
+}
+
+// Copy regions of LevelData::exchange: the cells of valid.grow(depth) of each
+// patch that lie in another patch's valid box or in a periodic image of one.
+static void add_regions(const mf_level* L, const mf_params& p, PatchIndex& ix, int depth,
+                        std::vector<CopyReg>& out) {
+  const int sd = p.space_dim;
+  const auto shifts = periodic_shifts(p);
   for (int dp = 0; dp < L->np; ++dp) {
-    mf_box dst = box_grow(L->valid[dp], depth, sd);
+    const mf_box dst = box_grow(L->valid[dp], depth, sd);
     int dfn[3];
     ext3(L->fab[dp], dfn);
-    for (int sp = 0; sp < L->np; ++sp) {
-      int sfn[3];
-      ext3(L->fab[sp], sfn);
-      for (int a = -rng[0]; a <= rng[0]; ++a)
-        for (int b = -rng[1]; b <= rng[1]; ++b)
-          for (int e = -rng[2]; e <= rng[2]; ++e) {
-            if (sp == dp && a == 0 && b == 0 && e == 0) continue;
-            int sh[3] = {a * Lp[0], b * Lp[1], e * Lp[2]};
-            mf_box src = L->valid[sp];
-            for (int d = 0; d < 3; ++d) {
-              src.lo[d] += sh[d];
-              src.hi[d] += sh[d];
-            }
-            mf_box r = box_isect(src, dst);
-            if (box_empty(r)) continue;
-            CopyReg R;
-            R.src_off = L->off[sp];
-            R.dst_off = L->off[dp];
-            for (int d = 0; d < 3; ++d) {
-              R.sfn[d] = sfn[d];
-              R.dfn[d] = dfn[d];
-              R.s0[d] = r.lo[d] - sh[d] - L->fab[sp].lo[d];
-              R.d0[d] = r.lo[d] - L->fab[dp].lo[d];
-              R.ext[d] = r.hi[d] - r.lo[d] + 1;
-            }
-            out.push_back(R);
-          }
+    for (size_t k = 0; k < shifts.size(); ++k) {
+      const auto& sh = shifts[k];
+      const std::array<int, 3> msh = {-sh[0], -sh[1], -sh[2]};
+      ix.query(box_shift(dst, msh), [&](int sp) {
+        if (sp == dp && k == 0) return;
+        const mf_box r = box_isect(box_shift(L->valid[sp], sh), dst);
+        if (box_empty(r)) return;
+        int sfn[3];
+        ext3(L->fab[sp], sfn);
+        CopyReg R;
+        R.src_off = L->off[sp];
+        R.dst_off = L->off[dp];
+        for (int d = 0; d < 3; ++d) {
+          R.sfn[d] = sfn[d];
+          R.dfn[d] = dfn[d];
+          R.s0[d] = r.lo[d] - sh[d] - L->fab[sp].lo[d];
+          R.d0[d] = r.lo[d] - L->fab[dp].lo[d];
+          R.ext[d] = r.hi[d] - r.lo[d] + 1;
+        }
+        out.push_back(R);
+      });
     }
   }
 }
+
+// valueBox of RK2 stage 1 for patch i.  Stage 2 needs the predictor on the
+// two ghost layers next to each face of the valid box (the face-normal
+// stencil of the fluxes on the valid faces).  Where sibling patches (or their
+// periodic images) cover such a slab, the exchange between the stages copies
+// it; where they do not (a coarse-fine edge of a level that does not cover
+// the domain), stage 1 computes it, as the reference does by running stage 1
+// on box.grow(2) (src/PatchMHDAM.cpp:1238-1246).  Cells outside a
+// non-periodic domain side are never computed (ProblemDomain clipping).
+static mf_box stage1_box(const mf_level* L, const mf_params& p, PatchIndex& ix, int i) {
+  const int sd = p.space_dim;
+  const mf_box& v = L->valid[i];
+  const auto shifts = periodic_shifts(p);
+  mf_box g = v;
+  for (int d = 0; d < sd; ++d)
+    for (int side = 0; side < 2; ++side) {
+      mf_box slab = v;
+      if (side == 0) {
+        slab.lo[d] = v.lo[d] - 2;
+        slab.hi[d] = v.lo[d] - 1;
+      } else {
+        slab.lo[d] = v.hi[d] + 1;
+        slab.hi[d] = v.hi[d] + 2;
+      }
+      slab = box_and_domain(slab, p);
+      if (box_empty(slab)) continue;
+      long long covered = 0;
+      for (const auto& sh : shifts) {
+        const std::array<int, 3> msh = {-sh[0], -sh[1], -sh[2]};
+        ix.query(box_shift(slab, msh), [&](int j) {
+          const mf_box r = box_isect(box_shift(L->valid[j], sh), slab);
+          if (!box_empty(r)) covered += box_cells(r);
+        });
+      }
+      if (covered < box_cells(slab)) {
+        if (side == 0)
+          g.lo[d] -= 2;
+        else
+          g.hi[d] += 2;
+      }
+    }
+  return box_and_domain(g, p);
+}
+
+extern "C" {
 
 // ev (nullable): events recorded after every launch, in launch order, with
 // kinds[] receiving 0 exchange, 1 prim, 2 flux, 3 update, 4 finalize.
@@ -714,9 +851,7 @@ static mf_status enqueue_level_step(mf_level* L, int advance, cudaEvent_t* ev = 
                                     int* kinds = nullptr, int* nev = nullptr) {
   mf_ctx* c = L->ctx;
   const mf_params& p = c->p;
-  const int mixed = (p.precision == MF_PREC_MIXED);
   cudaStream_t s = L->s;
-  StageDesc* dd = (StageDesc*)L->desc.p;
   StepState* ds = (StepState*)L->state.p;
   DtPartial* parts = (DtPartial*)L->partials.p;
   StageBuffers B;
@@ -749,8 +884,7 @@ static mf_status enqueue_level_step(mf_level* L, int advance, cudaEvent_t* ev = 
     B.uin = (const double*)L->U.p;
     B.uout = (double*)L->U1.p;
     B.ev = ev ? ev + ne : nullptr;
-    MF_CHECK_CUDA(mf::launch_stage(c->dp, p.precision,B, dd, L->np, L->max_w, L->max_f, L->max_v, 0,
-                                   1.0, ds, parts, &nb, s));
+    MF_CHECK_CUDA(mf::launch_stage(c->dp, p.precision, B, L->b1, 0, 1.0, ds, parts, &nb, s));
     stage_marks(ne);
     MF_CHECK_CUDA(
         mf::launch_exchange((double*)L->U1.p, (const CopyReg*)L->extwo.p, L->ntwo, nc, s));
@@ -759,15 +893,15 @@ static mf_status enqueue_level_step(mf_level* L, int advance, cudaEvent_t* ev = 
     B.uout = (double*)L->U.p;
     B.uold = (const double*)L->U.p;
     B.ev = ev ? ev + ne : nullptr;
-    MF_CHECK_CUDA(mf::launch_stage(c->dp, p.precision,B, dd, L->np, L->max_w, L->max_f, L->max_v,
-                                   mf::kStageAverage | mf::kStageDt, 0.5, ds, parts, &nb, s));
+    MF_CHECK_CUDA(mf::launch_stage(c->dp, p.precision, B, L->b2, mf::kStageAverage | mf::kStageDt,
+                                   0.5, ds, parts, &nb, s));
     stage_marks(ne);
   } else {
     B.uin = (const double*)L->U.p;
     B.uout = (double*)L->U.p;
     B.ev = ev ? ev + ne : nullptr;
-    MF_CHECK_CUDA(mf::launch_stage(c->dp, p.precision,B, dd, L->np, L->max_w, L->max_f, L->max_v,
-                                   mf::kStageDt, 1.0, ds, parts, &nb, s));
+    MF_CHECK_CUDA(
+        mf::launch_stage(c->dp, p.precision, B, L->b2, mf::kStageDt, 1.0, ds, parts, &nb, s));
     stage_marks(ne);
   }
   MF_CHECK_CUDA(mf::launch_finalize(c->dp, parts, nb, ds, advance, s));
@@ -851,29 +985,48 @@ mf_status mf_level_create(mf_ctx* c, int npatch, const mf_box* valid, mf_level**
   L->total = off;
   const int mixed = (p.precision == MF_PREC_MIXED);
   const size_t rs = mixed ? sizeof(float) : sizeof(double);
-  std::vector<StageDesc> hd(npatch);
-  long long foff[3] = {0, 0, 0}, boff[3] = {0, 0, 0};
-  for (int i = 0; i < npatch; ++i) {
-    mf_box wb = box_grow(valid[i], 2, sd);
-    fill_desc(hd[i], L->fab[i], valid[i], wb);
-    hd[i].u_off = L->off[i];
-    for (int d = 0; d < sd; ++d) {
-      long long nf = box_cells(box_nodes(valid[i], d));
-      hd[i].f_off[d] = foff[d];
-      hd[i].bn_off[d] = boff[d];
-      foff[d] += ((nf * nc + 63) / 64) * 64;
-      boff[d] += ((nf + 63) / 64) * 64;
-      L->max_f[d] = std::max(L->max_f[d], nf);
+  const bool rk2 = (p.time_approximation == MF_TA_RK2);
+  PatchIndex ix;
+  ix.build(L->valid, p);
+  // descs of both stages; face fluxes and Bn of one stage at a time, each
+  // patch's fab 64-element aligned
+  std::vector<StageDesc> hd(2 * (size_t)npatch);
+  long long fsize[3] = {0, 0, 0}, bsize[3] = {0, 0, 0};
+  for (int stg = 0; stg < 2; ++stg) {
+    long long foff[3] = {0, 0, 0}, boff[3] = {0, 0, 0};
+    for (int i = 0; i < npatch; ++i) {
+      StageDesc& D = hd[(size_t)stg * npatch + i];
+      const mf_box vb = (stg == 0 && rk2) ? stage1_box(L, p, ix, i) : valid[i];
+      fill_desc(D, L->fab[i], vb, box_isect(box_grow(vb, 2, sd), L->fab[i]));
+      D.u_off = L->off[i];
+      for (int d = 0; d < sd; ++d) {
+        const long long nf = box_cells(box_nodes(vb, d));
+        D.f_off[d] = foff[d];
+        D.bn_off[d] = boff[d];
+        foff[d] += ((nf * nc + 63) / 64) * 64;
+        boff[d] += ((nf + 63) / 64) * 64;
+      }
     }
-    L->max_w = std::max(L->max_w, box_cells(wb));
-    L->max_v = std::max(L->max_v, box_cells(valid[i]));
+    for (int d = 0; d < 3; ++d) {
+      fsize[d] = std::max(fsize[d], foff[d]);
+      bsize[d] = std::max(bsize[d], boff[d]);
+    }
   }
+  std::memset(&L->b1, 0, sizeof(L->b1));
+  std::memset(&L->b2, 0, sizeof(L->b2));
+  if (!mf::batch_offsets(hd.data(), npatch, sd, L->b1) ||
+      !mf::batch_offsets(hd.data() + npatch, npatch, sd, L->b2)) {
+    delete L;
+    return MF_ERR_UNSUPPORTED;  // more than 2^31 cells or faces in one launch
+  }
+  mf::batch_default_threads(L->b1);
+  mf::batch_default_threads(L->b2);
   std::vector<CopyReg> full, two;
-  add_regions(L, p, c->ng, full);
-  if (p.time_approximation == MF_TA_RK2) add_regions(L, p, 2, two);
+  add_regions(L, p, ix, c->ng, full);
+  if (rk2) add_regions(L, p, ix, 2, two);
   L->nfull = (int)full.size();
   L->ntwo = (int)two.size();
-  L->nparts = (int)(((L->max_v + 127) / 128) * npatch);
+  L->nparts = mf::dt_partials(L->b2);
   mf_status st = MF_OK;
   auto fail = [&](cudaError_t e) {
     st = (e == cudaErrorMemoryAllocation) ? MF_ERR_OOM : MF_ERR_CUDA;
@@ -888,14 +1041,16 @@ mf_status mf_level_create(mf_ctx* c, int npatch, const mf_box* valid, mf_level**
     }
     if ((e = L->W.ensure(sizeof(double) * L->total)) != cudaSuccess) break;
     for (int d = 0; d < sd && e == cudaSuccess; ++d) {
-      e = L->F[d].ensure(rs * foff[d]);
-      if (e == cudaSuccess) e = L->Bn[d].ensure(rs * boff[d]);
+      e = L->F[d].ensure(rs * fsize[d]);
+      if (e == cudaSuccess) e = L->Bn[d].ensure(rs * bsize[d]);
     }
     if (e != cudaSuccess) break;
-    if ((e = L->desc.ensure(sizeof(StageDesc) * npatch)) != cudaSuccess) break;
-    if ((e = cudaMemcpy(L->desc.p, hd.data(), sizeof(StageDesc) * npatch,
+    if ((e = L->desc.ensure(sizeof(StageDesc) * hd.size())) != cudaSuccess) break;
+    if ((e = cudaMemcpy(L->desc.p, hd.data(), sizeof(StageDesc) * hd.size(),
                         cudaMemcpyHostToDevice)) != cudaSuccess)
       break;
+    L->b1.desc = (const StageDesc*)L->desc.p;
+    L->b2.desc = (const StageDesc*)L->desc.p + npatch;
     if ((e = L->exfull.ensure(sizeof(CopyReg) * std::max<size_t>(1, full.size()))) != cudaSuccess)
       break;
     if (!full.empty() &&
@@ -1055,8 +1210,8 @@ mf_status mf_level_compute_dt(mf_level* L, double* dt, int* min_patch, int min_c
   std::memset(hs, 0, sizeof(*hs));
   MF_CHECK_CUDA(cudaMemcpyAsync(L->state2.p, hs, sizeof(StepState), cudaMemcpyHostToDevice, L->s));
   int nb = 0;
-  MF_CHECK_CUDA(mf::launch_dt(c->dp, (const double*)L->U.p, (const StageDesc*)L->desc.p, L->np,
-                              L->max_v, (DtPartial*)L->partials.p, &nb, L->s));
+  MF_CHECK_CUDA(
+      mf::launch_dt(c->dp, (const double*)L->U.p, L->b2, (DtPartial*)L->partials.p, &nb, L->s));
   MF_CHECK_CUDA(mf::launch_finalize(c->dp, (const DtPartial*)L->partials.p, nb,
                                     (StepState*)L->state2.p, 0, L->s));
   MF_CHECK_CUDA(
@@ -1143,6 +1298,110 @@ mf_status mf_level_profile_step(mf_level* L, double dt, float* ms, int* kinds, i
     *nlaunch = ne;
   } while (0);
   for (auto& e : ev) cudaEventDestroy(e);
+  return st;
+}
+
+// Time `reps` launches of one kernel kind of stage 1 (prim, fluxes of every
+// direction, update without averaging) with the level's current threads.
+// Stage 1 reads U and writes only W, F, Bn and U1, so the level's state is
+// left as it was; the step state used is a private copy with dt = 0.
+static mf_status time_kind(mf_level* L, int kind, int reps, cudaEvent_t e0, cudaEvent_t e1,
+                           float* ms) {
+  mf_ctx* c = L->ctx;
+  const mf_params& p = c->p;
+  StageBuffers B;
+  std::memset(&B, 0, sizeof(B));
+  B.uin = (const double*)L->U.p;
+  B.uout = (double*)(p.time_approximation == MF_TA_RK2 ? L->U1.p : L->W.p);
+  B.w = (double*)L->W.p;
+  for (int d = 0; d < 3; ++d) {
+    B.f[d] = L->F[d].p;
+    B.bn[d] = L->Bn[d].p;
+  }
+  StepState* ds = (StepState*)L->state2.p;
+  DtPartial* parts = (DtPartial*)L->partials.p;
+  const mf::Batch& b = (p.time_approximation == MF_TA_RK2) ? L->b1 : L->b2;
+  const int sd = p.space_dim;
+  MF_CHECK_CUDA(cudaEventRecord(e0, L->s));
+  for (int r = 0; r < reps; ++r) {
+    cudaError_t e = cudaSuccess;
+    if (kind == 0) {
+      e = mf::launch_prim(c->dp, B.uin, B.w, b, L->s);
+    } else if (kind == 1) {
+      for (int d = 0; d < sd && e == cudaSuccess; ++d) {
+        if (p.precision == MF_PREC_MIXED)
+          e = mf::launch_flux_fast<float>(c->dp, d, B.w, B.f[d], B.bn[d], b, ds, L->s);
+        else if (p.precision == MF_PREC_FP64_FAST)
+          e = mf::launch_flux_fast<double>(c->dp, d, B.w, B.f[d], B.bn[d], b, ds, L->s);
+        else
+          e = mf::launch_flux_exact(c->dp, d, B.w, B.f[d], B.bn[d], b, ds, L->s);
+      }
+    } else {
+      int nb = 0;
+      if (p.precision == MF_PREC_MIXED)
+        e = mf::launch_update_fast<float>(c->dp, B, b, 0, 1.0, ds, parts, &nb, L->s);
+      else if (p.precision == MF_PREC_FP64_FAST)
+        e = mf::launch_update_fast<double>(c->dp, B, b, 0, 1.0, ds, parts, &nb, L->s);
+      else
+        e = mf::launch_update_exact(c->dp, B, b, 0, 1.0, ds, parts, &nb, L->s);
+    }
+    MF_CHECK_CUDA(e);
+  }
+  MF_CHECK_CUDA(cudaEventRecord(e1, L->s));
+  mf_status st = wait_stream(L->s, c->timeout);
+  if (st != MF_OK) return st;
+  MF_CHECK_CUDA(cudaEventElapsedTime(ms, e0, e1));
+  return MF_OK;
+}
+
+mf_status mf_level_autotune(mf_level* L, int reps, int threads[3]) {
+  if (!L || reps <= 0 || reps > 1000) return MF_ERR_BAD_ARG;
+  mf_ctx* c = L->ctx;
+  StepState* hs = (StepState*)L->hstate.p;
+  std::memset(hs, 0, sizeof(*hs));
+  hs->ch = c->p.dedner_ch;
+  hs->cp = c->p.dedner_cp;
+  MF_CHECK_CUDA(cudaMemcpyAsync(L->state2.p, hs, sizeof(StepState), cudaMemcpyHostToDevice, L->s));
+  // dt partials of the tried launches: the largest count (fewest threads)
+  const int most = (int)mf::flat_blocks(std::max(L->b1.tot_v, L->b2.tot_v), 64);
+  MF_CHECK_CUDA(L->partials.ensure(sizeof(DtPartial) * (most + 1)));
+  cudaEvent_t e0, e1;
+  MF_CHECK_CUDA(cudaEventCreate(&e0));
+  if (cudaEventCreate(&e1) != cudaSuccess) {
+    cudaEventDestroy(e0);
+    return MF_ERR_CUDA;
+  }
+  static const int cand[3] = {64, 128, 256};
+  mf_status st = MF_OK;
+  for (int kind = 0; kind < 3 && st == MF_OK; ++kind) {
+    float best = 0.f;
+    int bnt = L->b1.nt[kind];
+    for (int q = 0; q < 3 && st == MF_OK; ++q) {
+      L->b1.nt[kind] = L->b2.nt[kind] = cand[q];
+      float ms = 0.f;
+      st = time_kind(L, kind, 1, e0, e1, &ms);  // warm-up
+      if (st == MF_OK) st = time_kind(L, kind, reps, e0, e1, &ms);
+      if (st == MF_OK && (q == 0 || ms < best)) {
+        best = ms;
+        bnt = cand[q];
+      }
+    }
+    L->b1.nt[kind] = L->b2.nt[kind] = bnt;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (st != MF_OK) {
+    mf::batch_default_threads(L->b1);
+    mf::batch_default_threads(L->b2);
+  }
+  L->nparts = mf::dt_partials(L->b2);
+  if ((size_t)(L->nparts + 1) * sizeof(DtPartial) > L->partials.bytes) return MF_ERR_CUDA;
+  // graphs captured with the old launch shapes are rebuilt on next use
+  if (L->gsync) cudaGraphExecDestroy(L->gsync);
+  if (L->gasync) cudaGraphExecDestroy(L->gasync);
+  L->gsync = L->gasync = nullptr;
+  if (threads)
+    for (int k = 0; k < 3; ++k) threads[k] = L->b2.nt[k];
   return st;
 }
 

@@ -63,6 +63,11 @@ struct StageDesc {
   int flo[3], fn[3];      // fab box lo and extents (U, W)
   int vlo[3], vn[3];      // valueBox lo and extents
   int wlo[3], wn[3];      // box on which W is computed
+  // first index of this patch's items in a flattened launch over a batch:
+  // [kRegW] cells of the W box, [kRegF + d] faces in direction d,
+  // [kRegV] cells of the valueBox.  Ascending over the batch.
+  int g0[5];
+  int pad0;
 };
 
 // Per-block partial of the dt reduction.

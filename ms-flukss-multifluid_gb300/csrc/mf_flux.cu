@@ -9,22 +9,22 @@ namespace mf {
 
 template <typename R>
 cudaError_t launch_flux_fast(const DevParams& P, int dir, const double* w, void* f, void* bn,
-                             const StageDesc* d_desc, int ndesc, long long max_f,
-                             const StepState* state, cudaStream_t s) {
-  const dim3 gf((unsigned)((max_f + kBlock - 1) / kBlock), (unsigned)ndesc);
+                             const Batch& b, const StepState* state, cudaStream_t s) {
+  const int tot = b.tot_f[dir];
+  if (tot <= 0) return cudaSuccess;
+  const int nt = b.nt[1];
+  const unsigned gf = flat_blocks(tot, nt);
   R* F = (R*)f;
   R* Bn = (R*)bn;
-  if (dir == 0) k_flux<R, 0><<<gf, kBlock, 0, s>>>(P, w, F, Bn, d_desc, state);
-  if (dir == 1) k_flux<R, 1><<<gf, kBlock, 0, s>>>(P, w, F, Bn, d_desc, state);
-  if (dir == 2) k_flux<R, 2><<<gf, kBlock, 0, s>>>(P, w, F, Bn, d_desc, state);
+  if (dir == 0) k_flux<R, 0><<<gf, nt, 0, s>>>(P, w, F, Bn, b.desc, b.ndesc, tot, state);
+  if (dir == 1) k_flux<R, 1><<<gf, nt, 0, s>>>(P, w, F, Bn, b.desc, b.ndesc, tot, state);
+  if (dir == 2) k_flux<R, 2><<<gf, nt, 0, s>>>(P, w, F, Bn, b.desc, b.ndesc, tot, state);
   return cudaGetLastError();
 }
 
 template cudaError_t launch_flux_fast<double>(const DevParams&, int, const double*, void*, void*,
-                                              const StageDesc*, int, long long, const StepState*,
-                                              cudaStream_t);
+                                              const Batch&, const StepState*, cudaStream_t);
 template cudaError_t launch_flux_fast<float>(const DevParams&, int, const double*, void*, void*,
-                                             const StageDesc*, int, long long, const StepState*,
-                                             cudaStream_t);
+                                             const Batch&, const StepState*, cudaStream_t);
 
 }  // namespace mf

@@ -7,14 +7,16 @@
 namespace mf {
 
 cudaError_t launch_flux_exact(const DevParams& P, int dir, const double* w, void* f, void* bn,
-                              const StageDesc* d_desc, int ndesc, long long max_f,
-                              const StepState* state, cudaStream_t s) {
-  const dim3 gf((unsigned)((max_f + kBlock - 1) / kBlock), (unsigned)ndesc);
+                              const Batch& b, const StepState* state, cudaStream_t s) {
+  const int tot = b.tot_f[dir];
+  if (tot <= 0) return cudaSuccess;
+  const int nt = b.nt[1];
+  const unsigned gf = flat_blocks(tot, nt);
   double* F = (double*)f;
   double* Bn = (double*)bn;
-  if (dir == 0) k_flux<double, 0><<<gf, kBlock, 0, s>>>(P, w, F, Bn, d_desc, state);
-  if (dir == 1) k_flux<double, 1><<<gf, kBlock, 0, s>>>(P, w, F, Bn, d_desc, state);
-  if (dir == 2) k_flux<double, 2><<<gf, kBlock, 0, s>>>(P, w, F, Bn, d_desc, state);
+  if (dir == 0) k_flux<double, 0><<<gf, nt, 0, s>>>(P, w, F, Bn, b.desc, b.ndesc, tot, state);
+  if (dir == 1) k_flux<double, 1><<<gf, nt, 0, s>>>(P, w, F, Bn, b.desc, b.ndesc, tot, state);
+  if (dir == 2) k_flux<double, 2><<<gf, nt, 0, s>>>(P, w, F, Bn, b.desc, b.ndesc, tot, state);
   return cudaGetLastError();
 }
 

@@ -10,16 +10,16 @@ namespace {
 using namespace MF_PHYS;
 
 template <typename R, int DIR>
-__global__ void __launch_bounds__(kBlock)
+__global__ void __launch_bounds__(kMaxBlock)
     k_flux(const DevParams P, const double* __restrict__ W, R* __restrict__ F,
-           R* __restrict__ Bn, const StageDesc* __restrict__ descs,
+           R* __restrict__ Bn, const StageDesc* __restrict__ descs, int ndesc, int total,
            const StepState* __restrict__ ss) {
-  const StageDesc& D = descs[blockIdx.y];
+  const int gi = blockIdx.x * blockDim.x + threadIdx.x;
+  if (gi >= total) return;
+  const StageDesc& D = descs[find_desc(descs, ndesc, kRegF + DIR, gi)];
+  const int lin = gi - D.g0[kRegF + DIR];
   int fnb[3] = {D.vn[0], D.vn[1], D.vn[2]};
   fnb[DIR] += 1;
-  const int n = fnb[0] * fnb[1] * fnb[2];
-  const int lin = blockIdx.x * blockDim.x + threadIdx.x;
-  if (lin >= n) return;
   int i, j, k;
   decode(lin, D.vlo, fnb, i, j, k);
   const long long cs = (long long)D.fn[0] * D.fn[1] * D.fn[2];

@@ -1,11 +1,15 @@
 // mf_kernels.cuh - launch interface of the stage kernels.
 //
 // One explicit stage of PatchMHDAM::EulerStep (src/PatchMHDAM.cpp:495-709) is
-// three kinds of kernel over every patch of a batch (blockIdx.y = patch):
+// three kinds of kernel over every patch of a batch:
 //   k_prim    (mf_prim_exact.cu) conserved -> primitive on valueBox.grow(2)
 //   k_flux<D> (mf_flux.cu)       face states + Riemann fluxes in direction D
 //   k_update  (mf_update.cu)     flux divergence, sources, positivity, RK2
 //                                averaging and the per-cell dt
+// A launch is flat over the concatenated items (cells or faces) of all
+// patches of the batch, so patches of uneven sizes share blocks and no lane
+// idles on padding; each thread finds its patch by a binary search over the
+// ascending start offsets StageDesc::g0.
 #pragma once
 
 #include <cfloat>
@@ -16,6 +20,71 @@
 namespace mf {
 
 constexpr int kBlock = 128;
+
+enum RegionKind : int { kRegW = 0, kRegF = 1, kRegV = 4 };
+
+// Patch whose items contain flattened index g (0 <= g < launch total): the
+// largest d with descs[d].g0[kind] <= g.  Patches with no items share their
+// start with the next one and are skipped by taking the largest such d.
+__device__ __forceinline__ int find_desc(const StageDesc* __restrict__ descs, int ndesc, int kind,
+                                         int g) {
+  int lo = 0, hi = ndesc - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (__ldg(&descs[mid].g0[kind]) <= g)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  return lo;
+}
+
+// A flattened launch over a batch of patches: the device descs, the total
+// item counts of each region kind, and the threads per block of the prim,
+// flux and update/dt kernels (multiples of 32, at most kMaxBlock).
+struct Batch {
+  const StageDesc* desc;
+  int ndesc;
+  int tot_w, tot_f[3], tot_v;
+  int nt[3];
+};
+
+constexpr int kMaxBlock = 256;
+
+// Fill the g0 offsets of n host descs and the totals of a Batch.  Returns
+// false when a total does not fit a 32-bit index.
+inline bool batch_offsets(StageDesc* hd, int n, int sd, Batch& b) {
+  long long t[5] = {0, 0, 0, 0, 0};
+  for (int i = 0; i < n; ++i) {
+    StageDesc& D = hd[i];
+    long long cnt[5];
+    cnt[kRegW] = (long long)D.wn[0] * D.wn[1] * D.wn[2];
+    for (int d = 0; d < 3; ++d) {
+      long long f = 0;
+      if (d < sd) {
+        long long e[3] = {D.vn[0], D.vn[1], D.vn[2]};
+        e[d] += 1;
+        f = e[0] * e[1] * e[2];
+      }
+      cnt[kRegF + d] = f;
+    }
+    cnt[kRegV] = (long long)D.vn[0] * D.vn[1] * D.vn[2];
+    for (int k = 0; k < 5; ++k) {
+      if (t[k] > INT_MAX - 1024) return false;
+      D.g0[k] = (int)t[k];
+      t[k] += cnt[k];
+    }
+  }
+  for (int k = 0; k < 5; ++k)
+    if (t[k] > INT_MAX - 1024) return false;
+  b.ndesc = n;
+  b.tot_w = (int)t[kRegW];
+  for (int d = 0; d < 3; ++d) b.tot_f[d] = (int)t[kRegF + d];
+  b.tot_v = (int)t[kRegV];
+  return true;
+}
+
+inline void batch_default_threads(Batch& b) { b.nt[0] = b.nt[1] = b.nt[2] = kBlock; }
 
 __device__ __forceinline__ long long loc(const int* lo, const int* n, int i, int j, int k) {
   return (long long)(i - lo[0]) +
@@ -53,43 +122,45 @@ struct StageBuffers {
 
 enum StageFlags : int { kStageAverage = 1, kStageDt = 2 };
 
-cudaError_t launch_prim(const DevParams& P, const double* uin, double* w, const StageDesc* d_desc,
-                        int ndesc, long long max_w, cudaStream_t s);
+cudaError_t launch_prim(const DevParams& P, const double* uin, double* w, const Batch& b,
+                        cudaStream_t s);
 
 // FP64 parity path (reference evaluation order, no contraction)
 cudaError_t launch_flux_exact(const DevParams& P, int dir, const double* w, void* f, void* bn,
-                              const StageDesc* d_desc, int ndesc, long long max_f,
-                              const StepState* state, cudaStream_t s);
-cudaError_t launch_update_exact(const DevParams& P, const StageBuffers& B,
-                                const StageDesc* d_desc, int ndesc, long long max_v, int flags,
-                                double dt_scale, StepState* state, DtPartial* partials,
-                                int* nblocks_v, cudaStream_t s);
+                              const Batch& b, const StepState* state, cudaStream_t s);
+cudaError_t launch_update_exact(const DevParams& P, const StageBuffers& B, const Batch& b,
+                                int flags, double dt_scale, StepState* state,
+                                DtPartial* partials, int* nblocks_v, cudaStream_t s);
 // fast physics: R = float (mixed precision) or double (fast FP64)
 template <typename R>
 cudaError_t launch_flux_fast(const DevParams& P, int dir, const double* w, void* f, void* bn,
-                             const StageDesc* d_desc, int ndesc, long long max_f,
-                             const StepState* state, cudaStream_t s);
+                             const Batch& b, const StepState* state, cudaStream_t s);
 template <typename R>
-cudaError_t launch_update_fast(const DevParams& P, const StageBuffers& B, const StageDesc* d_desc,
-                               int ndesc, long long max_v, int flags, double dt_scale,
-                               StepState* state, DtPartial* partials, int* nblocks_v,
-                               cudaStream_t s);
+cudaError_t launch_update_fast(const DevParams& P, const StageBuffers& B, const Batch& b,
+                               int flags, double dt_scale, StepState* state,
+                               DtPartial* partials, int* nblocks_v, cudaStream_t s);
 
 // Bytes of one face-flux value for a precision mode (MF_PREC_*).
 inline size_t flux_bytes(int precision) { return precision == MF_PREC_MIXED ? 4 : 8; }
 
-// Enqueue one stage (prim, fluxes in every direction, update) for ndesc
-// patches.  max_w / max_f[d] / max_v: largest region sizes over the descs.
-// precision: MF_PREC_FP64 (parity), MF_PREC_FP64_FAST or MF_PREC_MIXED.
+// Blocks of a flattened launch of n items with nt threads per block.
+inline unsigned flat_blocks(long long n, int nt) {
+  return (unsigned)(n > 0 ? (n + nt - 1) / nt : 1);
+}
+
+// Number of dt partials (blocks of the update or dt kernel) for b.
+inline int dt_partials(const Batch& b) { return (int)flat_blocks(b.tot_v, b.nt[2]); }
+
+// Enqueue one stage (prim, fluxes in every direction, update) for the
+// patches of b.  precision: MF_PREC_FP64 (parity), MF_PREC_FP64_FAST or
+// MF_PREC_MIXED.
 cudaError_t launch_stage(const DevParams& P, int precision, const StageBuffers& B,
-                         const StageDesc* d_desc, int ndesc, long long max_w,
-                         const long long max_f[3], long long max_v, int flags,
-                         double dt_scale, StepState* state, DtPartial* partials,
-                         int* nblocks_v, cudaStream_t s);
+                         const Batch& b, int flags, double dt_scale, StepState* state,
+                         DtPartial* partials, int* nblocks_v, cudaStream_t s);
 
 // dx / max wave speed over each desc's valueBox into per-block partials.
-cudaError_t launch_dt(const DevParams& P, const double* u, const StageDesc* d_desc, int ndesc,
-                      long long max_v, DtPartial* partials, int* nblocks, cudaStream_t s);
+cudaError_t launch_dt(const DevParams& P, const double* u, const Batch& b, DtPartial* partials,
+                      int* nblocks, cudaStream_t s);
 
 // Reduce the dt partials of the last stage; advance = 1 also writes the next
 // dt (cfl * minimum) and the GLM speeds into *state.

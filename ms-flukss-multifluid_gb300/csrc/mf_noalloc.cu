@@ -207,6 +207,15 @@ extern "C" mf_status mf_patch_update_noalloc(mf_ctx* ctx, mf_fab* U, const mf_bo
   hs.ch = p.dedner_ch;
   hs.cp = p.dedner_cp;
   StageDesc* dd = (StageDesc*)(base + o_desc);
+  mf::Batch b1, b2;
+  std::memset(&b1, 0, sizeof(b1));
+  std::memset(&b2, 0, sizeof(b2));
+  mf::batch_offsets(&hd[0], 1, sd, b1);  // the fab-size check keeps counts < 2^31
+  mf::batch_offsets(&hd[1], 1, sd, b2);
+  b1.desc = dd;
+  b2.desc = dd + 1;
+  mf::batch_default_threads(b1);
+  mf::batch_default_threads(b2);
   StepState* ds = (StepState*)(base + o_state);
   DtPartial* parts = (DtPartial*)(base + o_parts);
   NA_CUDA(cudaMemcpyAsync(dd, hd, sizeof(hd), cudaMemcpyHostToDevice, s));
@@ -232,8 +241,7 @@ extern "C" mf_status mf_patch_update_noalloc(mf_ctx* ctx, mf_fab* U, const mf_bo
       B.f[d] = d < sd ? (void*)(base + o_f1[d]) : nullptr;
       B.bn[d] = d < sd ? (void*)(base + o_b1[d]) : nullptr;
     }
-    NA_CUDA(mf::launch_stage(*cv.dp, p.precision, B, dd, 1, cells(w1), nf1, cells(v1), 0, 1.0, ds,
-                             parts, &nb, s));
+    NA_CUDA(mf::launch_stage(*cv.dp, p.precision, B, b1, 0, 1.0, ds, parts, &nb, s));
     B.uin = pred;
     B.uout = U->data;
     B.uold = U->data;
@@ -242,8 +250,8 @@ extern "C" mf_status mf_patch_update_noalloc(mf_ctx* ctx, mf_fab* U, const mf_bo
       B.bn[d] = d < sd ? (void*)(base + o_b2[d]) : nullptr;
     }
     B.divb = (divB && divB->data) ? divB->data : nullptr;
-    NA_CUDA(mf::launch_stage(*cv.dp, p.precision, B, dd + 1, 1, cells(w2), nf2, cells(v2),
-                             mf::kStageAverage | mf::kStageDt, 0.5, ds, parts, &nb, s));
+    NA_CUDA(mf::launch_stage(*cv.dp, p.precision, B, b2, mf::kStageAverage | mf::kStageDt, 0.5,
+                             ds, parts, &nb, s));
   } else {
     B.uin = U->data;
     B.uout = U->data;
@@ -252,8 +260,7 @@ extern "C" mf_status mf_patch_update_noalloc(mf_ctx* ctx, mf_fab* U, const mf_bo
       B.bn[d] = d < sd ? (void*)(base + o_b1[d]) : nullptr;
     }
     B.divb = (divB && divB->data) ? divB->data : nullptr;
-    NA_CUDA(mf::launch_stage(*cv.dp, p.precision, B, dd + 1, 1, cells(w2), nf2, cells(v2),
-                             mf::kStageDt, 1.0, ds, parts, &nb, s));
+    NA_CUDA(mf::launch_stage(*cv.dp, p.precision, B, b2, mf::kStageDt, 1.0, ds, parts, &nb, s));
   }
   NA_CUDA(mf::launch_finalize(*cv.dp, parts, nb, ds, 0, s));
   if (F) {

@@ -8,14 +8,14 @@
 namespace mf {
 namespace {
 template <int GLM>
-__global__ void __launch_bounds__(kBlock)
+__global__ void __launch_bounds__(kMaxBlock)
     k_prim(const DevParams P, const double* __restrict__ U, double* __restrict__ W,
-           const StageDesc* __restrict__ descs) {
+           const StageDesc* __restrict__ descs, int ndesc, int total) {
   constexpr int IRHON = 8 + GLM;
-  const StageDesc& D = descs[blockIdx.y];
-  const int n = D.wn[0] * D.wn[1] * D.wn[2];
-  const int lin = blockIdx.x * blockDim.x + threadIdx.x;
-  if (lin >= n) return;
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= total) return;
+  const StageDesc& D = descs[find_desc(descs, ndesc, kRegW, g)];
+  const int lin = g - D.g0[kRegW];
   int i, j, k;
   decode(lin, D.wlo, D.wn, i, j, k);
   const long long cs = (long long)D.fn[0] * D.fn[1] * D.fn[2];
@@ -70,13 +70,15 @@ __global__ void __launch_bounds__(kBlock)
 // face fluxes in direction DIR
 }  // namespace
 
-cudaError_t launch_prim(const DevParams& P, const double* uin, double* w, const StageDesc* d_desc,
-                        int ndesc, long long max_w, cudaStream_t s) {
-  const dim3 gw((unsigned)((max_w + kBlock - 1) / kBlock), (unsigned)ndesc);
+cudaError_t launch_prim(const DevParams& P, const double* uin, double* w, const Batch& b,
+                        cudaStream_t s) {
+  if (b.tot_w <= 0) return cudaSuccess;
+  const int nt = b.nt[0];
+  const unsigned gw = flat_blocks(b.tot_w, nt);
   if (P.glm)
-    k_prim<1><<<gw, kBlock, 0, s>>>(P, uin, w, d_desc);
+    k_prim<1><<<gw, nt, 0, s>>>(P, uin, w, b.desc, b.ndesc, b.tot_w);
   else
-    k_prim<0><<<gw, kBlock, 0, s>>>(P, uin, w, d_desc);
+    k_prim<0><<<gw, nt, 0, s>>>(P, uin, w, b.desc, b.ndesc, b.tot_w);
   return cudaGetLastError();
 }
 

@@ -7,13 +7,15 @@
 namespace mf {
 
 template <typename R>
-cudaError_t launch_update_fast(const DevParams& P, const StageBuffers& B, const StageDesc* d_desc,
-                               int ndesc, long long max_v, int flags, double dt_scale,
-                               StepState* state, DtPartial* partials, int* nblocks_v,
-                               cudaStream_t s) {
-  const dim3 gv((unsigned)((max_v + kBlock - 1) / kBlock), (unsigned)ndesc);
-  if (nblocks_v) *nblocks_v = (int)(gv.x * gv.y);
-#define MF_UPD(G, FL) k_update<R, G, FL><<<gv, kBlock, 0, s>>>(P, B, d_desc, state, dt_scale, partials)
+cudaError_t launch_update_fast(const DevParams& P, const StageBuffers& B, const Batch& b,
+                               int flags, double dt_scale, StepState* state,
+                               DtPartial* partials, int* nblocks_v, cudaStream_t s) {
+  const int nt = b.nt[2];
+  const unsigned gv = flat_blocks(b.tot_v, nt);
+  if (nblocks_v) *nblocks_v = (int)gv;
+#define MF_UPD(G, FL)                                                                    \
+  k_update<R, G, FL><<<gv, nt, 0, s>>>(P, B, b.desc, b.ndesc, b.tot_v, state, dt_scale, \
+                                       partials)
   if (P.glm) {
     if (flags == 0) MF_UPD(1, 0);
     else if (flags == kStageDt) MF_UPD(1, kStageDt);
@@ -28,10 +30,10 @@ cudaError_t launch_update_fast(const DevParams& P, const StageBuffers& B, const 
 }
 
 template cudaError_t launch_update_fast<double>(const DevParams&, const StageBuffers&,
-                                                const StageDesc*, int, long long, int, double,
-                                                StepState*, DtPartial*, int*, cudaStream_t);
+                                                const Batch&, int, double, StepState*,
+                                                DtPartial*, int*, cudaStream_t);
 template cudaError_t launch_update_fast<float>(const DevParams&, const StageBuffers&,
-                                               const StageDesc*, int, long long, int, double,
-                                               StepState*, DtPartial*, int*, cudaStream_t);
+                                               const Batch&, int, double, StepState*,
+                                               DtPartial*, int*, cudaStream_t);
 
 }  // namespace mf

@@ -13,16 +13,16 @@ namespace {
 using namespace MF_PHYS;
 
 template <int GLM>
-__global__ void __launch_bounds__(kBlock)
+__global__ void __launch_bounds__(kMaxBlock)
     k_dt(const DevParams P, const double* __restrict__ U, const StageDesc* __restrict__ descs,
-         DtPartial* __restrict__ partials) {
+         int ndesc, int total, DtPartial* __restrict__ partials) {
   constexpr int IRHON = 8 + GLM;
-  const StageDesc& D = descs[blockIdx.y];
-  const int n = D.vn[0] * D.vn[1] * D.vn[2];
-  const int lin = blockIdx.x * blockDim.x + threadIdx.x;
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
   double dtc = DBL_MAX;
   int myidx = INT_MAX;
-  if (lin < n) {
+  if (g < total) {
+    const StageDesc& D = descs[find_desc(descs, ndesc, kRegV, g)];
+    const int lin = g - D.g0[kRegV];
     int i, j, k;
     decode(lin, D.vlo, D.vn, i, j, k);
     const long long cs = (long long)D.fn[0] * D.fn[1] * D.fn[2];
@@ -32,39 +32,9 @@ __global__ void __launch_bounds__(kBlock)
     for (int q = 0; q < MF_MAX_COMP; ++q)
       if (q < P.nc) u[q] = U[base + q * cs];
     dtc = P.dx / max_wave_speed<IRHON>(P, u);
-    myidx = lin;
+    myidx = g;
   }
-#pragma unroll
-  for (int off = 16; off > 0; off >>= 1) {
-    double od = __shfl_down_sync(0xffffffffu, dtc, off);
-    int oi = __shfl_down_sync(0xffffffffu, myidx, off);
-    if (dt_less(od, oi, dtc, myidx)) {
-      dtc = od;
-      myidx = oi;
-    }
-  }
-  __shared__ double sdt[kBlock / 32];
-  __shared__ int sidx[kBlock / 32];
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  if (lane == 0) {
-    sdt[wid] = dtc;
-    sidx[wid] = myidx;
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double bd = sdt[0];
-    int bi = sidx[0];
-    for (int q = 1; q < kBlock / 32; ++q)
-      if (dt_less(sdt[q], sidx[q], bd, bi)) {
-        bd = sdt[q];
-        bi = sidx[q];
-      }
-    DtPartial pr;
-    pr.dt = bd;
-    pr.desc = blockIdx.y;
-    pr.idx = bi;
-    partials[(long long)blockIdx.y * gridDim.x + blockIdx.x] = pr;
-  }
+  block_dt_min(dtc, myidx, descs, ndesc, partials);
 }
 
 __device__ __forceinline__ bool part_less(const DtPartial& a, const DtPartial& b) {
@@ -164,14 +134,15 @@ __global__ void k_flux_out(int nc, const R* __restrict__ f2, int l20, int l21, i
 
 }  // namespace
 
-cudaError_t launch_update_exact(const DevParams& P, const StageBuffers& B,
-                                const StageDesc* d_desc, int ndesc, long long max_v, int flags,
-                                double dt_scale, StepState* state, DtPartial* partials,
-                                int* nblocks_v, cudaStream_t s) {
-  const dim3 gv((unsigned)((max_v + kBlock - 1) / kBlock), (unsigned)ndesc);
-  if (nblocks_v) *nblocks_v = (int)(gv.x * gv.y);
-#define MF_UPD(G, FL) \
-  k_update<double, G, FL><<<gv, kBlock, 0, s>>>(P, B, d_desc, state, dt_scale, partials)
+cudaError_t launch_update_exact(const DevParams& P, const StageBuffers& B, const Batch& b,
+                                int flags, double dt_scale, StepState* state,
+                                DtPartial* partials, int* nblocks_v, cudaStream_t s) {
+  const int nt = b.nt[2];
+  const unsigned gv = flat_blocks(b.tot_v, nt);
+  if (nblocks_v) *nblocks_v = (int)gv;
+#define MF_UPD(G, FL)                                                                         \
+  k_update<double, G, FL><<<gv, nt, 0, s>>>(P, B, b.desc, b.ndesc, b.tot_v, state, dt_scale, \
+                                            partials)
   if (P.glm) {
     if (flags == 0) MF_UPD(1, 0);
     else if (flags == kStageDt) MF_UPD(1, kStageDt);
@@ -185,14 +156,15 @@ cudaError_t launch_update_exact(const DevParams& P, const StageBuffers& B,
   return cudaGetLastError();
 }
 
-cudaError_t launch_dt(const DevParams& P, const double* u, const StageDesc* d_desc, int ndesc,
-                      long long max_v, DtPartial* partials, int* nblocks, cudaStream_t s) {
-  const dim3 gv((unsigned)((max_v + kBlock - 1) / kBlock), (unsigned)ndesc);
-  if (nblocks) *nblocks = (int)(gv.x * gv.y);
+cudaError_t launch_dt(const DevParams& P, const double* u, const Batch& b, DtPartial* partials,
+                      int* nblocks, cudaStream_t s) {
+  const int nt = b.nt[2];
+  const unsigned gv = flat_blocks(b.tot_v, nt);
+  if (nblocks) *nblocks = (int)gv;
   if (P.glm)
-    k_dt<1><<<gv, kBlock, 0, s>>>(P, u, d_desc, partials);
+    k_dt<1><<<gv, nt, 0, s>>>(P, u, b.desc, b.ndesc, b.tot_v, partials);
   else
-    k_dt<0><<<gv, kBlock, 0, s>>>(P, u, d_desc, partials);
+    k_dt<0><<<gv, nt, 0, s>>>(P, u, b.desc, b.ndesc, b.tot_v, partials);
   return cudaGetLastError();
 }
 

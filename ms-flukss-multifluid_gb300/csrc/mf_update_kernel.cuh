@@ -21,17 +21,64 @@ __device__ __forceinline__ bool dt_less(double a, int ia, double b, int ib) {
   return (a < b) || (a == b && ia < ib);
 }
 
+// Block minimum of (dt, flattened index) into partials[blockIdx.x]: warp
+// shuffles, then one thread over the warps.  The flattened index orders cells
+// by (patch, Fortran-order index), so the minimum is the reference's
+// lexicographic one; it is turned back into (patch, index) once per block.
+__device__ __forceinline__ void block_dt_min(double dtc, int myidx,
+                                             const StageDesc* __restrict__ descs, int ndesc,
+                                             DtPartial* __restrict__ partials) {
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    double od = __shfl_down_sync(0xffffffffu, dtc, off);
+    int oi = __shfl_down_sync(0xffffffffu, myidx, off);
+    if (dt_less(od, oi, dtc, myidx)) {
+      dtc = od;
+      myidx = oi;
+    }
+  }
+  __shared__ double sdt[kMaxBlock / 32];
+  __shared__ int sidx[kMaxBlock / 32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) {
+    sdt[wid] = dtc;
+    sidx[wid] = myidx;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double bd = sdt[0];
+    int bi = sidx[0];
+    const int nw = blockDim.x >> 5;
+    for (int q = 1; q < nw; ++q)
+      if (dt_less(sdt[q], sidx[q], bd, bi)) {
+        bd = sdt[q];
+        bi = sidx[q];
+      }
+    DtPartial pr;
+    pr.dt = bd;
+    pr.desc = INT_MAX;
+    pr.idx = INT_MAX;
+    if (bi != INT_MAX) {
+      const int di = find_desc(descs, ndesc, kRegV, bi);
+      pr.desc = di;
+      pr.idx = bi - descs[di].g0[kRegV];
+    }
+    partials[blockIdx.x] = pr;
+  }
+}
+
 template <typename R, int GLM, int FLAGS>
-__global__ void __launch_bounds__(kBlock)
+__global__ void __launch_bounds__(kMaxBlock)
     k_update(const DevParams P, const StageBuffers B, const StageDesc* __restrict__ descs,
-             StepState* __restrict__ ss, const double dt_scale, DtPartial* __restrict__ partials) {
+             int ndesc, int total, StepState* __restrict__ ss, const double dt_scale,
+             DtPartial* __restrict__ partials) {
   constexpr int IRHON = 8 + GLM;
-  const StageDesc& D = descs[blockIdx.y];
-  const int n = D.vn[0] * D.vn[1] * D.vn[2];
-  const int lin = blockIdx.x * blockDim.x + threadIdx.x;
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
   double dtc = DBL_MAX;
   int myidx = INT_MAX;
-  if (lin < n) {
+  if (g < total) {
+    const StageDesc& D = descs[find_desc(descs, ndesc, kRegV, g)];
+    const int lin = g - D.g0[kRegV];
     int i, j, k;
     decode(lin, D.vlo, D.vn, i, j, k);
     const long long cs = (long long)D.fn[0] * D.fn[1] * D.fn[2];
@@ -121,44 +168,11 @@ __global__ void __launch_bounds__(kBlock)
     if (!finite) atomicOr(&ss->flags, kFlagNonFinite);
     if (FLAGS & kStageDt) {
       dtc = P.dx / max_wave_speed<IRHON>(P, u);
-      myidx = lin;
+      myidx = g;
       if (B.divb && P.use8) B.divb[loc(B.divb_lo, B.divb_n, i, j, k)] = divB;
     }
   }
-  if (FLAGS & kStageDt) {
-    // block minimum of (dt, index): warp shuffles, then one warp
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) {
-      double od = __shfl_down_sync(0xffffffffu, dtc, off);
-      int oi = __shfl_down_sync(0xffffffffu, myidx, off);
-      if (dt_less(od, oi, dtc, myidx)) {
-        dtc = od;
-        myidx = oi;
-      }
-    }
-    __shared__ double sdt[kBlock / 32];
-    __shared__ int sidx[kBlock / 32];
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    if (lane == 0) {
-      sdt[wid] = dtc;
-      sidx[wid] = myidx;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      double bd = sdt[0];
-      int bi = sidx[0];
-      for (int q = 1; q < kBlock / 32; ++q)
-        if (dt_less(sdt[q], sidx[q], bd, bi)) {
-          bd = sdt[q];
-          bi = sidx[q];
-        }
-      DtPartial pr;
-      pr.dt = bd;
-      pr.desc = blockIdx.y;
-      pr.idx = bi;
-      partials[(long long)blockIdx.y * gridDim.x + blockIdx.x] = pr;
-    }
-  }
+  if (FLAGS & kStageDt) block_dt_min(dtc, myidx, descs, ndesc, partials);
 }
 
 }  // namespace

@@ -159,6 +159,7 @@ _SIGS = {
     "mf_level_profile_step": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double,
                                              _P(ctypes.c_float), _P(ctypes.c_int),
                                              _P(ctypes.c_int), ctypes.c_int]),
+    "mf_level_autotune": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _P(ctypes.c_int)]),
     "mf_init_orszag_host": (ctypes.c_int, [_P(MfParams), _P(MfFab), _P(MfBox)]),
     "mf_init_helio_host": (ctypes.c_int, [_P(MfParams), _P(ctypes.c_double), _P(ctypes.c_double),
                                           _P(MfFab), _P(MfBox)]),
@@ -498,6 +499,12 @@ class Level:
         lo, hi = self.boxes[i]
         return grow(lo, hi, self.ctx.ng, self.ctx.p.space_dim)
 
+    def patch_fab_ptr(self, i) -> int:
+        """Device address of patch i's fab inside the level (mf_level_patch_fab)."""
+        fab = MfFab()
+        check(self.lib.mf_level_patch_fab(self.h, i, ctypes.byref(fab)), "mf_level_patch_fab")
+        return int(fab.data)
+
     def patch_view(self, flat: np.ndarray, i: int) -> np.ndarray:
         """numpy view (nc, nz, ny, nx) of patch i inside a level-layout buffer."""
         lo, hi = self.fab_box(i)
@@ -557,3 +564,10 @@ class Level:
         check(self.lib.mf_level_profile_step(self.h, dt, ms, kinds, ctypes.byref(cnt), n),
               "mf_level_profile_step")
         return [(self.KIND_NAMES[kinds[i]], float(ms[i])) for i in range(cnt.value)]
+
+    def autotune(self, reps=3):
+        """mf_level_autotune: threads per block of the prim, flux and update
+        kernels picked by timing; returns the chosen (prim, flux, update)."""
+        t = c_int3()
+        check(self.lib.mf_level_autotune(self.h, reps, t), "mf_level_autotune")
+        return tuple(t)
