@@ -50,8 +50,9 @@ typedef enum mf_status {
   MF_ERR_TIMEOUT = 5,      /* a bounded wait on the device gave up */
   MF_ERR_CUDA = 6,         /* a CUDA runtime call failed */
   MF_ERR_UNSUPPORTED = 7,  /* option combination not implemented */
-  MF_ERR_SCRATCH_LIMIT = 8 /* mf_patch_update_noalloc: the patch needs more scratch than
-                              MF_NOALLOC_SCRATCH_BYTES */
+  MF_ERR_SCRATCH_LIMIT = 8, /* mf_patch_update_noalloc: the patch needs more scratch than
+                               MF_NOALLOC_SCRATCH_BYTES */
+  MF_ERR_NO_ROOM = 9         /* mf_server_admit: no free run slot or arena space (retry later) */
 } mf_status;
 
 /* time_approximation (PatchMHDAM::eTimeApproximation) */
@@ -243,6 +244,16 @@ int mf_level_launches_per_step(const mf_level* lev);
 mf_status mf_level_profile_step(mf_level* lev, double dt, float* ms, int* kinds, int* nlaunch,
                                 int max_launch);
 
+/* Riemann fluxes of n face-state pairs in direction dir (device pointers:
+   wl, wr = n x nc primitive values laid out face by face, f = n x nc fluxes
+   out): the context's plasma solver (RIEMANNF / RIEMANN7F / RUSANOVF), the
+   GLM (Bn, psi) flux with the context's Ch (DEDNER2X2F) and the neutral van
+   Leer fluxes (VANLEERF), in the context's precision mode; returns after
+   the kernel finished.  The per-face form of the fluxes the patch update
+   computes, for tests of the solvers in isolation. */
+mf_status mf_face_fluxes(mf_ctx* ctx, int dir, int n, const double* wl, const double* wr,
+                         double* f, void* stream);
+
 /* Autotuner (no reference counterpart: the reference runs one Fortran call
    per patch).  Times the prim, flux and update kernels of the level's batch
    at 64, 128 and 256 threads per block (reps launches each, stage-1 form, so
@@ -251,6 +262,51 @@ mf_status mf_level_profile_step(mf_level* lev, double dt, float* ms, int* kinds,
    threads (nullable) receives the chosen {prim, flux, update} shapes.
    Results of a step do not depend on the shapes. */
 mf_status mf_level_autotune(mf_level* lev, int reps, int threads[3]);
+
+/* ---- Serving: independent runs stepped together in shared launches ----
+   No reference counterpart (the reference advances one simulation per
+   process).  A server keeps every admitted run resident in device arenas
+   sized once from an HBM budget and advances all of them with one set of
+   batched launches per step: a run is a level of patches covering its own
+   domain [0, n-1]^d, with the physics of the server's context (equations,
+   solvers, limiters, sources, inner sphere) and its own grid size, spacing,
+   far-field state, CFL number, dt and GLM speeds.  The numbers of a run do
+   not depend on which other runs share its launches.  Calls on one server
+   are not thread-safe. */
+typedef struct mf_server mf_server;
+
+typedef struct {
+  int n[3];              /* cells per direction; 1 for unused directions */
+  int patch;             /* patch edge length (the last patch of a row may be shorter) */
+  double dx;             /* grid spacing */
+  double cfl;            /* dt of each step = cfl * dx / (largest signal speed) */
+  double bc_plasma[8];   /* far-field primitive states (MF_BC_FARFIELD contexts) */
+  double bc_neutral1[5];
+} mf_run_spec;
+
+mf_status mf_server_create(mf_ctx* physics, double hbm_budget_bytes, int max_runs,
+                           mf_server** out);
+void mf_server_destroy(mf_server* srv);
+/* Device bytes a run of this spec holds while admitted (-1: invalid spec). */
+long long mf_server_run_bytes(const mf_server* srv, const mf_run_spec* spec);
+/* Largest free cell range of the arena, in bytes of the three cell arrays. */
+long long mf_server_free_bytes(const mf_server* srv);
+/* Admit a run whose initial conserved state is `state` (host: the run's
+   domain as one FArrayBox without ghosts, nc components, x fastest).  Waits
+   for the server's queued work.  MF_ERR_NO_ROOM: no slot or arena space. */
+mf_status mf_server_admit(mf_server* srv, const mf_run_spec* spec, const double* state,
+                          int* run);
+/* Enqueue one step of every admitted run on the stream (asynchronous). */
+mf_status mf_server_step(mf_server* srv, void* stream);
+/* Wait for the enqueued steps and fetch every run's last results. */
+mf_status mf_server_sync(mf_server* srv, void* stream);
+/* Steps taken, dt_min of the last synced step, and the run's status. */
+mf_status mf_server_run_info(const mf_server* srv, int run, long long* steps, double* dt_min,
+                             mf_status* run_status);
+/* Copy the run's state to `state` (nullable; layout of mf_server_admit) and
+   release its slot and arena ranges. */
+mf_status mf_server_retire(mf_server* srv, int run, double* state, void* stream);
+int mf_server_active(const mf_server* srv);
 
 /* Problem set-up on host fabs (PhysProblem::initialize):
    Orszag-Tang vortex (problems/OrszagF.ChF:27-79) and the synthetic

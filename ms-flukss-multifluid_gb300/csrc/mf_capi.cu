@@ -25,6 +25,7 @@ using mf::CopyReg;
 using mf::DevParams;
 using mf::DtPartial;
 using mf::StageBuffers;
+using mf::RunParams;
 using mf::StageDesc;
 using mf::StepState;
 
@@ -376,6 +377,7 @@ const char* mf_status_string(mf_status s) {
     case MF_ERR_CUDA: return "CUDA error";
     case MF_ERR_UNSUPPORTED: return "unsupported option";
     case MF_ERR_SCRATCH_LIMIT: return "patch exceeds the static scratch of the no-allocation update";
+    case MF_ERR_NO_ROOM: return "no free run slot or arena space";
   }
   return "unknown status";
 }
@@ -468,13 +470,30 @@ static void fill_desc(StageDesc& D, const mf_box& fab, const mf_box& vbox, const
 
 // A batch of one patch: g0 = 0 in the host desc, device desc at dd.  The
 // fab-size check of check_fab keeps every count inside a 32-bit index.
-static mf::Batch single_batch(StageDesc& hd, const StageDesc* dd, int sd) {
+static mf::Batch single_batch(StageDesc& hd, const StageDesc* dd, int sd, const RunParams* runs) {
   mf::Batch b;
   std::memset(&b, 0, sizeof(b));
   mf::batch_offsets(&hd, 1, sd, b);
   b.desc = dd;
+  b.runs = runs;
+  b.nruns = 1;
   mf::batch_default_threads(b);
   return b;
+}
+
+// Descriptor block of a single-patch call (host copy and device copy): the
+// descs of the two stages and the run's parameters, uploaded together.
+struct SingleBlock {
+  StageDesc d[2];
+  RunParams r;
+};
+
+static void single_run(const mf_ctx* c, const mf::Batch& last, RunParams& r) {
+  r = mf::run_params_of(c->dp);
+  r.d0 = 0;
+  r.nd = 1;
+  r.v0 = 0;
+  r.v1 = last.tot_v;
 }
 
 mf_status mf_patch_update(mf_ctx* c, mf_fab* U, const mf_box* valid, double dt, mf_fab* F,
@@ -512,19 +531,23 @@ mf_status mf_patch_update(mf_ctx* c, mf_fab* U, const mf_box* valid, double dt, 
       MF_CHECK_CUDA(c->bn2[d].ensure(rs * box_cells(box_nodes(v2, d))));
     }
   }
-  MF_CHECK_CUDA(c->desc.ensure(sizeof(StageDesc) * 2));
-  MF_CHECK_CUDA(c->hdesc.ensure(sizeof(StageDesc) * 2));
+  MF_CHECK_CUDA(c->desc.ensure(sizeof(SingleBlock)));
+  MF_CHECK_CUDA(c->hdesc.ensure(sizeof(SingleBlock)));
   MF_CHECK_CUDA(c->state.ensure(sizeof(StepState)));
   MF_CHECK_CUDA(c->hstate.ensure(sizeof(StepState)));
   const long long vmax = box_cells(v2);
   const long long nparts = (vmax + 127) / 128 + 1;
   MF_CHECK_CUDA(c->partials.ensure(sizeof(DtPartial) * nparts));
 
-  StageDesc* hd = (StageDesc*)c->hdesc.p;
+  SingleBlock* hb = (SingleBlock*)c->hdesc.p;
+  SingleBlock* db = (SingleBlock*)c->desc.p;
+  StageDesc* hd = hb->d;
   fill_desc(hd[0], U->box, v1, w1);
   fill_desc(hd[1], U->box, v2, w2);
-  StageDesc* dd = (StageDesc*)c->desc.p;
-  mf::Batch b1 = single_batch(hd[0], dd, sd), b2 = single_batch(hd[1], dd + 1, sd);
+  StageDesc* dd = db->d;
+  mf::Batch b1 = single_batch(hd[0], dd, sd, &db->r);
+  mf::Batch b2 = single_batch(hd[1], dd + 1, sd, &db->r);
+  single_run(c, b2, hb->r);
   StepState* hs = (StepState*)c->hstate.p;
   std::memset(hs, 0, sizeof(*hs));
   hs->dt = dt;
@@ -532,7 +555,7 @@ mf_status mf_patch_update(mf_ctx* c, mf_fab* U, const mf_box* valid, double dt, 
   hs->cp = p.dedner_cp;
   hs->cfl = 0.0;
   StepState* ds = (StepState*)c->state.p;
-  MF_CHECK_CUDA(cudaMemcpyAsync(dd, hd, sizeof(StageDesc) * 2, cudaMemcpyHostToDevice, s));
+  MF_CHECK_CUDA(cudaMemcpyAsync(db, hb, sizeof(SingleBlock), cudaMemcpyHostToDevice, s));
   MF_CHECK_CUDA(cudaMemcpyAsync(ds, hs, sizeof(StepState), cudaMemcpyHostToDevice, s));
 
   int nb = 0;
@@ -583,7 +606,7 @@ mf_status mf_patch_update(mf_ctx* c, mf_fab* U, const mf_box* valid, double dt, 
     MF_CHECK_CUDA(
         mf::launch_stage(c->dp, p.precision, B, b2, mf::kStageDt, 1.0, ds, parts, &nb, s));
   }
-  MF_CHECK_CUDA(mf::launch_finalize(c->dp, parts, nb, ds, 0, s));
+  MF_CHECK_CUDA(mf::launch_finalize(c->dp, parts, b2, b2.nt[2], ds, 0, s));
   if (F) {
     const void* f2p[3] = {nullptr, nullptr, nullptr};
     const void* f1p[3] = {nullptr, nullptr, nullptr};
@@ -633,6 +656,20 @@ mf_status mf_patch_update(mf_ctx* c, mf_fab* U, const mf_box* valid, double dt, 
   return flags_status(hs->flags);
 }
 
+mf_status mf_face_fluxes(mf_ctx* c, int dir, int n, const double* wl, const double* wr,
+                         double* f, void* stream) {
+  if (!c || n < 0 || !wl || !wr || !f || dir < 0 || dir >= c->p.space_dim) return MF_ERR_BAD_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  const double ch = c->p.dedner_ch;
+  if (c->p.precision == MF_PREC_MIXED)
+    MF_CHECK_CUDA(mf::launch_face_flux_fast<float>(c->dp, dir, wl, wr, f, n, ch, s));
+  else if (c->p.precision == MF_PREC_FP64_FAST)
+    MF_CHECK_CUDA(mf::launch_face_flux_fast<double>(c->dp, dir, wl, wr, f, n, ch, s));
+  else
+    MF_CHECK_CUDA(mf::launch_face_flux_exact(c->dp, dir, wl, wr, f, n, ch, s));
+  return wait_stream(s, c->timeout);
+}
+
 mf_status mf_compute_dt(mf_ctx* c, const mf_fab* U, const mf_box* box, double* dt,
                         int min_cell[3], void* stream) {
   if (!c || !U || !U->data || !box || box_empty(*box) || !box_contains(U->box, *box))
@@ -641,24 +678,26 @@ mf_status mf_compute_dt(mf_ctx* c, const mf_fab* U, const mf_box* box, double* d
   cudaStream_t s = (cudaStream_t)stream;
   const long long nv = box_cells(*box);
   if (nv >= (1LL << 31) - 1024) return MF_ERR_BAD_ARG;
-  MF_CHECK_CUDA(c->desc.ensure(sizeof(StageDesc) * 2));
-  MF_CHECK_CUDA(c->hdesc.ensure(sizeof(StageDesc) * 2));
+  MF_CHECK_CUDA(c->desc.ensure(sizeof(SingleBlock)));
+  MF_CHECK_CUDA(c->hdesc.ensure(sizeof(SingleBlock)));
   MF_CHECK_CUDA(c->state.ensure(sizeof(StepState)));
   MF_CHECK_CUDA(c->hstate.ensure(sizeof(StepState)));
   MF_CHECK_CUDA(c->partials.ensure(sizeof(DtPartial) * ((nv + 127) / 128 + 1)));
-  StageDesc* hd = (StageDesc*)c->hdesc.p;
+  SingleBlock* hb = (SingleBlock*)c->hdesc.p;
+  SingleBlock* db = (SingleBlock*)c->desc.p;
+  StageDesc* hd = hb->d;
   fill_desc(hd[0], U->box, *box, *box);
-  StageDesc* dd = (StageDesc*)c->desc.p;
-  mf::Batch b = single_batch(hd[0], dd, c->p.space_dim);
+  mf::Batch b = single_batch(hd[0], db->d, c->p.space_dim, &db->r);
+  single_run(c, b, hb->r);
   StepState* hs = (StepState*)c->hstate.p;
   std::memset(hs, 0, sizeof(*hs));
   StepState* ds = (StepState*)c->state.p;
   DtPartial* parts = (DtPartial*)c->partials.p;
-  MF_CHECK_CUDA(cudaMemcpyAsync(dd, hd, sizeof(StageDesc), cudaMemcpyHostToDevice, s));
+  MF_CHECK_CUDA(cudaMemcpyAsync(db, hb, sizeof(SingleBlock), cudaMemcpyHostToDevice, s));
   MF_CHECK_CUDA(cudaMemcpyAsync(ds, hs, sizeof(StepState), cudaMemcpyHostToDevice, s));
   int nb = 0;
   MF_CHECK_CUDA(mf::launch_dt(c->dp, U->data, b, parts, &nb, s));
-  MF_CHECK_CUDA(mf::launch_finalize(c->dp, parts, nb, ds, 0, s));
+  MF_CHECK_CUDA(mf::launch_finalize(c->dp, parts, b, b.nt[2], ds, 0, s));
   MF_CHECK_CUDA(cudaMemcpyAsync(hs, ds, sizeof(StepState), cudaMemcpyDeviceToHost, s));
   mf_status st = wait_stream(s, c->timeout);
   if (st != MF_OK) return st;
@@ -767,31 +806,31 @@ static mf_box box_shift(mf_box b, const std::array<int, 3>& sh) {
 
 // Copy regions of LevelData::exchange: the cells of valid.grow(depth) of each
 // patch that lie in another patch's valid box or in a periodic image of one.
-static void add_regions(const mf_level* L, const mf_params& p, PatchIndex& ix, int depth,
+static void add_regions(const mf::LevelPlan& L, const mf_params& p, PatchIndex& ix, int depth,
                         std::vector<CopyReg>& out) {
   const int sd = p.space_dim;
   const auto shifts = periodic_shifts(p);
-  for (int dp = 0; dp < L->np; ++dp) {
-    const mf_box dst = box_grow(L->valid[dp], depth, sd);
+  for (int dp = 0; dp < L.np; ++dp) {
+    const mf_box dst = box_grow(L.valid[dp], depth, sd);
     int dfn[3];
-    ext3(L->fab[dp], dfn);
+    ext3(L.fab[dp], dfn);
     for (size_t k = 0; k < shifts.size(); ++k) {
       const auto& sh = shifts[k];
       const std::array<int, 3> msh = {-sh[0], -sh[1], -sh[2]};
       ix.query(box_shift(dst, msh), [&](int sp) {
         if (sp == dp && k == 0) return;
-        const mf_box r = box_isect(box_shift(L->valid[sp], sh), dst);
+        const mf_box r = box_isect(box_shift(L.valid[sp], sh), dst);
         if (box_empty(r)) return;
         int sfn[3];
-        ext3(L->fab[sp], sfn);
+        ext3(L.fab[sp], sfn);
         CopyReg R;
-        R.src_off = L->off[sp];
-        R.dst_off = L->off[dp];
+        R.src_off = L.off[sp];
+        R.dst_off = L.off[dp];
         for (int d = 0; d < 3; ++d) {
           R.sfn[d] = sfn[d];
           R.dfn[d] = dfn[d];
-          R.s0[d] = r.lo[d] - sh[d] - L->fab[sp].lo[d];
-          R.d0[d] = r.lo[d] - L->fab[dp].lo[d];
+          R.s0[d] = r.lo[d] - sh[d] - L.fab[sp].lo[d];
+          R.d0[d] = r.lo[d] - L.fab[dp].lo[d];
           R.ext[d] = r.hi[d] - r.lo[d] + 1;
         }
         out.push_back(R);
@@ -808,9 +847,9 @@ static void add_regions(const mf_level* L, const mf_params& p, PatchIndex& ix, i
 // the domain), stage 1 computes it, as the reference does by running stage 1
 // on box.grow(2) (src/PatchMHDAM.cpp:1238-1246).  Cells outside a
 // non-periodic domain side are never computed (ProblemDomain clipping).
-static mf_box stage1_box(const mf_level* L, const mf_params& p, PatchIndex& ix, int i) {
+static mf_box stage1_box(const mf::LevelPlan& L, const mf_params& p, PatchIndex& ix, int i) {
   const int sd = p.space_dim;
-  const mf_box& v = L->valid[i];
+  const mf_box& v = L.valid[i];
   const auto shifts = periodic_shifts(p);
   mf_box g = v;
   for (int d = 0; d < sd; ++d)
@@ -829,7 +868,7 @@ static mf_box stage1_box(const mf_level* L, const mf_params& p, PatchIndex& ix, 
       for (const auto& sh : shifts) {
         const std::array<int, 3> msh = {-sh[0], -sh[1], -sh[2]};
         ix.query(box_shift(slab, msh), [&](int j) {
-          const mf_box r = box_isect(box_shift(L->valid[j], sh), slab);
+          const mf_box r = box_isect(box_shift(L.valid[j], sh), slab);
           if (!box_empty(r)) covered += box_cells(r);
         });
       }
@@ -842,6 +881,79 @@ static mf_box stage1_box(const mf_level* L, const mf_params& p, PatchIndex& ix, 
     }
   return box_and_domain(g, p);
 }
+
+namespace mf {
+
+mf_status build_level_plan(const mf_params& p, int ng, int nc, int npatch, const mf_box* valid,
+                           LevelPlan& L) {
+  if (!valid || npatch <= 0) return MF_ERR_BAD_ARG;
+  const int sd = p.space_dim;
+  for (int d = 0; d < sd; ++d)
+    if (!p.periodic[d] && p.bc_kind != MF_BC_FARFIELD) return MF_ERR_UNSUPPORTED;
+  L = LevelPlan();
+  L.np = npatch;
+  L.valid.assign(valid, valid + npatch);
+  L.fab.resize(npatch);
+  L.off.resize(npatch);
+  mf_box dom;
+  for (int d = 0; d < 3; ++d) {
+    dom.lo[d] = p.domain_lo[d];
+    dom.hi[d] = p.domain_hi[d];
+  }
+  long long off = 0;
+  for (int i = 0; i < npatch; ++i) {
+    const mf_box& v = valid[i];
+    bool bad = box_empty(v) || !box_contains(dom, v);
+    for (int d = sd; d < 3; ++d)
+      if (v.lo[d] != 0 || v.hi[d] != 0) bad = true;
+    if (bad) return MF_ERR_BAD_ARG;
+    L.fab[i] = box_grow(v, ng, sd);
+    L.off[i] = off;
+    off += ((box_cells(L.fab[i]) * nc + 31) / 32) * 32;  // 256-byte aligned fabs
+    L.cells += box_cells(v);
+  }
+  L.total = off;
+  PatchIndex ix;
+  ix.build(L.valid, p);
+  // valid boxes must not overlap
+  for (int i = 0; i < npatch; ++i) {
+    bool overlap = false;
+    ix.query(valid[i], [&](int j) {
+      if (j != i && !box_empty(box_isect(valid[i], valid[j]))) overlap = true;
+    });
+    if (overlap) return MF_ERR_BAD_ARG;
+  }
+  const bool rk2 = (p.time_approximation == MF_TA_RK2);
+  // descs of both stages; face fluxes and Bn of one stage at a time, each
+  // patch's face fab 64-element aligned
+  L.d1.resize(npatch);
+  L.d2.resize(npatch);
+  for (int stg = 0; stg < 2; ++stg) {
+    long long foff[3] = {0, 0, 0}, boff[3] = {0, 0, 0};
+    for (int i = 0; i < npatch; ++i) {
+      StageDesc& D = (stg == 0) ? L.d1[i] : L.d2[i];
+      const mf_box vb = (stg == 0 && rk2) ? stage1_box(L, p, ix, i) : valid[i];
+      fill_desc(D, L.fab[i], vb, box_isect(box_grow(vb, 2, sd), L.fab[i]));
+      D.u_off = L.off[i];
+      for (int d = 0; d < sd; ++d) {
+        const long long nf = box_cells(box_nodes(vb, d));
+        D.f_off[d] = foff[d];
+        D.bn_off[d] = boff[d];
+        foff[d] += ((nf * nc + 63) / 64) * 64;
+        boff[d] += ((nf + 63) / 64) * 64;
+      }
+    }
+    for (int d = 0; d < 3; ++d) {
+      L.fsize[d] = std::max(L.fsize[d], foff[d]);
+      L.bsize[d] = std::max(L.bsize[d], boff[d]);
+    }
+  }
+  add_regions(L, p, ix, ng, L.full);
+  if (rk2) add_regions(L, p, ix, 2, L.two);
+  return MF_OK;
+}
+
+}  // namespace mf
 
 extern "C" {
 
@@ -904,7 +1016,7 @@ static mf_status enqueue_level_step(mf_level* L, int advance, cudaEvent_t* ev = 
         mf::launch_stage(c->dp, p.precision, B, L->b2, mf::kStageDt, 1.0, ds, parts, &nb, s));
     stage_marks(ne);
   }
-  MF_CHECK_CUDA(mf::launch_finalize(c->dp, parts, nb, ds, advance, s));
+  MF_CHECK_CUDA(mf::launch_finalize(c->dp, parts, L->b2, L->b2.nt[2], ds, advance, s));
   mark(4);
   if (nev) *nev = ne;
   return MF_OK;
@@ -946,84 +1058,36 @@ mf_status mf_level_create(mf_ctx* c, int npatch, const mf_box* valid, mf_level**
   *out = nullptr;
   const mf_params& p = c->p;
   const int sd = p.space_dim, nc = c->nc;
-  for (int d = 0; d < sd; ++d)
-    if (!p.periodic[d] && p.bc_kind != MF_BC_FARFIELD) return MF_ERR_UNSUPPORTED;
+  mf::LevelPlan plan;
+  mf_status pst = mf::build_level_plan(p, c->ng, nc, npatch, valid, plan);
+  if (pst != MF_OK) return pst;
   mf_level* L = new (std::nothrow) mf_level();
   if (!L) return MF_ERR_OOM;
   L->ctx = c;
   L->np = npatch;
-  L->valid.assign(valid, valid + npatch);
-  L->fab.resize(npatch);
-  L->off.resize(npatch);
-  mf_box dom;
-  for (int d = 0; d < 3; ++d) {
-    dom.lo[d] = p.domain_lo[d];
-    dom.hi[d] = p.domain_hi[d];
-  }
-  long long off = 0;
-  for (int i = 0; i < npatch; ++i) {
-    const mf_box& v = valid[i];
-    bool bad = box_empty(v) || !box_contains(dom, v);
-    for (int d = sd; d < 3; ++d)
-      if (v.lo[d] != 0 || v.hi[d] != 0) bad = true;
-    if (bad) {
-      delete L;
-      return MF_ERR_BAD_ARG;
-    }
-    L->fab[i] = box_grow(v, c->ng, sd);
-    L->off[i] = off;
-    off += ((box_cells(L->fab[i]) * nc + 31) / 32) * 32;  // 256-byte aligned fabs
-    L->cells += box_cells(v);
-  }
-  // valid boxes must not overlap
-  for (int i = 0; i < npatch; ++i)
-    for (int j = i + 1; j < npatch; ++j)
-      if (!box_empty(box_isect(valid[i], valid[j]))) {
-        delete L;
-        return MF_ERR_BAD_ARG;
-      }
-  L->total = off;
+  L->valid = plan.valid;
+  L->fab = plan.fab;
+  L->off = plan.off;
+  L->total = plan.total;
+  L->cells = plan.cells;
   const int mixed = (p.precision == MF_PREC_MIXED);
   const size_t rs = mixed ? sizeof(float) : sizeof(double);
-  const bool rk2 = (p.time_approximation == MF_TA_RK2);
-  PatchIndex ix;
-  ix.build(L->valid, p);
-  // descs of both stages; face fluxes and Bn of one stage at a time, each
-  // patch's fab 64-element aligned
-  std::vector<StageDesc> hd(2 * (size_t)npatch);
-  long long fsize[3] = {0, 0, 0}, bsize[3] = {0, 0, 0};
-  for (int stg = 0; stg < 2; ++stg) {
-    long long foff[3] = {0, 0, 0}, boff[3] = {0, 0, 0};
-    for (int i = 0; i < npatch; ++i) {
-      StageDesc& D = hd[(size_t)stg * npatch + i];
-      const mf_box vb = (stg == 0 && rk2) ? stage1_box(L, p, ix, i) : valid[i];
-      fill_desc(D, L->fab[i], vb, box_isect(box_grow(vb, 2, sd), L->fab[i]));
-      D.u_off = L->off[i];
-      for (int d = 0; d < sd; ++d) {
-        const long long nf = box_cells(box_nodes(vb, d));
-        D.f_off[d] = foff[d];
-        D.bn_off[d] = boff[d];
-        foff[d] += ((nf * nc + 63) / 64) * 64;
-        boff[d] += ((nf + 63) / 64) * 64;
-      }
-    }
-    for (int d = 0; d < 3; ++d) {
-      fsize[d] = std::max(fsize[d], foff[d]);
-      bsize[d] = std::max(bsize[d], boff[d]);
-    }
-  }
+  std::vector<StageDesc> hd(plan.d1);
+  hd.insert(hd.end(), plan.d2.begin(), plan.d2.end());
+  const long long* fsize = plan.fsize;
+  const long long* bsize = plan.bsize;
   std::memset(&L->b1, 0, sizeof(L->b1));
   std::memset(&L->b2, 0, sizeof(L->b2));
+  RunParams hrun = mf::run_params_of(c->dp);
   if (!mf::batch_offsets(hd.data(), npatch, sd, L->b1) ||
-      !mf::batch_offsets(hd.data() + npatch, npatch, sd, L->b2)) {
+      !mf::batch_offsets(hd.data() + npatch, npatch, sd, L->b2, &hrun, 1)) {
     delete L;
     return MF_ERR_UNSUPPORTED;  // more than 2^31 cells or faces in one launch
   }
   mf::batch_default_threads(L->b1);
   mf::batch_default_threads(L->b2);
-  std::vector<CopyReg> full, two;
-  add_regions(L, p, ix, c->ng, full);
-  if (rk2) add_regions(L, p, ix, 2, two);
+  const std::vector<CopyReg>& full = plan.full;
+  const std::vector<CopyReg>& two = plan.two;
   L->nfull = (int)full.size();
   L->ntwo = (int)two.size();
   L->nparts = mf::dt_partials(L->b2);
@@ -1045,12 +1109,17 @@ mf_status mf_level_create(mf_ctx* c, int npatch, const mf_box* valid, mf_level**
       if (e == cudaSuccess) e = L->Bn[d].ensure(rs * bsize[d]);
     }
     if (e != cudaSuccess) break;
-    if ((e = L->desc.ensure(sizeof(StageDesc) * hd.size())) != cudaSuccess) break;
-    if ((e = cudaMemcpy(L->desc.p, hd.data(), sizeof(StageDesc) * hd.size(),
-                        cudaMemcpyHostToDevice)) != cudaSuccess)
+    // descs of both stages, then the level's run parameters
+    const size_t dbytes = sizeof(StageDesc) * hd.size();
+    if ((e = L->desc.ensure(dbytes + sizeof(RunParams))) != cudaSuccess) break;
+    if ((e = cudaMemcpy(L->desc.p, hd.data(), dbytes, cudaMemcpyHostToDevice)) != cudaSuccess)
+      break;
+    RunParams* druns = (RunParams*)((char*)L->desc.p + dbytes);
+    if ((e = cudaMemcpy(druns, &hrun, sizeof(RunParams), cudaMemcpyHostToDevice)) != cudaSuccess)
       break;
     L->b1.desc = (const StageDesc*)L->desc.p;
     L->b2.desc = (const StageDesc*)L->desc.p + npatch;
+    L->b1.runs = L->b2.runs = druns;
     if ((e = L->exfull.ensure(sizeof(CopyReg) * std::max<size_t>(1, full.size()))) != cudaSuccess)
       break;
     if (!full.empty() &&
@@ -1212,8 +1281,8 @@ mf_status mf_level_compute_dt(mf_level* L, double* dt, int* min_patch, int min_c
   int nb = 0;
   MF_CHECK_CUDA(
       mf::launch_dt(c->dp, (const double*)L->U.p, L->b2, (DtPartial*)L->partials.p, &nb, L->s));
-  MF_CHECK_CUDA(mf::launch_finalize(c->dp, (const DtPartial*)L->partials.p, nb,
-                                    (StepState*)L->state2.p, 0, L->s));
+  MF_CHECK_CUDA(mf::launch_finalize(c->dp, (const DtPartial*)L->partials.p, L->b2,
+                                    L->b2.nt[2], (StepState*)L->state2.p, 0, L->s));
   MF_CHECK_CUDA(
       cudaMemcpyAsync(hs, L->state2.p, sizeof(StepState), cudaMemcpyDeviceToHost, L->s));
   st = wait_stream(L->s, c->timeout);
@@ -1490,7 +1559,7 @@ mf_status mf_init_helio_host(const mf_params* p, const double* wp, const double*
           u[s + 3] = r * w[3];
           u[s + 4] = w[4] * invhg + 0.5 * r * ke2;
         }
-        if (p->reinit_sphere) mf::exact::reinit_cell(P, i, j, k, u);
+        if (p->reinit_sphere) mf::exact::reinit_cell(P, P.dx, i, j, k, u);
         for (int q = 0; q < U->ncomp; ++q) U->data[hidx(U, i, j, k, q)] = u[q];
       }
   return MF_OK;
@@ -1506,6 +1575,11 @@ CtxView ctx_view(const mf_ctx* c) {
   v.dp = &c->dp;
   v.ng = c->ng;
   v.nc = c->nc;
+  v.timeout = c->timeout;
   return v;
 }
+
+mf_status host_wait(cudaStream_t s, double timeout_s) { return wait_stream(s, timeout_s); }
+
+mf_status status_of_flags(unsigned flags) { return flags_status(flags); }
 }  // namespace mf

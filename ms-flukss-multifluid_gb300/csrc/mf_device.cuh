@@ -52,6 +52,23 @@ struct StepState {
   int pad;
 };
 
+// Values that differ between the runs of one batch (independent simulations,
+// or AMR levels, stepped in shared launches): grid spacing, domain extent in
+// cells, far-field state, and where the run's items sit in the launch.
+struct RunParams {
+  double dx, invdx;
+  int dlo[3], dhi[3];
+  double bc_plasma[8], bc_n1[5];
+  int d0, nd;    // first desc of the run and number of descs
+  int v0, v1;    // flattened valueBox-cell range [v0, v1); v0 is a multiple of kRunAlign
+  int pad;
+};
+
+// Alignment of every run's valueBox-cell range in a flattened launch: no
+// block of the update or dt kernel (<= 256 threads) holds cells of two runs,
+// so block partials of the dt reduction belong to one run.
+constexpr int kRunAlign = 256;
+
 constexpr unsigned kFlagNonFinite = 1u;
 constexpr unsigned kFlagBadDt = 2u;
 
@@ -67,7 +84,7 @@ struct StageDesc {
   // [kRegW] cells of the W box, [kRegF + d] faces in direction d,
   // [kRegV] cells of the valueBox.  Ascending over the batch.
   int g0[5];
-  int pad0;
+  int run;                // index of the run (RunParams / StepState) of this patch
 };
 
 // Per-block partial of the dt reduction.

@@ -16,11 +16,24 @@ cudaError_t launch_flux_fast(const DevParams& P, int dir, const double* w, void*
   const unsigned gf = flat_blocks(tot, nt);
   R* F = (R*)f;
   R* Bn = (R*)bn;
-  if (dir == 0) k_flux<R, 0><<<gf, nt, 0, s>>>(P, w, F, Bn, b.desc, b.ndesc, tot, state);
-  if (dir == 1) k_flux<R, 1><<<gf, nt, 0, s>>>(P, w, F, Bn, b.desc, b.ndesc, tot, state);
-  if (dir == 2) k_flux<R, 2><<<gf, nt, 0, s>>>(P, w, F, Bn, b.desc, b.ndesc, tot, state);
+  if (dir == 0) k_flux<R, 0><<<gf, nt, 0, s>>>(P, w, F, Bn, b.desc, b.ndesc, tot, b.runs, state);
+  if (dir == 1) k_flux<R, 1><<<gf, nt, 0, s>>>(P, w, F, Bn, b.desc, b.ndesc, tot, b.runs, state);
+  if (dir == 2) k_flux<R, 2><<<gf, nt, 0, s>>>(P, w, F, Bn, b.desc, b.ndesc, tot, b.runs, state);
   return cudaGetLastError();
 }
+
+template <typename R>
+cudaError_t launch_face_flux_fast(const DevParams& P, int dir, const double* wl,
+                                  const double* wr, double* f, int n, double ch, cudaStream_t s) {
+  return launch_face_flux_t<R>(P, dir, wl, wr, f, n, ch, s);
+}
+
+template cudaError_t launch_face_flux_fast<double>(const DevParams&, int, const double*,
+                                                   const double*, double*, int, double,
+                                                   cudaStream_t);
+template cudaError_t launch_face_flux_fast<float>(const DevParams&, int, const double*,
+                                                  const double*, double*, int, double,
+                                                  cudaStream_t);
 
 template cudaError_t launch_flux_fast<double>(const DevParams&, int, const double*, void*, void*,
                                               const Batch&, const StepState*, cudaStream_t);

@@ -9,15 +9,42 @@ namespace mf {
 namespace {
 using namespace MF_PHYS;
 
+// Plasma flux of one face with the configured solver.  Mixed-precision
+// guard: the Roe eigenvectors carry factors 1/c and 1/c^2 of the gas sound
+// speed, so where c^2 is far below the magnetic speed^2 (cold, magnetically
+// dominated plasma, e.g. a cell at the pressure floor) the FP32 products in
+// R |Lambda| L dU lose every digit and the flux can be off by orders of
+// magnitude.  There (c^2 < 1e-3 b^2 on either side) the FP32 path takes the
+// Rusanov flux of the same states instead; FP64 keeps the Roe flux.
+template <typename R, int DIR>
+__device__ __forceinline__ void plasma_flux(const DevParams& P, const R* wl, const R* wr, R* g) {
+  bool cold = false;
+  if (sizeof(R) == 4 && P.rs != kRusanov) {
+    const R rl = rmax<R>(R(P.smallr), wl[0]), rr = rmax<R>(R(P.smallr), wr[0]);
+    const R pl = rmax<R>(R(P.smallp), wl[4]), pr = rmax<R>(R(P.smallp), wr[4]);
+    const R a2 = R(P.gamma) * rmin<R>(pl / rl, pr / rr);
+    const R bl = (wl[5] * wl[5] + wl[6] * wl[6] + wl[7] * wl[7]) / rl;
+    const R br = (wr[5] * wr[5] + wr[6] * wr[6] + wr[7] * wr[7]) / rr;
+    cold = a2 < R(1.0e-3) * R(kInv4Pi) * rmax<R>(bl, br);
+  }
+  if (cold || P.rs == kRusanov)
+    rusanov_mhd<R, DIR>(P, wl, wr, g);
+  else if (P.rs == kRoe8)
+    roe_mhd<R, DIR, false>(P, wl, wr, g);
+  else
+    roe_mhd<R, DIR, true>(P, wl, wr, g);
+}
+
 template <typename R, int DIR>
 __global__ void __launch_bounds__(kMaxBlock)
     k_flux(const DevParams P, const double* __restrict__ W, R* __restrict__ F,
            R* __restrict__ Bn, const StageDesc* __restrict__ descs, int ndesc, int total,
-           const StepState* __restrict__ ss) {
+           const RunParams* __restrict__ runs, const StepState* __restrict__ states) {
   const int gi = blockIdx.x * blockDim.x + threadIdx.x;
   if (gi >= total) return;
   const StageDesc& D = descs[find_desc(descs, ndesc, kRegF + DIR, gi)];
   const int lin = gi - D.g0[kRegF + DIR];
+  const RunParams& RP = runs[D.run];
   int fnb[3] = {D.vn[0], D.vn[1], D.vn[2]};
   fnb[DIR] += 1;
   int i, j, k;
@@ -69,15 +96,10 @@ __global__ void __launch_bounds__(kMaxBlock)
     }
   }
   R g[9];
-  if (P.rs == kRoe8)
-    roe_mhd<R, DIR, false>(P, wl, wr, g);
-  else if (P.rs == kRoe7)
-    roe_mhd<R, DIR, true>(P, wl, wr, g);
-  else
-    rusanov_mhd<R, DIR>(P, wl, wr, g);
+  plasma_flux<R, DIR>(P, wl, wr, g);
   if (P.glm) {
     R fbn, fpsi;
-    dedner_2x2<R>(R(ss->ch), wl[5 + DIR], wl[8], wr[5 + DIR], wr[8], fbn, fpsi);
+    dedner_2x2<R>(R(states[D.run].ch), wl[5 + DIR], wl[8], wr[5 + DIR], wr[8], fbn, fpsi);
     g[5 + DIR] = fbn;
     g[8] = fpsi;
   }
@@ -91,8 +113,8 @@ __global__ void __launch_bounds__(kMaxBlock)
     bn = R(0.5) * (wl[5 + DIR] + wr[5 + DIR]);
     if (!P.periodic[DIR]) {
       const int f = (DIR == 0) ? i : (DIR == 1) ? j : k;
-      if (f == P.dlo[DIR]) bn = wr[5 + DIR];
-      if (f == P.dhi[DIR] + 1) bn = wl[5 + DIR];
+      if (f == RP.dlo[DIR]) bn = wr[5 + DIR];
+      if (f == RP.dhi[DIR] + 1) bn = wl[5 + DIR];
     }
   } else if (P.divb_method == 2) {
     const double* wv = w0 + (5 + DIR) * cs;
@@ -118,6 +140,59 @@ __global__ void __launch_bounds__(kMaxBlock)
 #pragma unroll
     for (int m = 0; m < 5; ++m) Fo[(s + m) * fcs] = gn[m];
   }
+}
+
+// Fluxes of given face states (no reconstruction): the plasma solver, the
+// GLM (Bn, psi) system with speed ch and the neutral van Leer fluxes of
+// k_flux, one face per thread.  wl / wr / f: n faces x nc primitive values
+// (fluxes out as FP64).
+template <typename R, int DIR>
+__global__ void __launch_bounds__(128)
+    k_face_flux(const DevParams P, const double* __restrict__ wl, const double* __restrict__ wr,
+                double* __restrict__ f, int n, double ch) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const long long o = (long long)t * P.nc;
+  R L[9], Rt[9], g[9];
+#pragma unroll
+  for (int v = 0; v < 9; ++v) {
+    const bool on = (v < 8) || P.glm;
+    L[v] = on ? R(wl[o + v]) : R(0);
+    Rt[v] = on ? R(wr[o + v]) : R(0);
+  }
+  plasma_flux<R, DIR>(P, L, Rt, g);
+  if (P.glm) {
+    R fbn, fpsi;
+    dedner_2x2<R>(R(ch), L[5 + DIR], L[8], Rt[5 + DIR], Rt[8], fbn, fpsi);
+    g[5 + DIR] = fbn;
+    g[8] = fpsi;
+  }
+#pragma unroll
+  for (int q = 0; q < 8; ++q) f[o + q] = (double)g[q];
+  if (P.glm) f[o + 8] = (double)g[8];
+  for (int fl = 1; fl < P.nf; ++fl) {
+    const int s0 = P.irhon + (fl - 1) * 5;
+    R nl[5], nr[5], gn[5];
+#pragma unroll
+    for (int m = 0; m < 5; ++m) {
+      nl[m] = R(wl[o + s0 + m]);
+      nr[m] = R(wr[o + s0 + m]);
+    }
+    vanleer_euler<R, DIR>(P, nl, nr, gn);
+#pragma unroll
+    for (int m = 0; m < 5; ++m) f[o + s0 + m] = (double)gn[m];
+  }
+}
+
+template <typename R>
+cudaError_t launch_face_flux_t(const DevParams& P, int dir, const double* wl, const double* wr,
+                               double* f, int n, double ch, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  const unsigned g = (unsigned)((n + 127) / 128);
+  if (dir == 0) k_face_flux<R, 0><<<g, 128, 0, s>>>(P, wl, wr, f, n, ch);
+  if (dir == 1) k_face_flux<R, 1><<<g, 128, 0, s>>>(P, wl, wr, f, n, ch);
+  if (dir == 2) k_face_flux<R, 2><<<g, 128, 0, s>>>(P, wl, wr, f, n, ch);
+  return cudaGetLastError();
 }
 
 // ---------------------------------------------------------------------------

@@ -2,7 +2,9 @@
 // (not part of the public C ABI).
 #pragma once
 
-#include "mf_device.cuh"
+#include <vector>
+
+#include "mf_kernels.cuh"
 
 namespace mf {
 
@@ -10,9 +12,35 @@ struct CtxView {
   const mf_params* p;
   const DevParams* dp;
   int ng, nc;
+  double timeout;  // bounded host waits (seconds)
 };
 
 // Parameters, device parameters, ghost width and component count of a context.
 CtxView ctx_view(const mf_ctx* c);
+
+// Bounded host wait for the work enqueued on s (MF_ERR_TIMEOUT after
+// timeout_s seconds), and the status of a step state's error flags.
+mf_status host_wait(cudaStream_t s, double timeout_s);
+mf_status status_of_flags(unsigned flags);
+
+// Host-side plan of a level of patches: fab layout (offsets in doubles from
+// the level's base, every fab 256-byte aligned), the descs of both stages
+// (run 0; face offsets in elements from the face arrays' bases), the face
+// array sizes, and the ghost-exchange regions (LevelData::exchange: all ng
+// layers before a step, 2 layers of the predictor between the RK2 stages).
+struct LevelPlan {
+  int np = 0;
+  std::vector<mf_box> valid, fab;
+  std::vector<long long> off;
+  long long total = 0, cells = 0;
+  std::vector<StageDesc> d1, d2;
+  long long fsize[3] = {0, 0, 0}, bsize[3] = {0, 0, 0};
+  std::vector<CopyReg> full, two;
+};
+
+// MF_ERR_BAD_ARG for empty, overlapping or out-of-domain boxes, boxes with
+// extent in unused dimensions, or a physical side without the far-field BC.
+mf_status build_level_plan(const mf_params& p, int ng, int nc, int npatch, const mf_box* valid,
+                           LevelPlan& out);
 
 }  // namespace mf

@@ -14,6 +14,7 @@
 
 #include <cfloat>
 #include <climits>
+#include <cstring>
 
 #include "mf_device.cuh"
 
@@ -47,16 +48,35 @@ struct Batch {
   int ndesc;
   int tot_w, tot_f[3], tot_v;
   int nt[3];
+  const RunParams* runs;  // device array, nruns entries (StageDesc::run indexes it)
+  int nruns;
 };
 
 constexpr int kMaxBlock = 256;
 
-// Fill the g0 offsets of n host descs and the totals of a Batch.  Returns
-// false when a total does not fit a 32-bit index.
-inline bool batch_offsets(StageDesc* hd, int n, int sd, Batch& b) {
+// Fill the g0 offsets of n host descs and the totals of a Batch.  The descs
+// of one run are consecutive and runs ascend (StageDesc::run); each run's
+// valueBox cells start on a multiple of kRunAlign, and hruns (nruns host
+// entries, nullable for a single run) receive their desc and cell ranges.
+// Returns false when a total does not fit a 32-bit index.
+inline bool batch_offsets(StageDesc* hd, int n, int sd, Batch& b, RunParams* hruns = nullptr,
+                          int nruns = 1) {
   long long t[5] = {0, 0, 0, 0, 0};
+  int cur = -1;
   for (int i = 0; i < n; ++i) {
     StageDesc& D = hd[i];
+    if (D.run != cur) {
+      if (D.run < cur || D.run >= nruns) return false;
+      if (hruns && cur >= 0) hruns[cur].v1 = (int)t[kRegV];
+      t[kRegV] = (t[kRegV] + kRunAlign - 1) / kRunAlign * kRunAlign;
+      for (int r = cur + 1; r <= D.run && hruns; ++r) {
+        hruns[r].d0 = i;
+        hruns[r].nd = 0;
+        hruns[r].v0 = hruns[r].v1 = (int)t[kRegV];
+      }
+      cur = D.run;
+    }
+    if (hruns) hruns[cur].nd += 1;
     long long cnt[5];
     cnt[kRegW] = (long long)D.wn[0] * D.wn[1] * D.wn[2];
     for (int d = 0; d < 3; ++d) {
@@ -70,18 +90,40 @@ inline bool batch_offsets(StageDesc* hd, int n, int sd, Batch& b) {
     }
     cnt[kRegV] = (long long)D.vn[0] * D.vn[1] * D.vn[2];
     for (int k = 0; k < 5; ++k) {
-      if (t[k] > INT_MAX - 1024) return false;
+      if (t[k] > INT_MAX - 4096) return false;
       D.g0[k] = (int)t[k];
       t[k] += cnt[k];
     }
   }
   for (int k = 0; k < 5; ++k)
-    if (t[k] > INT_MAX - 1024) return false;
+    if (t[k] > INT_MAX - 4096) return false;
+  if (hruns && cur >= 0) hruns[cur].v1 = (int)t[kRegV];
+  for (int r = cur + 1; r < nruns && hruns; ++r) {
+    hruns[r].d0 = n;
+    hruns[r].nd = 0;
+    hruns[r].v0 = hruns[r].v1 = (int)t[kRegV];
+  }
   b.ndesc = n;
   b.tot_w = (int)t[kRegW];
   for (int d = 0; d < 3; ++d) b.tot_f[d] = (int)t[kRegF + d];
   b.tot_v = (int)t[kRegV];
+  b.nruns = nruns;
   return true;
+}
+
+// The per-run values of a single run with parameters P.
+inline RunParams run_params_of(const DevParams& P) {
+  RunParams r;
+  std::memset(&r, 0, sizeof(r));
+  r.dx = P.dx;
+  r.invdx = P.invdx;
+  for (int d = 0; d < 3; ++d) {
+    r.dlo[d] = P.dlo[d];
+    r.dhi[d] = P.dhi[d];
+  }
+  for (int q = 0; q < 8; ++q) r.bc_plasma[q] = P.bc_plasma[q];
+  for (int q = 0; q < 5; ++q) r.bc_n1[q] = P.bc_n1[q];
+  return r;
 }
 
 inline void batch_default_threads(Batch& b) { b.nt[0] = b.nt[1] = b.nt[2] = kBlock; }
@@ -140,6 +182,14 @@ cudaError_t launch_update_fast(const DevParams& P, const StageBuffers& B, const 
                                int flags, double dt_scale, StepState* state,
                                DtPartial* partials, int* nblocks_v, cudaStream_t s);
 
+// Riemann fluxes of n given face-state pairs (primitive, nc values each) in
+// the exact or the fast physics (R = float: mixed precision).
+cudaError_t launch_face_flux_exact(const DevParams& P, int dir, const double* wl,
+                                   const double* wr, double* f, int n, double ch, cudaStream_t s);
+template <typename R>
+cudaError_t launch_face_flux_fast(const DevParams& P, int dir, const double* wl,
+                                  const double* wr, double* f, int n, double ch, cudaStream_t s);
+
 // Bytes of one face-flux value for a precision mode (MF_PREC_*).
 inline size_t flux_bytes(int precision) { return precision == MF_PREC_MIXED ? 4 : 8; }
 
@@ -162,10 +212,11 @@ cudaError_t launch_stage(const DevParams& P, int precision, const StageBuffers& 
 cudaError_t launch_dt(const DevParams& P, const double* u, const Batch& b, DtPartial* partials,
                       int* nblocks, cudaStream_t s);
 
-// Reduce the dt partials of the last stage; advance = 1 also writes the next
-// dt (cfl * minimum) and the GLM speeds into *state.
-cudaError_t launch_finalize(const DevParams& P, const DtPartial* partials, int npart,
-                            StepState* state, int advance, cudaStream_t s);
+// Reduce the dt partials of the last stage per run (one block per run, over
+// the run's blocks of a launch with nt threads per block); advance = 1 also
+// writes each run's next dt (cfl * minimum) and GLM speeds into state[run].
+cudaError_t launch_finalize(const DevParams& P, const DtPartial* partials, const Batch& b,
+                            int nt, StepState* state, int advance, cudaStream_t s);
 
 cudaError_t launch_exchange(double* u, const CopyReg* regs, int nreg, int nc, cudaStream_t s);
 

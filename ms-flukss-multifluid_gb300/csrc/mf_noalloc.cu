@@ -181,8 +181,8 @@ extern "C" mf_status mf_patch_update_noalloc(mf_ctx* ctx, mf_fab* U, const mf_bo
       off += up256(rs * nf2[d]);
     }
   }
-  const size_t o_desc = off;
-  off += up256(sizeof(StageDesc) * 2);
+  const size_t o_desc = off;  // two stage descs, then the run's parameters
+  off += up256(sizeof(StageDesc) * 2 + sizeof(mf::RunParams));
   const size_t o_state = off;
   off += up256(sizeof(StepState));
   const long long nparts = (cells(v2) + mf::kBlock - 1) / mf::kBlock + 1;
@@ -198,7 +198,11 @@ extern "C" mf_status mf_patch_update_noalloc(mf_ctx* ctx, mf_fab* U, const mf_bo
 
   // descriptors and step state travel from host stack memory: a copy from
   // pageable memory returns once the data has been taken
-  StageDesc hd[2];
+  struct {
+    StageDesc d[2];
+    mf::RunParams r;
+  } hblk;
+  StageDesc* hd = hblk.d;
   fill(hd[0], U->box, v1, w1);
   fill(hd[1], U->box, v2, w2);
   StepState hs;
@@ -216,9 +220,17 @@ extern "C" mf_status mf_patch_update_noalloc(mf_ctx* ctx, mf_fab* U, const mf_bo
   b2.desc = dd + 1;
   mf::batch_default_threads(b1);
   mf::batch_default_threads(b2);
+  mf::RunParams* druns = (mf::RunParams*)(base + o_desc + sizeof(StageDesc) * 2);
+  b1.runs = b2.runs = druns;
+  b1.nruns = b2.nruns = 1;
+  hblk.r = mf::run_params_of(*cv.dp);
+  hblk.r.d0 = 0;
+  hblk.r.nd = 1;
+  hblk.r.v0 = 0;
+  hblk.r.v1 = b2.tot_v;
   StepState* ds = (StepState*)(base + o_state);
   DtPartial* parts = (DtPartial*)(base + o_parts);
-  NA_CUDA(cudaMemcpyAsync(dd, hd, sizeof(hd), cudaMemcpyHostToDevice, s));
+  NA_CUDA(cudaMemcpyAsync(dd, &hblk, sizeof(hblk), cudaMemcpyHostToDevice, s));
   NA_CUDA(cudaMemcpyAsync(ds, &hs, sizeof(hs), cudaMemcpyHostToDevice, s));
 
   StageBuffers B;
@@ -262,7 +274,7 @@ extern "C" mf_status mf_patch_update_noalloc(mf_ctx* ctx, mf_fab* U, const mf_bo
     B.divb = (divB && divB->data) ? divB->data : nullptr;
     NA_CUDA(mf::launch_stage(*cv.dp, p.precision, B, b2, mf::kStageDt, 1.0, ds, parts, &nb, s));
   }
-  NA_CUDA(mf::launch_finalize(*cv.dp, parts, nb, ds, 0, s));
+  NA_CUDA(mf::launch_finalize(*cv.dp, parts, b2, b2.nt[2], ds, 0, s));
   if (F) {
     const void* f2p[3] = {nullptr, nullptr, nullptr};
     const void* f1p[3] = {nullptr, nullptr, nullptr};

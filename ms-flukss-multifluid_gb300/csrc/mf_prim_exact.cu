@@ -10,12 +10,14 @@ namespace {
 template <int GLM>
 __global__ void __launch_bounds__(kMaxBlock)
     k_prim(const DevParams P, const double* __restrict__ U, double* __restrict__ W,
-           const StageDesc* __restrict__ descs, int ndesc, int total) {
+           const StageDesc* __restrict__ descs, int ndesc, int total,
+           const RunParams* __restrict__ runs) {
   constexpr int IRHON = 8 + GLM;
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= total) return;
   const StageDesc& D = descs[find_desc(descs, ndesc, kRegW, g)];
   const int lin = g - D.g0[kRegW];
+  const RunParams& R = runs[D.run];
   int i, j, k;
   decode(lin, D.wlo, D.wn, i, j, k);
   const long long cs = (long long)D.fn[0] * D.fn[1] * D.fn[2];
@@ -24,7 +26,7 @@ __global__ void __launch_bounds__(kMaxBlock)
   if (P.bc_kind == MF_BC_FARFIELD) {
     const int x[3] = {i, j, k};
     for (int d = 0; d < P.sd; ++d)
-      if (!P.periodic[d] && (x[d] < P.dlo[d] || x[d] > P.dhi[d])) od = d;
+      if (!P.periodic[d] && (x[d] < R.dlo[d] || x[d] > R.dhi[d])) od = d;
   }
   double w[MF_MAX_COMP];
   if (od < 0) {
@@ -42,14 +44,14 @@ __global__ void __launch_bounds__(kMaxBlock)
     // neutral fluid 1 from the boundary state, the other neutral fluids copy the
     // primitive state of the nearest domain cell along the boundary normal.
 #pragma unroll
-    for (int q = 0; q < 8; ++q) w[q] = P.bc_plasma[q];
+    for (int q = 0; q < 8; ++q) w[q] = R.bc_plasma[q];
     if (GLM) w[8] = 0.0;
     if (P.nf > 1) {
 #pragma unroll
-      for (int q = 0; q < 5; ++q) w[IRHON + q] = P.bc_n1[q];
+      for (int q = 0; q < 5; ++q) w[IRHON + q] = R.bc_n1[q];
     }
     int x[3] = {i, j, k};
-    x[od] = (x[od] < P.dlo[od]) ? P.dlo[od] : P.dhi[od];
+    x[od] = (x[od] < R.dlo[od]) ? R.dlo[od] : R.dhi[od];
     const long long eb = D.u_off + loc(D.flo, D.fn, x[0], x[1], x[2]);
 #pragma unroll
     for (int f = 2; f < MF_MAX_FLUIDS; ++f) {
@@ -76,9 +78,9 @@ cudaError_t launch_prim(const DevParams& P, const double* uin, double* w, const 
   const int nt = b.nt[0];
   const unsigned gw = flat_blocks(b.tot_w, nt);
   if (P.glm)
-    k_prim<1><<<gw, nt, 0, s>>>(P, uin, w, b.desc, b.ndesc, b.tot_w);
+    k_prim<1><<<gw, nt, 0, s>>>(P, uin, w, b.desc, b.ndesc, b.tot_w, b.runs);
   else
-    k_prim<0><<<gw, nt, 0, s>>>(P, uin, w, b.desc, b.ndesc, b.tot_w);
+    k_prim<0><<<gw, nt, 0, s>>>(P, uin, w, b.desc, b.ndesc, b.tot_w, b.runs);
   return cudaGetLastError();
 }
 

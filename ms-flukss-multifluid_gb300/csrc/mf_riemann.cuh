@@ -109,7 +109,9 @@ __device__ __forceinline__ void roe_mhd(const DevParams& P, const R* wl, const R
     hyy = BY * ihyz;
     hzz = BZ * ihyz;
     const R szb = cc + (BxBH + BxBH) * iRho;
-    const R h = sqrt(szb * szb - R(4) * cc * bb);
+    // szb^2 - 4 cc bb >= 0 exactly; rounding (FP32 above all) can make it
+    // slightly negative where cc ~ bb and the transverse field is weak
+    const R h = sqrt(rmax<R>(R(0), szb * szb - R(4) * cc * bb));
     aas = R(0.5) * (szb - h);
     if (aas <= R(0)) { aas = R(0); as = R(0); }
     else if (aas >= cc) { aas = cc; as = c; }
@@ -135,13 +137,21 @@ __device__ __forceinline__ void roe_mhd(const DevParams& P, const R* wl, const R
 
   R alf, als;
   const R dfs = aaf - aas;
-  if (dfs < R(1.0e-8)) { alf = R(1); als = R(0); }
+  // Near the triple point (aaf ~ cc ~ aas) cc - aas and aaf - cc are
+  // differences of nearly equal numbers.  The reference's absolute 1e-8
+  // cut-off suits FP64 rounding; in FP32 dfs can sit far above it and still be
+  // rounding noise, so the fast path also treats dfs below a few FP32 ulps of
+  // aaf as degenerate, and renormalises so that alf^2 + als^2 = 1 (the
+  // condition under which the left and right eigenvectors stay inverse).
+  const R dfs_tol = (sizeof(R) == 4) ? rmax<R>(R(1.0e-8), R(4.0e-6) * aaf) : R(1.0e-8);
+  if (dfs < dfs_tol) { alf = R(1); als = R(0); }
   else if ((cc - aas) <= R(0)) { alf = R(0); als = R(1); }
   else if ((aaf - cc) <= R(0)) { alf = R(1); als = R(0); }
   else {
-    const R idfs = R(1) / dfs;
-    alf = sqrt((cc - aas) * idfs);
-    als = sqrt((aaf - cc) * idfs);
+    const R a2f = cc - aas, a2s = aaf - cc;
+    const R inorm = rrsqrt<R>(a2f + a2s);
+    alf = sqrt(a2f) * inorm;
+    als = sqrt(a2s) * inorm;
   }
   const R sih = (BX >= R(0)) ? R(1) : R(-1);
 
@@ -298,7 +308,7 @@ __device__ __forceinline__ void rusanov_mhd(const DevParams& P, const R* wl, con
   }
   const R bb = i4pi * BX2 * iRho;
   const R szb = A2 + (BxBH + BxBH) * iRho;
-  const R h = sqrt(szb * szb - R(4) * A2 * bb);
+  const R h = sqrt(rmax<R>(R(0), szb * szb - R(4) * A2 * bb));
   const R em = rabs<R>(U) + sqrt(R(0.5) * (szb + h));
   g[0] = R(0.5) * (RUL + RUR + em * (RhoL - RhoR));
   g[in] = R(0.5) * ((UL * RUL - BXL_4PI * BXL + PL) + (UR * RUR - BXR_4PI * BXR + PR) + em * (RUL - RUR));

@@ -15,13 +15,13 @@ namespace fast {
 constexpr double kInvPi = 0.318309886183790671537767526745028724;
 
 // DEFINE_REGIONS_2F (swlism/SWLISMF.ChF:654-742), Cartesian branch.
-__device__ __forceinline__ int region_cell(const DevParams& P, int i, int j, int k,
+__device__ __forceinline__ int region_cell(const DevParams& P, double dx, int i, int j, int k,
                                            const double* w) {
-  const double x = __dadd_rn(__dmul_rn(i + 0.5, P.dx), -P.sun_c[0]);
-  const double y = __dadd_rn(__dmul_rn(j + 0.5, P.dx), -P.sun_c[1]);
+  const double x = __dadd_rn(__dmul_rn(i + 0.5, dx), -P.sun_c[0]);
+  const double y = __dadd_rn(__dmul_rn(j + 0.5, dx), -P.sun_c[1]);
   double z = 0.0, r2, invr, ur;
   if (P.sd == 3) {
-    z = __dadd_rn(__dmul_rn(k + 0.5, P.dx), -P.sun_c[2]);
+    z = __dadd_rn(__dmul_rn(k + 0.5, dx), -P.sun_c[2]);
     r2 = __dadd_rn(__dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y)), __dmul_rn(z, z));
     invr = __ddiv_rn(1.0, __dsqrt_rn(r2));
     ur = __dadd_rn(__dadd_rn(__dmul_rn(w[1], __dmul_rn(x, invr)), __dmul_rn(w[2], __dmul_rn(y, invr))),
@@ -159,19 +159,20 @@ __device__ __forceinline__ void charge_exchange_add(const DevParams& P, const do
 // HELIOREINIT_DEFAULT (swlism/HeliosphericPlasmaBCF.ChF:1435-1555) with a
 // monopolar field: the plasma in r <= Rinit becomes the radial wind.  The
 // membership test uses non-fused arithmetic (host and device agree exactly).
-__device__ __host__ inline void reinit_cell(const DevParams& P, int i, int j, int k, double* u) {
+__device__ __host__ inline void reinit_cell(const DevParams& P, double dx, int i, int j, int k,
+                                            double* u) {
 #ifdef __CUDA_ARCH__
-  const double x = __dadd_rn(__dmul_rn(i + 0.5, P.dx), -P.sun_c[0]);
-  const double y = __dadd_rn(__dmul_rn(j + 0.5, P.dx), -P.sun_c[1]);
-  const double z = (P.sd == 3) ? __dadd_rn(__dmul_rn(k + 0.5, P.dx), -P.sun_c[2]) : 0.0;
+  const double x = __dadd_rn(__dmul_rn(i + 0.5, dx), -P.sun_c[0]);
+  const double y = __dadd_rn(__dmul_rn(j + 0.5, dx), -P.sun_c[1]);
+  const double z = (P.sd == 3) ? __dadd_rn(__dmul_rn(k + 0.5, dx), -P.sun_c[2]) : 0.0;
   const double r2 = (P.sd == 3)
                         ? __dadd_rn(__dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y)), __dmul_rn(z, z))
                         : __dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y));
   if (!(r2 <= __dmul_rn(P.r0, P.r0))) return;
 #else
-  const double x = (i + 0.5) * P.dx - P.sun_c[0];
-  const double y = (j + 0.5) * P.dx - P.sun_c[1];
-  const double z = (P.sd == 3) ? (k + 0.5) * P.dx - P.sun_c[2] : 0.0;
+  const double x = (i + 0.5) * dx - P.sun_c[0];
+  const double y = (j + 0.5) * dx - P.sun_c[1];
+  const double z = (P.sd == 3) ? (k + 0.5) * dx - P.sun_c[2] : 0.0;
   const double r2 = (P.sd == 3) ? (x * x + y * y + z * z) : (x * x + y * y);
   if (!(r2 <= P.r0 * P.r0)) return;
 #endif
@@ -179,7 +180,7 @@ __device__ __host__ inline void reinit_cell(const DevParams& P, int i, int j, in
   const double rr = r / P.rint;
   const double xy = sqrt(x * x + y * y);
   const double cosT = z / r;
-  const double sinT = sqrt(1.0 - cosT * cosT);
+  const double sinT = sqrt(fmax(0.0, 1.0 - cosT * cosT));
   const double cosF = x / xy;
   const double sinF = y / xy;
   const double rho = P.sun_rho / (rr * rr);
@@ -286,9 +287,10 @@ __device__ __forceinline__ double max_wave_speed(const DevParams& P, const doubl
     const double as2 = 0.5 * (a2 + invrho * b);
     const double as4 = as2 * as2;
     const double k4 = kInv4Pi * invrho * a2;
-    double umax = fabs(uu) + sqrt(as2 + sqrt(as4 - k4 * bx * bx));
-    umax = fmax(fabs(vv) + sqrt(as2 + sqrt(as4 - k4 * by * by)), umax);
-    umax = fmax(fabs(ww) + sqrt(as2 + sqrt(as4 - k4 * bz * bz)), umax);
+    // as4 - k4 b^2 >= 0 exactly; contracted rounding can push it below 0
+    double umax = fabs(uu) + sqrt(as2 + sqrt(fmax(0.0, as4 - k4 * bx * bx)));
+    umax = fmax(fabs(vv) + sqrt(as2 + sqrt(fmax(0.0, as4 - k4 * by * by))), umax);
+    umax = fmax(fabs(ww) + sqrt(as2 + sqrt(fmax(0.0, as4 - k4 * bz * bz))), umax);
     cmax = fmax(umax, cmax);
   }
 #pragma unroll

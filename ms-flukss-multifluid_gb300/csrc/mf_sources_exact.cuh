@@ -11,13 +11,13 @@ namespace exact {
 
 // ---------------------------------------------------------------------------
 // DEFINE_REGIONS_2F (swlism/SWLISMF.ChF:654-742), Cartesian branch.
-__device__ __forceinline__ int region_cell(const DevParams& P, int i, int j, int k,
+__device__ __forceinline__ int region_cell(const DevParams& P, double dx, int i, int j, int k,
                                            const double* w) {
-  double x = (i + 0.5) * P.dx - P.sun_c[0];
-  double y = (j + 0.5) * P.dx - P.sun_c[1];
+  double x = (i + 0.5) * dx - P.sun_c[0];
+  double y = (j + 0.5) * dx - P.sun_c[1];
   double z = 0.0, r2, invr, ur;
   if (P.sd == 3) {
-    z = (k + 0.5) * P.dx - P.sun_c[2];
+    z = (k + 0.5) * dx - P.sun_c[2];
     r2 = x * x + y * y + z * z;
     invr = 1.0 / sqrt(r2);
     ur = w[1] * (x * invr) + w[2] * (y * invr) + w[3] * (z * invr);
@@ -151,11 +151,12 @@ __device__ __forceinline__ void charge_exchange_add(const DevParams& P, const do
 }
 
 // HELIOREINIT_DEFAULT (swlism/HeliosphericPlasmaBCF.ChF:1435-1555), monopolar field.
-__device__ __host__ inline void reinit_cell(const DevParams& P, int i, int j, int k, double* u) {
-  double x = (i + 0.5) * P.dx - P.sun_c[0];
-  double y = (j + 0.5) * P.dx - P.sun_c[1];
+__device__ __host__ inline void reinit_cell(const DevParams& P, double dx, int i, int j, int k,
+                                            double* u) {
+  double x = (i + 0.5) * dx - P.sun_c[0];
+  double y = (j + 0.5) * dx - P.sun_c[1];
   double z = 0.0;
-  if (P.sd == 3) z = (k + 0.5) * P.dx - P.sun_c[2];
+  if (P.sd == 3) z = (k + 0.5) * dx - P.sun_c[2];
   double r2 = (P.sd == 3) ? (x * x + y * y + z * z) : (x * x + y * y);
   if (!(r2 <= P.r0 * P.r0)) return;
   double r = sqrt(r2);

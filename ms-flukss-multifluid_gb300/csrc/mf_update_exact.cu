@@ -15,14 +15,21 @@ using namespace MF_PHYS;
 template <int GLM>
 __global__ void __launch_bounds__(kMaxBlock)
     k_dt(const DevParams P, const double* __restrict__ U, const StageDesc* __restrict__ descs,
-         int ndesc, int total, DtPartial* __restrict__ partials) {
+         int ndesc, int total, const RunParams* __restrict__ runs,
+         DtPartial* __restrict__ partials) {
   constexpr int IRHON = 8 + GLM;
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
   double dtc = DBL_MAX;
   int myidx = INT_MAX;
+  const StageDesc* Dp = nullptr;
+  int lin = 0;
   if (g < total) {
-    const StageDesc& D = descs[find_desc(descs, ndesc, kRegV, g)];
-    const int lin = g - D.g0[kRegV];
+    Dp = &descs[find_desc(descs, ndesc, kRegV, g)];
+    lin = g - Dp->g0[kRegV];
+    if (lin >= Dp->vn[0] * Dp->vn[1] * Dp->vn[2]) Dp = nullptr;  // run-alignment gap
+  }
+  if (Dp) {
+    const StageDesc& D = *Dp;
     int i, j, k;
     decode(lin, D.vlo, D.vn, i, j, k);
     const long long cs = (long long)D.fn[0] * D.fn[1] * D.fn[2];
@@ -31,7 +38,7 @@ __global__ void __launch_bounds__(kMaxBlock)
 #pragma unroll
     for (int q = 0; q < MF_MAX_COMP; ++q)
       if (q < P.nc) u[q] = U[base + q * cs];
-    dtc = P.dx / max_wave_speed<IRHON>(P, u);
+    dtc = runs[D.run].dx / max_wave_speed<IRHON>(P, u);
     myidx = g;
   }
   block_dt_min(dtc, myidx, descs, ndesc, partials);
@@ -44,14 +51,21 @@ __device__ __forceinline__ bool part_less(const DtPartial& a, const DtPartial& b
   return a.idx < b.idx;
 }
 
+// One block per run: the minimum over the run's block partials, then the
+// run's next dt and GLM speeds (AMRLevelIdealMHD::advance,
+// srcIdeal/AMRLevelIdealMHD.cpp:1531-1548, 1588).
 __global__ void __launch_bounds__(256)
-    k_finalize(const DevParams P, const DtPartial* __restrict__ parts, int np,
-               StepState* __restrict__ ss, int advance) {
+    k_finalize(const DevParams P, const DtPartial* __restrict__ parts,
+               const RunParams* __restrict__ runs, int nt, StepState* __restrict__ states,
+               int advance) {
+  const RunParams& R = runs[blockIdx.x];
+  StepState* __restrict__ ss = states + blockIdx.x;
+  const int p0 = R.v0 / nt, p1 = (R.v1 + nt - 1) / nt;
   DtPartial best;
   best.dt = DBL_MAX;
   best.desc = INT_MAX;
   best.idx = INT_MAX;
-  for (int q = threadIdx.x; q < np; q += blockDim.x) {
+  for (int q = p0 + threadIdx.x; q < p1; q += blockDim.x) {
     DtPartial c = parts[q];
     if (part_less(c, best)) best = c;
   }
@@ -66,17 +80,16 @@ __global__ void __launch_bounds__(256)
   if (threadIdx.x == 0) {
     best = sb[0];
     ss->dt_min = best.dt;
-    ss->min_desc = best.desc;
+    ss->min_desc = (best.desc == INT_MAX) ? INT_MAX : best.desc - R.d0;
     ss->min_idx = best.idx;
     if (!(best.dt > 0.0) || best.dt >= DBL_MAX) atomicOr(&ss->flags, kFlagBadDt);
     if (advance) {
-      // AMRLevelIdealMHD::advance (srcIdeal/AMRLevelIdealMHD.cpp:1531-1548, 1588)
       const double dtn = best.dt;
       ss->dt = ss->cfl * dtn;
       if (P.glm && P.factor_ch > 0.0) {
-        const double ch = P.factor_ch * P.dx / dtn;
+        const double ch = P.factor_ch * R.dx / dtn;
         ss->ch = ch;
-        ss->cp = sqrt(ch * P.dx / P.factor_cp);
+        ss->cp = sqrt(ch * R.dx / P.factor_cp);
       }
     }
   }
@@ -141,8 +154,8 @@ cudaError_t launch_update_exact(const DevParams& P, const StageBuffers& B, const
   const unsigned gv = flat_blocks(b.tot_v, nt);
   if (nblocks_v) *nblocks_v = (int)gv;
 #define MF_UPD(G, FL)                                                                         \
-  k_update<double, G, FL><<<gv, nt, 0, s>>>(P, B, b.desc, b.ndesc, b.tot_v, state, dt_scale, \
-                                            partials)
+  k_update<double, G, FL><<<gv, nt, 0, s>>>(P, B, b.desc, b.ndesc, b.tot_v, b.runs, state, \
+                                            dt_scale, partials)
   if (P.glm) {
     if (flags == 0) MF_UPD(1, 0);
     else if (flags == kStageDt) MF_UPD(1, kStageDt);
@@ -162,15 +175,16 @@ cudaError_t launch_dt(const DevParams& P, const double* u, const Batch& b, DtPar
   const unsigned gv = flat_blocks(b.tot_v, nt);
   if (nblocks) *nblocks = (int)gv;
   if (P.glm)
-    k_dt<1><<<gv, nt, 0, s>>>(P, u, b.desc, b.ndesc, b.tot_v, partials);
+    k_dt<1><<<gv, nt, 0, s>>>(P, u, b.desc, b.ndesc, b.tot_v, b.runs, partials);
   else
-    k_dt<0><<<gv, nt, 0, s>>>(P, u, b.desc, b.ndesc, b.tot_v, partials);
+    k_dt<0><<<gv, nt, 0, s>>>(P, u, b.desc, b.ndesc, b.tot_v, b.runs, partials);
   return cudaGetLastError();
 }
 
-cudaError_t launch_finalize(const DevParams& P, const DtPartial* partials, int npart,
-                            StepState* state, int advance, cudaStream_t s) {
-  k_finalize<<<1, 256, 0, s>>>(P, partials, npart, state, advance);
+cudaError_t launch_finalize(const DevParams& P, const DtPartial* partials, const Batch& b,
+                            int nt, StepState* state, int advance, cudaStream_t s) {
+  if (b.nruns <= 0) return cudaSuccess;
+  k_finalize<<<b.nruns, 256, 0, s>>>(P, partials, b.runs, nt, state, advance);
   return cudaGetLastError();
 }
 

@@ -70,15 +70,24 @@ __device__ __forceinline__ void block_dt_min(double dtc, int myidx,
 template <typename R, int GLM, int FLAGS>
 __global__ void __launch_bounds__(kMaxBlock)
     k_update(const DevParams P, const StageBuffers B, const StageDesc* __restrict__ descs,
-             int ndesc, int total, StepState* __restrict__ ss, const double dt_scale,
+             int ndesc, int total, const RunParams* __restrict__ runs,
+             StepState* __restrict__ states, const double dt_scale,
              DtPartial* __restrict__ partials) {
   constexpr int IRHON = 8 + GLM;
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
   double dtc = DBL_MAX;
   int myidx = INT_MAX;
+  const StageDesc* Dp = nullptr;
+  int lin = 0;
   if (g < total) {
-    const StageDesc& D = descs[find_desc(descs, ndesc, kRegV, g)];
-    const int lin = g - D.g0[kRegV];
+    Dp = &descs[find_desc(descs, ndesc, kRegV, g)];
+    lin = g - Dp->g0[kRegV];
+    if (lin >= Dp->vn[0] * Dp->vn[1] * Dp->vn[2]) Dp = nullptr;  // run-alignment gap
+  }
+  if (Dp) {
+    const StageDesc& D = *Dp;
+    const RunParams& RP = runs[D.run];
+    StepState* __restrict__ ss = states + D.run;
     int i, j, k;
     decode(lin, D.vlo, D.vn, i, j, k);
     const long long cs = (long long)D.fn[0] * D.fn[1] * D.fn[2];
@@ -90,7 +99,7 @@ __global__ void __launch_bounds__(kMaxBlock)
       if (q < P.nc) u[q] = B.uin[base + q * cs];
 
     // UPDATECONS (src/PatchMHDAMF.ChF:542-587), one direction after another
-    const double dtinv = dt * P.invdx;
+    const double dtinv = dt * RP.invdx;
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
       if (d < P.sd) {
@@ -130,7 +139,7 @@ __global__ void __launch_bounds__(kMaxBlock)
         }
       }
       // SOURCE8WAVES (srcIdeal/PatchIdealMHDF.ChF:681-722) + ADDSOURCES
-      const double dtbydx = dt / P.dx;
+      const double dtbydx = dt / RP.dx;
       const double dB = -divB * dtbydx;
       const double Ux = w[1], Uy = w[2], Uz = w[3];
       const double Bx = kInv4Pi * w[5], By = kInv4Pi * w[6], Bz = kInv4Pi * w[7];
@@ -147,10 +156,10 @@ __global__ void __launch_bounds__(kMaxBlock)
       u[8] = exp(-dt * ch * ch / (cp * cp)) * u[8];
     }
     if (P.ce && P.nf >= 2) {
-      const int reg = region_cell(P, i, j, k, w);
+      const int reg = region_cell(P, RP.dx, i, j, k, w);
       charge_exchange_add<IRHON>(P, w, reg, dt, u);
     }
-    if (P.reinit) reinit_cell(P, i, j, k, u);
+    if (P.reinit) reinit_cell(P, RP.dx, i, j, k, u);
     positivity_cell<IRHON>(P, u);
 
     if (FLAGS & kStageAverage) {  // AVERAGESTATE (src/PatchMHDAMF.ChF:289-316)
@@ -167,7 +176,7 @@ __global__ void __launch_bounds__(kMaxBlock)
       }
     if (!finite) atomicOr(&ss->flags, kFlagNonFinite);
     if (FLAGS & kStageDt) {
-      dtc = P.dx / max_wave_speed<IRHON>(P, u);
+      dtc = RP.dx / max_wave_speed<IRHON>(P, u);
       myidx = g;
       if (B.divb && P.use8) B.divb[loc(B.divb_lo, B.divb_n, i, j, k)] = divB;
     }

@@ -28,6 +28,7 @@ MF_ERR_TIMEOUT = 5
 MF_ERR_CUDA = 6
 MF_ERR_UNSUPPORTED = 7
 MF_ERR_SCRATCH_LIMIT = 8
+MF_ERR_NO_ROOM = 9
 NOALLOC_SCRATCH_BYTES = 16 << 20
 
 TA_FIRST_ORDER, TA_HANCOCK, TA_RK2 = 0, 1, 2
@@ -47,6 +48,12 @@ class MfBox(ctypes.Structure):
 
 class MfFab(ctypes.Structure):
     _fields_ = [("data", ctypes.c_void_p), ("box", MfBox), ("ncomp", ctypes.c_int)]
+
+
+class MfRunSpec(ctypes.Structure):
+    _fields_ = [("n", c_int3), ("patch", ctypes.c_int), ("dx", ctypes.c_double),
+                ("cfl", ctypes.c_double), ("bc_plasma", ctypes.c_double * 8),
+                ("bc_neutral1", ctypes.c_double * 5)]
 
 
 class MfParams(ctypes.Structure):
@@ -159,7 +166,24 @@ _SIGS = {
     "mf_level_profile_step": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double,
                                              _P(ctypes.c_float), _P(ctypes.c_int),
                                              _P(ctypes.c_int), ctypes.c_int]),
+    "mf_face_fluxes": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
+                                      ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                      ctypes.c_void_p]),
     "mf_level_autotune": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _P(ctypes.c_int)]),
+    "mf_server_create": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double, ctypes.c_int,
+                                        _P(ctypes.c_void_p)]),
+    "mf_server_destroy": (None, [ctypes.c_void_p]),
+    "mf_server_run_bytes": (ctypes.c_longlong, [ctypes.c_void_p, _P(MfRunSpec)]),
+    "mf_server_free_bytes": (ctypes.c_longlong, [ctypes.c_void_p]),
+    "mf_server_admit": (ctypes.c_int, [ctypes.c_void_p, _P(MfRunSpec), ctypes.c_void_p,
+                                       _P(ctypes.c_int)]),
+    "mf_server_step": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "mf_server_sync": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "mf_server_run_info": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _P(ctypes.c_longlong),
+                                          _P(ctypes.c_double), _P(ctypes.c_int)]),
+    "mf_server_retire": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
+                                        ctypes.c_void_p]),
+    "mf_server_active": (ctypes.c_int, [ctypes.c_void_p]),
     "mf_init_orszag_host": (ctypes.c_int, [_P(MfParams), _P(MfFab), _P(MfBox)]),
     "mf_init_helio_host": (ctypes.c_int, [_P(MfParams), _P(ctypes.c_double), _P(ctypes.c_double),
                                           _P(MfFab), _P(MfBox)]),
@@ -324,7 +348,11 @@ def helio_params(n: int = 128, seed: int = 20240601, time_approximation: int = T
     p.flux = 1
     p.use_8wave = 0
     p.divb_method = 1
-    p.factor_ch = 1.0
+    # mhdam.factorCh (main/MHDAM.cpp:763-767; default 1).  With 1, this problem
+    # grows an odd-even mode in B and psi near the upstream wind front after
+    # t ~ 0.2 in the CPU restatement and on the GPU alike (identical
+    # arithmetic); 0.5 keeps it stable past t = 0.58.
+    p.factor_ch = 0.5
     p.factor_cp = 1.0
     rng = np.random.default_rng(seed)
     p.charge_exchange = 1
@@ -466,6 +494,19 @@ class Context:
         return st, ndt.value, tuple(cell)
 
 
+def face_fluxes(ctx: "Context", direction: int, wl, wr) -> np.ndarray:
+    """mf_face_fluxes on host arrays (n x nc primitive states); returns the
+    n x nc fluxes (copies through the device with torch)."""
+    import torch
+    a = torch.from_numpy(np.ascontiguousarray(wl, dtype=np.float64).reshape(-1, ctx.nc)).cuda()
+    b = torch.from_numpy(np.ascontiguousarray(wr, dtype=np.float64).reshape(-1, ctx.nc)).cuda()
+    f = torch.zeros_like(a)
+    torch.cuda.synchronize()
+    check(ctx.lib.mf_face_fluxes(ctx.h, direction, a.shape[0], a.data_ptr(), b.data_ptr(),
+                                 f.data_ptr(), None), "mf_face_fluxes")
+    return f.cpu().numpy()
+
+
 class Level:
     """Owner of an mf_level: every patch of a level resident on the device."""
 
@@ -571,3 +612,92 @@ class Level:
         t = c_int3()
         check(self.lib.mf_level_autotune(self.h, reps, t), "mf_level_autotune")
         return tuple(t)
+
+
+def run_spec(n, patch, dx, cfl, bc_plasma=None, bc_neutral1=None) -> MfRunSpec:
+    """mf_run_spec of a run on [0, n-1]^d (n: list of 2 or 3 cell counts)."""
+    sp = MfRunSpec()
+    nn = list(n) + [1] * (3 - len(n))
+    for d in range(3):
+        sp.n[d] = int(nn[d])
+    sp.patch = int(patch)
+    sp.dx = float(dx)
+    sp.cfl = float(cfl)
+    if bc_plasma is not None:
+        for q in range(8):
+            sp.bc_plasma[q] = float(bc_plasma[q])
+    if bc_neutral1 is not None:
+        for q in range(5):
+            sp.bc_neutral1[q] = float(bc_neutral1[q])
+    return sp
+
+
+class Server:
+    """Owner of an mf_server: independent runs resident on the device and
+    stepped together in shared launches (see mf_server_* in mf_patch.h)."""
+
+    def __init__(self, ctx: Context, hbm_budget_bytes: float, max_runs: int = 64):
+        self.ctx = ctx
+        self.lib = ctx.lib
+        h = ctypes.c_void_p()
+        check(self.lib.mf_server_create(ctx.h, float(hbm_budget_bytes), int(max_runs),
+                                        ctypes.byref(h)), "mf_server_create")
+        self.h = h
+        self.specs = {}
+
+    def close(self):
+        if self.h:
+            self.lib.mf_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def run_bytes(self, spec: MfRunSpec) -> int:
+        return int(self.lib.mf_server_run_bytes(self.h, ctypes.byref(spec)))
+
+    def admit(self, spec: MfRunSpec, state: np.ndarray):
+        """Returns the run id, or None when there is no room (MF_ERR_NO_ROOM)."""
+        st = np.ascontiguousarray(state, dtype=np.float64)
+        rid = ctypes.c_int(-1)
+        code = self.lib.mf_server_admit(self.h, ctypes.byref(spec), st.ctypes.data,
+                                        ctypes.byref(rid))
+        if code == MF_ERR_NO_ROOM:
+            return None
+        check(code, "mf_server_admit")
+        self.specs[rid.value] = spec
+        return rid.value
+
+    def step(self, stream=None):
+        check(self.lib.mf_server_step(self.h, stream), "mf_server_step")
+
+    def sync(self, stream=None):
+        check(self.lib.mf_server_sync(self.h, stream), "mf_server_sync")
+
+    def info(self, run: int):
+        steps = ctypes.c_longlong()
+        dt = ctypes.c_double()
+        st = ctypes.c_int()
+        check(self.lib.mf_server_run_info(self.h, run, ctypes.byref(steps), ctypes.byref(dt),
+                                          ctypes.byref(st)), "mf_server_run_info")
+        return steps.value, dt.value, st.value
+
+    def retire(self, run: int, want_state: bool = True, stream=None):
+        out = None
+        if want_state:
+            sp = self.specs[run]
+            n = [sp.n[0], sp.n[1], sp.n[2]]
+            shape = (self.ctx.nc, n[2], n[1], n[0]) if self.ctx.p.space_dim == 3 else \
+                (self.ctx.nc, 1, n[1], n[0])
+            out = np.zeros(shape)
+        check(self.lib.mf_server_retire(self.h, run, out.ctypes.data if out is not None else None,
+                                        stream), "mf_server_retire")
+        self.specs.pop(run, None)
+        return out
+
+    def active(self) -> int:
+        return int(self.lib.mf_server_active(self.h))
+

@@ -84,7 +84,7 @@ def test_params_default_and_validation(gpulib):
     q.use_8wave = 1            # GLM with the 8-wave source (main/MHDAM.cpp:1042-1046)
     h = ctypes.c_void_p()
     assert gpulib.mf_create(ctypes.byref(q), ctypes.byref(h)) == mfgpu.MF_ERR_UNSUPPORTED
-    for code in range(8):
+    for code in range(10):
         assert mfgpu.status_string(code) != "unknown status"
 
 
