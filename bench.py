@@ -608,7 +608,7 @@ def run_serving(mfgpu, torch, a):
         eng = serving.Engine(prec, a.serve_budget_gb * 1e9, max_runs=64)
         prepared = {r.rid: eng.spec_state(r) for r in reqs}
         torch.cuda.synchronize()
-        info = eng.serve(reqs, realtime=True, prepared=prepared)
+        info = eng.serve(reqs, prepared=prepared)
         torch.cuda.synchronize()
         summ = serving.summarize(reqs, info["wall_s"])
         summ["iterations"] = info["iterations"]
@@ -621,7 +621,8 @@ def run_serving(mfgpu, torch, a):
                      f"{a.serve_steps} steps each, 2D n in 64..512 (patches 32^2) or 3D n in "
                      "32..128 (patches 16^3), heliosphere physics (plasma + 3 neutral fluids, "
                      "GLM, charge exchange), HBM budget "
-                     f"{a.serve_budget_gb:g} GB per precision, one server per dimension")
+                     f"{a.serve_budget_gb:g} GB per precision, lanes (one server, stream and "
+                     "host thread each): 2D, 3D n<=64, 3D n>64")
     return out
 
 

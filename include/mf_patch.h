@@ -307,6 +307,11 @@ mf_status mf_server_run_info(const mf_server* srv, int run, long long* steps, do
    release its slot and arena ranges. */
 mf_status mf_server_retire(mf_server* srv, int run, double* state, void* stream);
 int mf_server_active(const mf_server* srv);
+/* CUDA stream priority of the server's launches (lower = more urgent,
+   clamped to the device's range): servers of short runs given a higher
+   priority than servers of long runs finish their runs first when both
+   share the GPU. */
+mf_status mf_server_set_priority(mf_server* srv, int priority);
 
 /* Problem set-up on host fabs (PhysProblem::initialize):
    Orszag-Tang vortex (problems/OrszagF.ChF:27-79) and the synthetic

@@ -649,6 +649,21 @@ mf_status mf_server_retire(mf_server* S, int run, double* state, void* stream) {
   return MF_OK;
 }
 
+mf_status mf_server_set_priority(mf_server* S, int priority) {
+  if (!S) return MF_ERR_BAD_ARG;
+  int least = 0, greatest = 0;
+  SV_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+  // greatest is the numerically lowest value (highest priority)
+  const int pr = std::min(least, std::max(greatest, priority));
+  mf_status st = mf::host_wait(S->s, S->cv.timeout);
+  if (st != MF_OK) return st;
+  cudaStream_t ns = nullptr;
+  SV_CUDA(cudaStreamCreateWithPriority(&ns, cudaStreamNonBlocking, pr));
+  cudaStreamDestroy(S->s);
+  S->s = ns;
+  return MF_OK;
+}
+
 int mf_server_active(const mf_server* S) {
   if (!S) return -1;
   int n = 0;

@@ -184,6 +184,7 @@ _SIGS = {
     "mf_server_retire": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
                                         ctypes.c_void_p]),
     "mf_server_active": (ctypes.c_int, [ctypes.c_void_p]),
+    "mf_server_set_priority": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "mf_init_orszag_host": (ctypes.c_int, [_P(MfParams), _P(MfFab), _P(MfBox)]),
     "mf_init_helio_host": (ctypes.c_int, [_P(MfParams), _P(ctypes.c_double), _P(ctypes.c_double),
                                           _P(MfFab), _P(MfBox)]),
@@ -700,4 +701,7 @@ class Server:
 
     def active(self) -> int:
         return int(self.lib.mf_server_active(self.h))
+
+    def set_priority(self, priority: int):
+        check(self.lib.mf_server_set_priority(self.h, int(priority)), "mf_server_set_priority")
 
