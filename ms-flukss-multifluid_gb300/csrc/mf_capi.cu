@@ -139,7 +139,8 @@ mf_status validate_params(const mf_params& p) {
   if (!space_dim_ok(p.space_dim)) return MF_ERR_BAD_ARG;
   if (p.n_fluids < 1 || p.n_fluids > MF_MAX_FLUIDS) return MF_ERR_BAD_ARG;
   if (!(p.gamma > 1.0) || !(p.dx > 0.0)) return MF_ERR_BAD_ARG;
-  if (p.time_approximation != MF_TA_RK2 && p.time_approximation != MF_TA_FIRST_ORDER)
+  if (p.time_approximation != MF_TA_RK2 && p.time_approximation != MF_TA_FIRST_ORDER &&
+      p.time_approximation != MF_TA_HANCOCK)
     return MF_ERR_UNSUPPORTED;
   if (p.precision != MF_PREC_FP64 && p.precision != MF_PREC_MIXED &&
       p.precision != MF_PREC_FP64_FAST)
@@ -297,6 +298,7 @@ struct mf_ctx {
   double time = 0.0;
   double timeout = 600.0;
   DevBuf pred, w, f1[3], bn1[3], f2[3], bn2[3], desc, partials, state;
+  DevBuf fv[3], w2;  // Hancock face values and predicted primitive state
   PinnedBuf hdesc, hstate;
 };
 
@@ -308,6 +310,7 @@ struct mf_level {
   long long total = 0;
   long long cells = 0;
   DevBuf U, U1, W, F[3], Bn[3], desc, exfull, extwo, partials, state, state2;
+  DevBuf FV[3];  // Hancock face values (U1 holds W(t+dt/2))
   int nfull = 0, ntwo = 0;
   // b1: RK2 stage 1 (valid boxes grown on uncovered sides); b2: the stage
   // on the valid boxes (RK2 stage 2, first order).  Descs at desc.p: b1's
@@ -407,7 +410,9 @@ void mf_destroy(mf_ctx* c) {
     c->bn1[d].release();
     c->f2[d].release();
     c->bn2[d].release();
+    c->fv[d].release();
   }
+  c->w2.release();
   c->desc.release();
   c->partials.release();
   c->state.release();
@@ -468,6 +473,16 @@ static void fill_desc(StageDesc& D, const mf_box& fab, const mf_box& vbox, const
   }
 }
 
+// Hancock slope box of a desc and its face-value offsets (fv_off: doubles
+// from the start of each direction's face-value array; null = 0).
+static void set_slope(StageDesc& D, const mf_box& sb, const long long* fv_off) {
+  for (int d = 0; d < 3; ++d) {
+    D.slo[d] = sb.lo[d];
+    D.sn[d] = sb.hi[d] - sb.lo[d] + 1;
+    D.fv_off[d] = fv_off ? fv_off[d] : 0;
+  }
+}
+
 // A batch of one patch: g0 = 0 in the host desc, device desc at dd.  The
 // fab-size check of check_fab keeps every count inside a 32-bit index.
 static mf::Batch single_batch(StageDesc& hd, const StageDesc* dd, int sd, const RunParams* runs) {
@@ -507,11 +522,14 @@ mf_status mf_patch_update(mf_ctx* c, mf_fab* U, const mf_box* valid, double dt, 
   const int mixed = (p.precision == MF_PREC_MIXED);
   const size_t rs = mixed ? sizeof(float) : sizeof(double);
   const bool rk2 = (p.time_approximation == MF_TA_RK2);
+  const bool hk = (p.time_approximation == MF_TA_HANCOCK);
   cudaStream_t s = (cudaStream_t)stream;
   const long long fabn = box_cells(U->box);
 
+  // stage-1 box: RK2 predictor on box.grow(2), Hancock predictor on box.grow(1)
   mf_box v2 = box_and_domain(*valid, p);
-  mf_box v1 = rk2 ? box_and_domain(box_grow(*valid, 2, sd), p) : v2;
+  mf_box v1 = rk2 ? box_and_domain(box_grow(*valid, 2, sd), p)
+                  : hk ? box_and_domain(box_grow(*valid, 1, sd), p) : v2;
   mf_box w1 = box_isect(box_grow(v1, 2, sd), U->box);
   mf_box w2 = box_isect(box_grow(v2, 2, sd), U->box);
   if (divB && divB->data && !box_contains(divB->box, v2)) return MF_ERR_BAD_ARG;
@@ -523,6 +541,12 @@ mf_status mf_patch_update(mf_ctx* c, mf_fab* U, const mf_box* valid, double dt, 
 
   MF_CHECK_CUDA(c->w.ensure(sizeof(double) * fabn * nc));
   if (rk2) MF_CHECK_CUDA(c->pred.ensure(sizeof(double) * fabn * nc));
+  const mf_box s1 = box_grow(v1, 1, sd);  // Hancock slope box
+  if (hk) {
+    MF_CHECK_CUDA(c->w2.ensure(sizeof(double) * fabn * nc));
+    for (int d = 0; d < sd; ++d)
+      MF_CHECK_CUDA(c->fv[d].ensure(sizeof(double) * box_cells(s1) * 2 * nc));
+  }
   for (int d = 0; d < sd; ++d) {
     MF_CHECK_CUDA(c->f1[d].ensure(rs * box_cells(box_nodes(v1, d)) * nc));
     MF_CHECK_CUDA(c->bn1[d].ensure(rs * box_cells(box_nodes(v1, d))));
@@ -544,6 +568,8 @@ mf_status mf_patch_update(mf_ctx* c, mf_fab* U, const mf_box* valid, double dt, 
   StageDesc* hd = hb->d;
   fill_desc(hd[0], U->box, v1, w1);
   fill_desc(hd[1], U->box, v2, w2);
+  if (hk)
+    for (int e = 0; e < 2; ++e) set_slope(hd[e], s1, nullptr);
   StageDesc* dd = db->d;
   mf::Batch b1 = single_batch(hd[0], dd, sd, &db->r);
   mf::Batch b2 = single_batch(hd[1], dd + 1, sd, &db->r);
@@ -589,6 +615,24 @@ mf_status mf_patch_update(mf_ctx* c, mf_fab* U, const mf_box* valid, double dt, 
     }
     MF_CHECK_CUDA(mf::launch_stage(c->dp, p.precision, B, b2, mf::kStageAverage | mf::kStageDt,
                                    0.5, ds, parts, &nb, s));
+  } else if (hk) {
+    B.uin = U->data;
+    B.uout = U->data;
+    for (int d = 0; d < 3; ++d) {
+      B.f[d] = c->f1[d].p;
+      B.bn[d] = c->bn1[d].p;
+    }
+    if (divB && divB->data) {
+      B.divb = divB->data;
+      for (int d = 0; d < 3; ++d) {
+        B.divb_lo[d] = divB->box.lo[d];
+        B.divb_n[d] = divB->box.hi[d] - divB->box.lo[d] + 1;
+      }
+    }
+    mf::HancockBuffers H;
+    for (int d = 0; d < 3; ++d) H.fv[d] = (double*)c->fv[d].p;
+    H.w2 = (double*)c->w2.p;
+    MF_CHECK_CUDA(mf::launch_hancock(c->dp, p.precision, B, H, b1, b2, ds, parts, &nb, s));
   } else {
     B.uin = U->data;
     B.uout = U->data;
@@ -924,16 +968,36 @@ mf_status build_level_plan(const mf_params& p, int ng, int nc, int npatch, const
     if (overlap) return MF_ERR_BAD_ARG;
   }
   const bool rk2 = (p.time_approximation == MF_TA_RK2);
+  const bool hk = (p.time_approximation == MF_TA_HANCOCK);
   // descs of both stages; face fluxes and Bn of one stage at a time, each
-  // patch's face fab 64-element aligned
+  // patch's face fab 64-element aligned.  Hancock: stage 0 is the predictor
+  // on valid.grow(1) & domain (as predictorHancock), stage 1 the corrector.
   L.d1.resize(npatch);
   L.d2.resize(npatch);
+  long long fvo = 0;
   for (int stg = 0; stg < 2; ++stg) {
     long long foff[3] = {0, 0, 0}, boff[3] = {0, 0, 0};
     for (int i = 0; i < npatch; ++i) {
       StageDesc& D = (stg == 0) ? L.d1[i] : L.d2[i];
-      const mf_box vb = (stg == 0 && rk2) ? stage1_box(L, p, ix, i) : valid[i];
+      const mf_box vb = (stg == 0 && rk2)  ? stage1_box(L, p, ix, i)
+                        : (stg == 0 && hk) ? box_and_domain(box_grow(valid[i], 1, sd), p)
+                                           : valid[i];
       fill_desc(D, L.fab[i], vb, box_isect(box_grow(vb, 2, sd), L.fab[i]));
+      if (hk) {
+        if (stg == 0) {
+          const mf_box sb = box_grow(vb, 1, sd);
+          const long long o3[3] = {fvo, fvo, fvo};
+          set_slope(D, sb, o3);
+          fvo += ((box_cells(sb) * 2 * nc + 31) / 32) * 32;
+        } else {
+          const StageDesc& A = L.d1[i];
+          for (int d = 0; d < 3; ++d) {
+            D.slo[d] = A.slo[d];
+            D.sn[d] = A.sn[d];
+            D.fv_off[d] = A.fv_off[d];
+          }
+        }
+      }
       D.u_off = L.off[i];
       for (int d = 0; d < sd; ++d) {
         const long long nf = box_cells(box_nodes(vb, d));
@@ -948,6 +1012,7 @@ mf_status build_level_plan(const mf_params& p, int ng, int nc, int npatch, const
       L.bsize[d] = std::max(L.bsize[d], boff[d]);
     }
   }
+  L.fvsize = fvo;
   add_regions(L, p, ix, ng, L.full);
   if (rk2) add_regions(L, p, ix, 2, L.two);
   return MF_OK;
@@ -1008,6 +1073,21 @@ static mf_status enqueue_level_step(mf_level* L, int advance, cudaEvent_t* ev = 
     MF_CHECK_CUDA(mf::launch_stage(c->dp, p.precision, B, L->b2, mf::kStageAverage | mf::kStageDt,
                                    0.5, ds, parts, &nb, s));
     stage_marks(ne);
+  } else if (p.time_approximation == MF_TA_HANCOCK) {
+    B.uin = (const double*)L->U.p;
+    B.uout = (double*)L->U.p;
+    B.ev = ev ? ev + ne : nullptr;
+    mf::HancockBuffers H;
+    for (int d = 0; d < 3; ++d) H.fv[d] = (double*)L->FV[d].p;
+    H.w2 = (double*)L->U1.p;
+    MF_CHECK_CUDA(mf::launch_hancock(c->dp, p.precision, B, H, L->b1, L->b2, ds, parts, &nb, s));
+    if (ev) {  // prim, faces, predictor, shift, fluxes, update
+      const int k0[4] = {1, 1, 3, 1};
+      for (int q = 0; q < 4; ++q) kinds[ne + q] = k0[q];
+      for (int d = 0; d < sd; ++d) kinds[ne + 4 + d] = 2;
+      kinds[ne + 4 + sd] = 3;
+      ne += mf::hancock_launches(sd);
+    }
   } else {
     B.uin = (const double*)L->U.p;
     B.uout = (double*)L->U.p;
@@ -1099,10 +1179,14 @@ mf_status mf_level_create(mf_ctx* c, int npatch, const mf_box* valid, mf_level**
   do {
     if ((e = L->U.ensure(sizeof(double) * L->total)) != cudaSuccess) break;
     if ((e = cudaMemset(L->U.p, 0, sizeof(double) * L->total)) != cudaSuccess) break;
-    if (p.time_approximation == MF_TA_RK2) {
+    if (p.time_approximation == MF_TA_RK2 || p.time_approximation == MF_TA_HANCOCK) {
       if ((e = L->U1.ensure(sizeof(double) * L->total)) != cudaSuccess) break;
       if ((e = cudaMemset(L->U1.p, 0, sizeof(double) * L->total)) != cudaSuccess) break;
     }
+    if (p.time_approximation == MF_TA_HANCOCK)
+      for (int d = 0; d < sd && e == cudaSuccess; ++d)
+        e = L->FV[d].ensure(sizeof(double) * std::max<long long>(plan.fvsize, 1));
+    if (e != cudaSuccess) break;
     if ((e = L->W.ensure(sizeof(double) * L->total)) != cudaSuccess) break;
     for (int d = 0; d < sd && e == cudaSuccess; ++d) {
       e = L->F[d].ensure(rs * fsize[d]);
@@ -1147,7 +1231,9 @@ mf_status mf_level_create(mf_ctx* c, int npatch, const mf_box* valid, mf_level**
     return st;
   }
   const int per_stage = mf::stage_launches(sd);
-  L->launches = (p.time_approximation == MF_TA_RK2) ? (2 * per_stage + 2 + 1) : (per_stage + 1 + 1);
+  L->launches = (p.time_approximation == MF_TA_RK2) ? (2 * per_stage + 2 + 1)
+                : (p.time_approximation == MF_TA_HANCOCK) ? (mf::hancock_launches(sd) + 1 + 1)
+                                                          : (per_stage + 1 + 1);
   if (L->nfull == 0) L->launches -= 1;
   if (p.time_approximation == MF_TA_RK2 && L->ntwo == 0) L->launches -= 1;
   *out = L;
@@ -1165,6 +1251,7 @@ void mf_level_destroy(mf_level* L) {
   for (int d = 0; d < 3; ++d) {
     L->F[d].release();
     L->Bn[d].release();
+    L->FV[d].release();
   }
   L->desc.release();
   L->exfull.release();

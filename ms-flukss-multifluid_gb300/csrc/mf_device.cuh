@@ -82,9 +82,15 @@ struct StageDesc {
   int wlo[3], wn[3];      // box on which W is computed
   // first index of this patch's items in a flattened launch over a batch:
   // [kRegW] cells of the W box, [kRegF + d] faces in direction d,
-  // [kRegV] cells of the valueBox.  Ascending over the batch.
-  int g0[5];
+  // [kRegV] cells of the valueBox, [kRegS] cells of the slope box.
+  // Ascending over the batch.
+  int g0[6];              // [kRegS]: cells of the slope box (Hancock)
   int run;                // index of the run (RunParams / StepState) of this patch
+  // Hancock: the predictor's slope box (valueBox.grow(1)) and the offsets
+  // (doubles) of the patch's face-value arrays (low then high face value of
+  // every primitive component per cell of the slope box), per direction.
+  int slo[3], sn[3];
+  long long fv_off[3];
 };
 
 // Per-block partial of the dt reduction.

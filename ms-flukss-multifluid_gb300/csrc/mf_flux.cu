@@ -28,6 +28,20 @@ cudaError_t launch_face_flux_fast(const DevParams& P, int dir, const double* wl,
   return launch_face_flux_t<R>(P, dir, wl, wr, f, n, ch, s);
 }
 
+template <typename R>
+cudaError_t launch_hflux_fast(const DevParams& P, int dir, const double* w, const double* fv,
+                              void* f, void* bn, const Batch& b, const StepState* state,
+                              cudaStream_t s) {
+  return launch_hflux_t<R>(P, dir, w, fv, f, bn, b, state, s);
+}
+
+template cudaError_t launch_hflux_fast<double>(const DevParams&, int, const double*,
+                                               const double*, void*, void*, const Batch&,
+                                               const StepState*, cudaStream_t);
+template cudaError_t launch_hflux_fast<float>(const DevParams&, int, const double*,
+                                              const double*, void*, void*, const Batch&,
+                                              const StepState*, cudaStream_t);
+
 template cudaError_t launch_face_flux_fast<double>(const DevParams&, int, const double*,
                                                    const double*, double*, int, double,
                                                    cudaStream_t);

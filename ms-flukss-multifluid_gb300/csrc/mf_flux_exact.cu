@@ -26,4 +26,10 @@ cudaError_t launch_face_flux_exact(const DevParams& P, int dir, const double* wl
   return launch_face_flux_t<double>(P, dir, wl, wr, f, n, ch, s);
 }
 
+cudaError_t launch_hflux_exact(const DevParams& P, int dir, const double* w, const double* fv,
+                               void* f, void* bn, const Batch& b, const StepState* state,
+                               cudaStream_t s) {
+  return launch_hflux_t<double>(P, dir, w, fv, f, bn, b, state, s);
+}
+
 }  // namespace mf

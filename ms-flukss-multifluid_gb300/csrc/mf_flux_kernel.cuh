@@ -142,6 +142,98 @@ __global__ void __launch_bounds__(kMaxBlock)
   }
 }
 
+// Corrector fluxes of the Hancock step (correctorHancock, src/PatchMHDAM.cpp:
+// 1002-1189): the Riemann problem of each face of the valueBox between the
+// high-face value of the low cell and the low-face value of the high cell,
+// both shifted by W(t+dt/2) - W(t); Bn from the same states (recomputed
+// after the shift in predictorHancock, :981-985).  Face values: fv[(side*nc
+// + v)*cells(slope) + cell], side 0 = low face, 1 = high face.
+template <typename R, int DIR>
+__global__ void __launch_bounds__(kMaxBlock)
+    k_hflux(const DevParams P, const double* __restrict__ W, const double* __restrict__ FV,
+            R* __restrict__ F, R* __restrict__ Bn, const StageDesc* __restrict__ descs, int ndesc,
+            int total, const RunParams* __restrict__ runs, const StepState* __restrict__ states) {
+  const int gi = blockIdx.x * blockDim.x + threadIdx.x;
+  if (gi >= total) return;
+  const StageDesc& D = descs[find_desc(descs, ndesc, kRegF + DIR, gi)];
+  const int lin = gi - D.g0[kRegF + DIR];
+  const RunParams& RP = runs[D.run];
+  int fnb[3] = {D.vn[0], D.vn[1], D.vn[2]};
+  fnb[DIR] += 1;
+  int i, j, k;
+  decode(lin, D.vlo, fnb, i, j, k);
+  const long long scs = (long long)D.sn[0] * D.sn[1] * D.sn[2];
+  const double* __restrict__ fv = FV + D.fv_off[DIR];
+  const long long cr = loc(D.slo, D.sn, i, j, k);
+  const long long cl = cr - ((DIR == 0) ? 1 : (DIR == 1) ? (long long)D.sn[0]
+                                                         : (long long)D.sn[0] * D.sn[1]);
+  const int nc = P.nc;
+  const long long fcs = (long long)fnb[0] * fnb[1] * fnb[2];
+  R* __restrict__ Fo = F + D.f_off[DIR] + loc(D.vlo, fnb, i, j, k);
+  R wl[9], wr[9];
+#pragma unroll
+  for (int v = 0; v < 9; ++v) {
+    const bool on = (v < 8) || P.glm;
+    wl[v] = on ? R(fv[(nc + v) * scs + cl]) : R(0);
+    wr[v] = on ? R(fv[v * scs + cr]) : R(0);
+  }
+  R g[9];
+  plasma_flux<R, DIR>(P, wl, wr, g);
+  if (P.glm) {
+    R fbn, fpsi;
+    dedner_2x2<R>(R(states[D.run].ch), wl[5 + DIR], wl[8], wr[5 + DIR], wr[8], fbn, fpsi);
+    g[5 + DIR] = fbn;
+    g[8] = fpsi;
+  }
+#pragma unroll
+  for (int q = 0; q < 8; ++q) Fo[q * fcs] = g[q];
+  if (P.glm) Fo[8 * fcs] = g[8];
+  R bn = R(0);
+  if (P.divb_method == 1) {
+    bn = R(0.5) * (wl[5 + DIR] + wr[5 + DIR]);
+    if (!P.periodic[DIR]) {
+      const int f = (DIR == 0) ? i : (DIR == 1) ? j : k;
+      if (f == RP.dlo[DIR]) bn = wr[5 + DIR];
+      if (f == RP.dhi[DIR] + 1) bn = wl[5 + DIR];
+    }
+  } else if (P.divb_method == 2) {
+    const long long cs = (long long)D.fn[0] * D.fn[1] * D.fn[2];
+    const long long st = (DIR == 0) ? 1 : (DIR == 1) ? (long long)D.fn[0]
+                                                     : (long long)D.fn[0] * D.fn[1];
+    const double* wv = W + D.u_off + loc(D.flo, D.fn, i, j, k) + (5 + DIR) * cs;
+    bn = R(0.5 * (wv[-st] + wv[0]));
+  }
+  Bn[D.bn_off[DIR] + loc(D.vlo, fnb, i, j, k)] = bn;
+  for (int fl = 1; fl < P.nf; ++fl) {
+    const int s0 = P.irhon + (fl - 1) * 5;
+    R nl[5], nr[5], gn[5];
+#pragma unroll
+    for (int m = 0; m < 5; ++m) {
+      nl[m] = R(fv[(nc + s0 + m) * scs + cl]);
+      nr[m] = R(fv[(s0 + m) * scs + cr]);
+    }
+    vanleer_euler<R, DIR>(P, nl, nr, gn);
+#pragma unroll
+    for (int m = 0; m < 5; ++m) Fo[(s0 + m) * fcs] = gn[m];
+  }
+}
+
+template <typename R>
+cudaError_t launch_hflux_t(const DevParams& P, int dir, const double* w, const double* fv,
+                           void* f, void* bn, const Batch& b, const StepState* state,
+                           cudaStream_t s) {
+  const int tot = b.tot_f[dir];
+  if (tot <= 0) return cudaSuccess;
+  const int nt = b.nt[1];
+  const unsigned g = flat_blocks(tot, nt);
+  R* F = (R*)f;
+  R* Bn = (R*)bn;
+  if (dir == 0) k_hflux<R, 0><<<g, nt, 0, s>>>(P, w, fv, F, Bn, b.desc, b.ndesc, tot, b.runs, state);
+  if (dir == 1) k_hflux<R, 1><<<g, nt, 0, s>>>(P, w, fv, F, Bn, b.desc, b.ndesc, tot, b.runs, state);
+  if (dir == 2) k_hflux<R, 2><<<g, nt, 0, s>>>(P, w, fv, F, Bn, b.desc, b.ndesc, tot, b.runs, state);
+  return cudaGetLastError();
+}
+
 // Fluxes of given face states (no reconstruction): the plasma solver, the
 // GLM (Bn, psi) system with speed ch and the neutral van Leer fluxes of
 // k_flux, one face per thread.  wl / wr / f: n faces x nc primitive values

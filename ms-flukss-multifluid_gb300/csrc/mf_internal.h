@@ -35,6 +35,7 @@ struct LevelPlan {
   long long total = 0, cells = 0;
   std::vector<StageDesc> d1, d2;
   long long fsize[3] = {0, 0, 0}, bsize[3] = {0, 0, 0};
+  long long fvsize = 0;  // Hancock face values per direction (doubles)
   std::vector<CopyReg> full, two;
 };
 

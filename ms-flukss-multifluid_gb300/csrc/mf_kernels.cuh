@@ -22,7 +22,7 @@ namespace mf {
 
 constexpr int kBlock = 128;
 
-enum RegionKind : int { kRegW = 0, kRegF = 1, kRegV = 4 };
+enum RegionKind : int { kRegW = 0, kRegF = 1, kRegV = 4, kRegS = 5 };
 
 // Patch whose items contain flattened index g (0 <= g < launch total): the
 // largest d with descs[d].g0[kind] <= g.  Patches with no items share their
@@ -46,7 +46,7 @@ __device__ __forceinline__ int find_desc(const StageDesc* __restrict__ descs, in
 struct Batch {
   const StageDesc* desc;
   int ndesc;
-  int tot_w, tot_f[3], tot_v;
+  int tot_w, tot_f[3], tot_v, tot_s;
   int nt[3];
   const RunParams* runs;  // device array, nruns entries (StageDesc::run indexes it)
   int nruns;
@@ -61,7 +61,7 @@ constexpr int kMaxBlock = 256;
 // Returns false when a total does not fit a 32-bit index.
 inline bool batch_offsets(StageDesc* hd, int n, int sd, Batch& b, RunParams* hruns = nullptr,
                           int nruns = 1) {
-  long long t[5] = {0, 0, 0, 0, 0};
+  long long t[6] = {0, 0, 0, 0, 0, 0};
   int cur = -1;
   for (int i = 0; i < n; ++i) {
     StageDesc& D = hd[i];
@@ -77,8 +77,9 @@ inline bool batch_offsets(StageDesc* hd, int n, int sd, Batch& b, RunParams* hru
       cur = D.run;
     }
     if (hruns) hruns[cur].nd += 1;
-    long long cnt[5];
+    long long cnt[6];
     cnt[kRegW] = (long long)D.wn[0] * D.wn[1] * D.wn[2];
+    cnt[kRegS] = (long long)D.sn[0] * D.sn[1] * D.sn[2];
     for (int d = 0; d < 3; ++d) {
       long long f = 0;
       if (d < sd) {
@@ -89,13 +90,13 @@ inline bool batch_offsets(StageDesc* hd, int n, int sd, Batch& b, RunParams* hru
       cnt[kRegF + d] = f;
     }
     cnt[kRegV] = (long long)D.vn[0] * D.vn[1] * D.vn[2];
-    for (int k = 0; k < 5; ++k) {
+    for (int k = 0; k < 6; ++k) {
       if (t[k] > INT_MAX - 4096) return false;
       D.g0[k] = (int)t[k];
       t[k] += cnt[k];
     }
   }
-  for (int k = 0; k < 5; ++k)
+  for (int k = 0; k < 6; ++k)
     if (t[k] > INT_MAX - 4096) return false;
   if (hruns && cur >= 0) hruns[cur].v1 = (int)t[kRegV];
   for (int r = cur + 1; r < nruns && hruns; ++r) {
@@ -107,6 +108,7 @@ inline bool batch_offsets(StageDesc* hd, int n, int sd, Batch& b, RunParams* hru
   b.tot_w = (int)t[kRegW];
   for (int d = 0; d < 3; ++d) b.tot_f[d] = (int)t[kRegF + d];
   b.tot_v = (int)t[kRegV];
+  b.tot_s = (int)t[kRegS];
   b.nruns = nruns;
   return true;
 }
@@ -229,5 +231,29 @@ cudaError_t launch_flux_out(int mixed, int sd, int nc, const void* const f2[3],
 
 // Number of kernel launches enqueued by launch_stage for sd dimensions.
 inline int stage_launches(int sd) { return 2 + sd; }
+
+// Hancock step (predictorHancock + correctorHancock) of the patches of a
+// (predictor descs: valueBox = box.grow(1) & domain, W box, slope box, face
+// values) and c (corrector descs: valueBox = box & domain, with the same
+// slope boxes and face-value offsets).  fv[d]: face values per direction;
+// w2: the predicted primitive state W(t + dt/2), laid out like W.
+struct HancockBuffers {
+  double* fv[3];
+  double* w2;
+};
+cudaError_t launch_hancock(const DevParams& P, int precision, const StageBuffers& B,
+                           const HancockBuffers& H, const Batch& a, const Batch& c,
+                           StepState* state, DtPartial* partials, int* nblocks_v,
+                           cudaStream_t s);
+inline int hancock_launches(int sd) { return 5 + sd; }
+
+// Corrector fluxes of the Hancock step from the shifted face values.
+cudaError_t launch_hflux_exact(const DevParams& P, int dir, const double* w, const double* fv,
+                               void* f, void* bn, const Batch& b, const StepState* state,
+                               cudaStream_t s);
+template <typename R>
+cudaError_t launch_hflux_fast(const DevParams& P, int dir, const double* w, const double* fv,
+                              void* f, void* bn, const Batch& b, const StepState* state,
+                              cudaStream_t s);
 
 }  // namespace mf

@@ -417,6 +417,7 @@ mf_status mf_server_create(mf_ctx* physics, double hbm_budget_bytes, int max_run
   if (!physics || !out || max_runs <= 0 || max_runs > 4096 || !(hbm_budget_bytes > 0.0))
     return MF_ERR_BAD_ARG;
   *out = nullptr;
+  if (mf::ctx_view(physics).p->time_approximation == MF_TA_HANCOCK) return MF_ERR_UNSUPPORTED;
   mf_server* S = new (std::nothrow) mf_server();
   if (!S) return MF_ERR_OOM;
   S->ctx = physics;

@@ -174,7 +174,8 @@ static int ctx_init(Ctx* c, const mf_params* p) {
       default: c->rs = RS_ROE8; c->aver = 0; break;
     }
   }
-  if (p->time_approximation != MF_TA_FIRST_ORDER && p->time_approximation != MF_TA_RK2)
+  if (p->time_approximation != MF_TA_FIRST_ORDER && p->time_approximation != MF_TA_RK2 &&
+      p->time_approximation != MF_TA_HANCOCK)
     return MF_ERR_UNSUPPORTED;
   return MF_OK;
 }
@@ -1717,6 +1718,283 @@ static int euler_step(const Ctx* c, double time, Fab* U, Fab* F /* [sd] or NULL 
   return MF_OK;
 }
 
+
+/* ------------------------------------------------------------------------ */
+/* Hancock                                                                   */
+/* ------------------------------------------------------------------------ */
+
+/* Reconstruction::faceValues + checkPositivity on slopeBox (as EulerStep):
+   Wm = value on the low face of each cell, Wp on the high face. */
+static void reconstruct_faces(const Ctx* c, const Fab* W, mf_box slopeBox, Fab* Wm, Fab* Wp) {
+  const mf_params* p = c->p;
+  const int np = c->nprim;
+  for (int d = 0; d < c->sd; ++d) {
+    Wm[d] = fab_alloc(slopeBox, np);
+    Wp[d] = fab_alloc(slopeBox, np);
+    int o[3] = {0, 0, 0};
+    o[d] = 1;
+    FOR_BOX(slopeBox, i, j, k) {
+      for (int v = 0; v < np; ++v) {
+        double lo, hi;
+        face_values(limiter_of(c, v), AT(W, i - o[0], j - o[1], k - o[2], v), AT(W, i, j, k, v),
+                    AT(W, i + o[0], j + o[1], k + o[2], v), &lo, &hi);
+        AT(&Wm[d], i, j, k, v) = lo;
+        AT(&Wp[d], i, j, k, v) = hi;
+      }
+    }
+    if (p->check_positivity) {
+      FOR_BOX(slopeBox, i, j, k) {
+        int neg = 0;
+        if (AT(&Wm[d], i, j, k, 0) <= 0.0) neg = 1;
+        if (AT(&Wp[d], i, j, k, 0) <= 0.0) neg = 1;
+        if (AT(&Wm[d], i, j, k, 4) <= 0.0) neg = 1;
+        if (AT(&Wp[d], i, j, k, 4) <= 0.0) neg = 1;
+        if (neg)
+          for (int v = 0; v < np; ++v) {
+            AT(&Wm[d], i, j, k, v) = AT(W, i, j, k, v);
+            AT(&Wp[d], i, j, k, v) = AT(W, i, j, k, v);
+          }
+      }
+    }
+  }
+}
+
+/* PatchMHDMF::computeBn (srcIdeal/PatchMHDMF.cpp:509-620) on the faces fb of
+   direction d: method 1 = average of the two face states (one-sided on
+   non-periodic domain faces), method 2 = central average of W. */
+static void compute_bn(const Ctx* c, const Fab* W, const Fab* Wm, const Fab* Wp, int d, mf_box fb,
+                       Fab* Bn) {
+  const mf_params* p = c->p;
+  int o[3] = {0, 0, 0};
+  o[d] = 1;
+  FOR_BOX(fb, i, j, k) {
+    double wl = AT(Wp, i - o[0], j - o[1], k - o[2], 5 + d);
+    double wr = AT(Wm, i, j, k, 5 + d);
+    int f = (d == 0) ? i : (d == 1) ? j : k;
+    double bn;
+    if (p->divb_method == 2) {
+      bn = 0.5 * (AT(W, i - o[0], j - o[1], k - o[2], 5 + d) + AT(W, i, j, k, 5 + d));
+    } else {
+      bn = 0.5 * (wl + wr);
+      if (!p->periodic[d]) {
+        if (f == p->domain_lo[d]) bn = wr;
+        if (f == p->domain_hi[d] + 1) bn = wl;
+      }
+    }
+    if (p->divb_method == 0) bn = 0.0;
+    AT(Bn, i, j, k, 0) = bn;
+  }
+}
+
+/* FLUXESHANCOCK (srcIdeal/PatchIdealMHDF.ChF:235-297) for the plasma and
+   FLUXESHANCOCK_E (srcIdeal/PatchEulerF.ChF:417-468) for each neutral
+   fluid: the physical flux in direction d of one primitive state.  The psi
+   flux is not set by the reference (FArrayBox::resize leaves it
+   uninitialised); here it is zero. */
+static void hancock_point_flux(const Ctx* c, int d, const double* w, double* F) {
+  const int in = 1 + d, it1 = 1 + (d + 1) % 3, it2 = 1 + (d + 2) % 3;
+  const int inB = 5 + d, itB1 = 5 + (d + 1) % 3, itB2 = 5 + (d + 2) % 3;
+  double rho = w[0] > c->smallr ? w[0] : c->smallr;
+  double u = w[in], v = w[it1], ww = w[it2];
+  double pr = w[4] > c->smallp ? w[4] : c->smallp;
+  double bx = w[inB], by = w[itB1], bz = w[itB2];
+  double b = D_1_8PI * (bx * bx + by * by + bz * bz);
+  double ke = 0.5 * (u * u + v * v + ww * ww);
+  double bu = bx * u + by * v + bz * ww;
+  double e = pr * c->invhgamma + rho * ke;
+  pr = pr + b;
+  e = e + b;
+  F[0] = rho * u;
+  F[in] = rho * u * u + pr - D_1_4PI * bx * bx;
+  F[it1] = rho * u * v - D_1_4PI * bx * by;
+  F[it2] = rho * u * ww - D_1_4PI * bx * bz;
+  F[4] = u * (e + pr) - D_1_4PI * bx * bu;
+  F[inB] = 0.0;
+  F[itB1] = u * by - v * bx;
+  F[itB2] = u * bz - ww * bx;
+  if (c->glm) F[8] = 0.0;
+  for (int f = 1; f < c->nf; ++f) {
+    const int s = c->irhon + (f - 1) * 5;
+    double r = w[s] > c->smallr ? w[s] : c->smallr;
+    double un = w[s + 1 + d], vn = w[s + 1 + (d + 1) % 3], wn = w[s + 1 + (d + 2) % 3];
+    double pn = w[s + 4] > c->smallp ? w[s + 4] : c->smallp;
+    double k2 = 0.5 * (un * un + vn * vn + wn * wn);
+    double en = pn * c->invhgamma + r * k2;
+    F[s] = r * un;
+    F[s + 1 + d] = r * un * un + pn;
+    F[s + 1 + (d + 1) % 3] = r * un * vn;
+    F[s + 1 + (d + 2) % 3] = r * un * wn;
+    F[s + 4] = un * (en + pn);
+  }
+}
+
+/* addExplicitSources for PatchMHDMF (srcIdeal/PatchMHDMF.cpp:1149-1389) on
+   box with the primitive state W and face Bn: 8-wave, PSIPARABOLIC, charge
+   exchange (regions from W). */
+static void explicit_sources(const Ctx* c, Fab* U, const Fab* W, Fab* Bn, double dt, mf_box box,
+                             Fab* divBout) {
+  const mf_params* p = c->p;
+  const int sd = c->sd, np = c->nprim;
+  double psicoef = 0.0;
+  if (c->glm) psicoef = exp(-dt * c->dCh * c->dCh / (c->dCp * c->dCp));
+  double dtbydx = dt / p->dx;
+  double S[MF_MAX_COMP], w[MF_MAX_COMP];
+  FOR_BOX(box, i, j, k) {
+    double divB = 0.0;
+    for (int d = 0; d < sd; ++d) {
+      int o[3] = {0, 0, 0};
+      o[d] = 1;
+      divB = divB + AT(&Bn[d], i + o[0], j + o[1], k + o[2], 0) - AT(&Bn[d], i, j, k, 0);
+    }
+    for (int q = 0; q < np; ++q) w[q] = AT(W, i, j, k, q);
+    if (p->use_8wave) {
+      double dB = -divB * dtbydx;
+      double Ux = w[1], Uy = w[2], Uz = w[3];
+      double Bx = D_1_4PI * w[5], By = D_1_4PI * w[6], Bz = D_1_4PI * w[7];
+      S[1] = dB * Bx;
+      S[2] = dB * By;
+      S[3] = dB * Bz;
+      S[4] = dB * (Bx * Ux + By * Uy + Bz * Uz);
+      S[5] = dB * Ux;
+      S[6] = dB * Uy;
+      S[7] = dB * Uz;
+      for (int q = 1; q <= 7; ++q) AT(U, i, j, k, q) = AT(U, i, j, k, q) + S[q];
+      if (divBout && box_in(&divBout->b, i, j, k)) AT(divBout, i, j, k, 0) = divB;
+    }
+    if (c->glm) AT(U, i, j, k, 8) = psicoef * AT(U, i, j, k, 8);
+    if (p->charge_exchange && c->nf >= 2) {
+      int reg = region_cell(c, i, j, k, w);
+      charge_exchange_cell(c, w, reg, dt, S);
+      int iEND = c->irhon + (c->nf - 2) * 5 + 4;
+      for (int q = 1; q <= iEND; ++q) AT(U, i, j, k, q) = AT(U, i, j, k, q) + S[q];
+    }
+  }
+}
+
+static void prim_fab(const Ctx* c, const Fab* U, mf_box WBoxB, Fab* W) {
+  double u[MF_MAX_COMP], w[MF_MAX_COMP];
+  FOR_BOX(WBoxB, i, j, k) {
+    for (int q = 0; q < c->nc; ++q) u[q] = AT(U, i, j, k, q);
+    cons_to_prim_cell(c, u, w);
+    for (int q = 0; q < c->nprim; ++q) AT(W, i, j, k, q) = w[q];
+  }
+  fill_ghost_cells(c, W);
+}
+
+/* updateState, TA_Hancock (src/PatchMHDAM.cpp:1287-1301): predictorHancock
+   (:836-1000) with dt/2 on box.grow(1), then correctorHancock (:1002-1189)
+   with dt on box. */
+static int hancock_step(const Ctx* c, double time, Fab* U, Fab* F, Fab* divBout, double dt,
+                        mf_box a_box) {
+  const mf_params* p = c->p;
+  const int sd = c->sd, nc = c->nc, np = c->nprim;
+  (void)time;
+  mf_box UBox = U->b;
+  mf_box WBoxB = (p->bc_kind == MF_BC_FARFIELD) ? box_and_domain(UBox, p) : UBox;
+  const double dtp = 0.5 * dt;
+
+  /* ---- predictor ---- */
+  Fab W = fab_alloc(UBox, np);
+  prim_fab(c, U, WBoxB, &W);
+  mf_box valueBox = box_and_domain(box_grow(a_box, 1, sd), p);
+  mf_box slopeBox = box_grow(valueBox, 1, sd);
+  Fab Wm[3], Wp[3], Bn[3];
+  reconstruct_faces(c, &W, slopeBox, Wm, Wp);
+  for (int d = 0; d < sd; ++d) {
+    Bn[d] = fab_alloc(box_nodes(valueBox, d), 1);
+    compute_bn(c, &W, &Wm[d], &Wp[d], d, box_nodes(valueBox, d), &Bn[d]);
+  }
+  Fab Up = fab_alloc(UBox, nc);
+  memcpy(Up.p, U->p, sizeof(double) * (size_t)(Up.csz * nc));
+  /* updateHancock -> UPDATECONSHANCOCK (src/PatchMHDAMF.ChF:589-638), one
+     direction after another, every conserved component */
+  double invvol = 1.0 / p->dx;
+  double wm[MF_MAX_COMP], wp[MF_MAX_COMP], fm[MF_MAX_COMP], fp[MF_MAX_COMP];
+  for (int d = 0; d < sd; ++d) {
+    FOR_BOX(valueBox, i, j, k) {
+      for (int v = 0; v < np; ++v) {
+        wm[v] = AT(&Wm[d], i, j, k, v);
+        wp[v] = AT(&Wp[d], i, j, k, v);
+      }
+      hancock_point_flux(c, d, wm, fm);
+      hancock_point_flux(c, d, wp, fp);
+      for (int q = 0; q < nc; ++q)
+        AT(&Up, i, j, k, q) = AT(&Up, i, j, k, q) - dtp * invvol * (fp[q] - fm[q]);
+    }
+  }
+  explicit_sources(c, &Up, &W, Bn, dtp, valueBox, NULL);
+  /* predicted primitive state, then UPDATEVALUESONFACES (:640-661) */
+  Fab Wpr = fab_alloc(UBox, np);
+  prim_fab(c, &Up, WBoxB, &Wpr);
+  for (int d = 0; d < sd; ++d) {
+    FOR_BOX(slopeBox, i, j, k) {
+      for (int v = 0; v < np; ++v) {
+        double aux = AT(&Wpr, i, j, k, v) - AT(&W, i, j, k, v);
+        AT(&Wm[d], i, j, k, v) = AT(&Wm[d], i, j, k, v) + aux;
+        AT(&Wp[d], i, j, k, v) = AT(&Wp[d], i, j, k, v) + aux;
+      }
+    }
+    compute_bn(c, &W, &Wm[d], &Wp[d], d, box_nodes(valueBox, d), &Bn[d]);
+  }
+
+  /* ---- corrector ---- */
+  mf_box vb2 = box_and_domain(a_box, p);
+  Fab Fl[3];
+  double wl[MF_MAX_COMP], wr[MF_MAX_COMP], g[MF_MAX_COMP];
+  for (int d = 0; d < sd; ++d) {
+    mf_box fb = box_nodes(vb2, d);
+    Fl[d] = fab_alloc(fb, nc);
+    int o[3] = {0, 0, 0};
+    o[d] = 1;
+    FOR_BOX(fb, i, j, k) {
+      for (int v = 0; v < np; ++v) {
+        wl[v] = AT(&Wp[d], i - o[0], j - o[1], k - o[2], v);
+        wr[v] = AT(&Wm[d], i, j, k, v);
+      }
+      for (int q = 0; q < nc; ++q) g[q] = NAN;
+      face_flux(c, d, wl, wr, g);
+      for (int q = 0; q < nc; ++q) AT(&Fl[d], i, j, k, q) = g[q];
+    }
+  }
+  /* finalUpdate -> UPDATECONS with the full dt */
+  for (int d = 0; d < sd; ++d) {
+    int o[3] = {0, 0, 0};
+    o[d] = 1;
+    for (int q = 0; q < nc; ++q) {
+      FOR_BOX(vb2, i, j, k) {
+        AT(U, i, j, k, q) = AT(U, i, j, k, q) - dt * invvol *
+                                                    (AT(&Fl[d], i + o[0], j + o[1], k + o[2], q) -
+                                                     AT(&Fl[d], i, j, k, q));
+      }
+    }
+  }
+  explicit_sources(c, U, &Wpr, Bn, dt, vb2, divBout);
+  double u[MF_MAX_COMP];
+  FOR_BOX(vb2, i, j, k) {
+    for (int q = 0; q < nc; ++q) u[q] = AT(U, i, j, k, q);
+    if (p->reinit_sphere) reinit_cell(c, i, j, k, u);
+    positivity_cell(c, u);
+    for (int q = 0; q < nc; ++q) AT(U, i, j, k, q) = u[q];
+  }
+  if (F) {
+    for (int d = 0; d < sd; ++d) {
+      mf_box fb = box_nodes(vb2, d);
+      if (!box_contains(&F[d].b, &fb)) continue;
+      for (int q = 0; q < nc; ++q) FOR_BOX(fb, i, j, k) AT(&F[d], i, j, k, q) = AT(&Fl[d], i, j, k, q);
+    }
+  }
+  for (int d = 0; d < sd; ++d) {
+    fab_free(&Wm[d]);
+    fab_free(&Wp[d]);
+    fab_free(&Bn[d]);
+    fab_free(&Fl[d]);
+  }
+  fab_free(&W);
+  fab_free(&Wpr);
+  fab_free(&Up);
+  return MF_OK;
+}
+
 /* ------------------------------------------------------------------------ */
 /* dt                                                                        */
 /* ------------------------------------------------------------------------ */
@@ -1851,6 +2129,8 @@ int mf_oracle_patch_update(const mf_params* p, double time, mf_fab* Uf, const mf
     for (int d = 0; d < c.sd; ++d) fab_free(&Fp[d]);
     fab_free(&Uold);
     fab_free(&Upred);
+  } else if (p->time_approximation == MF_TA_HANCOCK) {
+    hancock_step(&c, time, &U, pF, pdivB, dt, *valid);
   } else {
     euler_step(&c, time, &U, pF, pdivB, dt, *valid);
   }

@@ -73,7 +73,7 @@ def test_params_default_and_validation(gpulib):
     assert ctx.nc == 24 and ctx.ng == 4
     ctx.close()
     bad = [("space_dim", 4, mfgpu.MF_ERR_BAD_ARG), ("flux", 5, mfgpu.MF_ERR_UNSUPPORTED),
-           ("time_approximation", mfgpu.TA_HANCOCK, mfgpu.MF_ERR_UNSUPPORTED),
+           ("time_approximation", 7, mfgpu.MF_ERR_UNSUPPORTED),
            ("precision", 9, mfgpu.MF_ERR_BAD_ARG)]
     for field, val, code in bad:
         q = mfgpu.orszag_params(16)
