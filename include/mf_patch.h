@@ -134,6 +134,11 @@ typedef struct mf_params {
   int bc_kind;             /* MF_BC_NONE or MF_BC_FARFIELD */
   double bc_plasma[8];     /* far-field plasma primitives rho,u,v,w,p,bx,by,bz */
   double bc_neutral1[5];   /* far-field primitives of neutral fluid 1 */
+  /* characteristic reconstruction of the plasma variables (mhdam.char_reconstruction,
+     Reconstruction::faceValues, src/Reconstruction.cpp:178-203) and its TVD check
+     (mhdam.check_tvd: 1 = the 8 plasma variables, 2 = density and pressure) */
+  int char_reconstruction;
+  int check_tvd;
 } mf_params;
 
 struct mf_ctx;

@@ -146,6 +146,7 @@ mf_status validate_params(const mf_params& p) {
       p.precision != MF_PREC_FP64_FAST)
     return MF_ERR_BAD_ARG;
   if (p.divb_cleaning != 0 && p.divb_cleaning != 5) return MF_ERR_UNSUPPORTED;
+  if (p.check_tvd < 0 || p.check_tvd > 2) return MF_ERR_BAD_ARG;
   if (p.divb_cleaning == 5) {
     // main/MHDAM.cpp:1042-1046
     if (p.use_8wave) return MF_ERR_UNSUPPORTED;
@@ -191,6 +192,8 @@ DevParams make_dev(const mf_params& p) {
   P.use8 = p.use_8wave ? 1 : 0;
   P.divb_method = p.divb_method;
   P.check_pos = p.check_positivity ? 1 : 0;
+  P.char_rec = p.char_reconstruction ? 1 : 0;
+  P.check_tvd = p.check_tvd;
   P.ce = (p.charge_exchange && p.n_fluids >= 2) ? 1 : 0;
   P.reinit = p.reinit_sphere ? 1 : 0;
   P.bc_kind = p.bc_kind;

@@ -29,6 +29,7 @@ struct DevParams {
   int sd, nf, glm, nc, irhon;
   int rs, aver;
   int use8, divb_method, check_pos, ce, reinit, bc_kind;
+  int char_rec, check_tvd;
   int lim[8];
   int periodic[3], dlo[3], dhi[3];
   double gamma, hgamma, invhgamma, invgamma, smallr, smallp, del2, smallB, dx, invdx;
@@ -208,6 +209,233 @@ __device__ __forceinline__ void face_values(int lim, R wm1, R wp, R wp1, R& lo, 
   }
   lo = wp - slope;
   hi = wp + slope;
+}
+
+}  // namespace mf
+
+namespace mf {
+
+// ---------------------------------------------------------------------------
+// characteristic reconstruction (Reconstruction::faceValues with
+// isCharactistic(), src/Reconstruction.cpp:178-203)
+// ---------------------------------------------------------------------------
+template <typename R>
+__device__ __forceinline__ R minmod3_(R A, R B, R C) {  // reconstructionF.ChF:15-22
+  R signA = copysign(R(1), A);
+  return signA * rmax<R>(R(0), rmin<R>(rabs<R>(A), rmin<R>(signA * B, signA * C)));
+}
+
+// *FACESLOPES of one variable (reconstructionF.ChF: MINMOD :157-178,
+// SUPERBEE :356-392, HARMONIC :526-550, VANALBADA :591-622, MC :664-697,
+// VANLEER :843-880, CD :1081-1096): Sleft/Sright in = left/right
+// differences, out = limited slopes.
+template <typename R>
+__device__ __forceinline__ void face_slopes(int lim, R& Sleft, R& Sright) {
+  const R dSR = Sright, dSL = Sleft;
+  R SLOPE = R(0);
+  switch (lim) {
+    case MF_LIM_CD:
+      Sleft = R(0.5) * Sleft;
+      Sright = R(0.5) * Sright;
+      return;
+    case MF_LIM_SUPERBEE:
+      if (dSL * dSR > R(0)) {
+        const R AR = rabs<R>(dSR), AL = rabs<R>(dSL);
+        if (AL <= R(0.5) * AR) SLOPE = dSL;
+        else if (AL <= AR) SLOPE = R(0.5) * dSR;
+        else if (AL <= AR + AR) SLOPE = R(0.5) * dSL;
+        else SLOPE = dSR;
+      }
+      break;
+    case MF_LIM_HARMONIC:
+      if (dSL * dSR > R(0)) SLOPE = dSR * dSL / (dSL + dSR);
+      break;
+    case MF_LIM_VANALBADA: {
+      const R dSave = R(1.0e-6), dSaveS = dSave + dSave;
+      if (dSL * dSR > R(0))
+        SLOPE = R(0.5) * (dSR * dSL + dSave) * (dSR + dSL) / (dSR * dSR + dSL * dSL + dSaveS);
+      break;
+    }
+    case MF_LIM_MC:
+      if (dSL * dSR > R(0)) {
+        const R AR = rabs<R>(dSR), AL = rabs<R>(dSL);
+        if (R(3) * AL <= AR) SLOPE = dSL;
+        else if (AL <= R(3) * AR) SLOPE = R(0.25) * (dSR + dSL);
+        else SLOPE = dSR;
+      }
+      break;
+    case MF_LIM_VANLEER: {
+      const R dSLim = R(1.0 / 3.0);
+      const R BT = (R(3) - dSLim) / (R(1) - dSLim);
+      const R SL1 = R(0.25) * (R(1) - dSLim);
+      const R SL2 = R(0.25) * (R(1) + dSLim);
+      R SLOPL = R(0), SLOPR = R(0);
+      if (dSL * dSR > R(0)) {
+        const R SL = rmin<R>(rabs<R>(dSR), rabs<R>(BT * dSL));
+        const R SR = rmin<R>(rabs<R>(dSL), rabs<R>(BT * dSR));
+        SLOPL = SL1 * SL + SL2 * SR;
+        SLOPR = SL1 * SR + SL2 * SL;
+        if (dSR < R(0)) {
+          SLOPL = -SLOPL;
+          SLOPR = -SLOPR;
+        }
+      }
+      Sleft = SLOPL;
+      Sright = SLOPR;
+      return;
+    }
+    default:
+      SLOPE = R(0.5) * minmod_<R>(dSR, dSL);
+      break;
+  }
+  Sleft = SLOPE;
+  Sright = SLOPE;
+}
+
+// Wave speeds and mixing coefficients at a cell state, as CHARANALYSISF
+// (srcIdeal/PatchIdealMHDF.ChF:1167-1328, dfs cut-off 1e-12) and
+// CHARSYNTHESISF (:1330-1500, cut-off 1e-8) compute them.
+struct CharState {
+  double Rho, cc, c, as, af, alphaF, alphaS, betaY, betaZ, BX;
+};
+
+template <int D>
+__device__ __forceinline__ void char_state(const DevParams& P, const double* w, double dfs_cut,
+                                           CharState& s) {
+  constexpr int inB = 5 + D, itB1 = 5 + (D + 1) % 3, itB2 = 5 + (D + 2) % 3;
+  const double PGas = fmax(P.smallp, w[4]);
+  const double Rho = fmax(P.smallr, w[0]);
+  const double BX = w[inB], BY = w[itB1], BZ = w[itB2];
+  const double cc = P.gamma * PGas / Rho;
+  const double cs = sqrt(cc);
+  const double BX2 = BX * BX, BY2 = BY * BY, BZ2 = BZ * BZ;
+  const double BYZ2 = BY2 + BZ2;
+  const double BxBH = kInv8Pi * (BX2 + BYZ2);
+  const double bb = kInv4Pi * BX2 / Rho;
+  const double b = sqrt(bb);
+  double betaY, betaZ, aaf, aas, af, as;
+  if (BYZ2 < P.smallB * P.smallB) {
+    betaY = kSqrtHalf;
+    betaZ = kSqrtHalf;
+    if (bb > cc) { aaf = bb; aas = cc; af = b; as = cs; }
+    else { aaf = cc; aas = bb; af = cs; as = b; }
+  } else {
+    const double hyz = sqrt(BYZ2);
+    betaY = BY / hyz;
+    betaZ = BZ / hyz;
+    const double szb = cc + (BxBH + BxBH) / Rho;
+    const double h = sqrt(szb * szb - 4.0 * cc * bb);
+    aas = 0.5 * (szb - h);
+    as = sqrt(aas);
+    aaf = 0.5 * (szb + h);
+    af = sqrt(aaf);
+  }
+  const double dfs = aaf - aas;
+  double alphaF, alphaS;
+  if (dfs < dfs_cut) { alphaF = 1.0; alphaS = 0.0; }
+  else if ((cc - aas) <= 0.0) { alphaF = 0.0; alphaS = 1.0; }
+  else if ((aaf - cc) <= 0.0) { alphaF = 1.0; alphaS = 0.0; }
+  else {
+    alphaF = sqrt((cc - aas) / dfs);
+    alphaS = sqrt((aaf - cc) / dfs);
+  }
+  s.Rho = Rho; s.cc = cc; s.c = cs; s.as = as; s.af = af;
+  s.alphaF = alphaF; s.alphaS = alphaS; s.betaY = betaY; s.betaZ = betaZ; s.BX = BX;
+}
+
+// CHARANALYSISF on one slope vector (plasma primitives), in place.
+template <int D>
+__device__ __forceinline__ void char_analysis(const CharState& s, double* dW) {
+  constexpr int in = 1 + D, it1 = 1 + (D + 1) % 3, it2 = 1 + (D + 2) % 3;
+  constexpr int inB = 5 + D, itB1 = 5 + (D + 1) % 3, itB2 = 5 + (D + 2) % 3;
+  const double siBX = copysign(1.0, s.BX);
+  const double dP = dW[4], dRho = dW[0], dUn = dW[in], dUt1 = dW[it1], dUt2 = dW[it2];
+  const double dBn = dW[inB], dBt1 = dW[itB1], dBt2 = dW[itB2];
+  const double Rho = s.Rho, cc = s.cc, betaY = s.betaY, betaZ = s.betaZ;
+  dW[0] = dRho - dP / cc;
+  dW[1] = dBn;
+  double h1 = kSqrtHalf * (betaY * dUt2 - betaZ * dUt1);
+  double h2 = siBX * (betaZ * dBt1 - betaY * dBt2) / (2.0 * sqrt(2.0 * kPi * Rho));
+  dW[2] = h1 + h2;
+  dW[3] = h1 - h2;
+  h1 = dP / (2.0 * Rho * cc);
+  h2 = dUn / (2.0 * cc);
+  const double h3 = (betaY * dBt1 + betaZ * dBt2) / (4.0 * s.c * sqrt(kPi * Rho));
+  const double h4 = siBX * (betaY * dUt1 + betaZ * dUt2) / (2.0 * cc);
+  const double aF = s.alphaF, aS = s.alphaS, af = s.af, as = s.as;
+  dW[4] = aF * (h1 + af * h2) + aS * (h3 - as * h4);
+  dW[5] = aF * (h1 - af * h2) + aS * (h3 + as * h4);
+  dW[6] = aS * (h1 + as * h2) - aF * (h3 - af * h4);
+  dW[7] = aS * (h1 - as * h2) - aF * (h3 + af * h4);
+}
+
+// CHARSYNTHESISF on one vector of wave amplitudes, in place.
+template <int D>
+__device__ __forceinline__ void char_synthesis(const CharState& s, double* dW) {
+  constexpr int in = 1 + D, it1 = 1 + (D + 1) % 3, it2 = 1 + (D + 2) % 3;
+  constexpr int inB = 5 + D, itB1 = 5 + (D + 1) % 3, itB2 = 5 + (D + 2) % 3;
+  const double betaY = s.betaY, betaZ = s.betaZ;
+  const double betaYX = (s.BX < 0.0) ? -betaY : betaY;
+  const double betaZX = (s.BX < 0.0) ? -betaZ : betaZ;
+  const double alpha1 = dW[0], alpha2 = dW[1];
+  const double alpha3 = kSqrtHalf * dW[2], alpha4 = kSqrtHalf * dW[3];
+  const double alpha5 = dW[4], alpha6 = dW[5], alpha7 = dW[6], alpha8 = dW[7];
+  const double alph3p4 = alpha3 + alpha4, alph3m4 = alpha3 - alpha4;
+  const double alph5p6 = alpha5 + alpha6, alph5m6 = alpha5 - alpha6;
+  const double alph7p8 = alpha7 + alpha8, alph7m8 = alpha7 - alpha8;
+  const double aF = s.alphaF, aS = s.alphaS, af = s.af, as = s.as;
+  const double DN = 2.0 * sqrt(kPi * s.Rho);
+  const double HRho = s.Rho * (aF * alph5p6 + aS * alph7p8);
+  const double HU = aS * as * alph5m6 - aF * af * alph7m8;
+  const double HB = s.c * (aS * alph5p6 - aF * alph7p8);
+  dW[0] = alpha1 + HRho;
+  dW[in] = aF * af * alph5m6 + aS * as * alph7m8;
+  dW[it1] = -betaZ * alph3p4 - betaYX * HU;
+  dW[it2] = betaY * alph3p4 - betaZX * HU;
+  dW[4] = s.cc * HRho;
+  dW[inB] = alpha2;
+  dW[itB1] = DN * (betaZX * alph3m4 + betaY * HB);
+  dW[itB2] = DN * (-betaYX * alph3m4 + betaZ * HB);
+}
+
+// Characteristic face values of the 8 plasma variables of one cell from the
+// cells c-1, c, c+1 (FP64): lo = value on the low face, hi on the high face.
+template <int D>
+__device__ __forceinline__ void char_face_values(const DevParams& P, const double* wm1,
+                                                 const double* w0, const double* wp1,
+                                                 double* lo, double* hi) {
+  double SL[8], SR[8];
+#pragma unroll
+  for (int v = 0; v < 8; ++v) {
+    SL[v] = w0[v] - wm1[v];
+    SR[v] = wp1[v] - w0[v];
+  }
+  CharState s;
+  char_state<D>(P, w0, 1.0e-12, s);
+  char_analysis<D>(s, SL);
+  char_analysis<D>(s, SR);
+#pragma unroll
+  for (int v = 0; v < 8; ++v) face_slopes<double>(P.lim[v], SL[v], SR[v]);
+  char_state<D>(P, w0, 1.0e-8, s);
+  char_synthesis<D>(s, SL);
+  char_synthesis<D>(s, SR);
+#pragma unroll
+  for (int v = 0; v < 8; ++v) {
+    lo[v] = w0[v] - SL[v];
+    hi[v] = w0[v] + SR[v];
+  }
+  if (P.check_tvd) {  // CHECKTVD (reconstructionF.ChF:1248-1279)
+#pragma unroll
+    for (int v = 0; v < 8; ++v) {
+      if (P.check_tvd == 1 || v == 0 || v == 4) {
+        const double WP = w0[v];
+        const double dWR = wp1[v] - WP, dWL = WP - wm1[v];
+        const double dSL = WP - lo[v], dSR = hi[v] - WP;
+        lo[v] = WP - minmod3_<double>(dWL, dWR, dSL);
+        hi[v] = WP + minmod3_<double>(dWL, dWR, dSR);
+      }
+    }
+  }
 }
 
 }  // namespace mf

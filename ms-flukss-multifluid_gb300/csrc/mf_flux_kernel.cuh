@@ -61,7 +61,29 @@ __global__ void __launch_bounds__(kMaxBlock)
   // positivity check of rho and p face values (CHECKPOSITIVITY / REDUCEORDER,
   // src/reconstructionF.ChF:1023-1054): first order for the whole cell
   bool negL = false, negR = false;
-  if (P.check_pos) {
+  R wl[9], wr[9];
+  if (P.char_rec) {
+    // characteristic limiting of the plasma variables (FP64 in every mode:
+    // the projections carry 1/c^2), then the same positivity fallback
+    double a8[8], b8[8], c8[8], d8[8], lo8[8], hiL[8], loR[8], hi8[8];
+#pragma unroll
+    for (int v = 0; v < 8; ++v) {
+      const double* wv = w0 + v * cs;
+      a8[v] = wv[-2 * st];
+      b8[v] = wv[-st];
+      c8[v] = wv[0];
+      d8[v] = wv[st];
+    }
+    char_face_values<DIR>(P, a8, b8, c8, lo8, hiL);
+    if (P.check_pos) negL = lo8[0] <= 0.0 || hiL[0] <= 0.0 || lo8[4] <= 0.0 || hiL[4] <= 0.0;
+    char_face_values<DIR>(P, b8, c8, d8, loR, hi8);
+    if (P.check_pos) negR = loR[0] <= 0.0 || hi8[0] <= 0.0 || loR[4] <= 0.0 || hi8[4] <= 0.0;
+#pragma unroll
+    for (int v = 0; v < 8; ++v) {
+      wl[v] = R(negL ? b8[v] : hiL[v]);
+      wr[v] = R(negR ? c8[v] : loR[v]);
+    }
+  } else if (P.check_pos) {
 #pragma unroll
     for (int t = 0; t < 2; ++t) {
       const int v = t ? 4 : 0;
@@ -78,9 +100,9 @@ __global__ void __launch_bounds__(kMaxBlock)
   // plasma (+ psi) face states: left = high-face value of the low cell,
   // right = low-face value of the high cell (Roe8WavesRS::fluxes,
   // src/Roe8WavesRS.cpp:38-78)
-  R wl[9], wr[9];
 #pragma unroll
   for (int v = 0; v < 9; ++v) {
+    if (v < 8 && P.char_rec) continue;
     if (v < 8 || P.glm) {
       const int lim = (v < 8) ? P.lim[v] : (int)MF_LIM_MINMOD;
       const double* wv = w0 + v * cs;

@@ -45,7 +45,21 @@ __global__ void __launch_bounds__(kMaxBlock)
     const long long st = dstride(D.fn, d);
     double* __restrict__ fv = H.fv[d] + D.fv_off[d] + lin;
     bool neg = false;
-    if (P.check_pos) {
+    double clo[8], chi[8];
+    if (P.char_rec) {
+      double a8[8], b8[8], c8[8];
+#pragma unroll
+      for (int v = 0; v < 8; ++v) {
+        const double* wv = w0 + v * cs;
+        a8[v] = wv[-st];
+        b8[v] = wv[0];
+        c8[v] = wv[st];
+      }
+      if (d == 0) char_face_values<0>(P, a8, b8, c8, clo, chi);
+      else if (d == 1) char_face_values<1>(P, a8, b8, c8, clo, chi);
+      else char_face_values<2>(P, a8, b8, c8, clo, chi);
+      if (P.check_pos) neg = clo[0] <= 0.0 || chi[0] <= 0.0 || clo[4] <= 0.0 || chi[4] <= 0.0;
+    } else if (P.check_pos) {
 #pragma unroll
       for (int t = 0; t < 2; ++t) {
         const int v = t ? 4 : 0;
@@ -61,6 +75,9 @@ __global__ void __launch_bounds__(kMaxBlock)
       if (neg) {
         lo = wv[0];
         hi = wv[0];
+      } else if (P.char_rec && v < 8) {
+        lo = clo[v];
+        hi = chi[v];
       } else {
         const int lim = (v < 8) ? P.lim[v] : (int)MF_LIM_MINMOD;
         face_values<double>(lim, wv[-st], wv[0], wv[st], lo, hi);
@@ -72,11 +89,12 @@ __global__ void __launch_bounds__(kMaxBlock)
 }
 
 // FLUXESHANCOCK (srcIdeal/PatchIdealMHDF.ChF:235-297) + FLUXESHANCOCK_E
-// (srcIdeal/PatchEulerF.ChF:417-468): physical flux in direction d of one
+// (srcIdeal/PatchEulerF.ChF:417-468): physical flux in direction D of one
 // primitive state.  The psi flux is unset in the reference; zero here.
-__device__ __forceinline__ void point_flux(const DevParams& P, int d, const double* w, double* F) {
-  const int in = 1 + d, it1 = 1 + (d + 1) % 3, it2 = 1 + (d + 2) % 3;
-  const int inB = 5 + d, itB1 = 5 + (d + 1) % 3, itB2 = 5 + (d + 2) % 3;
+template <int D, int IRHON>
+__device__ __forceinline__ void point_flux(const DevParams& P, const double* w, double* F) {
+  constexpr int in = 1 + D, it1 = 1 + (D + 1) % 3, it2 = 1 + (D + 2) % 3;
+  constexpr int inB = 5 + D, itB1 = 5 + (D + 1) % 3, itB2 = 5 + (D + 2) % 3;
   const double rho = fmax(P.smallr, w[0]);
   const double u = w[in], v = w[it1], ww = w[it2];
   double pr = fmax(P.smallp, w[4]);
@@ -95,19 +113,22 @@ __device__ __forceinline__ void point_flux(const DevParams& P, int d, const doub
   F[inB] = 0.0;
   F[itB1] = u * by - v * bx;
   F[itB2] = u * bz - ww * bx;
-  if (P.glm) F[8] = 0.0;
-  for (int f = 1; f < P.nf; ++f) {
-    const int s = P.irhon + (f - 1) * 5;
-    const double r = fmax(P.smallr, w[s]);
-    const double un = w[s + 1 + d], vn = w[s + 1 + (d + 1) % 3], wn = w[s + 1 + (d + 2) % 3];
-    const double pn = fmax(P.smallp, w[s + 4]);
-    const double k2 = 0.5 * (un * un + vn * vn + wn * wn);
-    const double en = pn * P.invhgamma + r * k2;
-    F[s] = r * un;
-    F[s + 1 + d] = r * un * un + pn;
-    F[s + 1 + (d + 1) % 3] = r * un * vn;
-    F[s + 1 + (d + 2) % 3] = r * un * wn;
-    F[s + 4] = un * (en + pn);
+  if (IRHON == 9) F[8] = 0.0;
+#pragma unroll
+  for (int f = 1; f < MF_MAX_FLUIDS; ++f) {
+    if (f < P.nf) {
+      const int s = IRHON + (f - 1) * 5;
+      const double r = fmax(P.smallr, w[s]);
+      const double un = w[s + 1 + D], vn = w[s + 1 + (D + 1) % 3], wn = w[s + 1 + (D + 2) % 3];
+      const double pn = fmax(P.smallp, w[s + 4]);
+      const double k2 = 0.5 * (un * un + vn * vn + wn * wn);
+      const double en = pn * P.invhgamma + r * k2;
+      F[s] = r * un;
+      F[s + 1 + D] = r * un * un + pn;
+      F[s + 1 + (D + 1) % 3] = r * un * vn;
+      F[s + 1 + (D + 2) % 3] = r * un * wn;
+      F[s + 4] = un * (en + pn);
+    }
   }
 }
 
@@ -124,6 +145,38 @@ __device__ __forceinline__ double face_bn(const DevParams& P, const RunParams& R
     if (f == RP.dhi[d] + 1) bn = wl;
   }
   return bn;
+}
+
+// One direction of the predictor update of a cell: the point fluxes of its
+// two face values, the flux difference with dt/2, and the two face Bn.
+template <int D, int IRHON>
+__device__ __forceinline__ void hpredict_dir(const DevParams& P, const RunParams& RP,
+                                             const StageDesc& Dc, const HancockBuffers& H,
+                                             const double* __restrict__ W, long long base,
+                                             long long cs, long long scs, long long c,
+                                             const int* x, int nc, double dtinv, double* u,
+                                             double& divB) {
+  const double* __restrict__ fv = H.fv[D] + Dc.fv_off[D];
+  double wm[MF_MAX_COMP], wp[MF_MAX_COMP], fm[MF_MAX_COMP], fp[MF_MAX_COMP];
+#pragma unroll
+  for (int v = 0; v < MF_MAX_COMP; ++v)
+    if (v < nc) {
+      wm[v] = fv[v * scs + c];
+      wp[v] = fv[(nc + v) * scs + c];
+    }
+  point_flux<D, IRHON>(P, wm, fm);
+  point_flux<D, IRHON>(P, wp, fp);
+#pragma unroll
+  for (int q = 0; q < MF_MAX_COMP; ++q)
+    if (q < nc) u[q] = u[q] - dtinv * (fp[q] - fm[q]);
+  const long long ss = dstride(Dc.sn, D);
+  const long long fs = dstride(Dc.fn, D);
+  const double* wbn = W + base + (5 + D) * cs;
+  const double bn_lo = face_bn(P, RP, D, x[D], fv[(nc + 5 + D) * scs + c - ss],
+                               fv[(5 + D) * scs + c], wbn[-fs], wbn[0]);
+  const double bn_hi = face_bn(P, RP, D, x[D] + 1, fv[(nc + 5 + D) * scs + c],
+                               fv[(5 + D) * scs + c + ss], wbn[0], wbn[fs]);
+  divB = divB + bn_hi - bn_lo;
 }
 
 template <int GLM>
@@ -147,32 +200,17 @@ __global__ void __launch_bounds__(kMaxBlock)
   const long long c = loc(D.slo, D.sn, i, j, k);
   const int nc = P.nc;
   const double dtp = 0.5 * SS.dt;
-  double u[MF_MAX_COMP], wm[MF_MAX_COMP], wp[MF_MAX_COMP], fm[MF_MAX_COMP], fp[MF_MAX_COMP];
+  double u[MF_MAX_COMP];
 #pragma unroll
   for (int q = 0; q < MF_MAX_COMP; ++q)
     if (q < nc) u[q] = U[base + q * cs];
-  // updateHancock -> UPDATECONSHANCOCK (src/PatchMHDAMF.ChF:589-638)
+  // updateHancock -> UPDATECONSHANCOCK (src/PatchMHDAMF.ChF:589-638), one
+  // direction after another; divB from Bn of the face values (COMPUTEDIVB)
   const double dtinv = dtp * RP.invdx;
   double divB = 0.0;
-  for (int d = 0; d < P.sd; ++d) {
-    const double* __restrict__ fv = H.fv[d] + D.fv_off[d];
-    for (int v = 0; v < nc; ++v) {
-      wm[v] = fv[v * scs + c];
-      wp[v] = fv[(nc + v) * scs + c];
-    }
-    point_flux(P, d, wm, fm);
-    point_flux(P, d, wp, fp);
-    for (int q = 0; q < nc; ++q) u[q] = u[q] - dtinv * (fp[q] - fm[q]);
-    // divB from Bn of the face values (COMPUTEDIVB)
-    const long long ss = dstride(D.sn, d);
-    const long long fs = dstride(D.fn, d);
-    const double* wbn = W + base + (5 + d) * cs;
-    const double bn_lo = face_bn(P, RP, d, x[d], fv[(nc + 5 + d) * scs + c - ss],
-                                 fv[(5 + d) * scs + c], wbn[-fs], wbn[0]);
-    const double bn_hi = face_bn(P, RP, d, x[d] + 1, fv[(nc + 5 + d) * scs + c],
-                                 fv[(5 + d) * scs + c + ss], wbn[0], wbn[fs]);
-    divB = divB + bn_hi - bn_lo;
-  }
+  hpredict_dir<0, IRHON>(P, RP, D, H, W, base, cs, scs, c, x, nc, dtinv, u, divB);
+  if (P.sd > 1) hpredict_dir<1, IRHON>(P, RP, D, H, W, base, cs, scs, c, x, nc, dtinv, u, divB);
+  if (P.sd > 2) hpredict_dir<2, IRHON>(P, RP, D, H, W, base, cs, scs, c, x, nc, dtinv, u, divB);
   // addExplicitSources with W(t) and dt/2 (srcIdeal/PatchMHDMF.cpp:1149-1389)
   double w[MF_MAX_COMP];
 #pragma unroll
@@ -233,7 +271,9 @@ __global__ void __launch_bounds__(kMaxBlock)
   for (int q = 0; q < MF_MAX_COMP; ++q) delta[q] = 0.0;
   if (in_v(x)) {
     const long long b = D.u_off + loc(D.flo, D.fn, x[0], x[1], x[2]);
-    for (int q = 0; q < nc; ++q) delta[q] = H.w2[b + q * cs] - W[b + q * cs];
+#pragma unroll
+    for (int q = 0; q < MF_MAX_COMP; ++q)
+      if (q < nc) delta[q] = H.w2[b + q * cs] - W[b + q * cs];
   } else if (P.bc_kind == MF_BC_FARFIELD && P.nf > 2) {
     int od = -1;
     for (int d = 0; d < P.sd; ++d)
@@ -243,16 +283,20 @@ __global__ void __launch_bounds__(kMaxBlock)
       y[od] = (y[od] < RP.dlo[od]) ? RP.dlo[od] : RP.dhi[od];
       if (in_v(y)) {
         const long long b = D.u_off + loc(D.flo, D.fn, y[0], y[1], y[2]);
-        for (int q = P.irhon + 5; q < nc; ++q) delta[q] = H.w2[b + q * cs] - W[b + q * cs];
+#pragma unroll
+        for (int q = 0; q < MF_MAX_COMP; ++q)
+          if (q >= P.irhon + 5 && q < nc) delta[q] = H.w2[b + q * cs] - W[b + q * cs];
       }
     }
   }
   for (int d = 0; d < P.sd; ++d) {
     double* __restrict__ fv = H.fv[d] + D.fv_off[d] + lin;
-    for (int q = 0; q < nc; ++q) {
-      fv[q * scs] = fv[q * scs] + delta[q];
-      fv[(nc + q) * scs] = fv[(nc + q) * scs] + delta[q];
-    }
+#pragma unroll
+    for (int q = 0; q < MF_MAX_COMP; ++q)
+      if (q < nc) {
+        fv[q * scs] = fv[q * scs] + delta[q];
+        fv[(nc + q) * scs] = fv[(nc + q) * scs] + delta[q];
+      }
   }
 }
 

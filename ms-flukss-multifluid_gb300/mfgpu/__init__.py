@@ -106,6 +106,8 @@ class MfParams(ctypes.Structure):
         ("bc_kind", ctypes.c_int),
         ("bc_plasma", ctypes.c_double * 8),
         ("bc_neutral1", ctypes.c_double * 5),
+        ("char_reconstruction", ctypes.c_int),
+        ("check_tvd", ctypes.c_int),
     ]
 
 

@@ -358,6 +358,238 @@ static int limiter_of(const Ctx* c, int v) {
   return MF_LIM_MINMOD;
 }
 
+
+/* ------------------------------------------------------------------------ */
+/* characteristic reconstruction                                             */
+/* ------------------------------------------------------------------------ */
+
+/* minmod3 (src/reconstructionF.ChF:15-22) */
+static double minmod3(double A, double B, double C) {
+  double signA = copysign(1.0, A);
+  return signA * fmax(0.0, fmin(fabs(A), fmin(signA * B, signA * C)));
+}
+
+/* *FACESLOPES: limited slopes of one variable from the left and right
+   differences (src/reconstructionF.ChF: MINMODFACESLOPES :157-178,
+   SUPERBEEFACESLOPES :356-392, HARMONICFACESLOPES :526-550,
+   VANALBADAFACESLOPES :591-622, MCFACESLOPES :664-697,
+   VANLEERFACESLOPES :843-880, CDFACESLOPES :1081-1096). */
+static void face_slopes(int lim, double* Sleft, double* Sright) {
+  double dSR = *Sright, dSL = *Sleft, SLOPE = 0.0;
+  switch (lim) {
+    case MF_LIM_CD:
+      *Sleft = 0.5 * *Sleft;
+      *Sright = 0.5 * *Sright;
+      return;
+    case MF_LIM_SUPERBEE:
+      if (dSL * dSR > 0.0) {
+        double AR = fabs(dSR), AL = fabs(dSL);
+        if (AL <= 0.5 * AR)
+          SLOPE = dSL;
+        else if (AL <= AR)
+          SLOPE = 0.5 * dSR;
+        else if (AL <= AR + AR)
+          SLOPE = 0.5 * dSL;
+        else
+          SLOPE = dSR;
+      }
+      break;
+    case MF_LIM_HARMONIC:
+      if (dSL * dSR > 0.0) SLOPE = dSR * dSL / (dSL + dSR);
+      break;
+    case MF_LIM_VANALBADA: {
+      const double dSave = 1.0e-6, dSaveS = dSave + dSave;
+      if (dSL * dSR > 0.0)
+        SLOPE = 0.5 * (dSR * dSL + dSave) * (dSR + dSL) / (dSR * dSR + dSL * dSL + dSaveS);
+      break;
+    }
+    case MF_LIM_MC:
+      if (dSL * dSR > 0.0) {
+        double AR = fabs(dSR), AL = fabs(dSL);
+        if (3.0 * AL <= AR)
+          SLOPE = dSL;
+        else if (AL <= 3.0 * AR)
+          SLOPE = 0.25 * (dSR + dSL);
+        else
+          SLOPE = dSR;
+      }
+      break;
+    case MF_LIM_VANLEER: {
+      const double dSLim = 1.0 / 3.0;
+      const double BT = (3.0 - dSLim) / (1.0 - dSLim);
+      const double SL1 = 0.25 * (1.0 - dSLim);
+      const double SL2 = 0.25 * (1.0 + dSLim);
+      double SLOPL = 0.0, SLOPR = 0.0;
+      if (dSL * dSR > 0.0) {
+        double SL = fmin(fabs(dSR), fabs(BT * dSL));
+        double SR = fmin(fabs(dSL), fabs(BT * dSR));
+        SLOPL = SL1 * SL + SL2 * SR;
+        SLOPR = SL1 * SR + SL2 * SL;
+        if (dSR < 0.0) {
+          SLOPL = -SLOPL;
+          SLOPR = -SLOPR;
+        }
+      }
+      *Sleft = SLOPL;
+      *Sright = SLOPR;
+      return;
+    }
+    case MF_LIM_MINMOD:
+    default:
+      SLOPE = 0.5 * minmod(dSR, dSL);
+      break;
+  }
+  *Sleft = SLOPE;
+  *Sright = SLOPE;
+}
+
+/* Wave speeds and mixing coefficients of CHARANALYSISF / CHARSYNTHESISF at
+   a cell state (the two routines differ only in the dfs cut-off). */
+typedef struct {
+  double Rho, cc, c, as, af, alphaF, alphaS, betaY, betaZ, BX;
+} CharState;
+
+static void char_state(const Ctx* c, int d, const double* w, double dfs_cut, CharState* s) {
+  const int inB = 5 + d, itB1 = 5 + (d + 1) % 3, itB2 = 5 + (d + 2) % 3;
+  double PGas = w[4] > c->smallp ? w[4] : c->smallp;
+  double Rho = w[0] > c->smallr ? w[0] : c->smallr;
+  double BX = w[inB], BY = w[itB1], BZ = w[itB2];
+  double cc = c->gamma * PGas / Rho;
+  double cs = sqrt(cc);
+  double BX2 = BX * BX, BY2 = BY * BY, BZ2 = BZ * BZ;
+  double BYZ2 = BY2 + BZ2;
+  double BxBH = D_1_8PI * (BX2 + BYZ2);
+  double bb = D_1_4PI * BX2 / Rho;
+  double b = sqrt(bb);
+  double betaY, betaZ, aaf, aas, af, as;
+  if (BYZ2 < c->smallB * c->smallB) {
+    betaY = D_SQRT_2;
+    betaZ = D_SQRT_2;
+    if (bb > cc) {
+      aaf = bb; aas = cc; af = b; as = cs;
+    } else {
+      aaf = cc; aas = bb; af = cs; as = b;
+    }
+  } else {
+    double hyz = sqrt(BYZ2);
+    betaY = BY / hyz;
+    betaZ = BZ / hyz;
+    double szb = cc + (BxBH + BxBH) / Rho;
+    double h = sqrt(szb * szb - 4.0 * cc * bb);
+    aas = 0.5 * (szb - h);
+    as = sqrt(aas);
+    aaf = 0.5 * (szb + h);
+    af = sqrt(aaf);
+  }
+  double dfs = aaf - aas, alphaF, alphaS;
+  if (dfs < dfs_cut) {
+    alphaF = 1.0; alphaS = 0.0;
+  } else if ((cc - aas) <= 0.0) {
+    alphaF = 0.0; alphaS = 1.0;
+  } else if ((aaf - cc) <= 0.0) {
+    alphaF = 1.0; alphaS = 0.0;
+  } else {
+    alphaF = sqrt((cc - aas) / dfs);
+    alphaS = sqrt((aaf - cc) / dfs);
+  }
+  s->Rho = Rho; s->cc = cc; s->c = cs; s->as = as; s->af = af;
+  s->alphaF = alphaF; s->alphaS = alphaS; s->betaY = betaY; s->betaZ = betaZ; s->BX = BX;
+}
+
+/* CHARANALYSISF (srcIdeal/PatchIdealMHDF.ChF:1167-1328) on one slope vector
+   dW (plasma primitives, global frame), in place. */
+static void char_analysis1(const CharState* s, int d, double* dW) {
+  const int in = 1 + d, it1 = 1 + (d + 1) % 3, it2 = 1 + (d + 2) % 3;
+  const int inB = 5 + d, itB1 = 5 + (d + 1) % 3, itB2 = 5 + (d + 2) % 3;
+  double siBX = copysign(1.0, s->BX);
+  double dP = dW[4], dRho = dW[0], dUn = dW[in], dUt1 = dW[it1], dUt2 = dW[it2];
+  double dBn = dW[inB], dBt1 = dW[itB1], dBt2 = dW[itB2];
+  double Rho = s->Rho, cc = s->cc, betaY = s->betaY, betaZ = s->betaZ;
+  dW[0] = dRho - dP / cc;
+  dW[1] = dBn;
+  double h1 = D_SQRT_2 * (betaY * dUt2 - betaZ * dUt1);
+  double h2 = siBX * (betaZ * dBt1 - betaY * dBt2) / (2.0 * sqrt(2.0 * D_PI * Rho));
+  dW[2] = h1 + h2;
+  dW[3] = h1 - h2;
+  h1 = dP / (2.0 * Rho * cc);
+  h2 = dUn / (2.0 * cc);
+  double h3 = (betaY * dBt1 + betaZ * dBt2) / (4.0 * s->c * sqrt(D_PI * Rho));
+  double h4 = siBX * (betaY * dUt1 + betaZ * dUt2) / (2.0 * cc);
+  double aF = s->alphaF, aS = s->alphaS, af = s->af, as = s->as;
+  dW[4] = aF * (h1 + af * h2) + aS * (h3 - as * h4);
+  dW[5] = aF * (h1 - af * h2) + aS * (h3 + as * h4);
+  dW[6] = aS * (h1 + as * h2) - aF * (h3 - af * h4);
+  dW[7] = aS * (h1 - as * h2) - aF * (h3 + af * h4);
+}
+
+/* CHARSYNTHESISF (srcIdeal/PatchIdealMHDF.ChF:1330-1500) on one vector of
+   wave amplitudes, in place (back to primitive slopes, global frame). */
+static void char_synthesis1(const CharState* s, int d, double* dW) {
+  const int in = 1 + d, it1 = 1 + (d + 1) % 3, it2 = 1 + (d + 2) % 3;
+  const int inB = 5 + d, itB1 = 5 + (d + 1) % 3, itB2 = 5 + (d + 2) % 3;
+  double betaY = s->betaY, betaZ = s->betaZ, betaYX = betaY, betaZX = betaZ;
+  if (s->BX < 0.0) {
+    betaYX = -betaY;
+    betaZX = -betaZ;
+  }
+  double alpha1 = dW[0], alpha2 = dW[1], alpha3 = dW[2], alpha4 = dW[3];
+  double alpha5 = dW[4], alpha6 = dW[5], alpha7 = dW[6], alpha8 = dW[7];
+  alpha3 = D_SQRT_2 * alpha3;
+  alpha4 = D_SQRT_2 * alpha4;
+  double alph3p4 = alpha3 + alpha4, alph3m4 = alpha3 - alpha4;
+  double alph5p6 = alpha5 + alpha6, alph5m6 = alpha5 - alpha6;
+  double alph7p8 = alpha7 + alpha8, alph7m8 = alpha7 - alpha8;
+  double aF = s->alphaF, aS = s->alphaS, af = s->af, as = s->as;
+  double DN = 2.0 * sqrt(D_PI * s->Rho);
+  double HRho = s->Rho * (aF * alph5p6 + aS * alph7p8);
+  double HU = aS * as * alph5m6 - aF * af * alph7m8;
+  double HB = s->c * (aS * alph5p6 - aF * alph7p8);
+  dW[0] = alpha1 + HRho;
+  dW[in] = aF * af * alph5m6 + aS * as * alph7m8;
+  dW[it1] = -betaZ * alph3p4 - betaYX * HU;
+  dW[it2] = betaY * alph3p4 - betaZX * HU;
+  dW[4] = s->cc * HRho;
+  dW[inB] = alpha2;
+  dW[itB1] = DN * (betaZX * alph3m4 + betaY * HB);
+  dW[itB2] = DN * (-betaYX * alph3m4 + betaZ * HB);
+}
+
+/* One cell of Reconstruction::faceValues with characteristic limiting
+   (src/Reconstruction.cpp:178-203): INITIALSLOPES, CHARANALYSISF on the
+   plasma variables, the FACESLOPES of every variable, CHARSYNTHESISF,
+   FROMSLOPESTOVALUES, then CHECKTVD on the variables main/MHDAM.cpp:939-968
+   selects (check_tvd 1: the 8 plasma variables, 2: density and pressure). */
+static void char_face_values(const Ctx* c, int d, const double* wm1, const double* w0,
+                             const double* wp1, double* lo, double* hi) {
+  const int np = c->nprim;
+  double SL[MF_MAX_COMP], SR[MF_MAX_COMP];
+  for (int v = 0; v < np; ++v) {
+    SL[v] = w0[v] - wm1[v];
+    SR[v] = wp1[v] - w0[v];
+  }
+  CharState sa, ss;
+  char_state(c, d, w0, 1.0e-12, &sa);
+  char_analysis1(&sa, d, SL);
+  char_analysis1(&sa, d, SR);
+  for (int v = 0; v < np; ++v) face_slopes(limiter_of(c, v), &SL[v], &SR[v]);
+  char_state(c, d, w0, 1.0e-8, &ss);
+  char_synthesis1(&ss, d, SL);
+  char_synthesis1(&ss, d, SR);
+  for (int v = 0; v < np; ++v) {
+    lo[v] = w0[v] - SL[v];
+    hi[v] = w0[v] + SR[v];
+  }
+  const int tvd = c->p->check_tvd;
+  for (int v = 0; v < 8; ++v) {
+    if (!(tvd == 1 || (tvd == 2 && (v == 0 || v == 4)))) continue;
+    double WP = w0[v];
+    double dWR = wp1[v] - WP, dWL = WP - wm1[v];
+    double dSL = WP - lo[v], dSR = hi[v] - WP;
+    lo[v] = WP - minmod3(dWL, dWR, dSL);
+    hi[v] = WP + minmod3(dWL, dWR, dSR);
+  }
+}
+
 /* ------------------------------------------------------------------------ */
 /* Riemann solvers                                                           */
 /* ------------------------------------------------------------------------ */
@@ -1577,6 +1809,20 @@ static int euler_step(const Ctx* c, double time, Fab* U, Fab* F /* [sd] or NULL 
     int o[3] = {0, 0, 0};
     o[d] = 1;
     FOR_BOX(slopeBox, i, j, k) {
+      if (p->char_reconstruction) {
+        double a[MF_MAX_COMP], b[MF_MAX_COMP], e[MF_MAX_COMP], lo[MF_MAX_COMP], hi[MF_MAX_COMP];
+        for (int v = 0; v < np; ++v) {
+          a[v] = AT(&W, i - o[0], j - o[1], k - o[2], v);
+          b[v] = AT(&W, i, j, k, v);
+          e[v] = AT(&W, i + o[0], j + o[1], k + o[2], v);
+        }
+        char_face_values(c, d, a, b, e, lo, hi);
+        for (int v = 0; v < np; ++v) {
+          AT(&Wm[d], i, j, k, v) = lo[v];
+          AT(&Wp[d], i, j, k, v) = hi[v];
+        }
+        continue;
+      }
       for (int v = 0; v < np; ++v) {
         double lo, hi;
         face_values(limiter_of(c, v), AT(&W, i - o[0], j - o[1], k - o[2], v), AT(&W, i, j, k, v),
@@ -1734,6 +1980,20 @@ static void reconstruct_faces(const Ctx* c, const Fab* W, mf_box slopeBox, Fab* 
     int o[3] = {0, 0, 0};
     o[d] = 1;
     FOR_BOX(slopeBox, i, j, k) {
+      if (p->char_reconstruction) {
+        double a[MF_MAX_COMP], b[MF_MAX_COMP], e[MF_MAX_COMP], lo[MF_MAX_COMP], hi[MF_MAX_COMP];
+        for (int v = 0; v < np; ++v) {
+          a[v] = AT(W, i - o[0], j - o[1], k - o[2], v);
+          b[v] = AT(W, i, j, k, v);
+          e[v] = AT(W, i + o[0], j + o[1], k + o[2], v);
+        }
+        char_face_values(c, d, a, b, e, lo, hi);
+        for (int v = 0; v < np; ++v) {
+          AT(&Wm[d], i, j, k, v) = lo[v];
+          AT(&Wp[d], i, j, k, v) = hi[v];
+        }
+        continue;
+      }
       for (int v = 0; v < np; ++v) {
         double lo, hi;
         face_values(limiter_of(c, v), AT(W, i - o[0], j - o[1], k - o[2], v), AT(W, i, j, k, v),
