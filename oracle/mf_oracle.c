@@ -2571,3 +2571,607 @@ int mf_oracle_max_threads(void) {
   return 1;
 #endif
 }
+
+/* ------------------------------------------------------------------------ */
+/* coarse-fine coupling of a subcycled hierarchy                             */
+/* ------------------------------------------------------------------------ */
+/* Boxes below are in the index space of their level; a level refined by r
+   has cell iv above coarse cell floor(iv / r).  Coarse data outside the
+   domain in a periodic direction is the periodic image of valid data. */
+
+static int imod_(int a, int n) {
+  int m = a % n;
+  return m < 0 ? m + n : m;
+}
+
+static int floordiv_(int a, int r) { return (a >= 0) ? a / r : -((-a + r - 1) / r); }
+
+static mf_box box_coarsen(mf_box b, int r, int sd) {
+  for (int d = 0; d < sd; ++d) {
+    b.lo[d] = floordiv_(b.lo[d], r);
+    b.hi[d] = floordiv_(b.hi[d], r);
+  }
+  return b;
+}
+
+/* Periodic image inside the domain; 0 outside the domain in a non-periodic
+   direction. */
+static int wrap_cell(const mf_params* p, int iv[3]) {
+  for (int d = 0; d < p->space_dim; ++d) {
+    int lo = p->domain_lo[d], n = p->domain_hi[d] - lo + 1;
+    if (p->periodic[d])
+      iv[d] = lo + imod_(iv[d] - lo, n);
+    else if (iv[d] < lo || iv[d] > p->domain_hi[d])
+      return 0;
+  }
+  return 1;
+}
+
+/* Index of the box holding the periodic image of cell c, -1 if none. */
+static int find_box_wrapped(const mf_params* p, int n, const mf_box* b, const int c[3]) {
+  int w[3] = {c[0], c[1], c[2]};
+  if (!wrap_cell(p, w)) return -1;
+  for (int q = 0; q < n; ++q)
+    if (box_in(&b[q], w[0], w[1], w[2])) return q;
+  return -1;
+}
+
+/* Is the image of coarse cell c under a coarsened fine box? */
+static int covered_by_fine(const mf_params* pc, int r, int nf, const mf_box* vf, const int c[3]) {
+  int w[3] = {c[0], c[1], c[2]};
+  if (!wrap_cell(pc, w)) return 0;
+  for (int q = 0; q < nf; ++q) {
+    mf_box cb = box_coarsen(vf[q], r, pc->space_dim);
+    if (box_in(&cb, w[0], w[1], w[2])) return 1;
+  }
+  return 0;
+}
+
+/* interp_divB_0 (srcIdeal/FineInterpMHDAMF.ChF:449-555): correct the limited
+   slopes d(Bx)/dx, d(By)/dy, d(Bz)/dz of one coarse cell towards a
+   divergence-free linear profile. */
+static void interp_divb0(int sd, double* sx, double* sy, double* sz) {
+  const double eps_divB = 1.0e-8;
+  double DBXDX = *sx, DBYDY = *sy, DBZDZ = (sd == 3) ? *sz : 0.0;
+  double fact = (sd == 3) ? -1.0 / (1.0 + 1.0 + 1.0) : -1.0 / (1.0 + 1.0);
+  double divB = (sd == 3) ? DBXDX + DBYDY + DBZDZ : DBXDX + DBYDY;
+  double del = fact * divB;
+  double adel = fabs(del);
+  if (!(adel > eps_divB)) return;
+  double delX = minmod(-DBXDX, del), delY = minmod(-DBYDY, del);
+  double delZ = (sd == 3) ? minmod(-DBZDZ, del) : 0.0;
+  double del2 = (sd == 3) ? delX + delY + delZ : delX + delY;
+  if (fabs(del2) < fabs(divB)) {
+    if (sd == 2) {
+      delX = minmod(DBXDX, -DBYDY);
+      delY = -delX;
+      delX = delX - DBXDX;
+      delY = delY - DBYDY;
+    } else if (fabs(delX) < adel) {
+      del = -0.5 * (delX + divB);
+      delY = minmod(-DBYDY, del);
+      delZ = minmod(-DBZDZ, del);
+      del2 = delX + delY + delZ;
+      if (fabs(del2) < fabs(divB)) {
+        if (fabs(delY) < adel)
+          delZ = -(divB + delX + delY);
+        else
+          delY = -(divB + delX + delZ);
+      }
+    } else if (fabs(delY) < adel) {
+      del = -0.5 * (delY + divB);
+      delX = minmod(-DBXDX, del);
+      delZ = minmod(-DBZDZ, del);
+      del2 = delX + delY + delZ;
+      if (fabs(del2) < fabs(divB)) {
+        if (fabs(delX) < adel)
+          delZ = -(divB + delX + delY);
+        else
+          delX = -(divB + delY + delZ);
+      }
+    } else {
+      del = -0.5 * (delZ + divB);
+      adel = fabs(del);
+      delX = minmod(-DBXDX, del);
+      delY = minmod(-DBYDY, del);
+      del2 = delX + delY + delZ;
+      if (fabs(del2) < fabs(divB)) {
+        if (fabs(delX) < adel)
+          delY = -(divB + delX + delZ);
+        else
+          delX = -(divB + delY + delZ);
+      }
+    }
+  }
+  *sx = *sx + delX;
+  *sy = *sy + delY;
+  if (sd == 3) *sz = *sz + delZ;
+}
+
+/* PiecewiseLinearFillPatchMHDAM::define + fillInterp
+   (srcIdeal/PiecewiseLinearFillPatchMHDAM.cpp:120-380, 382-900): fill the ghost
+   cells of every fine patch that lie over coarse cells no coarsened fine box
+   covers, from the coarse data interpolated in time (alpha between the old
+   and new coarse states) and linearly in space with limited slopes
+   (INTERPLIMIT_V, srcIdeal/FineInterpMHDAMF.ChF:235-386). */
+static int cf_fill(const mf_params* pc, const mf_params* pf, int r, int ncp, mf_fab* Uold,
+                   mf_fab* Unew, const mf_box* vc, int nfp, mf_fab* Uf, const mf_box* vf,
+                   double alpha, int ng) {
+  const int sd = pc->space_dim, nc = Unew[0].ncomp;
+  const int csr = (ng + r - 1) / r, cgr = csr + 1;
+  const double dxc = pc->dx, dxf = pf->dx;
+  const int divb = (pc->divb_cleaning != 0);
+  const int iBX = 5;
+  double volc = (sd == 3) ? dxc * dxc * dxc : dxc * dxc;
+  double volf = (sd == 3) ? dxf * dxf * dxf : dxf * dxf;
+  double refScale = 1.0;
+  for (int d = 0; d < sd; ++d) refScale *= r;
+  const double coeff = volc / (volf * refScale);
+  for (int f = 0; f < nfp; ++f) {
+    mf_box cfb = box_coarsen(vf[f], r, sd);
+    mf_box wb = box_grow(cfb, cgr, sd);
+    Fab Wk = fab_alloc(wb, nc), Sl[3];
+    for (long q = 0; q < Wk.csz * nc; ++q) Wk.p[q] = -666.666;
+    for (int d = 0; d < 3; ++d) {
+      Sl[d] = fab_alloc(wb, nc);
+      for (long q = 0; q < Sl[d].csz * nc; ++q) Sl[d].p[q] = -666.666;
+    }
+    /* timeInterp: coarse valid data (and periodic images) into the work box */
+    FOR_BOX(wb, i, j, k) {
+      int c[3] = {i, j, k};
+      int b = find_box_wrapped(pc, ncp, vc, c);
+      if (b < 0) continue;
+      int w[3] = {i, j, k};
+      wrap_cell(pc, w);
+      Fab O = fab_wrap(Uold[b].data, Uold[b].box, nc), N = fab_wrap(Unew[b].data, Unew[b].box, nc);
+      for (int q = 0; q < nc; ++q) {
+        double vn = AT(&N, w[0], w[1], w[2], q), vo = AT(&O, w[0], w[1], w[2], q);
+        double v;
+        if (alpha == 1.0)
+          v = vn;
+        else if (alpha == 0.0)
+          v = vo;
+        else
+          v = vn * alpha + vo * (1.0 - alpha);
+        AT(&Wk, i, j, k, q) = v;
+      }
+    }
+    /* coarse cells to interpolate from */
+    mf_box ib = box_and_domain(box_coarsen(box_grow(vf[f], ng, sd), r, sd), pc);
+    Fab In = fab_alloc(ib, 1);
+    FOR_BOX(ib, i, j, k) {
+      int c[3] = {i, j, k};
+      AT(&In, i, j, k, 0) = covered_by_fine(pc, r, nfp, vf, c) ? 0.0 : 1.0;
+    }
+    /* slopes: centred where both neighbours are coarse valid cells, one-sided
+       otherwise (computeSlopes, :585-760; the high-sided difference wins where
+       both neighbours are missing) */
+    for (int d = 0; d < sd; ++d) {
+      int e[3] = {0, 0, 0};
+      e[d] = 1;
+      const double c1c = 0.5 / dxc, c1s = 1.0 / dxc;
+      FOR_BOX(ib, i, j, k) {
+        if (AT(&In, i, j, k, 0) == 0.0) continue;
+        int cp[3] = {i + e[0], j + e[1], k + e[2]}, cm[3] = {i - e[0], j - e[1], k - e[2]};
+        int hasp = find_box_wrapped(pc, ncp, vc, cp) >= 0;
+        int hasm = find_box_wrapped(pc, ncp, vc, cm) >= 0;
+        for (int q = 0; q < nc; ++q) {
+          double s;
+          double v0 = AT(&Wk, i, j, k, q);
+          double vp = AT(&Wk, cp[0], cp[1], cp[2], q), vm = AT(&Wk, cm[0], cm[1], cm[2], q);
+          if (!hasm)
+            s = c1s * (vp - v0);
+          else if (!hasp)
+            s = c1s * (v0 - vm);
+          else
+            s = c1c * (vp - vm);
+          AT(&Sl[d], i, j, k, q) = s;
+        }
+      }
+    }
+    /* limiting (INTERPLIMIT_V) away from non-periodic domain edges, then the
+       divergence correction of the B slopes */
+    FOR_BOX(ib, i, j, k) {
+      if (AT(&In, i, j, k, 0) == 0.0) continue;
+      int c[3] = {i, j, k}, edge = 0;
+      for (int d = 0; d < sd; ++d)
+        if (!pc->periodic[d] && (c[d] == pc->domain_lo[d] || c[d] == pc->domain_hi[d])) edge = 1;
+      if (edge) continue;
+      for (int q = 0; q < nc; ++q) {
+        double s0 = AT(&Wk, i, j, k, q);
+        double smax = s0, smin = s0;
+        for (int kk = (sd == 3 ? -1 : 0); kk <= (sd == 3 ? 1 : 0); ++kk)
+          for (int jj = -1; jj <= 1; ++jj)
+            for (int ii = -1; ii <= 1; ++ii) {
+              if (!box_in(&wb, i + ii, j + jj, k + kk)) continue;
+              double v = AT(&Wk, i + ii, j + jj, k + kk, q);
+              smax = fmax(smax, v);
+              smin = fmin(smin, v);
+            }
+        double dsum = (sd == 3) ? 0.5 * (fabs(AT(&Sl[0], i, j, k, q) * dxc) +
+                                         fabs(AT(&Sl[1], i, j, k, q) * dxc) +
+                                         fabs(AT(&Sl[2], i, j, k, q) * dxc))
+                                : 0.5 * (fabs(AT(&Sl[0], i, j, k, q) * dxc) +
+                                         fabs(AT(&Sl[1], i, j, k, q) * dxc));
+        double eta = fmin(smax - s0, s0 - smin);
+        if (eta <= 1.0e-9 * fabs(smax))
+          eta = 0.0;
+        else if (dsum > eta)
+          eta = eta / dsum;
+        else
+          eta = 1.0;
+        for (int d = 0; d < sd; ++d) AT(&Sl[d], i, j, k, q) = eta * AT(&Sl[d], i, j, k, q);
+      }
+      if (divb)
+        interp_divb0(sd, &AT(&Sl[0], i, j, k, iBX), &AT(&Sl[1], i, j, k, iBX + 1),
+                     sd == 3 ? &AT(&Sl[2], i, j, k, iBX + 2) : NULL);
+    }
+    /* fine cells: constant part, then the linear term of each direction */
+    mf_box fb = box_and_domain(box_grow(vf[f], ng, sd), pf);
+    Fab U = fab_wrap(Uf[f].data, Uf[f].box, nc);
+    FOR_BOX(fb, i, j, k) {
+      int c[3] = {floordiv_(i, r), floordiv_(j, r), sd == 3 ? floordiv_(k, r) : k};
+      if (!box_in(&ib, c[0], c[1], c[2]) || AT(&In, c[0], c[1], c[2], 0) == 0.0) continue;
+      for (int q = 0; q < nc; ++q) AT(&U, i, j, k, q) = AT(&Wk, c[0], c[1], c[2], q);
+    }
+    for (int d = 0; d < sd; ++d) FOR_BOX(fb, i, j, k) {
+        int iv[3] = {i, j, k};
+        int c[3] = {floordiv_(i, r), floordiv_(j, r), sd == 3 ? floordiv_(k, r) : k};
+        if (!box_in(&ib, c[0], c[1], c[2]) || AT(&In, c[0], c[1], c[2], 0) == 0.0) continue;
+        double icoef = dxf * (iv[d] + 0.5) - dxc * (c[d] + 0.5);
+        for (int q = 0; q < nc; ++q) {
+          double slope = coeff * icoef * AT(&Sl[d], c[0], c[1], c[2], q);
+          AT(&U, i, j, k, q) = AT(&U, i, j, k, q) + slope;
+        }
+      }
+    fab_free(&In);
+    fab_free(&Wk);
+    for (int d = 0; d < 3; ++d) fab_free(&Sl[d]);
+  }
+  return MF_OK;
+}
+
+/* One face of a flux register (LevelFluxRegister between a coarse level and
+   the next finer one): the coarse cell outside the fine region next to a
+   fine patch's side, its coarse patch, and where the fine faces lie. */
+typedef struct {
+  int pc, cell[3]; /* coarse patch and the (wrapped) coarse cell */
+  int d, side;     /* direction; side 0: cell below the fine region, 1: above */
+  int fp, fnode;   /* fine patch, node index of the fine faces along d */
+  int tlo[3];      /* fine cell index of the first fine face (other directions) */
+} RegFace;
+
+typedef struct {
+  int n;
+  RegFace* f;
+  double* reg; /* n * nc */
+} Register;
+
+static int reg_build(const mf_params* pc, int r, int ncp, const mf_box* vc, int nfp,
+                     const mf_box* vf, int nc, Register* R) {
+  const int sd = pc->space_dim;
+  int cap = 64;
+  R->n = 0;
+  R->f = (RegFace*)malloc(sizeof(RegFace) * (size_t)cap);
+  R->reg = NULL;
+  for (int f = 0; f < nfp; ++f) {
+    mf_box cb = box_coarsen(vf[f], r, sd);
+    for (int d = 0; d < sd; ++d)
+      for (int side = 0; side < 2; ++side) {
+        mf_box sb = cb;
+        sb.lo[d] = sb.hi[d] = side ? cb.hi[d] + 1 : cb.lo[d] - 1;
+        FOR_BOX(sb, i, j, k) {
+          int c[3] = {i, j, k};
+          int w[3] = {i, j, k};
+          if (!wrap_cell(pc, w)) continue; /* physical boundary */
+          if (covered_by_fine(pc, r, nfp, vf, c)) continue;
+          int b = find_box_wrapped(pc, ncp, vc, c);
+          if (b < 0) return MF_ERR_BAD_ARG; /* fine level not nested */
+          if (R->n == cap) {
+            cap *= 2;
+            R->f = (RegFace*)realloc(R->f, sizeof(RegFace) * (size_t)cap);
+          }
+          RegFace* F = &R->f[R->n++];
+          F->pc = b;
+          memcpy(F->cell, w, sizeof(w));
+          F->d = d;
+          F->side = side;
+          F->fp = f;
+          F->fnode = side ? vf[f].hi[d] + 1 : vf[f].lo[d];
+          for (int e = 0; e < 3; ++e) F->tlo[e] = (e < sd) ? c[e] * r : c[e];
+        }
+      }
+  }
+  R->reg = (double*)calloc((size_t)(R->n > 0 ? R->n : 1) * (size_t)nc, sizeof(double));
+  return MF_OK;
+}
+
+/* incrementCoarse: the register of each face starts as -dt * coarse flux
+   (updateState's flux: for RK2 the average of both stages). */
+static void reg_set_coarse(Register* R, int nc, Fab* const* Fc /* [patch][d] */, double dt) {
+  for (int n = 0; n < R->n; ++n) {
+    const RegFace* F = &R->f[n];
+    int node[3] = {F->cell[0], F->cell[1], F->cell[2]};
+    if (F->side == 0) node[F->d] += 1; /* the cell's high face */
+    for (int q = 0; q < nc; ++q) {
+      double v = 0.0;
+      v = v + (-dt) * AT(&Fc[F->pc][F->d], node[0], node[1], node[2], q);
+      R->reg[(long)n * nc + q] = v;
+    }
+  }
+}
+
+/* incrementFine: add dt/r^(D-1) times every fine flux on the coarse face,
+   the first transverse direction fastest. */
+static void reg_add_fine(Register* R, int nc, int sd, int r, Fab* const* Ff, double dt) {
+  double denom = 1.0;
+  for (int e = 0; e < sd - 1; ++e) denom *= r;
+  const double s = dt / denom;
+  for (int n = 0; n < R->n; ++n) {
+    const RegFace* F = &R->f[n];
+    int t[2] = {0, 0}, nt = 0;
+    for (int e = 0; e < sd; ++e)
+      if (e != F->d) t[nt++] = e;
+    const int n1 = (nt > 1) ? r : 1;
+    for (int b = 0; b < n1; ++b)
+      for (int a = 0; a < r; ++a) {
+        int node[3] = {F->tlo[0], F->tlo[1], F->tlo[2]};
+        node[F->d] = F->fnode;
+        node[t[0]] += a;
+        if (nt > 1) node[t[1]] += b;
+        for (int q = 0; q < nc; ++q)
+          R->reg[(long)n * nc + q] =
+              R->reg[(long)n * nc + q] + s * AT(&Ff[F->fp][F->d], node[0], node[1], node[2], q);
+      }
+  }
+}
+
+/* reflux (scale -1 with the inverse cell size): per direction, the cells
+   below the fine region first, then those above. */
+static void reg_reflux(const Register* R, const mf_params* pc, int nc, mf_fab* Uc) {
+  const double invdx = 1.0 / pc->dx;
+  for (int d = 0; d < pc->space_dim; ++d)
+    for (int side = 0; side < 2; ++side)
+      for (int n = 0; n < R->n; ++n) {
+        const RegFace* F = &R->f[n];
+        if (F->d != d || F->side != side) continue;
+        Fab U = fab_wrap(Uc[F->pc].data, Uc[F->pc].box, nc);
+        for (int q = 0; q < nc; ++q) {
+          double rg = R->reg[(long)n * nc + q];
+          double* u = &AT(&U, F->cell[0], F->cell[1], F->cell[2], q);
+          *u = side ? *u + invdx * rg : *u - invdx * rg;
+        }
+      }
+}
+
+/* CoarseAverageExt::averageToCoarse with AVERAGEWITHVOLUMES
+   (src/CoarseAverageExt.cpp:117-192, src/CoarseAverageExtF.ChF:10-50). */
+static int average_down(const mf_params* pc, const mf_params* pf, int r, int ncp, mf_fab* Uc,
+                        const mf_box* vc, int nfp, mf_fab* Uf, const mf_box* vf) {
+  const int sd = pc->space_dim, nc = Uc[0].ncomp;
+  const double dxf = pf->dx;
+  const double vol = (sd == 3) ? dxf * dxf * dxf : dxf * dxf;
+  for (int f = 0; f < nfp; ++f) {
+    mf_box cb = box_coarsen(vf[f], r, sd);
+    Fab Fi = fab_wrap(Uf[f].data, Uf[f].box, nc);
+    FOR_BOX(cb, i, j, k) {
+      int c[3] = {i, j, k};
+      int b = find_box_wrapped(pc, ncp, vc, c);
+      if (b < 0) return MF_ERR_BAD_ARG;
+      Fab C = fab_wrap(Uc[b].data, Uc[b].box, nc);
+      const int rk = (sd == 3) ? r : 1;
+      for (int q = 0; q < nc; ++q) {
+        double sum = 0.0, volc = 0.0;
+        for (int kk = 0; kk < rk; ++kk)
+          for (int jj = 0; jj < r; ++jj)
+            for (int ii = 0; ii < r; ++ii) {
+              int fi = i * r + ii, fj = j * r + jj, fk = (sd == 3) ? k * r + kk : k;
+              sum = sum + vol * AT(&Fi, fi, fj, fk, q);
+              volc = volc + vol;
+            }
+        AT(&C, i, j, k, q) = sum / volc;
+      }
+    }
+  }
+  return MF_OK;
+}
+
+typedef struct {
+  const mf_oracle_level* lev;
+  int nlev;
+  const int* ratio;
+  int nthreads;
+  mf_params* p;  /* per-level copies (GLM speeds updated during the step) */
+  double* t;     /* level times */
+  double* dt;    /* level steps */
+  double* ndt;   /* per level: last new dt */
+  mf_fab** old;  /* UOld per level (levels with a finer level) */
+  Fab** F;       /* per level: npatch * 3 face-flux fabs */
+  Register* reg; /* per pair (l, l+1) */
+  int ng;
+} Hier;
+
+/* AMRLevelIdealMHD::advance of level l: UOld, preTimeStep's ghost
+   interpolation (srcIdeal/AMRLevelIdealMHD.cpp:669-752), exchange, the
+   patch updates with the register increments (:1248-1308), the level time
+   and the GLM speeds of the base level (:1528-1548). */
+static int hier_advance(Hier* H, int l) {
+  const mf_oracle_level* L = &H->lev[l];
+  const int nc = L->U[0].ncomp, sd = H->p[l].space_dim;
+  int st = MF_OK;
+  if (l + 1 < H->nlev)
+    for (int b = 0; b < L->npatch; ++b) {
+      Fab f = fab_wrap(L->U[b].data, L->U[b].box, nc);
+      memcpy(H->old[l][b].data, L->U[b].data, sizeof(double) * (size_t)(f.csz * nc));
+    }
+  if (l > 0) {
+    const int r = H->ratio[l - 1];
+    double tNew = H->t[l - 1], tOld = tNew - H->dt[l - 1];
+    double alpha = (H->t[l] - tOld) / (tNew - tOld);
+    double eps = 0.04 * H->dt[l] / r;
+    if (fabs(alpha) < eps) alpha = 0.0;
+    if (fabs(1.0 - alpha) < eps) alpha = 1.0;
+    if (alpha < 0.0 || alpha > 1.0) return MF_ERR_BAD_ARG;
+    const mf_oracle_level* C = &H->lev[l - 1];
+    st = cf_fill(&H->p[l - 1], &H->p[l], r, C->npatch, H->old[l - 1], C->U, C->valid,
+                 L->npatch, L->U, L->valid, alpha, H->ng);
+    if (st) return st;
+  }
+  st = mf_oracle_level_exchange(&H->p[l], L->npatch, L->U, L->valid);
+  if (st) return st;
+  double* dts = (double*)malloc(sizeof(double) * (size_t)L->npatch);
+  int* sts = (int*)malloc(sizeof(int) * (size_t)L->npatch);
+#ifdef _OPENMP
+  int nth = H->nthreads > 0 ? H->nthreads : omp_get_max_threads();
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nth)
+#endif
+  for (int b = 0; b < L->npatch; ++b) {
+    mf_fab Fo[3];
+    for (int d = 0; d < 3; ++d) {
+      Fo[d].data = H->F[l][3 * b + d].p;
+      Fo[d].box = H->F[l][3 * b + d].b;
+      Fo[d].ncomp = nc;
+    }
+    int cell[3];
+    sts[b] = mf_oracle_patch_update(&H->p[l], H->t[l], &L->U[b], &L->valid[b], H->dt[l], Fo,
+                                    NULL, &dts[b], cell);
+  }
+  double nd = 0.0;
+  for (int b = 0; b < L->npatch; ++b) {
+    if (sts[b]) st = sts[b];
+    if (b == 0 || dts[b] < nd) nd = dts[b];
+  }
+  free(dts);
+  free(sts);
+  if (st) return st;
+  H->ndt[l] = nd;
+  Fab** Fl = (Fab**)malloc(sizeof(Fab*) * (size_t)L->npatch);
+  for (int b = 0; b < L->npatch; ++b) Fl[b] = &H->F[l][3 * b];
+  if (l + 1 < H->nlev) reg_set_coarse(&H->reg[l], nc, Fl, H->dt[l]);
+  if (l > 0) reg_add_fine(&H->reg[l - 1], nc, sd, H->ratio[l - 1], Fl, H->dt[l]);
+  free(Fl);
+  H->t[l] = H->t[l] + H->dt[l];
+  if (l == 0 && H->p[0].divb_cleaning == 5 && H->p[0].factor_ch > 0.0) {
+    double dx = H->p[0].dx;
+    double Ch = H->p[0].factor_ch * dx / nd;
+    double Cp = sqrt(Ch * dx / H->p[0].factor_cp);
+    for (int q = 0; q < H->nlev; ++q) {
+      H->p[q].dedner_ch = Ch;
+      H->p[q].dedner_cp = Cp;
+    }
+  }
+  return MF_OK;
+}
+
+/* AMR_MHDAM::timeStep (srcIdeal/AMR_MHDAM.cpp:1707-1880): advance, then the
+   finer level ratio times, then postTimeStep (reflux, average down;
+   srcIdeal/AMRLevelIdealMHD.cpp:1633-1646). */
+static int hier_time_step(Hier* H, int l) {
+  int st = hier_advance(H, l);
+  if (st) return st;
+  if (l + 1 < H->nlev) {
+    for (int k = 0; k < H->ratio[l]; ++k) {
+      st = hier_time_step(H, l + 1);
+      if (st) return st;
+    }
+    const mf_oracle_level *C = &H->lev[l], *Fn = &H->lev[l + 1];
+    reg_reflux(&H->reg[l], &H->p[l], C->U[0].ncomp, C->U);
+    st = average_down(&H->p[l], &H->p[l + 1], H->ratio[l], C->npatch, C->U, C->valid,
+                      Fn->npatch, Fn->U, Fn->valid);
+  }
+  return st;
+}
+
+int mf_oracle_hier_step(int nlev, const mf_oracle_level* lev, const int* ratio, double* time,
+                        double dt0, int nthreads, double* new_dt, double* dedner) {
+  if (nlev < 1 || !lev || (nlev > 1 && !ratio) || !time || !(dt0 > 0.0)) return MF_ERR_BAD_ARG;
+  Hier H;
+  memset(&H, 0, sizeof(H));
+  H.lev = lev;
+  H.nlev = nlev;
+  H.ratio = ratio;
+  H.nthreads = nthreads;
+  H.p = (mf_params*)malloc(sizeof(mf_params) * (size_t)nlev);
+  H.t = (double*)malloc(sizeof(double) * (size_t)nlev);
+  H.dt = (double*)malloc(sizeof(double) * (size_t)nlev);
+  H.ndt = (double*)malloc(sizeof(double) * (size_t)nlev);
+  H.old = (mf_fab**)calloc((size_t)nlev, sizeof(mf_fab*));
+  H.F = (Fab**)calloc((size_t)nlev, sizeof(Fab*));
+  H.reg = (Register*)calloc((size_t)nlev, sizeof(Register));
+  int st = MF_OK;
+  for (int l = 0; l < nlev; ++l) {
+    H.p[l] = *lev[l].p;
+    H.t[l] = time[l];
+    H.dt[l] = (l == 0) ? dt0 : H.dt[l - 1] / ratio[l - 1];
+  }
+  H.ng = num_ghost(lev[0].p);
+  for (int l = 0; l < nlev && st == MF_OK; ++l) {
+    const mf_oracle_level* L = &lev[l];
+    const int nc = L->U[0].ncomp, sd = L->p->space_dim;
+    H.F[l] = (Fab*)malloc(sizeof(Fab) * 3 * (size_t)L->npatch);
+    for (int b = 0; b < L->npatch; ++b)
+      for (int d = 0; d < 3; ++d)
+        H.F[l][3 * b + d] = fab_alloc(box_nodes(L->valid[b], d < sd ? d : 0), nc);
+    if (l + 1 < nlev) {
+      H.old[l] = (mf_fab*)malloc(sizeof(mf_fab) * (size_t)L->npatch);
+      for (int b = 0; b < L->npatch; ++b) {
+        Fab f = fab_wrap(L->U[b].data, L->U[b].box, nc);
+        H.old[l][b] = L->U[b];
+        H.old[l][b].data = (double*)malloc(sizeof(double) * (size_t)(f.csz * nc));
+      }
+      st = reg_build(L->p, ratio[l], L->npatch, L->valid, lev[l + 1].npatch, lev[l + 1].valid,
+                     nc, &H.reg[l]);
+    }
+  }
+  if (st == MF_OK) st = hier_time_step(&H, 0);
+  if (st == MF_OK) {
+    double m = 1.0, best = 0.0;
+    for (int l = 0; l < nlev; ++l) {
+      if (l > 0) m *= ratio[l - 1];
+      double v = H.ndt[l] * m;
+      if (l == 0 || v < best) best = v;
+    }
+    if (new_dt) *new_dt = best;
+    for (int l = 0; l < nlev; ++l) time[l] = H.t[l];
+    if (dedner) {
+      dedner[0] = H.p[0].dedner_ch;
+      dedner[1] = H.p[0].dedner_cp;
+    }
+  }
+  for (int l = 0; l < nlev; ++l) {
+    const mf_oracle_level* L = &lev[l];
+    if (H.F[l]) {
+      for (int q = 0; q < 3 * L->npatch; ++q) fab_free(&H.F[l][q]);
+      free(H.F[l]);
+    }
+    if (H.old[l]) {
+      for (int b = 0; b < L->npatch; ++b) free(H.old[l][b].data);
+      free(H.old[l]);
+    }
+    free(H.reg[l].f);
+    free(H.reg[l].reg);
+  }
+  free(H.p);
+  free(H.t);
+  free(H.dt);
+  free(H.ndt);
+  free(H.old);
+  free(H.F);
+  free(H.reg);
+  return st;
+}
+
+int mf_oracle_cf_fill(const mf_params* pc, const mf_params* pf, int ratio, int ncoarse,
+                      mf_fab* Uc_old, mf_fab* Uc_new, const mf_box* vc, int nfine, mf_fab* Uf,
+                      const mf_box* vf, double alpha) {
+  if (!pc || !pf || ratio < 2 || ncoarse < 1 || nfine < 1) return MF_ERR_BAD_ARG;
+  return cf_fill(pc, pf, ratio, ncoarse, Uc_old, Uc_new, vc, nfine, Uf, vf, alpha,
+                 num_ghost(pf));
+}
+
+int mf_oracle_average_down(const mf_params* pc, const mf_params* pf, int ratio, int ncoarse,
+                           mf_fab* Uc, const mf_box* vc, int nfine, mf_fab* Uf,
+                           const mf_box* vf) {
+  if (!pc || !pf || ratio < 2 || ncoarse < 1 || nfine < 1) return MF_ERR_BAD_ARG;
+  return average_down(pc, pf, ratio, ncoarse, Uc, vc, nfine, Uf, vf);
+}

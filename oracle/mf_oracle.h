@@ -37,6 +37,38 @@ int mf_oracle_level_step(const mf_params* p, double time, int npatch, mf_fab* U,
                          const mf_box* valid, double dt, int nthreads, double* new_dt,
                          int* min_patch, int min_cell[3]);
 
+/* A level of a hierarchy: its parameters (dx and domain in the level's own
+   index space), patches (host fabs with ghosts) and valid boxes. */
+typedef struct {
+  const mf_params* p;
+  int npatch;
+  mf_fab* U;
+  const mf_box* valid;
+} mf_oracle_level;
+
+/* One time step of the coarsest level of a subcycled hierarchy
+   (AMR_MHDAM::timeStep srcIdeal/AMR_MHDAM.cpp:1707-1880 with
+   AMRLevelIdealMHD::advance / postTimeStep): level l steps ratio[l-1] times
+   per step of level l-1 with dt0 / prod(ratio); fine ghosts are interpolated
+   from the coarse level in space and time, coarse cells next to the fine
+   region are refluxed and covered coarse cells are averaged from the fine
+   level.  time[l] is advanced; new_dt = min over levels of the level's new dt
+   times the level's refinement; dedner (nullable) receives Ch, Cp as the base
+   level leaves them. */
+int mf_oracle_hier_step(int nlev, const mf_oracle_level* lev, const int* ratio, double* time,
+                        double dt0, int nthreads, double* new_dt, double* dedner);
+
+/* PiecewiseLinearFillPatchMHDAM::fillInterp on its own (alpha: time
+   fraction between the old and new coarse states). */
+int mf_oracle_cf_fill(const mf_params* pc, const mf_params* pf, int ratio, int ncoarse,
+                      mf_fab* Uc_old, mf_fab* Uc_new, const mf_box* vc, int nfine, mf_fab* Uf,
+                      const mf_box* vf, double alpha);
+
+/* CoarseAverageExt::averageToCoarse on its own. */
+int mf_oracle_average_down(const mf_params* pc, const mf_params* pf, int ratio, int ncoarse,
+                           mf_fab* Uc, const mf_box* vc, int nfine, mf_fab* Uf,
+                           const mf_box* vf);
+
 /* Single-face and single-cell kernels exposed for known-answer tests.
    wl / wr: primitive states (nprim entries, W layout); f: fluxes (ncons). */
 int mf_oracle_face_flux(const mf_params* p, int dir, const double* wl, const double* wr,

@@ -65,6 +65,15 @@ def load():
                                             ctypes.c_int, _DP]),
         "mf_oracle_init_orszag": (ctypes.c_int, [_P(MfParams), _P(MfFab), _P(MfBox)]),
         "mf_oracle_max_threads": (ctypes.c_int, []),
+        "mf_oracle_hier_step": (ctypes.c_int, [ctypes.c_int, ctypes.c_void_p, _P(ctypes.c_int),
+                                               _DP, ctypes.c_double, ctypes.c_int, _DP, _DP]),
+        "mf_oracle_cf_fill": (ctypes.c_int, [_P(MfParams), _P(MfParams), ctypes.c_int,
+                                             ctypes.c_int, _P(MfFab), _P(MfFab), _P(MfBox),
+                                             ctypes.c_int, _P(MfFab), _P(MfBox),
+                                             ctypes.c_double]),
+        "mf_oracle_average_down": (ctypes.c_int, [_P(MfParams), _P(MfParams), ctypes.c_int,
+                                                  ctypes.c_int, _P(MfFab), _P(MfBox),
+                                                  ctypes.c_int, _P(MfFab), _P(MfBox)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -191,3 +200,61 @@ def init_orszag(p: MfParams, U: np.ndarray, fab_lo, fab_hi, lo, hi):
 
 def max_threads() -> int:
     return load().mf_oracle_max_threads()
+
+
+class _Level(ctypes.Structure):
+    _fields_ = [("p", _P(MfParams)), ("npatch", ctypes.c_int), ("U", _P(MfFab)),
+                ("valid", _P(MfBox))]
+
+
+def _boxes(valid_boxes):
+    return (MfBox * len(valid_boxes))(*[make_box(lo, hi) for lo, hi in valid_boxes])
+
+
+def hier_step(levels, ratios, times, dt0, nthreads=0):
+    """One step of the coarsest level of a subcycled hierarchy.  levels: list
+    of (params, arrays, fab_boxes, valid_boxes) from coarse to fine (arrays
+    modified in place); times: list of level times (updated in place).
+    Returns (status, new_dt, (Ch, Cp))."""
+    lib = load()
+    n = len(levels)
+    keep = []
+    arr = (_Level * n)()
+    for lev, (p, arrays, fboxes, vboxes) in enumerate(levels):
+        fabs = _fab_array(arrays, fboxes)
+        vb = _boxes(vboxes)
+        keep += [fabs, vb]
+        arr[lev] = _Level(ctypes.pointer(p), len(arrays), fabs, vb)
+    rl = list(ratios)[:n - 1] or [1]
+    rat = (ctypes.c_int * len(rl))(*rl)
+    t = (ctypes.c_double * n)(*times)
+    ndt = ctypes.c_double()
+    ded = (ctypes.c_double * 2)()
+    st = lib.mf_oracle_hier_step(n, ctypes.cast(arr, ctypes.c_void_p), rat, t, dt0, nthreads,
+                                 ctypes.byref(ndt), ded)
+    for lev in range(n):
+        times[lev] = t[lev]
+    return st, ndt.value, (ded[0], ded[1])
+
+
+def cf_fill(pc, pf, ratio, coarse_old, coarse_new, coarse_fboxes, coarse_valid, fine_arrays,
+            fine_fboxes, fine_valid, alpha):
+    """Interpolate the fine ghost cells over uncovered coarse cells (in place)."""
+    lib = load()
+    fo = _fab_array(coarse_old, coarse_fboxes)
+    fn = _fab_array(coarse_new, coarse_fboxes)
+    ff = _fab_array(fine_arrays, fine_fboxes)
+    return lib.mf_oracle_cf_fill(ctypes.byref(pc), ctypes.byref(pf), ratio, len(coarse_new), fo,
+                                 fn, _boxes(coarse_valid), len(fine_arrays), ff,
+                                 _boxes(fine_valid), alpha)
+
+
+def average_down(pc, pf, ratio, coarse, coarse_fboxes, coarse_valid, fine_arrays, fine_fboxes,
+                 fine_valid):
+    """Average the fine level onto the coarse cells it covers (in place)."""
+    lib = load()
+    fc = _fab_array(coarse, coarse_fboxes)
+    ff = _fab_array(fine_arrays, fine_fboxes)
+    return lib.mf_oracle_average_down(ctypes.byref(pc), ctypes.byref(pf), ratio, len(coarse), fc,
+                                      _boxes(coarse_valid), len(fine_arrays), ff,
+                                      _boxes(fine_valid))
