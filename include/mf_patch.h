@@ -28,6 +28,14 @@
  *                              the patch loop (:1203-1309) and the dt MIN
  *                              reduction (:1517-1529) with the GLM Ch/Cp update
  *                              (:1531-1548).
+ *   mf_hier_*                  a subcycled hierarchy of levels: AMR_MHDAM::timeStep
+ *                              (srcIdeal/AMR_MHDAM.cpp:1707-1880) with the coarse-fine
+ *                              ghost interpolation PiecewiseLinearFillPatchMHDAM::fillInterp
+ *                              (srcIdeal/PiecewiseLinearFillPatchMHDAM.cpp:382-900,
+ *                              called at srcIdeal/AMRLevelIdealMHD.cpp:748-752), the
+ *                              LevelFluxRegister increments and reflux (:1276-1308,
+ *                              :1633-1642) and CoarseAverageExt::averageToCoarse (:1646,
+ *                              src/CoarseAverageExt.cpp:117-192).
  *
  * Data layout (Chombo FArrayBox): one contiguous FP64 array per patch covering
  * the valid box grown by mf_num_ghost() cells on every side, component-major,
@@ -267,6 +275,49 @@ mf_status mf_face_fluxes(mf_ctx* ctx, int dir, int n, const double* wl, const do
    threads (nullable) receives the chosen {prim, flux, update} shapes.
    Results of a step do not depend on the shapes. */
 mf_status mf_level_autotune(mf_level* lev, int reps, int threads[3]);
+
+/* ---- Hierarchy: levels coupled across refinement (Berger-Oliger) ----
+   levels[0] is the coarsest; level l+1 is refined by ratios[l] with respect
+   to level l (its mf_params: dx = dx_l / ratio, domain refined by ratio, same
+   time approximation and precision), each level with its own context.  Fine
+   boxes must be aligned to the ratio and properly nested: every coarse cell
+   the interpolation stencil, the flux register or the averaging reads must be
+   a valid cell of the coarser level (else MF_ERR_BAD_ARG at creation).
+   While a hierarchy exists its levels copy the fluxes of the register faces
+   out of every step (extra gather launches); destroy it before the levels. */
+typedef struct mf_hier mf_hier;
+mf_status mf_hier_create(int nlevels, mf_level* const* levels, const int* ratios,
+                         mf_hier** out);
+void mf_hier_destroy(mf_hier* h);
+/* Level times (all levels start at the same time; default 0). */
+mf_status mf_hier_set_time(mf_hier* h, double time);
+mf_status mf_hier_times(const mf_hier* h, double* times);
+/* One step dt0 of level 0 (AMR_MHDAM::timeStep): level l advances
+   ratio[l-1] times per step of level l-1 with dt_l = dt_{l-1} / ratio.
+   Before each level step its ghost cells over coarse cells not covered by the
+   finer level are interpolated from the coarser level (in time between its
+   states before and after its step, in space with limited slopes and, with
+   GLM, the divergence correction of the B slopes); after the finer level has
+   caught up, the coarse cells next to the fine region are refluxed with the
+   fine fluxes and the covered coarse cells are averaged from the fine cells.
+   With GLM (divb_cleaning 5) and factor_ch > 0, Ch and Cp of every level are
+   set from level 0's new dt after its step, as the reference does.
+   new_dt: min over levels of the level's dx/cmax times its refinement with
+   respect to level 0 (multiply by the CFL number for the next dt0).
+   Synchronous: returns after the step finished. */
+mf_status mf_hier_step(mf_hier* h, double dt0, double* new_dt, void* stream);
+/* The coupling operations on their own: copy the coarse values that the
+   interpolation onto level+1 reads (the "old" coarse state); interpolate the
+   coarse-fine ghosts of level (>= 1) with time fraction alpha between that
+   copy and the current coarse state; average level+1 onto level. */
+mf_status mf_hier_snapshot(mf_hier* h, int level, void* stream);
+mf_status mf_hier_fill_ghosts(mf_hier* h, int level, double alpha, void* stream);
+mf_status mf_hier_average_down(mf_hier* h, int level, void* stream);
+/* Sizes of the coupling of levels (pair, pair+1): interpolation sites,
+   interpolated fine cells, register faces, refluxed cells, averaged cells,
+   coarse cells read by the interpolation. */
+mf_status mf_hier_info(const mf_hier* h, int pair, long long counts[6]);
+int mf_hier_launches_per_step(const mf_hier* h);
 
 /* ---- Serving: independent runs stepped together in shared launches ----
    No reference counterpart (the reference advances one simulation per

@@ -48,7 +48,7 @@ def _compile(src: str, verbose: bool) -> str:
     if "_exact" in os.path.basename(src):
         # no fused multiply-add: every operation rounds as in
         # the CPU restatement of the reference
-        cmd += ["-fmad=false"]
+        cmd += ["-fmad=false", "-Xcompiler", "-ffp-contract=off"]
     if src.endswith(".cpp"):
         cmd += ["-x", "cu"]
     cmd += ["-c", src, "-o", obj]

@@ -323,7 +323,9 @@ struct mf_level {
   PinnedBuf hstate;
   cudaStream_t s = nullptr;
   cudaGraphExec_t gsync = nullptr, gasync = nullptr;
-  int launches = 0;
+  int launches = 0, base_launches = 0;
+  std::vector<StageDesc> hd1, hd2;         // host copies of the stage descs
+  std::vector<mf::FaceGather> gathers;     // flux-register faces of a hierarchy
 };
 
 extern "C" {
@@ -1060,12 +1062,23 @@ static mf_status enqueue_level_step(mf_level* L, int advance, cudaEvent_t* ev = 
   };
   MF_CHECK_CUDA(mf::launch_exchange((double*)L->U.p, (const CopyReg*)L->exfull.p, L->nfull, nc, s));
   if (L->nfull) mark(0);
+  const int mixed = (p.precision == MF_PREC_MIXED);
+  const void* fl[3] = {L->F[0].p, L->F[1].p, L->F[2].p};
+  auto gather = [&](int mode) -> mf_status {
+    for (const mf::FaceGather& g : L->gathers) {
+      MF_CHECK_CUDA(mf::launch_face_gather(mixed, fl, g, mode, nc, s));
+      mark(5);
+    }
+    return MF_OK;
+  };
+  mf_status gst = MF_OK;
   if (p.time_approximation == MF_TA_RK2) {
     B.uin = (const double*)L->U.p;
     B.uout = (double*)L->U1.p;
     B.ev = ev ? ev + ne : nullptr;
     MF_CHECK_CUDA(mf::launch_stage(c->dp, p.precision, B, L->b1, 0, 1.0, ds, parts, &nb, s));
     stage_marks(ne);
+    if ((gst = gather(0)) != MF_OK) return gst;
     MF_CHECK_CUDA(
         mf::launch_exchange((double*)L->U1.p, (const CopyReg*)L->extwo.p, L->ntwo, nc, s));
     if (L->ntwo) mark(0);
@@ -1076,6 +1089,7 @@ static mf_status enqueue_level_step(mf_level* L, int advance, cudaEvent_t* ev = 
     MF_CHECK_CUDA(mf::launch_stage(c->dp, p.precision, B, L->b2, mf::kStageAverage | mf::kStageDt,
                                    0.5, ds, parts, &nb, s));
     stage_marks(ne);
+    if ((gst = gather(1)) != MF_OK) return gst;
   } else if (p.time_approximation == MF_TA_HANCOCK) {
     B.uin = (const double*)L->U.p;
     B.uout = (double*)L->U.p;
@@ -1091,6 +1105,7 @@ static mf_status enqueue_level_step(mf_level* L, int advance, cudaEvent_t* ev = 
       kinds[ne + 4 + sd] = 3;
       ne += mf::hancock_launches(sd);
     }
+    if ((gst = gather(2)) != MF_OK) return gst;
   } else {
     B.uin = (const double*)L->U.p;
     B.uout = (double*)L->U.p;
@@ -1098,6 +1113,7 @@ static mf_status enqueue_level_step(mf_level* L, int advance, cudaEvent_t* ev = 
     MF_CHECK_CUDA(
         mf::launch_stage(c->dp, p.precision, B, L->b2, mf::kStageDt, 1.0, ds, parts, &nb, s));
     stage_marks(ne);
+    if ((gst = gather(2)) != MF_OK) return gst;
   }
   MF_CHECK_CUDA(mf::launch_finalize(c->dp, parts, L->b2, L->b2.nt[2], ds, advance, s));
   mark(4);
@@ -1153,6 +1169,8 @@ mf_status mf_level_create(mf_ctx* c, int npatch, const mf_box* valid, mf_level**
   L->off = plan.off;
   L->total = plan.total;
   L->cells = plan.cells;
+  L->hd1 = plan.d1;
+  L->hd2 = plan.d2;
   const int mixed = (p.precision == MF_PREC_MIXED);
   const size_t rs = mixed ? sizeof(float) : sizeof(double);
   std::vector<StageDesc> hd(plan.d1);
@@ -1239,6 +1257,7 @@ mf_status mf_level_create(mf_ctx* c, int npatch, const mf_box* valid, mf_level**
                                                           : (per_stage + 1 + 1);
   if (L->nfull == 0) L->launches -= 1;
   if (p.time_approximation == MF_TA_RK2 && L->ntwo == 0) L->launches -= 1;
+  L->base_launches = L->launches;
   *out = L;
   return MF_OK;
 }
@@ -1670,6 +1689,32 @@ CtxView ctx_view(const mf_ctx* c) {
 }
 
 mf_status host_wait(cudaStream_t s, double timeout_s) { return wait_stream(s, timeout_s); }
+
+LevelView level_view(mf_level* L) {
+  LevelView v;
+  v.ctx = L->ctx;
+  v.p = &L->ctx->p;
+  v.np = L->np;
+  v.nc = L->ctx->nc;
+  v.ng = L->ctx->ng;
+  v.valid = &L->valid;
+  v.fab = &L->fab;
+  v.off = &L->off;
+  v.d1 = &L->hd1;
+  v.d2 = &L->hd2;
+  v.U = (double*)L->U.p;
+  v.s = L->s;
+  return v;
+}
+
+void level_set_gathers(mf_level* L, const std::vector<FaceGather>& g) {
+  L->gathers = g;
+  if (L->gsync) cudaGraphExecDestroy(L->gsync);
+  if (L->gasync) cudaGraphExecDestroy(L->gasync);
+  L->gsync = L->gasync = nullptr;
+  const int per = (L->ctx->p.time_approximation == MF_TA_RK2) ? 2 : 1;
+  L->launches = L->base_launches + per * (int)g.size();
+}
 
 mf_status status_of_flags(unsigned flags) { return flags_status(flags); }
 }  // namespace mf

@@ -44,4 +44,41 @@ struct LevelPlan {
 mf_status build_level_plan(const mf_params& p, int ng, int nc, int npatch, const mf_box* valid,
                            LevelPlan& out);
 
+// A face of a level's face-flux arrays, for the flux registers of a
+// hierarchy: offset (elements) of component 0 and the component stride in
+// the layout of the RK2 stage-1 batch [0] and of the final stage [1].
+struct FaceRef {
+  long long off[2];
+  int cs[2];
+  int dir, pad;
+};
+// Faces whose fluxes a level step copies out (out[q * n + i], FP64): the
+// flux of updateState's result, i.e. the average of both RK2 stages, the
+// corrector flux of Hancock, the single stage of first order.
+struct FaceGather {
+  const FaceRef* refs;
+  int n;
+  double* out;
+};
+// mode 0: out = stage-1 flux; 1: out = (out + final flux) / 2; 2: out = final flux
+cudaError_t launch_face_gather(int mixed, const void* const f[3], const FaceGather& g, int mode,
+                               int nc, cudaStream_t s);
+
+// What the coarse-fine coupling needs of a level.
+struct LevelView {
+  mf_ctx* ctx;
+  const mf_params* p;
+  int np, nc, ng;
+  const std::vector<mf_box>* valid;
+  const std::vector<mf_box>* fab;
+  const std::vector<long long>* off;
+  const std::vector<StageDesc>* d1;  // RK2 stage-1 descs (face offsets)
+  const std::vector<StageDesc>* d2;  // final-stage descs
+  double* U;
+  cudaStream_t s;
+};
+LevelView level_view(mf_level* L);
+// Replace the face gathers a level step runs (drops the cached step graphs).
+void level_set_gathers(mf_level* L, const std::vector<FaceGather>& g);
+
 }  // namespace mf

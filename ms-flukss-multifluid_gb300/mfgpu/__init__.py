@@ -187,6 +187,19 @@ _SIGS = {
                                         ctypes.c_void_p]),
     "mf_server_active": (ctypes.c_int, [ctypes.c_void_p]),
     "mf_server_set_priority": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "mf_hier_create": (ctypes.c_int, [ctypes.c_int, _P(ctypes.c_void_p), _P(ctypes.c_int),
+                                      _P(ctypes.c_void_p)]),
+    "mf_hier_destroy": (None, [ctypes.c_void_p]),
+    "mf_hier_set_time": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double]),
+    "mf_hier_times": (ctypes.c_int, [ctypes.c_void_p, _P(ctypes.c_double)]),
+    "mf_hier_step": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double, _P(ctypes.c_double),
+                                    ctypes.c_void_p]),
+    "mf_hier_snapshot": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]),
+    "mf_hier_fill_ghosts": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_double,
+                                           ctypes.c_void_p]),
+    "mf_hier_average_down": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]),
+    "mf_hier_info": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _P(ctypes.c_longlong)]),
+    "mf_hier_launches_per_step": (ctypes.c_int, [ctypes.c_void_p]),
     "mf_init_orszag_host": (ctypes.c_int, [_P(MfParams), _P(MfFab), _P(MfBox)]),
     "mf_init_helio_host": (ctypes.c_int, [_P(MfParams), _P(ctypes.c_double), _P(ctypes.c_double),
                                           _P(MfFab), _P(MfBox)]),
@@ -596,7 +609,7 @@ class Level:
     def launches_per_step(self):
         return self.lib.mf_level_launches_per_step(self.h)
 
-    KIND_NAMES = {0: "exchange", 1: "prim", 2: "flux", 3: "update", 4: "finalize"}
+    KIND_NAMES = {0: "exchange", 1: "prim", 2: "flux", 3: "update", 4: "finalize", 5: "coupling"}
 
     def profile_step(self, dt):
         """One step launch by launch with CUDA events between the launches;
@@ -615,6 +628,66 @@ class Level:
         t = c_int3()
         check(self.lib.mf_level_autotune(self.h, reps, t), "mf_level_autotune")
         return tuple(t)
+
+
+class Hier:
+    """Owner of an mf_hier: levels (coarse to fine, each an open Level with its
+    own Context) coupled by refinement ratios, stepped Berger-Oliger style."""
+
+    def __init__(self, levels, ratios):
+        self.levels = list(levels)
+        self.ratios = list(ratios)
+        self.lib = self.levels[0].lib
+        n = len(self.levels)
+        arr = (ctypes.c_void_p * n)(*[lv.h.value for lv in self.levels])
+        rat = (ctypes.c_int * max(1, n - 1))(*(self.ratios[:n - 1] or [1]))
+        h = ctypes.c_void_p()
+        check(self.lib.mf_hier_create(n, arr, rat, ctypes.byref(h)), "mf_hier_create")
+        self.h = h
+
+    def close(self):
+        if self.h:
+            self.lib.mf_hier_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_time(self, t):
+        check(self.lib.mf_hier_set_time(self.h, t), "mf_hier_set_time")
+
+    def times(self):
+        t = (ctypes.c_double * len(self.levels))()
+        check(self.lib.mf_hier_times(self.h, t), "mf_hier_times")
+        return list(t)
+
+    def step(self, dt0, stream=None):
+        """One step of level 0 with subcycled finer levels; returns new_dt
+        (in level-0 units, before the CFL factor)."""
+        nd = ctypes.c_double()
+        check(self.lib.mf_hier_step(self.h, dt0, ctypes.byref(nd), stream), "mf_hier_step")
+        return nd.value
+
+    def snapshot(self, level, stream=None):
+        check(self.lib.mf_hier_snapshot(self.h, level, stream), "mf_hier_snapshot")
+
+    def fill_ghosts(self, level, alpha, stream=None):
+        check(self.lib.mf_hier_fill_ghosts(self.h, level, alpha, stream), "mf_hier_fill_ghosts")
+
+    def average_down(self, level, stream=None):
+        check(self.lib.mf_hier_average_down(self.h, level, stream), "mf_hier_average_down")
+
+    def info(self, pair):
+        c = (ctypes.c_longlong * 6)()
+        check(self.lib.mf_hier_info(self.h, pair, c), "mf_hier_info")
+        keys = ("sites", "interpolated", "register_faces", "refluxed", "averaged", "coarse_read")
+        return dict(zip(keys, [int(x) for x in c]))
+
+    def launches_per_step(self):
+        return self.lib.mf_hier_launches_per_step(self.h)
 
 
 def run_spec(n, patch, dx, cfl, bc_plasma=None, bc_neutral1=None) -> MfRunSpec:

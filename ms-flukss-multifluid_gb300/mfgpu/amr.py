@@ -11,14 +11,16 @@ batched launches.  Levels are built the way the reference regrids
   the directions;
 * tags are covered by cubic patches whose edge lengths are drawn from a
   seeded distribution over a set of sizes (8, 16, 24, 32 cells by default),
-  on a granule grid of 8 cells, each patch nested inside the next coarser
-  level's patches.  (Chombo's Berger-Rigoutsos clustering is replaced by
-  this seeded cover: the sizes of the patches are the point of the batched
-  form, not the cluster efficiency.)
+  on a granule grid of 8 cells, each patch properly nested inside the next
+  coarser level's patches: a granule is refined only if the granules around
+  it are covered by the coarser level too, so that the coarse-fine
+  interpolation, the flux registers and the averaging of mf_hier read coarse
+  valid cells only (Chombo's proper nesting).  Chombo's Berger-Rigoutsos
+  clustering is replaced by this seeded cover: the sizes of the patches are
+  the point of the batched form, not the cluster efficiency.
 
-The ghost cells of a patch that no sibling covers (coarse-fine edges) hold
-data prolonged from the coarse level when the level is built and are not
-refreshed during the steps: levels are stepped independently.
+DeviceHierarchy steps such a hierarchy on the device through mf_hier
+(subcycled, coarse-fine ghosts interpolated, refluxed, averaged down).
 """
 from __future__ import annotations
 
@@ -194,13 +196,16 @@ def coverage(boxes, n: int) -> np.ndarray:
 
 
 def build_hierarchy(tags0: np.ndarray, ratios=(2, 4), sizes=SIZES, granule: int = GRANULE,
-                    seed: int = 0):
-    """Levels of patches over an n0^3 base grid with cell tags tags0 (z, y, x).
+                    seed: int = 0, nest: int = 1):
+    """Levels of patches over a periodic n0^3 base grid with cell tags tags0
+    (z, y, x).
 
     Level 0 covers the domain; level l (refinement R_l = prod(ratios[:l]))
-    covers the granules whose footprint on the base grid holds a tag, inside
-    the patches of level l-1.  Returns [(refinement, n_l, boxes_l), ...] with
-    boxes in cells of level l."""
+    covers the granules whose footprint on the base grid holds a tag and
+    whose neighbourhood of `nest` granules (periodic) lies inside the patches
+    of level l-1.  One granule (8 fine cells, 8/r coarse cells) is enough
+    buffer for 4 ghost layers at ratios 2 and 4.  Returns
+    [(refinement, n_l, boxes_l), ...] with boxes in cells of level l."""
     rng = np.random.default_rng(seed)
     n0 = tags0.shape[0]
     assert tags0.shape == (n0, n0, n0) and n0 % granule == 0
@@ -223,8 +228,14 @@ def build_hierarchy(tags0: np.ndarray, ratios=(2, 4), sizes=SIZES, granule: int 
         else:
             rep = R // granule
             gt = np.repeat(np.repeat(np.repeat(tags0, rep, 0), rep, 1), rep, 2)
-        # nesting: the granule's footprint on level l-1 (granule / r cells)
-        allowed = _block_all(coverage(bp, np_), granule // r)
+        # nesting: the footprints on level l-1 (granule / r cells) of the
+        # granule and of its neighbours within `nest` granules
+        inside = _block_all(coverage(bp, np_), granule // r)
+        allowed = inside.copy()
+        for dz in range(-nest, nest + 1):
+            for dy in range(-nest, nest + 1):
+                for dx in range(-nest, nest + 1):
+                    allowed &= np.roll(inside, (dz, dy, dx), axis=(0, 1, 2))
         gb = cover(gt, allowed, sizes_g, rng)
         levels.append((R, n, [_cells(b, granule) for b in gb]))
     return levels
@@ -255,3 +266,89 @@ def fill_level_buffer(level, coarse: np.ndarray, refinement: int) -> np.ndarray:
         lo, hi = level.fab_box(i)
         level.patch_view(buf, i)[...] = prolong_fab(coarse, refinement, lo, hi)
     return buf
+
+
+# ---------------------------------------------------------------------------
+# a coupled hierarchy on the device
+# ---------------------------------------------------------------------------
+class DeviceHierarchy:
+    """Levels of a hierarchy resident on the device and coupled by mf_hier.
+
+    params: per-level MfParams (level_params of the base parameters);
+    boxes: per-level valid boxes; ratios: refinement between consecutive
+    levels; init(p, lo, hi) -> conserved state (nc, nz, ny, nx) on a fab box.
+    After the upload the coarse cells under finer patches are averaged from
+    them, so that the composite state is consistent."""
+
+    def __init__(self, mfgpu, params, boxes, ratios, init):
+        self.mfgpu = mfgpu
+        self.params = list(params)
+        self.boxes = [list(b) for b in boxes]
+        self.ratios = list(ratios)
+        self.ctxs = [mfgpu.Context(p) for p in self.params]
+        self.levels = [mfgpu.Level(c, b) for c, b in zip(self.ctxs, self.boxes)]
+        self.bufs = []
+        for lev, p in zip(self.levels, self.params):
+            buf = np.zeros(lev.ndoubles)
+            for i in range(len(lev.boxes)):
+                lo, hi = lev.fab_box(i)
+                lev.patch_view(buf, i)[...] = init(p, lo, hi)
+            lev.upload(buf.ctypes.data)
+            self.bufs.append(buf)
+        self.hier = mfgpu.Hier(self.levels, self.ratios)
+        for lv in range(len(self.levels) - 2, -1, -1):
+            self.hier.average_down(lv)
+
+    def set_dedner_from_dt(self, dt_base):
+        """GLM speeds of every level from the base level's dt (Ch = factor_ch
+        dx0 / dt, Cp = sqrt(Ch dx0 / factor_cp))."""
+        p0 = self.params[0]
+        ch = p0.factor_ch * p0.dx / dt_base
+        cp = float(np.sqrt(ch * p0.dx / p0.factor_cp))
+        for c, p in zip(self.ctxs, self.params):
+            p.dedner_ch, p.dedner_cp = ch, cp
+            c.set_dedner(ch, cp)
+        return ch, cp
+
+    def compute_dt(self):
+        """min over levels of dx/cmax times the level's refinement."""
+        best, R = None, 1
+        for lv, lev in enumerate(self.levels):
+            if lv > 0:
+                R *= self.ratios[lv - 1]
+            v = lev.compute_dt()[0] * R
+            best = v if best is None else min(best, v)
+        return best
+
+    def step(self, dt0, stream=None):
+        return self.hier.step(dt0, stream)
+
+    def download(self, lv):
+        """Host copy (level layout) of level lv's state."""
+        out = np.zeros(self.levels[lv].ndoubles)
+        self.levels[lv].download(out.ctypes.data)
+        return out
+
+    def upload(self, lv, arrays):
+        """Replace level lv's fabs (ghosts included) by host arrays."""
+        buf = np.zeros(self.levels[lv].ndoubles)
+        for i, a in enumerate(arrays):
+            self.levels[lv].patch_view(buf, i)[...] = a
+        self.levels[lv].upload(buf.ctypes.data)
+        self.bufs[lv] = buf
+
+    def cells_per_step(self):
+        """Zone updates of one base step (each level's cells times its steps)."""
+        z, R = 0, 1
+        for lv, lev in enumerate(self.levels):
+            if lv > 0:
+                R *= self.ratios[lv - 1]
+            z += lev.ncells * R
+        return z
+
+    def close(self):
+        self.hier.close()
+        for lev in self.levels:
+            lev.close()
+        for c in self.ctxs:
+            c.close()

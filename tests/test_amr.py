@@ -76,9 +76,14 @@ def test_hierarchy_cover_and_nesting():
             r = R // pR
             under = pcov[::1, ::1, ::1].repeat(r, 0).repeat(r, 1).repeat(r, 2)
             assert not np.any((cov > 0) & (under == 0))
-            # every tagged base cell under the allowed granules is covered
+            # every tagged base cell under the allowed granules is covered; a
+            # granule is allowed when it and its 26 neighbours (periodic) lie
+            # inside level l-1 (proper nesting)
             t = tags.repeat(R, 0).repeat(R, 1).repeat(R, 2) if R > 1 else tags
-            allowed = amr._block_all(under > 0, amr.GRANULE)
+            inside = amr._block_all(under > 0, amr.GRANULE)
+            allowed = inside.copy()
+            for sh in np.ndindex(3, 3, 3):
+                allowed &= np.roll(inside, tuple(x - 1 for x in sh), axis=(0, 1, 2))
             allowed_cells = allowed.repeat(amr.GRANULE, 0).repeat(amr.GRANULE, 1).repeat(
                 amr.GRANULE, 2)
             assert not np.any(t & allowed_cells & (cov == 0))
