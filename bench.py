@@ -463,11 +463,15 @@ def run_amr(mfgpu, torch, stream, a):
     """Batched AMR hierarchy: a three-dimensional Orszag-Tang vortex on an
     n0^3 base grid, 3 levels with refinement ratios 2 then 4, patches of
     8/16/24/32 cells on a side drawn from a seeded distribution where the
-    undivided relative density gradient is >= 0.3.  Each level steps in
-    batched launches replayed from a CUDA graph with autotuned block shapes;
-    a hierarchy step is 1, 2 and 8 steps of levels 0, 1, 2 (subcycling).
-    Beside it: the same levels' patches stepped one mf_patch_update call each
-    (the per-patch form of the reference's level loop)."""
+    undivided relative density gradient is >= 0.3, properly nested.  The
+    levels are coupled by mf_hier_step: a hierarchy step is 1, 2 and 8 steps
+    of levels 0, 1, 2 (subcycling) with the coarse-fine ghosts interpolated
+    in space and time before every fine step, the flux registers fed by every
+    level step, and reflux plus average down when a finer level catches up.
+    Every level steps in batched launches replayed from a CUDA graph with
+    autotuned block shapes.  Beside it: the patches of level 1 stepped one
+    mf_patch_update call each (the per-patch form of the reference's level
+    loop)."""
     import numpy as np
     from mfgpu import amr
 
@@ -496,62 +500,56 @@ def run_amr(mfgpu, torch, stream, a):
     ctx0.close()
     tags = amr.relgrad_tags(U0[0], AMR_THRESHOLD)
     hier = amr.build_hierarchy(tags, ratios=(2, 4), seed=AMR_SEED)
-    nsub = [1, 2, 8]
+    ratios = [2, 4]
 
     def make(prec):
-        levels = []
-        for (R, n, boxes) in hier:
-            p = amr.level_params(amr.orszag3d_params(n0, precision=prec), R)
-            ctx = mfgpu.Context(p)
-            lev = mfgpu.Level(ctx, boxes)
-            buf = amr.fill_level_buffer(lev, U0, R)
-            lev.upload(buf.ctypes.data)
-            shapes = lev.autotune(3)
-            dtl = lev.compute_dt()[0]
-            lev.seed_dt(CFL * dtl, CFL, stream.cuda_stream)
-            levels.append((ctx, lev, shapes))
-        return levels
+        pb = amr.orszag3d_params(n0, precision=prec)
+        params = [amr.level_params(pb, R) for (R, n, boxes) in hier]
+        refine = {id(p): R for p, (R, n, boxes) in zip(params, hier)}
 
-    def hstep(levels):
-        for (ctx, lev, _), k in zip(levels, nsub):
-            for _ in range(k):
-                lev.step_async(stream.cuda_stream)
+        def init(p, lo, hi):
+            return amr.prolong_fab(U0, refine[id(p)], lo, hi)
+
+        dh = amr.DeviceHierarchy(mfgpu, params, [b for (R, n, b) in hier], ratios, init)
+        shapes = [lev.autotune(3) for lev in dh.levels]
+        return dh, shapes
 
     res = {}
     zones = 0
     for name in ("fp64", "mixed"):
-        levels = make(mfgpu.PREC_FP64 if name == "fp64" else mfgpu.PREC_MIXED)
-        zones = sum(lev.ncells * k for (_, lev, _), k in zip(levels, nsub))
+        dh, shapes = make(mfgpu.PREC_FP64 if name == "fp64" else mfgpu.PREC_MIXED)
+        zones = dh.cells_per_step()
+        dt = CFL * dh.compute_dt()
         for _ in range(max(1, min(a.warmup, 2))):
-            hstep(levels)
+            dt = CFL * dh.step(dt, stream.cuda_stream)
         torch.cuda.synchronize()
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(stream)
         for _ in range(a.amr_steps):
-            hstep(levels)
+            dt = CFL * dh.step(dt, stream.cuda_stream)
         e1.record(stream)
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1) / a.amr_steps
-        for (_, lev, _) in levels:
-            mfgpu.check(lev.result(stream.cuda_stream)[0], f"amr {name} steps")
         res[name] = {"value": zones / (ms * 1e-3), "ms_per_hierarchy_step": ms,
-                     "gpu_launches_per_hierarchy_step":
-                         sum(lev.launches_per_step() * k for (_, lev, _), k in zip(levels, nsub))}
+                     "gpu_launches_per_hierarchy_step": dh.hier.launches_per_step()}
         if name == "fp64":
             info = []
-            for (R, n, boxes), (ctx, lev, shapes) in zip(hier, levels):
+            for lv, ((R, n, boxes), lev) in enumerate(zip(hier, dh.levels)):
                 sizes = {}
                 for lo, hi in boxes:
-                    s = hi[0] - lo[0] + 1
-                    sizes[str(s)] = sizes.get(str(s), 0) + 1
-                info.append({"refinement": R, "domain": n, "patches": len(boxes),
-                             "cells": lev.ncells, "patch_sizes": sizes,
-                             "threads_prim_flux_update": list(shapes)})
+                    s_ = hi[0] - lo[0] + 1
+                    sizes[str(s_)] = sizes.get(str(s_), 0) + 1
+                e = {"refinement": R, "domain": n, "patches": len(boxes),
+                     "cells": lev.ncells, "patch_sizes": sizes,
+                     "threads_prim_flux_update": list(shapes[lv])}
+                if lv > 0:
+                    e["coupling_to_coarser"] = dh.hier.info(lv - 1)
+                info.append(e)
             res["levels"] = info
             # per-patch calls: every patch of level 1 once (mf_patch_update
             # returns the patch's dt to the host, as updateState does)
-            ctx1, lev1, _ = levels[1]
+            ctx1, lev1 = dh.ctxs[1], dh.levels[1]
             boxes1 = hier[1][2]
             t0 = time.perf_counter()
             for i, (lo, hi) in enumerate(boxes1):
@@ -559,6 +557,7 @@ def run_amr(mfgpu, torch, stream, a):
                 ctx1.patch_update(lev1.patch_fab_ptr(i), flo, fhi, lo, hi, 1e-9)
             torch.cuda.synchronize()
             wall = time.perf_counter() - t0
+            lev1.seed_dt(1e-9, CFL, stream.cuda_stream)
             ev0 = torch.cuda.Event(enable_timing=True)
             ev1 = torch.cuda.Event(enable_timing=True)
             ev0.record(stream)
@@ -573,17 +572,16 @@ def run_amr(mfgpu, torch, stream, a):
                 "batched_speedup": (lev1.ncells / (lev_ms * 1e-3)) / (lev1.ncells / wall),
                 "path": "one mf_patch_update per patch (host-synchronous, as the reference's "
                         "per-patch loop) vs the batched level step"}
-        for (ctx, lev, _) in levels:
-            lev.close()
-            ctx.close()
+        dh.close()
     res["value"] = res["fp64"]["value"]
     res["zone_updates_per_hierarchy_step"] = zones
     res["mixed_speedup"] = res["mixed"]["value"] / res["fp64"]["value"]
     res["config"] = (f"3D Orszag-Tang (single-fluid ideal MHD, Roe 8-wave, minmod, 8-wave "
                      f"source, RK2), base {n0}^3, ratios 2,4, tags |relgrad rho| >= "
                      f"{AMR_THRESHOLD} after {AMR_TAG_STEPS} base steps, patch sizes "
-                     f"{list(amr.SIZES)} seeded, levels stepped independently "
-                     f"(coarse-fine ghosts held), subcycled 1/2/8")
+                     f"{list(amr.SIZES)} seeded, properly nested; levels coupled by "
+                     f"mf_hier_step (subcycled 1/2/8, coarse-fine ghosts interpolated in "
+                     f"space and time, reflux, average down)")
     return res
 
 
