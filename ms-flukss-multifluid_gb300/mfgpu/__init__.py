@@ -302,7 +302,13 @@ def _base_params(space_dim: int, n_fluids: int) -> MfParams:
     p.factor_ch = 0.0
     p.factor_cp = 1.0
     p.ce_scale_vel = 1.0
-    p.ce_sigma_scale = 1.0
+    # Scale of the charge-exchange rates (the reference's SETCHARGEEX_PARS
+    # dimensional factor).  Inside the reset sphere the wind density grows as
+    # (R0/r)^2, to ~55 in the cell next to the centre on 128^3, where a scale
+    # of 1 puts dt * (loss rate) near 0.7 per stage: the explicit source then
+    # drives the neutral populations through their density floors, in FP64 as
+    # well as in mixed precision.  0.1 keeps that product below ~0.07.
+    p.ce_sigma_scale = 0.1
     p.ce_sigma_a = 2.1
     p.ce_sigma_b = 0.092
     p.ce_damp_c = 0.0
@@ -373,7 +379,13 @@ def helio_params(n: int = 128, seed: int = 20240601, time_approximation: int = T
     rng = np.random.default_rng(seed)
     p.charge_exchange = 1
     p.ce_scale_vel = 1.0
-    p.ce_sigma_scale = 1.0
+    # Scale of the charge-exchange rates (the reference's SETCHARGEEX_PARS
+    # dimensional factor).  Inside the reset sphere the wind density grows as
+    # (R0/r)^2, to ~55 in the cell next to the centre on 128^3, where a scale
+    # of 1 puts dt * (loss rate) near 0.7 per stage: the explicit source then
+    # drives the neutral populations through their density floors, in FP64 as
+    # well as in mixed precision.  0.1 keeps that product below ~0.07.
+    p.ce_sigma_scale = 0.1
     p.ce_sigma_a = float(rng.uniform(1.5, 2.5))
     p.ce_sigma_b = float(rng.uniform(0.05, 0.15))
     p.ce_damp_c = 0.0
