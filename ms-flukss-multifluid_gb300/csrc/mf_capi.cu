@@ -152,7 +152,6 @@ mf_status validate_params(const mf_params& p) {
     if (p.use_8wave) return MF_ERR_UNSUPPORTED;
     if (!(p.flux == 1 || p.flux == 3)) return MF_ERR_UNSUPPORTED;
   }
-  if (p.flux == 5) return MF_ERR_UNSUPPORTED;
   for (int v = 0; v < 8; ++v) {
     int l = p.limiter[v];
     if (!(l == MF_LIM_CD || l == MF_LIM_MINMOD || l == MF_LIM_SUPERBEE || l == MF_LIM_VANALBADA ||
@@ -184,6 +183,7 @@ DevParams make_dev(const mf_params& p) {
       case 2: P.rs = mf::kRusanov; P.aver = 0; break;
       case 3: P.rs = mf::kRoe8; P.aver = 1; break;
       case 4: P.rs = mf::kRusanov; P.aver = 1; break;
+      case 5: P.rs = mf::kVFRoe; P.aver = 0; break;
       case 11: P.rs = mf::kRoe7; P.aver = 0; break;
       case 13: P.rs = mf::kRoe7; P.aver = 1; break;
       default: P.rs = mf::kRoe8; P.aver = 0; break;

@@ -22,7 +22,7 @@ constexpr double k2Pi = 6.28318530717958647692528676655900576;
 constexpr double kNet2Dens = 1.0e-6, kNet2Pres = 1.0e-8;
 constexpr double kNet3Dens = 1.0e-7, kNet3Pres = 1.0e-9;
 
-enum RsKind : int { kRoe8 = 0, kRoe7 = 1, kRusanov = 2 };
+enum RsKind : int { kRoe8 = 0, kRoe7 = 1, kRusanov = 2, kVFRoe = 3 };
 
 // Parameters as the kernels see them (mf_params + derived constants).
 struct DevParams {
@@ -108,6 +108,127 @@ template <typename R> __device__ __forceinline__ R rmax(R a, R b) { return fmax(
 template <typename R> __device__ __forceinline__ R rmin(R a, R b) { return fmin(a, b); }
 template <typename R> __device__ __forceinline__ R rabs(R a) { return fabs(a); }
 template <typename R> __device__ __forceinline__ R rsqrt_(R a) { return sqrt(a); }
+
+// ---------------------------------------------------------------------------
+// VFRoe MHD flux: VFROE_FLUXES (src/VFRoeF.ChF:327-658) with arithmetic
+// averaging, the form RiemannSolver::make builds for flux 5
+// (src/RiemannSolver.cpp:69-74).  The middle state of the linearised Riemann
+// problem (each wave strength times sign(1/2, eigenvalue)) and the exact MHD
+// flux of that state, in the Fortran's order of operations.  wl/wr: rho, u,
+// v, w, p, bx, by, bz in the global frame; g: fluxes in the same order.  One
+// template for every precision mode: the translation unit's contraction
+// flags decide whether products fuse.
+// ---------------------------------------------------------------------------
+template <typename R, int DIR>
+__device__ __forceinline__ void vfroe_mhd(const DevParams& P, const R* wl, const R* wr, R* g) {
+  constexpr int in = 1 + DIR, it1 = 1 + (DIR + 1) % 3, it2 = 1 + (DIR + 2) % 3;
+  constexpr int inB = 5 + DIR, it1B = 5 + (DIR + 1) % 3, it2B = 5 + (DIR + 2) % 3;
+  const R gamma = R(P.gamma), hgamma = R(P.hgamma);
+  const R i4pi = R(kInv4Pi), i8pi = R(kInv8Pi), sq2 = R(kSqrtHalf), pi = R(kPi);
+  const R PGasL = rmax<R>(R(P.smallp), wl[4]), RhoL = rmax<R>(R(P.smallr), wl[0]);
+  const R UL = wl[in], VL = wl[it1], WL = wl[it2], BXL = wl[inB], BYL = wl[it1B], BZL = wl[it2B];
+  const R PGasR = rmax<R>(R(P.smallp), wr[4]), RhoR = rmax<R>(R(P.smallr), wr[0]);
+  const R UR = wr[in], VR = wr[it1], WR = wr[it2], BXR = wr[inB], BYR = wr[it1B], BZR = wr[it2B];
+  // average state
+  const R Rho = R(0.5) * (RhoL + RhoR);
+  const R U = R(0.5) * (UL + UR);
+  const R BX = R(0.5) * (BXL + BXR), BY = R(0.5) * (BYL + BYR), BZ = R(0.5) * (BZL + BZR);
+  const R PGas = R(0.5) * (PGasL + PGasR);
+  const R BX2 = BX * BX, BY2 = BY * BY, BZ2 = BZ * BZ;
+  const R BYZ2 = BY2 + BZ2;
+  const R BxBH = i8pi * (BX2 + BYZ2);
+  const R cc = gamma * PGas / Rho;
+  const R bb = i4pi * BX2 / Rho;
+  const R szb = cc + (BxBH + BxBH) / Rho;
+  const R h = rsqrt_<R>(szb * szb - R(4) * cc * bb);
+  const R aaf = R(0.5) * (szb + h);
+  const R aas = cc * bb / aaf;
+  const R b = rsqrt_<R>(bb), c = rsqrt_<R>(cc), af = rsqrt_<R>(aaf), as = rsqrt_<R>(aas);
+  const R eig[9] = {R(0), U, U, U + b, U - b, U + af, U - af, U + as, U - as};
+  // alphas
+  R alphaF, alphaS;
+  const R dfs = aaf - aas;
+  if (dfs < R(1.0e-12)) {
+    alphaF = R(1);
+    alphaS = R(0);
+  } else if ((cc - aas) <= R(0)) {
+    alphaF = R(0);
+    alphaS = R(1);
+  } else if ((aaf - cc) <= R(0)) {
+    alphaF = R(1);
+    alphaS = R(0);
+  } else {
+    alphaF = rsqrt_<R>((cc - aas) / dfs);
+    alphaS = rsqrt_<R>((aaf - cc) / dfs);
+  }
+  R betaY, betaZ;
+  if (BYZ2 < R(P.smallB) * R(P.smallB)) {
+    betaY = sq2;
+    betaZ = sq2;
+  } else {
+    const R hyz = rsqrt_<R>(BYZ2);
+    betaY = BY / hyz;
+    betaZ = BZ / hyz;
+  }
+  const R siBX = copysign(R(1), BX);
+  R betaYX = betaY, betaZX = betaZ;
+  if (BX < R(0)) {
+    betaYX = -betaY;
+    betaZX = -betaZ;
+  }
+  const R dP = PGasR - PGasL, dRho = RhoR - RhoL, dUn = UR - UL, dUt1 = VR - VL, dUt2 = WR - WL;
+  const R dBt1 = BYR - BYL, dBt2 = BZR - BZL;
+  R a[9];
+  a[0] = R(0);
+  a[1] = dRho - dP / cc;
+  a[2] = BXR - BXL;
+  R h1 = sq2 * (betaY * dUt2 - betaZ * dUt1);
+  R h2 = siBX * (betaZ * dBt1 - betaY * dBt2) / (R(2) * rsqrt_<R>(R(2) * pi * Rho));
+  a[3] = h1 + h2;
+  a[4] = h1 - h2;
+  h1 = dP / (R(2) * Rho * cc);
+  h2 = dUn / (R(2) * cc);
+  const R h3 = (betaY * dBt1 + betaZ * dBt2) / (R(4) * c * rsqrt_<R>(pi * Rho));
+  const R h4 = siBX * (betaY * dUt1 + betaZ * dUt2) / (R(2) * cc);
+  a[5] = alphaF * (h1 + af * h2) + alphaS * (h3 - as * h4);
+  a[6] = alphaF * (h1 - af * h2) + alphaS * (h3 + as * h4);
+  a[7] = alphaS * (h1 + as * h2) - alphaF * (h3 - af * h4);
+  a[8] = alphaS * (h1 - as * h2) - alphaF * (h3 + af * h4);
+  // middle state
+#pragma unroll
+  for (int q = 1; q <= 8; ++q) a[q] = (eig[q] == R(0)) ? R(0) : a[q] * copysign(R(0.5), eig[q]);
+  a[3] = sq2 * a[3];
+  a[4] = sq2 * a[4];
+  const R a34p = a[3] + a[4], a34m = a[3] - a[4];
+  const R a56p = a[5] + a[6], a56m = a[5] - a[6];
+  const R a78p = a[7] + a[8], a78m = a[7] - a[8];
+  const R DN = R(2) * rsqrt_<R>(pi * Rho);
+  const R HRho = Rho * (alphaF * a56p + alphaS * a78p);
+  const R HU = alphaS * as * a56m - alphaF * af * a78m;
+  const R HB = c * (alphaS * a56p - alphaF * a78p);
+  const R RhoM = R(0.5) * (RhoR + RhoL) - (a[1] + HRho);
+  const R UM = R(0.5) * (UR + UL) - (alphaF * af * a56m + alphaS * as * a78m);
+  const R VM = R(0.5) * (VR + VL) + (betaZ * a34p + betaYX * HU);
+  const R WM = R(0.5) * (WR + WL) - (betaY * a34p - betaZX * HU);
+  const R PGasM = R(0.5) * (PGasR + PGasL) - cc * HRho;
+  const R BXM = R(0.5) * (BXR + BXL);
+  const R BYM = R(0.5) * (BYR + BYL) - DN * (betaZX * a34m + betaY * HB);
+  const R BZM = R(0.5) * (BZR + BZL) - DN * (-betaYX * a34m + betaZ * HB);
+  const R BxBM = i8pi * (BXM * BXM + BYM * BYM + BZM * BZM);
+  const R kk = R(0.5) * (UM * UM + VM * VM + WM * WM);
+  const R HUM = BXM * UM + BYM * VM + BZM * WM;
+  R E = PGasM / hgamma + RhoM * kk;
+  const R Pt = PGasM + BxBM;
+  E = E + BxBM;
+  g[0] = RhoM * UM;
+  g[in] = RhoM * UM * UM + Pt - i4pi * BXM * BXM;
+  g[it1] = RhoM * UM * VM - i4pi * BXM * BYM;
+  g[it2] = RhoM * UM * WM - i4pi * BXM * BZM;
+  g[4] = UM * (E + Pt) - i4pi * BXM * HUM;
+  g[inB] = R(0);
+  g[it1B] = UM * BYM - VM * BXM;
+  g[it2B] = UM * BZM - WM * BXM;
+}
 
 // ---------------------------------------------------------------------------
 // conserved -> primitive: CONSTOPRIM (srcIdeal/PatchIdealMHDF.ChF:143-189),

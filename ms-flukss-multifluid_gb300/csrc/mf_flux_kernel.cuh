@@ -15,7 +15,8 @@ using namespace MF_PHYS;
 // dominated plasma, e.g. a cell at the pressure floor) the FP32 products in
 // R |Lambda| L dU lose every digit and the flux can be off by orders of
 // magnitude.  There (c^2 < 1e-3 b^2 on either side) the FP32 path takes the
-// Rusanov flux of the same states instead; FP64 keeps the Roe flux.
+// Rusanov flux of the same states instead; FP64 keeps the Roe flux.  The
+// same holds for VFRoe, whose wave strengths carry 1/c^2 too.
 template <typename R, int DIR>
 __device__ __forceinline__ void plasma_flux(const DevParams& P, const R* wl, const R* wr, R* g) {
   bool cold = false;
@@ -29,6 +30,8 @@ __device__ __forceinline__ void plasma_flux(const DevParams& P, const R* wl, con
   }
   if (cold || P.rs == kRusanov)
     rusanov_mhd<R, DIR>(P, wl, wr, g);
+  else if (P.rs == kVFRoe)
+    vfroe_mhd<R, DIR>(P, wl, wr, g);
   else if (P.rs == kRoe8)
     roe_mhd<R, DIR, false>(P, wl, wr, g);
   else

@@ -125,7 +125,7 @@ static int box_contains(const mf_box* outer, const mf_box* inner) {
 /* model constants                                                           */
 /* ------------------------------------------------------------------------ */
 
-enum { RS_ROE8 = 0, RS_ROE7 = 1, RS_RUSANOV = 2 };
+enum { RS_ROE8 = 0, RS_ROE7 = 1, RS_RUSANOV = 2, RS_VFROE = 3 };
 
 typedef struct {
   const mf_params* p;
@@ -168,7 +168,7 @@ static int ctx_init(Ctx* c, const mf_params* p) {
       case 2: c->rs = RS_RUSANOV; c->aver = 0; break;
       case 3: c->rs = RS_ROE8; c->aver = 1; break;
       case 4: c->rs = RS_RUSANOV; c->aver = 1; break;
-      case 5: return MF_ERR_UNSUPPORTED;
+      case 5: c->rs = RS_VFROE; c->aver = 0; break; /* VFRoeRS, arithmetic averaging */
       case 11: c->rs = RS_ROE7; c->aver = 0; break;
       case 13: c->rs = RS_ROE7; c->aver = 1; break;
       default: c->rs = RS_ROE8; c->aver = 0; break;
@@ -1431,11 +1431,134 @@ static void vanleer_face(const Ctx* c, int idir, int irho, const double* wl, con
 }
 
 /* PatchMHDMF::fluxesRP (srcIdeal/PatchMHDMF.cpp:408-440) on one face. */
+/* VFROE_FLUXES (src/VFRoeF.ChF:327-658) with arithmetic averaging, the only
+   form RiemannSolver::make builds (flux 5, src/RiemannSolver.cpp:69-74): the
+   middle state of the linearised Riemann problem (each wave strength times
+   sign(1/2, eigenvalue)) and the exact MHD flux of that state. */
+static void vfroe_face(const Ctx* c, int idir, const double* wl, const double* wr, double* g) {
+  const double gamma = c->gamma, hgamma = c->hgamma, smallp = c->smallp, smallr = c->smallr;
+  const int inorm = 1 + idir, itan1 = 1 + (idir + 1) % 3, itan2 = 1 + (idir + 2) % 3;
+  const int inormB = 5 + idir, itanB1 = 5 + (idir + 1) % 3, itanB2 = 5 + (idir + 2) % 3;
+  double PGasL = fmax(smallp, wl[4]), RhoL = fmax(smallr, wl[0]);
+  double UL = wl[inorm], VL = wl[itan1], WL = wl[itan2];
+  double BXL = wl[inormB], BYL = wl[itanB1], BZL = wl[itanB2];
+  double PGasR = fmax(smallp, wr[4]), RhoR = fmax(smallr, wr[0]);
+  double UR = wr[inorm], VR = wr[itan1], WR = wr[itan2];
+  double BXR = wr[inormB], BYR = wr[itanB1], BZR = wr[itanB2];
+  /* average state */
+  double Rho = 0.5 * (RhoL + RhoR);
+  double U = 0.5 * (UL + UR);
+  double BX = 0.5 * (BXL + BXR), BY = 0.5 * (BYL + BYR), BZ = 0.5 * (BZL + BZR);
+  double PGas = 0.5 * (PGasL + PGasR);
+  double BX2 = BX * BX, BY2 = BY * BY, BZ2 = BZ * BZ;
+  double BYZ2 = BY2 + BZ2;
+  double BxBH = D_1_8PI * (BX2 + BYZ2);
+  double cc = gamma * PGas / Rho;
+  double bb = D_1_4PI * BX2 / Rho;
+  double szb = cc + (BxBH + BxBH) / Rho;
+  double h = sqrt(szb * szb - 4.0 * cc * bb);
+  double aaf = 0.5 * (szb + h);
+  double aas = cc * bb / aaf;
+  double cs = sqrt(cc), af = sqrt(aaf), as = sqrt(aas);
+  double eig[9];
+  eig[1] = U;
+  eig[2] = U;
+  eig[3] = U + sqrt(bb);
+  eig[4] = U - sqrt(bb);
+  eig[5] = U + af;
+  eig[6] = U - af;
+  eig[7] = U + as;
+  eig[8] = U - as;
+  /* alphas */
+  double alphaF, alphaS;
+  double dfs = aaf - aas;
+  if (dfs < 1.0e-12) {
+    alphaF = 1.0;
+    alphaS = 0.0;
+  } else if ((cc - aas) <= 0.0) {
+    alphaF = 0.0;
+    alphaS = 1.0;
+  } else if ((aaf - cc) <= 0.0) {
+    alphaF = 1.0;
+    alphaS = 0.0;
+  } else {
+    alphaF = sqrt((cc - aas) / dfs);
+    alphaS = sqrt((aaf - cc) / dfs);
+  }
+  double betaY, betaZ;
+  if (BYZ2 < c->smallB * c->smallB) {
+    betaY = D_SQRT_2;
+    betaZ = D_SQRT_2;
+  } else {
+    double hyz = sqrt(BYZ2);
+    betaY = BY / hyz;
+    betaZ = BZ / hyz;
+  }
+  double siBX = copysign(1.0, BX);
+  double betaYX = betaY, betaZX = betaZ;
+  if (BX < 0.0) {
+    betaYX = -betaY;
+    betaZX = -betaZ;
+  }
+  double dP = PGasR - PGasL, dRho = RhoR - RhoL, dUn = UR - UL, dUt1 = VR - VL, dUt2 = WR - WL;
+  double dBt1 = BYR - BYL, dBt2 = BZR - BZL;
+  double a[9];
+  a[1] = dRho - dP / cc;
+  a[2] = BXR - BXL;
+  double h1 = D_SQRT_2 * (betaY * dUt2 - betaZ * dUt1);
+  double h2 = siBX * (betaZ * dBt1 - betaY * dBt2) / (2.0 * sqrt(2.0 * D_PI * Rho));
+  a[3] = h1 + h2;
+  a[4] = h1 - h2;
+  h1 = dP / (2.0 * Rho * cc);
+  h2 = dUn / (2.0 * cc);
+  double h3 = (betaY * dBt1 + betaZ * dBt2) / (4.0 * cs * sqrt(D_PI * Rho));
+  double h4 = siBX * (betaY * dUt1 + betaZ * dUt2) / (2.0 * cc);
+  a[5] = alphaF * (h1 + af * h2) + alphaS * (h3 - as * h4);
+  a[6] = alphaF * (h1 - af * h2) + alphaS * (h3 + as * h4);
+  a[7] = alphaS * (h1 + as * h2) - alphaF * (h3 - af * h4);
+  a[8] = alphaS * (h1 - as * h2) - alphaF * (h3 + af * h4);
+  /* middle state */
+  for (int q = 1; q <= 8; ++q) a[q] = (eig[q] == 0.0) ? 0.0 : a[q] * copysign(0.5, eig[q]);
+  a[3] = D_SQRT_2 * a[3];
+  a[4] = D_SQRT_2 * a[4];
+  double alph3p4 = a[3] + a[4], alph3m4 = a[3] - a[4];
+  double alph5p6 = a[5] + a[6], alph5m6 = a[5] - a[6];
+  double alph7p8 = a[7] + a[8], alph7m8 = a[7] - a[8];
+  double DN = 2.0 * sqrt(D_PI * Rho);
+  double HRho = Rho * (alphaF * alph5p6 + alphaS * alph7p8);
+  double HU = alphaS * as * alph5m6 - alphaF * af * alph7m8;
+  double HB = cs * (alphaS * alph5p6 - alphaF * alph7p8);
+  double RhoM = 0.5 * (RhoR + RhoL) - (a[1] + HRho);
+  double UM = 0.5 * (UR + UL) - (alphaF * af * alph5m6 + alphaS * as * alph7m8);
+  double VM = 0.5 * (VR + VL) + (betaZ * alph3p4 + betaYX * HU);
+  double WM = 0.5 * (WR + WL) - (betaY * alph3p4 - betaZX * HU);
+  double PGasM = 0.5 * (PGasR + PGasL) - cc * HRho;
+  double BXM = 0.5 * (BXR + BXL);
+  double BYM = 0.5 * (BYR + BYL) - DN * (betaZX * alph3m4 + betaY * HB);
+  double BZM = 0.5 * (BZR + BZL) - DN * (-betaYX * alph3m4 + betaZ * HB);
+  double BxBM = D_1_8PI * (BXM * BXM + BYM * BYM + BZM * BZM);
+  double kk = 0.5 * (UM * UM + VM * VM + WM * WM);
+  double HUM = BXM * UM + BYM * VM + BZM * WM;
+  double E = PGasM / hgamma + RhoM * kk;
+  double P = PGasM + BxBM;
+  E = E + BxBM;
+  g[0] = RhoM * UM;
+  g[inorm] = RhoM * UM * UM + P - D_1_4PI * BXM * BXM;
+  g[itan1] = RhoM * UM * VM - D_1_4PI * BXM * BYM;
+  g[itan2] = RhoM * UM * WM - D_1_4PI * BXM * BZM;
+  g[4] = UM * (E + P) - D_1_4PI * BXM * HUM;
+  g[inormB] = 0.0;
+  g[itanB1] = UM * BYM - VM * BXM;
+  g[itanB2] = UM * BZM - WM * BXM;
+}
+
 static void face_flux(const Ctx* c, int dir, const double* wl, const double* wr, double* g) {
   if (c->rs == RS_ROE8)
     roe8_face(c, dir, wl, wr, g);
   else if (c->rs == RS_ROE7)
     roe7_face(c, dir, wl, wr, g);
+  else if (c->rs == RS_VFROE)
+    vfroe_face(c, dir, wl, wr, g);
   else
     rusanov_face(c, dir, wl, wr, g);
   if (c->glm) dedner_face(c, dir, wl, wr, g);

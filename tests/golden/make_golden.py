@@ -21,7 +21,7 @@ import mfgpu  # noqa: E402
 import pyoracle  # noqa: E402
 from helpers import periodic_fill  # noqa: E402
 
-SOLVERS = [(1, 0), (3, 0), (2, 0), (4, 0), (11, 0), (13, 0), (1, 5), (3, 5)]
+SOLVERS = [(1, 0), (3, 0), (2, 0), (4, 0), (11, 0), (13, 0), (1, 5), (3, 5), (5, 0)]
 
 
 def solver_params(flux, cleaning):

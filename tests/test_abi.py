@@ -72,7 +72,7 @@ def test_params_default_and_validation(gpulib):
     ctx = mfgpu.Context(mfgpu.helio_params(32))
     assert ctx.nc == 24 and ctx.ng == 4
     ctx.close()
-    bad = [("space_dim", 4, mfgpu.MF_ERR_BAD_ARG), ("flux", 5, mfgpu.MF_ERR_UNSUPPORTED),
+    bad = [("space_dim", 4, mfgpu.MF_ERR_BAD_ARG), ("divb_method", 3, mfgpu.MF_ERR_BAD_ARG),
            ("time_approximation", 7, mfgpu.MF_ERR_UNSUPPORTED),
            ("precision", 9, mfgpu.MF_ERR_BAD_ARG)]
     for field, val, code in bad:
@@ -83,6 +83,9 @@ def test_params_default_and_validation(gpulib):
     q = mfgpu.helio_params(16)
     q.use_8wave = 1            # GLM with the 8-wave source (main/MHDAM.cpp:1042-1046)
     h = ctypes.c_void_p()
+    assert gpulib.mf_create(ctypes.byref(q), ctypes.byref(h)) == mfgpu.MF_ERR_UNSUPPORTED
+    q = mfgpu.helio_params(16)
+    q.flux = 5                 # GLM with VFRoe (main/MHDAM.cpp:1045)
     assert gpulib.mf_create(ctypes.byref(q), ctypes.byref(h)) == mfgpu.MF_ERR_UNSUPPORTED
     for code in range(10):
         assert mfgpu.status_string(code) != "unknown status"

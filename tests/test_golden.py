@@ -10,7 +10,7 @@ import mfgpu
 from helpers import rel_err, to_device, to_host
 
 HERE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-SOLVERS = [(1, 0), (3, 0), (2, 0), (4, 0), (11, 0), (13, 0), (1, 5), (3, 5)]
+SOLVERS = [(1, 0), (3, 0), (2, 0), (4, 0), (11, 0), (13, 0), (1, 5), (3, 5), (5, 0)]
 RTOL_CPU = 1e-13
 RTOL_GPU = 1e-12
 
