@@ -344,8 +344,8 @@ def test_bad_arguments(gpulib):
     st, _, _ = ctx.patch_update(t.data_ptr(), lo, hi, [0, 0, 0], [15, 15, 0], -1.0,
                                 allow_error=True)
     assert st == mfgpu.MF_ERR_BAD_ARG
-    q = mfgpu.orszag_params(16)
-    q.flux = 5
+    q = mfgpu.helio_params(16)
+    q.flux = 5  # VFRoe with GLM cleaning (main/MHDAM.cpp:1045)
     with pytest.raises(mfgpu.MfError) as ei:
         mfgpu.Context(q)
     assert ei.value.code == mfgpu.MF_ERR_UNSUPPORTED
