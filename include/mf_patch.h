@@ -147,6 +147,15 @@ typedef struct mf_params {
      (mhdam.check_tvd: 1 = the 8 plasma variables, 2 = density and pressure) */
   int char_reconstruction;
   int check_tvd;
+  /* heliosphere boundary fluxes (HeliosphericProblem::fluxBC -> HELIOBC,
+     swlism/HeliosphericProblem.cpp:1994-2188, swlism/HeliosphericF.ChF:221-910):
+     with MF_BC_FARFIELD, the fluxes of the faces on the domain boundary are
+     replaced by the heliosphere's characteristic boundary fluxes (plasma:
+     BFLUXR at the low-x exit, the exact far-field flux at the high-x inflow,
+     BFLUX on the other sides; neutrals: van Leer with outflow copy for fluid 1
+     (and 4), one-way outflow for fluids 2 and 3).  0 keeps the Riemann fluxes
+     of the ghost-filled states. */
+  int helio_bc;
 } mf_params;
 
 struct mf_ctx;

@@ -147,6 +147,7 @@ mf_status validate_params(const mf_params& p) {
     return MF_ERR_BAD_ARG;
   if (p.divb_cleaning != 0 && p.divb_cleaning != 5) return MF_ERR_UNSUPPORTED;
   if (p.check_tvd < 0 || p.check_tvd > 2) return MF_ERR_BAD_ARG;
+  if (p.helio_bc && (p.bc_kind != MF_BC_FARFIELD || p.space_dim != 3)) return MF_ERR_UNSUPPORTED;
   if (p.divb_cleaning == 5) {
     // main/MHDAM.cpp:1042-1046
     if (p.use_8wave) return MF_ERR_UNSUPPORTED;
@@ -194,6 +195,7 @@ DevParams make_dev(const mf_params& p) {
   P.check_pos = p.check_positivity ? 1 : 0;
   P.char_rec = p.char_reconstruction ? 1 : 0;
   P.check_tvd = p.check_tvd;
+  P.helio_bc = (p.helio_bc && p.bc_kind == MF_BC_FARFIELD && p.space_dim == 3) ? 1 : 0;
   P.ce = (p.charge_exchange && p.n_fluids >= 2) ? 1 : 0;
   P.reinit = p.reinit_sphere ? 1 : 0;
   P.bc_kind = p.bc_kind;

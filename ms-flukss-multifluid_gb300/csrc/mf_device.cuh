@@ -30,6 +30,7 @@ struct DevParams {
   int rs, aver;
   int use8, divb_method, check_pos, ce, reinit, bc_kind;
   int char_rec, check_tvd;
+  int helio_bc;  // HELIOBC fluxes on the faces of the domain boundary
   int lim[8];
   int periodic[3], dlo[3], dhi[3];
   double gamma, hgamma, invhgamma, invgamma, smallr, smallp, del2, smallB, dx, invdx;

@@ -38,6 +38,272 @@ __device__ __forceinline__ void plasma_flux(const DevParams& P, const R* wl, con
     roe_mhd<R, DIR, true>(P, wl, wr, g);
 }
 
+
+// ---------------------------------------------------------------------------
+// Heliosphere boundary fluxes: HELIOBC (swlism/HeliosphericF.ChF:221-910)
+// as HeliosphericProblem::fluxBC applies it after the Riemann fluxes
+// (swlism/HeliosphericProblem.cpp:1994-2188), in FP64 in every precision
+// mode (the faces of the domain boundary are a few percent of all faces).
+// Face-frame states: rho, vn, vt1, vt2, p, Bn, Bt1, Bt2; fluxes in the same
+// order.  ROE8WAVEF is RIEMANNF's body without the input floors (the states
+// are floored before), so the unit's Roe 8-wave flux in a frame whose
+// normal is x gives it; VANLEERRS likewise is VANLEERF without its floors.
+// ---------------------------------------------------------------------------
+// BFLUX (:1363-1560) and, with exitR, BFLUXR (:1562-1768); in: domain side,
+// out: ghost side, normal pointing out of the domain.
+__device__ void hbc_bflux(const DevParams& P, bool exitR, const double* in, const double* out,
+                          double* F, double& BnValue) {
+  const double gamma = P.gamma, hgamma = P.hgamma, d_4PI = 4.0 * kPi;
+  const double U = in[1], V = in[2], W = in[3], R = in[0], BX = in[5], BY = in[6], BZ = in[7];
+  const double PG = in[4];
+  const double BB = BX * BX + BY * BY + BZ * BZ;
+  const double Pt = PG + kInv8Pi * BB;
+  const double KE = 0.5 * (in[1] * in[1] + in[2] * in[2] + in[3] * in[3]);
+  const double E = PG / hgamma + in[0] * KE + kInv8Pi * BB;
+  const double SZ = sqrt(gamma * PG / R);
+  const double SP = 0.5 * sqrt(d_4PI * R);
+  const double EM = SZ * SZ + BB / (d_4PI * R) + SZ * fabs(BX) / SP;
+  const double EMM = SZ * SZ + BB / (d_4PI * R) - SZ * fabs(BX) / SP;
+  const double CF = 0.5 * (sqrt(EM) + sqrt(EMM));
+  const double CS = 0.5 * (sqrt(EM) - sqrt(EMM));
+  if (U >= CF) {
+    BnValue = BX;
+    F[0] = R * U;
+    F[1] = R * U * U + Pt - kInv4Pi * BX * BX;
+    F[2] = R * U * V - kInv4Pi * BX * BY;
+    F[3] = R * U * W - kInv4Pi * BX * BZ;
+    F[4] = U * (E + Pt) - kInv4Pi * BX * (U * BX + V * BY + W * BZ);
+    F[5] = 0.0;
+    F[6] = U * BY - V * BX;
+    F[7] = U * BZ - W * BX;
+    return;
+  }
+  const double U1 = out[1], V1 = out[2], W1 = out[3], R1 = out[0], BX1 = out[5], BY1 = out[6];
+  const double BZ1 = out[7], PG1 = out[4];
+  const double BB1 = BX1 * BX1 + BY1 * BY1 + BZ1 * BZ1;
+  const double P1 = PG1 + kInv8Pi * BB1;
+  const double KE1 = 0.5 * (out[1] * out[1] + out[2] * out[2] + out[3] * out[3]);
+  const double E1 = PG1 / hgamma + out[0] * KE1 + kInv8Pi * BB1;
+  if (U < -CF) {
+    BnValue = BX1;
+    F[0] = R1 * U1;
+    F[1] = R1 * U1 * U1 + P1 - kInv4Pi * BX1 * BX1;
+    F[2] = R1 * U1 * V1 - kInv4Pi * BX1 * BY1;
+    F[3] = R1 * U1 * W1 - kInv4Pi * BX1 * BZ1;
+    F[4] = U1 * (E1 + P1) - kInv4Pi * BX1 * (U1 * BX1 + V1 * BY1 + W1 * BZ1);
+    F[5] = 0.0;
+    F[6] = U1 * BY1 - V1 * BX1;
+    F[7] = U1 * BZ1 - W1 * BX1;
+    return;
+  }
+  const double SZ1 = sqrt(gamma * PG1 / R1);
+  const double SP1 = 0.5 * sqrt(d_4PI * R1);
+  const double EM1 = SZ1 * SZ1 + BB1 / (d_4PI * R1) + SZ1 * fabs(BX1) / SP1;
+  const double EMM1 = SZ1 * SZ1 + BB1 / (d_4PI * R1) - SZ1 * fabs(BX1) / SP1;
+  const double CF1 = 0.5 * (sqrt(EM1) + sqrt(EMM1));
+  const bool middle = exitR ? ((U < CF) && (U >= 0.0)) : ((U < CF) && (U >= 0.0) && (U1 > CF1));
+  if (middle) {
+    const double SCM = SZ * SZ - CS * CS;
+    const double SCP = SZ * SZ + CS * CS;
+    const double DEM = sqrt(EM * EMM);
+    double THE = -0.5 * CF * (BX * BX) / (R * d_4PI * DEM);
+    THE = THE + (BZ * BZ + BY * BY) * CF * SCP * 0.5 / (R * DEM * d_4PI * SCM);
+    THE = THE + 0.5 * CF * hgamma * (SZ * SZ) / DEM;
+    THE = THE - SZ * fabs(BX) * CS * (gamma - 2.0) * 0.25 / (SP * DEM);
+    const double hyz = BY * BY + BZ * BZ;
+    double hy2, hz2;
+    if (hyz < 1.0e-10) {
+      hy2 = 0.5;
+      hz2 = 0.5;
+    } else {
+      hy2 = BY * BY / hyz;
+      hz2 = BZ * BZ / hyz;
+    }
+    double U16, R16, DRho, HRho, SZ16, BY16, BZ16;
+    if (exitR) {
+      const double BE = 2.0 * d_4PI * (CF * CF - SZ * SZ);
+      R16 = fmax(R + R * (U - CF) / (THE + CF), 1.0e-14);
+      DRho = R16 - R;
+      HRho = DRho / R;
+      U16 = U - HRho * CF;
+      SZ16 = SZ * (1.0 + 0.5 * hgamma * HRho);
+      BZ16 = BZ * BZ + BE * hz2 * DRho;
+      BY16 = BY * BY + BE * hy2 * DRho;
+    } else {
+      U16 = (U * THE + CF * CF) / (THE + CF);
+      HRho = (U - CF) / (THE + CF);
+      DRho = R * HRho;
+      R16 = R + DRho;
+      SZ16 = SZ * (1.0 + 0.5 * hgamma * HRho);
+      const double BE = 2.0 * d_4PI * (CF * CF - SZ * SZ) * DRho;
+      BZ16 = BZ * BZ + BE * hz2;
+      BY16 = BY * BY + BE * hy2;
+    }
+    if (BZ16 <= 0.0) {
+      BZ16 = 0.0;
+    } else {
+      BZ16 = sqrt(BZ16);
+      if (BZ < 0.0) BZ16 = -BZ16;
+    }
+    if (BY16 <= 0.0) {
+      BY16 = 0.0;
+    } else {
+      BY16 = sqrt(BY16);
+      if (BY < 0.0) BY16 = -BY16;
+    }
+    const double BX16 = BX;
+    const double ALF = kInv4Pi * BX / (R * CF);
+    const double W16 = W + ALF * (BZ16 - BZ);
+    const double V16 = V + ALF * (BY16 - BY);
+    const double PG16 = SZ16 * SZ16 * R16 / gamma;
+    const double BB16 = kInv4Pi * (BX16 * BX16 + BY16 * BY16 + BZ16 * BZ16);
+    const double P16 = PG16 + 0.5 * BB16;
+    const double E16 = PG16 / hgamma + 0.5 * (R16 * (U16 * U16 + V16 * V16 + W16 * W16) + BB16);
+    const double BXq = kInv4Pi * BX16;
+    BnValue = BX16;
+    F[0] = R16 * U16;
+    F[1] = R16 * U16 * U16 + P16 - BXq * BX16;
+    F[2] = R16 * U16 * V16 - BXq * BY16;
+    F[3] = R16 * U16 * W16 - BXq * BZ16;
+    F[4] = U16 * (E16 + P16) - BXq * (U16 * BX16 + V16 * BY16 + W16 * BZ16);
+    F[5] = 0.0;
+    F[6] = U16 * BY16 - V16 * BX16;
+    F[7] = U16 * BZ16 - W16 * BX16;
+    return;
+  }
+  if (exitR && U >= 0.0) {
+    const double o2[8] = {in[0], in[1], in[2], in[3], out[4], out[5], out[6], out[7]};
+    BnValue = BX;
+    roe_mhd<double, 0, false>(P, in, o2, F);
+  } else {
+    BnValue = 0.5 * (BX + BX1);
+    roe_mhd<double, 0, false>(P, in, out, F);
+  }
+}
+
+// plasma fluxes 0..7 and Bn of a face on the domain boundary (side 0: low
+// face, wl is the ghost side; 1: high face, wr is the ghost side)
+template <int DIR>
+__device__ void helio_plasma(const DevParams& P, const RunParams& RP, int side, const double* wl,
+                             const double* wr, double* g, double& bn) {
+  constexpr int t1 = (DIR + 1) % 3, t2 = (DIR + 2) % 3;
+  const int iv[3] = {1 + DIR, 1 + t1, 1 + t2}, ib[3] = {5 + DIR, 5 + t1, 5 + t2};
+  if (DIR == 0 && side == 1) {  // inflow: the exact flux of the far-field state
+    const double* b = RP.bc_plasma;
+    const double density = b[0], velx = b[1], vely = b[2], velz = b[3], pressure = b[4];
+    const double Bx = b[5], By = b[6], Bz = b[7];
+    const double bm = kInv8Pi * (Bx * Bx + By * By + Bz * Bz);
+    const double ke = density * (velx * velx + vely * vely + velz * velz);
+    const double bu = Bx * velx + By * vely + Bz * velz;
+    const double Pt = pressure + bm;
+    const double e = pressure / P.hgamma + 0.5 * ke + bm;
+    g[0] = density * velx;
+    g[1] = density * velx * velx - kInv4Pi * Bx * Bx + Pt;
+    g[2] = density * velx * vely - kInv4Pi * Bx * By;
+    g[3] = density * velx * velz - kInv4Pi * Bx * Bz;
+    g[4] = velx * (e + Pt) - kInv4Pi * Bx * bu;
+    g[5] = 0.0;
+    g[6] = velx * By - vely * Bx;
+    g[7] = velx * Bz - velz * Bx;
+    bn = Bx;
+    return;
+  }
+  const double* Win = side ? wl : wr;
+  const double* Wout = side ? wr : wl;
+  const double sg = side ? 1.0 : -1.0;
+  double L[8], Rt[8], F[8], Bv;
+  L[0] = Win[0];
+  Rt[0] = Wout[0];
+  L[4] = Win[4];
+  Rt[4] = Wout[4];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    L[1 + a] = sg * Win[iv[a]];
+    Rt[1 + a] = sg * Wout[iv[a]];
+    L[5 + a] = sg * Win[ib[a]];
+    Rt[5 + a] = sg * Wout[ib[a]];
+  }
+  Rt[0] = fmax(P.smallr, Rt[0]);
+  Rt[4] = fmax(P.smallp, Rt[4]);
+  L[0] = fmax(P.smallr, L[0]);
+  L[4] = fmax(P.smallp, L[4]);
+  hbc_bflux(P, DIR == 0, L, Rt, F, Bv);
+  g[0] = sg * F[0];
+  g[iv[0]] = F[1];
+  g[iv[1]] = F[2];
+  g[iv[2]] = F[3];
+  g[4] = sg * F[4];
+  g[ib[0]] = F[5];
+  g[ib[1]] = F[6];
+  g[ib[2]] = F[7];
+  bn = sg * Bv;
+}
+
+// one neutral population (fl = 1, 2, 3, 4) of a face on the domain boundary;
+// nl / nr: rho, u, v, w, p of the two face states (global frame)
+template <int DIR>
+__device__ void helio_neutral(const DevParams& P, int side, int fl, const double* nl,
+                              const double* nr, double* gn) {
+  constexpr int t1 = (DIR + 1) % 3, t2 = (DIR + 2) % 3;
+  const int nv[3] = {1 + DIR, 1 + t1, 1 + t2};
+  const double* Win = side ? nl : nr;
+  const double* Wout = side ? nr : nl;
+  auto outflow = [&](const double* st, double vn) {
+    const double rho = st[0], vt1 = st[2], vt2 = st[3], p = st[4];
+    const double ke = rho * (vn * vn + vt1 * vt1 + vt2 * vt2);
+    const double e = p / P.hgamma + 0.5 * ke;
+    gn[0] = rho * vn;
+    gn[nv[0]] = rho * vn * vn + p;
+    gn[nv[1]] = rho * vn * vt1;
+    gn[nv[2]] = rho * vn * vt2;
+    gn[4] = vn * (e + p);
+  };
+  if (fl == 2 || fl == 3) {
+    const double fd = (fl == 2) ? kNet2Dens : kNet3Dens, fp = (fl == 2) ? kNet2Pres : kNet3Pres;
+    const double st[5] = {fmax(fd, Win[0]), Win[nv[0]], Win[nv[1]], Win[nv[2]], fmax(fp, Win[4])};
+    outflow(st, side ? fmax(0.0, st[1]) : fmin(0.0, st[1]));
+    return;
+  }
+  if (side == 0 && DIR == 0) {
+    const double st[5] = {fmax(P.smallr, Win[0]), Win[nv[0]], Win[nv[1]], Win[nv[2]],
+                          fmax(P.smallp, Win[4])};
+    outflow(st, fmin(-1.0e-6, st[1]));
+    return;
+  }
+  const double sg = side ? 1.0 : -1.0;
+  double Ln[5], Rn[5], gl[5];
+  Ln[0] = fmax(P.smallr, Win[0]);
+  Ln[4] = fmax(P.smallp, Win[4]);
+  Rn[0] = fmax(P.smallr, Wout[0]);
+  Rn[4] = fmax(P.smallp, Wout[4]);
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    Ln[1 + a] = sg * Win[nv[a]];
+    Rn[1 + a] = sg * Wout[nv[a]];
+  }
+  if (Ln[1] > 0.0) {
+    Rn[1] = Ln[1];
+    Rn[2] = Ln[2];
+    Rn[3] = Ln[3];
+    if (fl == 1) Rn[0] = Ln[0];
+  }
+  vanleer_euler<double, 0>(P, Ln, Rn, gl);
+  gn[0] = sg * gl[0];
+  gn[nv[0]] = gl[1];
+  gn[nv[1]] = gl[2];
+  gn[nv[2]] = gl[3];
+  gn[4] = sg * gl[4];
+}
+
+// side of the domain boundary a face lies on (-1: interior or periodic)
+template <int DIR>
+__device__ __forceinline__ int helio_side(const DevParams& P, const RunParams& RP, int i, int j,
+                                          int k) {
+  if (!P.helio_bc || P.periodic[DIR]) return -1;
+  const int f = (DIR == 0) ? i : (DIR == 1) ? j : k;
+  return (f == RP.dlo[DIR]) ? 0 : (f == RP.dhi[DIR] + 1) ? 1 : -1;
+}
+
 template <typename R, int DIR>
 __global__ void __launch_bounds__(kMaxBlock)
     k_flux(const DevParams P, const double* __restrict__ W, R* __restrict__ F,
@@ -128,9 +394,6 @@ __global__ void __launch_bounds__(kMaxBlock)
     g[5 + DIR] = fbn;
     g[8] = fpsi;
   }
-#pragma unroll
-  for (int q = 0; q < 8; ++q) Fo[q * fcs] = g[q];
-  if (P.glm) Fo[8 * fcs] = g[8];
 
   // face-normal B (PatchMHDMF::computeBn, srcIdeal/PatchMHDMF.cpp:509-620)
   R bn = R(0);
@@ -145,6 +408,23 @@ __global__ void __launch_bounds__(kMaxBlock)
     const double* wv = w0 + (5 + DIR) * cs;
     bn = R(0.5 * (wv[-st] + wv[0]));
   }
+  // HELIOBC on the domain boundary (after the Riemann fluxes and Bn)
+  const int hside = helio_side<DIR>(P, RP, i, j, k);
+  if (hside >= 0) {
+    double dl[8], dr[8], dg[8], dbn = double(bn);
+#pragma unroll
+    for (int v = 0; v < 8; ++v) {
+      dl[v] = double(wl[v]);
+      dr[v] = double(wr[v]);
+    }
+    helio_plasma<DIR>(P, RP, hside, dl, dr, dg, dbn);
+#pragma unroll
+    for (int v = 0; v < 8; ++v) g[v] = R(dg[v]);
+    bn = R(dbn);
+  }
+#pragma unroll
+  for (int q = 0; q < 8; ++q) Fo[q * fcs] = g[q];
+  if (P.glm) Fo[8 * fcs] = g[8];
   Bn[D.bn_off[DIR] + fo] = bn;
 
   // neutral fluids: minmod face states, van Leer splitting (VANLEERF)
@@ -161,7 +441,19 @@ __global__ void __launch_bounds__(kMaxBlock)
       face_values<R>(MF_LIM_MINMOD, b, c, d, lo, hi);
       nr[m] = negR ? c : lo;
     }
-    vanleer_euler<R, DIR>(P, nl, nr, gn);
+    if (hside >= 0) {
+      double dl[5], dr[5], dg[5];
+#pragma unroll
+      for (int m = 0; m < 5; ++m) {
+        dl[m] = double(nl[m]);
+        dr[m] = double(nr[m]);
+      }
+      helio_neutral<DIR>(P, hside, fl, dl, dr, dg);
+#pragma unroll
+      for (int m = 0; m < 5; ++m) gn[m] = R(dg[m]);
+    } else {
+      vanleer_euler<R, DIR>(P, nl, nr, gn);
+    }
 #pragma unroll
     for (int m = 0; m < 5; ++m) Fo[(s + m) * fcs] = gn[m];
   }
@@ -210,9 +502,6 @@ __global__ void __launch_bounds__(kMaxBlock)
     g[5 + DIR] = fbn;
     g[8] = fpsi;
   }
-#pragma unroll
-  for (int q = 0; q < 8; ++q) Fo[q * fcs] = g[q];
-  if (P.glm) Fo[8 * fcs] = g[8];
   R bn = R(0);
   if (P.divb_method == 1) {
     bn = R(0.5) * (wl[5 + DIR] + wr[5 + DIR]);
@@ -228,6 +517,23 @@ __global__ void __launch_bounds__(kMaxBlock)
     const double* wv = W + D.u_off + loc(D.flo, D.fn, i, j, k) + (5 + DIR) * cs;
     bn = R(0.5 * (wv[-st] + wv[0]));
   }
+  // fluxBC of correctorHancock (src/PatchMHDAM.cpp:1105-1106)
+  const int hside = helio_side<DIR>(P, RP, i, j, k);
+  if (hside >= 0) {
+    double dl[8], dr[8], dg[8], dbn = double(bn);
+#pragma unroll
+    for (int v = 0; v < 8; ++v) {
+      dl[v] = double(wl[v]);
+      dr[v] = double(wr[v]);
+    }
+    helio_plasma<DIR>(P, RP, hside, dl, dr, dg, dbn);
+#pragma unroll
+    for (int v = 0; v < 8; ++v) g[v] = R(dg[v]);
+    bn = R(dbn);
+  }
+#pragma unroll
+  for (int q = 0; q < 8; ++q) Fo[q * fcs] = g[q];
+  if (P.glm) Fo[8 * fcs] = g[8];
   Bn[D.bn_off[DIR] + loc(D.vlo, fnb, i, j, k)] = bn;
   for (int fl = 1; fl < P.nf; ++fl) {
     const int s0 = P.irhon + (fl - 1) * 5;
@@ -237,7 +543,19 @@ __global__ void __launch_bounds__(kMaxBlock)
       nl[m] = R(fv[(nc + s0 + m) * scs + cl]);
       nr[m] = R(fv[(s0 + m) * scs + cr]);
     }
-    vanleer_euler<R, DIR>(P, nl, nr, gn);
+    if (hside >= 0) {
+      double dl[5], dr[5], dg[5];
+#pragma unroll
+      for (int m = 0; m < 5; ++m) {
+        dl[m] = double(nl[m]);
+        dr[m] = double(nr[m]);
+      }
+      helio_neutral<DIR>(P, hside, fl, dl, dr, dg);
+#pragma unroll
+      for (int m = 0; m < 5; ++m) gn[m] = R(dg[m]);
+    } else {
+      vanleer_euler<R, DIR>(P, nl, nr, gn);
+    }
 #pragma unroll
     for (int m = 0; m < 5; ++m) Fo[(s0 + m) * fcs] = gn[m];
   }

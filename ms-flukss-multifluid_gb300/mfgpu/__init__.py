@@ -108,6 +108,7 @@ class MfParams(ctypes.Structure):
         ("bc_neutral1", ctypes.c_double * 5),
         ("char_reconstruction", ctypes.c_int),
         ("check_tvd", ctypes.c_int),
+        ("helio_bc", ctypes.c_int),
     ]
 
 
@@ -407,6 +408,9 @@ def helio_params(n: int = 128, seed: int = 20240601, time_approximation: int = T
     p.sun_beta = 2.0
     p.dir_br = 1.0
     p.bc_kind = BC_FARFIELD
+    # the heliosphere's boundary fluxes on the faces of the domain boundary
+    # (HeliosphericProblem::fluxBC -> HELIOBC)
+    p.helio_bc = 1
     wp, wn = helio_inflow()
     for q in range(8):
         p.bc_plasma[q] = wp[q]

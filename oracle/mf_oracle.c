@@ -1565,6 +1565,286 @@ static void face_flux(const Ctx* c, int dir, const double* wl, const double* wr,
   for (int f = 1; f < c->nf; ++f) vanleer_face(c, dir, c->irhon + (f - 1) * 5, wl, wr, g);
 }
 
+
+/* ------------------------------------------------------------------------ */
+/* heliosphere boundary fluxes                                               */
+/* ------------------------------------------------------------------------ */
+/* States below are in the frame of a face: rho, vn, vt1, vt2, p, Bn, Bt1, Bt2
+   (tangential directions (d+1)%3, (d+2)%3); fluxes in the same order
+   (mass, normal and tangential momentum, energy, Bn, Bt1, Bt2). */
+
+/* ROE8WAVEF (src/Roe8WaveF.ChF:604-1144) is the body of RIEMANNF without the
+   input floors; its callers floor rho and p first, so RIEMANNF on the same
+   states in a frame whose normal is x gives it exactly. */
+static void roe8_local(const Ctx* c, const double* L, const double* R, double* F) {
+  roe8_face(c, 0, L, R, F);
+}
+
+/* BFLUX (swlism/HeliosphericF.ChF:1363-1560) and, with exitR, BFLUXR
+   (:1562-1768; its position arguments only feed a radial speed it does not
+   use).  in: the domain side, out: the ghost side, normal pointing out. */
+static void bflux(const Ctx* c, int exitR, const double* in, const double* out, double* F,
+                  double* BnValue) {
+  const double gamma = c->gamma, hgamma = c->hgamma, d_4PI = 4.0 * D_PI;
+  double U = in[1], V = in[2], W = in[3], R = in[0], BX = in[5], BY = in[6], BZ = in[7];
+  double PG = in[4];
+  double BB = BX * BX + BY * BY + BZ * BZ;
+  double P = PG + D_1_8PI * BB;
+  double KE = 0.5 * (in[1] * in[1] + in[2] * in[2] + in[3] * in[3]);
+  double E = PG / hgamma + in[0] * KE + D_1_8PI * BB;
+  double SZ = sqrt(gamma * PG / R);
+  double B2 = BB;
+  double SP = 0.5 * sqrt(d_4PI * R);
+  double EM = SZ * SZ + B2 / (d_4PI * R) + SZ * fabs(BX) / SP;
+  double EMM = SZ * SZ + B2 / (d_4PI * R) - SZ * fabs(BX) / SP;
+  double CF = 0.5 * (sqrt(EM) + sqrt(EMM));
+  double CS = 0.5 * (sqrt(EM) - sqrt(EMM));
+  if (U >= CF) {
+    *BnValue = BX;
+    F[0] = R * U;
+    F[1] = R * U * U + P - D_1_4PI * BX * BX;
+    F[2] = R * U * V - D_1_4PI * BX * BY;
+    F[3] = R * U * W - D_1_4PI * BX * BZ;
+    F[4] = U * (E + P) - D_1_4PI * BX * (U * BX + V * BY + W * BZ);
+    F[5] = 0.0;
+    F[6] = U * BY - V * BX;
+    F[7] = U * BZ - W * BX;
+    return;
+  }
+  double U1 = out[1], V1 = out[2], W1 = out[3], R1 = out[0], BX1 = out[5], BY1 = out[6];
+  double BZ1 = out[7], PG1 = out[4];
+  double BB1 = BX1 * BX1 + BY1 * BY1 + BZ1 * BZ1;
+  double P1 = PG1 + D_1_8PI * BB1;
+  double KE1 = 0.5 * (out[1] * out[1] + out[2] * out[2] + out[3] * out[3]);
+  double E1 = PG1 / hgamma + out[0] * KE1 + D_1_8PI * BB1;
+  if (U < -CF) {
+    *BnValue = BX1;
+    F[0] = R1 * U1;
+    F[1] = R1 * U1 * U1 + P1 - D_1_4PI * BX1 * BX1;
+    F[2] = R1 * U1 * V1 - D_1_4PI * BX1 * BY1;
+    F[3] = R1 * U1 * W1 - D_1_4PI * BX1 * BZ1;
+    F[4] = U1 * (E1 + P1) - D_1_4PI * BX1 * (U1 * BX1 + V1 * BY1 + W1 * BZ1);
+    F[5] = 0.0;
+    F[6] = U1 * BY1 - V1 * BX1;
+    F[7] = U1 * BZ1 - W1 * BX1;
+    return;
+  }
+  double SZ1 = sqrt(gamma * PG1 / R1);
+  double SP1 = 0.5 * sqrt(d_4PI * R1);
+  double EM1 = SZ1 * SZ1 + BB1 / (d_4PI * R1) + SZ1 * fabs(BX1) / SP1;
+  double EMM1 = SZ1 * SZ1 + BB1 / (d_4PI * R1) - SZ1 * fabs(BX1) / SP1;
+  double CF1 = 0.5 * (sqrt(EM1) + sqrt(EMM1));
+  int middle = exitR ? ((U < CF) && (U >= 0.0)) : ((U < CF) && (U >= 0.0) && (U1 > CF1));
+  if (middle) {
+    double SCM = SZ * SZ - CS * CS;
+    double SCP = SZ * SZ + CS * CS;
+    double DEM = sqrt(EM * EMM);
+    double THE = -0.5 * CF * (BX * BX) / (R * d_4PI * DEM);
+    THE = THE + (BZ * BZ + BY * BY) * CF * SCP * 0.5 / (R * DEM * d_4PI * SCM);
+    THE = THE + 0.5 * CF * hgamma * (SZ * SZ) / DEM;
+    THE = THE - SZ * fabs(BX) * CS * (gamma - 2.0) * 0.25 / (SP * DEM);
+    double hyz = BY * BY + BZ * BZ, hy2, hz2;
+    if (hyz < 1.0e-10) {
+      hy2 = 0.5;
+      hz2 = 0.5;
+    } else {
+      hy2 = BY * BY / hyz;
+      hz2 = BZ * BZ / hyz;
+    }
+    double U16, R16, DRho, HRho, SZ16, BY16, BZ16;
+    if (exitR) {
+      double BE = 2.0 * d_4PI * (CF * CF - SZ * SZ);
+      R16 = fmax(R + R * (U - CF) / (THE + CF), 1.0e-14);
+      DRho = R16 - R;
+      HRho = DRho / R;
+      U16 = U - HRho * CF;
+      SZ16 = SZ * (1.0 + 0.5 * hgamma * HRho);
+      BZ16 = BZ * BZ + BE * hz2 * DRho;
+      BY16 = BY * BY + BE * hy2 * DRho;
+    } else {
+      U16 = (U * THE + CF * CF) / (THE + CF);
+      HRho = (U - CF) / (THE + CF);
+      DRho = R * HRho;
+      R16 = R + DRho;
+      SZ16 = SZ * (1.0 + 0.5 * hgamma * HRho);
+      double BE = 2.0 * d_4PI * (CF * CF - SZ * SZ) * DRho;
+      BZ16 = BZ * BZ + BE * hz2;
+      BY16 = BY * BY + BE * hy2;
+    }
+    if (BZ16 <= 0.0) {
+      BZ16 = 0.0;
+    } else {
+      BZ16 = sqrt(BZ16);
+      if (BZ < 0.0) BZ16 = -BZ16;
+    }
+    if (BY16 <= 0.0) {
+      BY16 = 0.0;
+    } else {
+      BY16 = sqrt(BY16);
+      if (BY < 0.0) BY16 = -BY16;
+    }
+    double BX16 = BX;
+    double ALF = D_1_4PI * BX / (R * CF);
+    double W16 = W + ALF * (BZ16 - BZ);
+    double V16 = V + ALF * (BY16 - BY);
+    double PG16 = SZ16 * SZ16 * R16 / gamma;
+    double BB16 = D_1_4PI * (BX16 * BX16 + BY16 * BY16 + BZ16 * BZ16);
+    double P16 = PG16 + 0.5 * BB16;
+    double E16 = PG16 / hgamma + 0.5 * (R16 * (U16 * U16 + V16 * V16 + W16 * W16) + BB16);
+    double BXq = D_1_4PI * BX16;
+    *BnValue = BX16;
+    F[0] = R16 * U16;
+    F[1] = R16 * U16 * U16 + P16 - BXq * BX16;
+    F[2] = R16 * U16 * V16 - BXq * BY16;
+    F[3] = R16 * U16 * W16 - BXq * BZ16;
+    F[4] = U16 * (E16 + P16) - BXq * (U16 * BX16 + V16 * BY16 + W16 * BZ16);
+    F[5] = 0.0;
+    F[6] = U16 * BY16 - V16 * BX16;
+    F[7] = U16 * BZ16 - W16 * BX16;
+    return;
+  }
+  if (exitR && U >= 0.0) {
+    double o2[8] = {in[0], in[1], in[2], in[3], out[4], out[5], out[6], out[7]};
+    *BnValue = BX;
+    roe8_local(c, in, o2, F);
+  } else {
+    *BnValue = 0.5 * (BX + BX1);
+    roe8_local(c, in, out, F);
+  }
+}
+
+/* One neutral population's outflow-only flux from the domain-side state
+   (HELIOBC, the formula of the fluid 2/3 branches and of fluid 1 on the
+   low-x side). */
+static void neutral_outflow(const Ctx* c, const double* s, double vn, double* F) {
+  double rho = s[0], vt1 = s[2], vt2 = s[3], p = s[4];
+  double ke = rho * (vn * vn + vt1 * vt1 + vt2 * vt2);
+  double e = p / c->hgamma + 0.5 * ke;
+  F[0] = rho * vn;
+  F[1] = rho * vn * vn + p;
+  F[2] = rho * vn * vt1;
+  F[3] = rho * vn * vt2;
+  F[4] = vn * (e + p);
+}
+
+/* HELIOBC (swlism/HeliosphericF.ChF:221-910) on one face of the domain
+   boundary in direction d; side 0: low face (wl is the ghost side), 1: high
+   face (wr is the ghost side).  Overwrites the plasma fluxes 0..7, the
+   neutral fluxes and Bn (the GLM psi flux stays). */
+static void helio_bc_face(const Ctx* c, int d, int side, const double* wl, const double* wr,
+                          double* g, double* bn) {
+  const int t1 = (d + 1) % 3, t2 = (d + 2) % 3;
+  const int iv[3] = {1 + d, 1 + t1, 1 + t2}, ib[3] = {5 + d, 5 + t1, 5 + t2};
+  const double smallr = c->smallr, smallp = c->smallp;
+  double F[8], Bv;
+  /* local states: inner (domain side) and outer (ghost side); low faces are
+     mirrored so that the normal points out of the domain */
+  const double* Win = side ? wl : wr;
+  const double* Wout = side ? wr : wl;
+  const double sg = side ? 1.0 : -1.0;
+  if (d == 0 && side == 1) {
+    /* inflow: the exact flux of the far-field state */
+    const double* b = c->p->bc_plasma;
+    double density = b[0], velx = b[1], vely = b[2], velz = b[3], pressure = b[4];
+    double Bx = b[5], By = b[6], Bz = b[7];
+    double bm = D_1_8PI * (Bx * Bx + By * By + Bz * Bz);
+    double ke = density * (velx * velx + vely * vely + velz * velz);
+    double bu = Bx * velx + By * vely + Bz * velz;
+    double Pt = pressure + bm;
+    double e = pressure / c->hgamma + 0.5 * ke + bm;
+    g[0] = density * velx;
+    g[1] = density * velx * velx - D_1_4PI * Bx * Bx + Pt;
+    g[2] = density * velx * vely - D_1_4PI * Bx * By;
+    g[3] = density * velx * velz - D_1_4PI * Bx * Bz;
+    g[4] = velx * (e + Pt) - D_1_4PI * Bx * bu;
+    g[5] = 0.0;
+    g[6] = velx * By - vely * Bx;
+    g[7] = velx * Bz - velz * Bx;
+    *bn = Bx;
+  } else {
+    double L[8], Rt[8];
+    L[0] = Win[0];
+    Rt[0] = Wout[0];
+    L[4] = Win[4];
+    Rt[4] = Wout[4];
+    for (int a = 0; a < 3; ++a) {
+      L[1 + a] = sg * Win[iv[a]];
+      Rt[1 + a] = sg * Wout[iv[a]];
+      L[5 + a] = sg * Win[ib[a]];
+      Rt[5 + a] = sg * Wout[ib[a]];
+    }
+    Rt[0] = fmax(smallr, Rt[0]);
+    Rt[4] = fmax(smallp, Rt[4]);
+    L[0] = fmax(smallr, L[0]);
+    L[4] = fmax(smallp, L[4]);
+    bflux(c, d == 0, L, Rt, F, &Bv);
+    g[0] = sg * F[0];
+    g[iv[0]] = F[1];
+    g[iv[1]] = F[2];
+    g[iv[2]] = F[3];
+    g[4] = sg * F[4];
+    g[ib[0]] = F[5];
+    g[ib[1]] = F[6];
+    g[ib[2]] = F[7];
+    *bn = sg * Bv;
+  }
+  /* neutral populations */
+  for (int f = 1; f < c->nf; ++f) {
+    const int s0 = c->irhon + (f - 1) * 5;
+    const int nv[3] = {s0 + 1 + d, s0 + 1 + t1, s0 + 1 + t2};
+    double Fn[5];
+    if (f == 2 || f == 3) {
+      double fd = (f == 2) ? NETF2_DENS : NETF3_DENS, fp = (f == 2) ? NETF2_PRES : NETF3_PRES;
+      double st[5] = {fmax(fd, Win[s0]), Win[nv[0]], Win[nv[1]], Win[nv[2]], fmax(fp, Win[s0 + 4])};
+      double vn = side ? fmax(0.0, st[1]) : fmin(0.0, st[1]);
+      neutral_outflow(c, st, vn, Fn);
+      g[s0] = Fn[0];
+      g[nv[0]] = Fn[1];
+      g[nv[1]] = Fn[2];
+      g[nv[2]] = Fn[3];
+      g[s0 + 4] = Fn[4];
+      continue;
+    }
+    /* fluids 1 and 4 */
+    if (side == 0 && d == 0) {
+      double st[5] = {fmax(smallr, Win[s0]), Win[nv[0]], Win[nv[1]], Win[nv[2]],
+                      fmax(smallp, Win[s0 + 4])};
+      double vn = fmin(-1.0e-6, st[1]);
+      neutral_outflow(c, st, vn, Fn);
+      g[s0] = Fn[0];
+      g[nv[0]] = Fn[1];
+      g[nv[1]] = Fn[2];
+      g[nv[2]] = Fn[3];
+      g[s0 + 4] = Fn[4];
+      continue;
+    }
+    double Ln[5], Rn[5];
+    Ln[0] = fmax(smallr, Win[s0]);
+    Ln[4] = fmax(smallp, Win[s0 + 4]);
+    Rn[0] = fmax(smallr, Wout[s0]);
+    Rn[4] = fmax(smallp, Wout[s0 + 4]);
+    for (int a = 0; a < 3; ++a) {
+      Ln[1 + a] = sg * Win[nv[a]];
+      Rn[1 + a] = sg * Wout[nv[a]];
+    }
+    if (Ln[1] > 0.0) {
+      Rn[1] = Ln[1];
+      Rn[2] = Ln[2];
+      Rn[3] = Ln[3];
+      if (f == 1) Rn[0] = Ln[0];
+    }
+    /* VANLEERRS (src/VanLeerRSF.ChF:132-236) = VANLEERF without its floors,
+       which the floors above make no-ops */
+    double gl[5];
+    vanleer_face(c, 0, 0, Ln, Rn, gl);
+    g[s0] = sg * gl[0];
+    g[nv[0]] = gl[1];
+    g[nv[1]] = gl[2];
+    g[nv[2]] = gl[3];
+    g[s0 + 4] = sg * gl[4];
+  }
+}
+
 /* ------------------------------------------------------------------------ */
 /* sources                                                                   */
 /* ------------------------------------------------------------------------ */
@@ -2004,6 +2284,13 @@ static int euler_step(const Ctx* c, double time, Fab* U, Fab* F /* [sd] or NULL 
         }
       }
       if (p->divb_method == 0) bn = 0.0;
+      /* HeliosphericProblem::fluxBC (swlism/HeliosphericProblem.cpp:1994-2188)
+         after the Riemann fluxes and computeBn (src/PatchMHDAM.cpp:608-623) */
+      if (p->helio_bc && p->bc_kind == MF_BC_FARFIELD && !p->periodic[d] &&
+          (f == p->domain_lo[d] || f == p->domain_hi[d] + 1)) {
+        helio_bc_face(c, d, f == p->domain_lo[d] ? 0 : 1, wl, wr, g, &bn);
+        for (int q = 0; q < nc; ++q) AT(&Fl[d], i, j, k, q) = g[q];
+      }
       AT(&Bn[d], i, j, k, 0) = bn;
     }
   }
@@ -2336,6 +2623,15 @@ static int hancock_step(const Ctx* c, double time, Fab* U, Fab* F, Fab* divBout,
       }
       for (int q = 0; q < nc; ++q) g[q] = NAN;
       face_flux(c, d, wl, wr, g);
+      /* fluxBC of correctorHancock (src/PatchMHDAM.cpp:1105-1106): also
+         replaces the predictor's Bn of the boundary faces */
+      int f = (d == 0) ? i : (d == 1) ? j : k;
+      if (p->helio_bc && p->bc_kind == MF_BC_FARFIELD && !p->periodic[d] &&
+          (f == p->domain_lo[d] || f == p->domain_hi[d] + 1)) {
+        double bnv = AT(&Bn[d], i, j, k, 0);
+        helio_bc_face(c, d, f == p->domain_lo[d] ? 0 : 1, wl, wr, g, &bnv);
+        AT(&Bn[d], i, j, k, 0) = bnv;
+      }
       for (int q = 0; q < nc; ++q) AT(&Fl[d], i, j, k, q) = g[q];
     }
   }
@@ -2628,6 +2924,17 @@ int mf_oracle_face_flux(const mf_params* p, int dir, const double* wl, const dou
   int st = ctx_init(&c, p);
   if (st) return st;
   face_flux(&c, dir, wl, wr, f);
+  return MF_OK;
+}
+
+int mf_oracle_helio_bc_face(const mf_params* p, int dir, int side, const double* wl,
+                            const double* wr, double* f, double* bn) {
+  Ctx c;
+  int st = ctx_init(&c, p);
+  if (st) return st;
+  if (dir < 0 || dir >= c.sd || side < 0 || side > 1 || c.sd != 3) return MF_ERR_BAD_ARG;
+  face_flux(&c, dir, wl, wr, f);
+  helio_bc_face(&c, dir, side, wl, wr, f, bn);
   return MF_OK;
 }
 

@@ -74,6 +74,12 @@ int mf_oracle_average_down(const mf_params* pc, const mf_params* pf, int ratio, 
 int mf_oracle_face_flux(const mf_params* p, int dir, const double* wl, const double* wr,
                         double* f);
 int mf_oracle_cons_to_prim(const mf_params* p, const double* u, double* w);
+/* HELIOBC (swlism/HeliosphericF.ChF:221-910) on one face of the domain
+   boundary: the face fluxes of (wl, wr) by the configured solvers, then the
+   heliosphere's boundary fluxes over them (side 0: low face, wl is the ghost
+   side; 1: high face, wr is the ghost side); bn: the face-normal B. */
+int mf_oracle_helio_bc_face(const mf_params* p, int dir, int side, const double* wl,
+                            const double* wr, double* f, double* bn);
 int mf_oracle_charge_exchange(const mf_params* p, const double* w, int reg, double dt,
                               double* s);
 int mf_oracle_region(const mf_params* p, int i, int j, int k, const double* w);

@@ -59,6 +59,8 @@ def load():
                                                 ctypes.c_int * 3]),
         "mf_oracle_face_flux": (ctypes.c_int, [_P(MfParams), ctypes.c_int, _DP, _DP, _DP]),
         "mf_oracle_cons_to_prim": (ctypes.c_int, [_P(MfParams), _DP, _DP]),
+        "mf_oracle_helio_bc_face": (ctypes.c_int, [_P(MfParams), ctypes.c_int, ctypes.c_int, _DP,
+                                                   _DP, _DP, _DP]),
         "mf_oracle_charge_exchange": (ctypes.c_int, [_P(MfParams), _DP, ctypes.c_int,
                                                      ctypes.c_double, _DP]),
         "mf_oracle_region": (ctypes.c_int, [_P(MfParams), ctypes.c_int, ctypes.c_int,
@@ -258,3 +260,16 @@ def average_down(pc, pf, ratio, coarse, coarse_fboxes, coarse_valid, fine_arrays
     return lib.mf_oracle_average_down(ctypes.byref(pc), ctypes.byref(pf), ratio, len(coarse), fc,
                                       _boxes(coarse_valid), len(fine_arrays), ff,
                                       _boxes(fine_valid))
+
+
+def helio_bc_face(p: MfParams, direction: int, side: int, wl, wr):
+    """Fluxes and face-normal B of a face on the domain boundary with HELIOBC."""
+    lib = load()
+    wl = np.ascontiguousarray(wl, dtype=np.float64)
+    wr = np.ascontiguousarray(wr, dtype=np.float64)
+    f = np.full(mfgpu.num_cons(p), np.nan)
+    bn = ctypes.c_double()
+    st = lib.mf_oracle_helio_bc_face(ctypes.byref(p), direction, side, _dp(wl), _dp(wr), _dp(f),
+                                     ctypes.byref(bn))
+    assert st == 0, st
+    return f, bn.value
