@@ -156,6 +156,15 @@ typedef struct mf_params {
      (and 4), one-way outflow for fluids 2 and 3).  0 keeps the Riemann fluxes
      of the ghost-filled states. */
   int helio_bc;
+  /* neutral pass-through at the sun (HeliosphericProblem::postTimeStep ->
+     NEUTRALS_SUNBC, swlism/HeliosphericProblem.cpp:2472-2535,
+     swlism/SWLISMF.ChF:1555-1598; strips :489-527): after every level step,
+     the cells of the inner sphere (radius sun_r) downstream of the sun
+     (x >= sun) take neutral fluid 1 (and 4 with 5 fluids) from the cell
+     mirrored across the sun's x plane, y and z momenta reversed.  Level
+     steps only (it is a level post-processing in the reference); the sun
+     centre must lie on a grid node. */
+  int neutral_sun_bc;
 } mf_params;
 
 struct mf_ctx;

@@ -17,7 +17,10 @@ LIB = os.path.join(OUT_DIR, "libmfgpu.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", INCLUDE]
+# host code: no contraction either, so that host-side geometry (plans) rounds
+# as in the CPU restatement on every host architecture
+NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler",
+              "-ffp-contract=off", "-I", INCLUDE]
 
 
 def _nvcc() -> str:
@@ -48,7 +51,7 @@ def _compile(src: str, verbose: bool) -> str:
     if "_exact" in os.path.basename(src):
         # no fused multiply-add: every operation rounds as in
         # the CPU restatement of the reference
-        cmd += ["-fmad=false", "-Xcompiler", "-ffp-contract=off"]
+        cmd += ["-fmad=false"]
     if src.endswith(".cpp"):
         cmd += ["-x", "cu"]
     cmd += ["-c", src, "-o", obj]

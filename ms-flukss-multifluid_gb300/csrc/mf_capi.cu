@@ -148,6 +148,7 @@ mf_status validate_params(const mf_params& p) {
   if (p.divb_cleaning != 0 && p.divb_cleaning != 5) return MF_ERR_UNSUPPORTED;
   if (p.check_tvd < 0 || p.check_tvd > 2) return MF_ERR_BAD_ARG;
   if (p.helio_bc && (p.bc_kind != MF_BC_FARFIELD || p.space_dim != 3)) return MF_ERR_UNSUPPORTED;
+  if (p.neutral_sun_bc && (p.space_dim != 3 || p.n_fluids < 2)) return MF_ERR_UNSUPPORTED;
   if (p.divb_cleaning == 5) {
     // main/MHDAM.cpp:1042-1046
     if (p.use_8wave) return MF_ERR_UNSUPPORTED;
@@ -328,6 +329,8 @@ struct mf_level {
   int launches = 0, base_launches = 0;
   std::vector<StageDesc> hd1, hd2;         // host copies of the stage descs
   std::vector<mf::FaceGather> gathers;     // flux-register faces of a hierarchy
+  DevBuf sun;                              // NEUTRALS_SUNBC cell pairs
+  int nsun = 0;
 };
 
 extern "C" {
@@ -1022,6 +1025,50 @@ mf_status build_level_plan(const mf_params& p, int ng, int nc, int npatch, const
   L.fvsize = fvo;
   add_regions(L, p, ix, ng, L.full);
   if (rk2) add_regions(L, p, ix, 2, L.two);
+  if (p.neutral_sun_bc && p.n_fluids > 1 && sd == 3) {
+    // HeliosphericProblem::define (swlism/HeliosphericProblem.cpp:476-527):
+    // the sun on a grid node, strips of iR0 planes on either side of it
+    int sun[3];
+    for (int d = 0; d < 3; ++d) {
+      sun[d] = (int)std::floor(p.sun_center[d] / p.dx + 0.5);
+      if (std::fabs(sun[d] * p.dx - p.sun_center[d]) >= 1e-6) return MF_ERR_UNSUPPORTED;
+    }
+    const int iR0 = 1 + (int)std::floor(p.reinit_r0 / p.dx + 0.5);
+    const double sunR2 = p.sun_r * p.sun_r;
+    auto cell_of = [&](const int c[3], long long& off, int& cs) -> bool {
+      mf_box q;
+      for (int d = 0; d < 3; ++d) q.lo[d] = q.hi[d] = c[d];
+      int found = -1;
+      ix.query(q, [&](int b) {
+        const mf_box& v = L.valid[b];
+        if (c[0] >= v.lo[0] && c[0] <= v.hi[0] && c[1] >= v.lo[1] && c[1] <= v.hi[1] &&
+            c[2] >= v.lo[2] && c[2] <= v.hi[2])
+          found = b;
+      });
+      if (found < 0) return false;
+      const mf_box& f = L.fab[found];
+      const int n[3] = {f.hi[0] - f.lo[0] + 1, f.hi[1] - f.lo[1] + 1, f.hi[2] - f.lo[2] + 1};
+      off = L.off[found] + (c[0] - f.lo[0]) +
+            (long long)n[0] * ((c[1] - f.lo[1]) + (long long)n[1] * (c[2] - f.lo[2]));
+      cs = n[0] * n[1] * n[2];
+      return true;
+    };
+    for (int a = 0; a < iR0; ++a)
+      for (int k = sun[2] - iR0 - 1; k <= sun[2] + iR0; ++k)
+        for (int j = sun[1] - iR0 - 1; j <= sun[1] + iR0; ++j) {
+          const int i = sun[0] + a;
+          // NEUTRALS_SUNBC (swlism/SWLISMF.ChF:1555-1598)
+          const double x = (i + 0.5) * p.dx - p.sun_center[0];
+          const double y = (j + 0.5) * p.dx - p.sun_center[1];
+          const double z = (k + 0.5) * p.dx - p.sun_center[2];
+          const double r2 = x * x + y * y + z * z;
+          if (!(r2 <= sunR2)) continue;
+          const int to[3] = {i, j, k}, from[3] = {sun[0] - (i - sun[0] + 1), j, k};
+          SunPair sp;
+          if (cell_of(to, sp.to, sp.cs_to) && cell_of(from, sp.from, sp.cs_from))
+            L.sun.push_back(sp);
+        }
+  }
   return MF_OK;
 }
 
@@ -1119,6 +1166,13 @@ static mf_status enqueue_level_step(mf_level* L, int advance, cudaEvent_t* ev = 
   }
   MF_CHECK_CUDA(mf::launch_finalize(c->dp, parts, L->b2, L->b2.nt[2], ds, advance, s));
   mark(4);
+  // HeliosphericProblem::postTimeStep (swlism/HeliosphericProblem.cpp:2472-2535),
+  // after the step and its dt (AMRLevelIdealMHD::advance)
+  if (L->nsun) {
+    MF_CHECK_CUDA(mf::launch_sun_copy((double*)L->U.p, (const mf::SunPair*)L->sun.p, L->nsun,
+                                      c->dp.irhon, c->dp.nf, s));
+    mark(6);
+  }
   if (nev) *nev = ne;
   return MF_OK;
 }
@@ -1238,6 +1292,14 @@ mf_status mf_level_create(mf_ctx* c, int npatch, const mf_box* valid, mf_level**
     if (!two.empty() && (e = cudaMemcpy(L->extwo.p, two.data(), sizeof(CopyReg) * two.size(),
                                         cudaMemcpyHostToDevice)) != cudaSuccess)
       break;
+    L->nsun = (int)plan.sun.size();
+    if ((e = L->sun.ensure(sizeof(mf::SunPair) * std::max<size_t>(1, plan.sun.size()))) !=
+        cudaSuccess)
+      break;
+    if (!plan.sun.empty() &&
+        (e = cudaMemcpy(L->sun.p, plan.sun.data(), sizeof(mf::SunPair) * plan.sun.size(),
+                        cudaMemcpyHostToDevice)) != cudaSuccess)
+      break;
     if ((e = L->partials.ensure(sizeof(DtPartial) * (L->nparts + 1))) != cudaSuccess) break;
     if ((e = L->state.ensure(sizeof(StepState))) != cudaSuccess) break;
     if ((e = L->state2.ensure(sizeof(StepState))) != cudaSuccess) break;
@@ -1259,6 +1321,7 @@ mf_status mf_level_create(mf_ctx* c, int npatch, const mf_box* valid, mf_level**
                                                           : (per_stage + 1 + 1);
   if (L->nfull == 0) L->launches -= 1;
   if (p.time_approximation == MF_TA_RK2 && L->ntwo == 0) L->launches -= 1;
+  if (L->nsun) L->launches += 1;
   L->base_launches = L->launches;
   *out = L;
   return MF_OK;
@@ -1283,6 +1346,7 @@ void mf_level_destroy(mf_level* L) {
   L->partials.release();
   L->state.release();
   L->state2.release();
+  L->sun.release();
   L->hstate.release();
   delete L;
 }

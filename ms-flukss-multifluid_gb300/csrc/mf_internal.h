@@ -28,6 +28,15 @@ mf_status status_of_flags(unsigned flags);
 // (run 0; face offsets in elements from the face arrays' bases), the face
 // array sizes, and the ghost-exchange regions (LevelData::exchange: all ng
 // layers before a step, 2 layers of the predictor between the RK2 stages).
+// A cell that takes neutral fluid 1 (and 4) from its mirror across the
+// sun's x plane (NEUTRALS_SUNBC): offsets of component 0 and component strides.
+struct SunPair {
+  long long to, from;
+  int cs_to, cs_from;
+};
+cudaError_t launch_sun_copy(double* U, const SunPair* pairs, int n, int irhon, int nf,
+                            cudaStream_t s);
+
 struct LevelPlan {
   int np = 0;
   std::vector<mf_box> valid, fab;
@@ -37,6 +46,7 @@ struct LevelPlan {
   long long fsize[3] = {0, 0, 0}, bsize[3] = {0, 0, 0};
   long long fvsize = 0;  // Hancock face values per direction (doubles)
   std::vector<CopyReg> full, two;
+  std::vector<SunPair> sun;  // neutral pass-through at the sun (level steps)
 };
 
 // MF_ERR_BAD_ARG for empty, overlapping or out-of-domain boxes, boxes with

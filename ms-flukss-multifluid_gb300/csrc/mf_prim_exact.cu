@@ -1,8 +1,10 @@
-// mf_prim_exact.cu - conserved -> primitive variables on valueBox.grow(2).
+// mf_prim_exact.cu - conserved -> primitive variables on valueBox.grow(2), and
+// the neutral pass-through at the sun after a level step.
 //
 // Built with -fmad=false: the primitive state feeds the limiter sign tests
 // and the region thresholds, so it is rounded exactly as in the CPU
 // restatement of the reference (EqSysMHDMF::stateToPrim).
+#include "mf_internal.h"
 #include "mf_kernels.cuh"
 
 namespace mf {
@@ -84,4 +86,32 @@ cudaError_t launch_prim(const DevParams& P, const double* uin, double* w, const 
   return cudaGetLastError();
 }
 
+}  // namespace mf
+
+namespace mf {
+namespace {
+// NEUTRALS_SUNBC (swlism/SWLISMF.ChF:1555-1598): neutral fluid 1 (and 4)
+// from the mirror cell, y and z momenta reversed.
+__global__ void k_sun_copy(double* __restrict__ U, const SunPair* __restrict__ pairs, int n,
+                           int irhon, int nf) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const SunPair sp = pairs[t];
+  const double sg[5] = {1.0, 1.0, -1.0, -1.0, 1.0};
+  for (int f = 1; f < nf; f += 3) {  // fluids 1 and 4
+    const int s0 = irhon + (f - 1) * 5;
+#pragma unroll
+    for (int m = 0; m < 5; ++m)
+      U[sp.to + (long long)(s0 + m) * sp.cs_to] =
+          sg[m] * U[sp.from + (long long)(s0 + m) * sp.cs_from];
+  }
+}
+}  // namespace
+
+cudaError_t launch_sun_copy(double* U, const SunPair* pairs, int n, int irhon, int nf,
+                            cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  k_sun_copy<<<(n + 127) / 128, 128, 0, s>>>(U, pairs, n, irhon, nf);
+  return cudaGetLastError();
+}
 }  // namespace mf

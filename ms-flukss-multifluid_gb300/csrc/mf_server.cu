@@ -155,8 +155,8 @@ struct mf_server {
   bool dirty = true;
   int nslots = 0;  // runs in the launch: highest admitted slot + 1
   mf::Batch b1, b2;
-  DevMem desc, runtab, exfull, extwo, partials, states, tstates;
-  int nfull = 0, ntwo = 0;
+  DevMem desc, runtab, exfull, extwo, partials, states, tstates, sun;
+  int nfull = 0, ntwo = 0, nsun = 0;
   HostMem hstates, staging;
   cudaStream_t s = nullptr;
   cudaGraphExec_t graph = nullptr;
@@ -220,6 +220,7 @@ mf_status rebuild(mf_server* S) {
   S->nslots = hi + 1;
   std::vector<StageDesc> d1, d2;
   std::vector<CopyReg> full, two;
+  std::vector<mf::SunPair> sun;
   for (int r = 0; r <= hi; ++r) {
     const Run& R = S->runs[r];
     if (!R.used) continue;
@@ -244,6 +245,11 @@ mf_status rebuild(mf_server* S) {
         C.dst_off += R.coff;
         dst.push_back(C);
       }
+    }
+    for (mf::SunPair sp : R.plan.sun) {
+      sp.to += R.coff;
+      sp.from += R.coff;
+      sun.push_back(sp);
     }
   }
   std::memset(&S->b1, 0, sizeof(S->b1));
@@ -287,6 +293,11 @@ mf_status rebuild(mf_server* S) {
   if (!two.empty())
     SV_CUDA(cudaMemcpy(S->extwo.p, two.data(), sizeof(CopyReg) * two.size(),
                        cudaMemcpyHostToDevice));
+  S->nsun = (int)sun.size();
+  SV_CUDA(S->sun.ensure(sizeof(mf::SunPair) * std::max<size_t>(1, sun.size())));
+  if (!sun.empty())
+    SV_CUDA(cudaMemcpy(S->sun.p, sun.data(), sizeof(mf::SunPair) * sun.size(),
+                       cudaMemcpyHostToDevice));
   SV_CUDA(S->partials.ensure(sizeof(DtPartial) * (mf::dt_partials(S->b2) + 1)));
   return MF_OK;
 }
@@ -326,6 +337,9 @@ mf_status enqueue_step(mf_server* S) {
     SV_CUDA(mf::launch_stage(P, p.precision, B, S->b2, mf::kStageDt, 1.0, ds, parts, &nb, S->s));
   }
   SV_CUDA(mf::launch_finalize(P, parts, S->b2, S->b2.nt[2], ds, 1, S->s));
+  // neutral pass-through at the sun of every run (NEUTRALS_SUNBC)
+  SV_CUDA(mf::launch_sun_copy((double*)S->U.p, (const mf::SunPair*)S->sun.p, S->nsun, P.irhon,
+                              P.nf, S->s));
   return MF_OK;
 }
 
@@ -477,6 +491,7 @@ void mf_server_destroy(mf_server* S) {
   }
   S->desc.release();
   S->runtab.release();
+  S->sun.release();
   S->exfull.release();
   S->extwo.release();
   S->partials.release();

@@ -109,6 +109,7 @@ class MfParams(ctypes.Structure):
         ("char_reconstruction", ctypes.c_int),
         ("check_tvd", ctypes.c_int),
         ("helio_bc", ctypes.c_int),
+        ("neutral_sun_bc", ctypes.c_int),
     ]
 
 
@@ -408,9 +409,16 @@ def helio_params(n: int = 128, seed: int = 20240601, time_approximation: int = T
     p.sun_beta = 2.0
     p.dir_br = 1.0
     p.bc_kind = BC_FARFIELD
-    # the heliosphere's boundary fluxes on the faces of the domain boundary
-    # (HeliosphericProblem::fluxBC -> HELIOBC)
-    p.helio_bc = 1
+    # The heliosphere's boundary fluxes (HELIOBC) treat the high-x face as the
+    # interstellar inflow at all times, as in the reference's decks, whose
+    # domains reach far beyond the heliopause.  In this [-1,1]^3 box the solar
+    # wind reaches that face at t ~ 0.24 and the imposed inflow flux against
+    # the outflowing wind drives the face cells to extreme states; the preset
+    # keeps the Riemann fluxes of the far-field ghost states (helio_bc = 0),
+    # which let the wind leave.  helio_bc = 1 selects HELIOBC.
+    p.helio_bc = 0
+    # neutral pass-through at the sun after every level step (NEUTRALS_SUNBC)
+    p.neutral_sun_bc = 1
     wp, wn = helio_inflow()
     for q in range(8):
         p.bc_plasma[q] = wp[q]
@@ -625,7 +633,8 @@ class Level:
     def launches_per_step(self):
         return self.lib.mf_level_launches_per_step(self.h)
 
-    KIND_NAMES = {0: "exchange", 1: "prim", 2: "flux", 3: "update", 4: "finalize", 5: "coupling"}
+    KIND_NAMES = {0: "exchange", 1: "prim", 2: "flux", 3: "update", 4: "finalize", 5: "coupling",
+                  6: "postprocess"}
 
     def profile_step(self, dt):
         """One step launch by launch with CUDA events between the launches;

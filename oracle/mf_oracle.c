@@ -2881,6 +2881,49 @@ int mf_oracle_level_exchange(const mf_params* p, int npatch, mf_fab* Uf, const m
   return MF_OK;
 }
 
+/* HeliosphericProblem::postTimeStep -> NEUTRALS_SUNBC (swlism/SWLISMF.ChF:
+   1555-1598) on the strips of HeliosphericProblem::define
+   (swlism/HeliosphericProblem.cpp:476-527): the cells of the sphere of radius
+   sunR downstream of the sun take neutral fluid 1 (and 4) from the cell
+   mirrored across the sun's x plane, y and z momenta reversed. */
+static int neutral_sun_bc(const mf_params* p, int npatch, mf_fab* Uf, const mf_box* valid) {
+  if (!p->neutral_sun_bc || p->n_fluids < 2 || p->space_dim != 3) return MF_OK;
+  int sun[3];
+  for (int d = 0; d < 3; ++d) {
+    sun[d] = (int)floor(p->sun_center[d] / p->dx + 0.5);
+    if (fabs(sun[d] * p->dx - p->sun_center[d]) >= 1e-6) return MF_ERR_UNSUPPORTED;
+  }
+  const int iR0 = 1 + (int)floor(p->reinit_r0 / p->dx + 0.5);
+  const double sunR2 = p->sun_r * p->sun_r;
+  const int irhon = 8 + (p->divb_cleaning == 5 ? 1 : 0);
+  const double sg[5] = {1.0, 1.0, -1.0, -1.0, 1.0};
+  for (int a = 0; a < iR0; ++a)
+    for (int k = sun[2] - iR0 - 1; k <= sun[2] + iR0; ++k)
+      for (int j = sun[1] - iR0 - 1; j <= sun[1] + iR0; ++j) {
+        const int i = sun[0] + a;
+        double x = (i + 0.5) * p->dx - p->sun_center[0];
+        double y = (j + 0.5) * p->dx - p->sun_center[1];
+        double z = (k + 0.5) * p->dx - p->sun_center[2];
+        double r2 = x * x + y * y + z * z;
+        if (!(r2 <= sunR2)) continue;
+        const int iRefl = sun[0] - (i - sun[0] + 1);
+        int bt = -1, bf = -1;
+        for (int b = 0; b < npatch; ++b) {
+          if (box_in(&valid[b], i, j, k)) bt = b;
+          if (box_in(&valid[b], iRefl, j, k)) bf = b;
+        }
+        if (bt < 0 || bf < 0) continue;
+        Fab T = fab_wrap(Uf[bt].data, Uf[bt].box, Uf[bt].ncomp);
+        Fab S = fab_wrap(Uf[bf].data, Uf[bf].box, Uf[bf].ncomp);
+        for (int f = 1; f < p->n_fluids; f += 3)
+          for (int m = 0; m < 5; ++m) {
+            const int q = irhon + (f - 1) * 5 + m;
+            AT(&T, i, j, k, q) = sg[m] * AT(&S, iRefl, j, k, q);
+          }
+      }
+  return MF_OK;
+}
+
 int mf_oracle_level_step(const mf_params* p, double time, int npatch, mf_fab* Uf,
                          const mf_box* valid, double dt, int nthreads, double* new_dt,
                          int* min_patch, int min_cell[3]) {
@@ -2899,6 +2942,7 @@ int mf_oracle_level_step(const mf_params* p, double time, int npatch, mf_fab* Uf
     sts[ip] = mf_oracle_patch_update(p, time, &Uf[ip], &valid[ip], dt, NULL, NULL, &dts[ip],
                                      &cells[3 * ip]);
   int best = -1;
+  if (st == MF_OK) st = neutral_sun_bc(p, npatch, Uf, valid);
   for (int ip = 0; ip < npatch; ++ip) {
     if (sts[ip]) st = sts[ip];
     if (best < 0 || dts[ip] < dts[best]) best = ip;
@@ -3473,6 +3517,8 @@ static int hier_advance(Hier* H, int l) {
   }
   free(dts);
   free(sts);
+  if (st) return st;
+  st = neutral_sun_bc(&H->p[l], L->npatch, L->U, L->valid);
   if (st) return st;
   H->ndt[l] = nd;
   Fab** Fl = (Fab**)malloc(sizeof(Fab*) * (size_t)L->npatch);
