@@ -165,6 +165,31 @@ typedef struct mf_params {
      steps only (it is a level post-processing in the reference); the sun
      centre must lie on a grid node. */
   int neutral_sun_bc;
+  /* tracking surfaces (level sets; mhdam.num_tracking_surfaces and
+     mhdam.region_tracer, main/MHDAM.cpp:709-718): components after the last
+     fluid, carried by the plasma velocity (PhysProblem::lsIndexField,
+     src/PhysProblem.cpp:327-330).  Face values with limiter_ls, upwind face
+     value by the sign of sqrt(rho_L) u_L + sqrt(rho_R) u_R (LEVELSETFLUX,
+     src/LevelSetF.ChF:37-105), non-conservative update
+     phi -= dt/dx u (F(i+1) - F(i)) with the stage-start cell velocity
+     (UPDATELEVELSET :200-234; Hancock: FLUXESHANCOCK_LS :9-35 and
+     UPDATELEVELSETHANCOCK :354-388), then the floor of POSTPROCESSING_LS
+     (:426-465).  Not refluxed at coarse-fine faces (the flux registers cover
+     the fluid components only).  At most 2; plasma, psi, neutrals and
+     surfaces together at most MF_MAX_COMP. */
+  int num_tracking_surfaces;
+  int limiter_ls;          /* mhdam.limiter_LS (the reference reads it into the variable of
+                              the other limiter keys, so a deck without it takes the last
+                              limiter key read) */
+  /* 1: the last tracking surface is the heliosphere's region tracer
+     (HeliosphericProblem::defineRegions with m_region_tracer,
+     swlism/HeliosphericProblem.cpp:2538-2575 -> DEFINE_REGIONS_TRACER_4F,
+     swlism/SWLISMF.ChF:839-1016): negative = solar wind (regions 2/3 by the
+     radial speed and temperature, 4 outside the z band), positive =
+     interstellar (1, or 4 where the flow is dense, slow, deflected from
+     lism_u or hot); far-field ghosts hold +1 (HELIOGS). */
+  int region_tracer;
+  double lism_u[3];        /* lismUX, lismUY, lismUZ: interstellar flow direction */
 } mf_params;
 
 struct mf_ctx;

@@ -446,6 +446,7 @@ struct mf_cf {
   mf_level *lc = nullptr, *lf = nullptr;
   LevelView vc, vf;
   int r = 2, nc = 0, sd = 3, divb = 0;
+  int ncons = 0;  // fluid components: the flux registers skip the tracking surfaces
   int nnb = 0, nsites = 0, ntg = 0, nreg = 0, nsub = 1, nrc = 0, navg = 0;
   double c1c = 0, c1s = 0, dxc = 0, dxf = 0, coeff = 0, invdx = 0, vol = 0;
   DBuf nb, sites, tg, old, sv;     // interpolation
@@ -718,6 +719,9 @@ static mf_status build_cf(mf_cf* C) {
       fref.size() > (size_t)INT32_MAX / 32 || avgs.size() > (size_t)INT32_MAX / 32)
     return MF_ERR_UNSUPPORTED;
   C->nc = nc;
+  // incrementCoarse / incrementFine over consInterval only
+  // (srcIdeal/AMRLevelIdealMHD.cpp:1282-1305)
+  C->ncons = nc - pc.num_tracking_surfaces;
   C->sd = sd;
   C->divb = (pc.divb_cleaning != 0);
   C->nnb = (int)nbs.size();
@@ -802,7 +806,7 @@ static mf_status cf_interp(mf_cf* C, double alpha, cudaStream_t s) {
 }
 
 static mf_status cf_reg_coarse(mf_cf* C, double dt, cudaStream_t s) {
-  const long long n = (long long)C->nreg * C->nc;
+  const long long n = (long long)C->nreg * C->ncons;
   if (n > 0)
     k_reg_coarse<<<blocks(n), kThreads, 0, s>>>((double*)C->reg.p, (const double*)C->rfc.p, n,
                                                  -dt);
@@ -813,10 +817,10 @@ static mf_status cf_reg_coarse(mf_cf* C, double dt, cudaStream_t s) {
 static mf_status cf_reg_fine(mf_cf* C, double dt, cudaStream_t s) {
   double denom = 1.0;
   for (int e = 0; e < C->sd - 1; ++e) denom *= C->r;
-  const long long n = (long long)C->nreg * C->nc;
+  const long long n = (long long)C->nreg * C->ncons;
   if (n > 0)
     k_reg_fine<<<blocks(n), kThreads, 0, s>>>((double*)C->reg.p, (const double*)C->rff.p,
-                                               C->nreg, C->nsub, C->nc, dt / denom);
+                                               C->nreg, C->nsub, C->ncons, dt / denom);
   MF_CUDA(cudaGetLastError());
   return MF_OK;
 }
@@ -831,11 +835,12 @@ static mf_status cf_average(mf_cf* C, cudaStream_t s) {
 }
 
 static mf_status cf_reflux_average(mf_cf* C, cudaStream_t s) {
-  const long long n = (long long)C->nrc * C->nc;
+  const long long n = (long long)C->nrc * C->ncons;
   if (n > 0)
     k_reflux<<<blocks(n), kThreads, 0, s>>>(C->vc.U, (const RefluxCell*)C->rcell.p, C->nrc,
                                              (const RefluxTerm*)C->rterm.p,
-                                             (const double*)C->reg.p, C->nreg, C->nc, C->invdx);
+                                             (const double*)C->reg.p, C->nreg, C->ncons,
+                                             C->invdx);
   MF_CUDA(cudaGetLastError());
   return cf_average(C, s);
 }

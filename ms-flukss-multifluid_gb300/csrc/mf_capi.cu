@@ -125,9 +125,13 @@ void ext3(const mf_box& b, int n[3]) {
   for (int d = 0; d < 3; ++d) n[d] = b.hi[d] - b.lo[d] + 1;
 }
 
-int num_cons(const mf_params& p) {
+// fluid components (EqSysMHDMF::consInterval) and the tracking surfaces after
+// them (lvlsStateInterval, srcIdeal/EqSysMHDMF.cpp:11-48)
+int num_fluid_cons(const mf_params& p) {
   return 8 + (p.divb_cleaning == 5 ? 1 : 0) + (p.n_fluids - 1) * 5;
 }
+
+int num_cons(const mf_params& p) { return num_fluid_cons(p) + p.num_tracking_surfaces; }
 
 int num_ghost_of(const mf_params& p) {
   if (p.time_approximation == MF_TA_RK2) return 4;
@@ -149,6 +153,15 @@ mf_status validate_params(const mf_params& p) {
   if (p.check_tvd < 0 || p.check_tvd > 2) return MF_ERR_BAD_ARG;
   if (p.helio_bc && (p.bc_kind != MF_BC_FARFIELD || p.space_dim != 3)) return MF_ERR_UNSUPPORTED;
   if (p.neutral_sun_bc && (p.space_dim != 3 || p.n_fluids < 2)) return MF_ERR_UNSUPPORTED;
+  if (p.num_tracking_surfaces < 0) return MF_ERR_BAD_ARG;
+  if (p.num_tracking_surfaces > 2 || num_cons(p) > MF_MAX_COMP) return MF_ERR_UNSUPPORTED;
+  if (p.region_tracer && p.num_tracking_surfaces < 1) return MF_ERR_BAD_ARG;
+  if (p.num_tracking_surfaces > 0) {
+    const int l = p.limiter_ls;
+    if (!(l == MF_LIM_CD || l == MF_LIM_MINMOD || l == MF_LIM_SUPERBEE || l == MF_LIM_VANALBADA ||
+          l == MF_LIM_MC || l == MF_LIM_HARMONIC || l == MF_LIM_VANLEER))
+      return MF_ERR_UNSUPPORTED;
+  }
   if (p.divb_cleaning == 5) {
     // main/MHDAM.cpp:1042-1046
     if (p.use_8wave) return MF_ERR_UNSUPPORTED;
@@ -175,6 +188,11 @@ DevParams make_dev(const mf_params& p) {
   P.nf = p.n_fluids;
   P.glm = (p.divb_cleaning == 5) ? 1 : 0;
   P.nc = num_cons(p);
+  P.ils = num_fluid_cons(p);
+  P.nls = p.num_tracking_surfaces;
+  P.lim_ls = p.limiter_ls;
+  P.reg_tracer = (p.region_tracer && P.nls > 0) ? 1 : 0;
+  for (int d = 0; d < 3; ++d) P.lism_u[d] = p.lism_u[d];
   P.irhon = 8 + P.glm;
   // RiemannSolver::make (src/RiemannSolver.cpp:13-112)
   if (P.glm) {
@@ -375,6 +393,10 @@ void mf_params_default(mf_params* p, int space_dim, int n_fluids) {
     p->periodic[d] = 1;
   }
   p->bc_kind = MF_BC_NONE;
+  p->num_tracking_surfaces = 0;
+  p->limiter_ls = MF_LIM_MINMOD;
+  p->region_tracer = 0;
+  p->lism_u[0] = -1.0;
 }
 
 int mf_params_num_cons(const mf_params* p) { return p ? num_cons(*p) : 0; }
@@ -1115,7 +1137,8 @@ static mf_status enqueue_level_step(mf_level* L, int advance, cudaEvent_t* ev = 
   const void* fl[3] = {L->F[0].p, L->F[1].p, L->F[2].p};
   auto gather = [&](int mode) -> mf_status {
     for (const mf::FaceGather& g : L->gathers) {
-      MF_CHECK_CUDA(mf::launch_face_gather(mixed, fl, g, mode, nc, s));
+      // fluid components only: the registers skip the tracking surfaces
+      MF_CHECK_CUDA(mf::launch_face_gather(mixed, fl, g, mode, L->ctx->dp.ils, s));
       mark(5);
     }
     return MF_OK;
@@ -1735,6 +1758,16 @@ mf_status mf_init_helio_host(const mf_params* p, const double* wp, const double*
           u[s + 4] = w[4] * invhg + 0.5 * r * ke2;
         }
         if (p->reinit_sphere) mf::exact::reinit_cell(P, P.dx, i, j, k, u);
+        // tracking surfaces: the region tracer -1 in the wind sphere, +1
+        // outside (HELIOINIT, swlism/HeliosphericF.ChF:1228-1231,1302-1304);
+        // any other surface r - R0, a level set of the sphere
+        if (P.nls) {
+          const double x = (i + 0.5) * P.dx - P.sun_c[0], y = (j + 0.5) * P.dx - P.sun_c[1];
+          const double z = (P.sd == 3) ? (k + 0.5) * P.dx - P.sun_c[2] : 0.0;
+          const double r2 = x * x + y * y + z * z;
+          for (int q = P.ils; q < P.nc; ++q) u[q] = std::sqrt(r2) - P.r0;
+          if (P.reg_tracer) u[P.nc - 1] = (r2 <= P.r0 * P.r0) ? -1.0 : 1.0;
+        }
         for (int q = 0; q < U->ncomp; ++q) U->data[hidx(U, i, j, k, q)] = u[q];
       }
   return MF_OK;

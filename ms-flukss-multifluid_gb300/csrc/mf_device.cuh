@@ -31,6 +31,10 @@ struct DevParams {
   int use8, divb_method, check_pos, ce, reinit, bc_kind;
   int char_rec, check_tvd;
   int helio_bc;  // HELIOBC fluxes on the faces of the domain boundary
+  // tracking surfaces: components [ils, nc) after the fluids (ils = number of
+  // fluid components), limiter lim_ls; reg_tracer: the last one is the
+  // region tracer, lism_u the interstellar flow direction
+  int ils, nls, lim_ls, reg_tracer;
   int lim[8];
   int periodic[3], dlo[3], dhi[3];
   double gamma, hgamma, invhgamma, invgamma, smallr, smallp, del2, smallB, dx, invdx;
@@ -39,6 +43,7 @@ struct DevParams {
   double sun_c[3], sun_r, sun_v, t_coeff, tmlim, zbot, ztop;
   double r0, rint, sun_rho, sun_p, sun_b, sun_beta, dir_br;
   double bc_plasma[8], bc_n1[5];
+  double lism_u[3];
 };
 
 // Values that change from step to step; kept in device memory so that a
@@ -412,6 +417,22 @@ __device__ __forceinline__ void face_slopes(int lim, R& Sleft, R& Sright) {
   }
   Sleft = SLOPE;
   Sright = SLOPE;
+}
+
+// Face values of a tracking surface from the cell values a, b, c (b the
+// cell): the *FACEVALUES form with limiter_LS, or with characteristic
+// reconstruction INITIALSLOPES + *FACESLOPES (the surfaces are not projected;
+// src/Reconstruction.cpp:178-203).
+template <typename R>
+__device__ __forceinline__ void ls_face_values(const DevParams& P, R a, R b, R c, R& lo, R& hi) {
+  if (P.char_rec) {
+    R SL = b - a, SR = c - b;
+    face_slopes<R>(P.lim_ls, SL, SR);
+    lo = b - SL;
+    hi = b + SR;
+  } else {
+    face_values<R>(P.lim_ls, a, b, c, lo, hi);
+  }
 }
 
 // Wave speeds and mixing coefficients at a cell state, as CHARANALYSISF

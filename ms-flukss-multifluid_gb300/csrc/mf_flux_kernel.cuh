@@ -457,6 +457,23 @@ __global__ void __launch_bounds__(kMaxBlock)
 #pragma unroll
     for (int m = 0; m < 5; ++m) Fo[(s + m) * fcs] = gn[m];
   }
+
+  // tracking surfaces: LEVELSETFLUX (src/LevelSetF.ChF:37-105) after the
+  // boundary fluxes (src/PatchMHDAM.cpp:644-648): the upwind face value by the
+  // sign of sqrt(rho_L) u_L + sqrt(rho_R) u_R of the plasma face states
+  if (P.nls) {
+    const R uavg = sqrt(wl[0]) * wl[1 + DIR] + sqrt(wr[0]) * wr[1 + DIR];
+    for (int q = P.ils; q < P.nc; ++q) {
+      const double* wv = w0 + q * cs;
+      const R a = R(wv[-2 * st]), b = R(wv[-st]), c = R(wv[0]), d = R(wv[st]);
+      R lo, hi;
+      ls_face_values<R>(P, a, b, c, lo, hi);
+      const R l = negL ? b : hi;
+      ls_face_values<R>(P, b, c, d, lo, hi);
+      const R r = negR ? c : lo;
+      Fo[q * fcs] = (uavg > R(0)) ? l : r;
+    }
+  }
 }
 
 // Corrector fluxes of the Hancock step (correctorHancock, src/PatchMHDAM.cpp:
@@ -558,6 +575,15 @@ __global__ void __launch_bounds__(kMaxBlock)
     }
 #pragma unroll
     for (int m = 0; m < 5; ++m) Fo[(s0 + m) * fcs] = gn[m];
+  }
+  // tracking surfaces (LEVELSETFLUX of the shifted face values,
+  // src/PatchMHDAM.cpp:1111-1115)
+  if (P.nls) {
+    const R uavg = sqrt(wl[0]) * wl[1 + DIR] + sqrt(wr[0]) * wr[1 + DIR];
+    for (int q = P.ils; q < P.nc; ++q) {
+      const R l = R(fv[(nc + q) * scs + cl]), r = R(fv[q * scs + cr]);
+      Fo[q * fcs] = (uavg > R(0)) ? l : r;
+    }
   }
 }
 

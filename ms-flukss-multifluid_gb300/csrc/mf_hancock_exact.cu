@@ -78,6 +78,8 @@ __global__ void __launch_bounds__(kMaxBlock)
       } else if (P.char_rec && v < 8) {
         lo = clo[v];
         hi = chi[v];
+      } else if (v >= P.ils) {
+        ls_face_values<double>(P, wv[-st], wv[0], wv[st], lo, hi);
       } else {
         const int lim = (v < 8) ? P.lim[v] : (int)MF_LIM_MINMOD;
         face_values<double>(lim, wv[-st], wv[0], wv[st], lo, hi);
@@ -130,6 +132,11 @@ __device__ __forceinline__ void point_flux(const DevParams& P, const double* w, 
       F[s + 4] = un * (en + pn);
     }
   }
+  // FLUXESHANCOCK_LS (src/LevelSetF.ChF:9-35): surface times the plasma
+  // normal velocity
+#pragma unroll
+  for (int q = 0; q < MF_MAX_COMP; ++q)
+    if (q >= P.ils && q < P.nc) F[q] = w[q] * w[in];
 }
 
 // Bn of one face (PatchMHDMF::computeBn, srcIdeal/PatchMHDMF.cpp:509-620)
@@ -154,8 +161,8 @@ __device__ __forceinline__ void hpredict_dir(const DevParams& P, const RunParams
                                              const StageDesc& Dc, const HancockBuffers& H,
                                              const double* __restrict__ W, long long base,
                                              long long cs, long long scs, long long c,
-                                             const int* x, int nc, double dtinv, double* u,
-                                             double& divB) {
+                                             const int* x, int nc, double dtinv, double dtp,
+                                             double* u, double& divB) {
   const double* __restrict__ fv = H.fv[D] + Dc.fv_off[D];
   double wm[MF_MAX_COMP], wp[MF_MAX_COMP], fm[MF_MAX_COMP], fp[MF_MAX_COMP];
 #pragma unroll
@@ -168,7 +175,13 @@ __device__ __forceinline__ void hpredict_dir(const DevParams& P, const RunParams
   point_flux<D, IRHON>(P, wp, fp);
 #pragma unroll
   for (int q = 0; q < MF_MAX_COMP; ++q)
-    if (q < nc) u[q] = u[q] - dtinv * (fp[q] - fm[q]);
+    if (q < P.ils) u[q] = u[q] - dtinv * (fp[q] - fm[q]);
+  if (P.nls) {  // UPDATELEVELSETHANCOCK (src/LevelSetF.ChF:354-388), W(t) velocity
+    const double cf = dtp / RP.dx * W[base + (1 + D) * cs];
+#pragma unroll
+    for (int q = 0; q < MF_MAX_COMP; ++q)
+      if (q >= P.ils && q < nc) u[q] = u[q] - cf * (fp[q] - fm[q]);
+  }
   const long long ss = dstride(Dc.sn, D);
   const long long fs = dstride(Dc.fn, D);
   const double* wbn = W + base + (5 + D) * cs;
@@ -208,9 +221,11 @@ __global__ void __launch_bounds__(kMaxBlock)
   // direction after another; divB from Bn of the face values (COMPUTEDIVB)
   const double dtinv = dtp * RP.invdx;
   double divB = 0.0;
-  hpredict_dir<0, IRHON>(P, RP, D, H, W, base, cs, scs, c, x, nc, dtinv, u, divB);
-  if (P.sd > 1) hpredict_dir<1, IRHON>(P, RP, D, H, W, base, cs, scs, c, x, nc, dtinv, u, divB);
-  if (P.sd > 2) hpredict_dir<2, IRHON>(P, RP, D, H, W, base, cs, scs, c, x, nc, dtinv, u, divB);
+  hpredict_dir<0, IRHON>(P, RP, D, H, W, base, cs, scs, c, x, nc, dtinv, dtp, u, divB);
+  if (P.sd > 1)
+    hpredict_dir<1, IRHON>(P, RP, D, H, W, base, cs, scs, c, x, nc, dtinv, dtp, u, divB);
+  if (P.sd > 2)
+    hpredict_dir<2, IRHON>(P, RP, D, H, W, base, cs, scs, c, x, nc, dtinv, dtp, u, divB);
   // addExplicitSources with W(t) and dt/2 (srcIdeal/PatchMHDMF.cpp:1149-1389)
   double w[MF_MAX_COMP];
 #pragma unroll
@@ -230,7 +245,8 @@ __global__ void __launch_bounds__(kMaxBlock)
   }
   if (GLM) u[8] = exp(-dtp * SS.ch * SS.ch / (SS.cp * SS.cp)) * u[8];
   if (P.ce && P.nf >= 2) {
-    const int reg = region_cell(P, RP.dx, i, j, k, w);
+    const double regtr = P.reg_tracer ? W[base + (nc - 1) * cs] : 0.0;
+    const int reg = region_cell(P, RP.dx, i, j, k, w, regtr);
     charge_exchange_add<IRHON>(P, w, reg, dtp, u);
   }
   // W(t + dt/2) (stateToPrim of the predicted state)
@@ -240,6 +256,9 @@ __global__ void __launch_bounds__(kMaxBlock)
 #pragma unroll
   for (int f = 1; f < MF_MAX_FLUIDS; ++f)
     if (f < P.nf) cons_to_prim_euler(P, u + IRHON + (f - 1) * 5, wo + IRHON + (f - 1) * 5);
+#pragma unroll
+  for (int q = 0; q < MF_MAX_COMP; ++q)
+    if (q >= P.ils && q < nc) wo[q] = u[q];
 #pragma unroll
   for (int q = 0; q < MF_MAX_COMP; ++q)
     if (q < nc) H.w2[base + q * cs] = wo[q];
@@ -345,6 +364,7 @@ cudaError_t launch_hancock(const DevParams& P, int precision, const StageBuffers
   }
   StageBuffers B2 = B;
   B2.w = H.w2;
+  B2.wls = B.w;
   if (precision == MF_PREC_MIXED)
     e = launch_update_fast<float>(P, B2, c, kStageDt, 1.0, state, partials, nblocks_v, s);
   else if (precision == MF_PREC_FP64_FAST)

@@ -157,6 +157,10 @@ struct StageBuffers {
   double* uout;        // state the stage writes (valueBox cells only)
   const double* uold;  // state before the time step (RK2 averaging)
   double* w;           // primitive scratch, same layout as uin
+  // primitive state at the stage start when it is not w (the Hancock
+  // corrector: w holds W(t+dt/2), wls W(t)): the velocity of the tracking
+  // surfaces' update and their stage-start values (Uold); null = w
+  const double* wls;
   void* f[3];          // face fluxes (double or float), per direction
   void* bn[3];         // face-normal B (double or float), per direction
   double* divb;        // optional divB output (single patch: fab on the valid box)

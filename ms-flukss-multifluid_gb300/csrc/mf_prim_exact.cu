@@ -35,7 +35,7 @@ __global__ void __launch_bounds__(kMaxBlock)
     double u[MF_MAX_COMP];
 #pragma unroll
     for (int q = 0; q < MF_MAX_COMP; ++q)
-      if (q < P.nc) u[q] = U[base + q * cs];
+      if (q < P.ils) u[q] = U[base + q * cs];
     cons_to_prim_plasma(P, u, w);
     if (GLM) w[8] = u[8];
 #pragma unroll
@@ -67,7 +67,13 @@ __global__ void __launch_bounds__(kMaxBlock)
   }
 #pragma unroll
   for (int q = 0; q < MF_MAX_COMP; ++q)
-    if (q < P.nc) W[base + q * cs] = w[q];
+    if (q < P.ils) W[base + q * cs] = w[q];
+  // tracking surfaces: copied (EqSysMHDMF::stateToPrim, srcIdeal/EqSysMHDMF.cpp:
+  // 207-210); on far-field ghosts the region tracer holds +1 (HELIOGS
+  // :996-1000) and the other surfaces, which HELIOGS leaves unassigned, keep
+  // U's ghost value
+  for (int q = P.ils; q < P.nc; ++q)
+    W[base + q * cs] = (od >= 0 && P.reg_tracer && q == P.nc - 1) ? 1.0 : U[base + q * cs];
 }
 
 // ---------------------------------------------------------------------------

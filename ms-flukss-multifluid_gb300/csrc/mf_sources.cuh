@@ -14,9 +14,62 @@ namespace fast {
 
 constexpr double kInvPi = 0.318309886183790671537767526745028724;
 
-// DEFINE_REGIONS_2F (swlism/SWLISMF.ChF:654-742), Cartesian branch.
+// DEFINE_REGIONS_TRACER_4F (swlism/SWLISMF.ChF:839-1016), Cartesian: regtr
+// is the region tracer of the cell (negative: solar wind).  The thresholds
+// are the routine's literals.  Its x > 650 test reads the x of the last
+// solar-wind cell the routine visited (x is assigned in that branch only);
+// here the cell's own x, the same on every domain within x <= 650.
+__device__ __forceinline__ int region_tracer_cell(const DevParams& P, double dx, int i, int j,
+                                                  int k, const double* w, double regtr) {
+  const double x = __dadd_rn(__dmul_rn(i + 0.5, dx), -P.sun_c[0]);
+  const double ux = w[1], uy = w[2], uz = w[3];
+  int reg;
+  if (regtr < 0.0) {
+    const double y = __dadd_rn(__dmul_rn(j + 0.5, dx), -P.sun_c[1]);
+    double z = 0.0, r2, invr, ur;
+    if (P.sd == 3) {
+      z = __dadd_rn(__dmul_rn(k + 0.5, dx), -P.sun_c[2]);
+      r2 = __dadd_rn(__dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y)), __dmul_rn(z, z));
+      invr = __ddiv_rn(1.0, __dsqrt_rn(r2));
+      ur = __dadd_rn(__dadd_rn(__dmul_rn(ux, __dmul_rn(x, invr)), __dmul_rn(uy, __dmul_rn(y, invr))),
+                     __dmul_rn(uz, __dmul_rn(z, invr)));
+    } else {
+      r2 = __dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y));
+      invr = __ddiv_rn(1.0, __dsqrt_rn(r2));
+      ur = __dadd_rn(__dmul_rn(ux, __dmul_rn(x, invr)), __dmul_rn(uy, __dmul_rn(y, invr)));
+    }
+    if (fabs(ur) >= __dmul_rn(0.6, P.sun_v)) {
+      const double TEMP = __ddiv_rn(__dmul_rn(P.t_coeff, w[4]), w[0]);
+      reg = ((TEMP >= 1.0e6) && (r2 > __dmul_rn(P.sun_r, P.sun_r))) ? 2 : 3;
+    } else {
+      reg = 2;
+    }
+    if (P.sd == 3 && ((z < P.zbot) || (z > P.ztop))) reg = 4;
+  } else {
+    reg = 1;
+    double vel = __dadd_rn(__dmul_rn(ux, ux), __dmul_rn(uy, uy));
+    if (P.sd == 3) vel = __dadd_rn(vel, __dmul_rn(uz, uz));
+    vel = __dsqrt_rn(vel);
+    const double ang = __ddiv_rn(
+        __dadd_rn(__dadd_rn(__dmul_rn(ux, P.lism_u[0]), __dmul_rn(uy, P.lism_u[1])),
+                  __dmul_rn(uz, P.lism_u[2])),
+        vel);
+    const double TEMP = __ddiv_rn(__dmul_rn(P.t_coeff, w[4]), w[0]);
+    if (w[0] > 1.2) reg = 4;
+    if (vel < 0.8) reg = 4;
+    if (ang < 0.95) reg = 4;
+    if (TEMP > 9000.0) reg = 4;
+    if (x > 650.0) reg = 1;
+  }
+  return reg;
+}
+
+// DEFINE_REGIONS_2F (swlism/SWLISMF.ChF:654-742), Cartesian branch, or the
+// tracer variant above (HeliosphericProblem::defineRegions,
+// swlism/HeliosphericProblem.cpp:2538-2575).
 __device__ __forceinline__ int region_cell(const DevParams& P, double dx, int i, int j, int k,
-                                           const double* w) {
+                                           const double* w, double regtr) {
+  if (P.reg_tracer) return region_tracer_cell(P, dx, i, j, k, w, regtr);
   const double x = __dadd_rn(__dmul_rn(i + 0.5, dx), -P.sun_c[0]);
   const double y = __dadd_rn(__dmul_rn(j + 0.5, dx), -P.sun_c[1]);
   double z = 0.0, r2, invr, ur;

@@ -10,9 +10,57 @@ namespace mf {
 namespace exact {
 
 // ---------------------------------------------------------------------------
-// DEFINE_REGIONS_2F (swlism/SWLISMF.ChF:654-742), Cartesian branch.
+// DEFINE_REGIONS_TRACER_4F (swlism/SWLISMF.ChF:839-1016), Cartesian: regtr
+// is the region tracer of the cell (negative: solar wind).  The thresholds
+// are the routine's literals.  Its x > 650 test reads the x of the last
+// solar-wind cell the routine visited (x is assigned in that branch only);
+// here the cell's own x, the same on every domain within x <= 650.
+__device__ __forceinline__ int region_tracer_cell(const DevParams& P, double dx, int i, int j,
+                                                  int k, const double* w, double regtr) {
+  const double x = (i + 0.5) * dx - P.sun_c[0];
+  const double ux = w[1], uy = w[2], uz = w[3];
+  int reg;
+  if (regtr < 0.0) {
+    const double y = (j + 0.5) * dx - P.sun_c[1];
+    double z = 0.0, r2, invr, ur;
+    if (P.sd == 3) {
+      z = (k + 0.5) * dx - P.sun_c[2];
+      r2 = x * x + y * y + z * z;
+      invr = 1.0 / sqrt(r2);
+      ur = ux * (x * invr) + uy * (y * invr) + uz * (z * invr);
+    } else {
+      r2 = x * x + y * y;
+      invr = 1.0 / sqrt(r2);
+      ur = ux * (x * invr) + uy * (y * invr);
+    }
+    if (fabs(ur) >= 0.6 * P.sun_v) {
+      const double TEMP = P.t_coeff * w[4] / w[0];
+      reg = ((TEMP >= 1.0e6) && (r2 > P.sun_r * P.sun_r)) ? 2 : 3;
+    } else {
+      reg = 2;
+    }
+    if (P.sd == 3 && ((z < P.zbot) || (z > P.ztop))) reg = 4;
+  } else {
+    reg = 1;
+    double vel = (P.sd == 3) ? (ux * ux + uy * uy + uz * uz) : (ux * ux + uy * uy);
+    vel = sqrt(vel);
+    const double ang = (ux * P.lism_u[0] + uy * P.lism_u[1] + uz * P.lism_u[2]) / vel;
+    const double TEMP = P.t_coeff * w[4] / w[0];
+    if (w[0] > 1.2) reg = 4;
+    if (vel < 0.8) reg = 4;
+    if (ang < 0.95) reg = 4;
+    if (TEMP > 9000.0) reg = 4;
+    if (x > 650.0) reg = 1;
+  }
+  return reg;
+}
+
+// DEFINE_REGIONS_2F (swlism/SWLISMF.ChF:654-742), Cartesian branch, or the
+// tracer variant above (HeliosphericProblem::defineRegions,
+// swlism/HeliosphericProblem.cpp:2538-2575).
 __device__ __forceinline__ int region_cell(const DevParams& P, double dx, int i, int j, int k,
-                                           const double* w) {
+                                           const double* w, double regtr) {
+  if (P.reg_tracer) return region_tracer_cell(P, dx, i, j, k, w, regtr);
   double x = (i + 0.5) * dx - P.sun_c[0];
   double y = (j + 0.5) * dx - P.sun_c[1];
   double z = 0.0, r2, invr, ur;

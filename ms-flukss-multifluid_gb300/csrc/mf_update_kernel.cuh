@@ -17,6 +17,41 @@ using namespace MF_PHYS;
 __device__ __forceinline__ double flux_diff(double hi, double lo) { return hi - lo; }
 __device__ __forceinline__ double flux_diff(float hi, float lo) { return (double)(hi - lo); }
 
+// Floor of POSTPROCESSING_LS (src/LevelSetF.ChF:426-465) for surface q of
+// the cell at x (offset base): the minimum of the stage-start values of the
+// cell and its 2*SpaceDim neighbours, lowered to -|maximum|.  Stage-start
+// values: the primitive copy wls inside the domain, the state uin on
+// far-field ghosts (where the primitive ghost holds boundary values; no stage
+// writes there, so uin is the stage-start state even for in-place stages).
+__device__ __forceinline__ double ls_floor(const DevParams& P, const RunParams& RP,
+                                           const double* __restrict__ wls,
+                                           const double* __restrict__ uin, const int* fn,
+                                           long long base, long long cs, const int* x, int q) {
+  auto old_at = [&](int d, int o) {
+    const long long st = (d == 0) ? 1 : (d == 1) ? (long long)fn[0] : (long long)fn[0] * fn[1];
+    const long long idx = base + o * st + q * cs;
+    const int y = x[d] + o;
+    const bool ghost = P.bc_kind == MF_BC_FARFIELD && !P.periodic[d] &&
+                       (y < RP.dlo[d] || y > RP.dhi[d]);
+    return ghost ? uin[idx] : wls[idx];
+  };
+  const double c = wls[base + q * cs];
+  double Umax = c, Umin = c;
+#pragma unroll
+  for (int o = -1; o <= 1; o += 2) {
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      if (d < P.sd) {
+        const double v = old_at(d, o);
+        Umax = fmax(Umax, v);
+        Umin = fmin(Umin, v);
+      }
+    }
+  }
+  const double abmax = fabs(Umax);
+  return fmin(Umin, -abmax);
+}
+
 __device__ __forceinline__ bool dt_less(double a, int ia, double b, int ib) {
   return (a < b) || (a == b && ia < ib);
 }
@@ -93,6 +128,7 @@ __global__ void __launch_bounds__(kMaxBlock)
     const long long cs = (long long)D.fn[0] * D.fn[1] * D.fn[2];
     const long long base = D.u_off + loc(D.flo, D.fn, i, j, k);
     const double dt = ss->dt * dt_scale;
+    const double* __restrict__ wst = B.wls ? B.wls : B.w;
     double u[MF_MAX_COMP];
 #pragma unroll
     for (int q = 0; q < MF_MAX_COMP; ++q)
@@ -111,8 +147,18 @@ __global__ void __launch_bounds__(kMaxBlock)
         const R* __restrict__ Fd = (const R*)B.f[d] + D.f_off[d] + loc(D.vlo, fnb, i, j, k);
 #pragma unroll
         for (int q = 0; q < MF_MAX_COMP; ++q)
-          if (q < P.nc)
+          if (q < P.ils)
             u[q] = u[q] - dtinv * flux_diff(Fd[q * fcs + sf], Fd[q * fcs]);
+        // UPDATELEVELSET (src/LevelSetF.ChF:200-234): the tracking surfaces,
+        // non-conservative with the stage-start cell velocity
+        if (P.nls) {
+          const double vel = wst[base + (1 + d) * cs];
+          const double cf = dt / RP.dx * vel;
+#pragma unroll
+          for (int q = 0; q < MF_MAX_COMP; ++q)
+            if (q >= P.ils && q < P.nc)
+              u[q] = u[q] - cf * flux_diff(Fd[q * fcs + sf], Fd[q * fcs]);
+        }
       }
     }
 
@@ -123,7 +169,7 @@ __global__ void __launch_bounds__(kMaxBlock)
     if (need_w) {
 #pragma unroll
       for (int q = 0; q < MF_MAX_COMP; ++q)
-        if (q < P.nc) w[q] = B.w[base + q * cs];
+        if (q < P.ils) w[q] = B.w[base + q * cs];
     }
     double divB = 0.0;
     if (P.use8) {
@@ -156,13 +202,23 @@ __global__ void __launch_bounds__(kMaxBlock)
       u[8] = exp(-dt * ch * ch / (cp * cp)) * u[8];
     }
     if (P.ce && P.nf >= 2) {
-      const int reg = region_cell(P, RP.dx, i, j, k, w);
+      const double regtr = P.reg_tracer ? B.w[base + (P.nc - 1) * cs] : 0.0;
+      const int reg = region_cell(P, RP.dx, i, j, k, w, regtr);
       charge_exchange_add<IRHON>(P, w, reg, dt, u);
     }
     if (P.reinit) reinit_cell(P, RP.dx, i, j, k, u);
     positivity_cell<IRHON>(P, u);
+    if (P.nls) {  // POSTPROCESSING_LS (srcIdeal/PatchMHDMF.cpp:1414-1424)
+      const int x[3] = {i, j, k};
+      const double f0 = ls_floor(P, RP, wst, B.uin, D.fn, base, cs, x, P.ils);
+      const double f1 = (P.nls > 1) ? ls_floor(P, RP, wst, B.uin, D.fn, base, cs, x, P.ils + 1)
+                                    : 0.0;
+#pragma unroll
+      for (int q = 0; q < MF_MAX_COMP; ++q)
+        if (q >= P.ils && q < P.nc) u[q] = fmax(u[q], (q == P.ils) ? f0 : f1);
+    }
 
-    if (FLAGS & kStageAverage) {  // AVERAGESTATE (src/PatchMHDAMF.ChF:289-316)
+    if (FLAGS & kStageAverage) {  // AVERAGESTATE (src/PatchMHDAMF.ChF:289-316), every state
 #pragma unroll
       for (int q = 0; q < MF_MAX_COMP; ++q)
         if (q < P.nc) u[q] = u[q] + 0.5 * (B.uold[base + q * cs] - B.uin[base + q * cs]);

@@ -110,12 +110,23 @@ class MfParams(ctypes.Structure):
         ("check_tvd", ctypes.c_int),
         ("helio_bc", ctypes.c_int),
         ("neutral_sun_bc", ctypes.c_int),
+        ("num_tracking_surfaces", ctypes.c_int),
+        ("limiter_ls", ctypes.c_int),
+        ("region_tracer", ctypes.c_int),
+        ("lism_u", ctypes.c_double * 3),
     ]
 
 
-def num_cons(p: MfParams) -> int:
-    """EqSysMHDMF component count (srcIdeal/EqSysMHDMF.cpp:11-48)."""
+def num_fluid_cons(p: MfParams) -> int:
+    """Fluid components (EqSysMHDMF::consInterval, srcIdeal/EqSysMHDMF.cpp:
+    11-48): plasma, psi with GLM, 5 per neutral fluid."""
     return 8 + (1 if p.divb_cleaning == 5 else 0) + (p.n_fluids - 1) * 5
+
+
+def num_cons(p: MfParams) -> int:
+    """EqSysMHDMF state count: the fluid components, then the tracking
+    surfaces (lvlsStateInterval)."""
+    return num_fluid_cons(p) + p.num_tracking_surfaces
 
 
 def num_ghost(p: MfParams) -> int:
@@ -304,13 +315,7 @@ def _base_params(space_dim: int, n_fluids: int) -> MfParams:
     p.factor_ch = 0.0
     p.factor_cp = 1.0
     p.ce_scale_vel = 1.0
-    # Scale of the charge-exchange rates (the reference's SETCHARGEEX_PARS
-    # dimensional factor).  Inside the reset sphere the wind density grows as
-    # (R0/r)^2, to ~55 in the cell next to the centre on 128^3, where a scale
-    # of 1 puts dt * (loss rate) near 0.7 per stage: the explicit source then
-    # drives the neutral populations through their density floors, in FP64 as
-    # well as in mixed precision.  0.1 keeps that product below ~0.07.
-    p.ce_sigma_scale = 0.1
+    p.ce_sigma_scale = 1.0
     p.ce_sigma_a = 2.1
     p.ce_sigma_b = 0.092
     p.ce_damp_c = 0.0
@@ -325,6 +330,10 @@ def _base_params(space_dim: int, n_fluids: int) -> MfParams:
         p.domain_hi[d] = 63 if d < space_dim else 0
         p.periodic[d] = 1
     p.bc_kind = BC_NONE
+    p.num_tracking_surfaces = 0
+    p.limiter_ls = LIM_MINMOD
+    p.region_tracer = 0
+    p.lism_u[0] = -1.0
     return p
 
 
@@ -354,13 +363,15 @@ HELIO_T_INFLOW = 0.5
 
 
 def helio_params(n: int = 128, seed: int = 20240601, time_approximation: int = TA_RK2,
-                 precision: int = PREC_FP64) -> MfParams:
+                 precision: int = PREC_FP64, region_tracer: bool = False) -> MfParams:
     """Synthetic heliosphere on [-1,1]^3 with n^3 cells (index space 0..n-1):
     MHD plasma + 3 neutral H fluids, gamma 5/3, GLM cleaning (Roe 7-wave +
     Dedner), van Leer neutral fluxes, charge exchange with a seeded cross-section
     sigma(v) = (a - b ln v)^2, regions after DEFINE_REGIONS_2F, an inner
     solar-wind sphere of radius 0.1 reset after every stage, far-field
-    boundaries holding the inflow state."""
+    boundaries holding the inflow state.  region_tracer: one more component,
+    the region tracer (-1 in the wind sphere, +1 outside), and regions after
+    DEFINE_REGIONS_TRACER_4F with the inflow direction as the LISM flow."""
     p = _base_params(3, 4)
     p.time_approximation = time_approximation
     p.precision = precision
@@ -427,6 +438,13 @@ def helio_params(n: int = 128, seed: int = 20240601, time_approximation: int = T
     # initial GLM speeds; the level step replaces them from its dt
     p.dedner_ch = 10.0
     p.dedner_cp = float(np.sqrt(10.0 * p.dx))
+    if region_tracer:
+        p.num_tracking_surfaces = 1
+        p.region_tracer = 1
+        p.limiter_ls = LIM_MINMOD
+        v = np.array(wp[1:4])
+        for d in range(3):
+            p.lism_u[d] = float(v[d] / np.linalg.norm(v))
     return p
 
 

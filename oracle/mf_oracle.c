@@ -130,6 +130,7 @@ enum { RS_ROE8 = 0, RS_ROE7 = 1, RS_RUSANOV = 2, RS_VFROE = 3 };
 typedef struct {
   const mf_params* p;
   int sd, nf, glm, nc, nprim, irhon, ipsi;
+  int ils, nls; /* tracking surfaces: components ils .. nc-1 after the fluids */
   int rs, aver;
   double gamma, hgamma, invhgamma, smallr, smallp, del2, smallB;
   double dCh, dCp;
@@ -144,7 +145,14 @@ static int ctx_init(Ctx* c, const mf_params* p) {
   c->sd = p->space_dim;
   c->nf = p->n_fluids;
   c->glm = (p->divb_cleaning == 5) ? 1 : 0;
-  c->nc = 8 + c->glm + (c->nf - 1) * 5;
+  /* lvlsStateInterval after consStateInterval; the primitive interval is
+     the same (srcIdeal/EqSysMHDMF.cpp:32-42) */
+  c->ils = 8 + c->glm + (c->nf - 1) * 5;
+  c->nls = p->num_tracking_surfaces;
+  if (c->nls < 0) return MF_ERR_BAD_ARG;
+  if (c->nls > 2 || c->ils + c->nls > MF_MAX_COMP) return MF_ERR_UNSUPPORTED;
+  if (p->region_tracer && c->nls < 1) return MF_ERR_BAD_ARG;
+  c->nc = c->ils + c->nls;
   c->nprim = c->nc;
   c->irhon = 8 + c->glm;
   c->ipsi = c->glm ? 8 : -1;
@@ -241,6 +249,8 @@ static void cons_to_prim_cell(const Ctx* c, const double* U, double* W) {
     W[s + 4] = p;
   }
   if (c->glm) W[8] = U[8];
+  /* EqSysMHDMF::stateToPrim copies the tracking surfaces (:207-210) */
+  for (int q = c->ils; q < c->nc; ++q) W[q] = U[q];
 }
 
 /* ------------------------------------------------------------------------ */
@@ -355,6 +365,7 @@ static void face_values(int lim, double Wm1, double WP, double Wp1, double* WL, 
    (main/MHDAM.cpp:927-1009). */
 static int limiter_of(const Ctx* c, int v) {
   if (v < 8) return c->p->limiter[v];
+  if (v >= c->ils) return c->p->limiter_ls; /* main/MHDAM.cpp:1005-1006 */
   return MF_LIM_MINMOD;
 }
 
@@ -1850,8 +1861,70 @@ static void helio_bc_face(const Ctx* c, int d, int side, const double* wl, const
 /* ------------------------------------------------------------------------ */
 
 /* DEFINE_REGIONS_2F (swlism/SWLISMF.ChF:654-742), Cartesian branch. */
+/* DEFINE_REGIONS_TRACER_4F (swlism/SWLISMF.ChF:839-1016), Cartesian: the
+   sign of the region tracer W[nc-1] separates the solar wind (< 0) from the
+   interstellar medium.  The thresholds are the routine's literals (its "3mG"
+   set).  Its last test, x > 650 -> 1, reads x, which the routine assigns only
+   in the solar-wind branch (so it holds the x of the last solar-wind cell
+   visited); here it is the cell's own x.  The two agree on every domain
+   whose cells all lie at x <= 650 from the sun. */
+static int region_tracer_cell(const Ctx* c, int i, int j, int k, const double* W) {
+  const mf_params* p = c->p;
+  const double rho_thr = 1.2, vel_thr = 0.8, vel_ang_thr = 0.95, temp_thr = 9000;
+  double dx = p->dx;
+  double LIMSUN = 0.6 * p->sun_v;
+  double coeff = p->region_t_coeff;
+  double sunR2 = p->sun_r * p->sun_r;
+  double regtr = W[c->nc - 1];
+  double x = (i + 0.5) * dx - p->sun_center[0];
+  double ux = W[1], uy = W[2], uz = W[3];
+  int reg;
+  if (regtr < 0.0) {
+    double y = (j + 0.5) * dx - p->sun_center[1];
+    double z = 0.0, r2, invr, ur;
+    if (c->sd == 3) {
+      z = (k + 0.5) * dx - p->sun_center[2];
+      r2 = x * x + y * y + z * z;
+      invr = 1.0 / sqrt(r2);
+      ur = ux * (x * invr) + uy * (y * invr) + uz * (z * invr);
+    } else {
+      r2 = x * x + y * y;
+      invr = 1.0 / sqrt(r2);
+      ur = ux * (x * invr) + uy * (y * invr);
+    }
+    if (fabs(ur) >= LIMSUN) {
+      double TEMP = coeff * W[4] / W[0];
+      if ((TEMP >= 1.0e6) && (r2 > sunR2))
+        reg = 2;
+      else
+        reg = 3;
+    } else {
+      reg = 2;
+    }
+    if (c->sd == 3 && ((z < p->region_zbot) || (z > p->region_ztop))) reg = 4;
+  } else {
+    reg = 1;
+    double vel = (c->sd == 3) ? (ux * ux + uy * uy + uz * uz) : (ux * ux + uy * uy);
+    vel = sqrt(vel);
+    double ang = (ux * p->lism_u[0] + uy * p->lism_u[1] + uz * p->lism_u[2]) / vel;
+    double rho = W[0], pr = W[4];
+    double TEMP = coeff * pr / rho;
+    if (rho > rho_thr) reg = 4;
+    if (vel < vel_thr) reg = 4;
+    if (ang < vel_ang_thr) reg = 4;
+    if (TEMP > temp_thr) reg = 4;
+    if (x > 650) reg = 1;
+  }
+  return reg;
+}
+
+/* DEFINE_REGIONS_2F (swlism/SWLISMF.ChF:654-742), Cartesian; the region
+   tracer variant above when mf_params.region_tracer is set
+   (HeliosphericProblem::defineRegions, swlism/HeliosphericProblem.cpp:
+   2538-2575). */
 static int region_cell(const Ctx* c, int i, int j, int k, const double* W) {
   const mf_params* p = c->p;
+  if (p->region_tracer) return region_tracer_cell(c, i, j, k, W);
   double dx = p->dx;
   double LIMSUN = 0.6 * p->sun_v;
   double coeff = p->region_t_coeff;
@@ -2139,7 +2212,11 @@ static void positivity_cell(const Ctx* c, double* U) {
    Applied per direction in order 0,1,2 over the part of W's box outside the
    domain in that direction (HeliosphericProblem::fillGhostCells,
    swlism/HeliosphericProblem.cpp:1663-1760). */
-static void fill_ghost_cells(const Ctx* c, Fab* W) {
+/* HELIOGS (swlism/HeliosphericF.ChF:978-1140) on the primitive ghosts outside
+   the domain.  The region tracer holds +1 there (:996-1000).  Other tracking
+   surfaces are not set by HELIOGS (the reference leaves those ghosts of W
+   unassigned); here they copy U's ghost value. */
+static void fill_ghost_cells(const Ctx* c, const Fab* U, Fab* W) {
   const mf_params* p = c->p;
   if (p->bc_kind != MF_BC_FARFIELD) return;
   for (int d = 0; d < c->sd; ++d) {
@@ -2157,6 +2234,8 @@ static void fill_ghost_cells(const Ctx* c, Fab* W) {
         edge = p->domain_hi[d];
       }
       FOR_BOX(bb, i, j, k) {
+        for (int q = c->ils; q < c->nc; ++q) AT(W, i, j, k, q) = AT(U, i, j, k, q);
+        if (p->region_tracer) AT(W, i, j, k, c->nc - 1) = 1.0;
         for (int q = 0; q < 8; ++q) AT(W, i, j, k, q) = p->bc_plasma[q];
         if (c->glm) AT(W, i, j, k, 8) = 0.0;
         if (c->nf > 1)
@@ -2172,6 +2251,66 @@ static void fill_ghost_cells(const Ctx* c, Fab* W) {
       }
     }
   }
+}
+
+/* ------------------------------------------------------------------------ */
+/* tracking surfaces (level sets)                                            */
+/* ------------------------------------------------------------------------ */
+
+/* LEVELSETFLUX (src/LevelSetF.ChF:37-105) of one face for every surface:
+   the left face state (high face of the low cell) where
+   sqrt(rho_L) u_L + sqrt(rho_R) u_R > 0 with the plasma density and normal
+   velocity (lsIndexField = WVELX, src/PhysProblem.cpp:327-330), else the
+   right one.  Called after fluxBC (src/PatchMHDAM.cpp:644-648). */
+static void level_set_flux(const Ctx* c, int d, const double* wl, const double* wr, double* g) {
+  double Uavg = sqrt(wl[0]) * wl[1 + d] + sqrt(wr[0]) * wr[1 + d];
+  for (int q = c->ils; q < c->nc; ++q) g[q] = (Uavg > 0.0) ? wl[q] : wr[q];
+}
+
+/* UPDATELEVELSET (src/LevelSetF.ChF:200-234), Cartesian (dx constant, metric
+   coefficient 1): phi -= dt/dx * u_d * (F(i+e_d) - F(i)), u_d the cell's
+   velocity of the primitive state W. */
+static void level_set_update(const Ctx* c, Fab* U, const Fab* W, const Fab* Fl, int d, double dt,
+                             mf_box box) {
+  int o[3] = {0, 0, 0};
+  o[d] = 1;
+  const double du = c->p->dx * 1.0;
+  for (int q = c->ils; q < c->nc; ++q)
+    FOR_BOX(box, i, j, k) {
+      double vel = AT(W, i, j, k, 1 + d);
+      AT(U, i, j, k, q) = AT(U, i, j, k, q) - dt / du * vel *
+                                                  (AT(Fl, i + o[0], j + o[1], k + o[2], q) -
+                                                   AT(Fl, i, j, k, q));
+    }
+}
+
+/* POSTPROCESSING_LS (src/LevelSetF.ChF:426-465) from PatchMHDMF::
+   postprocessing (srcIdeal/PatchMHDMF.cpp:1414-1424): Umin = min of the
+   stage-start values of the cell and its 2*SpaceDim neighbours, lowered to
+   -|max|.  The routine assigns min(LS, Umax) and then max(LS, Umin) from the
+   same LS, so only the floor remains. */
+static void level_set_postprocess(const Ctx* c, Fab* U, const Fab* Uold, mf_box box) {
+  for (int q = c->ils; q < c->nc; ++q)
+    FOR_BOX(box, i, j, k) {
+      double Umax = AT(Uold, i, j, k, q), Umin = AT(Uold, i, j, k, q);
+      for (int ii = -1; ii <= 1; ii += 2) {
+        Umax = fmax(Umax, AT(Uold, i + ii, j, k, q));
+        Umin = fmin(Umin, AT(Uold, i + ii, j, k, q));
+        Umax = fmax(Umax, AT(Uold, i, j + ii, k, q));
+        Umin = fmin(Umin, AT(Uold, i, j + ii, k, q));
+        if (c->sd == 3) {
+          Umax = fmax(Umax, AT(Uold, i, j, k + ii, q));
+          Umin = fmin(Umin, AT(Uold, i, j, k + ii, q));
+        }
+      }
+      double abmax = fabs(Umax);
+      double abmin = fabs(Umin);
+      Umax = fmax(Umax, abmin);
+      Umin = fmin(Umin, -abmax);
+      double LS = AT(U, i, j, k, q);
+      AT(U, i, j, k, q) = fmin(LS, Umax);
+      AT(U, i, j, k, q) = fmax(LS, Umin);
+    }
 }
 
 /* ------------------------------------------------------------------------ */
@@ -2199,7 +2338,7 @@ static int euler_step(const Ctx* c, double time, Fab* U, Fab* F /* [sd] or NULL 
     cons_to_prim_cell(c, u, w);
     for (int q = 0; q < np; ++q) AT(&W, i, j, k, q) = w[q];
   }
-  fill_ghost_cells(c, &W);
+  fill_ghost_cells(c, U, &W);
 
   mf_box valueBox = box_and_domain(a_box, p);
   mf_box slopeBox = box_grow(valueBox, 1, sd);
@@ -2292,21 +2431,27 @@ static int euler_step(const Ctx* c, double time, Fab* U, Fab* F /* [sd] or NULL 
         for (int q = 0; q < nc; ++q) AT(&Fl[d], i, j, k, q) = g[q];
       }
       AT(&Bn[d], i, j, k, 0) = bn;
+      if (c->nls) {
+        level_set_flux(c, d, wl, wr, g);
+        for (int q = c->ils; q < nc; ++q) AT(&Fl[d], i, j, k, q) = g[q];
+      }
     }
   }
 
-  /* finalUpdate -> UPDATECONS (src/PatchMHDAMF.ChF:542-587) */
+  /* finalUpdate (src/PatchMHDAM.cpp:475-493): UPDATECONS (src/PatchMHDAMF.ChF:
+     542-587) on the fluid components, then UPDATELEVELSET */
   double invvol = 1.0 / p->dx;
   for (int d = 0; d < sd; ++d) {
     int o[3] = {0, 0, 0};
     o[d] = 1;
-    for (int q = 0; q < nc; ++q) {
+    for (int q = 0; q < c->ils; ++q) {
       FOR_BOX(valueBox, i, j, k) {
         AT(U, i, j, k, q) = AT(U, i, j, k, q) - dt * invvol *
                                                     (AT(&Fl[d], i + o[0], j + o[1], k + o[2], q) -
                                                      AT(&Fl[d], i, j, k, q));
       }
     }
+    level_set_update(c, U, &W, &Fl[d], d, dt, valueBox);
   }
 
   /* addExplicitSources (srcIdeal/PatchMHDMF.cpp:1149-1389) */
@@ -2354,6 +2499,7 @@ static int euler_step(const Ctx* c, double time, Fab* U, Fab* F /* [sd] or NULL 
     positivity_cell(c, u);
     for (int q = 0; q < nc; ++q) AT(U, i, j, k, q) = u[q];
   }
+  if (c->nls) level_set_postprocess(c, U, &Uold, valueBox);
 
   if (F) {
     for (int d = 0; d < sd; ++d) {
@@ -2496,6 +2642,9 @@ static void hancock_point_flux(const Ctx* c, int d, const double* w, double* F) 
     F[s + 1 + (d + 2) % 3] = r * un * wn;
     F[s + 4] = un * (en + pn);
   }
+  /* FLUXESHANCOCK_LS (src/LevelSetF.ChF:9-35): surface times the plasma
+     normal velocity */
+  for (int q = c->ils; q < c->nc; ++q) F[q] = w[q] * w[in];
 }
 
 /* addExplicitSources for PatchMHDMF (srcIdeal/PatchMHDMF.cpp:1149-1389) on
@@ -2548,7 +2697,7 @@ static void prim_fab(const Ctx* c, const Fab* U, mf_box WBoxB, Fab* W) {
     cons_to_prim_cell(c, u, w);
     for (int q = 0; q < c->nprim; ++q) AT(W, i, j, k, q) = w[q];
   }
-  fill_ghost_cells(c, W);
+  fill_ghost_cells(c, U, W);
 }
 
 /* updateState, TA_Hancock (src/PatchMHDAM.cpp:1287-1301): predictorHancock
@@ -2588,7 +2737,11 @@ static int hancock_step(const Ctx* c, double time, Fab* U, Fab* F, Fab* divBout,
       }
       hancock_point_flux(c, d, wm, fm);
       hancock_point_flux(c, d, wp, fp);
-      for (int q = 0; q < nc; ++q)
+      /* UPDATELEVELSETHANCOCK (src/LevelSetF.ChF:354-388), Cartesian */
+      double vel = AT(&W, i, j, k, 1 + d);
+      for (int q = c->ils; q < nc; ++q)
+        AT(&Up, i, j, k, q) = AT(&Up, i, j, k, q) - dtp / (p->dx * 1.0) * vel * (fp[q] - fm[q]);
+      for (int q = 0; q < c->ils; ++q)
         AT(&Up, i, j, k, q) = AT(&Up, i, j, k, q) - dtp * invvol * (fp[q] - fm[q]);
     }
   }
@@ -2632,20 +2785,27 @@ static int hancock_step(const Ctx* c, double time, Fab* U, Fab* F, Fab* divBout,
         helio_bc_face(c, d, f == p->domain_lo[d] ? 0 : 1, wl, wr, g, &bnv);
         AT(&Bn[d], i, j, k, 0) = bnv;
       }
+      if (c->nls) level_set_flux(c, d, wl, wr, g);
       for (int q = 0; q < nc; ++q) AT(&Fl[d], i, j, k, q) = g[q];
     }
   }
-  /* finalUpdate -> UPDATECONS with the full dt */
+  /* the corrector's Uold: the state before the step (src/PatchMHDAM.cpp:
+     1043-1044; the predictor advanced a copy) */
+  Fab Uold = fab_alloc(UBox, nc);
+  memcpy(Uold.p, U->p, sizeof(double) * (size_t)(Uold.csz * nc));
+  /* finalUpdate with the full dt: UPDATECONS, then UPDATELEVELSET with the
+     velocity of W(t) (correctorHancock receives the predictor's WOld) */
   for (int d = 0; d < sd; ++d) {
     int o[3] = {0, 0, 0};
     o[d] = 1;
-    for (int q = 0; q < nc; ++q) {
+    for (int q = 0; q < c->ils; ++q) {
       FOR_BOX(vb2, i, j, k) {
         AT(U, i, j, k, q) = AT(U, i, j, k, q) - dt * invvol *
                                                     (AT(&Fl[d], i + o[0], j + o[1], k + o[2], q) -
                                                      AT(&Fl[d], i, j, k, q));
       }
     }
+    level_set_update(c, U, &W, &Fl[d], d, dt, vb2);
   }
   explicit_sources(c, U, &Wpr, Bn, dt, vb2, divBout);
   double u[MF_MAX_COMP];
@@ -2655,6 +2815,8 @@ static int hancock_step(const Ctx* c, double time, Fab* U, Fab* F, Fab* divBout,
     positivity_cell(c, u);
     for (int q = 0; q < nc; ++q) AT(U, i, j, k, q) = u[q];
   }
+  if (c->nls) level_set_postprocess(c, U, &Uold, vb2);
+  fab_free(&Uold);
   if (F) {
     for (int d = 0; d < sd; ++d) {
       mf_box fb = box_nodes(vb2, d);
@@ -3523,8 +3685,9 @@ static int hier_advance(Hier* H, int l) {
   H->ndt[l] = nd;
   Fab** Fl = (Fab**)malloc(sizeof(Fab*) * (size_t)L->npatch);
   for (int b = 0; b < L->npatch; ++b) Fl[b] = &H->F[l][3 * b];
-  if (l + 1 < H->nlev) reg_set_coarse(&H->reg[l], nc, Fl, H->dt[l]);
-  if (l > 0) reg_add_fine(&H->reg[l - 1], nc, sd, H->ratio[l - 1], Fl, H->dt[l]);
+  const int ncons = nc - H->p[l].num_tracking_surfaces;
+  if (l + 1 < H->nlev) reg_set_coarse(&H->reg[l], ncons, Fl, H->dt[l]);
+  if (l > 0) reg_add_fine(&H->reg[l - 1], ncons, sd, H->ratio[l - 1], Fl, H->dt[l]);
   free(Fl);
   H->t[l] = H->t[l] + H->dt[l];
   if (l == 0 && H->p[0].divb_cleaning == 5 && H->p[0].factor_ch > 0.0) {
@@ -3551,7 +3714,7 @@ static int hier_time_step(Hier* H, int l) {
       if (st) return st;
     }
     const mf_oracle_level *C = &H->lev[l], *Fn = &H->lev[l + 1];
-    reg_reflux(&H->reg[l], &H->p[l], C->U[0].ncomp, C->U);
+    reg_reflux(&H->reg[l], &H->p[l], C->U[0].ncomp - H->p[l].num_tracking_surfaces, C->U);
     st = average_down(&H->p[l], &H->p[l + 1], H->ratio[l], C->npatch, C->U, C->valid,
                       Fn->npatch, Fn->U, Fn->valid);
   }
@@ -3595,8 +3758,10 @@ int mf_oracle_hier_step(int nlev, const mf_oracle_level* lev, const int* ratio, 
         H.old[l][b] = L->U[b];
         H.old[l][b].data = (double*)malloc(sizeof(double) * (size_t)(f.csz * nc));
       }
+      /* the registers hold the fluid components (consInterval,
+         srcIdeal/AMRLevelIdealMHD.cpp:1282-1305), not the tracking surfaces */
       st = reg_build(L->p, ratio[l], L->npatch, L->valid, lev[l + 1].npatch, lev[l + 1].valid,
-                     nc, &H.reg[l]);
+                     nc - L->p->num_tracking_surfaces, &H.reg[l]);
     }
   }
   if (st == MF_OK) st = hier_time_step(&H, 0);

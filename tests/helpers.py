@@ -25,29 +25,32 @@ def valid_view(U: np.ndarray, ng: int, sd: int) -> np.ndarray:
     return U[:, ng:-ng, ng:-ng, ng:-ng]
 
 
-def component_groups(nc: int) -> list[list[int]]:
+def component_groups(nc: int, nls: int = 0) -> list[list[int]]:
     """Physical groups of the conserved components: density, momentum vector,
     energy, magnetic field vector, psi, then density / momentum / energy of
-    each neutral fluid."""
-    glm = 1 if (nc - 8) % 5 == 1 else 0
+    each neutral fluid, then each of the nls tracking surfaces."""
+    nf = nc - nls
+    glm = 1 if (nf - 8) % 5 == 1 else 0
     groups = [[0], [1, 2, 3], [4], [5, 6, 7]]
     if glm:
         groups.append([8])
     s = 8 + glm
-    while s + 5 <= nc:
+    while s + 5 <= nf:
         groups += [[s], [s + 1, s + 2, s + 3], [s + 4]]
         s += 5
+    groups += [[q] for q in range(nf, nc)]
     return groups
 
 
-def rel_err(a: np.ndarray, b: np.ndarray, floor_frac: float = 1e-3) -> np.ndarray:
+def rel_err(a: np.ndarray, b: np.ndarray, floor_frac: float = 1e-3, nls: int = 0) -> np.ndarray:
     """Per-component maximum of |a-b| / max(|b|, floor_frac * S): pointwise
     relative error, where S is the largest magnitude of the component's
     physical group (a vector component that is zero, e.g. the z-momentum of a
-    2D run, is measured against the magnitude of its vector)."""
+    2D run, is measured against the magnitude of its vector).  nls: number of
+    tracking surfaces after the fluid components."""
     nc = b.shape[0]
     scale = np.zeros(nc)
-    for g in component_groups(nc):
+    for g in component_groups(nc, nls):
         s = max(float(np.max(np.abs(b[c]))) if b[c].size else 0.0 for c in g)
         for c in g:
             scale[c] = s

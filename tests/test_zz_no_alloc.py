@@ -41,7 +41,7 @@ def _case(case):
         dt = 2e-3
     else:
         n, sd = 16, 3
-        p = mfgpu.helio_params(n)
+        p = mfgpu.helio_params(n, region_tracer=(case == "helio_tracer"))
         ctx = mfgpu.Context(p)
         lo, hi = mfgpu.grow([0, 0, 0], [n - 1] * 3, ctx.ng, 3)
         U = mfgpu.init_host_fab(p, lo, hi, "helio")
@@ -50,7 +50,7 @@ def _case(case):
     return p, ctx, U, lo, hi, vlo, vhi, sd, dt
 
 
-@pytest.mark.parametrize("case", ["orszag", "helio"])
+@pytest.mark.parametrize("case", ["orszag", "helio", "helio_tracer"])
 def test_noalloc_matches_patch_update(gpulib, case):
     p, ctx, U, lo, hi, vlo, vhi, sd, dt = _case(case)
     lib = ctx.lib
@@ -62,7 +62,7 @@ def test_noalloc_matches_patch_update(gpulib, case):
         sb, dtb, cb = _call(lib.mf_patch_update_noalloc, ctx, tb, lo, hi, vlo, vhi, dt)
         assert sa == mfgpu.MF_OK and sb == mfgpu.MF_OK, (call, sa, sb)
         ua, ub = to_host(ta), to_host(tb)
-        e = rel_err(valid_view(ub, ng, sd), valid_view(ua, ng, sd))
+        e = rel_err(valid_view(ub, ng, sd), valid_view(ua, ng, sd), nls=p.num_tracking_surfaces)
         assert np.all(e <= RTOL), (call, e)
         assert abs(dtb - dta) <= RTOL * dta, (call, dta, dtb)
         assert ca == cb, (call, ca, cb)
