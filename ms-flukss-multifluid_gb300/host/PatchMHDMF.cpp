@@ -30,6 +30,16 @@ void PatchMHDMF::setReconstruction(const int limiters[8], bool checkPositivity) 
   invalidate();
 }
 
+void PatchMHDMF::setTrackingSurfaces(int nSurfaces, int limiterLS, bool regionTracer,
+                                     const double* lismU) {
+  m_p.num_tracking_surfaces = nSurfaces;
+  m_p.limiter_ls = limiterLS;
+  m_p.region_tracer = regionTracer ? 1 : 0;
+  if (lismU)
+    for (int d = 0; d < 3; ++d) m_p.lism_u[d] = lismU[d];
+  invalidate();
+}
+
 void PatchMHDMF::setTimeApproximation(eTimeApproximation m) {
   m_p.time_approximation = (int)m;
   invalidate();

@@ -38,6 +38,13 @@ class PatchMHDMF {
   void setCurrentTime(double t);
   // EOS constants of /eos/ (gamma, smallr, smallp)
   void setEOS(double gamma, double smallr, double smallp);
+  // Tracking surfaces: EqSysMHDMF(iDedner, nFluids, nTrackingSurfaces) and the
+  // limiter of their slopes (main/MHDAM.cpp:709-718, 1005-1006).  regionTracer:
+  // the last surface is the heliosphere's region tracer (region_tracer,
+  // swlism/HeliosphericProblem.cpp:2538-2575) and lismU the interstellar flow
+  // direction (lismUX/UY/UZ); null keeps the current one.
+  void setTrackingSurfaces(int nSurfaces, int limiterLS, bool regionTracer = false,
+                           const double* lismU = nullptr);
   // Problem domain in index space, periodicity and the uniform cell size.
   void define(const mf_box& domain, const int periodic[3], double dx);
   // Full parameter access for the physics options the setters do not cover
