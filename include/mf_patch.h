@@ -105,7 +105,12 @@ typedef struct mf_params {
   int time_approximation;  /* MF_TA_FIRST_ORDER or MF_TA_RK2 */
   int flux;                /* mhdam.flux: 0/1 Roe 8-wave arithmetic avg, 3 Roe 8-wave Roe avg,
                               2/4 Rusanov (arith/Roe avg), 11/13 Roe 7-wave (arith/Roe avg) */
-  int divb_cleaning;       /* 0: none; 5: GLM/Dedner (Roe 7-wave + 2x2 (Bn,psi) flux) */
+  int divb_cleaning;       /* eDivergenceCleaning (src/PatchMHDAM.H:43-50): 0 none;
+                              1-3 constrained transport with the edge field of
+                              Balsara-Spicer (1) or Gardiner-Stone (2, 3; 2D only:
+                              the reference's 3D routines store the z-edge field
+                              through EX); 5 GLM/Dedner (Roe 7-wave + 2x2 (Bn,psi)
+                              flux); 4 (projection) is not supported */
   int use_8wave;           /* Powell 8-wave source (mhdam.8wave_use) */
   int divb_method;         /* 0: none; 1: Bn = average of face states; 2: central */
   int limiter[8];          /* limiter per plasma primitive rho,u,v,w,p,bx,by,bz */
@@ -231,6 +236,28 @@ mf_status mf_set_wait_timeout(mf_ctx* ctx, double seconds);
 mf_status mf_patch_update(mf_ctx* ctx, mf_fab* U, const mf_box* valid, double dt,
                           mf_fab* F, mf_fab* divB, double* new_dt, int min_cell[3],
                           void* stream);
+
+/* mf_patch_update with updateState's EdgeBox argument (src/PatchMHDAM.H:
+   252-260): with constrained transport (divb_cleaning 1-3), E receives the
+   edge field of the step (the average of the two RK2 stages' fields, or the
+   one stage's), as EdgeBox fabs on `valid`: in 3D three device fabs,
+   E[d] on the valid box made nodal in the two directions other than d; in
+   2D one nodal fab E[0].  E may be NULL; without constrained transport it is
+   not touched. */
+mf_status mf_patch_update_e(mf_ctx* ctx, mf_fab* U, const mf_box* valid, double dt,
+                            mf_fab* F, mf_fab* divB, mf_fab* E, double* new_dt,
+                            int min_cell[3], void* stream);
+
+/* PatchMHDMF::recalculateMagneticField (srcIdeal/PatchMHDMF.cpp:1461-1484 ->
+   recalculateB, srcIdeal/DivCleaningF.ChF:4-72): on `box`, B = Uold's B minus
+   dt times the discrete curl of the edge field E (EdgeBox fabs as above),
+   and U's energy keeps its non-magnetic part.  What AMRLevelIdealMHD::
+   postTimeStep does after a level step with constrained transport
+   (srcIdeal/AMRLevelIdealMHD.cpp:1649-1688), with the level's UOld.
+   Requires divb_cleaning 1-3. */
+mf_status mf_recalculate_magnetic_field(mf_ctx* ctx, mf_fab* U, const mf_fab* Uold,
+                                        const mf_fab* E, double dt, const mf_box* box,
+                                        void* stream);
 
 /* Size of the device scratch array of mf_patch_update_noalloc: 16 MiB, enough
    for a 16^3 patch of the 24-component multi-fluid model with 4 ghost layers

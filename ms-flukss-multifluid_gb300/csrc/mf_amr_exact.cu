@@ -947,6 +947,12 @@ mf_status mf_hier_create(int nlevels, mf_level* const* levels, const int* ratios
     for (int m = l + 1; m < nlevels; ++m)
       if (levels[l] == levels[m] || level_view(levels[l]).ctx == level_view(levels[m]).ctx)
         return MF_ERR_BAD_ARG;  // one context (dx, domain, GLM speeds) per level
+  // constrained transport across levels (the accumulated edge field averaged
+  // onto the coarser level, srcIdeal/AMRLevelIdealMHD.cpp:1649-1688) is not built
+  for (int l = 0; l < nlevels && nlevels > 1; ++l) {
+    const int dc = level_view(levels[l]).p->divb_cleaning;
+    if (dc >= 1 && dc <= 3) return MF_ERR_UNSUPPORTED;
+  }
   mf_hier* h = new (std::nothrow) mf_hier();
   if (!h) return MF_ERR_OOM;
   h->lv.assign(levels, levels + nlevels);

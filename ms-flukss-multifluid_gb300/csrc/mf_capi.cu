@@ -149,7 +149,12 @@ mf_status validate_params(const mf_params& p) {
   if (p.precision != MF_PREC_FP64 && p.precision != MF_PREC_MIXED &&
       p.precision != MF_PREC_FP64_FAST)
     return MF_ERR_BAD_ARG;
-  if (p.divb_cleaning != 0 && p.divb_cleaning != 5) return MF_ERR_UNSUPPORTED;
+  if (!(p.divb_cleaning == 0 || (p.divb_cleaning >= 1 && p.divb_cleaning <= 3) ||
+        p.divb_cleaning == 5))
+    return MF_ERR_UNSUPPORTED;
+  // electricFieldGS0/GS1 in 3D store the z-edge field through EX
+  // (srcIdeal/DivCleaningF.ChF:478-566, 700-852): nothing defined to match
+  if (p.divb_cleaning >= 2 && p.divb_cleaning <= 3 && p.space_dim == 3) return MF_ERR_UNSUPPORTED;
   if (p.check_tvd < 0 || p.check_tvd > 2) return MF_ERR_BAD_ARG;
   if (p.helio_bc && (p.bc_kind != MF_BC_FARFIELD || p.space_dim != 3)) return MF_ERR_UNSUPPORTED;
   if (p.neutral_sun_bc && (p.space_dim != 3 || p.n_fluids < 2)) return MF_ERR_UNSUPPORTED;
@@ -192,6 +197,7 @@ DevParams make_dev(const mf_params& p) {
   P.nls = p.num_tracking_surfaces;
   P.lim_ls = p.limiter_ls;
   P.reg_tracer = (p.region_tracer && P.nls > 0) ? 1 : 0;
+  P.ct = (p.divb_cleaning >= 1 && p.divb_cleaning <= 3) ? p.divb_cleaning : 0;
   for (int d = 0; d < 3; ++d) P.lism_u[d] = p.lism_u[d];
   P.irhon = 8 + P.glm;
   // RiemannSolver::make (src/RiemannSolver.cpp:13-112)
@@ -323,6 +329,7 @@ struct mf_ctx {
   double timeout = 600.0;
   DevBuf pred, w, f1[3], bn1[3], f2[3], bn2[3], desc, partials, state;
   DevBuf fv[3], w2;  // Hancock face values and predicted primitive state
+  DevBuf ct_u0, ct_e1, ct_e2, ct_eo;  // constrained transport: U(t), stage edge fields, average
   PinnedBuf hdesc, hstate;
 };
 
@@ -349,6 +356,7 @@ struct mf_level {
   std::vector<mf::FaceGather> gathers;     // flux-register faces of a hierarchy
   DevBuf sun;                              // NEUTRALS_SUNBC cell pairs
   int nsun = 0;
+  DevBuf ct_u0, ct_e1, ct_e2, ct_eo;       // constrained transport: UOld, edge fields
 };
 
 extern "C" {
@@ -543,8 +551,49 @@ static void single_run(const mf_ctx* c, const mf::Batch& last, RunParams& r) {
   r.v1 = last.tot_v;
 }
 
+// Edge fabs of an EdgeBox on box (3 in 3D, 1 nodal in 2D) that contain it.
+static bool edges_ok(const mf_fab* E, const mf_box& box, int sd) {
+  const int nd = (sd == 3) ? 3 : 1;
+  for (int d = 0; d < nd; ++d) {
+    mf_box b = box;
+    for (int e = 0; e < sd; ++e) b.hi[e] += (sd == 3 && e == d) ? 0 : 1;
+    if (!E[d].data || E[d].ncomp != 1 || !box_contains(E[d].box, b)) return false;
+  }
+  return true;
+}
+
+static mf_status patch_update_impl(mf_ctx* c, mf_fab* U, const mf_box* valid, double dt,
+                                   mf_fab* F, mf_fab* divB, mf_fab* E, double* new_dt,
+                                   int min_cell[3], void* stream);
+
 mf_status mf_patch_update(mf_ctx* c, mf_fab* U, const mf_box* valid, double dt, mf_fab* F,
                           mf_fab* divB, double* new_dt, int min_cell[3], void* stream) {
+  return patch_update_impl(c, U, valid, dt, F, divB, nullptr, new_dt, min_cell, stream);
+}
+
+mf_status mf_patch_update_e(mf_ctx* c, mf_fab* U, const mf_box* valid, double dt, mf_fab* F,
+                            mf_fab* divB, mf_fab* E, double* new_dt, int min_cell[3],
+                            void* stream) {
+  return patch_update_impl(c, U, valid, dt, F, divB, E, new_dt, min_cell, stream);
+}
+
+mf_status mf_recalculate_magnetic_field(mf_ctx* c, mf_fab* U, const mf_fab* Uold,
+                                        const mf_fab* E, double dt, const mf_box* box,
+                                        void* stream) {
+  if (!c || !U || !U->data || !Uold || !Uold->data || !E || !box) return MF_ERR_BAD_ARG;
+  if (!c->dp.ct) return MF_ERR_BAD_ARG;
+  const int sd = c->p.space_dim;
+  if (U->ncomp != c->nc || Uold->ncomp < 8 || !box_contains(U->box, *box) ||
+      !box_contains(Uold->box, *box) || !edges_ok(E, *box, sd) || !std::isfinite(dt))
+    return MF_ERR_BAD_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  MF_CHECK_CUDA(mf::launch_recalc_ext(sd, c->p.dx, U, Uold, E, dt, *box, s));
+  return wait_stream(s, c->timeout);
+}
+
+static mf_status patch_update_impl(mf_ctx* c, mf_fab* U, const mf_box* valid, double dt,
+                                   mf_fab* F, mf_fab* divB, mf_fab* E, double* new_dt,
+                                   int min_cell[3], void* stream) {
   if (!c) return MF_ERR_BAD_ARG;
   mf_status st = check_fab(c, U, valid);
   if (st != MF_OK) return st;
@@ -570,8 +619,18 @@ mf_status mf_patch_update(mf_ctx* c, mf_fab* U, const mf_box* valid, double dt, 
       if (!F[d].data || F[d].ncomp != nc || !box_contains(F[d].box, box_nodes(v2, d)))
         return MF_ERR_BAD_ARG;
   }
+  const bool ct = c->dp.ct != 0;
+  if (E && ct && !edges_ok(E, *valid, sd)) return MF_ERR_BAD_ARG;
 
   MF_CHECK_CUDA(c->w.ensure(sizeof(double) * fabn * nc));
+  if (ct) {
+    MF_CHECK_CUDA(c->ct_e1.ensure(sizeof(double) * fabn * 3));
+    MF_CHECK_CUDA(c->ct_e2.ensure(sizeof(double) * fabn * 3));
+    if (rk2) {
+      MF_CHECK_CUDA(c->ct_u0.ensure(sizeof(double) * fabn * nc));
+      MF_CHECK_CUDA(c->ct_eo.ensure(sizeof(double) * fabn * 3));
+    }
+  }
   if (rk2) MF_CHECK_CUDA(c->pred.ensure(sizeof(double) * fabn * nc));
   const mf_box s1 = box_grow(v1, 1, sd);  // Hancock slope box
   if (hk) {
@@ -621,9 +680,17 @@ mf_status mf_patch_update(mf_ctx* c, mf_fab* U, const mf_box* valid, double dt, 
   StageBuffers B;
   std::memset(&B, 0, sizeof(B));
   B.w = (double*)c->w.p;
+  // constrained transport (src/PatchMHDAM.cpp:684-698, 1150-1160): after each
+  // stage's update, the edge field of its fluxes and B from the stage-start
+  // field; the dt then follows the last recalculation
+  double* e1 = (double*)c->ct_e1.p;
+  double* e2 = (double*)c->ct_e2.p;
   if (rk2) {
     MF_CHECK_CUDA(cudaMemcpyAsync(c->pred.p, U->data, sizeof(double) * fabn * nc,
                                   cudaMemcpyDeviceToDevice, s));
+    if (ct)
+      MF_CHECK_CUDA(cudaMemcpyAsync(c->ct_u0.p, U->data, sizeof(double) * fabn * nc,
+                                    cudaMemcpyDeviceToDevice, s));
     B.uin = U->data;
     B.uout = (double*)c->pred.p;
     for (int d = 0; d < 3; ++d) {
@@ -631,6 +698,10 @@ mf_status mf_patch_update(mf_ctx* c, mf_fab* U, const mf_box* valid, double dt, 
       B.bn[d] = c->bn1[d].p;
     }
     MF_CHECK_CUDA(mf::launch_stage(c->dp, p.precision, B, b1, 0, 1.0, ds, parts, &nb, s));
+    if (ct) {
+      MF_CHECK_CUDA(mf::launch_efield(c->dp, mixed, B.f, B.w, e1, nullptr, nullptr, b1, s));
+      MF_CHECK_CUDA(mf::launch_recalc_b(c->dp, B.uout, B.w, e1, nullptr, nullptr, ds, 1.0, b1, s));
+    }
     B.uin = (double*)c->pred.p;
     B.uout = U->data;
     B.uold = U->data;
@@ -645,8 +716,16 @@ mf_status mf_patch_update(mf_ctx* c, mf_fab* U, const mf_box* valid, double dt, 
         B.divb_n[d] = divB->box.hi[d] - divB->box.lo[d] + 1;
       }
     }
-    MF_CHECK_CUDA(mf::launch_stage(c->dp, p.precision, B, b2, mf::kStageAverage | mf::kStageDt,
-                                   0.5, ds, parts, &nb, s));
+    MF_CHECK_CUDA(mf::launch_stage(c->dp, p.precision, B, b2,
+                                   ct ? 0 : (mf::kStageAverage | mf::kStageDt), 0.5, ds, parts,
+                                   &nb, s));
+    if (ct) {
+      MF_CHECK_CUDA(mf::launch_efield(c->dp, mixed, B.f, B.w, e2, e1, (double*)c->ct_eo.p, b2,
+                                      s));
+      MF_CHECK_CUDA(mf::launch_recalc_b(c->dp, U->data, B.w, e2, (const double*)c->ct_u0.p,
+                                        (const double*)c->pred.p, ds, 0.5, b2, s));
+      MF_CHECK_CUDA(mf::launch_dt(c->dp, U->data, b2, parts, &nb, s));
+    }
   } else if (hk) {
     B.uin = U->data;
     B.uout = U->data;
@@ -664,7 +743,13 @@ mf_status mf_patch_update(mf_ctx* c, mf_fab* U, const mf_box* valid, double dt, 
     mf::HancockBuffers H;
     for (int d = 0; d < 3; ++d) H.fv[d] = (double*)c->fv[d].p;
     H.w2 = (double*)c->w2.p;
-    MF_CHECK_CUDA(mf::launch_hancock(c->dp, p.precision, B, H, b1, b2, ds, parts, &nb, s));
+    MF_CHECK_CUDA(mf::launch_hancock(c->dp, p.precision, B, H, b1, b2, ds, parts, &nb, s,
+                                     ct ? 0 : mf::kStageDt));
+    if (ct) {  // the corrector's field: W(t+dt/2) for the edges, B from W(t)
+      MF_CHECK_CUDA(mf::launch_efield(c->dp, mixed, B.f, H.w2, e2, nullptr, nullptr, b2, s));
+      MF_CHECK_CUDA(mf::launch_recalc_b(c->dp, U->data, B.w, e2, nullptr, nullptr, ds, 1.0, b2, s));
+      MF_CHECK_CUDA(mf::launch_dt(c->dp, U->data, b2, parts, &nb, s));
+    }
   } else {
     B.uin = U->data;
     B.uout = U->data;
@@ -679,10 +764,18 @@ mf_status mf_patch_update(mf_ctx* c, mf_fab* U, const mf_box* valid, double dt, 
         B.divb_n[d] = divB->box.hi[d] - divB->box.lo[d] + 1;
       }
     }
-    MF_CHECK_CUDA(
-        mf::launch_stage(c->dp, p.precision, B, b2, mf::kStageDt, 1.0, ds, parts, &nb, s));
+    MF_CHECK_CUDA(mf::launch_stage(c->dp, p.precision, B, b2, ct ? 0 : mf::kStageDt, 1.0, ds,
+                                   parts, &nb, s));
+    if (ct) {
+      MF_CHECK_CUDA(mf::launch_efield(c->dp, mixed, B.f, B.w, e2, nullptr, nullptr, b2, s));
+      MF_CHECK_CUDA(mf::launch_recalc_b(c->dp, U->data, B.w, e2, nullptr, nullptr, ds, 1.0, b2, s));
+      MF_CHECK_CUDA(mf::launch_dt(c->dp, U->data, b2, parts, &nb, s));
+    }
   }
   MF_CHECK_CUDA(mf::launch_finalize(c->dp, parts, b2, b2.nt[2], ds, 0, s));
+  if (ct && E)  // updateState's E: the step average (RK2) or the one stage's field
+    MF_CHECK_CUDA(
+        mf::launch_edges_out(sd, rk2 ? (const double*)c->ct_eo.p : e2, U->box, *valid, E, s));
   if (F) {
     const void* f2p[3] = {nullptr, nullptr, nullptr};
     const void* f1p[3] = {nullptr, nullptr, nullptr};
@@ -1134,6 +1227,32 @@ static mf_status enqueue_level_step(mf_level* L, int advance, cudaEvent_t* ev = 
   MF_CHECK_CUDA(mf::launch_exchange((double*)L->U.p, (const CopyReg*)L->exfull.p, L->nfull, nc, s));
   if (L->nfull) mark(0);
   const int mixed = (p.precision == MF_PREC_MIXED);
+  // constrained transport (src/PatchMHDAM.cpp:684-698, 1150-1160): the level's
+  // UOld (AMRLevelIdealMHD::preTimeStep), per stage the edge field of the
+  // stage's fluxes and B from the stage-start field, the dt after the last
+  // recalculation, and after the step B from UOld and the step's edge field
+  // (AMRLevelIdealMHD::postTimeStep, srcIdeal/AMRLevelIdealMHD.cpp:1649-1688)
+  const bool ct = c->dp.ct != 0;
+  double* e1 = (double*)L->ct_e1.p;
+  double* e2 = (double*)L->ct_e2.p;
+  double* u0 = (double*)L->ct_u0.p;
+  if (ct)
+    MF_CHECK_CUDA(cudaMemcpyAsync(u0, L->U.p, sizeof(double) * L->total,
+                                  cudaMemcpyDeviceToDevice, s));
+  auto ct_stage = [&](const mf::Batch& b, const double* wedge, double* e, const double* ep,
+                      double* eavg, double* u, const double* a0, const double* a1,
+                      double scale) -> mf_status {
+    MF_CHECK_CUDA(mf::launch_efield(c->dp, mixed, B.f, wedge, e, ep, eavg, b, s));
+    mark(7);
+    MF_CHECK_CUDA(mf::launch_recalc_b(c->dp, u, B.w, e, a0, a1, ds, scale, b, s));
+    mark(7);
+    return MF_OK;
+  };
+  auto ct_dt = [&]() -> mf_status {
+    MF_CHECK_CUDA(mf::launch_dt(c->dp, (const double*)L->U.p, L->b2, parts, &nb, s));
+    mark(3);
+    return MF_OK;
+  };
   const void* fl[3] = {L->F[0].p, L->F[1].p, L->F[2].p};
   auto gather = [&](int mode) -> mf_status {
     for (const mf::FaceGather& g : L->gathers) {
@@ -1150,6 +1269,9 @@ static mf_status enqueue_level_step(mf_level* L, int advance, cudaEvent_t* ev = 
     B.ev = ev ? ev + ne : nullptr;
     MF_CHECK_CUDA(mf::launch_stage(c->dp, p.precision, B, L->b1, 0, 1.0, ds, parts, &nb, s));
     stage_marks(ne);
+    if (ct && (gst = ct_stage(L->b1, B.w, e1, nullptr, nullptr, (double*)L->U1.p, nullptr,
+                              nullptr, 1.0)) != MF_OK)
+      return gst;
     if ((gst = gather(0)) != MF_OK) return gst;
     MF_CHECK_CUDA(
         mf::launch_exchange((double*)L->U1.p, (const CopyReg*)L->extwo.p, L->ntwo, nc, s));
@@ -1158,9 +1280,16 @@ static mf_status enqueue_level_step(mf_level* L, int advance, cudaEvent_t* ev = 
     B.uout = (double*)L->U.p;
     B.uold = (const double*)L->U.p;
     B.ev = ev ? ev + ne : nullptr;
-    MF_CHECK_CUDA(mf::launch_stage(c->dp, p.precision, B, L->b2, mf::kStageAverage | mf::kStageDt,
-                                   0.5, ds, parts, &nb, s));
+    MF_CHECK_CUDA(mf::launch_stage(c->dp, p.precision, B, L->b2,
+                                   ct ? 0 : (mf::kStageAverage | mf::kStageDt), 0.5, ds, parts,
+                                   &nb, s));
     stage_marks(ne);
+    if (ct) {
+      if ((gst = ct_stage(L->b2, B.w, e2, e1, (double*)L->ct_eo.p, (double*)L->U.p, u0,
+                          (const double*)L->U1.p, 0.5)) != MF_OK)
+        return gst;
+      if ((gst = ct_dt()) != MF_OK) return gst;
+    }
     if ((gst = gather(1)) != MF_OK) return gst;
   } else if (p.time_approximation == MF_TA_HANCOCK) {
     B.uin = (const double*)L->U.p;
@@ -1169,7 +1298,8 @@ static mf_status enqueue_level_step(mf_level* L, int advance, cudaEvent_t* ev = 
     mf::HancockBuffers H;
     for (int d = 0; d < 3; ++d) H.fv[d] = (double*)L->FV[d].p;
     H.w2 = (double*)L->U1.p;
-    MF_CHECK_CUDA(mf::launch_hancock(c->dp, p.precision, B, H, L->b1, L->b2, ds, parts, &nb, s));
+    MF_CHECK_CUDA(mf::launch_hancock(c->dp, p.precision, B, H, L->b1, L->b2, ds, parts, &nb, s,
+                                     ct ? 0 : mf::kStageDt));
     if (ev) {  // prim, faces, predictor, shift, fluxes, update
       const int k0[4] = {1, 1, 3, 1};
       for (int q = 0; q < 4; ++q) kinds[ne + q] = k0[q];
@@ -1177,14 +1307,26 @@ static mf_status enqueue_level_step(mf_level* L, int advance, cudaEvent_t* ev = 
       kinds[ne + 4 + sd] = 3;
       ne += mf::hancock_launches(sd);
     }
+    if (ct) {  // the corrector's edges from W(t+dt/2), B from W(t)
+      if ((gst = ct_stage(L->b2, H.w2, e2, nullptr, nullptr, (double*)L->U.p, nullptr, nullptr,
+                          1.0)) != MF_OK)
+        return gst;
+      if ((gst = ct_dt()) != MF_OK) return gst;
+    }
     if ((gst = gather(2)) != MF_OK) return gst;
   } else {
     B.uin = (const double*)L->U.p;
     B.uout = (double*)L->U.p;
     B.ev = ev ? ev + ne : nullptr;
-    MF_CHECK_CUDA(
-        mf::launch_stage(c->dp, p.precision, B, L->b2, mf::kStageDt, 1.0, ds, parts, &nb, s));
+    MF_CHECK_CUDA(mf::launch_stage(c->dp, p.precision, B, L->b2, ct ? 0 : mf::kStageDt, 1.0, ds,
+                                   parts, &nb, s));
     stage_marks(ne);
+    if (ct) {
+      if ((gst = ct_stage(L->b2, B.w, e2, nullptr, nullptr, (double*)L->U.p, nullptr, nullptr,
+                          1.0)) != MF_OK)
+        return gst;
+      if ((gst = ct_dt()) != MF_OK) return gst;
+    }
     if ((gst = gather(2)) != MF_OK) return gst;
   }
   MF_CHECK_CUDA(mf::launch_finalize(c->dp, parts, L->b2, L->b2.nt[2], ds, advance, s));
@@ -1195,6 +1337,12 @@ static mf_status enqueue_level_step(mf_level* L, int advance, cudaEvent_t* ev = 
     MF_CHECK_CUDA(mf::launch_sun_copy((double*)L->U.p, (const mf::SunPair*)L->sun.p, L->nsun,
                                       c->dp.irhon, c->dp.nf, s));
     mark(6);
+  }
+  if (ct) {  // the level's recalculation with the step's dt (scale 1)
+    const double* eo = (p.time_approximation == MF_TA_RK2) ? (const double*)L->ct_eo.p : e2;
+    MF_CHECK_CUDA(mf::launch_recalc_b(c->dp, (double*)L->U.p, u0, eo, nullptr, nullptr, ds, 1.0,
+                                      L->b2, s));
+    mark(7);
   }
   if (nev) *nev = ne;
   return MF_OK;
@@ -1323,6 +1471,13 @@ mf_status mf_level_create(mf_ctx* c, int npatch, const mf_box* valid, mf_level**
         (e = cudaMemcpy(L->sun.p, plan.sun.data(), sizeof(mf::SunPair) * plan.sun.size(),
                         cudaMemcpyHostToDevice)) != cudaSuccess)
       break;
+    if (c->dp.ct) {  // UOld of the level and three edge fields (3 per cell of U)
+      const size_t eb = sizeof(double) * 3 * (size_t)(L->total / c->nc + 1);
+      if ((e = L->ct_u0.ensure(sizeof(double) * L->total)) != cudaSuccess) break;
+      if ((e = L->ct_e1.ensure(eb)) != cudaSuccess) break;
+      if ((e = L->ct_e2.ensure(eb)) != cudaSuccess) break;
+      if ((e = L->ct_eo.ensure(eb)) != cudaSuccess) break;
+    }
     if ((e = L->partials.ensure(sizeof(DtPartial) * (L->nparts + 1))) != cudaSuccess) break;
     if ((e = L->state.ensure(sizeof(StepState))) != cudaSuccess) break;
     if ((e = L->state2.ensure(sizeof(StepState))) != cudaSuccess) break;
@@ -1345,6 +1500,9 @@ mf_status mf_level_create(mf_ctx* c, int npatch, const mf_box* valid, mf_level**
   if (L->nfull == 0) L->launches -= 1;
   if (p.time_approximation == MF_TA_RK2 && L->ntwo == 0) L->launches -= 1;
   if (L->nsun) L->launches += 1;
+  // constrained transport: edge field + recalculation per stage, the dt after
+  // them, and the level's recalculation
+  if (c->dp.ct) L->launches += (p.time_approximation == MF_TA_RK2) ? 6 : 4;
   L->base_launches = L->launches;
   *out = L;
   return MF_OK;

@@ -35,6 +35,7 @@ struct DevParams {
   // fluid components), limiter lim_ls; reg_tracer: the last one is the
   // region tracer, lism_u the interstellar flow direction
   int ils, nls, lim_ls, reg_tracer;
+  int ct;  // constrained transport: 0 off, 1 Balsara-Spicer, 2 / 3 Gardiner-Stone (2D)
   int lim[8];
   int periodic[3], dlo[3], dhi[3];
   double gamma, hgamma, invhgamma, invgamma, smallr, smallp, del2, smallB, dx, invdx;

@@ -324,7 +324,7 @@ __global__ void __launch_bounds__(kMaxBlock)
 cudaError_t launch_hancock(const DevParams& P, int precision, const StageBuffers& B,
                            const HancockBuffers& H, const Batch& a, const Batch& c,
                            StepState* state, DtPartial* partials, int* nblocks_v,
-                           cudaStream_t s) {
+                           cudaStream_t s, int corrector_flags) {
   int ne = 0;
   auto mark = [&]() {
     if (B.ev) cudaEventRecord(B.ev[ne++], s);
@@ -365,12 +365,13 @@ cudaError_t launch_hancock(const DevParams& P, int precision, const StageBuffers
   StageBuffers B2 = B;
   B2.w = H.w2;
   B2.wls = B.w;
+  const int fl = corrector_flags;
   if (precision == MF_PREC_MIXED)
-    e = launch_update_fast<float>(P, B2, c, kStageDt, 1.0, state, partials, nblocks_v, s);
+    e = launch_update_fast<float>(P, B2, c, fl, 1.0, state, partials, nblocks_v, s);
   else if (precision == MF_PREC_FP64_FAST)
-    e = launch_update_fast<double>(P, B2, c, kStageDt, 1.0, state, partials, nblocks_v, s);
+    e = launch_update_fast<double>(P, B2, c, fl, 1.0, state, partials, nblocks_v, s);
   else
-    e = launch_update_exact(P, B2, c, kStageDt, 1.0, state, partials, nblocks_v, s);
+    e = launch_update_exact(P, B2, c, fl, 1.0, state, partials, nblocks_v, s);
   if (e != cudaSuccess) return e;
   mark();
   return cudaSuccess;

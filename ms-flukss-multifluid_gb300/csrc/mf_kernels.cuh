@@ -233,6 +233,30 @@ cudaError_t launch_flux_out(int mixed, int sd, int nc, const void* const f2[3],
                             const int f1lo[3][3], const int f1n[3][3], double* const fout[3],
                             const int olo[3][3], const int on[3][3], cudaStream_t s);
 
+// Constrained transport (mf_ct_exact.cu).  Internal edge field: 3 components
+// laid out like U on each patch's fab, at 3 x the patch's cell offset.
+// efield: the edge field of the stage's fluxes f on the nodes of each
+// valueBox (W: stage-start primitive state, for the 2D Gardiner-Stone
+// methods); with e1 / eavg set also eavg = (e + e1) / 2 there.
+cudaError_t launch_efield(const DevParams& P, int mixed, const void* const f[3],
+                          const double* w, double* e, const double* e1, double* eavg,
+                          const Batch& b, cudaStream_t s);
+// recalculateB on each valueBox from bold (components 5..7, laid out like U)
+// and the edge field e with time step state[run].dt * dt_scale; with u0 / u1
+// set, AVERAGESTATE u += (u0 - u1) / 2 afterwards.
+cudaError_t launch_recalc_b(const DevParams& P, double* u, const double* bold, const double* e,
+                            const double* u0, const double* u1, const StepState* state,
+                            double dt_scale, const Batch& b, cudaStream_t s);
+
+// recalculateMagneticField on caller fabs: U (in place) from Uold's field and
+// the EdgeBox fabs E (3 in 3D, 1 nodal in 2D) on box.
+cudaError_t launch_recalc_ext(int sd, double dx, mf_fab* U, const mf_fab* Uold, const mf_fab* E,
+                              double dt, const mf_box& box, cudaStream_t s);
+// The internal edge field of a single-patch call on the fab box `fab` into
+// the caller's EdgeBox fabs, on the edges of the valid box.
+cudaError_t launch_edges_out(int sd, const double* e, const mf_box& fab, const mf_box& valid,
+                             mf_fab* out, cudaStream_t s);
+
 // Number of kernel launches enqueued by launch_stage for sd dimensions.
 inline int stage_launches(int sd) { return 2 + sd; }
 
@@ -245,10 +269,12 @@ struct HancockBuffers {
   double* fv[3];
   double* w2;
 };
+// corrector_flags: the flags of the corrector's update (kStageDt, or 0 when
+// the dt follows later, as with constrained transport).
 cudaError_t launch_hancock(const DevParams& P, int precision, const StageBuffers& B,
                            const HancockBuffers& H, const Batch& a, const Batch& c,
                            StepState* state, DtPartial* partials, int* nblocks_v,
-                           cudaStream_t s);
+                           cudaStream_t s, int corrector_flags = kStageDt);
 inline int hancock_launches(int sd) { return 5 + sd; }
 
 // Corrector fluxes of the Hancock step from the shifted face values.

@@ -142,6 +142,7 @@ extern "C" mf_status mf_patch_update_noalloc(mf_ctx* ctx, mf_fab* U, const mf_bo
   if (!contains(U->box, grow(*valid, ng, sd))) return MF_ERR_BAD_ARG;
 
   if (p.time_approximation == MF_TA_HANCOCK) return MF_ERR_UNSUPPORTED;
+  if (p.divb_cleaning >= 1 && p.divb_cleaning <= 3) return MF_ERR_UNSUPPORTED;  // CT
   const bool rk2 = (p.time_approximation == MF_TA_RK2);
   const int mixed = (p.precision == MF_PREC_MIXED);
   const size_t rs = mf::flux_bytes(p.precision);

@@ -432,6 +432,7 @@ mf_status mf_server_create(mf_ctx* physics, double hbm_budget_bytes, int max_run
     return MF_ERR_BAD_ARG;
   *out = nullptr;
   if (mf::ctx_view(physics).p->time_approximation == MF_TA_HANCOCK) return MF_ERR_UNSUPPORTED;
+  if (mf::ctx_view(physics).dp->ct) return MF_ERR_UNSUPPORTED;  // constrained transport
   mf_server* S = new (std::nothrow) mf_server();
   if (!S) return MF_ERR_OOM;
   S->ctx = physics;

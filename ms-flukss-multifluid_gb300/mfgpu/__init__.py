@@ -153,6 +153,12 @@ _SIGS = {
     "mf_patch_update": (ctypes.c_int, [ctypes.c_void_p, _P(MfFab), _P(MfBox), ctypes.c_double,
                                        ctypes.c_void_p, ctypes.c_void_p,
                                        _P(ctypes.c_double), c_int3, ctypes.c_void_p]),
+    "mf_patch_update_e": (ctypes.c_int, [ctypes.c_void_p, _P(MfFab), _P(MfBox), ctypes.c_double,
+                                         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                         _P(ctypes.c_double), c_int3, ctypes.c_void_p]),
+    "mf_recalculate_magnetic_field": (ctypes.c_int, [ctypes.c_void_p, _P(MfFab), _P(MfFab),
+                                                     ctypes.c_void_p, ctypes.c_double, _P(MfBox),
+                                                     ctypes.c_void_p]),
     "mf_patch_update_noalloc": (ctypes.c_int, [ctypes.c_void_p, _P(MfFab), _P(MfBox),
                                                ctypes.c_double, ctypes.c_void_p, ctypes.c_void_p,
                                                _P(ctypes.c_double), c_int3, ctypes.c_void_p]),
@@ -525,9 +531,30 @@ class Context:
     def set_dedner(self, ch, cp):
         check(self.lib.mf_set_dedner(self.h, ch, cp), "mf_set_dedner")
 
+    def _edges(self, E):
+        """EdgeBox fabs (list of (device pointer, lo, hi), 3 in 3D, 1 in 2D)."""
+        arr = (MfFab * 3)()
+        for d in range(3):
+            ptr, lo, hi = E[min(d, len(E) - 1)]
+            arr[d] = MfFab(ptr, make_box(lo, hi), 1)
+        self._keep_e = arr
+        return ctypes.cast(arr, ctypes.c_void_p)
+
+    def recalculate_magnetic_field(self, U_ptr, Uold_ptr, fab_lo, fab_hi, E, dt, lo, hi,
+                                   stream=None):
+        """mf_recalculate_magnetic_field on device fabs (U in place)."""
+        fu = MfFab(U_ptr, make_box(fab_lo, fab_hi), self.nc)
+        fo = MfFab(Uold_ptr, make_box(fab_lo, fab_hi), self.nc)
+        box = make_box(lo, hi)
+        check(self.lib.mf_recalculate_magnetic_field(self.h, ctypes.byref(fu), ctypes.byref(fo),
+                                                     self._edges(E), dt, ctypes.byref(box),
+                                                     stream), "mf_recalculate_magnetic_field")
+
     def patch_update(self, U_ptr, fab_lo, fab_hi, valid_lo, valid_hi, dt, F=None, divB=None,
-                     stream=None, allow_error=False):
-        """mf_patch_update on a device fab; returns (status, new_dt, min_cell)."""
+                     stream=None, allow_error=False, E=None):
+        """mf_patch_update (mf_patch_update_e with E: EdgeBox fabs as
+        (device pointer, lo, hi)) on a device fab; returns (status, new_dt,
+        min_cell)."""
         fab = MfFab(U_ptr, make_box(fab_lo, fab_hi), self.nc)
         valid = make_box(valid_lo, valid_hi)
         ndt = ctypes.c_double()
@@ -545,8 +572,13 @@ class Context:
             dfab = MfFab(ptr, make_box(lo, hi), 1)
             self._keep_d = dfab
             dptr = ctypes.cast(ctypes.pointer(dfab), ctypes.c_void_p)
-        st = self.lib.mf_patch_update(self.h, ctypes.byref(fab), ctypes.byref(valid), dt, fptr,
-                                      dptr, ctypes.byref(ndt), cell, stream)
+        if E is None:
+            st = self.lib.mf_patch_update(self.h, ctypes.byref(fab), ctypes.byref(valid), dt,
+                                          fptr, dptr, ctypes.byref(ndt), cell, stream)
+        else:
+            st = self.lib.mf_patch_update_e(self.h, ctypes.byref(fab), ctypes.byref(valid), dt,
+                                            fptr, dptr, self._edges(E), ctypes.byref(ndt), cell,
+                                            stream)
         if not allow_error:
             check(st, "mf_patch_update")
         return st, ndt.value, tuple(cell)
@@ -652,7 +684,7 @@ class Level:
         return self.lib.mf_level_launches_per_step(self.h)
 
     KIND_NAMES = {0: "exchange", 1: "prim", 2: "flux", 3: "update", 4: "finalize", 5: "coupling",
-                  6: "postprocess"}
+                  6: "postprocess", 7: "constrained transport"}
 
     def profile_step(self, dt):
         """One step launch by launch with CUDA events between the launches;

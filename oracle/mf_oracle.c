@@ -131,6 +131,7 @@ typedef struct {
   const mf_params* p;
   int sd, nf, glm, nc, nprim, irhon, ipsi;
   int ils, nls; /* tracking surfaces: components ils .. nc-1 after the fluids */
+  int ct;       /* constrained transport: 0 off, 1 Balsara-Spicer, 2/3 Gardiner-Stone 1/2 */
   int rs, aver;
   double gamma, hgamma, invhgamma, smallr, smallp, del2, smallB;
   double dCh, dCp;
@@ -144,7 +145,17 @@ static int ctx_init(Ctx* c, const mf_params* p) {
   c->p = p;
   c->sd = p->space_dim;
   c->nf = p->n_fluids;
+  /* eDivergenceCleaning (src/PatchMHDAM.H:43-50): 1-3 constrained transport,
+     5 GLM; 4 (projection) needs an elliptic solver and is not restated */
+  if (!(p->divb_cleaning == 0 || (p->divb_cleaning >= 1 && p->divb_cleaning <= 3) ||
+        p->divb_cleaning == 5))
+    return MF_ERR_UNSUPPORTED;
   c->glm = (p->divb_cleaning == 5) ? 1 : 0;
+  c->ct = (p->divb_cleaning >= 1 && p->divb_cleaning <= 3) ? p->divb_cleaning : 0;
+  /* electricFieldGS0/GS1 in 3D store the z-edge field into EX over the EZ
+     index range (srcIdeal/DivCleaningF.ChF:478-566, :700-852): EZ is left
+     unset and EX is written outside its box; nothing defined to restate */
+  if (c->ct >= 2 && p->space_dim == 3) return MF_ERR_UNSUPPORTED;
   /* lvlsStateInterval after consStateInterval; the primitive interval is
      the same (srcIdeal/EqSysMHDMF.cpp:32-42) */
   c->ils = 8 + c->glm + (c->nf - 1) * 5;
@@ -2314,12 +2325,271 @@ static void level_set_postprocess(const Ctx* c, Fab* U, const Fab* Uold, mf_box 
 }
 
 /* ------------------------------------------------------------------------ */
+/* constrained transport                                                     */
+/* ------------------------------------------------------------------------ */
+
+/* EdgeBox (src/EdgeBox.cpp:105-131): in 3D, E[d] on surroundingNodes(box)
+   .enclosedCells(d) (cell-centred along d, nodal across); in 2D one nodal
+   array that E[0], E[1] and E[2] all address (operator[], :63-73). */
+typedef struct {
+  Fab e[3];
+  int n;
+} Edges;
+
+static void edges_alloc(Edges* E, mf_box box, int sd) {
+  mf_box nb = box;
+  for (int d = 0; d < sd; ++d) nb.hi[d] += 1;
+  if (sd == 3) {
+    E->n = 3;
+    for (int d = 0; d < 3; ++d) {
+      mf_box b = nb;
+      b.hi[d] -= 1;
+      E->e[d] = fab_alloc(b, 1);
+    }
+  } else {
+    E->n = 1;
+    E->e[0] = fab_alloc(nb, 1);
+    E->e[1] = E->e[2] = E->e[0];
+  }
+}
+
+static void edges_free(Edges* E) {
+  for (int d = 0; d < E->n; ++d) fab_free(&E->e[d]);
+}
+
+/* dst = src on the edges both hold (EdgeBox::copy on the intersection) */
+static void edges_copy(Edges* dst, const Edges* src) {
+  for (int d = 0; d < dst->n; ++d) {
+    mf_box b = dst->e[d].b;
+    for (int q = 0; q < 3; ++q) {
+      if (src->e[d].b.lo[q] > b.lo[q]) b.lo[q] = src->e[d].b.lo[q];
+      if (src->e[d].b.hi[q] < b.hi[q]) b.hi[q] = src->e[d].b.hi[q];
+    }
+    FOR_BOX(b, i, j, k) AT(&dst->e[d], i, j, k, 0) = AT(&src->e[d], i, j, k, 0);
+  }
+}
+
+/* electricFieldBS (srcIdeal/DivCleaningF.ChF:75-310): the edge field as the
+   mean of the tangential magnetic-field fluxes of the faces around the edge
+   that lie in the flux boxes of box (the faces of box).  2D: EZ from the
+   x-flux of By and the y-flux of Bx with weights 1/4, 1/3, 1/2 as the
+   literal H4, H3, H2; 3D: the sum over the present faces divided by their
+   count, EX from the z-flux of By and the y-flux of Bz, EY from the z-flux of
+   Bx and the x-flux of Bz, EZ from the y-flux of Bx and the x-flux of By. */
+static void electric_field_bs(const Ctx* c, const Fab* Fl, mf_box box, Edges* E) {
+  const double H2 = 0.5, H3 = 0.333333333333333333333333333333333333, H4 = 0.25;
+  const int lo0 = box.lo[0], hi0 = box.hi[0], lo1 = box.lo[1], hi1 = box.hi[1];
+  if (c->sd == 2) {
+    const Fab *F = &Fl[0], *G = &Fl[1];
+    Fab* EZ = &E->e[0];
+    FOR_BOX(EZ->b, i, j, k) {
+      double s = 0.0;
+      int n = 0;
+      if (i > lo0) {
+        s = AT(G, i - 1, j, k, 5);
+        n = 1;
+      }
+      if (i <= hi0) {
+        s = n ? s + AT(G, i, j, k, 5) : AT(G, i, j, k, 5);
+        n += 1;
+      }
+      if (j > lo1) {
+        s = s - AT(F, i, j - 1, k, 6);
+        n += 1;
+      }
+      if (j <= hi1) {
+        s = s - AT(F, i, j, k, 6);
+        n += 1;
+      }
+      const double h = (n == 4) ? H4 : (n == 3) ? H3 : H2;
+      AT(EZ, i, j, k, 0) = h * s;
+    }
+    return;
+  }
+  const int lo2 = box.lo[2], hi2 = box.hi[2];
+  const Fab *F = &Fl[0], *G = &Fl[1], *H = &Fl[2];
+  FOR_BOX(E->e[0].b, i, j, k) {
+    double EE = 0.0;
+    int iE = 0;
+    if (j > lo1) { EE = EE + AT(H, i, j - 1, k, 6); iE = iE + 1; }
+    if (j <= hi1) { EE = EE + AT(H, i, j, k, 6); iE = iE + 1; }
+    if (k > lo2) { EE = EE - AT(G, i, j, k - 1, 7); iE = iE + 1; }
+    if (k <= hi2) { EE = EE - AT(G, i, j, k, 7); iE = iE + 1; }
+    AT(&E->e[0], i, j, k, 0) = EE / iE;
+  }
+  FOR_BOX(E->e[1].b, i, j, k) {
+    double EE = 0.0;
+    int iE = 0;
+    if (i > lo0) { EE = EE - AT(H, i - 1, j, k, 5); iE = iE + 1; }
+    if (i <= hi0) { EE = EE - AT(H, i, j, k, 5); iE = iE + 1; }
+    if (k > lo2) { EE = EE + AT(F, i, j, k - 1, 7); iE = iE + 1; }
+    if (k <= hi2) { EE = EE + AT(F, i, j, k, 7); iE = iE + 1; }
+    AT(&E->e[1], i, j, k, 0) = EE / iE;
+  }
+  FOR_BOX(E->e[2].b, i, j, k) {
+    double EE = 0.0;
+    int iE = 0;
+    if (i > lo0) { EE = EE + AT(G, i - 1, j, k, 5); iE = iE + 1; }
+    if (i <= hi0) { EE = EE + AT(G, i, j, k, 5); iE = iE + 1; }
+    if (j > lo1) { EE = EE - AT(F, i, j - 1, k, 6); iE = iE + 1; }
+    if (j <= hi1) { EE = EE - AT(F, i, j, k, 6); iE = iE + 1; }
+    AT(&E->e[2], i, j, k, 0) = EE / iE;
+  }
+}
+
+/* electricFieldGS0 / electricFieldGS1 in 2D (srcIdeal/DivCleaningF.ChF:
+   335-408, 596-697; the result is stored through EX, which in 2D is the one
+   nodal array): the face average corrected by the difference between the
+   face fluxes and the cell-centred field EQ = u_y B_x - u_x B_y of the
+   cells around the node (W: velocity at 1..3, field at 5..7).  GS1 takes
+   the cell on the upwind side of each face by the sign of its mass flux. */
+static void electric_field_gs(const Ctx* c, const Fab* W, const Fab* Fl, mf_box box, Edges* E,
+                              int upwind) {
+  const int lo0 = box.lo[0], hi0 = box.hi[0], lo1 = box.lo[1], hi1 = box.hi[1];
+  const Fab *F = &Fl[0], *G = &Fl[1];
+  (void)c;
+  Fab* EX = &E->e[0];
+  FOR_BOX(EX->b, i, j, k) {
+    double EE = 0.0, EQ, DEDD;
+    int iE = 0;
+    double D1_00 = 0.0, D2_00 = 0.0, D1_10 = 0.0, D2_10 = 0.0;
+    double D1_01 = 0.0, D2_01 = 0.0, D1_11 = 0.0, D2_11 = 0.0;
+    int i00 = 0, i10 = 0, i01 = 0, i11 = 0;
+#define EQAT(ii, jj) \
+  (AT(W, ii, jj, k, 2) * AT(W, ii, jj, k, 5) - AT(W, ii, jj, k, 1) * AT(W, ii, jj, k, 6))
+    if ((lo0 < i) && (lo1 < j)) {
+      EQ = EQAT(i - 1, j - 1);
+      D1_00 = -AT(F, i, j - 1, k, 6) - EQ;
+      D2_00 = AT(G, i - 1, j, k, 5) - EQ;
+      i00 = 1;
+    }
+    if ((hi0 >= i) && (lo1 < j)) {
+      EQ = EQAT(i, j - 1);
+      D1_10 = EQ + AT(F, i, j - 1, k, 6);
+      D2_10 = AT(G, i, j, k, 5) - EQ;
+      i10 = 1;
+    }
+    if ((lo0 < i) && (hi1 >= j)) {
+      EQ = EQAT(i - 1, j);
+      D1_01 = -AT(F, i, j, k, 6) - EQ;
+      D2_01 = EQ - AT(G, i - 1, j, k, 5);
+      i01 = 1;
+    }
+    if ((hi0 >= i) && (hi1 >= j)) {
+      EQ = EQAT(i, j);
+      D1_11 = EQ + AT(F, i, j, k, 6);
+      D2_11 = EQ - AT(G, i, j, k, 5);
+      i11 = 1;
+    }
+#undef EQAT
+    if (lo0 < i) {
+      if (upwind) {
+        int iMN = i00, iPL = i01;
+        const double m = AT(G, i - 1, j, k, 0);
+        if (iMN * m > 0.0) iPL = 0;
+        else if (iPL * m < 0.0) iMN = 0;
+        DEDD = (iPL * D1_01 + iMN * D1_00) / (iPL + iMN);
+      } else {
+        DEDD = (D1_01 + D1_00) / (i01 + i00);
+      }
+      EE = EE + AT(G, i - 1, j, k, 5) + DEDD;
+      iE = iE + 1;
+    }
+    if (hi0 >= i) {
+      if (upwind) {
+        int iMN = i10, iPL = i11;
+        const double m = AT(G, i, j, k, 0);
+        if (iMN * m > 0.0) iPL = 0;
+        else if (iPL * m < 0.0) iMN = 0;
+        DEDD = (iMN * D1_10 + iPL * D1_11) / (iMN + iPL);
+      } else {
+        DEDD = (D1_10 + D1_11) / (i10 + i11);
+      }
+      EE = EE + AT(G, i, j, k, 5) - DEDD;
+      iE = iE + 1;
+    }
+    if (lo1 < j) {
+      if (upwind) {
+        int iMN = i00, iPL = i10;
+        const double m = AT(F, i, j - 1, k, 0);
+        if (iMN * m > 0.0) iPL = 0;
+        else if (iPL * m < 0.0) iMN = 0;
+        DEDD = (iMN * D2_00 + iPL * D2_10) / (iMN + iPL);
+      } else {
+        DEDD = (D2_00 + D2_10) / (i00 + i10);
+      }
+      EE = EE - AT(F, i, j - 1, k, 6) + DEDD;
+      iE = iE + 1;
+    }
+    if (hi1 >= j) {
+      if (upwind) {
+        int iMN = i01, iPL = i11;
+        const double m = AT(F, i, j, k, 0);
+        if (iMN * m > 0.0) iPL = 0;
+        else if (iPL * m < 0.0) iMN = 0;
+        DEDD = (iMN * D2_01 + iPL * D2_11) / (iMN + iPL);
+      } else {
+        DEDD = (D2_01 + D2_11) / (i01 + i11);
+      }
+      EE = EE - AT(F, i, j, k, 6) - DEDD;
+      iE = iE + 1;
+    }
+    AT(EX, i, j, k, 0) = EE / iE;
+  }
+}
+
+/* PatchMHDMF::calculateElectricField (srcIdeal/PatchMHDMF.cpp:1487-1560) */
+static void electric_field(const Ctx* c, const Fab* W, const Fab* Fl, mf_box box, Edges* E) {
+  if (c->ct == 1)
+    electric_field_bs(c, Fl, box, E);
+  else
+    electric_field_gs(c, W, Fl, box, E, c->ct == 3);
+}
+
+/* recalculateB (srcIdeal/DivCleaningF.ChF:4-72) from PatchMHDMF::
+   recalculateMagneticField (srcIdeal/PatchMHDMF.cpp:1461-1484): the cell
+   field from the old one and the circulation of the edge field around the
+   cell, HX = dt/(2 dx); the energy keeps its non-magnetic part.  Bold: any
+   array with the old field at components 5..7 (U or W). */
+static void recalc_b(const Ctx* c, Fab* U, const Fab* Bold, const Edges* E, double dt,
+                     mf_box box) {
+  const double HX = 0.5 * dt / c->p->dx;
+  const Fab *EX = &E->e[0], *EY = &E->e[1], *EZ = &E->e[2];
+  FOR_BOX(box, i, j, k) {
+    double bx = AT(U, i, j, k, 5), by = AT(U, i, j, k, 6), bz = AT(U, i, j, k, 7);
+    double b = D_1_8PI * (bx * bx + by * by + bz * bz);
+    double e = AT(U, i, j, k, 4) - b;
+    const int kk = (c->sd == 3) ? 1 : 0;
+    bx = AT(Bold, i, j, k, 5) - HX * (AT(EZ, i + 1, j + 1, k, 0) + AT(EZ, i, j + 1, k, 0) -
+                                      AT(EZ, i + 1, j, k, 0) - AT(EZ, i, j, k, 0));
+    by = AT(Bold, i, j, k, 6) + HX * (AT(EZ, i + 1, j + 1, k, 0) + AT(EZ, i + 1, j, k, 0) -
+                                      AT(EZ, i, j + 1, k, 0) - AT(EZ, i, j, k, 0));
+    if (kk) {
+      bx = bx + HX * (AT(EY, i + 1, j, k + 1, 0) + AT(EY, i, j, k + 1, 0) -
+                      AT(EY, i + 1, j, k, 0) - AT(EY, i, j, k, 0));
+      by = by - HX * (AT(EX, i, j + 1, k + 1, 0) + AT(EX, i, j, k + 1, 0) -
+                      AT(EX, i, j + 1, k, 0) - AT(EX, i, j, k, 0));
+      bz = AT(Bold, i, j, k, 7) -
+           HX * (AT(EY, i + 1, j, k + 1, 0) + AT(EY, i + 1, j, k, 0) - AT(EY, i, j, k + 1, 0) -
+                 AT(EY, i, j, k, 0) -
+                 (AT(EX, i, j + 1, k + 1, 0) + AT(EX, i, j + 1, k, 0) - AT(EX, i, j, k + 1, 0) -
+                  AT(EX, i, j, k, 0)));
+    }
+    b = D_1_8PI * (bx * bx + by * by + bz * bz);
+    AT(U, i, j, k, 4) = e + b;
+    AT(U, i, j, k, 5) = bx;
+    AT(U, i, j, k, 6) = by;
+    AT(U, i, j, k, 7) = bz;
+  }
+}
+
+/* ------------------------------------------------------------------------ */
 /* EulerStep                                                                 */
 /* ------------------------------------------------------------------------ */
 
 /* PatchMHDAM::EulerStep (src/PatchMHDAM.cpp:495-709) for PatchMHDMF. */
 static int euler_step(const Ctx* c, double time, Fab* U, Fab* F /* [sd] or NULL */, Fab* divBout,
-                      double dt, mf_box a_box) {
+                      double dt, mf_box a_box, Edges* Eout /* nullable */) {
   const mf_params* p = c->p;
   const int sd = c->sd, nc = c->nc, np = c->nprim;
   (void)time;
@@ -2490,6 +2760,17 @@ static int euler_step(const Ctx* c, double time, Fab* U, Fab* F /* [sd] or NULL 
       int iEND = c->irhon + (c->nf - 2) * 5 + 4;
       for (int q = 1; q <= iEND; ++q) AT(U, i, j, k, q) = AT(U, i, j, k, q) + S[q];
     }
+  }
+
+  /* constrained transport: the edge field of the stage's fluxes and the cell
+     field from Uold (src/PatchMHDAM.cpp:684-698) */
+  if (c->ct) {
+    Edges E;
+    edges_alloc(&E, valueBox, sd);
+    electric_field(c, &W, Fl, valueBox, &E);
+    recalc_b(c, U, &Uold, &E, dt, valueBox);
+    if (Eout) edges_copy(Eout, &E);
+    edges_free(&E);
   }
 
   /* problem postprocessing, then positivity (src/PatchMHDAM.cpp:705-707) */
@@ -2704,7 +2985,7 @@ static void prim_fab(const Ctx* c, const Fab* U, mf_box WBoxB, Fab* W) {
    (:836-1000) with dt/2 on box.grow(1), then correctorHancock (:1002-1189)
    with dt on box. */
 static int hancock_step(const Ctx* c, double time, Fab* U, Fab* F, Fab* divBout, double dt,
-                        mf_box a_box) {
+                        mf_box a_box, Edges* Eout) {
   const mf_params* p = c->p;
   const int sd = c->sd, nc = c->nc, np = c->nprim;
   (void)time;
@@ -2808,6 +3089,15 @@ static int hancock_step(const Ctx* c, double time, Fab* U, Fab* F, Fab* divBout,
     level_set_update(c, U, &W, &Fl[d], d, dt, vb2);
   }
   explicit_sources(c, U, &Wpr, Bn, dt, vb2, divBout);
+  /* constrained transport with W(t+dt/2) (src/PatchMHDAM.cpp:1150-1160) */
+  if (c->ct) {
+    Edges E;
+    edges_alloc(&E, vb2, sd);
+    electric_field(c, &Wpr, Fl, vb2, &E);
+    recalc_b(c, U, &Uold, &E, dt, vb2);
+    if (Eout) edges_copy(Eout, &E);
+    edges_free(&E);
+  }
   double u[MF_MAX_COMP];
   FOR_BOX(vb2, i, j, k) {
     for (int q = 0; q < nc; ++q) u[q] = AT(U, i, j, k, q);
@@ -2919,14 +3209,41 @@ static int check_fab(const Ctx* c, const mf_fab* U, const mf_box* valid) {
   return MF_OK;
 }
 
+/* Edges view of caller fabs on the edges of box (E[0..2] in 3D, E[0] in 2D) */
+static int edges_wrap(const Ctx* c, mf_fab* Ef, mf_box box, Edges* E) {
+  Edges want;
+  edges_alloc(&want, box, c->sd);
+  int ok = 1;
+  E->n = want.n;
+  for (int d = 0; d < want.n; ++d) {
+    if (!Ef[d].data || !box_contains(&Ef[d].box, &want.e[d].b)) ok = 0;
+    E->e[d] = fab_wrap(Ef[d].data, Ef[d].box, 1);
+  }
+  if (c->sd == 2) E->e[1] = E->e[2] = E->e[0];
+  edges_free(&want);
+  return ok ? MF_OK : MF_ERR_BAD_ARG;
+}
+
 int mf_oracle_patch_update(const mf_params* p, double time, mf_fab* Uf, const mf_box* valid,
                            double dt, mf_fab* Fout, mf_fab* divBf, double* new_dt,
                            int min_cell[3]) {
+  return mf_oracle_patch_update_e(p, time, Uf, valid, dt, Fout, divBf, NULL, new_dt, min_cell);
+}
+
+int mf_oracle_patch_update_e(const mf_params* p, double time, mf_fab* Uf, const mf_box* valid,
+                             double dt, mf_fab* Fout, mf_fab* divBf, mf_fab* Ef, double* new_dt,
+                             int min_cell[3]) {
   Ctx c;
   int st = ctx_init(&c, p);
   if (st) return st;
   st = check_fab(&c, Uf, valid);
   if (st) return st;
+  Edges Eo, *pE = NULL;
+  if (Ef && c.ct) {
+    st = edges_wrap(&c, Ef, *valid, &Eo);
+    if (st) return st;
+    pE = &Eo;
+  }
   Fab U = fab_wrap(Uf->data, Uf->box, Uf->ncomp);
   Fab divB, *pdivB = NULL;
   if (divBf && divBf->data) {
@@ -2949,9 +3266,18 @@ int mf_oracle_patch_update(const mf_params* p, double time, mf_fab* Uf, const mf
     mf_box bp = box_grow(*valid, 2, c.sd);
     mf_box vbp = box_and_domain(bp, p);
     for (int d = 0; d < c.sd; ++d) Fp[d] = fab_alloc(box_nodes(vbp, d), c.nc);
-    euler_step(&c, time, &Upred, pF ? Fp : NULL, pdivB, dt, bp);
+    Edges Ep; /* EPredictor on the box of the caller's E */
+    if (pE) edges_alloc(&Ep, *valid, c.sd);
+    euler_step(&c, time, &Upred, pF ? Fp : NULL, pdivB, dt, bp, pE ? &Ep : NULL);
     memcpy(U.p, Upred.p, sizeof(double) * (size_t)n);
-    euler_step(&c, time, &U, pF, pdivB, 0.5 * dt, *valid);
+    euler_step(&c, time, &U, pF, pdivB, 0.5 * dt, *valid, pE);
+    if (pE) { /* a_E += EPredictor; a_E *= 0.5 */
+      for (int d = 0; d < pE->n; ++d) FOR_BOX(Ep.e[d].b, i, j, k) {
+          AT(&pE->e[d], i, j, k, 0) = AT(&pE->e[d], i, j, k, 0) + AT(&Ep.e[d], i, j, k, 0);
+          AT(&pE->e[d], i, j, k, 0) = AT(&pE->e[d], i, j, k, 0) * 0.5;
+        }
+      edges_free(&Ep);
+    }
     if (pF) {
       mf_box vb = box_and_domain(*valid, p);
       for (int d = 0; d < c.sd; ++d) {
@@ -2971,9 +3297,9 @@ int mf_oracle_patch_update(const mf_params* p, double time, mf_fab* Uf, const mf
     fab_free(&Uold);
     fab_free(&Upred);
   } else if (p->time_approximation == MF_TA_HANCOCK) {
-    hancock_step(&c, time, &U, pF, pdivB, dt, *valid);
+    hancock_step(&c, time, &U, pF, pdivB, dt, *valid, pE);
   } else {
-    euler_step(&c, time, &U, pF, pdivB, dt, *valid);
+    euler_step(&c, time, &U, pF, pdivB, dt, *valid, pE);
   }
   double ndt;
   int cell[3] = {0, 0, 0};
@@ -2984,6 +3310,24 @@ int mf_oracle_patch_update(const mf_params* p, double time, mf_fab* Uf, const mf
     min_cell[1] = cell[1];
     min_cell[2] = cell[2];
   }
+  return MF_OK;
+}
+
+int mf_oracle_recalculate_b(const mf_params* p, mf_fab* Uf, const mf_fab* Uoldf, mf_fab* Ef,
+                            double dt, const mf_box* box) {
+  Ctx c;
+  int st = ctx_init(&c, p);
+  if (st) return st;
+  if (!c.ct) return MF_ERR_BAD_ARG;
+  if (!Uf || !Uoldf || !Ef || !box || !box_contains(&Uf->box, box) ||
+      !box_contains(&Uoldf->box, box))
+    return MF_ERR_BAD_ARG;
+  Edges E;
+  st = edges_wrap(&c, Ef, *box, &E);
+  if (st) return st;
+  Fab U = fab_wrap(Uf->data, Uf->box, Uf->ncomp);
+  Fab Uo = fab_wrap(Uoldf->data, Uoldf->box, Uoldf->ncomp);
+  recalc_b(&c, &U, &Uo, &E, dt, *box);
   return MF_OK;
 }
 
@@ -3086,10 +3430,56 @@ static int neutral_sun_bc(const mf_params* p, int npatch, mf_fab* Uf, const mf_b
   return MF_OK;
 }
 
+/* per-patch state of constrained transport across a level step: the
+   level's UOld (AMRLevelIdealMHD::preTimeStep, srcIdeal/AMRLevelIdealMHD.cpp:
+   673-681) and the edge field each updateState returns */
+typedef struct {
+  int on;
+  Fab* uold;
+  mf_fab (*ef)[3];
+  Edges* e;
+} CtLevel;
+
+static int ct_level_init(CtLevel* L, const mf_params* p, int npatch, const mf_box* valid) {
+  Ctx c;
+  memset(L, 0, sizeof(*L));
+  int st = ctx_init(&c, p);
+  if (st) return st;
+  if (!c.ct) return MF_OK;
+  L->on = 1;
+  L->uold = (Fab*)calloc((size_t)npatch, sizeof(Fab));
+  L->ef = (mf_fab(*)[3])calloc((size_t)npatch, sizeof(mf_fab[3]));
+  L->e = (Edges*)calloc((size_t)npatch, sizeof(Edges));
+  for (int ip = 0; ip < npatch; ++ip) {
+    edges_alloc(&L->e[ip], valid[ip], c.sd);
+    for (int d = 0; d < 3; ++d) {
+      const Fab* f = &L->e[ip].e[d < L->e[ip].n ? d : 0];
+      L->ef[ip][d].data = f->p;
+      L->ef[ip][d].box = f->b;
+      L->ef[ip][d].ncomp = 1;
+    }
+  }
+  return MF_OK;
+}
+
+static void ct_level_free(CtLevel* L, int npatch) {
+  for (int ip = 0; ip < npatch; ++ip) {
+    edges_free(&L->e[ip]);
+    fab_free(&L->uold[ip]);
+  }
+  free(L->uold);
+  free(L->ef);
+  free(L->e);
+  memset(L, 0, sizeof(*L));
+}
+
 int mf_oracle_level_step(const mf_params* p, double time, int npatch, mf_fab* Uf,
                          const mf_box* valid, double dt, int nthreads, double* new_dt,
                          int* min_patch, int min_cell[3]) {
   int st = mf_oracle_level_exchange(p, npatch, Uf, valid);
+  if (st) return st;
+  CtLevel ct;
+  st = ct_level_init(&ct, p, npatch, valid);
   if (st) return st;
   double* dts = (double*)malloc(sizeof(double) * (size_t)npatch);
   int* cells = (int*)malloc(sizeof(int) * 3 * (size_t)npatch);
@@ -3100,11 +3490,31 @@ int mf_oracle_level_step(const mf_params* p, double time, int npatch, mf_fab* Uf
 #else
   (void)nthreads;
 #endif
-  for (int ip = 0; ip < npatch; ++ip)
-    sts[ip] = mf_oracle_patch_update(p, time, &Uf[ip], &valid[ip], dt, NULL, NULL, &dts[ip],
-                                     &cells[3 * ip]);
+  for (int ip = 0; ip < npatch; ++ip) {
+    mf_fab* Ep = NULL;
+    if (ct.on) {
+      ct.uold[ip] = fab_alloc(Uf[ip].box, Uf[ip].ncomp);
+      memcpy(ct.uold[ip].p, Uf[ip].data, sizeof(double) * (size_t)(ct.uold[ip].csz * Uf[ip].ncomp));
+      Ep = ct.ef[ip];
+    }
+    sts[ip] = mf_oracle_patch_update_e(p, time, &Uf[ip], &valid[ip], dt, NULL, NULL, Ep, &dts[ip],
+                                       &cells[3 * ip]);
+  }
   int best = -1;
   if (st == MF_OK) st = neutral_sun_bc(p, npatch, Uf, valid);
+  /* AMRLevelIdealMHD::postTimeStep with constrained transport on a single
+     level (srcIdeal/AMRLevelIdealMHD.cpp:1649-1688): every patch's field
+     again from the level's UOld and the patch's step-averaged edge field */
+  if (ct.on) {
+    for (int ip = 0; ip < npatch; ++ip) {
+      if (st == MF_OK && sts[ip] == MF_OK) {
+        mf_fab uo = {ct.uold[ip].p, Uf[ip].box, Uf[ip].ncomp};
+        int r = mf_oracle_recalculate_b(p, &Uf[ip], &uo, ct.ef[ip], dt, &valid[ip]);
+        if (r) st = r;
+      }
+    }
+    ct_level_free(&ct, npatch);
+  }
   for (int ip = 0; ip < npatch; ++ip) {
     if (sts[ip]) st = sts[ip];
     if (best < 0 || dts[ip] < dts[best]) best = ip;
@@ -3723,6 +4133,10 @@ static int hier_time_step(Hier* H, int l) {
 
 int mf_oracle_hier_step(int nlev, const mf_oracle_level* lev, const int* ratio, double* time,
                         double dt0, int nthreads, double* new_dt, double* dedner) {
+  /* constrained transport across levels (edge registers, averageToCoarse of
+     the accumulated edge field) is not restated */
+  for (int l = 0; l < nlev; ++l)
+    if (lev[l].p->divb_cleaning >= 1 && lev[l].p->divb_cleaning <= 3) return MF_ERR_UNSUPPORTED;
   if (nlev < 1 || !lev || (nlev > 1 && !ratio) || !time || !(dt0 > 0.0)) return MF_ERR_BAD_ARG;
   Hier H;
   memset(&H, 0, sizeof(H));

@@ -20,6 +20,14 @@ extern "C" {
 #endif
 
 /* PatchMHDAM::updateState (src/PatchMHDAM.cpp:1192-1317) on one host patch. */
+/* updateState with the edge field output of constrained transport: E = the
+   EdgeBox on valid (3 fabs in 3D, 1 nodal fab in 2D; NULL = not wanted) */
+int mf_oracle_patch_update_e(const mf_params* p, double time, mf_fab* U, const mf_box* valid,
+                             double dt, mf_fab* F, mf_fab* divB, mf_fab* E, double* new_dt,
+                             int min_cell[3]);
+/* PatchMHDMF::recalculateMagneticField (srcIdeal/PatchMHDMF.cpp:1461-1484) */
+int mf_oracle_recalculate_b(const mf_params* p, mf_fab* U, const mf_fab* Uold, mf_fab* E,
+                            double dt, const mf_box* box);
 int mf_oracle_patch_update(const mf_params* p, double time, mf_fab* U, const mf_box* valid,
                            double dt, mf_fab* F, mf_fab* divB, double* new_dt, int min_cell[3]);
 

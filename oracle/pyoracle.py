@@ -49,6 +49,12 @@ def load():
         "mf_oracle_patch_update": (ctypes.c_int, [_P(MfParams), ctypes.c_double, _P(MfFab),
                                                   _P(MfBox), ctypes.c_double, ctypes.c_void_p,
                                                   ctypes.c_void_p, _DP, ctypes.c_int * 3]),
+        "mf_oracle_patch_update_e": (ctypes.c_int, [_P(MfParams), ctypes.c_double, _P(MfFab),
+                                                    _P(MfBox), ctypes.c_double, ctypes.c_void_p,
+                                                    ctypes.c_void_p, ctypes.c_void_p, _DP,
+                                                    ctypes.c_int * 3]),
+        "mf_oracle_recalculate_b": (ctypes.c_int, [_P(MfParams), _P(MfFab), _P(MfFab),
+                                                   ctypes.c_void_p, ctypes.c_double, _P(MfBox)]),
         "mf_oracle_compute_dt": (ctypes.c_int, [_P(MfParams), _P(MfFab), _P(MfBox), _DP,
                                                 ctypes.c_int * 3]),
         "mf_oracle_level_exchange": (ctypes.c_int, [_P(MfParams), ctypes.c_int, _P(MfFab),
@@ -89,10 +95,51 @@ def _dp(a: np.ndarray):
     return a.ctypes.data_as(_DP)
 
 
+def _edge_fabs(E, keep):
+    """E: list of (array, lo, hi), one per edge direction (1 in 2D)."""
+    if E is None:
+        return None
+    arr = (MfFab * 3)()
+    for d in range(3):
+        a, lo, hi = E[min(d, len(E) - 1)]
+        arr[d] = MfFab(a.ctypes.data, make_box(lo, hi), 1)
+    keep.append(arr)
+    return ctypes.cast(arr, ctypes.c_void_p)
+
+
+def edge_boxes(lo, hi, sd):
+    """Boxes of the EdgeBox on the cell box [lo, hi]: in 3D the nodal box made
+    cell-centred along each direction, in 2D the nodal box."""
+    nlo, nhi = list(lo), list(hi)
+    for d in range(sd):
+        nhi[d] += 1
+    if sd == 2:
+        return [(nlo, nhi)]
+    out = []
+    for d in range(3):
+        h = list(nhi)
+        h[d] -= 1
+        out.append((list(nlo), h))
+    return out
+
+
+def recalculate_b(p: MfParams, U, Uold, fab_lo, fab_hi, E, dt, lo, hi):
+    """PatchMHDMF::recalculateMagneticField on host fabs (U in place)."""
+    lib = load()
+    keep = []
+    fu = MfFab(U.ctypes.data, make_box(fab_lo, fab_hi), U.shape[0])
+    fo = MfFab(Uold.ctypes.data, make_box(fab_lo, fab_hi), Uold.shape[0])
+    ep = _edge_fabs(E, keep)
+    box = make_box(lo, hi)
+    return lib.mf_oracle_recalculate_b(ctypes.byref(p), ctypes.byref(fu), ctypes.byref(fo), ep,
+                                       dt, ctypes.byref(box))
+
+
 def patch_update(p: MfParams, U: np.ndarray, fab_lo, fab_hi, valid_lo, valid_hi, dt,
-                 F=None, divB=None, time=0.0):
+                 F=None, divB=None, time=0.0, E=None):
     """updateState on a host fab (modified in place). F: list of
-    (array, lo, hi) per direction; divB: (array, lo, hi)."""
+    (array, lo, hi) per direction; divB: (array, lo, hi); E: the edge field
+    of constrained transport, list of (array, lo, hi) on edge_boxes(valid)."""
     lib = load()
     assert U.dtype == np.float64 and U.flags.c_contiguous
     nc = U.shape[0]
@@ -114,8 +161,10 @@ def patch_update(p: MfParams, U: np.ndarray, fab_lo, fab_hi, valid_lo, valid_hi,
         dptr = ctypes.cast(ctypes.pointer(dfab), ctypes.c_void_p)
     ndt = ctypes.c_double()
     cell = (ctypes.c_int * 3)()
-    st = lib.mf_oracle_patch_update(ctypes.byref(p), time, ctypes.byref(fab),
-                                    ctypes.byref(valid), dt, fptr, dptr, ctypes.byref(ndt), cell)
+    eptr = _edge_fabs(E, keep)
+    st = lib.mf_oracle_patch_update_e(ctypes.byref(p), time, ctypes.byref(fab),
+                                      ctypes.byref(valid), dt, fptr, dptr, eptr,
+                                      ctypes.byref(ndt), cell)
     return st, ndt.value, tuple(cell)
 
 
