@@ -20,8 +20,11 @@
  *   mf_set_current_time        PatchMHDAM::setCurrentTime (src/PatchMHDAM.cpp:272-276)
  *   mf_set_dedner              EqSysMHDMF::setCorrectionPotential -> SETDEDNERCONST
  *                              (src/DednerF.ChF:4-13)
- *   mf_patch_update            PatchMHDAM::updateState (src/PatchMHDAM.H:252-260,
- *                              src/PatchMHDAM.cpp:1192-1317)
+ *   mf_patch_update(_e)        PatchMHDAM::updateState (src/PatchMHDAM.H:252-260,
+ *                              src/PatchMHDAM.cpp:1192-1317); _e with its EdgeBox E
+ *   mf_recalculate_magnetic_field
+ *                              PatchMHDMF::recalculateMagneticField
+ *                              (srcIdeal/PatchMHDMF.cpp:1461-1484)
  *   mf_compute_dt              PatchMHDMF::computeDt (srcIdeal/PatchMHDMF.cpp:66-146)
  *   mf_level_*                 AMRLevelIdealMHD::advance/step over all patches of a
  *                              level: ghost exchange (srcIdeal/AMRLevelIdealMHD.cpp:772),

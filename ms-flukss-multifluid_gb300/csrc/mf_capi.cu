@@ -6,7 +6,8 @@
 // allocation and replace the redundant stage-1 ghost computation by a
 // device-side exchange of the stage-1 state between the two stages; both give
 // the same results because every stage-1 ghost value equals the value its
-// owner patch computes for that cell.
+// owner patch computes for that cell (with constrained transport it does not:
+// there every patch runs stage 1 on box.grow(2) and no exchange follows).
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -1016,9 +1017,16 @@ static void add_regions(const mf::LevelPlan& L, const mf_params& p, PatchIndex& 
 // the domain), stage 1 computes it, as the reference does by running stage 1
 // on box.grow(2) (src/PatchMHDAM.cpp:1238-1246).  Cells outside a
 // non-periodic domain side are never computed (ProblemDomain clipping).
+static bool ct_on(const mf_params& p) { return p.divb_cleaning >= 1 && p.divb_cleaning <= 3; }
+
 static mf_box stage1_box(const mf::LevelPlan& L, const mf_params& p, PatchIndex& ix, int i) {
   const int sd = p.space_dim;
   const mf_box& v = L.valid[i];
+  // Constrained transport: a stage's edge field is one-sided on its valueBox
+  // boundary, so a stage-1 ghost value depends on the patch that computes it;
+  // every patch runs stage 1 on box.grow(2), as the reference does, and no
+  // exchange follows.
+  if (ct_on(p)) return box_and_domain(box_grow(v, 2, sd), p);
   const auto shifts = periodic_shifts(p);
   mf_box g = v;
   for (int d = 0; d < sd; ++d)
@@ -1139,7 +1147,7 @@ mf_status build_level_plan(const mf_params& p, int ng, int nc, int npatch, const
   }
   L.fvsize = fvo;
   add_regions(L, p, ix, ng, L.full);
-  if (rk2) add_regions(L, p, ix, 2, L.two);
+  if (rk2 && !ct_on(p)) add_regions(L, p, ix, 2, L.two);
   if (p.neutral_sun_bc && p.n_fluids > 1 && sd == 3) {
     // HeliosphericProblem::define (swlism/HeliosphericProblem.cpp:476-527):
     // the sun on a grid node, strips of iR0 planes on either side of it

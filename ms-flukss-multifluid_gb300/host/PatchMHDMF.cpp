@@ -110,6 +110,18 @@ void PatchMHDMF::updateState(mf_fab& U, mf_fab* F, double& newDt, int minDtCell[
      "PatchMHDMF::updateState");
 }
 
+void PatchMHDMF::updateState(mf_fab& U, mf_fab* F, mf_fab* E, double& newDt, int minDtCell[3],
+                             mf_fab* divB, double dt, const mf_box& box, void* stream) {
+  ok(mf_patch_update_e(context(), &U, &box, dt, F, divB, E, &newDt, minDtCell, stream),
+     "PatchMHDMF::updateState");
+}
+
+void PatchMHDMF::recalculateMagneticField(mf_fab& U, const mf_fab& Uold, const mf_fab* E,
+                                          double dt, const mf_box& box, void* stream) {
+  ok(mf_recalculate_magnetic_field(context(), &U, &Uold, E, dt, &box, stream),
+     "PatchMHDMF::recalculateMagneticField");
+}
+
 double PatchMHDMF::computeDt(const mf_fab& U, const mf_box& box, int minDtCell[3],
                              void* stream) {
   double dt = 0.0;

@@ -60,6 +60,13 @@ class PatchMHDMF {
   // the fluxes; divB (nullable) the divergence of B on the box.
   void updateState(mf_fab& U, mf_fab* F, double& newDt, int minDtCell[3], mf_fab* divB,
                    double dt, const mf_box& box, void* stream = nullptr);
+  // The same with updateState's EdgeBox E (constrained transport: the step's
+  // edge field as EdgeBox fabs on box, 3 in 3D, 1 nodal in 2D; may be null).
+  void updateState(mf_fab& U, mf_fab* F, mf_fab* E, double& newDt, int minDtCell[3],
+                   mf_fab* divB, double dt, const mf_box& box, void* stream = nullptr);
+  // PatchMHDMF::recalculateMagneticField (srcIdeal/PatchMHDMF.cpp:1461-1484)
+  void recalculateMagneticField(mf_fab& U, const mf_fab& Uold, const mf_fab* E, double dt,
+                                const mf_box& box, void* stream = nullptr);
   // PatchMHDMF::computeDt (srcIdeal/PatchMHDMF.cpp:66-146)
   double computeDt(const mf_fab& U, const mf_box& box, int minDtCell[3],
                    void* stream = nullptr);
