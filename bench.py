@@ -278,22 +278,26 @@ def run_ours(a):
     achieved = alg / (dom_avg_ms * 1e-3) / 1e9
     traffic = _traffic_table().get(f"fp64_{dom}") if n == N_DEFAULT else None
 
-    # end to end through the C ABI with host buffers: H2D of the level state,
-    # one step (mf_level_step returns the new dt on the host), D2H of the state
+    # end to end through the C ABI with host buffers: H2D of the level's valid
+    # state (pinned, packed without ghosts), one step (mf_level_step fills the
+    # ghosts by its exchange and returns the new dt on the host), D2H of the
+    # valid state
     e2e_steps = max(1, a.e2e_steps)
-    nbytes = lev.ndoubles * 8
+    vhost = torch.empty(lev.valid_doubles(), dtype=torch.float64, pin_memory=True)
+    nbytes = vhost.numel() * 8
     dt_e = CFL * dt_min
     lev.upload(host.data_ptr(), stream.cuda_stream)
+    lev.download_valid(vhost.data_ptr(), stream.cuda_stream)
     torch.cuda.synchronize()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     t0 = time.perf_counter()
     e0.record(stream)
     for _ in range(e2e_steps):
-        lev.upload(host.data_ptr(), stream.cuda_stream)
+        lev.upload_valid(vhost.data_ptr(), stream.cuda_stream)
         st, ndt, _, _ = lev.step(dt_e, stream.cuda_stream)
         mfgpu.check(st, "e2e step")
-        lev.download(host.data_ptr(), stream.cuda_stream)
+        lev.download_valid(vhost.data_ptr(), stream.cuda_stream)
         dt_e = CFL * ndt
     e1.record(stream)
     torch.cuda.synchronize()
@@ -424,7 +428,8 @@ def run_ours(a):
                    "parallelism": f"{ws} independent replica(s), one per GPU"},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": nbytes,
                 "d2h_bytes_per_step": nbytes, "steps": e2e_steps,
-                "path": "mf_level_upload (pinned host) + mf_level_step + mf_level_download"},
+                "path": "mf_level_upload_valid (pinned host, valid cells) + mf_level_step + "
+                        "mf_level_download_valid"},
         "gpu_launches": launches * a.steps,
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,

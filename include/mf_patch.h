@@ -299,6 +299,17 @@ long long mf_level_num_cells(const mf_level* lev);
 /* Copy the whole level state host -> device / device -> host (layout as on the device). */
 mf_status mf_level_upload(mf_level* lev, const double* host, void* stream);
 mf_status mf_level_download(const mf_level* lev, double* host, void* stream);
+/* The valid cells only, packed on the host: patch p's valid box at
+   mf_level_valid_offset(p) doubles, component-major, x fastest (a LevelData
+   without ghosts).  One host copy through a device staging buffer (allocated
+   at the first call) and a scatter / gather kernel.  Ghost cells are not
+   transferred: the level step fills them by its exchange; those outside a
+   non-periodic domain keep what the last full upload placed there (zero on a
+   new level). */
+long long mf_level_valid_doubles(const mf_level* lev);
+long long mf_level_valid_offset(const mf_level* lev, int patch);
+mf_status mf_level_upload_valid(mf_level* lev, const double* host, void* stream);
+mf_status mf_level_download_valid(mf_level* lev, double* host, void* stream);
 /* Fill ghost cells of every patch from the valid cells of its neighbours
    (periodic images included); LevelData::exchange. */
 mf_status mf_level_exchange(mf_level* lev, void* stream);

@@ -358,6 +358,8 @@ struct mf_level {
   DevBuf sun;                              // NEUTRALS_SUNBC cell pairs
   int nsun = 0;
   DevBuf ct_u0, ct_e1, ct_e2, ct_eo;       // constrained transport: UOld, edge fields
+  DevBuf packed;                           // staging of the valid-cell transfers
+  std::vector<long long> voff;             // packed offset of each patch (doubles)
 };
 
 extern "C" {
@@ -1546,6 +1548,57 @@ long long mf_level_num_cells(const mf_level* L) { return L ? L->cells : -1; }
 long long mf_level_patch_offset(const mf_level* L, int p) {
   if (!L || p < 0 || p >= L->np) return -1;
   return L->off[p];
+}
+
+// Packed valid-cell offsets: nc x the patch's first cell in the order of the
+// stage descs (patch order, valid boxes back to back), as k_pack indexes them.
+static void level_voff(mf_level* L) {
+  if ((int)L->voff.size() == L->np + 1) return;
+  L->voff.assign(L->np + 1, 0);
+  for (int i = 0; i < L->np; ++i)
+    L->voff[i + 1] = L->voff[i] + box_cells(L->valid[i]) * L->ctx->nc;
+}
+
+long long mf_level_valid_doubles(const mf_level* L) {
+  if (!L) return -1;
+  level_voff(const_cast<mf_level*>(L));
+  return L->voff[L->np];
+}
+
+long long mf_level_valid_offset(const mf_level* L, int p) {
+  if (!L || p < 0 || p >= L->np) return -1;
+  level_voff(const_cast<mf_level*>(L));
+  return L->voff[p];
+}
+
+static mf_status level_pack(mf_level* L, double* host, int to_fab, void* stream) {
+  level_voff(L);
+  const long long n = L->voff[L->np];
+  MF_CHECK_CUDA(L->packed.ensure(sizeof(double) * (size_t)std::max<long long>(n, 1)));
+  cudaStream_t us = (cudaStream_t)stream;
+  mf_status st = join_streams(us, L->s);
+  if (st != MF_OK) return st;
+  double* dp = (double*)L->packed.p;
+  if (to_fab) {
+    MF_CHECK_CUDA(cudaMemcpyAsync(dp, host, sizeof(double) * n, cudaMemcpyHostToDevice, L->s));
+    MF_CHECK_CUDA(mf::launch_pack((double*)L->U.p, dp, L->b2, L->ctx->nc, 1, L->s));
+  } else {
+    MF_CHECK_CUDA(mf::launch_pack((double*)L->U.p, dp, L->b2, L->ctx->nc, 0, L->s));
+    MF_CHECK_CUDA(cudaMemcpyAsync(host, dp, sizeof(double) * n, cudaMemcpyDeviceToHost, L->s));
+  }
+  st = join_streams(L->s, us);
+  if (st != MF_OK) return st;
+  return wait_stream(L->s, L->ctx->timeout);
+}
+
+mf_status mf_level_upload_valid(mf_level* L, const double* host, void* stream) {
+  if (!L || !host) return MF_ERR_BAD_ARG;
+  return level_pack(L, const_cast<double*>(host), 1, stream);
+}
+
+mf_status mf_level_download_valid(mf_level* L, double* host, void* stream) {
+  if (!L || !host) return MF_ERR_BAD_ARG;
+  return level_pack(L, host, 0, stream);
 }
 
 mf_status mf_level_patch_fab(const mf_level* L, int p, mf_fab* out) {

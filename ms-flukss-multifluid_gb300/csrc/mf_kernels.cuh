@@ -226,6 +226,12 @@ cudaError_t launch_finalize(const DevParams& P, const DtPartial* partials, const
 
 cudaError_t launch_exchange(double* u, const CopyReg* regs, int nreg, int nc, cudaStream_t s);
 
+// The valid cells of the descs of b (valueBox = valid box, one run) between
+// the fab layout u and the packed layout (nc x the desc's first valid cell,
+// component-major): to_fab = 1 scatters packed into u, 0 gathers.
+cudaError_t launch_pack(double* u, double* packed, const Batch& b, int nc, int to_fab,
+                        cudaStream_t s);
+
 // Fout[d] = average of the two stages' face fluxes (or the single stage's)
 // on the faces of the valid box.
 cudaError_t launch_flux_out(int mixed, int sd, int nc, const void* const f2[3],

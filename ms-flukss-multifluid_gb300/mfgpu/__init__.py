@@ -173,6 +173,11 @@ _SIGS = {
     "mf_level_patch_fab": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _P(MfFab)]),
     "mf_level_upload": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "mf_level_download": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "mf_level_valid_doubles": (ctypes.c_longlong, [ctypes.c_void_p]),
+    "mf_level_valid_offset": (ctypes.c_longlong, [ctypes.c_void_p, ctypes.c_int]),
+    "mf_level_upload_valid": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "mf_level_download_valid": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p,
+                                               ctypes.c_void_p]),
     "mf_level_exchange": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "mf_level_compute_dt": (ctypes.c_int, [ctypes.c_void_p, _P(ctypes.c_double),
                                            _P(ctypes.c_int), c_int3, ctypes.c_void_p]),
@@ -649,6 +654,24 @@ class Level:
 
     def download(self, host_ptr, stream=None):
         check(self.lib.mf_level_download(self.h, host_ptr, stream), "mf_level_download")
+
+    def valid_doubles(self) -> int:
+        """Doubles of the packed valid state (no ghosts)."""
+        return self.lib.mf_level_valid_doubles(self.h)
+
+    def valid_view(self, packed: np.ndarray, i: int) -> np.ndarray:
+        """numpy view (nc, nz, ny, nx) of patch i's valid box in a packed buffer."""
+        lo, hi = self.boxes[i]
+        shp = fab_shape(lo, hi, self.ctx.nc)
+        o = self.lib.mf_level_valid_offset(self.h, i)
+        return packed[o:o + int(np.prod(shp))].reshape(shp)
+
+    def upload_valid(self, host_ptr, stream=None):
+        check(self.lib.mf_level_upload_valid(self.h, host_ptr, stream), "mf_level_upload_valid")
+
+    def download_valid(self, host_ptr, stream=None):
+        check(self.lib.mf_level_download_valid(self.h, host_ptr, stream),
+              "mf_level_download_valid")
 
     def compute_dt(self):
         dt = ctypes.c_double()
