@@ -437,7 +437,13 @@ def run_ours(a):
                      "algorithmic_bytes_per_launch": alg, "avg_launch_ms": dom_avg_ms,
                      "step_hbm_frac": (value * 16 * nc / 1e9) / peak,
                      "per_kind_ms": {k: v[0] for k, v in by_kind.items()},
-                     "profiled_step_ms": step_ms_prof},
+                     "profiled_step_ms": step_ms_prof,
+                     # the bound that binds: the FP64 pipe (2 FP64 instructions per SM per
+                     # clock on GB300), measured by ncu on this kernel (committed profile)
+                     "fp64_pipe_active": _traffic_table().get(f"fp64_pipe_active_{dom}")
+                     if n == N_DEFAULT else None,
+                     "fp64_pipe_source": "ncu sm__pipe_fp64_cycles_active, "
+                                         "profiles/ncu_flux_update_helio64_fp64.md"},
         "clocks": clocks,
     }
     if fast is not None:
