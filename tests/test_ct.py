@@ -345,3 +345,48 @@ def test_ct_refused_where_not_built(gpulib):
                                            None, None, ctypes.byref(ndt), cell, None) == \
         mfgpu.MF_ERR_UNSUPPORTED
     ctx.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("ta", [mfgpu.TA_RK2, mfgpu.TA_HANCOCK])
+def test_gpu_helio_ct_with_region_tracer_vs_oracle(gpulib, oracle, ta):
+    """Constrained transport in the full heliosphere problem: far-field ghosts,
+    three neutral fluids with charge exchange, the inner-sphere reset, the
+    neutral pass-through at the sun and the region tracer, level steps of
+    32^3 in 8 patches against the oracle (each step from the oracle's state)."""
+    n = 32
+    p = mfgpu.helio_params(n, time_approximation=ta, region_tracer=True)
+    p.divb_cleaning = 1
+    p.use_8wave = 0
+    boxes = mfgpu.tile_boxes(n, 16, 3)
+    ng = mfgpu.num_ghost(p)
+    arrays, fboxes = [], []
+    for lo, hi in boxes:
+        flo, fhi = mfgpu.grow(lo, hi, ng, 3)
+        arrays.append(np.ascontiguousarray(mfgpu.init_host_fab(p, flo, fhi, "helio")))
+        fboxes.append((flo, fhi))
+    ctx = mfgpu.Context(p)
+    lev = mfgpu.Level(ctx, boxes)
+    flat = np.zeros(lev.ndoubles)
+    for i, a in enumerate(arrays):
+        lev.patch_view(flat, i)[:] = a
+    lev.upload(flat.ctypes.data)
+    dt = 0.4 * lev.compute_dt()[0]
+    for step in range(2):
+        st, ndt_o, _, _ = oracle.level_step(p, arrays, fboxes, boxes, dt)
+        assert st == 0
+        st, ndt_g, _, _ = lev.step(dt)
+        assert st == 0
+        out = np.zeros(lev.ndoubles)
+        lev.download(out.ctypes.data)
+        for i in range(len(boxes)):
+            e = rel_err(valid_view(lev.patch_view(out, i), ng, 3), valid_view(arrays[i], ng, 3),
+                        nls=1)
+            assert np.all(e <= RTOL), (step, i, e)
+        assert abs(ndt_g - ndt_o) <= RTOL * ndt_o
+        for i in range(len(boxes)):
+            lev.patch_view(flat, i)[:] = arrays[i]
+        lev.upload(flat.ctypes.data)
+        dt = 0.4 * ndt_o
+    lev.close()
+    ctx.close()
