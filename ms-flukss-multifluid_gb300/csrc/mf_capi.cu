@@ -703,7 +703,8 @@ static mf_status patch_update_impl(mf_ctx* c, mf_fab* U, const mf_box* valid, do
     MF_CHECK_CUDA(mf::launch_stage(c->dp, p.precision, B, b1, 0, 1.0, ds, parts, &nb, s));
     if (ct) {
       MF_CHECK_CUDA(mf::launch_efield(c->dp, mixed, B.f, B.w, e1, nullptr, nullptr, b1, s));
-      MF_CHECK_CUDA(mf::launch_recalc_b(c->dp, B.uout, B.w, e1, nullptr, nullptr, ds, 1.0, b1, s));
+      MF_CHECK_CUDA(
+          mf::launch_recalc_b(c->dp, B.uout, B.w, e1, nullptr, nullptr, ds, 1.0, 1, b1, s));
     }
     B.uin = (double*)c->pred.p;
     B.uout = U->data;
@@ -726,7 +727,7 @@ static mf_status patch_update_impl(mf_ctx* c, mf_fab* U, const mf_box* valid, do
       MF_CHECK_CUDA(mf::launch_efield(c->dp, mixed, B.f, B.w, e2, e1, (double*)c->ct_eo.p, b2,
                                       s));
       MF_CHECK_CUDA(mf::launch_recalc_b(c->dp, U->data, B.w, e2, (const double*)c->ct_u0.p,
-                                        (const double*)c->pred.p, ds, 0.5, b2, s));
+                                        (const double*)c->pred.p, ds, 0.5, 1, b2, s));
       MF_CHECK_CUDA(mf::launch_dt(c->dp, U->data, b2, parts, &nb, s));
     }
   } else if (hk) {
@@ -750,7 +751,8 @@ static mf_status patch_update_impl(mf_ctx* c, mf_fab* U, const mf_box* valid, do
                                      ct ? 0 : mf::kStageDt));
     if (ct) {  // the corrector's field: W(t+dt/2) for the edges, B from W(t)
       MF_CHECK_CUDA(mf::launch_efield(c->dp, mixed, B.f, H.w2, e2, nullptr, nullptr, b2, s));
-      MF_CHECK_CUDA(mf::launch_recalc_b(c->dp, U->data, B.w, e2, nullptr, nullptr, ds, 1.0, b2, s));
+      MF_CHECK_CUDA(
+          mf::launch_recalc_b(c->dp, U->data, B.w, e2, nullptr, nullptr, ds, 1.0, 1, b2, s));
       MF_CHECK_CUDA(mf::launch_dt(c->dp, U->data, b2, parts, &nb, s));
     }
   } else {
@@ -771,7 +773,8 @@ static mf_status patch_update_impl(mf_ctx* c, mf_fab* U, const mf_box* valid, do
                                    parts, &nb, s));
     if (ct) {
       MF_CHECK_CUDA(mf::launch_efield(c->dp, mixed, B.f, B.w, e2, nullptr, nullptr, b2, s));
-      MF_CHECK_CUDA(mf::launch_recalc_b(c->dp, U->data, B.w, e2, nullptr, nullptr, ds, 1.0, b2, s));
+      MF_CHECK_CUDA(
+          mf::launch_recalc_b(c->dp, U->data, B.w, e2, nullptr, nullptr, ds, 1.0, 1, b2, s));
       MF_CHECK_CUDA(mf::launch_dt(c->dp, U->data, b2, parts, &nb, s));
     }
   }
@@ -1254,7 +1257,7 @@ static mf_status enqueue_level_step(mf_level* L, int advance, cudaEvent_t* ev = 
                       double scale) -> mf_status {
     MF_CHECK_CUDA(mf::launch_efield(c->dp, mixed, B.f, wedge, e, ep, eavg, b, s));
     mark(7);
-    MF_CHECK_CUDA(mf::launch_recalc_b(c->dp, u, B.w, e, a0, a1, ds, scale, b, s));
+    MF_CHECK_CUDA(mf::launch_recalc_b(c->dp, u, B.w, e, a0, a1, ds, scale, 1, b, s));
     mark(7);
     return MF_OK;
   };
@@ -1351,7 +1354,7 @@ static mf_status enqueue_level_step(mf_level* L, int advance, cudaEvent_t* ev = 
   if (ct) {  // the level's recalculation with the step's dt (scale 1)
     const double* eo = (p.time_approximation == MF_TA_RK2) ? (const double*)L->ct_eo.p : e2;
     MF_CHECK_CUDA(mf::launch_recalc_b(c->dp, (double*)L->U.p, u0, eo, nullptr, nullptr, ds, 1.0,
-                                      L->b2, s));
+                                      0, L->b2, s));
     mark(7);
   }
   if (nev) *nev = ne;

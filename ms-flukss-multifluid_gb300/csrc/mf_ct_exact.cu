@@ -25,6 +25,7 @@
 // 5-12, 63-73) is component 0.
 #include "mf_internal.h"
 #include "mf_kernels.cuh"
+#include "mf_sources_exact.cuh"
 
 namespace mf {
 namespace {
@@ -283,8 +284,14 @@ __device__ __forceinline__ void recalc_cell(int sd, double HX, const UAt& u, con
 
 // Per cell of each desc's valueBox: recalculateB from Bold (components 5..7
 // laid out like U: the stage-start primitive state or the level's UOld) and
-// the internal edge field; then, with U0 / U1 set, AVERAGESTATE
-// U += (U0 - U1) / 2 over every component (the second RK2 stage).
+// the internal edge field.  POST: a stage's recalculation, followed as in
+// EulerStep / correctorHancock (src/PatchMHDAM.cpp:684-707, 1150-1166) by the
+// inner-sphere reset and the positivity fix, and with U0 / U1 set by the
+// AVERAGESTATE of the second RK2 stage, U += (U0 - U1) / 2 over every
+// component.  Without POST: the level's recalculation alone
+// (AMRLevelIdealMHD::postTimeStep).  Constrained transport excludes GLM, so
+// the neutral fluids start at component 8.
+template <int POST>
 __global__ void __launch_bounds__(kMaxBlock)
     k_recalc_b(const DevParams P, double* __restrict__ U, const double* __restrict__ Bold,
                const double* __restrict__ E, const double* __restrict__ U0,
@@ -303,24 +310,36 @@ __global__ void __launch_bounds__(kMaxBlock)
   const long long base = D.u_off + c;
   const long long eb = D.u_off / P.nc * 3 + c;
   const long long sy = ct_stride(D.fn, 1), sz = ct_stride(D.fn, 2);
+  const RunParams& RP = runs[D.run];
   const double dt = states[D.run].dt * dt_scale;
-  const double HX = 0.5 * dt / runs[D.run].dx;
+  const double HX = 0.5 * dt / RP.dx;
+  double u[MF_MAX_COMP];
+#pragma unroll
+  for (int q = 0; q < MF_MAX_COMP; ++q)
+    if (q < P.nc) u[q] = U[base + q * cs];
   struct {
     double* p;
-    long long cs;
-    __device__ double operator()(int q) const { return p[q * cs]; }
-    __device__ void set(int q, double v) const { p[q * cs] = v; }
-  } u{U + base, cs};
+    __device__ double operator()(int q) const { return p[q]; }
+    __device__ void set(int q, double v) const { p[q] = v; }
+  } ua{u};
   auto bo = [&](int q) { return Bold[base + q * cs]; };
   const int sd = P.sd;
   auto ea = [&](int d, int di, int dj, int dk) {
     return E[eb + (sd == 3 ? d : 0) * cs + di + dj * sy + dk * sz];
   };
-  recalc_cell(P.sd, HX, u, bo, ea);
-  if (U0) {
-    for (int q = 0; q < P.nc; ++q)
-      U[base + q * cs] = U[base + q * cs] + 0.5 * (U0[base + q * cs] - U1[base + q * cs]);
+  recalc_cell(P.sd, HX, ua, bo, ea);
+  if (POST) {
+    if (P.reinit) exact::reinit_cell(P, RP.dx, i, j, k, u);
+    exact::positivity_cell<8>(P, u);
+    if (U0) {
+#pragma unroll
+      for (int q = 0; q < MF_MAX_COMP; ++q)
+        if (q < P.nc) u[q] = u[q] + 0.5 * (U0[base + q * cs] - U1[base + q * cs]);
+    }
   }
+#pragma unroll
+  for (int q = 0; q < MF_MAX_COMP; ++q)
+    if (q < P.nc) U[base + q * cs] = u[q];
 }
 
 // A fab given by pointer, box lo and extents.
@@ -394,11 +413,16 @@ cudaError_t launch_efield(const DevParams& P, int mixed, const void* const f[3],
 
 cudaError_t launch_recalc_b(const DevParams& P, double* u, const double* bold, const double* e,
                             const double* u0, const double* u1, const StepState* state,
-                            double dt_scale, const Batch& b, cudaStream_t s) {
+                            double dt_scale, int stage, const Batch& b, cudaStream_t s) {
   if (b.tot_v <= 0) return cudaSuccess;
   const int nt = b.nt[2];
-  k_recalc_b<<<flat_blocks(b.tot_v, nt), nt, 0, s>>>(P, u, bold, e, u0, u1, state, dt_scale,
-                                                       b.desc, b.ndesc, b.tot_v, b.runs);
+  const unsigned g = flat_blocks(b.tot_v, nt);
+  if (stage)
+    k_recalc_b<1><<<g, nt, 0, s>>>(P, u, bold, e, u0, u1, state, dt_scale, b.desc, b.ndesc,
+                                   b.tot_v, b.runs);
+  else
+    k_recalc_b<0><<<g, nt, 0, s>>>(P, u, bold, e, u0, u1, state, dt_scale, b.desc, b.ndesc,
+                                   b.tot_v, b.runs);
   return cudaGetLastError();
 }
 

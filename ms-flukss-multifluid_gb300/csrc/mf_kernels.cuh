@@ -248,11 +248,14 @@ cudaError_t launch_efield(const DevParams& P, int mixed, const void* const f[3],
                           const double* w, double* e, const double* e1, double* eavg,
                           const Batch& b, cudaStream_t s);
 // recalculateB on each valueBox from bold (components 5..7, laid out like U)
-// and the edge field e with time step state[run].dt * dt_scale; with u0 / u1
-// set, AVERAGESTATE u += (u0 - u1) / 2 afterwards.
+// and the edge field e with time step state[run].dt * dt_scale.  stage = 1:
+// a stage's recalculation, then the inner-sphere reset and the positivity fix
+// (which the update kernel leaves to it under constrained transport) and,
+// with u0 / u1 set, AVERAGESTATE u += (u0 - u1) / 2; stage = 0: the level's
+// recalculation after the step alone.
 cudaError_t launch_recalc_b(const DevParams& P, double* u, const double* bold, const double* e,
                             const double* u0, const double* u1, const StepState* state,
-                            double dt_scale, const Batch& b, cudaStream_t s);
+                            double dt_scale, int stage, const Batch& b, cudaStream_t s);
 
 // recalculateMagneticField on caller fabs: U (in place) from Uold's field and
 // the EdgeBox fabs E (3 in 3D, 1 nodal in 2D) on box.

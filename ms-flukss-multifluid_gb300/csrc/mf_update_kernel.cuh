@@ -206,8 +206,12 @@ __global__ void __launch_bounds__(kMaxBlock)
       const int reg = region_cell(P, RP.dx, i, j, k, w, regtr);
       charge_exchange_add<IRHON>(P, w, reg, dt, u);
     }
-    if (P.reinit) reinit_cell(P, RP.dx, i, j, k, u);
-    positivity_cell<IRHON>(P, u);
+    // problem post-processing and positivity (src/PatchMHDAM.cpp:705-707); with
+    // constrained transport they follow the recalculation of B (k_recalc_b)
+    if (!P.ct) {
+      if (P.reinit) reinit_cell(P, RP.dx, i, j, k, u);
+      positivity_cell<IRHON>(P, u);
+    }
     if (P.nls) {  // POSTPROCESSING_LS (srcIdeal/PatchMHDMF.cpp:1414-1424)
       const int x[3] = {i, j, k};
       const double f0 = ls_floor(P, RP, wst, B.uin, D.fn, base, cs, x, P.ils);
