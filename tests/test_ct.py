@@ -348,16 +348,20 @@ def test_ct_refused_where_not_built(gpulib):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("ta", [mfgpu.TA_RK2, mfgpu.TA_HANCOCK])
-def test_gpu_helio_ct_with_region_tracer_vs_oracle(gpulib, oracle, ta):
+@pytest.mark.parametrize("ta,hbc,use8", [(mfgpu.TA_RK2, 0, 0), (mfgpu.TA_HANCOCK, 0, 0),
+                                         (mfgpu.TA_RK2, 1, 0), (mfgpu.TA_FIRST_ORDER, 0, 1)])
+def test_gpu_helio_ct_with_region_tracer_vs_oracle(gpulib, oracle, ta, hbc, use8):
     """Constrained transport in the full heliosphere problem: far-field ghosts,
     three neutral fluids with charge exchange, the inner-sphere reset, the
-    neutral pass-through at the sun and the region tracer, level steps of
-    32^3 in 8 patches against the oracle (each step from the oracle's state)."""
+    neutral pass-through at the sun and the region tracer, with the
+    heliosphere boundary fluxes (HELIOBC, whose B fluxes enter the boundary
+    edges) or the 8-wave source; level steps of 32^3 in 8 patches against the
+    oracle (each step from the oracle's state)."""
     n = 32
     p = mfgpu.helio_params(n, time_approximation=ta, region_tracer=True)
     p.divb_cleaning = 1
-    p.use_8wave = 0
+    p.use_8wave = use8
+    p.helio_bc = hbc
     boxes = mfgpu.tile_boxes(n, 16, 3)
     ng = mfgpu.num_ghost(p)
     arrays, fboxes = [], []
