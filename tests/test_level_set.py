@@ -218,12 +218,13 @@ def test_gpu_orszag_surface_vs_oracle(gpulib, oracle, ta):
 @pytest.mark.parametrize("lim", [mfgpu.LIM_CD, mfgpu.LIM_SUPERBEE, mfgpu.LIM_VANALBADA,
                                  mfgpu.LIM_HARMONIC, mfgpu.LIM_VANLEER])
 @pytest.mark.parametrize("char", [0, 1])
-def test_gpu_surface_limiters(gpulib, oracle, lim, char):
+@pytest.mark.parametrize("ta", [mfgpu.TA_RK2, mfgpu.TA_HANCOCK])
+def test_gpu_surface_limiters(gpulib, oracle, lim, char, ta):
     """Every limiter_LS, with plain and with characteristic reconstruction
     (where the surfaces take the *FACESLOPES form), and the positivity
-    fallback on."""
+    fallback on; RK2 and Hancock (face values of the predictor)."""
     n = 32
-    p, U, lo, hi, ng = _orszag_surface(n, mfgpu.TA_RK2, lim, char_reconstruction=char,
+    p, U, lo, hi, ng = _orszag_surface(n, ta, lim, char_reconstruction=char,
                                        check_positivity=1)
     ctx = mfgpu.Context(p)
     vlo, vhi = [0, 0, 0], [n - 1, n - 1, 0]
@@ -282,12 +283,15 @@ def _device_level(p, boxes, arrays):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("ta", TAS)
-def test_gpu_helio_region_tracer_level_vs_oracle(gpulib, oracle, ta):
+@pytest.mark.parametrize("ta,hbc", [(mfgpu.TA_RK2, 0), (mfgpu.TA_HANCOCK, 0),
+                                    (mfgpu.TA_FIRST_ORDER, 0), (mfgpu.TA_RK2, 1)])
+def test_gpu_helio_region_tracer_level_vs_oracle(gpulib, oracle, ta, hbc):
     """32^3 heliosphere with the region tracer (8 patches, far-field ghosts
-    holding +1): two level steps, each from the oracle's state."""
+    holding +1), also with the heliosphere boundary fluxes: two level steps,
+    each from the oracle's state."""
     n = 32
     p = mfgpu.helio_params(n, time_approximation=ta, region_tracer=True)
+    p.helio_bc = hbc
     boxes, arrays, fboxes = _helio_level(p, n)
     ctx, lev, flat, dt0 = _device_level(p, boxes, arrays)
     ng = ctx.ng
