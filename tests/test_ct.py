@@ -394,3 +394,37 @@ def test_gpu_helio_ct_with_region_tracer_vs_oracle(gpulib, oracle, ta, hbc, use8
         dt = 0.4 * ndt_o
     lev.close()
     ctx.close()
+
+
+def test_ct_entry_points_reject_bad_arguments(gpulib):
+    """Argument checks of mf_patch_update_e and mf_recalculate_magnetic_field
+    (they come before any device work: the pointers are never dereferenced)."""
+    import ctypes
+    n = 16
+    p = _p2(n, mfgpu.TA_RK2, 1)
+    ctx = mfgpu.Context(p)
+    lib, ng, nc = ctx.lib, ctx.ng, ctx.nc
+    lo, hi = mfgpu.grow([0, 0, 0], [n - 1, n - 1, 0], ng, 2)
+    fab = mfgpu.MfFab(4096, mfgpu.make_box(lo, hi), nc)
+    valid = mfgpu.make_box([0, 0, 0], [n - 1, n - 1, 0])
+    ndt = ctypes.c_double()
+    cell = mfgpu.c_int3()
+    small = (mfgpu.MfFab * 3)()
+    small[0] = mfgpu.MfFab(8192, mfgpu.make_box([0, 0, 0], [n - 1, n - 1, 0]), 1)  # not nodal
+    assert lib.mf_patch_update_e(ctx.h, ctypes.byref(fab), ctypes.byref(valid), 1e-3, None, None,
+                                 ctypes.cast(small, ctypes.c_void_p), ctypes.byref(ndt), cell,
+                                 None) == mfgpu.MF_ERR_BAD_ARG
+    uold = mfgpu.MfFab(4096, mfgpu.make_box(lo, hi), nc)
+    assert lib.mf_recalculate_magnetic_field(ctx.h, ctypes.byref(fab), ctypes.byref(uold),
+                                             ctypes.cast(small, ctypes.c_void_p), 1e-3,
+                                             ctypes.byref(valid), None) == mfgpu.MF_ERR_BAD_ARG
+    ctx.close()
+    q = _p2(n, mfgpu.TA_RK2, 0)         # no constrained transport: nothing to recalculate
+    ctx = mfgpu.Context(q)
+    good = (mfgpu.MfFab * 3)()
+    good[0] = mfgpu.MfFab(8192, mfgpu.make_box([0, 0, 0], [n, n, 0]), 1)
+    assert ctx.lib.mf_recalculate_magnetic_field(ctx.h, ctypes.byref(fab), ctypes.byref(uold),
+                                                 ctypes.cast(good, ctypes.c_void_p), 1e-3,
+                                                 ctypes.byref(valid), None) == \
+        mfgpu.MF_ERR_BAD_ARG
+    ctx.close()
