@@ -331,6 +331,7 @@ struct mf_ctx {
   DevBuf pred, w, f1[3], bn1[3], f2[3], bn2[3], desc, partials, state;
   DevBuf fv[3], w2;  // Hancock face values and predicted primitive state
   DevBuf ct_u0, ct_e1, ct_e2, ct_eo;  // constrained transport: U(t), stage edge fields, average
+  DevBuf wf;                          // mixed precision: FP32 copy of w for the flux kernels
   PinnedBuf hdesc, hstate;
 };
 
@@ -359,6 +360,7 @@ struct mf_level {
   int nsun = 0;
   DevBuf ct_u0, ct_e1, ct_e2, ct_eo;       // constrained transport: UOld, edge fields
   DevBuf packed;                           // staging of the valid-cell transfers
+  DevBuf Wf;                               // mixed precision: FP32 copy of W
   std::vector<long long> voff;             // packed offset of each patch (doubles)
 };
 
@@ -626,6 +628,7 @@ static mf_status patch_update_impl(mf_ctx* c, mf_fab* U, const mf_box* valid, do
   if (E && ct && !edges_ok(E, *valid, sd)) return MF_ERR_BAD_ARG;
 
   MF_CHECK_CUDA(c->w.ensure(sizeof(double) * fabn * nc));
+  if (mixed) MF_CHECK_CUDA(c->wf.ensure(sizeof(float) * fabn * nc));
   if (ct) {
     MF_CHECK_CUDA(c->ct_e1.ensure(sizeof(double) * fabn * 3));
     MF_CHECK_CUDA(c->ct_e2.ensure(sizeof(double) * fabn * 3));
@@ -683,6 +686,7 @@ static mf_status patch_update_impl(mf_ctx* c, mf_fab* U, const mf_box* valid, do
   StageBuffers B;
   std::memset(&B, 0, sizeof(B));
   B.w = (double*)c->w.p;
+  B.wf = mixed ? (float*)c->wf.p : nullptr;
   // constrained transport (src/PatchMHDAM.cpp:684-698, 1150-1160): after each
   // stage's update, the edge field of its fluxes and B from the stage-start
   // field; the dt then follows the last recalculation
@@ -1216,6 +1220,7 @@ static mf_status enqueue_level_step(mf_level* L, int advance, cudaEvent_t* ev = 
   StageBuffers B;
   std::memset(&B, 0, sizeof(B));
   B.w = (double*)L->W.p;
+  B.wf = (p.precision == MF_PREC_MIXED) ? (float*)L->Wf.p : nullptr;
   for (int d = 0; d < 3; ++d) {
     B.f[d] = L->F[d].p;
     B.bn[d] = L->Bn[d].p;
@@ -1449,6 +1454,7 @@ mf_status mf_level_create(mf_ctx* c, int npatch, const mf_box* valid, mf_level**
         e = L->FV[d].ensure(sizeof(double) * std::max<long long>(plan.fvsize, 1));
     if (e != cudaSuccess) break;
     if ((e = L->W.ensure(sizeof(double) * L->total)) != cudaSuccess) break;
+    if (mixed && (e = L->Wf.ensure(sizeof(float) * L->total)) != cudaSuccess) break;
     for (int d = 0; d < sd && e == cudaSuccess; ++d) {
       e = L->F[d].ensure(rs * fsize[d]);
       if (e == cudaSuccess) e = L->Bn[d].ensure(rs * bsize[d]);
@@ -1803,6 +1809,7 @@ static mf_status time_kind(mf_level* L, int kind, int reps, cudaEvent_t e0, cuda
   B.uin = (const double*)L->U.p;
   B.uout = (double*)(p.time_approximation == MF_TA_RK2 ? L->U1.p : L->W.p);
   B.w = (double*)L->W.p;
+  B.wf = (p.precision == MF_PREC_MIXED) ? (float*)L->Wf.p : nullptr;
   for (int d = 0; d < 3; ++d) {
     B.f[d] = L->F[d].p;
     B.bn[d] = L->Bn[d].p;
@@ -1815,11 +1822,11 @@ static mf_status time_kind(mf_level* L, int kind, int reps, cudaEvent_t e0, cuda
   for (int r = 0; r < reps; ++r) {
     cudaError_t e = cudaSuccess;
     if (kind == 0) {
-      e = mf::launch_prim(c->dp, B.uin, B.w, b, L->s);
+      e = mf::launch_prim(c->dp, B.uin, B.w, b, L->s, B.wf);
     } else if (kind == 1) {
       for (int d = 0; d < sd && e == cudaSuccess; ++d) {
         if (p.precision == MF_PREC_MIXED)
-          e = mf::launch_flux_fast<float>(c->dp, d, B.w, B.f[d], B.bn[d], b, ds, L->s);
+          e = mf::launch_flux_fast<float>(c->dp, d, B.w, B.f[d], B.bn[d], b, ds, L->s, B.wf);
         else if (p.precision == MF_PREC_FP64_FAST)
           e = mf::launch_flux_fast<double>(c->dp, d, B.w, B.f[d], B.bn[d], b, ds, L->s);
         else

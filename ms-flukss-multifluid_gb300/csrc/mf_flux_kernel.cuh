@@ -304,11 +304,13 @@ __device__ __forceinline__ int helio_side(const DevParams& P, const RunParams& R
   return (f == RP.dlo[DIR]) ? 0 : (f == RP.dhi[DIR] + 1) ? 1 : -1;
 }
 
-template <typename R, int DIR>
+// WF: read the limiter inputs from Wf, the FP32 copy of W the prim kernel
+// wrote (R = float), instead of converting W value by value here.
+template <typename R, int DIR, int WF>
 __global__ void __launch_bounds__(kMaxBlock)
-    k_flux(const DevParams P, const double* __restrict__ W, R* __restrict__ F,
-           R* __restrict__ Bn, const StageDesc* __restrict__ descs, int ndesc, int total,
-           const RunParams* __restrict__ runs, const StepState* __restrict__ states) {
+    k_flux(const DevParams P, const double* __restrict__ W, const float* __restrict__ Wf,
+           R* __restrict__ F, R* __restrict__ Bn, const StageDesc* __restrict__ descs, int ndesc,
+           int total, const RunParams* __restrict__ runs, const StepState* __restrict__ states) {
   const int gi = blockIdx.x * blockDim.x + threadIdx.x;
   if (gi >= total) return;
   const StageDesc& D = descs[find_desc(descs, ndesc, kRegF + DIR, gi)];
@@ -323,6 +325,12 @@ __global__ void __launch_bounds__(kMaxBlock)
                                                    : (long long)D.fn[0] * D.fn[1];
   // cell on the high side of face (i,j,k) has the same index
   const double* __restrict__ w0 = W + D.u_off + loc(D.flo, D.fn, i, j, k);
+  const float* __restrict__ f0 = WF ? Wf + D.u_off + loc(D.flo, D.fn, i, j, k) : nullptr;
+  // component v of the cell o cells along DIR from the face's high-side cell
+  auto ld = [&](int v, long long o) -> R {
+    if (WF) return R(f0[v * cs + o * st]);
+    return R(w0[v * cs + o * st]);
+  };
   const long long fcs = (long long)fnb[0] * fnb[1] * fnb[2];
   const long long fo = loc(D.vlo, fnb, i, j, k);
   R* __restrict__ Fo = F + D.f_off[DIR] + fo;
@@ -356,8 +364,7 @@ __global__ void __launch_bounds__(kMaxBlock)
 #pragma unroll
     for (int t = 0; t < 2; ++t) {
       const int v = t ? 4 : 0;
-      const double* wv = w0 + v * cs;
-      R a = R(wv[-2 * st]), b = R(wv[-st]), c = R(wv[0]), d = R(wv[st]);
+      R a = ld(v, -2), b = ld(v, -1), c = ld(v, 0), d = ld(v, 1);
       R lo, hi;
       face_values<R>(P.lim[v], a, b, c, lo, hi);
       if (lo <= R(0) || hi <= R(0)) negL = true;
@@ -374,8 +381,7 @@ __global__ void __launch_bounds__(kMaxBlock)
     if (v < 8 && P.char_rec) continue;
     if (v < 8 || P.glm) {
       const int lim = (v < 8) ? P.lim[v] : (int)MF_LIM_MINMOD;
-      const double* wv = w0 + v * cs;
-      R a = R(wv[-2 * st]), b = R(wv[-st]), c = R(wv[0]), d = R(wv[st]);
+      R a = ld(v, -2), b = ld(v, -1), c = ld(v, 0), d = ld(v, 1);
       R lo, hi;
       face_values<R>(lim, a, b, c, lo, hi);
       wl[v] = negL ? b : hi;
@@ -433,8 +439,7 @@ __global__ void __launch_bounds__(kMaxBlock)
     R nl[5], nr[5], gn[5];
 #pragma unroll
     for (int m = 0; m < 5; ++m) {
-      const double* wv = w0 + (s + m) * cs;
-      R a = R(wv[-2 * st]), b = R(wv[-st]), c = R(wv[0]), d = R(wv[st]);
+      R a = ld(s + m, -2), b = ld(s + m, -1), c = ld(s + m, 0), d = ld(s + m, 1);
       R lo, hi;
       face_values<R>(MF_LIM_MINMOD, a, b, c, lo, hi);
       nl[m] = negL ? b : hi;
@@ -464,8 +469,7 @@ __global__ void __launch_bounds__(kMaxBlock)
   if (P.nls) {
     const R uavg = sqrt(wl[0]) * wl[1 + DIR] + sqrt(wr[0]) * wr[1 + DIR];
     for (int q = P.ils; q < P.nc; ++q) {
-      const double* wv = w0 + q * cs;
-      const R a = R(wv[-2 * st]), b = R(wv[-st]), c = R(wv[0]), d = R(wv[st]);
+      const R a = ld(q, -2), b = ld(q, -1), c = ld(q, 0), d = ld(q, 1);
       R lo, hi;
       ls_face_values<R>(P, a, b, c, lo, hi);
       const R l = negL ? b : hi;

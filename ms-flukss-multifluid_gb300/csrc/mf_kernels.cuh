@@ -161,6 +161,9 @@ struct StageBuffers {
   // corrector: w holds W(t+dt/2), wls W(t)): the velocity of the tracking
   // surfaces' update and their stage-start values (Uold); null = w
   const double* wls;
+  // mixed precision: an FP32 copy of w (same layout) that the FP32 flux
+  // kernels read, written by the prim kernel; null = convert w in the flux kernel
+  float* wf;
   void* f[3];          // face fluxes (double or float), per direction
   void* bn[3];         // face-normal B (double or float), per direction
   double* divb;        // optional divB output (single patch: fab on the valid box)
@@ -170,8 +173,10 @@ struct StageBuffers {
 
 enum StageFlags : int { kStageAverage = 1, kStageDt = 2 };
 
+// wf (nullable): also the FP32 copy of w (round to nearest, as the FP32 flux
+// kernels would convert each value)
 cudaError_t launch_prim(const DevParams& P, const double* uin, double* w, const Batch& b,
-                        cudaStream_t s);
+                        cudaStream_t s, float* wf = nullptr);
 
 // FP64 parity path (reference evaluation order, no contraction)
 cudaError_t launch_flux_exact(const DevParams& P, int dir, const double* w, void* f, void* bn,
@@ -180,9 +185,11 @@ cudaError_t launch_update_exact(const DevParams& P, const StageBuffers& B, const
                                 int flags, double dt_scale, StepState* state,
                                 DtPartial* partials, int* nblocks_v, cudaStream_t s);
 // fast physics: R = float (mixed precision) or double (fast FP64)
+// wf (R = float only, nullable): the FP32 copy of w the prim kernel wrote
 template <typename R>
 cudaError_t launch_flux_fast(const DevParams& P, int dir, const double* w, void* f, void* bn,
-                             const Batch& b, const StepState* state, cudaStream_t s);
+                             const Batch& b, const StepState* state, cudaStream_t s,
+                             const float* wf = nullptr);
 template <typename R>
 cudaError_t launch_update_fast(const DevParams& P, const StageBuffers& B, const Batch& b,
                                int flags, double dt_scale, StepState* state,

@@ -12,7 +12,7 @@ namespace {
 template <int GLM>
 __global__ void __launch_bounds__(kMaxBlock)
     k_prim(const DevParams P, const double* __restrict__ U, double* __restrict__ W,
-           const StageDesc* __restrict__ descs, int ndesc, int total,
+           float* __restrict__ Wf, const StageDesc* __restrict__ descs, int ndesc, int total,
            const RunParams* __restrict__ runs) {
   constexpr int IRHON = 8 + GLM;
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
@@ -74,6 +74,12 @@ __global__ void __launch_bounds__(kMaxBlock)
   // U's ghost value
   for (int q = P.ils; q < P.nc; ++q)
     W[base + q * cs] = (od >= 0 && P.reg_tracer && q == P.nc - 1) ? 1.0 : U[base + q * cs];
+  if (Wf) {  // the FP32 copy the mixed-precision flux kernels read
+#pragma unroll
+    for (int q = 0; q < MF_MAX_COMP; ++q)
+      if (q < P.ils) Wf[base + q * cs] = (float)w[q];
+    for (int q = P.ils; q < P.nc; ++q) Wf[base + q * cs] = (float)W[base + q * cs];
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -81,14 +87,14 @@ __global__ void __launch_bounds__(kMaxBlock)
 }  // namespace
 
 cudaError_t launch_prim(const DevParams& P, const double* uin, double* w, const Batch& b,
-                        cudaStream_t s) {
+                        cudaStream_t s, float* wf) {
   if (b.tot_w <= 0) return cudaSuccess;
   const int nt = b.nt[0];
   const unsigned gw = flat_blocks(b.tot_w, nt);
   if (P.glm)
-    k_prim<1><<<gw, nt, 0, s>>>(P, uin, w, b.desc, b.ndesc, b.tot_w, b.runs);
+    k_prim<1><<<gw, nt, 0, s>>>(P, uin, w, wf, b.desc, b.ndesc, b.tot_w, b.runs);
   else
-    k_prim<0><<<gw, nt, 0, s>>>(P, uin, w, b.desc, b.ndesc, b.tot_w, b.runs);
+    k_prim<0><<<gw, nt, 0, s>>>(P, uin, w, wf, b.desc, b.ndesc, b.tot_w, b.runs);
   return cudaGetLastError();
 }
 

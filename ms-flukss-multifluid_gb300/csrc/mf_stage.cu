@@ -8,12 +8,12 @@ cudaError_t launch_stage(const DevParams& P, int precision, const StageBuffers& 
                          const Batch& b, int flags, double dt_scale, StepState* state,
                          DtPartial* partials, int* nblocks_v, cudaStream_t s) {
   int ne = 0;
-  cudaError_t e = launch_prim(P, B.uin, B.w, b, s);
+  cudaError_t e = launch_prim(P, B.uin, B.w, b, s, precision == MF_PREC_MIXED ? B.wf : nullptr);
   if (e != cudaSuccess) return e;
   if (B.ev) cudaEventRecord(B.ev[ne++], s);
   for (int d = 0; d < P.sd; ++d) {
     if (precision == MF_PREC_MIXED)
-      e = launch_flux_fast<float>(P, d, B.w, B.f[d], B.bn[d], b, state, s);
+      e = launch_flux_fast<float>(P, d, B.w, B.f[d], B.bn[d], b, state, s, B.wf);
     else if (precision == MF_PREC_FP64_FAST)
       e = launch_flux_fast<double>(P, d, B.w, B.f[d], B.bn[d], b, state, s);
     else
