@@ -400,7 +400,7 @@ def run_ours(a):
                  "step_hbm_frac": (ws * zones * a.steps / (msm * 1e-3) * 16 * nc / 1e9) / peak,
                  "per_kind_ms": {},
                  "l1_rel_vs_fp64": l1, "l1_steps": acc_done, "l1_error": acc_error,
-                 "dtype": "f32 reconstruction+fluxes, f64 state/accumulation/sources"}
+                 "dtype": "f32 reconstruction+fluxes+charge-exchange rates+wave speeds, f64 state/accumulation"}
         for kind, t in profm:
             mixed["per_kind_ms"][kind] = mixed["per_kind_ms"].get(kind, 0.0) + t
         levm.close()

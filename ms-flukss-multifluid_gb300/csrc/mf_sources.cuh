@@ -109,81 +109,99 @@ __device__ __forceinline__ int ce_recipient(int nN, int reg) {
   return (reg >= 1 && reg <= nN) ? reg : 0;
 }
 
+// Arithmetic type of the charge-exchange rates: FP64, or FP32 in the mixed
+// precision mode (the rates scale a source that is a small fraction of the
+// state per step; their FP32 rounding stays far below the FP32 error the
+// fluxes carry).  The state update itself is FP64 either way.
+__device__ __forceinline__ double ce_rsqrt(double x) { return rsqrt(x); }
+__device__ __forceinline__ float ce_rsqrt(float x) { return rsqrtf(x); }
+__device__ __forceinline__ double ce_log(double x) { return log(x); }
+__device__ __forceinline__ float ce_log(float x) { return logf(x); }
+__device__ __forceinline__ double ce_exp(double x) { return exp(x); }
+__device__ __forceinline__ float ce_exp(float x) { return expf(x); }
+__device__ __forceinline__ double ce_pow(double x, double y) { return pow(x, y); }
+__device__ __forceinline__ float ce_pow(float x, float y) { return powf(x, y); }
+
 // Pauls & Zank charge-exchange rates of one cell; adds S = -dt*H to u
 // (HeliosphericProblem::explicitSource, swlism/HeliosphericProblem.cpp:1394-1539,
 // CHARGE_EXCHANGE_4F swlism/ChargeExchange2F.ChF:673-993 and _MF :995-1149).
-template <int IRHON>
+// T is the arithmetic type of the rates (double, or float in mixed precision).
+template <int IRHON, typename T = double>
 __device__ __forceinline__ void charge_exchange_add(const DevParams& P, const double* w, int reg,
                                                     double dt, double* u) {
   const int nN = P.nf - 1;
-  const double rho = w[0], ux = w[1], uy = w[2], uz = w[3];
-  const double U2 = ux * ux + uy * uy + uz * uz;
-  const double VVTP = w[4] / rho;
-  double h2 = 0, h3 = 0, h4 = 0, h5 = 0, PPLUX = 0, PPLUY = 0, PPLUZ = 0, ENPLU = 0;
-  double DENPLU[MF_MAX_FLUIDS], PMIX[MF_MAX_FLUIDS], PMIY[MF_MAX_FLUIDS], PMIZ[MF_MAX_FLUIDS],
+  constexpr T c4p = T(4.0 * kInvPi), c16p = T(16.0 * kInvPi), c94pi = T(2.25 * kPi);
+  constexpr T cip = T(kInvPi), c649 = T(64.0 / 9.0);
+  const T rho = T(w[0]), ux = T(w[1]), uy = T(w[2]), uz = T(w[3]);
+  const T U2 = ux * ux + uy * uy + uz * uz;
+  const T VVTP = T(w[4]) / rho;
+  const T scale_vel = T(P.ce_scale_vel), ce_a = T(P.ce_a), ce_b = T(P.ce_b);
+  const T damp_c = T(P.ce_damp_c), damp_pow = T(P.ce_damp_pow), sig_scale = T(P.ce_sigma_scale);
+  T h2 = 0, h3 = 0, h4 = 0, h5 = 0, PPLUX = 0, PPLUY = 0, PPLUZ = 0, ENPLU = 0;
+  T DENPLU[MF_MAX_FLUIDS], PMIX[MF_MAX_FLUIDS], PMIY[MF_MAX_FLUIDS], PMIZ[MF_MAX_FLUIDS],
       ENMI[MF_MAX_FLUIDS];
 #pragma unroll
   for (int f = 1; f < MF_MAX_FLUIDS; ++f) {
     if (f > nN) break;
     const double* wn = w + IRHON + (f - 1) * 5;
-    const double rhoN = wn[0], uxN = wn[1], uyN = wn[2], uzN = wn[3];
-    const double dx_ = ux - uxN, dy_ = uy - uyN, dz_ = uz - uzN;
-    const double UH2 = uxN * uxN + uyN * uyN + uzN * uzN;
-    const double DU2 = dx_ * dx_ + dy_ * dy_ + dz_ * dz_;
-    const double VPHH = dx_ * uxN + dy_ * uyN + dz_ * uzN;
-    const double VPHP = dx_ * ux + dy_ * uy + dz_ * uz;
-    const double VVTH = 2.0 * wn[4] / rhoN;
+    const T rhoN = T(wn[0]), uxN = T(wn[1]), uyN = T(wn[2]), uzN = T(wn[3]);
+    const T dx_ = ux - uxN, dy_ = uy - uyN, dz_ = uz - uzN;
+    const T UH2 = uxN * uxN + uyN * uyN + uzN * uzN;
+    const T DU2 = dx_ * dx_ + dy_ * dy_ + dz_ * dz_;
+    const T VPHH = dx_ * uxN + dy_ * uyN + dz_ * uzN;
+    const T VPHP = dx_ * ux + dy_ * uy + dz_ * uz;
+    const T VVTH = T(2) * T(wn[4]) / rhoN;
     // thermal + relative speeds; every argument is > 0, so sqrt(a) = a*rsqrt(a)
-    const double aUD = (4.0 * kInvPi) * (VVTP + VVTH) + DU2;
-    const double UD = aUD * rsqrt(aUD);
-    const double iUPM = rsqrt((16.0 * kInvPi) * VVTP + (2.25 * kPi) * VVTH + 4.0 * DU2);
-    const double iUHM = rsqrt((2.25 * kPi) * VVTP + (16.0 * kInvPi) * VVTH + 4.0 * DU2);
-    const double aPE = kInvPi * (4.0 * VVTP + (64.0 / 9.0) * VVTH) + DU2;
-    const double UPE = aPE * rsqrt(aPE);
-    const double aHE = kInvPi * ((64.0 / 9.0) * VVTP + 4.0 * VVTH) + DU2;
-    const double UHE = aHE * rsqrt(aHE);
-    const double UDS = P.ce_scale_vel * UD;
-    const double t = P.ce_a - P.ce_b * log(UDS);
-    double SIG = t * t;
-    if (P.ce_damp_c > 0.0) SIG = SIG * pow(1.0 - exp(-P.ce_damp_c / UDS), P.ce_damp_pow);
-    const double ARR = P.ce_sigma_scale * SIG * rhoN * rho;
-    const double VVTHU = VVTH * iUPM;
-    const double VP_UHM = VVTP * iUHM;
-    const double hv = ARR * (UD + VVTHU + VP_UHM);
+    const T aUD = c4p * (VVTP + VVTH) + DU2;
+    const T UD = aUD * ce_rsqrt(aUD);
+    const T iUPM = ce_rsqrt(c16p * VVTP + c94pi * VVTH + T(4) * DU2);
+    const T iUHM = ce_rsqrt(c94pi * VVTP + c16p * VVTH + T(4) * DU2);
+    const T aPE = cip * (T(4) * VVTP + c649 * VVTH) + DU2;
+    const T UPE = aPE * ce_rsqrt(aPE);
+    const T aHE = cip * (c649 * VVTP + T(4) * VVTH) + DU2;
+    const T UHE = aHE * ce_rsqrt(aHE);
+    const T UDS = scale_vel * UD;
+    const T t = ce_a - ce_b * ce_log(UDS);
+    T SIG = t * t;
+    if (damp_c > T(0)) SIG = SIG * ce_pow(T(1) - ce_exp(-damp_c / UDS), damp_pow);
+    const T ARR = sig_scale * SIG * rhoN * rho;
+    const T VVTHU = VVTH * iUPM;
+    const T VP_UHM = VVTP * iUHM;
+    const T hv = ARR * (UD + VVTHU + VP_UHM);
     h2 = h2 + hv * dx_;
     h3 = h3 + hv * dy_;
     h4 = h4 + hv * dz_;
-    h5 = h5 + 0.5 * ARR *
-                  (1.5 * (UHE * VVTP - UPE * VVTH) + UD * (U2 - UH2) +
-                   2.0 * (VVTHU * VPHH + VPHP * VP_UHM));
+    h5 = h5 + T(0.5) * ARR *
+                  (T(1.5) * (UHE * VVTP - UPE * VVTH) + UD * (U2 - UH2) +
+                   T(2) * (VVTHU * VPHH + VPHP * VP_UHM));
     DENPLU[f] = -ARR * UD;
     PPLUX = PPLUX - ARR * (ux * UD + dx_ * VP_UHM);
     PPLUY = PPLUY - ARR * (uy * UD + dy_ * VP_UHM);
     PPLUZ = PPLUZ - ARR * (uz * UD + dz_ * VP_UHM);
-    ENPLU = ENPLU - ARR * (0.5 * U2 * UD + VPHP * VP_UHM + 0.75 * VVTP * UHE);
+    ENPLU = ENPLU - ARR * (T(0.5) * U2 * UD + VPHP * VP_UHM + T(0.75) * VVTP * UHE);
     PMIX[f] = ARR * (uxN * UD - dx_ * VVTHU);
     PMIY[f] = ARR * (uyN * UD - dy_ * VVTHU);
     PMIZ[f] = ARR * (uzN * UD - dz_ * VVTHU);
-    ENMI[f] = ARR * (0.5 * UH2 * UD - VPHH * VVTHU + 0.75 * VVTH * UPE);
+    ENMI[f] = ARR * (T(0.5) * UH2 * UD - VPHH * VVTHU + T(0.75) * VVTH * UPE);
   }
-  u[1] = u[1] - dt * h2;
-  u[2] = u[2] - dt * h3;
-  u[3] = u[3] - dt * h4;
-  u[4] = u[4] - dt * h5;
+  u[1] = u[1] - dt * double(h2);
+  u[2] = u[2] - dt * double(h3);
+  u[3] = u[3] - dt * double(h4);
+  u[4] = u[4] - dt * double(h5);
   // S of the magnetic field (and of psi) is zero
   const int rk = ce_recipient(nN, reg);
 #pragma unroll
   for (int f = 1; f < MF_MAX_FLUIDS; ++f) {
     if (f > nN) break;
-    double H1, H2, H3, H4, H5;
+    T H1, H2, H3, H4, H5;
     if (f == rk) {
       if (nN <= 3) {
-        H1 = 0.0;
+        H1 = 0;
 #pragma unroll
         for (int q = 1; q < MF_MAX_FLUIDS; ++q)
           if (q <= nN && q != f) H1 = H1 + DENPLU[q];
       } else {
-        double sum = DENPLU[1];
+        T sum = DENPLU[1];
 #pragma unroll
         for (int q = 2; q < MF_MAX_FLUIDS; ++q)
           if (q <= nN) sum = sum + DENPLU[q];
@@ -201,11 +219,11 @@ __device__ __forceinline__ void charge_exchange_add(const DevParams& P, const do
       H5 = ENMI[f];
     }
     double* un = u + IRHON + (f - 1) * 5;
-    un[0] = un[0] - dt * H1;
-    un[1] = un[1] - dt * H2;
-    un[2] = un[2] - dt * H3;
-    un[3] = un[3] - dt * H4;
-    un[4] = un[4] - dt * H5;
+    un[0] = un[0] - dt * double(H1);
+    un[1] = un[1] - dt * double(H2);
+    un[2] = un[2] - dt * double(H3);
+    un[3] = un[3] - dt * double(H4);
+    un[4] = un[4] - dt * double(H5);
   }
 }
 
@@ -324,43 +342,50 @@ __device__ __forceinline__ void positivity_cell(const DevParams& P, double* u) {
 }
 
 // MAXWAVESPEED (srcIdeal/PatchIdealMHDF.ChF:5-63) + MAXWAVESPEED_E
-// (srcIdeal/PatchEulerF.ChF:5-50) of one cell.
-template <int IRHON>
+// (srcIdeal/PatchEulerF.ChF:5-50) of one cell, in T (FP64, or FP32 in the
+// mixed precision mode, whose time step then carries FP32 rounding).
+__device__ __forceinline__ double ws_sqrt(double x) { return sqrt(x); }
+__device__ __forceinline__ float ws_sqrt(float x) { return sqrtf(x); }
+
+template <int IRHON, typename T = double>
 __device__ __forceinline__ double max_wave_speed(const DevParams& P, const double* u) {
-  double cmax = 0.0;
+  const T i4pi = T(kInv4Pi), hg = T(P.hgamma), gam = T(P.gamma), sp = T(P.smallp);
+  T cmax = 0;
   {
-    const double invrho = 1.0 / u[0];
-    const double uu = u[1] * invrho, vv = u[2] * invrho, ww = u[3] * invrho;
-    const double ke = u[1] * uu + u[2] * vv + u[3] * ww;
-    const double bx = u[5], by = u[6], bz = u[7];
-    const double b = kInv4Pi * (bx * bx + by * by + bz * bz);
-    double p = P.hgamma * (u[4] - 0.5 * (ke + b));
-    p = fmax(p, P.smallp);
-    const double a2 = P.gamma * p * invrho;
-    const double as2 = 0.5 * (a2 + invrho * b);
-    const double as4 = as2 * as2;
-    const double k4 = kInv4Pi * invrho * a2;
+    const T invrho = T(1) / T(u[0]);
+    const T m1 = T(u[1]), m2 = T(u[2]), m3 = T(u[3]);
+    const T uu = m1 * invrho, vv = m2 * invrho, ww = m3 * invrho;
+    const T ke = m1 * uu + m2 * vv + m3 * ww;
+    const T bx = T(u[5]), by = T(u[6]), bz = T(u[7]);
+    const T b = i4pi * (bx * bx + by * by + bz * bz);
+    T p = hg * (T(u[4]) - T(0.5) * (ke + b));
+    p = fmax(p, sp);
+    const T a2 = gam * p * invrho;
+    const T as2 = T(0.5) * (a2 + invrho * b);
+    const T as4 = as2 * as2;
+    const T k4 = i4pi * invrho * a2;
     // as4 - k4 b^2 >= 0 exactly; contracted rounding can push it below 0
-    double umax = fabs(uu) + sqrt(as2 + sqrt(fmax(0.0, as4 - k4 * bx * bx)));
-    umax = fmax(fabs(vv) + sqrt(as2 + sqrt(fmax(0.0, as4 - k4 * by * by))), umax);
-    umax = fmax(fabs(ww) + sqrt(as2 + sqrt(fmax(0.0, as4 - k4 * bz * bz))), umax);
+    T umax = fabs(uu) + ws_sqrt(as2 + ws_sqrt(fmax(T(0), as4 - k4 * bx * bx)));
+    umax = fmax(fabs(vv) + ws_sqrt(as2 + ws_sqrt(fmax(T(0), as4 - k4 * by * by))), umax);
+    umax = fmax(fabs(ww) + ws_sqrt(as2 + ws_sqrt(fmax(T(0), as4 - k4 * bz * bz))), umax);
     cmax = fmax(umax, cmax);
   }
 #pragma unroll
   for (int f = 1; f < MF_MAX_FLUIDS; ++f) {
     if (f >= P.nf) break;
     const double* un = u + IRHON + (f - 1) * 5;
-    const double rho = fmax(un[0], P.smallr);
-    const double invrho = 1.0 / rho;
-    const double uu = un[1] * invrho, vv = un[2] * invrho, ww = un[3] * invrho;
-    const double ke = un[1] * uu + un[2] * vv + un[3] * ww;
-    double p = P.hgamma * (un[4] - 0.5 * ke);
-    p = fmax(p, P.smallp);
-    const double a = sqrt(P.gamma * p * invrho);
-    const double umax = fmax(fmax(fabs(uu), fabs(vv)), fabs(ww)) + a;
+    const T rho = fmax(T(un[0]), T(P.smallr));
+    const T invrho = T(1) / rho;
+    const T m1 = T(un[1]), m2 = T(un[2]), m3 = T(un[3]);
+    const T uu = m1 * invrho, vv = m2 * invrho, ww = m3 * invrho;
+    const T ke = m1 * uu + m2 * vv + m3 * ww;
+    T p = hg * (T(un[4]) - T(0.5) * ke);
+    p = fmax(p, sp);
+    const T a = ws_sqrt(gam * p * invrho);
+    const T umax = fmax(fmax(fabs(uu), fabs(vv)), fabs(ww)) + a;
     cmax = fmax(umax, cmax);
   }
-  return cmax;
+  return double(cmax);
 }
 
 }  // namespace fast

@@ -102,9 +102,12 @@ __device__ __forceinline__ int ce_recipient(int nN, int reg) {
 
 // Pauls & Zank charge-exchange rates of one cell; adds S = -dt*H to u
 // (HeliosphericProblem::explicitSource, swlism/HeliosphericProblem.cpp:1394-1539).
-template <int IRHON>
+// T names the arithmetic type for interface symmetry with the fast physics;
+// the parity physics is FP64 only.
+template <int IRHON, typename T = double>
 __device__ __forceinline__ void charge_exchange_add(const DevParams& P, const double* w, int reg,
                                                     double dt, double* u) {
+  static_assert(sizeof(T) == sizeof(double), "FP64 physics");
   const int nN = P.nf - 1;
   double rho = w[0], ux = w[1], uy = w[2], uz = w[3], pp = w[4];
   double U2 = ux * ux + uy * uy + uz * uz;
@@ -301,8 +304,9 @@ __device__ __forceinline__ void positivity_cell(const DevParams& P, double* u) {
 
 // MAXWAVESPEED (srcIdeal/PatchIdealMHDF.ChF:5-63) + MAXWAVESPEED_E
 // (srcIdeal/PatchEulerF.ChF:5-50) of one cell.
-template <int IRHON>
+template <int IRHON, typename T = double>
 __device__ __forceinline__ double max_wave_speed(const DevParams& P, const double* u) {
+  static_assert(sizeof(T) == sizeof(double), "FP64 physics");
   double cmax = 0.0;
   {
     double rho = u[0];

@@ -204,7 +204,7 @@ __global__ void __launch_bounds__(kMaxBlock)
     if (P.ce && P.nf >= 2) {
       const double regtr = P.reg_tracer ? B.w[base + (P.nc - 1) * cs] : 0.0;
       const int reg = region_cell(P, RP.dx, i, j, k, w, regtr);
-      charge_exchange_add<IRHON>(P, w, reg, dt, u);
+      charge_exchange_add<IRHON, R>(P, w, reg, dt, u);
     }
     // problem post-processing and positivity (src/PatchMHDAM.cpp:705-707); with
     // constrained transport they follow the recalculation of B (k_recalc_b)
@@ -236,7 +236,7 @@ __global__ void __launch_bounds__(kMaxBlock)
       }
     if (!finite) atomicOr(&ss->flags, kFlagNonFinite);
     if (FLAGS & kStageDt) {
-      dtc = RP.dx / max_wave_speed<IRHON>(P, u);
+      dtc = RP.dx / max_wave_speed<IRHON, R>(P, u);
       myidx = g;
       if (B.divb && P.use8) B.divb[loc(B.divb_lo, B.divb_n, i, j, k)] = divB;
     }
