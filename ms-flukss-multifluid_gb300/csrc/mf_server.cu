@@ -148,7 +148,7 @@ struct mf_server {
   mf::CtxView cv;
   int sd = 0, nc = 0, ng = 0;
   size_t rs = 8;
-  DevMem U, U1, W, F[3], Bn[3];
+  DevMem U, U1, W, Wf, F[3], Bn[3];
   Arena ac, af, ab;
   std::vector<Run> runs;
   // the batch of the admitted runs
@@ -313,6 +313,7 @@ mf_status enqueue_step(mf_server* S) {
   StageBuffers B;
   std::memset(&B, 0, sizeof(B));
   B.w = (double*)S->W.p;
+  B.wf = (p.precision == MF_PREC_MIXED) ? (float*)S->Wf.p : nullptr;
   for (int d = 0; d < 3; ++d) {
     B.f[d] = S->F[d].p;
     B.bn[d] = S->Bn[d].p;
@@ -442,10 +443,12 @@ mf_status mf_server_create(mf_ctx* physics, double hbm_budget_bytes, int max_run
   S->ng = S->cv.ng;
   S->rs = mf::flux_bytes(S->cv.p->precision);
   S->runs.resize(max_runs);
-  // split of the budget: cells (U, U1, W: 24 bytes per double of a fab),
-  // face fluxes (3 directions) and face-normal B (3 directions) with room for
-  // 0.75 face values per fab value
-  const double per = 24.0 + 3.0 * 0.75 * S->rs * (1.0 + 1.0 / S->nc);
+  // split of the budget: cells (U, U1, W: 24 bytes per double of a fab, and
+  // 4 more for the FP32 copy of W in mixed precision), face fluxes (3
+  // directions) and face-normal B (3 directions) with room for 0.75 face
+  // values per fab value
+  const double cell_bytes = (S->cv.p->precision == MF_PREC_MIXED) ? 28.0 : 24.0;
+  const double per = cell_bytes + 3.0 * 0.75 * S->rs * (1.0 + 1.0 / S->nc);
   const long long capC = (long long)(hbm_budget_bytes / per) / 64 * 64;
   const long long capF = (long long)(0.75 * capC) / 64 * 64;
   const long long capB = (long long)(0.75 * capC / S->nc) / 64 * 64 + 64 * max_runs;
@@ -455,6 +458,9 @@ mf_status mf_server_create(mf_ctx* physics, double hbm_budget_bytes, int max_run
     if ((e = S->U.ensure(sizeof(double) * capC)) != cudaSuccess) break;
     if ((e = S->U1.ensure(sizeof(double) * capC)) != cudaSuccess) break;
     if ((e = S->W.ensure(sizeof(double) * capC)) != cudaSuccess) break;
+    if (S->cv.p->precision == MF_PREC_MIXED &&
+        (e = S->Wf.ensure(sizeof(float) * capC)) != cudaSuccess)
+      break;
     for (int d = 0; d < S->sd && e == cudaSuccess; ++d) {
       e = S->F[d].ensure(S->rs * capF);
       if (e == cudaSuccess) e = S->Bn[d].ensure(S->rs * capB);
@@ -486,6 +492,7 @@ void mf_server_destroy(mf_server* S) {
   S->U.release();
   S->U1.release();
   S->W.release();
+  S->Wf.release();
   for (int d = 0; d < 3; ++d) {
     S->F[d].release();
     S->Bn[d].release();
