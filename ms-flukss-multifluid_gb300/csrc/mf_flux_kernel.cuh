@@ -307,7 +307,7 @@ __device__ __forceinline__ int helio_side(const DevParams& P, const RunParams& R
 // WF: read the limiter inputs from Wf, the FP32 copy of W the prim kernel
 // wrote (R = float), instead of converting W value by value here.
 template <typename R, int DIR, int WF>
-__global__ void __launch_bounds__(kMaxBlock)
+__global__ void __launch_bounds__(kMaxBlock, WF ? 2 : 1)
     k_flux(const DevParams P, const double* __restrict__ W, const float* __restrict__ Wf,
            R* __restrict__ F, R* __restrict__ Bn, const StageDesc* __restrict__ descs, int ndesc,
            int total, const RunParams* __restrict__ runs, const StepState* __restrict__ states) {

@@ -103,7 +103,7 @@ __device__ __forceinline__ void block_dt_min(double dtc, int myidx,
 }
 
 template <typename R, int GLM, int FLAGS>
-__global__ void __launch_bounds__(kMaxBlock)
+__global__ void __launch_bounds__(kMaxBlock, sizeof(R) == 4 ? 2 : 1)
     k_update(const DevParams P, const StageBuffers B, const StageDesc* __restrict__ descs,
              int ndesc, int total, const RunParams* __restrict__ runs,
              StepState* __restrict__ states, const double dt_scale,
