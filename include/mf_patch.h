@@ -429,7 +429,8 @@ mf_status mf_server_create(mf_ctx* physics, double hbm_budget_bytes, int max_run
 void mf_server_destroy(mf_server* srv);
 /* Device bytes a run of this spec holds while admitted (-1: invalid spec). */
 long long mf_server_run_bytes(const mf_server* srv, const mf_run_spec* spec);
-/* Largest free cell range of the arena, in bytes of the three cell arrays. */
+/* Largest free cell range of the arena, in bytes of the cell arrays (U, U1, W,
+   and the FP32 copy of W in mixed precision). */
 long long mf_server_free_bytes(const mf_server* srv);
 /* Admit a run whose initial conserved state is `state` (host: the run's
    domain as one FArrayBox without ghosts, nc components, x fastest).  Waits

@@ -302,6 +302,12 @@ mf_status rebuild(mf_server* S) {
   return MF_OK;
 }
 
+// Device bytes per fab value of the cell arrays: U, U1, W (FP64), plus the
+// FP32 copy of W in mixed precision.
+long long cell_bytes(const mf_server* S) {
+  return (S->cv.p->precision == MF_PREC_MIXED) ? 28 : 24;
+}
+
 // The step of every admitted run (the level step of mf_capi.cu with the
 // batch of runs): exchange, RK2 stage 1, exchange of the predictor, stage 2
 // with averaging and dt, per-run dt reduction and next dt / GLM speeds.
@@ -447,8 +453,7 @@ mf_status mf_server_create(mf_ctx* physics, double hbm_budget_bytes, int max_run
   // 4 more for the FP32 copy of W in mixed precision), face fluxes (3
   // directions) and face-normal B (3 directions) with room for 0.75 face
   // values per fab value
-  const double cell_bytes = (S->cv.p->precision == MF_PREC_MIXED) ? 28.0 : 24.0;
-  const double per = cell_bytes + 3.0 * 0.75 * S->rs * (1.0 + 1.0 / S->nc);
+  const double per = (double)cell_bytes(S) + 3.0 * 0.75 * S->rs * (1.0 + 1.0 / S->nc);
   const long long capC = (long long)(hbm_budget_bytes / per) / 64 * 64;
   const long long capF = (long long)(0.75 * capC) / 64 * 64;
   const long long capB = (long long)(0.75 * capC / S->nc) / 64 * 64 + 64 * max_runs;
@@ -514,7 +519,8 @@ long long mf_server_run_bytes(const mf_server* S, const mf_run_spec* spec) {
   if (!S || !spec_ok(S, spec)) return -1;
   mf::LevelPlan plan;
   if (plan_run(S, *spec, plan) != MF_OK) return -1;
-  return (long long)(24 * plan.total + 3 * S->rs * (fmax3(plan.fsize) + fmax3(plan.bsize)));
+  return (long long)(cell_bytes(S) * plan.total +
+                     3 * S->rs * (fmax3(plan.fsize) + fmax3(plan.bsize)));
 }
 
 mf_status mf_server_admit(mf_server* S, const mf_run_spec* spec, const double* state, int* run) {
@@ -699,7 +705,7 @@ long long mf_server_free_bytes(const mf_server* S) {
   if (!S) return -1;
   long long c = 0;
   for (const auto& kv : S->ac.free_) c = std::max(c, kv.second);
-  return 24 * c;
+  return cell_bytes(S) * c;
 }
 
 }  // extern "C"
