@@ -71,6 +71,28 @@ def test_noalloc_matches_patch_update(gpulib, case):
     ctx.close()
 
 
+def test_mixed_fp32_primitive_copy_matches_conversion(gpulib):
+    """Mixed precision: mf_patch_update's FP32 flux kernels read the FP32
+    copy of W that the primitive kernel writes; the no-allocation call has no
+    room for that copy and converts W face by face.  Both roundings are
+    round-to-nearest of the same FP64 values, so the states, the time step
+    and its cell agree bitwise."""
+    n = 16
+    p = mfgpu.helio_params(n)
+    p.precision = mfgpu.PREC_MIXED
+    ctx = mfgpu.Context(p)
+    lo, hi = mfgpu.grow([0, 0, 0], [n - 1] * 3, ctx.ng, 3)
+    U = mfgpu.init_host_fab(p, lo, hi, "helio")
+    vlo, vhi = [0, 0, 0], [n - 1] * 3
+    ta, tb = to_device(U), to_device(U)
+    sa, dta, ca = _call(ctx.lib.mf_patch_update, ctx, ta, lo, hi, vlo, vhi, 4e-3)
+    sb, dtb, cb = _call(ctx.lib.mf_patch_update_noalloc, ctx, tb, lo, hi, vlo, vhi, 4e-3)
+    assert sa == mfgpu.MF_OK and sb == mfgpu.MF_OK, (sa, sb)
+    assert np.array_equal(to_host(ta), to_host(tb))
+    assert dta == dtb and ca == cb, (dta, dtb, ca, cb)
+    ctx.close()
+
+
 def test_noalloc_rejects_patch_beyond_scratch(gpulib):
     n = 48
     p = mfgpu.helio_params(n)
