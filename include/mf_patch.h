@@ -71,20 +71,26 @@ enum { MF_TA_FIRST_ORDER = 0, MF_TA_HANCOCK = 1, MF_TA_RK2 = 2 };
 /* Precision modes.
    MF_PREC_FP64       FP64 everywhere, every operation in the reference's order
                       and rounding (no fused multiply-add): the parity path.
-   MF_PREC_MIXED      FP32 reconstruction + Riemann fluxes; state, flux
-                      accumulation, pressure recovery, positivity and charge
-                      exchange FP64.
+   MF_PREC_MIXED      FP32 reconstruction, Riemann fluxes and CFL wave speeds;
+                      conserved state, flux-divergence accumulation, pressure
+                      recovery, positivity fix and the charge-exchange rates
+                      FP64.
    MF_PREC_FP64_FAST  FP64 everywhere with fused multiply-adds and reused
                       reciprocals (results differ from MF_PREC_FP64 at the
                       rounding level; limiter and region decisions identical
-                      for identical input states). */
-enum { MF_PREC_FP64 = 0, MF_PREC_MIXED = 1, MF_PREC_FP64_FAST = 2 };
+                      for identical input states).
+   MF_PREC_MIXED_CE32 MF_PREC_MIXED with the charge-exchange rates in FP32 as
+                      well (opt-in: the rates are the dominant FP64 work of the
+                      update; the source they scale is still added to the
+                      FP64 state in FP64). */
+enum { MF_PREC_FP64 = 0, MF_PREC_MIXED = 1, MF_PREC_FP64_FAST = 2, MF_PREC_MIXED_CE32 = 3 };
 /* physical (non-periodic) boundary treatment of primitive ghost cells */
 enum { MF_BC_NONE = 0, MF_BC_FARFIELD = 1 };
 /* limiter1D::eLimiters (src/limiter1D.H:17-28) */
 enum {
   MF_LIM_CD = 0, MF_LIM_MINMOD = 1, MF_LIM_SUPERBEE = 2, MF_LIM_VANALBADA = 3,
-  MF_LIM_MC = 4, MF_LIM_HARMONIC = 5, MF_LIM_VANLEER = 9
+  MF_LIM_MC = 4, MF_LIM_HARMONIC = 5, MF_LIM_HYPERBEE = 6, MF_LIM_KOREN = 7,
+  MF_LIM_VENKATAKRISHNAN = 8, MF_LIM_VANLEER = 9, MF_LIM_WENO3 = 10, MF_LIM_WENO3YC = 11
 };
 
 #define MF_MAX_FLUIDS 5
@@ -139,7 +145,8 @@ typedef struct mf_params {
   double region_t_coeff;   /* TEMP = region_t_coeff * p / rho */
   double region_tmlim;     /* TMLIM */
   double region_zbot, region_ztop;  /* RegSafeZBot / RegSafeZTop (3D) */
-  /* inner solar-wind sphere reset after each stage (HELIOREINIT_DEFAULT, monopolar field) */
+  /* inner solar-wind sphere reset after each stage (HELIOREINIT_DEFAULT; field
+     polarity: sun_b_monopolar below) */
   int reinit_sphere;
   double reinit_r0;        /* Rinit */
   double sun_int_bc_radius;
@@ -198,6 +205,22 @@ typedef struct mf_params {
      lism_u or hot); far-field ghosts hold +1 (HELIOGS). */
   int region_tracer;
   double lism_u[3];        /* lismUX, lismUY, lismUZ: interstellar flow direction */
+  /* Growth cap of the time step that a level chains on the device
+     (AMR_MHDAM::assignDt, srcIdeal/AMR_MHDAM.cpp:1614-1624,1680; input key
+     max_dt_growth, default 1.1 at :94-95): the next dt of mf_level_step_async
+     and of a served run is min(cfl * dt_min, max_dt_growth * dt), and
+     mf_hier_assign_dt caps the next coarse dt the same way.  <= 0: no cap. */
+  double max_dt_growth;
+  /* Polarity of the inner-sphere field of HELIOREINIT_DEFAULT
+     (swlism/HeliosphericPlasmaBCF.ChF:1435-1566): 1 monopolar; 0 bipolar, the
+     reference default (HeliosphericProblem sets m_sunBmonopolar = -1 and maps
+     every value but 1 to 0, swlism/HeliosphericProblem.cpp:106,151,156).
+     Bipolar: B keeps its sign where the colatitude theta is below the
+     current-sheet colatitude thetaS(r, phi, t) and flips elsewhere, and the
+     heliospheric-current-sheet surface iHCS (the first tracking surface;
+     with the region tracer, the first of two) is set to +1 / -1 there. */
+  int sun_b_monopolar;
+  double sun_tilt;         /* sunTILT: tilt of the current sheet, degrees */
 } mf_params;
 
 struct mf_ctx;
@@ -267,19 +290,25 @@ mf_status mf_recalculate_magnetic_field(mf_ctx* ctx, mf_fab* U, const mf_fab* Uo
    (about 12.7 MiB) or a 2D single-fluid patch of about 200^2 cells. */
 #define MF_NOALLOC_SCRATCH_BYTES (16u << 20)
 
-/* mf_patch_update for callers that cannot allocate device memory: code that
-   runs inside another framework's stream capture (where cudaMalloc is not
-   allowed), processes whose device memory belongs to a pool allocator that
-   must not be bypassed, and loops that forbid allocation after start-up.
-   Same arguments, kernels and results as mf_patch_update; it calls no
-   cudaMalloc, cudaFree or other allocating routine.  Its scratch is one
-   file-scope device array of MF_NOALLOC_SCRATCH_BYTES that every GPU loading
-   the library holds until the process exits; a patch that needs more returns
-   MF_ERR_SCRATCH_LIMIT.  The first call on a device looks the array's device
-   address up (cudaGetSymbolAddress) and should come before any stream
-   capture.  All calls share the array and it keeps the last call's contents;
-   calls that overlap on the GPU race and must be serialised by the caller.
-   No counterpart in the reference (its patch update allocates per call). */
+/* mf_patch_update for callers that cannot allocate device memory: processes
+   whose device memory belongs to a pool allocator that must not be bypassed
+   (the host application owns all of HBM), and real-time or serving loops that
+   forbid allocation after start-up.  No counterpart in the reference (its
+   patch update allocates its temporaries on every call).  Same arguments and
+   results as mf_patch_update; it calls no cudaMalloc, cudaFree or other
+   allocating routine.  Its scratch is one file-scope device array of
+   MF_NOALLOC_SCRATCH_BYTES that every GPU loading the library holds until
+   the process exits; a patch that needs more returns MF_ERR_SCRATCH_LIMIT.
+   The Hancock time approximation and constrained transport (divb_cleaning
+   1-3) return MF_ERR_UNSUPPORTED.  In mixed precision the flux kernels
+   convert W to FP32 face by face instead of reading a stored FP32 copy of W
+   (the same values; the copy would not fit the array).  The first call on a
+   device looks the array's device address up (cudaGetSymbolAddress) and
+   should come before any stream capture; the device must not be reset while
+   the library is in use.  All calls share the array and it keeps the last
+   call's contents; calls that overlap on the GPU race and must be
+   serialised by the caller.  The call returns after the stream has finished
+   (a bounded wait: MF_ERR_TIMEOUT, as mf_set_wait_timeout sets). */
 mf_status mf_patch_update_noalloc(mf_ctx* ctx, mf_fab* U, const mf_box* valid, double dt,
                                   mf_fab* F, mf_fab* divB, double* new_dt, int min_cell[3],
                                   void* stream);
@@ -324,13 +353,23 @@ mf_status mf_level_compute_dt(mf_level* lev, double* dt, int* min_patch, int min
 mf_status mf_level_step(mf_level* lev, double dt, double* new_dt, int* min_patch,
                         int min_cell[3], void* stream);
 /* Enqueue one step without waiting: dt and the GLM speeds are read from the
-   device copy written by the previous step (dt = cfl * previous minimum;
+   device copy written by the previous step (dt = cfl * previous minimum,
+   capped at max_dt_growth times the previous dt as AMR_MHDAM::assignDt does;
    Ch = factor_ch*dx/min, Cp = sqrt(Ch*dx/factor_cp)).  Call
    mf_level_seed_dt first, mf_level_result to read the outcome. */
 mf_status mf_level_seed_dt(mf_level* lev, double dt, double cfl, void* stream);
 mf_status mf_level_step_async(mf_level* lev, void* stream);
 mf_status mf_level_result(mf_level* lev, double* new_dt, int* min_patch, int min_cell[3],
                           void* stream);
+/* Time of the level's state (AMRLevel::time, passed to the patch update by
+   AMRLevelIdealMHD::advance as setCurrentTime, srcIdeal/AMRLevelIdealMHD.cpp:
+   854): the start time of its next step.  A new level starts at the
+   context's current time (mf_set_current_time); every step advances it by
+   its dt (on the device for the async form).  The time enters the bipolar
+   inner-sphere field (HELIOREINIT_DEFAULT at time + stage dt).
+   mf_level_time waits for the level's queued work. */
+mf_status mf_level_set_time(mf_level* lev, double time);
+mf_status mf_level_time(mf_level* lev, double* time);
 /* Kernel launches enqueued by one mf_level_step (for accounting). */
 int mf_level_launches_per_step(const mf_level* lev);
 /* Diagnostic (no reference counterpart): one step enqueued launch by launch
@@ -390,6 +429,11 @@ mf_status mf_hier_times(const mf_hier* h, double* times);
    respect to level 0 (multiply by the CFL number for the next dt0).
    Synchronous: returns after the step finished. */
 mf_status mf_hier_step(mf_hier* h, double dt0, double* new_dt, void* stream);
+/* The next coarse time step after mf_hier_step (AMR_MHDAM::assignDt with
+   subcycling, srcIdeal/AMR_MHDAM.cpp:1570-1660): cfl times the new_dt of the
+   last step, capped at max_dt_growth (level 0's parameters) times the last
+   step's dt0.  MF_ERR_BAD_ARG before the first step. */
+mf_status mf_hier_assign_dt(const mf_hier* h, double cfl, double* dt0);
 /* The coupling operations on their own: copy the coarse values that the
    interpolation onto level+1 reads (the "old" coarse state); interpolate the
    coarse-fine ghosts of level (>= 1) with time fraction alpha between that

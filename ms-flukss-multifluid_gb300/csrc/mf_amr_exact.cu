@@ -463,6 +463,7 @@ struct mf_hier {
   std::vector<double> t, dt, ndt;
   cudaStream_t s = nullptr;
   int launches = 0;
+  double last_dt0 = 0.0, last_new_dt = 0.0;  // the last mf_hier_step (assignDt inputs)
 };
 
 static mf_status cuda_status(cudaError_t e) {
@@ -907,6 +908,7 @@ static mf_status hier_advance(mf_hier* h, int l) {
   }
   double nd = 0.0;
   int mp = 0, cell[3];
+  level_set_time_host(h->lv[l], h->t[l]);
   st = mf_level_step(h->lv[l], h->dt[l], &nd, &mp, cell, h->s);
   if (st != MF_OK) return st;
   h->ndt[l] = nd;
@@ -1075,6 +1077,21 @@ mf_status mf_hier_step(mf_hier* h, double dt0, double* new_dt, void* stream) {
     if (l == 0 || v < best) best = v;
   }
   if (new_dt) *new_dt = best;
+  h->last_dt0 = dt0;
+  h->last_new_dt = best;
+  return MF_OK;
+}
+
+mf_status mf_hier_assign_dt(const mf_hier* h, double cfl, double* dt0) {
+  if (!h || !dt0 || !(cfl > 0.0) || !(h->last_dt0 > 0.0)) return MF_ERR_BAD_ARG;
+  // AMR_MHDAM::assignDt with subcycling (srcIdeal/AMR_MHDAM.cpp:1586-1626):
+  // the minimum over the levels of cfl * dt_new[l] * refinement, i.e. cfl
+  // times mf_hier_step's new_dt, then at most max_dt_growth times the
+  // current dt of every level times its refinement, which is dt0 for all
+  const double g = level_view(h->lv[0]).p->max_dt_growth;
+  double d = cfl * h->last_new_dt;
+  if (g > 0.0) d = std::min(d, h->last_dt0 * g);
+  *dt0 = d;
   return MF_OK;
 }
 

@@ -148,8 +148,9 @@ mf_status validate_params(const mf_params& p) {
       p.time_approximation != MF_TA_HANCOCK)
     return MF_ERR_UNSUPPORTED;
   if (p.precision != MF_PREC_FP64 && p.precision != MF_PREC_MIXED &&
-      p.precision != MF_PREC_FP64_FAST)
+      p.precision != MF_PREC_FP64_FAST && p.precision != MF_PREC_MIXED_CE32)
     return MF_ERR_BAD_ARG;
+  if (!std::isfinite(p.max_dt_growth) || !std::isfinite(p.sun_tilt)) return MF_ERR_BAD_ARG;
   if (!(p.divb_cleaning == 0 || (p.divb_cleaning >= 1 && p.divb_cleaning <= 3) ||
         p.divb_cleaning == 5))
     return MF_ERR_UNSUPPORTED;
@@ -162,23 +163,16 @@ mf_status validate_params(const mf_params& p) {
   if (p.num_tracking_surfaces < 0) return MF_ERR_BAD_ARG;
   if (p.num_tracking_surfaces > 2 || num_cons(p) > MF_MAX_COMP) return MF_ERR_UNSUPPORTED;
   if (p.region_tracer && p.num_tracking_surfaces < 1) return MF_ERR_BAD_ARG;
-  if (p.num_tracking_surfaces > 0) {
-    const int l = p.limiter_ls;
-    if (!(l == MF_LIM_CD || l == MF_LIM_MINMOD || l == MF_LIM_SUPERBEE || l == MF_LIM_VANALBADA ||
-          l == MF_LIM_MC || l == MF_LIM_HARMONIC || l == MF_LIM_VANLEER))
-      return MF_ERR_UNSUPPORTED;
-  }
+  // limiter1D::eLimiters (src/limiter1D.H:17-28): every value 0..11
+  if (p.num_tracking_surfaces > 0 && (p.limiter_ls < MF_LIM_CD || p.limiter_ls > MF_LIM_WENO3YC))
+    return MF_ERR_UNSUPPORTED;
   if (p.divb_cleaning == 5) {
     // main/MHDAM.cpp:1042-1046
     if (p.use_8wave) return MF_ERR_UNSUPPORTED;
     if (!(p.flux == 1 || p.flux == 3)) return MF_ERR_UNSUPPORTED;
   }
-  for (int v = 0; v < 8; ++v) {
-    int l = p.limiter[v];
-    if (!(l == MF_LIM_CD || l == MF_LIM_MINMOD || l == MF_LIM_SUPERBEE || l == MF_LIM_VANALBADA ||
-          l == MF_LIM_MC || l == MF_LIM_HARMONIC || l == MF_LIM_VANLEER))
-      return MF_ERR_UNSUPPORTED;
-  }
+  for (int v = 0; v < 8; ++v)
+    if (p.limiter[v] < MF_LIM_CD || p.limiter[v] > MF_LIM_WENO3YC) return MF_ERR_UNSUPPORTED;
   if (p.divb_method < 0 || p.divb_method > 2) return MF_ERR_BAD_ARG;
   for (int d = 0; d < p.space_dim; ++d)
     if (p.domain_hi[d] < p.domain_lo[d]) return MF_ERR_BAD_ARG;
@@ -199,6 +193,13 @@ DevParams make_dev(const mf_params& p) {
   P.lim_ls = p.limiter_ls;
   P.reg_tracer = (p.region_tracer && P.nls > 0) ? 1 : 0;
   P.ct = (p.divb_cleaning >= 1 && p.divb_cleaning <= 3) ? p.divb_cleaning : 0;
+  P.ce32 = (p.precision == MF_PREC_MIXED_CE32) ? 1 : 0;
+  // HeliosphericProblem: every sunBmonopolar but 1 is bipolar
+  // (swlism/HeliosphericProblem.cpp:156); the current-sheet surface is the
+  // first tracking surface, the first of two with the region tracer (:616-631)
+  P.monopolar = (p.sun_b_monopolar == 1) ? 1 : 0;
+  P.ihcs = -1;
+  if (!P.monopolar && p.num_tracking_surfaces > (p.region_tracer ? 1 : 0)) P.ihcs = P.ils;
   for (int d = 0; d < 3; ++d) P.lism_u[d] = p.lism_u[d];
   P.irhon = 8 + P.glm;
   // RiemannSolver::make (src/RiemannSolver.cpp:13-112)
@@ -263,6 +264,11 @@ DevParams make_dev(const mf_params& p) {
   P.sun_b = p.sun_b;
   P.sun_beta = p.sun_beta;
   P.dir_br = p.dir_br;
+  // SETHELIOS: sunTILT = ausunTILT * d_PI_180 (swlism/HeliosphericF.ChF:66)
+  const double tilt = p.sun_tilt * (mf::kPi / 180.0);
+  P.sin_tilt = std::sin(tilt);
+  P.cos_tilt = std::cos(tilt);
+  P.max_growth = p.max_dt_growth;
   for (int q = 0; q < 8; ++q) P.bc_plasma[q] = p.bc_plasma[q];
   for (int q = 0; q < 5; ++q) P.bc_n1[q] = p.bc_neutral1[q];
   return P;
@@ -362,6 +368,7 @@ struct mf_level {
   DevBuf packed;                           // staging of the valid-cell transfers
   DevBuf Wf;                               // mixed precision: FP32 copy of W
   std::vector<long long> voff;             // packed offset of each patch (doubles)
+  double time = 0.0;                       // start time of the next step (host mirror)
 };
 
 extern "C" {
@@ -410,6 +417,9 @@ void mf_params_default(mf_params* p, int space_dim, int n_fluids) {
   p->limiter_ls = MF_LIM_MINMOD;
   p->region_tracer = 0;
   p->lism_u[0] = -1.0;
+  p->max_dt_growth = 1.1;   // srcIdeal/AMR_MHDAM.cpp:94
+  p->sun_b_monopolar = 0;   // swlism/HeliosphericProblem.cpp:106,156
+  p->sun_tilt = 0.0;        // :102
 }
 
 int mf_params_num_cons(const mf_params* p) { return p ? num_cons(*p) : 0; }
@@ -439,6 +449,9 @@ mf_status mf_create(const mf_params* p, mf_ctx** out) {
   if (!c) return MF_ERR_OOM;
   c->p = *p;
   c->dp = make_dev(*p);
+  // the FP32-rate form runs every mixed-precision path; only the update's
+  // charge-exchange rates differ (DevParams::ce32)
+  if (c->p.precision == MF_PREC_MIXED_CE32) c->p.precision = MF_PREC_MIXED;
   c->ng = num_ghost_of(*p);
   c->nc = num_cons(*p);
   c->timeout = default_timeout();
@@ -674,6 +687,7 @@ static mf_status patch_update_impl(mf_ctx* c, mf_fab* U, const mf_box* valid, do
   StepState* hs = (StepState*)c->hstate.p;
   std::memset(hs, 0, sizeof(*hs));
   hs->dt = dt;
+  hs->time = c->time;
   hs->ch = p.dedner_ch;
   hs->cp = p.dedner_cp;
   hs->cfl = 0.0;
@@ -1408,6 +1422,7 @@ mf_status mf_level_create(mf_ctx* c, int npatch, const mf_box* valid, mf_level**
   mf_level* L = new (std::nothrow) mf_level();
   if (!L) return MF_ERR_OOM;
   L->ctx = c;
+  L->time = c->time;
   L->np = npatch;
   L->valid = plan.valid;
   L->fab = plan.fab;
@@ -1681,6 +1696,7 @@ mf_status mf_level_step(mf_level* L, double dt, double* new_dt, int* min_patch, 
   StepState* hs = (StepState*)L->hstate.p;
   std::memset(hs, 0, sizeof(*hs));
   hs->dt = dt;
+  hs->time = L->time;
   hs->ch = c->p.dedner_ch;
   hs->cp = c->p.dedner_cp;
   MF_CHECK_CUDA(cudaMemcpyAsync(L->state.p, hs, sizeof(StepState), cudaMemcpyHostToDevice, L->s));
@@ -1690,6 +1706,7 @@ mf_status mf_level_step(mf_level* L, double dt, double* new_dt, int* min_patch, 
   if (st != MF_OK) return st;
   st = wait_stream(L->s, c->timeout);
   if (st != MF_OK) return st;
+  L->time = hs->time;
   decode_result(L, hs, new_dt, min_patch, min_cell);
   return flags_status(hs->flags);
 }
@@ -1726,6 +1743,7 @@ mf_status mf_level_seed_dt(mf_level* L, double dt, double cfl, void* stream) {
   StepState* hs = (StepState*)L->hstate.p;
   std::memset(hs, 0, sizeof(*hs));
   hs->dt = dt;
+  hs->time = L->time;
   hs->cfl = cfl;
   hs->ch = c->p.dedner_ch;
   hs->cp = c->p.dedner_cp;
@@ -1754,8 +1772,32 @@ mf_status mf_level_result(mf_level* L, double* new_dt, int* min_patch, int min_c
   MF_CHECK_CUDA(cudaMemcpyAsync(hs, L->state.p, sizeof(StepState), cudaMemcpyDeviceToHost, L->s));
   st = wait_stream(L->s, L->ctx->timeout);
   if (st != MF_OK) return st;
+  L->time = hs->time;
   decode_result(L, hs, new_dt, min_patch, min_cell);
   return flags_status(hs->flags);
+}
+
+mf_status mf_level_set_time(mf_level* L, double time) {
+  if (!L || !std::isfinite(time)) return MF_ERR_BAD_ARG;
+  L->time = time;
+  // the device copy, which the async steps read and advance
+  StepState* hs = (StepState*)L->hstate.p;
+  hs->time = time;
+  MF_CHECK_CUDA(cudaMemcpyAsync((char*)L->state.p + offsetof(StepState, time), &hs->time,
+                                sizeof(double), cudaMemcpyHostToDevice, L->s));
+  return wait_stream(L->s, L->ctx->timeout);
+}
+
+mf_status mf_level_time(mf_level* L, double* time) {
+  if (!L || !time) return MF_ERR_BAD_ARG;
+  StepState* hs = (StepState*)L->hstate.p;
+  MF_CHECK_CUDA(cudaMemcpyAsync(&hs->time, (const char*)L->state.p + offsetof(StepState, time),
+                                sizeof(double), cudaMemcpyDeviceToHost, L->s));
+  mf_status st = wait_stream(L->s, L->ctx->timeout);
+  if (st != MF_OK) return st;
+  L->time = hs->time;
+  *time = hs->time;
+  return MF_OK;
 }
 
 int mf_level_launches_per_step(const mf_level* L) { return L ? L->launches : -1; }
@@ -1770,6 +1812,7 @@ mf_status mf_level_profile_step(mf_level* L, double dt, float* ms, int* kinds, i
   StepState* hs = (StepState*)L->hstate.p;
   std::memset(hs, 0, sizeof(*hs));
   hs->dt = dt;
+  hs->time = L->time;
   hs->ch = c->p.dedner_ch;
   hs->cp = c->p.dedner_cp;
   mf_status st = MF_OK;
@@ -1785,6 +1828,7 @@ mf_status mf_level_profile_step(mf_level* L, double dt, float* ms, int* kinds, i
     if (st != MF_OK) break;
     st = wait_stream(L->s, c->timeout);
     if (st != MF_OK) break;
+    L->time += dt;
     for (int q = 0; q < ne; ++q) {
       float t = 0.f;
       cudaEventElapsedTime(&t, ev[q], ev[q + 1]);
@@ -1986,17 +2030,21 @@ mf_status mf_init_helio_host(const mf_params* p, const double* wp, const double*
           u[s + 3] = r * w[3];
           u[s + 4] = w[4] * invhg + 0.5 * r * ke2;
         }
-        if (p->reinit_sphere) mf::exact::reinit_cell(P, P.dx, i, j, k, u);
         // tracking surfaces: the region tracer -1 in the wind sphere, +1
         // outside (HELIOINIT, swlism/HeliosphericF.ChF:1228-1231,1302-1304);
-        // any other surface r - R0, a level set of the sphere
+        // the current-sheet surface of a bipolar field +1 (the component
+        // reset of swlism/HeliosphericProblem.cpp:2387-2393; the sphere's
+        // reset below sets +1 / -1 inside); any other surface r - R0, a
+        // level set of the sphere
         if (P.nls) {
           const double x = (i + 0.5) * P.dx - P.sun_c[0], y = (j + 0.5) * P.dx - P.sun_c[1];
           const double z = (P.sd == 3) ? (k + 0.5) * P.dx - P.sun_c[2] : 0.0;
           const double r2 = x * x + y * y + z * z;
           for (int q = P.ils; q < P.nc; ++q) u[q] = std::sqrt(r2) - P.r0;
           if (P.reg_tracer) u[P.nc - 1] = (r2 <= P.r0 * P.r0) ? -1.0 : 1.0;
+          if (P.reinit && P.ihcs >= 0) u[P.ihcs] = 1.0;
         }
+        if (p->reinit_sphere) mf::exact::reinit_cell(P, P.dx, i, j, k, 0.0, u);
         for (int q = 0; q < U->ncomp; ++q) U->data[hidx(U, i, j, k, q)] = u[q];
       }
   return MF_OK;
@@ -2013,6 +2061,7 @@ CtxView ctx_view(const mf_ctx* c) {
   v.ng = c->ng;
   v.nc = c->nc;
   v.timeout = c->timeout;
+  v.time = c->time;
   return v;
 }
 
@@ -2045,4 +2094,5 @@ void level_set_gathers(mf_level* L, const std::vector<FaceGather>& g) {
 }
 
 mf_status status_of_flags(unsigned flags) { return flags_status(flags); }
+void level_set_time_host(mf_level* L, double time) { L->time = time; }
 }  // namespace mf

@@ -329,7 +329,7 @@ __global__ void __launch_bounds__(kMaxBlock)
   };
   recalc_cell(P.sd, HX, ua, bo, ea);
   if (POST) {
-    if (P.reinit) exact::reinit_cell(P, RP.dx, i, j, k, u);
+    if (P.reinit) exact::reinit_cell(P, RP.dx, i, j, k, states[D.run].time + dt, u);
     exact::positivity_cell<8>(P, u);
     if (U0) {
 #pragma unroll

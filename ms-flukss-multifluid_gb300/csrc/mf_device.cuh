@@ -36,6 +36,10 @@ struct DevParams {
   // region tracer, lism_u the interstellar flow direction
   int ils, nls, lim_ls, reg_tracer;
   int ct;  // constrained transport: 0 off, 1 Balsara-Spicer, 2 / 3 Gardiner-Stone (2D)
+  int ce32;  // mixed precision with FP32 charge-exchange rates (MF_PREC_MIXED_CE32)
+  // inner-sphere field: 1 monopolar, 0 bipolar; ihcs: component of the
+  // current-sheet surface set by the bipolar reset (-1: none)
+  int monopolar, ihcs;
   int lim[8];
   int periodic[3], dlo[3], dhi[3];
   double gamma, hgamma, invhgamma, invgamma, smallr, smallp, del2, smallB, dx, invdx;
@@ -43,6 +47,8 @@ struct DevParams {
   double ce_scale_vel, ce_sigma_scale, ce_a, ce_b, ce_damp_c, ce_damp_pow;
   double sun_c[3], sun_r, sun_v, t_coeff, tmlim, zbot, ztop;
   double r0, rint, sun_rho, sun_p, sun_b, sun_beta, dir_br;
+  double sin_tilt, cos_tilt;  // sin / cos of the current-sheet tilt (radians)
+  double max_growth;          // assignDt growth cap of chained time steps (<= 0: none)
   double bc_plasma[8], bc_n1[5];
   double lism_u[3];
 };
@@ -51,6 +57,7 @@ struct DevParams {
 // captured CUDA graph reads the current ones.
 struct StepState {
   double dt;        // time step of the step being taken
+  double time;      // start time of the step being taken (advanced by dt after it)
   double ch, cp;    // GLM speeds
   double cfl;       // dt of the next async step = cfl * dt_min
   double dt_min;    // result: minimum of dx/cmax
@@ -59,6 +66,13 @@ struct StepState {
   unsigned flags;   // error bits (kFlag*)
   int pad;
 };
+
+// Problem time of a stage's post-processing: HeliosphericProblem::postprocessing
+// is called with the step's start time and the stage's dt and works at their
+// sum (swlism/HeliosphericProblem.cpp:2399-2405).
+__device__ __forceinline__ double stage_time(const StepState& ss, double dt_stage) {
+  return ss.time + dt_stage;
+}
 
 // Values that differ between the runs of one batch (independent simulations,
 // or AMR levels, stepped in shared launches): grid spacing, domain extent in
@@ -101,6 +115,12 @@ struct StageDesc {
   long long fv_off[3];
 };
 
+// Plasma state and current-sheet surface value of the inner-sphere reset.
+struct ReinitState {
+  double u[8];
+  double hcs;
+};
+
 // Per-block partial of the dt reduction.
 struct DtPartial {
   double dt;
@@ -114,7 +134,7 @@ struct DtPartial {
 template <typename R> __device__ __forceinline__ R rmax(R a, R b) { return fmax(a, b); }
 template <typename R> __device__ __forceinline__ R rmin(R a, R b) { return fmin(a, b); }
 template <typename R> __device__ __forceinline__ R rabs(R a) { return fabs(a); }
-template <typename R> __device__ __forceinline__ R rsqrt_(R a) { return sqrt(a); }
+template <typename R> __device__ __forceinline__ R sqrt_r(R a) { return sqrt(a); }
 
 // ---------------------------------------------------------------------------
 // VFRoe MHD flux: VFROE_FLUXES (src/VFRoeF.ChF:327-658) with arithmetic
@@ -147,10 +167,10 @@ __device__ __forceinline__ void vfroe_mhd(const DevParams& P, const R* wl, const
   const R cc = gamma * PGas / Rho;
   const R bb = i4pi * BX2 / Rho;
   const R szb = cc + (BxBH + BxBH) / Rho;
-  const R h = rsqrt_<R>(szb * szb - R(4) * cc * bb);
+  const R h = sqrt_r<R>(szb * szb - R(4) * cc * bb);
   const R aaf = R(0.5) * (szb + h);
   const R aas = cc * bb / aaf;
-  const R b = rsqrt_<R>(bb), c = rsqrt_<R>(cc), af = rsqrt_<R>(aaf), as = rsqrt_<R>(aas);
+  const R b = sqrt_r<R>(bb), c = sqrt_r<R>(cc), af = sqrt_r<R>(aaf), as = sqrt_r<R>(aas);
   const R eig[9] = {R(0), U, U, U + b, U - b, U + af, U - af, U + as, U - as};
   // alphas
   R alphaF, alphaS;
@@ -165,15 +185,15 @@ __device__ __forceinline__ void vfroe_mhd(const DevParams& P, const R* wl, const
     alphaF = R(1);
     alphaS = R(0);
   } else {
-    alphaF = rsqrt_<R>((cc - aas) / dfs);
-    alphaS = rsqrt_<R>((aaf - cc) / dfs);
+    alphaF = sqrt_r<R>((cc - aas) / dfs);
+    alphaS = sqrt_r<R>((aaf - cc) / dfs);
   }
   R betaY, betaZ;
   if (BYZ2 < R(P.smallB) * R(P.smallB)) {
     betaY = sq2;
     betaZ = sq2;
   } else {
-    const R hyz = rsqrt_<R>(BYZ2);
+    const R hyz = sqrt_r<R>(BYZ2);
     betaY = BY / hyz;
     betaZ = BZ / hyz;
   }
@@ -190,12 +210,12 @@ __device__ __forceinline__ void vfroe_mhd(const DevParams& P, const R* wl, const
   a[1] = dRho - dP / cc;
   a[2] = BXR - BXL;
   R h1 = sq2 * (betaY * dUt2 - betaZ * dUt1);
-  R h2 = siBX * (betaZ * dBt1 - betaY * dBt2) / (R(2) * rsqrt_<R>(R(2) * pi * Rho));
+  R h2 = siBX * (betaZ * dBt1 - betaY * dBt2) / (R(2) * sqrt_r<R>(R(2) * pi * Rho));
   a[3] = h1 + h2;
   a[4] = h1 - h2;
   h1 = dP / (R(2) * Rho * cc);
   h2 = dUn / (R(2) * cc);
-  const R h3 = (betaY * dBt1 + betaZ * dBt2) / (R(4) * c * rsqrt_<R>(pi * Rho));
+  const R h3 = (betaY * dBt1 + betaZ * dBt2) / (R(4) * c * sqrt_r<R>(pi * Rho));
   const R h4 = siBX * (betaY * dUt1 + betaZ * dUt2) / (R(2) * cc);
   a[5] = alphaF * (h1 + af * h2) + alphaS * (h3 - as * h4);
   a[6] = alphaF * (h1 - af * h2) + alphaS * (h3 + as * h4);
@@ -209,7 +229,7 @@ __device__ __forceinline__ void vfroe_mhd(const DevParams& P, const R* wl, const
   const R a34p = a[3] + a[4], a34m = a[3] - a[4];
   const R a56p = a[5] + a[6], a56m = a[5] - a[6];
   const R a78p = a[7] + a[8], a78m = a[7] - a[8];
-  const R DN = R(2) * rsqrt_<R>(pi * Rho);
+  const R DN = R(2) * sqrt_r<R>(pi * Rho);
   const R HRho = Rho * (alphaF * a56p + alphaS * a78p);
   const R HU = alphaS * as * a56m - alphaF * af * a78m;
   const R HB = c * (alphaS * a56p - alphaF * a78p);
@@ -269,8 +289,9 @@ __device__ __forceinline__ void cons_to_prim_euler(const DevParams& P, const dou
 }
 
 // ---------------------------------------------------------------------------
-// limited face values (src/reconstructionF.ChF): returns the value on the
-// low face (lo) and on the high face (hi) of the centre cell
+// limited face values (src/reconstructionF.ChF, every limiter of
+// limiter1D::make, src/limiter1D.cpp:21-63): returns the value on the low
+// face (lo) and on the high face (hi) of the centre cell
 // ---------------------------------------------------------------------------
 template <typename R>
 __device__ __forceinline__ R minmod_(R A, R B) {  // reconstructionF.ChF:5-13
@@ -316,6 +337,51 @@ __device__ __forceinline__ void face_values(int lim, R wm1, R wp, R wp1, R& lo, 
       slope = dWR / (R(1) + dWR / dWL);
       break;
     }
+    case MF_LIM_HYPERBEE: {  // :430-464
+      if (dWL * dWR <= R(0)) { lo = wp; hi = wp; return; }
+      const R A = R(1) + sqrt_r<R>(dWR / dWL);
+      slope = dWR / (A * A);
+      slope = slope + slope;
+      break;
+    }
+    case MF_LIM_KOREN: {  // :883-918
+      const R dSave = R(1.0e-10);
+      if (dWL * dWR <= R(0)) { lo = wp; hi = wp; return; }
+      const R H = dWL * dWR / (R(2) * (dWL * dWL + dWR * dWR + dSave) - dWL * dWR);
+      lo = wp - (dWL + R(0.5) * dWR) * H;
+      hi = wp + (dWR + R(0.5) * dWL) * H;
+      return;
+    }
+    case MF_LIM_VENKATAKRISHNAN: {  // :950-988
+      const R dSave = R(1.0e-10), dSave2 = R(1.0e-10 * 1.0e-10);
+      if (dWL * dWR <= R(0)) { lo = wp; hi = wp; return; }
+      const R H = (dWR + dWL) / (R(6) * (dWR * dWR + dWL * dWL + dSave2));
+      lo = wp - (dWR + R(2) * dWL) * (dWL + dSave) * H;
+      hi = wp + (dWL + R(2) * dWR) * (dWR + dSave) * H;
+      return;
+    }
+    case MF_LIM_WENO3: {  // :1096-1136
+      const R dSave = R(1.0e-6);
+      const R BR = dWR * dWR + dSave, AR = R(1) / (BR * BR);
+      const R BL = dWL * dWL + dSave, AL = R(1) / (BL * BL);
+      R H = AR / (AR + R(2) * AL);
+      lo = wp - R(0.5) * (dWL + H * (dWR - dWL));
+      H = AL / (AL + R(2) * AR);
+      hi = wp + R(0.5) * (dWR - H * (dWR - dWL));
+      return;
+    }
+    case MF_LIM_WENO3YC: {  // :1169-1212
+      const R dSave = R(1.0e-6);
+      const R BR = dWR * dWR + dSave, BL = dWL * dWL + dSave;
+      R D2P = dWR - dWL;
+      D2P = D2P * D2P;
+      const R AL = R(1) + D2P / BL, AR = R(1) + D2P / BR;
+      R H = AR / (AR + R(2) * AL);
+      lo = wp - R(0.5) * (dWL + H * (dWR - dWL));
+      H = AL / (AL + R(2) * AR);
+      hi = wp + R(0.5) * (dWR - H * (dWR - dWL));
+      return;
+    }
     case MF_LIM_VANLEER: {  // :794-841
       const R dSLim = R(1.0 / 3.0);
       const R BT = (R(3) - dSLim) / (R(1) - dSLim);
@@ -354,9 +420,10 @@ __device__ __forceinline__ R minmod3_(R A, R B, R C) {  // reconstructionF.ChF:1
 }
 
 // *FACESLOPES of one variable (reconstructionF.ChF: MINMOD :157-178,
-// SUPERBEE :356-392, HARMONIC :526-550, VANALBADA :591-622, MC :664-697,
-// VANLEER :843-880, CD :1081-1096): Sleft/Sright in = left/right
-// differences, out = limited slopes.
+// SUPERBEE :356-392, HYPERBEE :466-490, HARMONIC :526-550, VANALBADA
+// :591-622, MC :664-697, VANLEER :843-880, KOREN :920-948, VENKATAKRISHNAN
+// :990-1021, CD :1081-1096, WENO3 :1138-1167, WENO3YC :1214-1246):
+// Sleft/Sright in = left/right differences, out = limited slopes.
 template <typename R>
 __device__ __forceinline__ void face_slopes(int lim, R& Sleft, R& Sright) {
   const R dSR = Sright, dSL = Sleft;
@@ -392,6 +459,59 @@ __device__ __forceinline__ void face_slopes(int lim, R& Sleft, R& Sright) {
         else SLOPE = dSR;
       }
       break;
+    case MF_LIM_HYPERBEE:  // :466-490
+      if (dSL * dSR > R(0)) {
+        const R A = R(1) + sqrt_r<R>(dSR / dSL);
+        SLOPE = dSR / (A * A);
+        SLOPE = SLOPE + SLOPE;
+      }
+      break;
+    case MF_LIM_KOREN: {  // :920-948
+      const R dSave = R(1.0e-10);
+      R SLOPL = R(0), SLOPR = R(0);
+      if (dSL * dSR > R(0)) {
+        const R H = dSL * dSR / (R(2) * (dSL * dSL + dSR * dSR + dSave) - dSL * dSR);
+        SLOPL = (dSL + R(0.5) * dSR) * H;
+        SLOPR = (dSR + R(0.5) * dSL) * H;
+      }
+      Sleft = SLOPL;
+      Sright = SLOPR;
+      return;
+    }
+    case MF_LIM_VENKATAKRISHNAN: {  // :990-1021
+      const R dSave = R(1.0e-10), dSave2 = R(1.0e-10 * 1.0e-10);
+      R SLOPL = R(0), SLOPR = R(0);
+      if (dSL * dSR > R(0)) {
+        const R H = (dSR + dSL) / (R(6) * (dSR * dSR + dSL * dSL + dSave2));
+        SLOPL = (dSR + R(2) * dSL) * (dSL + dSave) * H;
+        SLOPR = (dSL + R(2) * dSR) * (dSR + dSave) * H;
+      }
+      Sleft = SLOPL;
+      Sright = SLOPR;
+      return;
+    }
+    case MF_LIM_WENO3: {  // :1138-1167
+      const R dSave = R(1.0e-6);
+      const R BR = dSR * dSR + dSave, AR = R(1) / (BR * BR);
+      const R BL = dSL * dSL + dSave, AL = R(1) / (BL * BL);
+      R H = AR / (AR + R(2) * AL);
+      Sleft = R(0.5) * (dSL + H * (dSR - dSL));
+      H = AL / (AL + R(2) * AR);
+      Sright = R(0.5) * (dSR - H * (dSR - dSL));
+      return;
+    }
+    case MF_LIM_WENO3YC: {  // :1214-1246
+      const R dSave = R(1.0e-6);
+      const R BR = dSR * dSR + dSave, BL = dSL * dSL + dSave;
+      R D2P = dSR - dSL;
+      D2P = D2P * D2P;
+      const R AL = R(1) + D2P / BL, AR = R(1) + D2P / BR;
+      R H = AR / (AR + R(2) * AL);
+      Sleft = R(0.5) * (dSL + H * (dSR - dSL));
+      H = AL / (AL + R(2) * AR);
+      Sright = R(0.5) * (dSR - H * (dSR - dSL));
+      return;
+    }
     case MF_LIM_VANLEER: {
       const R dSLim = R(1.0 / 3.0);
       const R BT = (R(3) - dSLim) / (R(1) - dSLim);

@@ -13,6 +13,7 @@ struct CtxView {
   const DevParams* dp;
   int ng, nc;
   double timeout;  // bounded host waits (seconds)
+  double time;     // current time (PatchMHDAM::setCurrentTime)
 };
 
 // Parameters, device parameters, ghost width and component count of a context.
@@ -90,5 +91,8 @@ struct LevelView {
 LevelView level_view(mf_level* L);
 // Replace the face gathers a level step runs (drops the cached step graphs).
 void level_set_gathers(mf_level* L, const std::vector<FaceGather>& g);
+// Start time of the level's next synchronous step (host mirror only; the
+// synchronous step uploads it with the step's dt).
+void level_set_time_host(mf_level* L, double time);
 
 }  // namespace mf

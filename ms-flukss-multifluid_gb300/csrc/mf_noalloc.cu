@@ -1,22 +1,28 @@
 // mf_noalloc.cu - a patch update that allocates nothing.
 //
-// Some callers cannot call cudaMalloc when they advance a patch: code running
-// inside another framework's CUDA stream capture (allocation is not permitted
-// while a stream is being captured), processes whose device memory is fully
-// handed to a pool allocator that must not be bypassed, and real-time loops
-// that forbid allocation after start-up.  mf_patch_update_noalloc serves them:
-// it runs the same kernels as mf_patch_update, with every scratch buffer
-// (RK2 predictor, primitive state, face fluxes, face-normal B, stage
-// descriptors, step state, dt partials) carved from one file-scope device
-// array of MF_NOALLOC_SCRATCH_BYTES.  The caller still passes the state, the
-// optional flux and divB outputs and the stream.
+// Some callers cannot call cudaMalloc when they advance a patch: processes
+// whose device memory is handed in full to a pool allocator that must not be
+// bypassed (the host application owns every byte of HBM), and real-time or
+// serving loops that forbid any allocation after start-up (an allocation can
+// synchronise the device and stalls the loop for an unbounded time).
+// mf_patch_update_noalloc serves them: it runs the same kernels as
+// mf_patch_update, with every scratch buffer (RK2 predictor, primitive
+// state, face fluxes, face-normal B, stage descriptors, step state, dt
+// partials) carved from one file-scope device array of
+// MF_NOALLOC_SCRATCH_BYTES.  The caller still passes the state, the optional
+// flux and divB outputs and the stream.
 //
 // The array is loaded with the library's device code, so every GPU that loads
-// the library holds it until the process exits.  All calls share it and it
-// keeps the last call's contents; the step state (error flags included) is
-// rewritten at the start of every call, and everything else is fully written
-// before it is read.  Calls that overlap on the GPU (same device, different
-// streams or threads) race on the array and must be serialised by the caller.
+// the library holds it until the process exits.  Its device address is looked
+// up once per device, at the first call on that device with the device
+// current (cudaGetSymbolAddress); that first call should come before any
+// stream capture, and the device must not be reset (cudaDeviceReset) while
+// the library is in use, since the address is kept.  All calls share the
+// array and it keeps the last call's contents; the step state (error flags
+// included) is rewritten at the start of every call, and everything else is
+// fully written before it is read.  Calls that overlap on the GPU (same
+// device, different streams or threads) race on the array and must be
+// serialised by the caller.
 #include <cmath>
 #include <cstring>
 #include <mutex>
@@ -210,6 +216,7 @@ extern "C" mf_status mf_patch_update_noalloc(mf_ctx* ctx, mf_fab* U, const mf_bo
   StepState hs;
   std::memset(&hs, 0, sizeof(hs));
   hs.dt = dt;
+  hs.time = cv.time;
   hs.ch = p.dedner_ch;
   hs.cp = p.dedner_cp;
   StageDesc* dd = (StageDesc*)(base + o_desc);
@@ -304,9 +311,12 @@ extern "C" mf_status mf_patch_update_noalloc(mf_ctx* ctx, mf_fab* U, const mf_bo
     }
     NA_CUDA(mf::launch_flux_out(mixed, sd, nc, f2p, f2lo, f2n, f1p, f1lo, f1n, fo, olo, on, s));
   }
-  // a copy into pageable memory returns once the data has arrived
+  // bounded wait for the step (MF_ERR_TIMEOUT after the context's wait
+  // limit, as every host wait of the library), then the step state: a copy
+  // into pageable memory returns once the data has arrived
+  st = mf::host_wait(s, cv.timeout);
+  if (st != MF_OK) return st;
   NA_CUDA(cudaMemcpyAsync(&hs, ds, sizeof(hs), cudaMemcpyDeviceToHost, s));
-  NA_CUDA(cudaStreamSynchronize(s));
   if (new_dt) *new_dt = hs.dt_min;
   if (min_cell) {
     const int n0 = valid->hi[0] - valid->lo[0] + 1, n1 = valid->hi[1] - valid->lo[1] + 1;

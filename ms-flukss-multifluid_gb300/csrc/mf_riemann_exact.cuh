@@ -52,7 +52,7 @@ __device__ __forceinline__ void roe_mhd(const DevParams& P, const R* wl, const R
   R Rho, U, V, W, BX, BY, BZ, BX2, BYZ2, BxBH, kk, cc;
   if (P.aver == 1) {
     R HL = (EL + PL) / RhoL, HR = (ER + PR) / RhoR;
-    R coefRL = R(1) / (R(1) + rsqrt_<R>(RhoR / RhoL));
+    R coefRL = R(1) / (R(1) + sqrt_r<R>(RhoR / RhoL));
     R coefRR = R(1) - coefRL;
     Rho = RhoR * coefRL + RhoL * coefRR;
     U = UL * coefRL + UR * coefRR;
@@ -90,10 +90,10 @@ __device__ __forceinline__ void roe_mhd(const DevParams& P, const R* wl, const R
   }
 
   R bb = i4pi * BX2 / Rho;
-  R b = rsqrt_<R>(bb);
+  R b = sqrt_r<R>(bb);
   if (cc < ccmi) cc = ccmi;
   if (cc > ccma) cc = ccma;
-  R c = rsqrt_<R>(cc);
+  R c = sqrt_r<R>(cc);
 
   R hyy, hzz, aaf, aas, af, as;
   const R smallB = R(P.smallB);
@@ -103,18 +103,18 @@ __device__ __forceinline__ void roe_mhd(const DevParams& P, const R* wl, const R
     if (bb > cc) { aaf = bb; aas = cc; af = b; as = c; }
     else { aaf = cc; aas = bb; af = c; as = b; }
   } else {
-    R hyz = rsqrt_<R>(BYZ2);
+    R hyz = sqrt_r<R>(BYZ2);
     hyy = BY / hyz;
     hzz = BZ / hyz;
     R szb = cc + (BxBH + BxBH) / Rho;
-    R h = rsqrt_<R>(szb * szb - R(4) * cc * bb);
+    R h = sqrt_r<R>(szb * szb - R(4) * cc * bb);
     aas = R(0.5) * (szb - h);
     if (aas <= R(0)) { aas = R(0); as = R(0); }
     else if (aas >= cc) { aas = cc; as = c; }
-    else { as = rsqrt_<R>(aas); }
+    else { as = sqrt_r<R>(aas); }
     aaf = R(0.5) * (szb + h);
     if (aaf <= cc) { aaf = cc; af = c; }
-    else { af = rsqrt_<R>(aaf); }
+    else { af = sqrt_r<R>(aaf); }
   }
 
   // entropy-fixed speeds (Roe8 numbering: 1 entropy, 2 div-B, 3/4 Alfven,
@@ -137,7 +137,7 @@ __device__ __forceinline__ void roe_mhd(const DevParams& P, const R* wl, const R
   if (dfs < R(1.0e-8)) { alf = R(1); als = R(0); }
   else if ((cc - aas) <= R(0)) { alf = R(0); als = R(1); }
   else if ((aaf - cc) <= R(0)) { alf = R(1); als = R(0); }
-  else { alf = rsqrt_<R>((cc - aas) / dfs); als = rsqrt_<R>((aaf - cc) / dfs); }
+  else { alf = sqrt_r<R>((cc - aas) / dfs); als = sqrt_r<R>((aaf - cc) / dfs); }
 
   R sih = R(-1);
   if (BX >= R(0)) sih = R(1);
@@ -174,8 +174,8 @@ __device__ __forceinline__ void roe_mhd(const DevParams& P, const R* wl, const R
   du3 = (-V * du1 + du3) / Rho;
   du4 = (-W * du1 + du4) / Rho;
 
-  const R sqPiRho = rsqrt_<R>(R(kPi) * Rho);
-  const R sq2PiRho = rsqrt_<R>(R(k2Pi) * Rho);
+  const R sqPiRho = sqrt_r<R>(R(kPi) * Rho);
+  const R sq2PiRho = sqrt_r<R>(R(k2Pi) * Rho);
 
   // left eigenvectors (non-zero entries only)
   R so15 = -R(1) / cc;
@@ -282,7 +282,7 @@ __device__ __forceinline__ void rusanov_mhd(const DevParams& P, const R* wl, con
   R Rho, U, BX2, BxBH, A2;
   if (P.aver == 1) {
     R HL = (EL + PL) / RhoL, HR = (ER + PR) / RhoR;
-    R coefRL = R(1) / (R(1) + rsqrt_<R>(RhoR / RhoL));
+    R coefRL = R(1) / (R(1) + sqrt_r<R>(RhoR / RhoL));
     R coefRR = R(1) - coefRL;
     Rho = RhoR * coefRL + RhoL * coefRR;
     U = UL * coefRL + UR * coefRR;
@@ -313,9 +313,9 @@ __device__ __forceinline__ void rusanov_mhd(const DevParams& P, const R* wl, con
   }
   R bb = i4pi * BX2 / Rho;
   R szb = A2 + (BxBH + BxBH) / Rho;
-  R h = rsqrt_<R>(szb * szb - R(4) * A2 * bb);
+  R h = sqrt_r<R>(szb * szb - R(4) * A2 * bb);
   R aaf = R(0.5) * (szb + h);
-  R af = rsqrt_<R>(aaf);
+  R af = sqrt_r<R>(aaf);
   R em = rabs<R>(U) + af;
   g[0] = R(0.5) * (RUL + RUR + em * (RhoL - RhoR));
   g[in] = R(0.5) * ((UL * RUL - BXL_4PI * BXL + PL) + (UR * RUR - BXR_4PI * BXR + PR) + em * (RUL - RUR));
@@ -353,7 +353,7 @@ __device__ __forceinline__ void vanleer_euler(const DevParams& P, const R* wl, c
   R RUL = RhoL * UL, RVL = RhoL * VL, RWL = RhoL * WL;
   R RUxUL = R(0.5) * (RUL * UL + RVL * VL + RWL * WL);
   R EL = PGasL / hgamma + RUxUL;
-  R AL = rsqrt_<R>(gamma * PGasL / RhoL);
+  R AL = sqrt_r<R>(gamma * PGasL / RhoL);
   if (UL <= -AL) {
     fr1 = fr2 = fr3 = fr4 = fr5 = R(0);
   } else if (UL >= AL) {
@@ -377,7 +377,7 @@ __device__ __forceinline__ void vanleer_euler(const DevParams& P, const R* wl, c
   R RUR = RhoR * UR, RVR = RhoR * VR, RWR = RhoR * WR;
   R RUxUR = R(0.5) * (RUR * UR + RVR * VR + RWR * WR);
   R ER = PGasR / hgamma + RUxUR;
-  R AR = rsqrt_<R>(gamma * PGasR / RhoR);
+  R AR = sqrt_r<R>(gamma * PGasR / RhoR);
   if (UR >= AR) {
     fl1 = fl2 = fl3 = fl4 = fl5 = R(0);
   } else if (UR <= -AR) {

@@ -227,11 +227,65 @@ __device__ __forceinline__ void charge_exchange_add(const DevParams& P, const do
   }
 }
 
-// HELIOREINIT_DEFAULT (swlism/HeliosphericPlasmaBCF.ChF:1435-1555) with a
-// monopolar field: the plasma in r <= Rinit becomes the radial wind.  The
-// membership test uses non-fused arithmetic (host and device agree exactly).
+// HELIOREINIT_DEFAULT (swlism/HeliosphericPlasmaBCF.ChF:1435-1566): the
+// plasma in r <= Rinit becomes the radial wind at time t (the stage's start
+// time plus its dt); bipolar field: B flips where the colatitude is not
+// below the current sheet's, and the current-sheet surface takes +1 / -1.
+// The wind state of a cell inside the sphere, out of line: only the few
+// cells of the sphere execute it.
+static __device__ __host__ __noinline__ void reinit_state(const DevParams& P, double x,
+                                                          double y, double z, double r2,
+                                                          double t, ReinitState& o) {
+  o.hcs = 0.0;
+  const double r = sqrt(r2);
+  const double rr = r / P.rint;
+  const double xy = sqrt(x * x + y * y);
+  const double cosT = z / r;
+  const double sinT = sqrt(fmax(0.0, 1.0 - cosT * cosT));
+  const double cosF = x / xy;
+  const double sinF = y / xy;
+  const double rho = P.sun_rho / (rr * rr);
+  const double ux = P.sun_v * sinT * cosF;
+  const double uy = P.sun_v * sinT * sinF;
+  const double uz = P.sun_v * cosT;
+  const double pr = P.sun_p / pow(rr, 2.0 * P.gamma);
+  const double br = P.dir_br * P.sun_b / (rr * rr);
+  const double bp = -P.sun_beta * br * r * sinT;
+  double bx = br * sinT * cosF - bp * sinF;
+  double by = br * sinT * sinF + bp * cosF;
+  double bz = br * cosT;
+  const double b = bx * bx + by * by + bz * bz;
+  const double e0 = pr / P.hgamma + 0.5 * (rho * P.sun_v * P.sun_v + kInv4Pi * b);
+  if (!P.monopolar) {
+    const double theta = acos(cosT);
+    const double ph = P.sun_beta * (r - P.sun_v * t);
+    const double cosBr = cos(ph), sinBr = sin(ph);
+    const double sinB = sinF * cosBr + cosF * sinBr;
+    const double cosB = cosF * cosBr - sinF * sinBr;
+    const double ct = P.cos_tilt * cosB;
+    const double thetaS = asin(P.sin_tilt * sinB / sqrt(ct * ct + sinB * sinB)) + 0.5 * kPi;
+    const bool keep = theta < thetaS;
+    if (!keep) {
+      bx = -bx;
+      by = -by;
+      bz = -bz;
+    }
+    o.hcs = keep ? 1.0 : -1.0;
+  }
+  o.u[0] = rho;
+  o.u[1] = rho * ux;
+  o.u[2] = rho * uy;
+  o.u[3] = rho * uz;
+  o.u[4] = e0;
+  o.u[5] = bx;
+  o.u[6] = by;
+  o.u[7] = bz;
+}
+
+// The reset of one cell: the membership test in non-fused arithmetic (host
+// and device agree exactly), then the wind state.
 __device__ __host__ inline void reinit_cell(const DevParams& P, double dx, int i, int j, int k,
-                                            double* u) {
+                                            double t, double* u) {
 #ifdef __CUDA_ARCH__
   const double x = __dadd_rn(__dmul_rn(i + 0.5, dx), -P.sun_c[0]);
   const double y = __dadd_rn(__dmul_rn(j + 0.5, dx), -P.sun_c[1]);
@@ -247,33 +301,16 @@ __device__ __host__ inline void reinit_cell(const DevParams& P, double dx, int i
   const double r2 = (P.sd == 3) ? (x * x + y * y + z * z) : (x * x + y * y);
   if (!(r2 <= P.r0 * P.r0)) return;
 #endif
-  const double r = sqrt(r2);
-  const double rr = r / P.rint;
-  const double xy = sqrt(x * x + y * y);
-  const double cosT = z / r;
-  const double sinT = sqrt(fmax(0.0, 1.0 - cosT * cosT));
-  const double cosF = x / xy;
-  const double sinF = y / xy;
-  const double rho = P.sun_rho / (rr * rr);
-  const double ux = P.sun_v * sinT * cosF;
-  const double uy = P.sun_v * sinT * sinF;
-  const double uz = P.sun_v * cosT;
-  const double pr = P.sun_p / pow(rr, 2.0 * P.gamma);
-  const double br = P.dir_br * P.sun_b / (rr * rr);
-  const double bp = -P.sun_beta * br * r * sinT;
-  const double bx = br * sinT * cosF - bp * sinF;
-  const double by = br * sinT * sinF + bp * cosF;
-  const double bz = br * cosT;
-  const double b = bx * bx + by * by + bz * bz;
-  const double e0 = pr / P.hgamma + 0.5 * (rho * P.sun_v * P.sun_v + kInv4Pi * b);
-  u[0] = rho;
-  u[1] = rho * ux;
-  u[2] = rho * uy;
-  u[3] = rho * uz;
-  u[4] = e0;
-  u[5] = bx;
-  u[6] = by;
-  u[7] = bz;
+  ReinitState o;
+  reinit_state(P, x, y, z, r2, t, o);
+#pragma unroll
+  for (int q = 0; q < 8; ++q) u[q] = o.u[q];
+  if (!P.monopolar) {
+    // static indices keep u in registers (ihcs is -1 or a surface component)
+#pragma unroll
+    for (int q = 8; q < MF_MAX_COMP; ++q)
+      if (q == P.ihcs) u[q] = o.hcs;
+  }
 }
 
 // POSTPROCESSING (srcIdeal/PatchIdealMHDF.ChF:1019-1070) and POSTPROCESSING_MF

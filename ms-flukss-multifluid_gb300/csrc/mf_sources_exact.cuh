@@ -201,15 +201,16 @@ __device__ __forceinline__ void charge_exchange_add(const DevParams& P, const do
   }
 }
 
-// HELIOREINIT_DEFAULT (swlism/HeliosphericPlasmaBCF.ChF:1435-1555), monopolar field.
-__device__ __host__ inline void reinit_cell(const DevParams& P, double dx, int i, int j, int k,
-                                            double* u) {
-  double x = (i + 0.5) * dx - P.sun_c[0];
-  double y = (j + 0.5) * dx - P.sun_c[1];
-  double z = 0.0;
-  if (P.sd == 3) z = (k + 0.5) * dx - P.sun_c[2];
-  double r2 = (P.sd == 3) ? (x * x + y * y + z * z) : (x * x + y * y);
-  if (!(r2 <= P.r0 * P.r0)) return;
+// HELIOREINIT_DEFAULT (swlism/HeliosphericPlasmaBCF.ChF:1435-1566) at time t
+// (the stage's start time plus its dt), in the routine's order of
+// operations; sunBmonopolar != 1: the bipolar field (sign by theta < thetaS)
+// and the current-sheet surface iHCS (:1537-1564).
+// The wind state of a cell inside the sphere, out of line: only the few
+// cells of the sphere execute it.
+static __device__ __host__ __noinline__ void reinit_state(const DevParams& P, double x,
+                                                          double y, double z, double r2,
+                                                          double t, ReinitState& o) {
+  o.hcs = 0.0;
   double r = sqrt(r2);
   double rr = r / P.rint;
   double xy = sqrt(x * x + y * y);
@@ -229,14 +230,50 @@ __device__ __host__ inline void reinit_cell(const DevParams& P, double dx, int i
   double bz = br * cosT;
   double b = bx * bx + by * by + bz * bz;
   double e0 = pr / P.hgamma + 0.5 * (rho * P.sun_v * P.sun_v + kInv4Pi * b);
-  u[0] = rho;
-  u[1] = rho * ux;
-  u[2] = rho * uy;
-  u[3] = rho * uz;
-  u[4] = e0;
-  u[5] = bx;
-  u[6] = by;
-  u[7] = bz;
+  if (!P.monopolar) {
+    double theta = acos(cosT);
+    double cosBr = cos(P.sun_beta * (r - P.sun_v * t));
+    double sinBr = sin(P.sun_beta * (r - P.sun_v * t));
+    double sinB = sinF * cosBr + cosF * sinBr;
+    double cosB = cosF * cosBr - sinF * sinBr;
+    double thetaS = P.sin_tilt * sinB / sqrt((P.cos_tilt * cosB) * (P.cos_tilt * cosB) + sinB * sinB);
+    thetaS = asin(thetaS) + 0.5 * kPi;
+    if (!(theta < thetaS)) {
+      bx = -bx;
+      by = -by;
+      bz = -bz;
+    }
+    o.hcs = (theta < thetaS) ? 1.0 : -1.0;
+  }
+  o.u[0] = rho;
+  o.u[1] = rho * ux;
+  o.u[2] = rho * uy;
+  o.u[3] = rho * uz;
+  o.u[4] = e0;
+  o.u[5] = bx;
+  o.u[6] = by;
+  o.u[7] = bz;
+}
+
+// The reset of one cell: the membership test, then the wind state.
+__device__ __host__ inline void reinit_cell(const DevParams& P, double dx, int i, int j, int k,
+                                            double t, double* u) {
+  double x = (i + 0.5) * dx - P.sun_c[0];
+  double y = (j + 0.5) * dx - P.sun_c[1];
+  double z = 0.0;
+  if (P.sd == 3) z = (k + 0.5) * dx - P.sun_c[2];
+  double r2 = (P.sd == 3) ? (x * x + y * y + z * z) : (x * x + y * y);
+  if (!(r2 <= P.r0 * P.r0)) return;
+  ReinitState o;
+  reinit_state(P, x, y, z, r2, t, o);
+#pragma unroll
+  for (int q = 0; q < 8; ++q) u[q] = o.u[q];
+  if (!P.monopolar) {
+    // static indices keep u in registers (ihcs is -1 or a surface component)
+#pragma unroll
+    for (int q = 8; q < MF_MAX_COMP; ++q)
+      if (q == P.ihcs) u[q] = o.hcs;
+  }
 }
 
 // POSTPROCESSING (srcIdeal/PatchIdealMHDF.ChF:1019-1070) and POSTPROCESSING_MF

@@ -13,18 +13,30 @@ cudaError_t launch_update_fast(const DevParams& P, const StageBuffers& B, const 
   const int nt = b.nt[2];
   const unsigned gv = flat_blocks(b.tot_v, nt);
   if (nblocks_v) *nblocks_v = (int)gv;
-#define MF_UPD(G, FL)                                                                    \
-  k_update<R, G, FL><<<gv, nt, 0, s>>>(P, B, b.desc, b.ndesc, b.tot_v, b.runs, state, \
-                                       dt_scale, partials)
+  // charge-exchange rates: FP64, or FP32 in the opt-in MF_PREC_MIXED_CE32 form
+#define MF_UPD(G, FL, CE)                                                                    \
+  k_update<R, G, FL, CE><<<gv, nt, 0, s>>>(P, B, b.desc, b.ndesc, b.tot_v, b.runs, state, \
+                                           dt_scale, partials)
+#define MF_UPD_CE(G, FL)                      \
+  do {                                        \
+    if constexpr (sizeof(R) == 4) {           \
+      if (P.ce32) {                           \
+        MF_UPD(G, FL, float);                 \
+        break;                                \
+      }                                       \
+    }                                         \
+    MF_UPD(G, FL, double);                    \
+  } while (0)
   if (P.glm) {
-    if (flags == 0) MF_UPD(1, 0);
-    else if (flags == kStageDt) MF_UPD(1, kStageDt);
-    else MF_UPD(1, kStageAverage | kStageDt);
+    if (flags == 0) MF_UPD_CE(1, 0);
+    else if (flags == kStageDt) MF_UPD_CE(1, kStageDt);
+    else MF_UPD_CE(1, kStageAverage | kStageDt);
   } else {
-    if (flags == 0) MF_UPD(0, 0);
-    else if (flags == kStageDt) MF_UPD(0, kStageDt);
-    else MF_UPD(0, kStageAverage | kStageDt);
+    if (flags == 0) MF_UPD_CE(0, 0);
+    else if (flags == kStageDt) MF_UPD_CE(0, kStageDt);
+    else MF_UPD_CE(0, kStageAverage | kStageDt);
   }
+#undef MF_UPD_CE
 #undef MF_UPD
   return cudaGetLastError();
 }

@@ -51,9 +51,9 @@ __device__ __forceinline__ bool part_less(const DtPartial& a, const DtPartial& b
   return a.idx < b.idx;
 }
 
-// One block per run: the minimum over the run's block partials, then the
-// run's next dt and GLM speeds (AMRLevelIdealMHD::advance,
-// srcIdeal/AMRLevelIdealMHD.cpp:1531-1548, 1588).
+// One block per run: the minimum over the run's block partials, the run's
+// time after the step, then (advance) its next dt and GLM speeds
+// (AMRLevelIdealMHD::advance, srcIdeal/AMRLevelIdealMHD.cpp:1531-1548, 1588).
 __global__ void __launch_bounds__(256)
     k_finalize(const DevParams P, const DtPartial* __restrict__ parts,
                const RunParams* __restrict__ runs, int nt, StepState* __restrict__ states,
@@ -83,9 +83,17 @@ __global__ void __launch_bounds__(256)
     ss->min_desc = (best.desc == INT_MAX) ? INT_MAX : best.desc - R.d0;
     ss->min_idx = best.idx;
     if (!(best.dt > 0.0) || best.dt >= DBL_MAX) atomicOr(&ss->flags, kFlagBadDt);
+    // the level's time after the step (AMRLevelIdealMHD::advance, :1587)
+    const double dt_step = ss->dt;
+    ss->time = ss->time + dt_step;
     if (advance) {
       const double dtn = best.dt;
-      ss->dt = ss->cfl * dtn;
+      // AMR_MHDAM::assignDt (srcIdeal/AMR_MHDAM.cpp:1675-1681): the next dt is
+      // cfl * dt_min, grown at most by max_dt_growth over the step's dt (a
+      // run's first dt, reduced before it has taken a step, is not capped)
+      double next = ss->cfl * dtn;
+      if (P.max_growth > 0.0 && dt_step > 0.0) next = fmin(next, dt_step * P.max_growth);
+      ss->dt = next;
       if (P.glm && P.factor_ch > 0.0) {
         const double ch = P.factor_ch * R.dx / dtn;
         ss->ch = ch;

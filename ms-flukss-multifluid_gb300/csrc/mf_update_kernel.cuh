@@ -102,7 +102,29 @@ __device__ __forceinline__ void block_dt_min(double dtc, int myidx,
   }
 }
 
-template <typename R, int GLM, int FLAGS>
+// GLM damping factor exp(-dt Ch^2 / Cp^2) of PSIPARABOLIC (src/DednerF.ChF:
+// 65-87) for the run of the calling warp: one evaluation per warp instead of
+// one per cell (the same expression on the same values), by the first lane
+// with a cell, broadcast by shuffle.  A warp never holds cells of two runs
+// (each run's cells start on a multiple of kRunAlign); every lane calls.
+__device__ __forceinline__ double warp_psi_damping(const StageDesc* Dp,
+                                                   const StepState* __restrict__ states,
+                                                   double dt_scale) {
+  const unsigned m = __ballot_sync(0xffffffffu, Dp != nullptr);
+  if (!m) return 1.0;
+  const int src = __ffs(m) - 1;
+  double v = 1.0;
+  if ((int)(threadIdx.x & 31) == src) {
+    const StepState& S = states[Dp->run];
+    const double dt = S.dt * dt_scale;
+    v = exp(-dt * S.ch * S.ch / (S.cp * S.cp));
+  }
+  return __shfl_sync(0xffffffffu, v, src);
+}
+
+// CE: arithmetic type of the charge-exchange rates (double, or float in the
+// MF_PREC_MIXED_CE32 form); R: type of the face fluxes.
+template <typename R, int GLM, int FLAGS, typename CE = double>
 __global__ void __launch_bounds__(kMaxBlock, sizeof(R) == 4 ? 2 : 1)
     k_update(const DevParams P, const StageBuffers B, const StageDesc* __restrict__ descs,
              int ndesc, int total, const RunParams* __restrict__ runs,
@@ -119,6 +141,7 @@ __global__ void __launch_bounds__(kMaxBlock, sizeof(R) == 4 ? 2 : 1)
     lin = g - Dp->g0[kRegV];
     if (lin >= Dp->vn[0] * Dp->vn[1] * Dp->vn[2]) Dp = nullptr;  // run-alignment gap
   }
+  const double psi_damp = GLM ? warp_psi_damping(Dp, states, dt_scale) : 1.0;
   if (Dp) {
     const StageDesc& D = *Dp;
     const RunParams& RP = runs[D.run];
@@ -134,8 +157,16 @@ __global__ void __launch_bounds__(kMaxBlock, sizeof(R) == 4 ? 2 : 1)
     for (int q = 0; q < MF_MAX_COMP; ++q)
       if (q < P.nc) u[q] = B.uin[base + q * cs];
 
-    // UPDATECONS (src/PatchMHDAMF.ChF:542-587), one direction after another
+    // UPDATECONS (src/PatchMHDAMF.ChF:542-587), one direction after another.
+    // FP32 fluxes (mixed precision): the differences of the directions are
+    // summed in FP32 and enter the FP64 state once per component, so that
+    // each component costs one conversion instead of one per direction.
     const double dtinv = dt * RP.invdx;
+    float fsum[sizeof(R) == 4 ? MF_MAX_COMP : 1];
+    if constexpr (sizeof(R) == 4) {
+#pragma unroll
+      for (int q = 0; q < MF_MAX_COMP; ++q) fsum[q] = 0.0f;
+    }
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
       if (d < P.sd) {
@@ -145,10 +176,16 @@ __global__ void __launch_bounds__(kMaxBlock, sizeof(R) == 4 ? 2 : 1)
         const long long sf = (d == 0) ? 1 : (d == 1) ? (long long)fnb[0]
                                                      : (long long)fnb[0] * fnb[1];
         const R* __restrict__ Fd = (const R*)B.f[d] + D.f_off[d] + loc(D.vlo, fnb, i, j, k);
+        if constexpr (sizeof(R) == 4) {
 #pragma unroll
-        for (int q = 0; q < MF_MAX_COMP; ++q)
-          if (q < P.ils)
-            u[q] = u[q] - dtinv * flux_diff(Fd[q * fcs + sf], Fd[q * fcs]);
+          for (int q = 0; q < MF_MAX_COMP; ++q)
+            if (q < P.ils) fsum[q] = fsum[q] + (Fd[q * fcs + sf] - Fd[q * fcs]);
+        } else {
+#pragma unroll
+          for (int q = 0; q < MF_MAX_COMP; ++q)
+            if (q < P.ils)
+              u[q] = u[q] - dtinv * flux_diff(Fd[q * fcs + sf], Fd[q * fcs]);
+        }
         // UPDATELEVELSET (src/LevelSetF.ChF:200-234): the tracking surfaces,
         // non-conservative with the stage-start cell velocity
         if (P.nls) {
@@ -160,6 +197,11 @@ __global__ void __launch_bounds__(kMaxBlock, sizeof(R) == 4 ? 2 : 1)
               u[q] = u[q] - cf * flux_diff(Fd[q * fcs + sf], Fd[q * fcs]);
         }
       }
+    }
+    if constexpr (sizeof(R) == 4) {
+#pragma unroll
+      for (int q = 0; q < MF_MAX_COMP; ++q)
+        if (q < P.ils) u[q] = u[q] - dtinv * (double)fsum[q];
     }
 
     // addExplicitSources (srcIdeal/PatchMHDMF.cpp:1149-1389) with the
@@ -181,7 +223,10 @@ __global__ void __launch_bounds__(kMaxBlock, sizeof(R) == 4 ? 2 : 1)
           const long long sf = (d == 0) ? 1 : (d == 1) ? (long long)fnb[0]
                                                        : (long long)fnb[0] * fnb[1];
           const R* __restrict__ Bd = (const R*)B.bn[d] + D.bn_off[d] + loc(D.vlo, fnb, i, j, k);
-          divB = divB + (double)Bd[sf] - (double)Bd[0];  // COMPUTEDIVB
+          if constexpr (sizeof(R) == 4)
+            divB = divB + (double)(Bd[sf] - Bd[0]);  // COMPUTEDIVB, FP32 difference
+          else
+            divB = divB + (double)Bd[sf] - (double)Bd[0];  // COMPUTEDIVB
         }
       }
       // SOURCE8WAVES (srcIdeal/PatchIdealMHDF.ChF:681-722) + ADDSOURCES
@@ -197,19 +242,16 @@ __global__ void __launch_bounds__(kMaxBlock, sizeof(R) == 4 ? 2 : 1)
       u[6] = u[6] + dB * Uy;
       u[7] = u[7] + dB * Uz;
     }
-    if (GLM) {  // PSIPARABOLIC (src/DednerF.ChF:65-87)
-      const double ch = ss->ch, cp = ss->cp;
-      u[8] = exp(-dt * ch * ch / (cp * cp)) * u[8];
-    }
+    if (GLM) u[8] = psi_damp * u[8];  // PSIPARABOLIC (src/DednerF.ChF:65-87)
     if (P.ce && P.nf >= 2) {
       const double regtr = P.reg_tracer ? B.w[base + (P.nc - 1) * cs] : 0.0;
       const int reg = region_cell(P, RP.dx, i, j, k, w, regtr);
-      charge_exchange_add<IRHON, R>(P, w, reg, dt, u);
+      charge_exchange_add<IRHON, CE>(P, w, reg, dt, u);
     }
     // problem post-processing and positivity (src/PatchMHDAM.cpp:705-707); with
     // constrained transport they follow the recalculation of B (k_recalc_b)
     if (!P.ct) {
-      if (P.reinit) reinit_cell(P, RP.dx, i, j, k, u);
+      if (P.reinit) reinit_cell(P, RP.dx, i, j, k, stage_time(*ss, dt), u);
       positivity_cell<IRHON>(P, u);
     }
     if (P.nls) {  // POSTPROCESSING_LS (srcIdeal/PatchMHDMF.cpp:1414-1424)

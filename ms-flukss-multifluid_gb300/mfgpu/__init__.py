@@ -32,10 +32,13 @@ MF_ERR_NO_ROOM = 9
 NOALLOC_SCRATCH_BYTES = 16 << 20
 
 TA_FIRST_ORDER, TA_HANCOCK, TA_RK2 = 0, 1, 2
-PREC_FP64, PREC_MIXED, PREC_FP64_FAST = 0, 1, 2
+PREC_FP64, PREC_MIXED, PREC_FP64_FAST, PREC_MIXED_CE32 = 0, 1, 2, 3
 BC_NONE, BC_FARFIELD = 0, 1
 LIM_CD, LIM_MINMOD, LIM_SUPERBEE, LIM_VANALBADA, LIM_MC, LIM_HARMONIC, LIM_VANLEER = (
     0, 1, 2, 3, 4, 5, 9)
+LIM_HYPERBEE, LIM_KOREN, LIM_VENKATAKRISHNAN, LIM_WENO3, LIM_WENO3YC = 6, 7, 8, 10, 11
+LIMITERS = (LIM_CD, LIM_MINMOD, LIM_SUPERBEE, LIM_VANALBADA, LIM_MC, LIM_HARMONIC, LIM_HYPERBEE,
+            LIM_KOREN, LIM_VENKATAKRISHNAN, LIM_VANLEER, LIM_WENO3, LIM_WENO3YC)
 MAX_COMP = 29
 
 c_int3 = ctypes.c_int * 3
@@ -114,6 +117,9 @@ class MfParams(ctypes.Structure):
         ("limiter_ls", ctypes.c_int),
         ("region_tracer", ctypes.c_int),
         ("lism_u", ctypes.c_double * 3),
+        ("max_dt_growth", ctypes.c_double),
+        ("sun_b_monopolar", ctypes.c_int),
+        ("sun_tilt", ctypes.c_double),
     ]
 
 
@@ -188,6 +194,8 @@ _SIGS = {
     "mf_level_step_async": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "mf_level_result": (ctypes.c_int, [ctypes.c_void_p, _P(ctypes.c_double), _P(ctypes.c_int),
                                        c_int3, ctypes.c_void_p]),
+    "mf_level_set_time": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double]),
+    "mf_level_time": (ctypes.c_int, [ctypes.c_void_p, _P(ctypes.c_double)]),
     "mf_level_launches_per_step": (ctypes.c_int, [ctypes.c_void_p]),
     "mf_level_profile_step": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double,
                                              _P(ctypes.c_float), _P(ctypes.c_int),
@@ -218,6 +226,8 @@ _SIGS = {
     "mf_hier_times": (ctypes.c_int, [ctypes.c_void_p, _P(ctypes.c_double)]),
     "mf_hier_step": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double, _P(ctypes.c_double),
                                     ctypes.c_void_p]),
+    "mf_hier_assign_dt": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double,
+                                         _P(ctypes.c_double)]),
     "mf_hier_snapshot": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]),
     "mf_hier_fill_ghosts": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_double,
                                            ctypes.c_void_p]),
@@ -345,6 +355,9 @@ def _base_params(space_dim: int, n_fluids: int) -> MfParams:
     p.limiter_ls = LIM_MINMOD
     p.region_tracer = 0
     p.lism_u[0] = -1.0
+    p.max_dt_growth = 1.1
+    p.sun_b_monopolar = 0
+    p.sun_tilt = 0.0
     return p
 
 
@@ -536,6 +549,9 @@ class Context:
     def set_dedner(self, ch, cp):
         check(self.lib.mf_set_dedner(self.h, ch, cp), "mf_set_dedner")
 
+    def set_current_time(self, t):
+        check(self.lib.mf_set_current_time(self.h, t), "mf_set_current_time")
+
     def _edges(self, E):
         """EdgeBox fabs (list of (device pointer, lo, hi), 3 in 3D, 1 in 2D)."""
         arr = (MfFab * 3)()
@@ -703,6 +719,14 @@ class Level:
         st = self.lib.mf_level_result(self.h, ctypes.byref(ndt), ctypes.byref(ip), cell, stream)
         return st, ndt.value, ip.value, tuple(cell)
 
+    def set_time(self, t):
+        check(self.lib.mf_level_set_time(self.h, t), "mf_level_set_time")
+
+    def time(self):
+        t = ctypes.c_double()
+        check(self.lib.mf_level_time(self.h, ctypes.byref(t)), "mf_level_time")
+        return t.value
+
     def launches_per_step(self):
         return self.lib.mf_level_launches_per_step(self.h)
 
@@ -768,6 +792,13 @@ class Hier:
         nd = ctypes.c_double()
         check(self.lib.mf_hier_step(self.h, dt0, ctypes.byref(nd), stream), "mf_hier_step")
         return nd.value
+
+    def assign_dt(self, cfl):
+        """mf_hier_assign_dt: the next dt0 (cfl * new_dt of the last step,
+        capped at max_dt_growth times the last dt0)."""
+        d = ctypes.c_double()
+        check(self.lib.mf_hier_assign_dt(self.h, cfl, ctypes.byref(d)), "mf_hier_assign_dt")
+        return d.value
 
     def snapshot(self, level, stream=None):
         check(self.lib.mf_hier_snapshot(self.h, level, stream), "mf_hier_snapshot")

@@ -30,6 +30,7 @@
 #define D_SQRT_2 0.707106781186547524400844362104849039
 #define D_PI 3.14159265358979323846264338327950288
 #define D_2PI 6.28318530717958647692528676655900576
+#define D_PI_2 1.57079632679489661923132169163975144
 /* srcIdeal/EosCommon.fh:31-37 */
 #define NETF2_DENS 1.0e-6
 #define NETF2_PRES 1.0e-8
@@ -135,6 +136,10 @@ typedef struct {
   int rs, aver;
   double gamma, hgamma, invhgamma, smallr, smallp, del2, smallB;
   double dCh, dCp;
+  /* inner-sphere field: monopolar (sunBmonopolar == 1) or bipolar with the
+     current-sheet surface ihcs (-1: none) and the sheet's tilt */
+  int monopolar, ihcs;
+  double sin_tilt, cos_tilt;
 } Ctx;
 
 /* EqSysMHDMF ctor (srcIdeal/EqSysMHDMF.cpp:11-48) and RiemannSolver::make
@@ -176,6 +181,18 @@ static int ctx_init(Ctx* c, const mf_params* p) {
   c->smallB = p->small_b;
   c->dCh = p->dedner_ch;
   c->dCp = p->dedner_cp;
+  /* HeliosphericProblem (swlism/HeliosphericProblem.cpp:156, 616-631):
+     every sunBmonopolar but 1 means bipolar; iHCS is the first tracking
+     surface (the first of two with the region tracer) */
+  c->monopolar = (p->sun_b_monopolar == 1);
+  c->ihcs = -1;
+  if (!c->monopolar && c->nls > (p->region_tracer ? 1 : 0)) c->ihcs = c->ils;
+  {
+    /* SETHELIOS: sunTILT in radians (swlism/HeliosphericF.ChF:66) */
+    double tilt = p->sun_tilt * (D_PI / 180.0);
+    c->sin_tilt = sin(tilt);
+    c->cos_tilt = cos(tilt);
+  }
   int f = p->flux;
   if (c->glm) {
     if (!(f == 1 || f == 3)) return MF_ERR_UNSUPPORTED;
@@ -277,9 +294,12 @@ static double minmod(double A, double B) {
 /* One cell, one variable: returns Wleft (value on the low face) and Wright
    (value on the high face) from W(i-1), W(i), W(i+1).
    MINMODFACEVALUES :126-155, SUPERBEEFACEVALUES :258-301,
-   VANALBADAFACEVALUES :550-589, MCFACEVALUES :622-661,
-   HARMONICFACEVALUES :492-524, VANLEERFACEVALUES :794-841,
-   CDFACEVALUES :1056-1079. */
+   HYPERBEEFACEVALUES :430-464, VANALBADAFACEVALUES :550-589,
+   MCFACEVALUES :622-661, HARMONICFACEVALUES :492-524,
+   VANLEERFACEVALUES :794-841, KORENFACEVALUES :883-918,
+   VENKATAKRISHNANFACEVALUES :950-988, CDFACEVALUES :1056-1079,
+   WENO3FACEVALUES :1096-1136, WENO3YCFACEVALUES :1169-1212; dispatch of
+   limiter1D::make (src/limiter1D.cpp:21-63). */
 static void face_values(int lim, double Wm1, double WP, double Wp1, double* WL, double* WR) {
   double dWR = Wp1 - WP;
   double dWL = WP - Wm1;
@@ -339,6 +359,67 @@ static void face_values(int lim, double Wm1, double WP, double Wp1, double* WL, 
       }
       SLOPE = dWR / (1.0 + dWR / dWL);
       break;
+    case MF_LIM_HYPERBEE: {
+      double A;
+      if (dWL * dWR <= 0.0) {
+        *WL = WP;
+        *WR = WP;
+        return;
+      }
+      A = 1.0 + sqrt(dWR / dWL);
+      SLOPE = dWR / (A * A);
+      SLOPE = SLOPE + SLOPE;
+      break;
+    }
+    case MF_LIM_KOREN: {
+      const double dSave = 1.0e-10;
+      double H;
+      if (dWL * dWR <= 0.0) {
+        *WL = WP;
+        *WR = WP;
+        return;
+      }
+      H = dWL * dWR / (2.0 * (dWL * dWL + dWR * dWR + dSave) - dWL * dWR);
+      *WL = WP - (dWL + 0.5 * dWR) * H;
+      *WR = WP + (dWR + 0.5 * dWL) * H;
+      return;
+    }
+    case MF_LIM_VENKATAKRISHNAN: {
+      const double dSave = 1.0e-10, dSave2 = dSave * dSave;
+      double H;
+      if (dWL * dWR <= 0.0) {
+        *WL = WP;
+        *WR = WP;
+        return;
+      }
+      H = (dWR + dWL) / (6.0 * (dWR * dWR + dWL * dWL + dSave2));
+      *WL = WP - (dWR + 2.0 * dWL) * (dWL + dSave) * H;
+      *WR = WP + (dWL + 2.0 * dWR) * (dWR + dSave) * H;
+      return;
+    }
+    case MF_LIM_WENO3: {
+      const double dSave = 1.0e-6;
+      double BR = dWR * dWR + dSave, AR = 1.0 / (BR * BR);
+      double BL = dWL * dWL + dSave, AL = 1.0 / (BL * BL);
+      double H = AR / (AR + 2.0 * AL);
+      *WL = WP - 0.5 * (dWL + H * (dWR - dWL));
+      H = AL / (AL + 2.0 * AR);
+      *WR = WP + 0.5 * (dWR - H * (dWR - dWL));
+      return;
+    }
+    case MF_LIM_WENO3YC: {
+      const double dSave = 1.0e-6;
+      double BR = dWR * dWR + dSave, BL = dWL * dWL + dSave;
+      double D2P = dWR - dWL, AL, AR, H;
+      D2P = D2P * D2P;
+      AL = 1.0 + D2P / BL;
+      AR = 1.0 + D2P / BR;
+      H = AR / (AR + 2.0 * AL);
+      *WL = WP - 0.5 * (dWL + H * (dWR - dWL));
+      H = AL / (AL + 2.0 * AR);
+      *WR = WP + 0.5 * (dWR - H * (dWR - dWL));
+      return;
+    }
     case MF_LIM_VANLEER: {
       const double dSLim = 1.0 / 3.0;
       const double BT = (3.0 - dSLim) / (1.0 - dSLim);
@@ -393,9 +474,11 @@ static double minmod3(double A, double B, double C) {
 
 /* *FACESLOPES: limited slopes of one variable from the left and right
    differences (src/reconstructionF.ChF: MINMODFACESLOPES :157-178,
-   SUPERBEEFACESLOPES :356-392, HARMONICFACESLOPES :526-550,
-   VANALBADAFACESLOPES :591-622, MCFACESLOPES :664-697,
-   VANLEERFACESLOPES :843-880, CDFACESLOPES :1081-1096). */
+   SUPERBEEFACESLOPES :356-392, HYPERBEEFACESLOPES :466-490,
+   HARMONICFACESLOPES :526-550, VANALBADAFACESLOPES :591-622,
+   MCFACESLOPES :664-697, VANLEERFACESLOPES :843-880, KORENFACESLOPES
+   :920-948, VENKATAKRISHNANFACESLOPES :990-1021, CDFACESLOPES :1081-1096,
+   WENO3FACESLOPES :1138-1167, WENO3YCFACESLOPES :1214-1246). */
 static void face_slopes(int lim, double* Sleft, double* Sright) {
   double dSR = *Sright, dSL = *Sleft, SLOPE = 0.0;
   switch (lim) {
@@ -436,6 +519,60 @@ static void face_slopes(int lim, double* Sleft, double* Sright) {
           SLOPE = dSR;
       }
       break;
+    case MF_LIM_HYPERBEE:
+      if (dSL * dSR > 0.0) {
+        double A = 1.0 + sqrt(dSR / dSL);
+        SLOPE = dSR / (A * A);
+        SLOPE = SLOPE + SLOPE;
+      }
+      break;
+    case MF_LIM_KOREN: {
+      const double dSave = 1.0e-10;
+      double SLOPL = 0.0, SLOPR = 0.0;
+      if (dSL * dSR > 0.0) {
+        double H = dSL * dSR / (2.0 * (dSL * dSL + dSR * dSR + dSave) - dSL * dSR);
+        SLOPL = (dSL + 0.5 * dSR) * H;
+        SLOPR = (dSR + 0.5 * dSL) * H;
+      }
+      *Sleft = SLOPL;
+      *Sright = SLOPR;
+      return;
+    }
+    case MF_LIM_VENKATAKRISHNAN: {
+      const double dSave = 1.0e-10, dSave2 = dSave * dSave;
+      double SLOPL = 0.0, SLOPR = 0.0;
+      if (dSL * dSR > 0.0) {
+        double H = (dSR + dSL) / (6.0 * (dSR * dSR + dSL * dSL + dSave2));
+        SLOPL = (dSR + 2.0 * dSL) * (dSL + dSave) * H;
+        SLOPR = (dSL + 2.0 * dSR) * (dSR + dSave) * H;
+      }
+      *Sleft = SLOPL;
+      *Sright = SLOPR;
+      return;
+    }
+    case MF_LIM_WENO3: {
+      const double dSave = 1.0e-6;
+      double BR = dSR * dSR + dSave, AR = 1.0 / (BR * BR);
+      double BL = dSL * dSL + dSave, AL = 1.0 / (BL * BL);
+      double H = AR / (AR + 2.0 * AL);
+      *Sleft = 0.5 * (dSL + H * (dSR - dSL));
+      H = AL / (AL + 2.0 * AR);
+      *Sright = 0.5 * (dSR - H * (dSR - dSL));
+      return;
+    }
+    case MF_LIM_WENO3YC: {
+      const double dSave = 1.0e-6;
+      double BR = dSR * dSR + dSave, BL = dSL * dSL + dSave;
+      double D2P = dSR - dSL, AL, AR, H;
+      D2P = D2P * D2P;
+      AL = 1.0 + D2P / BL;
+      AR = 1.0 + D2P / BR;
+      H = AR / (AR + 2.0 * AL);
+      *Sleft = 0.5 * (dSL + H * (dSR - dSL));
+      H = AL / (AL + 2.0 * AR);
+      *Sright = 0.5 * (dSR - H * (dSR - dSL));
+      return;
+    }
     case MF_LIM_VANLEER: {
       const double dSLim = 1.0 / 3.0;
       const double BT = (3.0 - dSLim) / (1.0 - dSLim);
@@ -2080,9 +2217,14 @@ static void charge_exchange_cell(const Ctx* c, const double* W, int reg, double 
   }
 }
 
-/* HELIOREINIT_DEFAULT (swlism/HeliosphericPlasmaBCF.ChF:1435-1555) with a
-   monopolar field: the plasma inside r <= Rinit is reset to the radial wind. */
-static void reinit_cell(const Ctx* c, int i, int j, int k, double* U) {
+/* HELIOREINIT_DEFAULT (swlism/HeliosphericPlasmaBCF.ChF:1435-1566): the
+   plasma inside r <= Rinit is reset to the radial wind at time t
+   (HeliosphericProblem::postprocessing passes the stage's time plus its dt,
+   swlism/HeliosphericProblem.cpp:2399-2405).  With sunBmonopolar != 1 the
+   field is bipolar: it keeps its sign where the colatitude theta is below
+   the current sheet's thetaS and flips elsewhere, and the current-sheet
+   surface iHCS is set to +1 / -1 (:1537-1564). */
+static void reinit_cell(const Ctx* c, int i, int j, int k, double t, double* U) {
   const mf_params* p = c->p;
   double dx = p->dx;
   double x = (i + 0.5) * dx - p->sun_center[0];
@@ -2111,6 +2253,24 @@ static void reinit_cell(const Ctx* c, int i, int j, int k, double* U) {
   double bz = br * cosT;
   double b = bx * bx + by * by + bz * bz;
   double e0 = pr / c->hgamma + 0.5 * (rho * p->sun_v * p->sun_v + D_1_4PI * b);
+  if (!c->monopolar) {
+    double theta = acos(cosT);
+    double cosBr = cos(p->sun_beta * (r - p->sun_v * t));
+    double sinBr = sin(p->sun_beta * (r - p->sun_v * t));
+    double sinB = sinF * cosBr + cosF * sinBr;
+    double cosB = cosF * cosBr - sinF * sinBr;
+    double thetaS =
+        c->sin_tilt * sinB / sqrt((c->cos_tilt * cosB) * (c->cos_tilt * cosB) + sinB * sinB);
+    thetaS = asin(thetaS) + D_PI_2;
+    if (theta < thetaS) {
+      /* the field as computed */
+    } else {
+      bx = -bx;
+      by = -by;
+      bz = -bz;
+    }
+    if (c->ihcs >= 0) U[c->ihcs] = (theta < thetaS) ? 1.0 : -1.0;
+  }
   U[0] = rho;
   U[1] = rho * ux;
   U[2] = rho * uy;
@@ -2592,7 +2752,7 @@ static int euler_step(const Ctx* c, double time, Fab* U, Fab* F /* [sd] or NULL 
                       double dt, mf_box a_box, Edges* Eout /* nullable */) {
   const mf_params* p = c->p;
   const int sd = c->sd, nc = c->nc, np = c->nprim;
-  (void)time;
+
   mf_box UBox = U->b;
   /* With a far-field boundary the primitive ghosts outside the domain come
      from the boundary state; otherwise the caller filled U's ghosts. */
@@ -2776,7 +2936,7 @@ static int euler_step(const Ctx* c, double time, Fab* U, Fab* F /* [sd] or NULL 
   /* problem postprocessing, then positivity (src/PatchMHDAM.cpp:705-707) */
   FOR_BOX(valueBox, i, j, k) {
     for (int q = 0; q < nc; ++q) u[q] = AT(U, i, j, k, q);
-    if (p->reinit_sphere) reinit_cell(c, i, j, k, u);
+    if (p->reinit_sphere) reinit_cell(c, i, j, k, time + dt, u);
     positivity_cell(c, u);
     for (int q = 0; q < nc; ++q) AT(U, i, j, k, q) = u[q];
   }
@@ -2988,7 +3148,7 @@ static int hancock_step(const Ctx* c, double time, Fab* U, Fab* F, Fab* divBout,
                         mf_box a_box, Edges* Eout) {
   const mf_params* p = c->p;
   const int sd = c->sd, nc = c->nc, np = c->nprim;
-  (void)time;
+
   mf_box UBox = U->b;
   mf_box WBoxB = (p->bc_kind == MF_BC_FARFIELD) ? box_and_domain(UBox, p) : UBox;
   const double dtp = 0.5 * dt;
@@ -3101,7 +3261,7 @@ static int hancock_step(const Ctx* c, double time, Fab* U, Fab* F, Fab* divBout,
   double u[MF_MAX_COMP];
   FOR_BOX(vb2, i, j, k) {
     for (int q = 0; q < nc; ++q) u[q] = AT(U, i, j, k, q);
-    if (p->reinit_sphere) reinit_cell(c, i, j, k, u);
+    if (p->reinit_sphere) reinit_cell(c, i, j, k, time + dt, u);
     positivity_cell(c, u);
     for (int q = 0; q < nc; ++q) AT(U, i, j, k, q) = u[q];
   }
@@ -3533,6 +3693,18 @@ int mf_oracle_level_step(const mf_params* p, double time, int npatch, mf_fab* Uf
 /* ------------------------------------------------------------------------ */
 /* single-point entry points for known-answer tests                          */
 /* ------------------------------------------------------------------------ */
+
+int mf_oracle_face_values(int lim, double wm1, double wp, double wp1, double* lo, double* hi) {
+  if (!lo || !hi) return MF_ERR_BAD_ARG;
+  face_values(lim, wm1, wp, wp1, lo, hi);
+  return MF_OK;
+}
+
+int mf_oracle_face_slopes(int lim, double* sleft, double* sright) {
+  if (!sleft || !sright) return MF_ERR_BAD_ARG;
+  face_slopes(lim, sleft, sright);
+  return MF_OK;
+}
 
 int mf_oracle_face_flux(const mf_params* p, int dir, const double* wl, const double* wr,
                         double* f) {

@@ -81,6 +81,11 @@ int mf_oracle_average_down(const mf_params* pc, const mf_params* pf, int ratio, 
    wl / wr: primitive states (nprim entries, W layout); f: fluxes (ncons). */
 int mf_oracle_face_flux(const mf_params* p, int dir, const double* wl, const double* wr,
                         double* f);
+/* One limiter on one cell: *FACEVALUES from W(i-1), W(i), W(i+1) (lo: value
+   on the low face, hi: on the high face), and *FACESLOPES in place on the
+   left / right differences (src/reconstructionF.ChF). */
+int mf_oracle_face_values(int lim, double wm1, double wp, double wp1, double* lo, double* hi);
+int mf_oracle_face_slopes(int lim, double* sleft, double* sright);
 int mf_oracle_cons_to_prim(const mf_params* p, const double* u, double* w);
 /* HELIOBC (swlism/HeliosphericF.ChF:221-910) on one face of the domain
    boundary: the face fluxes of (wl, wr) by the configured solvers, then the

@@ -65,6 +65,9 @@ def load():
                                                 ctypes.c_int * 3]),
         "mf_oracle_face_flux": (ctypes.c_int, [_P(MfParams), ctypes.c_int, _DP, _DP, _DP]),
         "mf_oracle_cons_to_prim": (ctypes.c_int, [_P(MfParams), _DP, _DP]),
+        "mf_oracle_face_values": (ctypes.c_int, [ctypes.c_int, ctypes.c_double,
+                                                 ctypes.c_double, ctypes.c_double, _DP, _DP]),
+        "mf_oracle_face_slopes": (ctypes.c_int, [ctypes.c_int, _DP, _DP]),
         "mf_oracle_helio_bc_face": (ctypes.c_int, [_P(MfParams), ctypes.c_int, ctypes.c_int, _DP,
                                                    _DP, _DP, _DP]),
         "mf_oracle_charge_exchange": (ctypes.c_int, [_P(MfParams), _DP, ctypes.c_int,
@@ -216,6 +219,22 @@ def face_flux(p: MfParams, direction: int, wl, wr):
     st = lib.mf_oracle_face_flux(ctypes.byref(p), direction, _dp(wl), _dp(wr), _dp(f))
     assert st == 0, st
     return f
+
+
+def face_values(lim: int, wm1: float, wp: float, wp1: float):
+    """(lo, hi): the limiter's values on the low and high face of the cell."""
+    lo, hi = ctypes.c_double(), ctypes.c_double()
+    st = load().mf_oracle_face_values(lim, wm1, wp, wp1, ctypes.byref(lo), ctypes.byref(hi))
+    assert st == 0
+    return lo.value, hi.value
+
+
+def face_slopes(lim: int, sleft: float, sright: float):
+    """(left, right) limited slopes from the left and right differences."""
+    a, b = ctypes.c_double(sleft), ctypes.c_double(sright)
+    st = load().mf_oracle_face_slopes(lim, ctypes.byref(a), ctypes.byref(b))
+    assert st == 0
+    return a.value, b.value
 
 
 def cons_to_prim(p: MfParams, u):

@@ -14,8 +14,7 @@ import mfgpu
 from helpers import orszag_patch, periodic_fill, rel_err, to_device, to_host, valid_view
 
 RTOL = 1e-12
-LIMS = [mfgpu.LIM_MINMOD, mfgpu.LIM_SUPERBEE, mfgpu.LIM_VANALBADA, mfgpu.LIM_MC,
-        mfgpu.LIM_HARMONIC, mfgpu.LIM_VANLEER, mfgpu.LIM_CD]
+LIMS = list(mfgpu.LIMITERS)
 
 
 def _case(n, ta=mfgpu.TA_RK2, lim=mfgpu.LIM_MINMOD, tvd=0, prec=mfgpu.PREC_FP64):

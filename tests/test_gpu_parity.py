@@ -84,8 +84,7 @@ def test_orszag_single_patch_steps(gpulib, oracle, ta):
     ctx.close()
 
 
-@pytest.mark.parametrize("lim", [mfgpu.LIM_CD, mfgpu.LIM_SUPERBEE, mfgpu.LIM_VANALBADA,
-                                 mfgpu.LIM_MC, mfgpu.LIM_HARMONIC, mfgpu.LIM_VANLEER])
+@pytest.mark.parametrize("lim", [lim for lim in mfgpu.LIMITERS if lim != mfgpu.LIM_MINMOD])
 def test_limiters(gpulib, oracle, lim):
     n = 32
     p = _orszag_case(n, mfgpu.TA_RK2, limiter=lim)
@@ -367,3 +366,98 @@ def test_nonfinite_input_reported(gpulib):
     t = to_device(U)
     st, ndt, _ = ctx.patch_update(t.data_ptr(), lo, hi, [0, 0, 0], [15, 15, 0], 1e-4)
     assert st == 0 and ndt > 0
+
+
+def _uniform_helio_patch(n, prec):
+    """Single heliosphere patch holding the uniform inflow state (no inner
+    sphere): away from the domain boundary (where the far-field ghosts hold
+    the exact inflow primitives and the cells their round trip through the
+    conserved form) every face flux difference is exactly zero, so one step
+    changes the state there by the charge-exchange source alone."""
+    p = mfgpu.helio_params(n, precision=prec)
+    p.reinit_sphere = 0
+    p.neutral_sun_bc = 0
+    ctx = mfgpu.Context(p)
+    lo, hi = mfgpu.grow([0, 0, 0], [n - 1] * 3, ctx.ng, 3)
+    U = mfgpu.init_host_fab(p, lo, hi, "helio")
+    return p, ctx, U, lo, hi
+
+
+def test_mixed_charge_exchange_rates_are_fp64(gpulib):
+    """MF_PREC_MIXED computes the charge-exchange rates in FP64: on a state
+    whose fluxes cancel exactly, its step equals the fast FP64 path's
+    bitwise.  MF_PREC_MIXED_CE32 (FP32 rates) differs at FP32 rounding of the
+    source."""
+    n, m = 24, 6  # interior: 6 cells from the domain boundary (two stages of stencils)
+    out = {}
+    for prec in (mfgpu.PREC_FP64_FAST, mfgpu.PREC_MIXED, mfgpu.PREC_MIXED_CE32):
+        p, ctx, U, lo, hi = _uniform_helio_patch(n, prec)
+        Ug = _gpu_patch_step(ctx, U, lo, hi, [0, 0, 0], [n - 1] * 3, 2e-3)[0]
+        g = ctx.ng + m
+        out[prec] = Ug[:, g:-g, g:-g, g:-g]
+        src = np.max(np.abs(out[prec] - U[:, g:-g, g:-g, g:-g]))
+        assert src > 1e-6, (prec, src)  # the source acts
+        ctx.close()
+    assert np.array_equal(out[mfgpu.PREC_MIXED], out[mfgpu.PREC_FP64_FAST])
+    d = np.max(np.abs(out[mfgpu.PREC_MIXED_CE32] - out[mfgpu.PREC_FP64_FAST]))
+    assert 0.0 < d <= 1e-6 * np.max(np.abs(out[mfgpu.PREC_FP64_FAST])), d
+
+
+@pytest.mark.parametrize("prec", [mfgpu.PREC_MIXED, mfgpu.PREC_MIXED_CE32])
+def test_mixed_modes_l1_vs_fp64(gpulib, prec):
+    """Both mixed-precision forms against the FP64 GPU path on the 48^3
+    heliosphere level (27 patches of 16^3, the inner sphere, GLM, charge
+    exchange) after 20 steps with the same dt sequence: L1 relative error of
+    rho, p, |B| and each neutral density <= 1e-5."""
+    n, patch = 48, 16
+    boxes = mfgpu.tile_boxes(n, patch, 3)
+    levs = {}
+    for pr in (mfgpu.PREC_FP64, prec):
+        p = mfgpu.helio_params(n, precision=pr)
+        ctx = mfgpu.Context(p)
+        lev = mfgpu.Level(ctx, boxes)
+        flat = np.zeros(lev.ndoubles)
+        for i in range(len(boxes)):
+            flo, fhi = lev.fab_box(i)
+            lev.patch_view(flat, i)[:] = mfgpu.init_host_fab(p, flo, fhi, "helio")
+        lev.upload(flat.ctypes.data)
+        levs[pr] = (p, ctx, lev)
+    p64, c64, l64 = levs[mfgpu.PREC_FP64]
+    dt0 = l64.compute_dt()[0]
+    dt = 0.4 * dt0
+    nd = dt0
+    for _ in range(20):
+        ch = p64.factor_ch * p64.dx / nd
+        cp = float(np.sqrt(ch * p64.dx / p64.factor_cp))
+        for p, ctx, lev in levs.values():
+            ctx.set_dedner(ch, cp)
+        st, nd, _, _ = l64.step(dt)
+        assert st == 0
+        assert levs[prec][2].step(dt)[0] == 0
+        dt = 0.4 * nd
+    a = np.zeros(l64.ndoubles)
+    b = np.zeros(l64.ndoubles)
+    l64.download(a.ctypes.data)
+    levs[prec][2].download(b.ctypes.data)
+    ng = c64.ng
+    num, den = {}, {}
+    for i in range(len(boxes)):
+        x = valid_view(l64.patch_view(a, i), ng, 3)
+        y = valid_view(l64.patch_view(b, i), ng, 3)
+        q = {"rho": (x[0], y[0]), "rho_n1": (x[9], y[9]), "rho_n2": (x[14], y[14]),
+             "rho_n3": (x[19], y[19]),
+             "absB": (np.sqrt((x[5:8] ** 2).sum(0)), np.sqrt((y[5:8] ** 2).sum(0)))}
+        pr = []
+        for z in (x, y):
+            ke = 0.5 * (z[1] ** 2 + z[2] ** 2 + z[3] ** 2) / z[0]
+            pr.append((2.0 / 3.0) * (z[4] - ke - (z[5:8] ** 2).sum(0) / (8 * np.pi)))
+        q["p"] = tuple(pr)
+        for k, (u, v) in q.items():
+            num[k] = num.get(k, 0.0) + float(np.abs(v - u).sum())
+            den[k] = den.get(k, 0.0) + float(np.abs(u).sum())
+    l1 = {k: num[k] / den[k] for k in num}
+    assert all(v <= 1e-5 for v in l1.values()), l1
+    assert l1["rho"] > 0.0
+    for p, ctx, lev in levs.values():
+        lev.close()
+        ctx.close()

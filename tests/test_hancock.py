@@ -54,7 +54,8 @@ def _gpu_step(ctx, U, lo, hi, vlo, vhi, dt):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("lim", [mfgpu.LIM_MINMOD, mfgpu.LIM_VANLEER])
+@pytest.mark.parametrize("lim", [mfgpu.LIM_MINMOD, mfgpu.LIM_VANLEER, mfgpu.LIM_KOREN,
+                                 mfgpu.LIM_WENO3YC])
 def test_gpu_hancock_orszag_vs_oracle(gpulib, oracle, lim):
     n = 64
     p, ng, lo, hi, U = _orszag(n)

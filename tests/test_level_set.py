@@ -216,7 +216,8 @@ def test_gpu_orszag_surface_vs_oracle(gpulib, oracle, ta):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("lim", [mfgpu.LIM_CD, mfgpu.LIM_SUPERBEE, mfgpu.LIM_VANALBADA,
-                                 mfgpu.LIM_HARMONIC, mfgpu.LIM_VANLEER])
+                                 mfgpu.LIM_HARMONIC, mfgpu.LIM_VANLEER, mfgpu.LIM_HYPERBEE,
+                                 mfgpu.LIM_VENKATAKRISHNAN, mfgpu.LIM_WENO3])
 @pytest.mark.parametrize("char", [0, 1])
 @pytest.mark.parametrize("ta", [mfgpu.TA_RK2, mfgpu.TA_HANCOCK])
 def test_gpu_surface_limiters(gpulib, oracle, lim, char, ta):

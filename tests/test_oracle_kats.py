@@ -314,3 +314,73 @@ def test_sod_against_exact_solution(oracle):
     sel = (xs > 0.2) & (xs < 0.78)
     l1 = np.mean(np.abs(num[sel] - ref[sel]))
     assert l1 < 6e-3, l1
+
+
+# ---------------------------------------------------------------------------
+# limiters (src/reconstructionF.ChF): known answers worked out by hand from the
+# routines' formulas for the cell values W(i-1), W(i), W(i+1) = 0, 1, 3
+# (left difference 1, right difference 2)
+# ---------------------------------------------------------------------------
+_SQ2 = 2.0 ** 0.5
+_KAT_FACE_VALUES = {
+    # A = 1 + sqrt(2); slope = 2 * 2 / A^2
+    mfgpu.LIM_HYPERBEE: (1.0 - 4.0 / (1.0 + _SQ2) ** 2, 1.0 + 4.0 / (1.0 + _SQ2) ** 2),
+    # H = 2 / (2 (1 + 4 + 1e-10) - 2) ~ 1/4: lo = 1 - 2 H, hi = 1 + 2.5 H
+    mfgpu.LIM_KOREN: (0.5, 1.625),
+    # H = 3 / (6 (4 + 1 + 1e-20)) = 1/10: lo = 1 - 4 (1 + 1e-10) H, hi = 1 + 5 (2 + 1e-10) H
+    mfgpu.LIM_VENKATAKRISHNAN: (0.6, 2.0),
+    # AR = 1/16, AL = 1 (dSave = 1e-6 aside): lo = 1 - (1 + AR/(AR+2AL))/2,
+    # hi = 1 + (2 - AL/(AL+2AR))/2
+    mfgpu.LIM_WENO3: (1.0 - 0.5 * (1.0 + (1 / 16) / (1 / 16 + 2)),
+                      1.0 + 0.5 * (2.0 - 1.0 / (1.0 + 2 / 16))),
+    # D2P = 1: AL = 2, AR = 5/4: lo = 1 - (1 + AR/(AR+2AL))/2, hi = 1 + (2 - AL/(AL+2AR))/2
+    mfgpu.LIM_WENO3YC: (1.0 - 0.5 * (1.0 + 1.25 / 5.25), 1.0 + 0.5 * (2.0 - 2.0 / 4.5)),
+}
+
+
+@pytest.mark.parametrize("lim", sorted(_KAT_FACE_VALUES))
+def test_limiter_known_answers(oracle, lim):
+    lo, hi = oracle.face_values(lim, 0.0, 1.0, 3.0)
+    elo, ehi = _KAT_FACE_VALUES[lim]
+    # the hand values leave out the dSave regularisations (1e-10, or 1e-6 for WENO3)
+    tol = 1e-6 if lim in (mfgpu.LIM_WENO3, mfgpu.LIM_WENO3YC) else 1e-9
+    assert abs(lo - elo) <= tol and abs(hi - ehi) <= tol, (lim, lo, hi, elo, ehi)
+    # *FACESLOPES on the same differences gives the same face values
+    sl, sr = oracle.face_slopes(lim, 1.0, 2.0)
+    assert abs((1.0 - sl) - lo) <= 1e-12 and abs((1.0 + sr) - hi) <= 1e-12, (lim, sl, sr)
+
+
+@pytest.mark.parametrize("lim", mfgpu.LIMITERS)
+def test_limiters_reproduce_linear_data(oracle, lim):
+    """Every limiter but the reference's centred-difference form (whose face
+    values are the averages with the neighbours, CDFACEVALUES :1056-1079)
+    puts the faces of a linear profile at W(i) -/+ dW/2 (up to the dSave
+    regularisations)."""
+    for w0, d in ((1.0, 0.5), (-2.0, -3.0), (10.0, 1e-2)):
+        lo, hi = oracle.face_values(lim, w0 - d, w0, w0 + d)
+        if lim == mfgpu.LIM_CD:
+            assert lo == 0.5 * (w0 + (w0 + d)) and hi == 0.5 * (w0 + (w0 - d)), (lo, hi)
+            continue
+        tol = 1e-5 * abs(d) if lim in (mfgpu.LIM_VANALBADA,) else 1e-6 * abs(d)
+        assert abs(lo - (w0 - 0.5 * d)) <= tol and abs(hi - (w0 + 0.5 * d)) <= tol, (lim, lo, hi)
+
+
+@pytest.mark.parametrize("lim", [mfgpu.LIM_HYPERBEE, mfgpu.LIM_KOREN,
+                                 mfgpu.LIM_VENKATAKRISHNAN])
+def test_limiters_flatten_extrema(oracle, lim):
+    """TVD limiters take the cell value on both faces at a local extremum, and
+    their slopes vanish there."""
+    assert oracle.face_values(lim, 0.0, 1.0, 0.5) == (1.0, 1.0)
+    assert oracle.face_slopes(lim, 1.0, -0.5) == (0.0, 0.0)
+
+
+@pytest.mark.parametrize("lim", [mfgpu.LIM_WENO3, mfgpu.LIM_WENO3YC])
+def test_weno3_weights_favour_the_smooth_side(oracle, lim):
+    """WENO3 is not TVD: at an extremum it keeps a slope, weighted towards the
+    smaller difference; the weights of a symmetric extremum cancel."""
+    # symmetric extremum: equal weights 1/3, both faces at W - |dW|/6
+    lo, hi = oracle.face_values(lim, 0.0, 1.0, 0.0)
+    assert abs(lo - 5.0 / 6.0) < 1e-9 and abs(hi - 5.0 / 6.0) < 1e-9, (lo, hi)
+    lo, hi = oracle.face_values(lim, 0.0, 1.0, 1.01)
+    # the right difference (0.01) is far smoother: both faces near the right one-sided value
+    assert abs(hi - 1.005) < 0.01 and abs(lo - 0.995) < 0.02, (lo, hi)

@@ -1,10 +1,11 @@
 """mf_patch_update_noalloc: the patch update for callers that cannot allocate
-device memory (code inside another framework's stream capture, processes whose
-device memory belongs to a pool allocator, loops that forbid allocation after
+device memory (processes whose device memory belongs to a pool allocator that
+must not be bypassed, serving or real-time loops that forbid allocation after
 start-up).  Its scratch lives in one static device array shared by all calls,
-so the test makes two calls in a row and checks each against the regular
+so the tests make two calls in a row and check each against the regular
 mf_patch_update on the same input, within the parity tolerance of the GPU
-tests.  The file name sorts last so that a run stopping at the first failure
+tests: the updated state, the time step and its cell, and the flux and divB
+outputs.  The file name sorts last so that a run stopping at the first failure
 has already run every other test; it also passes alone in a fresh process.
 """
 import ctypes
@@ -20,14 +21,35 @@ pytestmark = pytest.mark.gpu
 RTOL = 1e-12
 
 
-def _call(fn, ctx, t, lo, hi, vlo, vhi, dt):
+def _call(fn, ctx, t, lo, hi, vlo, vhi, dt, F=None, divB=None):
     fab = mfgpu.MfFab(t.data_ptr(), mfgpu.make_box(lo, hi), ctx.nc)
     valid = mfgpu.make_box(vlo, vhi)
     ndt = ctypes.c_double()
     cell = mfgpu.c_int3()
-    st = fn(ctx.h, ctypes.byref(fab), ctypes.byref(valid), dt, None, None, ctypes.byref(ndt),
-            cell, None)
+    st = fn(ctx.h, ctypes.byref(fab), ctypes.byref(valid), dt,
+            ctypes.byref(F) if F is not None else None,
+            ctypes.byref(divB) if divB is not None else None, ctypes.byref(ndt), cell, None)
     return st, ndt.value, tuple(cell)
+
+
+def _face_outputs(ctx, sd, vlo, vhi):
+    """Device tensors and mf_fab descriptors of the flux outputs (faces of the
+    valid box per direction) and of divB (the valid box)."""
+    import torch
+    fabs = (mfgpu.MfFab * 3)()
+    ts = []
+    for d in range(sd):
+        hi = list(vhi)
+        hi[d] += 1
+        n = [hi[e] - vlo[e] + 1 for e in range(3)]
+        t = torch.full((ctx.nc, n[2], n[1], n[0]), float("nan"), dtype=torch.float64,
+                       device="cuda")
+        ts.append(t)
+        fabs[d] = mfgpu.MfFab(t.data_ptr(), mfgpu.make_box(vlo, hi), ctx.nc)
+    n = [vhi[e] - vlo[e] + 1 for e in range(3)]
+    tdb = torch.full((1, n[2], n[1], n[0]), float("nan"), dtype=torch.float64, device="cuda")
+    dfab = mfgpu.MfFab(tdb.data_ptr(), mfgpu.make_box(vlo, vhi), 1)
+    return fabs, ts, dfab, tdb
 
 
 def _case(case):
@@ -103,5 +125,69 @@ def test_noalloc_rejects_patch_beyond_scratch(gpulib):
     st, _, _ = _call(ctx.lib.mf_patch_update_noalloc, ctx, t, lo, hi, [0, 0, 0], [n - 1] * 3,
                      1e-3)
     assert st == mfgpu.MF_ERR_SCRATCH_LIMIT
+    assert np.array_equal(to_host(t), U)
+    ctx.close()
+
+
+def test_noalloc_flux_and_divb_outputs(gpulib):
+    """The flux output (the RK2 average of both stages' face fluxes, from the
+    static array) and the divB output of two calls in a row equal those of
+    mf_patch_update (Orszag-Tang with the 8-wave source, which fills divB)."""
+    p, ctx, U, lo, hi, vlo, vhi, sd, dt = _case("orszag")
+    lib = ctx.lib
+    ng = ctx.ng
+    for call in range(2):
+        ta, tb = to_device(U), to_device(U)
+        Fa, fa, Da, da = _face_outputs(ctx, sd, vlo, vhi)
+        Fb, fb, Db, db = _face_outputs(ctx, sd, vlo, vhi)
+        sa, dta, _ = _call(lib.mf_patch_update, ctx, ta, lo, hi, vlo, vhi, dt, Fa, Da)
+        sb, dtb, _ = _call(lib.mf_patch_update_noalloc, ctx, tb, lo, hi, vlo, vhi, dt, Fb, Db)
+        assert sa == mfgpu.MF_OK and sb == mfgpu.MF_OK, (call, sa, sb)
+        for d in range(sd):
+            x, y = to_host(fa[d]), to_host(fb[d])
+            assert np.all(np.isfinite(x)) and np.all(np.isfinite(y)), (call, d)
+            assert np.all(rel_err(y, x) <= RTOL), (call, d)
+        x, y = to_host(da), to_host(db)
+        assert np.all(np.isfinite(x))
+        assert np.all(np.abs(y - x) <= RTOL * (np.max(np.abs(x)) + 1e-300)), call
+        U = periodic_fill(to_host(ta), ng, 2)
+        dt = 0.4 * dta
+    ctx.close()
+
+
+@pytest.mark.parametrize("what", ["hancock", "ct"])
+def test_noalloc_unsupported_options(gpulib, what):
+    """Hancock and constrained transport are refused before any device work."""
+    n = 16
+    p = mfgpu.orszag_params(n)
+    if what == "hancock":
+        p.time_approximation = mfgpu.TA_HANCOCK
+    else:
+        p.divb_cleaning = 1
+        p.use_8wave = 0
+    ctx = mfgpu.Context(p)
+    U = orszag_patch(n, ctx.ng, p)
+    lo, hi = mfgpu.grow([0, 0, 0], [n - 1, n - 1, 0], ctx.ng, 2)
+    t = to_device(U)
+    st, _, _ = _call(ctx.lib.mf_patch_update_noalloc, ctx, t, lo, hi, [0, 0, 0], [n - 1, n - 1, 0],
+                     1e-3)
+    assert st == mfgpu.MF_ERR_UNSUPPORTED
+    assert np.array_equal(to_host(t), U)
+    ctx.close()
+
+
+def test_noalloc_bad_arguments(gpulib):
+    """Argument checks: a fab without the ghost layers, a valid box outside a
+    non-periodic domain, a wrong flux box, a non-positive dt."""
+    p, ctx, U, lo, hi, vlo, vhi, sd, dt = _case("helio")
+    lib = ctx.lib
+    t = to_device(U)
+    f = lib.mf_patch_update_noalloc
+    assert _call(f, ctx, t, lo, hi, [-1, 0, 0], vhi, dt)[0] == mfgpu.MF_ERR_BAD_ARG
+    assert _call(f, ctx, t, lo, hi, vlo, [vhi[0] + 1] + vhi[1:], dt)[0] == mfgpu.MF_ERR_BAD_ARG
+    assert _call(f, ctx, t, lo, hi, vlo, vhi, 0.0)[0] == mfgpu.MF_ERR_BAD_ARG
+    assert _call(f, ctx, t, lo, hi, vlo, vhi, float("nan"))[0] == mfgpu.MF_ERR_BAD_ARG
+    F, _, _, _ = _face_outputs(ctx, sd, vlo, [vhi[0] - 1] + vhi[1:])
+    assert _call(f, ctx, t, lo, hi, vlo, vhi, dt, F)[0] == mfgpu.MF_ERR_BAD_ARG
     assert np.array_equal(to_host(t), U)
     ctx.close()
