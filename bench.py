@@ -438,10 +438,7 @@ def run_ours(a):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": a.steps,
         "warmup": a.warmup, "ms_per_step": ms_all / a.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"3D multi-fluid heliosphere {n}^3 on [-1,1]^3, "
-                               f"{len(boxes)} patches of {patch}^3 + 4 ghosts, plasma MHD + "
-                               "3 neutral H fluids (24 comps), GLM, charge exchange, RK2, CFL 0.4",
-                   "zones_per_step": zones, "patches": len(boxes), "patch": patch,
+        "config": {**_workload_config(n, patch, len(boxes)),
                    "l2": "inputs larger than L2 (state arrays > 1.3 GB); no flush",
                    "parallelism": f"{ws} independent replica(s), one per GPU"},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": nbytes,
@@ -656,51 +653,49 @@ def run_serving(mfgpu, torch, a):
     return out
 
 
-def _cpu_sample(n, patch):
-    """64 patches (a 4x4x4 block at the centre of the domain, containing the
-    inner sphere) of the full workload."""
-    import mfgpu
-    boxes = mfgpu.tile_boxes(n, patch, 3)
-    npb = n // patch
-    c0 = max(0, npb // 2 - 2)
-    sel = []
-    for lo, hi in boxes:
-        ib, jb, kb = lo[0] // patch, lo[1] // patch, lo[2] // patch
-        if c0 <= ib < c0 + 4 and c0 <= jb < c0 + 4 and c0 <= kb < c0 + 4:
-            sel.append((lo, hi))
-    return sel
+def _workload_config(n, patch, npatch):
+    """The workload as both arms name it."""
+    return {"workload": f"3D multi-fluid heliosphere {n}^3 on [-1,1]^3, {npatch} patches of "
+                        f"{patch}^3 + 4 ghosts, plasma MHD + 3 neutral H fluids (24 comps), GLM, "
+                        "charge exchange, bipolar inner sphere, RK2, CFL 0.4",
+            "zones_per_step": n ** 3, "patches": npatch, "patch": patch}
 
 
 def cpu_baseline(n, patch, min_seconds=10.0, max_steps=30, warmup=1, fixed_steps=None):
     """The oracle (C restatement of the reference patch update, OpenMP over
-    patches as AMRLevelIdealMHD::stepOMP) on a bounded sample of the workload."""
+    patches as AMRLevelIdealMHD::stepOMP) on the whole workload: every patch
+    of the level, initial state from the oracle's own set-up, the level's dt
+    chain (cfl * dt_min capped at max_dt_growth times the previous dt) and
+    GLM speeds from each step's dt_min.  Loads only the oracle library."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import numpy as np
-    import mfgpu
     import pyoracle
-    p = mfgpu.helio_params(n, precision=mfgpu.PREC_FP64)
-    sel = _cpu_sample(n, patch)
-    ng = mfgpu.num_ghost(p)
+    p = pyoracle.helio_params(n)
+    boxes = pyoracle.tile_boxes(n, patch, 3)
+    ng = pyoracle.num_ghost(p)
     arrays, fboxes = [], []
-    for lo, hi in sel:
-        flo, fhi = mfgpu.grow(lo, hi, ng, 3)
-        arrays.append(np.ascontiguousarray(mfgpu.init_host_fab(p, flo, fhi, "helio")))
+    for lo, hi in boxes:
+        flo, fhi = pyoracle.grow(lo, hi, ng, 3)
+        arrays.append(pyoracle.helio_fab(p, flo, fhi))
         fboxes.append((flo, fhi))
     threads = os.cpu_count() or 1
-    dt0 = min(pyoracle.compute_dt(p, a, fb[0], fb[1], b[0], b[1])[1]
-              for a, fb, b in zip(arrays, fboxes, sel))
-    ch = p.factor_ch * p.dx / dt0
-    p.dedner_ch, p.dedner_cp = ch, (ch * p.dx / p.factor_cp) ** 0.5
-    dt = CFL * dt0
+    dmin = min(pyoracle.compute_dt(p, a, fb[0], fb[1], b[0], b[1])[1]
+               for a, fb, b in zip(arrays, fboxes, boxes))
+    dt = CFL * dmin
+
+    def step(dt, dmin, t):
+        ch = p.factor_ch * p.dx / dmin
+        p.dedner_ch, p.dedner_cp = ch, (ch * p.dx / p.factor_cp) ** 0.5
+        st, ndt, _, _ = pyoracle.level_step(p, arrays, fboxes, boxes, dt, threads, time=t)
+        assert st == 0, st
+        return min(CFL * ndt, p.max_dt_growth * dt), ndt, t + dt
+
+    t = 0.0
     for _ in range(warmup):
-        st, ndt, _, _ = pyoracle.level_step(p, arrays, fboxes, sel, dt, threads)
-        dt = CFL * ndt
+        dt, dmin, t = step(dt, dmin, t)
     steps = 0
     t0 = time.perf_counter()
     while True:
-        st, ndt, _, _ = pyoracle.level_step(p, arrays, fboxes, sel, dt, threads)
-        assert st == 0, st
-        dt = CFL * ndt
+        dt, dmin, t = step(dt, dmin, t)
         steps += 1
         el = time.perf_counter() - t0
         if fixed_steps is not None:
@@ -709,11 +704,11 @@ def cpu_baseline(n, patch, min_seconds=10.0, max_steps=30, warmup=1, fixed_steps
         elif el >= min_seconds or steps >= max_steps:
             break
     el = time.perf_counter() - t0
-    zones = sum((hi[0] - lo[0] + 1) * (hi[1] - lo[1] + 1) * (hi[2] - lo[2] + 1) for lo, hi in sel)
+    zones = n ** 3
     return {"value": zones * steps / el, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{len(sel)} of the {(n // patch) ** 3} patches ({zones} zones, the "
-                      f"central 4x4x4 block), {steps} level steps after {warmup} warm-up, "
-                      f"{el:.1f} s", "threads": pyoracle.max_threads()}
+            "sample": f"the whole workload ({len(boxes)} patches, {zones} zones), {steps} level "
+                      f"steps after {warmup} warm-up, {el:.1f} s",
+            "threads": pyoracle.max_threads()}
 
 
 def run_reference(a):
@@ -721,12 +716,12 @@ def run_reference(a):
     if rank != 0:
         return
     cb = cpu_baseline(a.n, a.patch, warmup=max(1, a.warmup), fixed_steps=max(1, a.steps))
+    npatch = (a.n // a.patch) ** 3
     line = {
         "metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": ws, "steps": a.steps,
         "warmup": a.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64", "data": "synthetic", "impl": "reference",
-        "config": {"workload": f"3D multi-fluid heliosphere {a.n}^3, patches of {a.patch}^3 "
-                               "(bounded sample, see cpu_baseline.sample)"},
+        "config": _workload_config(a.n, a.patch, npatch),
         "cpu_baseline": cb,
         "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},

@@ -3782,6 +3782,67 @@ int mf_oracle_init_orszag(const mf_params* p, mf_fab* Uf, const mf_box* box) {
   return MF_OK;
 }
 
+/* The synthetic heliosphere's initial state: the uniform inflow given as
+   primitive states (wp: plasma rho, u, v, w, p, bx, by, bz; wn: rho, u, v, w,
+   p of each neutral fluid) through PRIMTOCONS_MF (srcIdeal/PatchMHDMFF.ChF:
+   82-149), psi = 0, the tracking surfaces (the region tracer -1 inside the
+   sphere r <= Rinit and +1 outside, as HELIOINIT sets it,
+   swlism/HeliosphericF.ChF:1228-1231,1302-1304; the current-sheet surface of
+   a bipolar field +1, as HeliosphericProblem's component reset sets it,
+   swlism/HeliosphericProblem.cpp:2387-2393; any other surface the signed
+   distance r - Rinit), then the inner sphere reset at time 0
+   (HELIOREINIT_DEFAULT). */
+int mf_oracle_init_helio(const mf_params* p, const double* wp, const double* wn, mf_fab* Uf,
+                         const mf_box* box) {
+  Ctx c;
+  int st = ctx_init(&c, p);
+  if (st) return st;
+  if (!wp || !Uf || !Uf->data || !box || !box_contains(&Uf->box, box)) return MF_ERR_BAD_ARG;
+  if (Uf->ncomp != c.nc || (c.nf > 1 && !wn)) return MF_ERR_BAD_ARG;
+  Fab U = fab_wrap(Uf->data, Uf->box, Uf->ncomp);
+  const double invhgamma = 1.0 / c.hgamma;
+  double u[MF_MAX_COMP];
+  FOR_BOX((*box), i, j, k) {
+    double rho = fmax(wp[0], c.smallr);
+    double uu = wp[1], vv = wp[2], ww = wp[3], pr = wp[4];
+    double bx = wp[5], by = wp[6], bz = wp[7];
+    double b = D_1_4PI * (bx * bx + by * by + bz * bz);
+    double ke = uu * uu + vv * vv + ww * ww;
+    u[0] = rho;
+    u[1] = rho * uu;
+    u[2] = rho * vv;
+    u[3] = rho * ww;
+    u[4] = pr * invhgamma + 0.5 * (rho * ke + b);
+    u[5] = bx;
+    u[6] = by;
+    u[7] = bz;
+    if (c.glm) u[8] = 0.0;
+    for (int f = 1; f < c.nf; ++f) {
+      const double* w = wn + 5 * (f - 1);
+      int s = c.irhon + 5 * (f - 1);
+      double r = fmax(w[0], c.smallr);
+      double k2 = w[1] * w[1] + w[2] * w[2] + w[3] * w[3];
+      u[s] = r;
+      u[s + 1] = r * w[1];
+      u[s + 2] = r * w[2];
+      u[s + 3] = r * w[3];
+      u[s + 4] = w[4] * invhgamma + 0.5 * r * k2;
+    }
+    if (c.nls) {
+      double x = (i + 0.5) * p->dx - p->sun_center[0];
+      double y = (j + 0.5) * p->dx - p->sun_center[1];
+      double z = (c.sd == 3) ? (k + 0.5) * p->dx - p->sun_center[2] : 0.0;
+      double r2 = x * x + y * y + z * z;
+      for (int q = c.ils; q < c.nc; ++q) u[q] = sqrt(r2) - p->reinit_r0;
+      if (p->region_tracer) u[c.nc - 1] = (r2 <= p->reinit_r0 * p->reinit_r0) ? -1.0 : 1.0;
+      if (p->reinit_sphere && c.ihcs >= 0) u[c.ihcs] = 1.0;
+    }
+    if (p->reinit_sphere) reinit_cell(&c, i, j, k, 0.0, u);
+    for (int q = 0; q < c.nc; ++q) AT(&U, i, j, k, q) = u[q];
+  }
+  return MF_OK;
+}
+
 int mf_oracle_max_threads(void) {
 #ifdef _OPENMP
   return omp_get_max_threads();

@@ -99,6 +99,11 @@ int mf_oracle_region(const mf_params* p, int i, int j, int k, const double* w);
 
 /* Orszag-Tang initial state (problems/OrszagF.ChF:4-79). */
 int mf_oracle_init_orszag(const mf_params* p, mf_fab* U, const mf_box* box);
+/* The synthetic heliosphere's initial state: uniform inflow (primitive
+   states wp, wn through PRIMTOCONS_MF), tracking surfaces, the inner sphere
+   reset at time 0. */
+int mf_oracle_init_helio(const mf_params* p, const double* wp, const double* wn, mf_fab* U,
+                         const mf_box* box);
 
 /* Number of OpenMP threads available to the oracle (1 without OpenMP). */
 int mf_oracle_max_threads(void);
