@@ -15,6 +15,7 @@
 #include <cstring>
 #include <new>
 #include <thread>
+#include <unordered_map>
 #include <array>
 #include <vector>
 
@@ -369,6 +370,12 @@ struct mf_level {
   DevBuf Wf;                               // mixed precision: FP32 copy of W
   std::vector<long long> voff;             // packed offset of each patch (doubles)
   double time = 0.0;                       // start time of the next step (host mirror)
+  // lean primitive part (LevelPlan::lean): prim batch over the valid boxes,
+  // far-field ghost boxes
+  bool lean = false;
+  mf::Batch bp;
+  DevBuf far;
+  mf::LeanPrim lp;
 };
 
 extern "C" {
@@ -1170,7 +1177,64 @@ mf_status build_level_plan(const mf_params& p, int ng, int nc, int npatch, const
   }
   L.fvsize = fvo;
   add_regions(L, p, ix, ng, L.full);
-  if (rk2 && !ct_on(p)) add_regions(L, p, ix, 2, L.two);
+  const bool lean_scheme = (rk2 || p.time_approximation == MF_TA_FIRST_ORDER) && !ct_on(p);
+  if (lean_scheme) add_regions(L, p, ix, 2, L.two);
+  if (lean_scheme) {
+    // the lean primitive part: stage 1 on the valid boxes, and the sibling
+    // copies cover every in-domain ghost cell of each valid.grow(2)
+    std::vector<long long> cov(npatch, 0);
+    std::unordered_map<long long, int> by_off;
+    for (int i = 0; i < npatch; ++i) by_off[L.off[i]] = i;
+    for (const CopyReg& R : L.two) cov[by_off[R.dst_off]] += (long long)R.ext[0] * R.ext[1] * R.ext[2];
+    bool lean = true;
+    for (int i = 0; i < npatch && lean; ++i) {
+      const StageDesc& A = L.d1[i];
+      for (int d = 0; d < 3; ++d)
+        if (A.vlo[d] != valid[i].lo[d] || A.vn[d] != valid[i].hi[d] - valid[i].lo[d] + 1)
+          lean = false;
+      const mf_box wb = box_and_domain(box_grow(valid[i], 2, sd), p);
+      if (cov[i] != box_cells(wb) - box_cells(valid[i])) lean = false;
+    }
+    L.lean = lean;
+    if (lean) {
+      L.dp = L.d2;
+      for (int i = 0; i < npatch; ++i) {
+        StageDesc& D = L.dp[i];
+        for (int d = 0; d < 3; ++d) {
+          D.wlo[d] = valid[i].lo[d];
+          D.wn[d] = valid[i].hi[d] - valid[i].lo[d] + 1;
+        }
+        // far-field ghosts of valid.grow(2): slabs peeled off the box one
+        // non-periodic direction at a time
+        mf_box rest = box_grow(valid[i], 2, sd);
+        for (int d = 0; d < sd; ++d) {
+          if (p.periodic[d]) continue;
+          for (int side = 0; side < 2; ++side) {
+            mf_box slab = rest;
+            if (side == 0)
+              slab.hi[d] = std::min(rest.hi[d], p.domain_lo[d] - 1);
+            else
+              slab.lo[d] = std::max(rest.lo[d], p.domain_hi[d] + 1);
+            if (box_empty(slab)) continue;
+            FarReg R;
+            std::memset(&R, 0, sizeof(R));
+            R.off = L.off[i];
+            ext3(L.fab[i], R.fn);
+            for (int e = 0; e < 3; ++e) {
+              R.flo[e] = L.fab[i].lo[e];
+              R.lo[e] = slab.lo[e];
+              R.ext[e] = slab.hi[e] - slab.lo[e] + 1;
+            }
+            R.run = 0;
+            L.far.push_back(R);
+          }
+          rest.lo[d] = std::max(rest.lo[d], p.domain_lo[d]);
+          rest.hi[d] = std::min(rest.hi[d], p.domain_hi[d]);
+        }
+      }
+    }
+    if (!rk2 && !lean) L.two.clear();
+  }
   if (p.neutral_sun_bc && p.n_fluids > 1 && sd == 3) {
     // HeliosphericProblem::define (swlism/HeliosphericProblem.cpp:476-527):
     // the sun on a grid node, strips of iR0 planes on either side of it
@@ -1249,16 +1313,26 @@ static mf_status enqueue_level_step(mf_level* L, int advance, cudaEvent_t* ev = 
     kinds[ne] = kind;
     ++ne;
   };
+  const int mixed = (p.precision == MF_PREC_MIXED);
+  // lean levels: the primitive part of each stage computes the valid cells
+  // and copies the ghosts; the conserved state is not exchanged (no kernel
+  // of the step reads its ghost cells then)
+  const mf::LeanPrim* lean = L->lean ? &L->lp : nullptr;
+  B.lean = lean;
+  const int np0 = mf::prim_launches(lean, mixed);
   auto stage_marks = [&](int n0) {
     if (!ev) return;
     kinds[n0] = 1;
-    for (int d = 0; d < sd; ++d) kinds[n0 + 1 + d] = 2;
-    kinds[n0 + 1 + sd] = 3;
-    ne = n0 + 2 + sd;
+    for (int q = 1; q < np0; ++q) kinds[n0 + q] = 0;
+    for (int d = 0; d < sd; ++d) kinds[n0 + np0 + d] = 2;
+    kinds[n0 + np0 + sd] = 3;
+    ne = n0 + np0 + 1 + sd;
   };
-  MF_CHECK_CUDA(mf::launch_exchange((double*)L->U.p, (const CopyReg*)L->exfull.p, L->nfull, nc, s));
-  if (L->nfull) mark(0);
-  const int mixed = (p.precision == MF_PREC_MIXED);
+  if (!lean) {
+    MF_CHECK_CUDA(
+        mf::launch_exchange((double*)L->U.p, (const CopyReg*)L->exfull.p, L->nfull, nc, s));
+    if (L->nfull) mark(0);
+  }
   // constrained transport (src/PatchMHDAM.cpp:684-698, 1150-1160): the level's
   // UOld (AMRLevelIdealMHD::preTimeStep), per stage the edge field of the
   // stage's fluxes and B from the stage-start field, the dt after the last
@@ -1305,9 +1379,11 @@ static mf_status enqueue_level_step(mf_level* L, int advance, cudaEvent_t* ev = 
                               nullptr, 1.0)) != MF_OK)
       return gst;
     if ((gst = gather(0)) != MF_OK) return gst;
-    MF_CHECK_CUDA(
-        mf::launch_exchange((double*)L->U1.p, (const CopyReg*)L->extwo.p, L->ntwo, nc, s));
-    if (L->ntwo) mark(0);
+    if (!lean) {
+      MF_CHECK_CUDA(
+          mf::launch_exchange((double*)L->U1.p, (const CopyReg*)L->extwo.p, L->ntwo, nc, s));
+      if (L->ntwo) mark(0);
+    }
     B.uin = (const double*)L->U1.p;
     B.uout = (double*)L->U.p;
     B.uold = (const double*)L->U.p;
@@ -1435,18 +1511,24 @@ mf_status mf_level_create(mf_ctx* c, int npatch, const mf_box* valid, mf_level**
   const size_t rs = mixed ? sizeof(float) : sizeof(double);
   std::vector<StageDesc> hd(plan.d1);
   hd.insert(hd.end(), plan.d2.begin(), plan.d2.end());
+  L->lean = plan.lean;
+  if (L->lean) hd.insert(hd.end(), plan.dp.begin(), plan.dp.end());
   const long long* fsize = plan.fsize;
   const long long* bsize = plan.bsize;
   std::memset(&L->b1, 0, sizeof(L->b1));
   std::memset(&L->b2, 0, sizeof(L->b2));
+  std::memset(&L->bp, 0, sizeof(L->bp));
+  std::memset(&L->lp, 0, sizeof(L->lp));
   RunParams hrun = mf::run_params_of(c->dp);
   if (!mf::batch_offsets(hd.data(), npatch, sd, L->b1) ||
-      !mf::batch_offsets(hd.data() + npatch, npatch, sd, L->b2, &hrun, 1)) {
+      !mf::batch_offsets(hd.data() + npatch, npatch, sd, L->b2, &hrun, 1) ||
+      (L->lean && !mf::batch_offsets(hd.data() + 2 * npatch, npatch, sd, L->bp))) {
     delete L;
     return MF_ERR_UNSUPPORTED;  // more than 2^31 cells or faces in one launch
   }
   mf::batch_default_threads(L->b1);
   mf::batch_default_threads(L->b2);
+  mf::batch_default_threads(L->bp);
   const std::vector<CopyReg>& full = plan.full;
   const std::vector<CopyReg>& two = plan.two;
   L->nfull = (int)full.size();
@@ -1485,7 +1567,17 @@ mf_status mf_level_create(mf_ctx* c, int npatch, const mf_box* valid, mf_level**
       break;
     L->b1.desc = (const StageDesc*)L->desc.p;
     L->b2.desc = (const StageDesc*)L->desc.p + npatch;
-    L->b1.runs = L->b2.runs = druns;
+    L->bp.desc = (const StageDesc*)L->desc.p + 2 * npatch;
+    L->b1.runs = L->b2.runs = L->bp.runs = druns;
+    if (L->lean) {
+      if ((e = L->far.ensure(sizeof(mf::FarReg) * std::max<size_t>(1, plan.far.size()))) !=
+          cudaSuccess)
+        break;
+      if (!plan.far.empty() &&
+          (e = cudaMemcpy(L->far.p, plan.far.data(), sizeof(mf::FarReg) * plan.far.size(),
+                          cudaMemcpyHostToDevice)) != cudaSuccess)
+        break;
+    }
     if ((e = L->exfull.ensure(sizeof(CopyReg) * std::max<size_t>(1, full.size()))) != cudaSuccess)
       break;
     if (!full.empty() &&
@@ -1527,12 +1619,32 @@ mf_status mf_level_create(mf_ctx* c, int npatch, const mf_box* valid, mf_level**
     mf_level_destroy(L);
     return st;
   }
+  if (L->lean) {
+    L->lp.prim = &L->bp;
+    L->lp.regs = (const CopyReg*)L->extwo.p;
+    L->lp.nregs = L->ntwo;
+    L->lp.far = (const mf::FarReg*)L->far.p;
+    L->lp.nfar = (int)plan.far.size();
+    // the FP64 primitive ghosts are read by the FP64 flux kernels, the
+    // characteristic projections, central Bn and the tracking surfaces'
+    // floor; the FP32 flux kernels read only the FP32 copy
+    L->lp.exchange_w = (!mixed || p.char_reconstruction || p.divb_method == 2 ||
+                        p.num_tracking_surfaces > 0)
+                           ? 1
+                           : 0;
+  }
   const int per_stage = mf::stage_launches(sd);
   L->launches = (p.time_approximation == MF_TA_RK2) ? (2 * per_stage + 2 + 1)
                 : (p.time_approximation == MF_TA_HANCOCK) ? (mf::hancock_launches(sd) + 1 + 1)
                                                           : (per_stage + 1 + 1);
   if (L->nfull == 0) L->launches -= 1;
   if (p.time_approximation == MF_TA_RK2 && L->ntwo == 0) L->launches -= 1;
+  if (L->lean) {  // no exchange of U; the primitive part of every stage instead
+    const int stages = (p.time_approximation == MF_TA_RK2) ? 2 : 1;
+    if (L->nfull) L->launches -= 1;
+    if (p.time_approximation == MF_TA_RK2 && L->ntwo) L->launches -= 1;
+    L->launches += stages * (mf::prim_launches(&L->lp, mixed) - 1);
+  }
   if (L->nsun) L->launches += 1;
   // constrained transport: edge field + recalculation per stage, the dt after
   // them, and the level's recalculation
@@ -1866,7 +1978,7 @@ static mf_status time_kind(mf_level* L, int kind, int reps, cudaEvent_t e0, cuda
   for (int r = 0; r < reps; ++r) {
     cudaError_t e = cudaSuccess;
     if (kind == 0) {
-      e = mf::launch_prim(c->dp, B.uin, B.w, b, L->s, B.wf);
+      e = mf::launch_prim(c->dp, B.uin, B.w, L->lean ? L->bp : b, L->s, B.wf);
     } else if (kind == 1) {
       for (int d = 0; d < sd && e == cudaSuccess; ++d) {
         if (p.precision == MF_PREC_MIXED)
@@ -1917,7 +2029,7 @@ mf_status mf_level_autotune(mf_level* L, int reps, int threads[3]) {
     float best = 0.f;
     int bnt = L->b1.nt[kind];
     for (int q = 0; q < 3 && st == MF_OK; ++q) {
-      L->b1.nt[kind] = L->b2.nt[kind] = cand[q];
+      L->b1.nt[kind] = L->b2.nt[kind] = L->bp.nt[kind] = cand[q];
       float ms = 0.f;
       st = time_kind(L, kind, 1, e0, e1, &ms);  // warm-up
       if (st == MF_OK) st = time_kind(L, kind, reps, e0, e1, &ms);
@@ -1926,13 +2038,14 @@ mf_status mf_level_autotune(mf_level* L, int reps, int threads[3]) {
         bnt = cand[q];
       }
     }
-    L->b1.nt[kind] = L->b2.nt[kind] = bnt;
+    L->b1.nt[kind] = L->b2.nt[kind] = L->bp.nt[kind] = bnt;
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (st != MF_OK) {
     mf::batch_default_threads(L->b1);
     mf::batch_default_threads(L->b2);
+    mf::batch_default_threads(L->bp);
   }
   L->nparts = mf::dt_partials(L->b2);
   if ((size_t)(L->nparts + 1) * sizeof(DtPartial) > L->partials.bytes) return MF_ERR_CUDA;

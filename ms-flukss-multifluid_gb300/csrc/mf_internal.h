@@ -48,6 +48,14 @@ struct LevelPlan {
   long long fvsize = 0;  // Hancock face values per direction (doubles)
   std::vector<CopyReg> full, two;
   std::vector<SunPair> sun;  // neutral pass-through at the sun (level steps)
+  // lean: every ghost cell of each patch's primitive box (valid.grow(2)) is a
+  // sibling's valid cell (or its periodic image) or lies outside the domain,
+  // and stage 1 runs on the valid box; the primitive state is then computed
+  // on the valid cells (dp: descs whose W box is the valid box), copied into
+  // the ghosts (two) and completed by the far-field fill (far).
+  bool lean = false;
+  std::vector<StageDesc> dp;
+  std::vector<FarReg> far;
 };
 
 // MF_ERR_BAD_ARG for empty, overlapping or out-of-domain boxes, boxes with

@@ -152,6 +152,33 @@ struct CopyReg {
   int ext[3];                  // region extents
 };
 
+// A box of far-field ghost cells of a patch's primitive-state box (cells
+// outside a non-periodic domain side): filled after the primitive variables
+// of the valid cells and the ghost exchange, as the primitive kernel fills
+// them (HELIOGS) when it runs over the whole box.
+struct FarReg {
+  long long off;  // fab offset (doubles) in U / W / Wf
+  int fn[3];      // fab extents
+  int flo[3];     // fab lo (index space)
+  int lo[3];      // region lo (index space)
+  int ext[3];     // region extents
+  int run;        // run of the patch (RunParams)
+  int pad;
+};
+
+// Primitive variables on the valid cells only (levels whose primitive-box
+// ghosts are all sibling cells or outside the domain): the ghosts come from a
+// copy of the siblings' primitive state and the far-field fill, which gives
+// the same values as computing them from exchanged conserved ghosts.
+struct LeanPrim {
+  const Batch* prim;         // descs with the W box = the valid box
+  const CopyReg* regs;       // sibling copies into the 2 ghost layers
+  int nregs;
+  const FarReg* far;         // far-field ghost boxes
+  int nfar;
+  int exchange_w;            // copy the FP64 W (else only the FP32 copy)
+};
+
 struct StageBuffers {
   const double* uin;   // state the stage starts from
   double* uout;        // state the stage writes (valueBox cells only)
@@ -169,6 +196,7 @@ struct StageBuffers {
   double* divb;        // optional divB output (single patch: fab on the valid box)
   int divb_lo[3], divb_n[3];
   cudaEvent_t* ev;     // optional: an event recorded after each launch (profiling)
+  const LeanPrim* lean;  // optional: primitive state on valid cells + ghost copies
 };
 
 enum StageFlags : int { kStageAverage = 1, kStageDt = 2 };
@@ -232,6 +260,20 @@ cudaError_t launch_finalize(const DevParams& P, const DtPartial* partials, const
                             int nt, StepState* state, int advance, cudaStream_t s);
 
 cudaError_t launch_exchange(double* u, const CopyReg* regs, int nreg, int nc, cudaStream_t s);
+cudaError_t launch_exchange_f(float* u, const CopyReg* regs, int nreg, int nc, cudaStream_t s);
+// Far-field ghosts of the primitive state (HELIOGS, as the primitive kernel
+// fills them) on the boxes far (W and, when set, its FP32 copy wf).
+cudaError_t launch_farfield(const DevParams& P, const double* u, double* w, float* wf,
+                            const FarReg* far, int nfar, const RunParams* runs, int have_w,
+                            cudaStream_t s);
+// Kernel launches of the primitive part of a stage (1 without lean).
+inline int prim_launches(const LeanPrim* lp, int mixed) {
+  if (!lp) return 1;
+  int n = 1;
+  if (lp->nregs) n += (lp->exchange_w ? 1 : 0) + (mixed ? 1 : 0);
+  if (lp->nfar) n += 1;
+  return n;
+}
 
 // The valid cells of the descs of b (valueBox = valid box, one run) between
 // the fab layout u and the packed layout (nc x the desc's first valid cell,
@@ -273,7 +315,8 @@ cudaError_t launch_recalc_ext(int sd, double dx, mf_fab* U, const mf_fab* Uold, 
 cudaError_t launch_edges_out(int sd, const double* e, const mf_box& fab, const mf_box& valid,
                              mf_fab* out, cudaStream_t s);
 
-// Number of kernel launches enqueued by launch_stage for sd dimensions.
+// Number of kernel launches enqueued by launch_stage for sd dimensions
+// (plus prim_launches - 1 with a lean primitive part).
 inline int stage_launches(int sd) { return 2 + sd; }
 
 // Hancock step (predictorHancock + correctorHancock) of the patches of a

@@ -82,9 +82,104 @@ __global__ void __launch_bounds__(kMaxBlock)
   }
 }
 
+// Far-field ghosts of the primitive state, exactly as k_prim's far-field
+// branch fills them (HELIOGS, swlism/HeliosphericF.ChF:978-1140), for the
+// levels whose valid-cell primitives and ghost copies come first: plasma and
+// neutral fluid 1 from the boundary state, the other neutral fluids from the
+// primitive state of the nearest cell along the boundary normal.  That cell,
+// when it lies in the domain, is a valid cell of the patch or a ghost cell
+// filled by the copy before this launch (its FP64 state when that copy ran,
+// else the FP32 copy, the only one read downstream); outside the domain (a
+// corner) its conserved state never changes and is converted here.
+template <int GLM>
+__global__ void __launch_bounds__(256)
+    k_farfield(const DevParams P, const double* __restrict__ U, double* __restrict__ W,
+               float* __restrict__ Wf, const FarReg* __restrict__ regs,
+               const RunParams* __restrict__ runs, int have_w) {
+  constexpr int IRHON = 8 + GLM;
+  const FarReg F = regs[blockIdx.x];
+  const RunParams& R = runs[F.run];
+  const int n = F.ext[0] * F.ext[1] * F.ext[2];
+  const long long cs = (long long)F.fn[0] * F.fn[1] * F.fn[2];
+  for (int t = threadIdx.x; t < n; t += blockDim.x) {
+    int i, j, k;
+    decode(t, F.lo, F.ext, i, j, k);
+    const long long base = F.off + loc(F.flo, F.fn, i, j, k);
+    int x[3] = {i, j, k};
+    int od = -1;
+    for (int d = 0; d < P.sd; ++d)
+      if (!P.periodic[d] && (x[d] < R.dlo[d] || x[d] > R.dhi[d])) od = d;
+    if (od < 0) continue;  // (the regions hold far-field cells only)
+    double w[MF_MAX_COMP];
+    float wf[MF_MAX_COMP];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) w[q] = R.bc_plasma[q];
+    if (GLM) w[8] = 0.0;
+    if (P.nf > 1) {
+#pragma unroll
+      for (int q = 0; q < 5; ++q) w[IRHON + q] = R.bc_n1[q];
+    }
+#pragma unroll
+    for (int q = 0; q < MF_MAX_COMP; ++q) wf[q] = (float)w[q];
+    x[od] = (x[od] < R.dlo[od]) ? R.dlo[od] : R.dhi[od];
+    bool inside = true;
+    for (int d = 0; d < P.sd; ++d)
+      if (!P.periodic[d] && (x[d] < R.dlo[d] || x[d] > R.dhi[d])) inside = false;
+    const long long eb = F.off + loc(F.flo, F.fn, x[0], x[1], x[2]);
+#pragma unroll
+    for (int f = 2; f < MF_MAX_FLUIDS; ++f) {
+      if (f < P.nf) {
+        const int s0 = IRHON + (f - 1) * 5;
+        if (!inside) {
+          double u5[5];
+#pragma unroll
+          for (int q = 0; q < 5; ++q) u5[q] = U[eb + (s0 + q) * cs];
+          cons_to_prim_euler(P, u5, w + s0);
+#pragma unroll
+          for (int q = 0; q < 5; ++q) wf[s0 + q] = (float)w[s0 + q];
+        } else if (have_w) {
+#pragma unroll
+          for (int q = 0; q < 5; ++q) {
+            w[s0 + q] = W[eb + (s0 + q) * cs];
+            wf[s0 + q] = (float)w[s0 + q];
+          }
+        } else {
+#pragma unroll
+          for (int q = 0; q < 5; ++q) {
+            wf[s0 + q] = Wf[eb + (s0 + q) * cs];
+            w[s0 + q] = (double)wf[s0 + q];
+          }
+        }
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < MF_MAX_COMP; ++q)
+      if (q < P.ils) {
+        W[base + q * cs] = w[q];
+        if (Wf) Wf[base + q * cs] = wf[q];
+      }
+    for (int q = P.ils; q < P.nc; ++q) {
+      const double v = (P.reg_tracer && q == P.nc - 1) ? 1.0 : U[base + q * cs];
+      W[base + q * cs] = v;
+      if (Wf) Wf[base + q * cs] = (float)v;
+    }
+  }
+}
+
 // ---------------------------------------------------------------------------
 // face fluxes in direction DIR
 }  // namespace
+
+cudaError_t launch_farfield(const DevParams& P, const double* u, double* w, float* wf,
+                            const FarReg* far, int nfar, const RunParams* runs, int have_w,
+                            cudaStream_t s) {
+  if (nfar <= 0) return cudaSuccess;
+  if (P.glm)
+    k_farfield<1><<<nfar, 256, 0, s>>>(P, u, w, wf, far, runs, have_w);
+  else
+    k_farfield<0><<<nfar, 256, 0, s>>>(P, u, w, wf, far, runs, have_w);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_prim(const DevParams& P, const double* uin, double* w, const Batch& b,
                         cudaStream_t s, float* wf) {

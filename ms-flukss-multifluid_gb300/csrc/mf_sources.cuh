@@ -284,7 +284,7 @@ static __device__ __host__ __noinline__ void reinit_state(const DevParams& P, do
 
 // The reset of one cell: the membership test in non-fused arithmetic (host
 // and device agree exactly), then the wind state.
-__device__ __host__ inline void reinit_cell(const DevParams& P, double dx, int i, int j, int k,
+__device__ __host__ __forceinline__ void reinit_cell(const DevParams& P, double dx, int i, int j, int k,
                                             double t, double* u) {
 #ifdef __CUDA_ARCH__
   const double x = __dadd_rn(__dmul_rn(i + 0.5, dx), -P.sun_c[0]);

@@ -256,7 +256,7 @@ static __device__ __host__ __noinline__ void reinit_state(const DevParams& P, do
 }
 
 // The reset of one cell: the membership test, then the wind state.
-__device__ __host__ inline void reinit_cell(const DevParams& P, double dx, int i, int j, int k,
+__device__ __host__ __forceinline__ void reinit_cell(const DevParams& P, double dx, int i, int j, int k,
                                             double t, double* u) {
   double x = (i + 0.5) * dx - P.sun_c[0];
   double y = (j + 0.5) * dx - P.sun_c[1];

@@ -103,8 +103,9 @@ __global__ void __launch_bounds__(256)
   }
 }
 
+template <typename T>
 __global__ void __launch_bounds__(256)
-    k_exchange(double* __restrict__ U, const CopyReg* __restrict__ regs, int nc) {
+    k_exchange(T* __restrict__ U, const CopyReg* __restrict__ regs, int nc) {
   const CopyReg R = regs[blockIdx.x];
   const int n = R.ext[0] * R.ext[1] * R.ext[2];
   const long long scs = (long long)R.sfn[0] * R.sfn[1] * R.sfn[2];
@@ -198,7 +199,13 @@ cudaError_t launch_finalize(const DevParams& P, const DtPartial* partials, const
 
 cudaError_t launch_exchange(double* u, const CopyReg* regs, int nreg, int nc, cudaStream_t s) {
   if (nreg <= 0) return cudaSuccess;
-  k_exchange<<<nreg, 256, 0, s>>>(u, regs, nc);
+  k_exchange<double><<<nreg, 256, 0, s>>>(u, regs, nc);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_exchange_f(float* u, const CopyReg* regs, int nreg, int nc, cudaStream_t s) {
+  if (nreg <= 0) return cudaSuccess;
+  k_exchange<float><<<nreg, 256, 0, s>>>(u, regs, nc);
   return cudaGetLastError();
 }
 
