@@ -372,11 +372,27 @@ mf_status mf_level_set_time(mf_level* lev, double time);
 mf_status mf_level_time(mf_level* lev, double* time);
 /* Kernel launches enqueued by one mf_level_step (for accounting). */
 int mf_level_launches_per_step(const mf_level* lev);
+/* Schedule of the level's stages (no reference counterpart; the results do
+   not depend on it beyond FP32 rounding of the fluxes).  tile = {0,0,0}: the
+   split kernels (face fluxes of each direction in HBM, then the update);
+   tile = a shape in cells (x, y, z; z ignored in 2D; at most 256 cells and
+   the shared memory of two blocks per SM): one fused kernel per stage that
+   computes the fluxes of each tile in shared memory and updates it.  The
+   fused kernel covers MF_PREC_MIXED and MF_PREC_MIXED_CE32 with RK2 or first
+   order, without constrained transport, characteristic reconstruction,
+   tracking surfaces or central Bn (else MF_ERR_UNSUPPORTED); while a
+   hierarchy's flux registers are attached the level uses the split kernels.
+   Mixed-precision levels start fused with 8x8x4 tiles (16x16 in 2D) when
+   supported.  mf_level_schedule returns the current tile ({0,0,0}: split). */
+mf_status mf_level_set_schedule(mf_level* lev, const int tile[3]);
+mf_status mf_level_schedule(const mf_level* lev, int tile[3]);
 /* Diagnostic (no reference counterpart): one step enqueued launch by launch
    (no graph) with a CUDA event after every launch on the launching stream;
    ms[i] is the device time of launch i, kinds[i] its kernel kind (0 ghost
    exchange, 1 primitive variables, 2 face fluxes, 3 update + sources,
-   4 dt reduction).  The state advances by one step with time step dt. */
+   4 dt reduction, 5 hierarchy coupling, 6 problem post-processing,
+   7 constrained transport, 8 fused fluxes + update).  The state advances by
+   one step with time step dt. */
 mf_status mf_level_profile_step(mf_level* lev, double dt, float* ms, int* kinds, int* nlaunch,
                                 int max_launch);
 

@@ -376,7 +376,69 @@ struct mf_level {
   mf::Batch bp;
   DevBuf far;
   mf::LeanPrim lp;
+  // fused flux + update kernel (mixed precision): tile work lists of both
+  // stages' batches (fp1 for b1, fp2 for b2), used while no flux-register
+  // gathers are attached
+  bool fused = false;
+  int fused_saving = 0;  // launches the fused kernel saves per step
+  DevBuf tiles;
+  mf::FusedPlan fp1, fp2;
 };
+
+// Work list of the fused kernel: each desc's valueBox cut into tiles of the
+// given shape (the last tile of a row may be shorter).
+static std::vector<mf::FusedTile> make_tiles(const std::vector<StageDesc>& hd, int sd,
+                                             const int tile[3]) {
+  std::vector<mf::FusedTile> out;
+  for (int i = 0; i < (int)hd.size(); ++i) {
+    const StageDesc& D = hd[i];
+    const int t[3] = {tile[0], tile[1], sd == 3 ? tile[2] : 1};
+    for (int z = 0; z < D.vn[2]; z += t[2])
+      for (int y = 0; y < D.vn[1]; y += t[1])
+        for (int x = 0; x < D.vn[0]; x += t[0]) {
+          mf::FusedTile T;
+          T.desc = i;
+          const int o[3] = {x, y, z};
+          for (int d = 0; d < 3; ++d) {
+            T.lo[d] = D.vlo[d] + o[d];
+            T.n[d] = std::min(t[d], D.vn[d] - o[d]);
+          }
+          out.push_back(T);
+        }
+  }
+  return out;
+}
+
+// (Re)build the fused work lists for a tile shape; *ok false when the shape
+// does not fit (threads, shared memory).
+static cudaError_t level_set_tiles(mf_level* L, const int tile[3], bool* ok) {
+  const mf_params& p = L->ctx->p;
+  const int sd = p.space_dim;
+  *ok = false;
+  if (!mf::fused_tile_ok(L->ctx->dp, tile)) return cudaSuccess;
+  cudaError_t e = mf::fused_prepare();
+  if (e != cudaSuccess) return e;
+  std::vector<mf::FusedTile> t1 = make_tiles(L->hd1, sd, tile);
+  std::vector<mf::FusedTile> t2 = make_tiles(L->hd2, sd, tile);
+  std::vector<mf::FusedTile> all(t1);
+  all.insert(all.end(), t2.begin(), t2.end());
+  e = L->tiles.ensure(sizeof(mf::FusedTile) * std::max<size_t>(1, all.size()));
+  if (e != cudaSuccess) return e;
+  e = cudaMemcpy(L->tiles.p, all.data(), sizeof(mf::FusedTile) * all.size(),
+                 cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return e;
+  const int most = (int)std::max(t1.size(), t2.size());
+  e = L->partials.ensure(sizeof(DtPartial) * (std::max(L->nparts, most) + 1));
+  if (e != cudaSuccess) return e;
+  for (int q = 0; q < 2; ++q) {
+    mf::FusedPlan& fp = q ? L->fp2 : L->fp1;
+    fp.tiles = (const mf::FusedTile*)L->tiles.p + (q ? t1.size() : 0);
+    fp.ntiles = (int)(q ? t2.size() : t1.size());
+    for (int d = 0; d < 3; ++d) fp.tile[d] = (d < sd) ? tile[d] : 1;
+  }
+  *ok = true;
+  return cudaSuccess;
+}
 
 extern "C" {
 
@@ -1320,10 +1382,17 @@ static mf_status enqueue_level_step(mf_level* L, int advance, cudaEvent_t* ev = 
   const mf::LeanPrim* lean = L->lean ? &L->lp : nullptr;
   B.lean = lean;
   const int np0 = mf::prim_launches(lean, mixed);
+  // the fused flux + update kernel, unless flux registers need the face fluxes
+  const bool fused = L->fused && L->gathers.empty();
   auto stage_marks = [&](int n0) {
     if (!ev) return;
     kinds[n0] = 1;
     for (int q = 1; q < np0; ++q) kinds[n0 + q] = 0;
+    if (fused) {
+      kinds[n0 + np0] = 8;
+      ne = n0 + np0 + 1;
+      return;
+    }
     for (int d = 0; d < sd; ++d) kinds[n0 + np0 + d] = 2;
     kinds[n0 + np0 + sd] = 3;
     ne = n0 + np0 + 1 + sd;
@@ -1373,6 +1442,7 @@ static mf_status enqueue_level_step(mf_level* L, int advance, cudaEvent_t* ev = 
     B.uin = (const double*)L->U.p;
     B.uout = (double*)L->U1.p;
     B.ev = ev ? ev + ne : nullptr;
+    B.fused = fused ? &L->fp1 : nullptr;
     MF_CHECK_CUDA(mf::launch_stage(c->dp, p.precision, B, L->b1, 0, 1.0, ds, parts, &nb, s));
     stage_marks(ne);
     if (ct && (gst = ct_stage(L->b1, B.w, e1, nullptr, nullptr, (double*)L->U1.p, nullptr,
@@ -1388,6 +1458,7 @@ static mf_status enqueue_level_step(mf_level* L, int advance, cudaEvent_t* ev = 
     B.uout = (double*)L->U.p;
     B.uold = (const double*)L->U.p;
     B.ev = ev ? ev + ne : nullptr;
+    B.fused = fused ? &L->fp2 : nullptr;
     MF_CHECK_CUDA(mf::launch_stage(c->dp, p.precision, B, L->b2,
                                    ct ? 0 : (mf::kStageAverage | mf::kStageDt), 0.5, ds, parts,
                                    &nb, s));
@@ -1426,6 +1497,7 @@ static mf_status enqueue_level_step(mf_level* L, int advance, cudaEvent_t* ev = 
     B.uin = (const double*)L->U.p;
     B.uout = (double*)L->U.p;
     B.ev = ev ? ev + ne : nullptr;
+    B.fused = fused ? &L->fp2 : nullptr;
     MF_CHECK_CUDA(mf::launch_stage(c->dp, p.precision, B, L->b2, ct ? 0 : mf::kStageDt, 1.0, ds,
                                    parts, &nb, s));
     stage_marks(ne);
@@ -1437,7 +1509,8 @@ static mf_status enqueue_level_step(mf_level* L, int advance, cudaEvent_t* ev = 
     }
     if ((gst = gather(2)) != MF_OK) return gst;
   }
-  MF_CHECK_CUDA(mf::launch_finalize(c->dp, parts, L->b2, L->b2.nt[2], ds, advance, s));
+  MF_CHECK_CUDA(mf::launch_finalize(c->dp, parts, L->b2, L->b2.nt[2], ds, advance, s,
+                                    fused ? L->fp2.ntiles : 0));
   mark(4);
   // HeliosphericProblem::postTimeStep (swlism/HeliosphericProblem.cpp:2472-2535),
   // after the step and its dt (AMRLevelIdealMHD::advance)
@@ -1633,6 +1706,16 @@ mf_status mf_level_create(mf_ctx* c, int npatch, const mf_box* valid, mf_level**
                            ? 1
                            : 0;
   }
+  if (mf::fused_supported(c->dp, p.precision, p.time_approximation)) {
+    const int t3[3] = {8, 8, 4}, t2[3] = {16, 16, 1};
+    bool ok = false;
+    cudaError_t te = level_set_tiles(L, sd == 3 ? t3 : t2, &ok);
+    if (te != cudaSuccess) {
+      mf_level_destroy(L);
+      return te == cudaErrorMemoryAllocation ? MF_ERR_OOM : MF_ERR_CUDA;
+    }
+    L->fused = ok;
+  }
   const int per_stage = mf::stage_launches(sd);
   L->launches = (p.time_approximation == MF_TA_RK2) ? (2 * per_stage + 2 + 1)
                 : (p.time_approximation == MF_TA_HANCOCK) ? (mf::hancock_launches(sd) + 1 + 1)
@@ -1645,11 +1728,14 @@ mf_status mf_level_create(mf_ctx* c, int npatch, const mf_box* valid, mf_level**
     if (p.time_approximation == MF_TA_RK2 && L->ntwo) L->launches -= 1;
     L->launches += stages * (mf::prim_launches(&L->lp, mixed) - 1);
   }
+  // one fused kernel instead of the fluxes and the update (while no gathers)
+  L->fused_saving = L->fused ? ((p.time_approximation == MF_TA_RK2) ? 2 : 1) * sd : 0;
   if (L->nsun) L->launches += 1;
   // constrained transport: edge field + recalculation per stage, the dt after
   // them, and the level's recalculation
   if (c->dp.ct) L->launches += (p.time_approximation == MF_TA_RK2) ? 6 : 4;
   L->base_launches = L->launches;
+  L->launches -= L->fused_saving;
   *out = L;
   return MF_OK;
 }
@@ -1675,6 +1761,14 @@ void mf_level_destroy(mf_level* L) {
   L->state2.release();
   L->sun.release();
   L->hstate.release();
+  L->ct_u0.release();
+  L->ct_e1.release();
+  L->ct_e2.release();
+  L->ct_eo.release();
+  L->packed.release();
+  L->Wf.release();
+  L->far.release();
+  L->tiles.release();
   delete L;
 }
 
@@ -1913,6 +2007,40 @@ mf_status mf_level_time(mf_level* L, double* time) {
 }
 
 int mf_level_launches_per_step(const mf_level* L) { return L ? L->launches : -1; }
+
+mf_status mf_level_set_schedule(mf_level* L, const int tile[3]) {
+  if (!L || !tile) return MF_ERR_BAD_ARG;
+  const mf_params& p = L->ctx->p;
+  const int sd = p.space_dim;
+  bool fused = false;
+  if (tile[0] != 0) {
+    if (!mf::fused_supported(L->ctx->dp, p.precision, p.time_approximation))
+      return MF_ERR_UNSUPPORTED;
+    const int t[3] = {tile[0], tile[1], sd == 3 ? tile[2] : 1};
+    if (!mf::fused_tile_ok(L->ctx->dp, t)) return MF_ERR_BAD_ARG;
+    mf_status st = wait_stream(L->s, L->ctx->timeout);  // the old lists may be in use
+    if (st != MF_OK) return st;
+    bool ok = false;
+    MF_CHECK_CUDA(level_set_tiles(L, t, &ok));
+    if (!ok) return MF_ERR_BAD_ARG;
+    fused = true;
+  }
+  const int per = (p.time_approximation == MF_TA_RK2) ? 2 : 1;
+  L->fused = fused;
+  L->fused_saving = fused ? per * sd : 0;
+  L->launches = L->base_launches + per * (int)L->gathers.size() -
+                (L->gathers.empty() ? L->fused_saving : 0);
+  if (L->gsync) cudaGraphExecDestroy(L->gsync);
+  if (L->gasync) cudaGraphExecDestroy(L->gasync);
+  L->gsync = L->gasync = nullptr;
+  return MF_OK;
+}
+
+mf_status mf_level_schedule(const mf_level* L, int tile[3]) {
+  if (!L || !tile) return MF_ERR_BAD_ARG;
+  for (int d = 0; d < 3; ++d) tile[d] = L->fused ? L->fp1.tile[d] : 0;
+  return MF_OK;
+}
 
 mf_status mf_level_profile_step(mf_level* L, double dt, float* ms, int* kinds, int* nlaunch,
                                 int max_launch) {
@@ -2203,7 +2331,9 @@ void level_set_gathers(mf_level* L, const std::vector<FaceGather>& g) {
   if (L->gasync) cudaGraphExecDestroy(L->gasync);
   L->gsync = L->gasync = nullptr;
   const int per = (L->ctx->p.time_approximation == MF_TA_RK2) ? 2 : 1;
-  L->launches = L->base_launches + per * (int)g.size();
+  // the fused kernel keeps no face fluxes to gather: with gathers the level
+  // steps through the split flux and update kernels
+  L->launches = L->base_launches + per * (int)g.size() - (g.empty() ? L->fused_saving : 0);
 }
 
 mf_status status_of_flags(unsigned flags) { return flags_status(flags); }

@@ -179,6 +179,14 @@ struct LeanPrim {
   int exchange_w;            // copy the FP64 W (else only the FP32 copy)
 };
 
+struct FusedTile;
+// The tiles of one stage's batch for the fused flux + update kernel.
+struct FusedPlan {
+  const FusedTile* tiles;  // device work list
+  int ntiles;
+  int tile[3];             // tile shape (cells)
+};
+
 struct StageBuffers {
   const double* uin;   // state the stage starts from
   double* uout;        // state the stage writes (valueBox cells only)
@@ -197,6 +205,7 @@ struct StageBuffers {
   int divb_lo[3], divb_n[3];
   cudaEvent_t* ev;     // optional: an event recorded after each launch (profiling)
   const LeanPrim* lean;  // optional: primitive state on valid cells + ghost copies
+  const FusedPlan* fused;  // optional (mixed precision): fluxes + update in one kernel
 };
 
 enum StageFlags : int { kStageAverage = 1, kStageDt = 2 };
@@ -254,10 +263,13 @@ cudaError_t launch_dt(const DevParams& P, const double* u, const Batch& b, DtPar
                       int* nblocks, cudaStream_t s);
 
 // Reduce the dt partials of the last stage per run (one block per run, over
-// the run's blocks of a launch with nt threads per block); advance = 1 also
-// writes each run's next dt (cfl * minimum) and GLM speeds into state[run].
+// the run's blocks of a launch with nt threads per block; nparts > 0: a
+// single run whose partials are [0, nparts), e.g. one per fused tile);
+// advance = 1 also writes each run's next dt (cfl * minimum) and GLM speeds
+// into state[run].
 cudaError_t launch_finalize(const DevParams& P, const DtPartial* partials, const Batch& b,
-                            int nt, StepState* state, int advance, cudaStream_t s);
+                            int nt, StepState* state, int advance, cudaStream_t s,
+                            int nparts = 0);
 
 cudaError_t launch_exchange(double* u, const CopyReg* regs, int nreg, int nc, cudaStream_t s);
 cudaError_t launch_exchange_f(float* u, const CopyReg* regs, int nreg, int nc, cudaStream_t s);
@@ -318,6 +330,24 @@ cudaError_t launch_edges_out(int sd, const double* e, const mf_box& fab, const m
 // Number of kernel launches enqueued by launch_stage for sd dimensions
 // (plus prim_launches - 1 with a lean primitive part).
 inline int stage_launches(int sd) { return 2 + sd; }
+
+// Fused flux + update stage kernel of the mixed-precision level step
+// (mf_fused.cu): one block per tile of a desc's valueBox.
+struct FusedTile {
+  int desc;   // desc index in the batch
+  int lo[3];  // first cell (index space)
+  int n[3];   // extents (at most the tile shape)
+};
+// the options the fused kernel covers, and the tile shapes it accepts
+bool fused_supported(const DevParams& P, int precision, int time_approximation);
+bool fused_tile_ok(const DevParams& P, const int tile[3]);
+size_t fused_smem_bytes(const DevParams& P, const int tile[3]);
+// once per device before the first launch (sets the kernels' shared-memory limit)
+cudaError_t fused_prepare();
+// fluxes + update of the tiles; the dt partials are per tile (one per block)
+cudaError_t launch_fused(const DevParams& P, const StageBuffers& B, const Batch& b,
+                         const FusedTile* tiles, int ntiles, const int tile[3], int flags,
+                         double dt_scale, StepState* state, DtPartial* partials, cudaStream_t s);
 
 // Hancock step (predictorHancock + correctorHancock) of the patches of a
 // (predictor descs: valueBox = box.grow(1) & domain, W box, slope box, face

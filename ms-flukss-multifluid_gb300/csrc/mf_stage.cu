@@ -37,6 +37,14 @@ cudaError_t launch_stage(const DevParams& P, int precision, const StageBuffers& 
     if (e != cudaSuccess) return e;
     if (B.ev) cudaEventRecord(B.ev[ne++], s);
   }
+  if (B.fused && precision == MF_PREC_MIXED) {
+    e = launch_fused(P, B, b, B.fused->tiles, B.fused->ntiles, B.fused->tile, flags, dt_scale,
+                     state, partials, s);
+    if (e != cudaSuccess) return e;
+    if (nblocks_v) *nblocks_v = B.fused->ntiles;
+    if (B.ev) cudaEventRecord(B.ev[ne++], s);
+    return cudaSuccess;
+  }
   for (int d = 0; d < P.sd; ++d) {
     if (precision == MF_PREC_MIXED)
       e = launch_flux_fast<float>(P, d, B.w, B.f[d], B.bn[d], b, state, s, B.wf);

@@ -57,10 +57,11 @@ __device__ __forceinline__ bool part_less(const DtPartial& a, const DtPartial& b
 __global__ void __launch_bounds__(256)
     k_finalize(const DevParams P, const DtPartial* __restrict__ parts,
                const RunParams* __restrict__ runs, int nt, StepState* __restrict__ states,
-               int advance) {
+               int advance, int nparts) {
   const RunParams& R = runs[blockIdx.x];
   StepState* __restrict__ ss = states + blockIdx.x;
-  const int p0 = R.v0 / nt, p1 = (R.v1 + nt - 1) / nt;
+  const int p0 = (nparts > 0) ? 0 : R.v0 / nt;
+  const int p1 = (nparts > 0) ? nparts : (R.v1 + nt - 1) / nt;
   DtPartial best;
   best.dt = DBL_MAX;
   best.desc = INT_MAX;
@@ -191,9 +192,10 @@ cudaError_t launch_dt(const DevParams& P, const double* u, const Batch& b, DtPar
 }
 
 cudaError_t launch_finalize(const DevParams& P, const DtPartial* partials, const Batch& b,
-                            int nt, StepState* state, int advance, cudaStream_t s) {
+                            int nt, StepState* state, int advance, cudaStream_t s, int nparts) {
   if (b.nruns <= 0) return cudaSuccess;
-  k_finalize<<<b.nruns, 256, 0, s>>>(P, partials, b.runs, nt, state, advance);
+  k_finalize<<<nparts > 0 ? 1 : b.nruns, 256, 0, s>>>(P, partials, b.runs, nt, state, advance,
+                                                     nparts);
   return cudaGetLastError();
 }
 

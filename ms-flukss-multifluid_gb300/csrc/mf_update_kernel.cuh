@@ -122,15 +122,95 @@ __device__ __forceinline__ double warp_psi_damping(const StageDesc* Dp,
   return __shfl_sync(0xffffffffu, v, src);
 }
 
+// The update of one cell after its flux divergence: u holds the stage-start
+// state minus dt/dx times the flux differences (UPDATECONS); divB is the
+// cell's face-normal B divergence (8-wave source).  Sources with the
+// stage-start primitive state, the GLM damping psi_damp, charge exchange,
+// problem post-processing and positivity, the tracking surfaces' floor, RK2
+// averaging, the store, and the cell's dt (into dtc / myidx = g).
 // CE: arithmetic type of the charge-exchange rates (double, or float in the
-// MF_PREC_MIXED_CE32 form); R: type of the face fluxes.
+// MF_PREC_MIXED_CE32 form); R: type of the face fluxes (the wave speeds'
+// type).
+template <typename R, int GLM, int FLAGS, typename CE>
+__device__ __forceinline__ void update_tail(const DevParams& P, const StageBuffers& B,
+                                            const StageDesc& D, const RunParams& RP,
+                                            StepState* __restrict__ ss, int i, int j, int k,
+                                            long long base, long long cs, double dt,
+                                            double psi_damp, double divB, double* u, int g,
+                                            double& dtc, int& myidx) {
+  constexpr int IRHON = 8 + GLM;
+  const double* __restrict__ wst = B.wls ? B.wls : B.w;
+  // addExplicitSources (srcIdeal/PatchMHDMF.cpp:1149-1389) with the
+  // stage-start primitive state
+  double w[MF_MAX_COMP];
+  const bool need_w = P.use8 || (P.ce && P.nf >= 2);
+  if (need_w) {
+#pragma unroll
+    for (int q = 0; q < MF_MAX_COMP; ++q)
+      if (q < P.ils) w[q] = B.w[base + q * cs];
+  }
+  if (P.use8) {
+    // SOURCE8WAVES (srcIdeal/PatchIdealMHDF.ChF:681-722) + ADDSOURCES
+    const double dtbydx = dt / RP.dx;
+    const double dB = -divB * dtbydx;
+    const double Ux = w[1], Uy = w[2], Uz = w[3];
+    const double Bx = kInv4Pi * w[5], By = kInv4Pi * w[6], Bz = kInv4Pi * w[7];
+    u[1] = u[1] + dB * Bx;
+    u[2] = u[2] + dB * By;
+    u[3] = u[3] + dB * Bz;
+    u[4] = u[4] + dB * (Bx * Ux + By * Uy + Bz * Uz);
+    u[5] = u[5] + dB * Ux;
+    u[6] = u[6] + dB * Uy;
+    u[7] = u[7] + dB * Uz;
+  }
+  if (GLM) u[8] = psi_damp * u[8];  // PSIPARABOLIC (src/DednerF.ChF:65-87)
+  if (P.ce && P.nf >= 2) {
+    const double regtr = P.reg_tracer ? B.w[base + (P.nc - 1) * cs] : 0.0;
+    const int reg = region_cell(P, RP.dx, i, j, k, w, regtr);
+    charge_exchange_add<IRHON, CE>(P, w, reg, dt, u);
+  }
+  // problem post-processing and positivity (src/PatchMHDAM.cpp:705-707); with
+  // constrained transport they follow the recalculation of B (k_recalc_b)
+  if (!P.ct) {
+    if (P.reinit) reinit_cell(P, RP.dx, i, j, k, stage_time(*ss, dt), u);
+    positivity_cell<IRHON>(P, u);
+  }
+  if (P.nls) {  // POSTPROCESSING_LS (srcIdeal/PatchMHDMF.cpp:1414-1424)
+    const int x[3] = {i, j, k};
+    const double f0 = ls_floor(P, RP, wst, B.uin, D.fn, base, cs, x, P.ils);
+    const double f1 = (P.nls > 1) ? ls_floor(P, RP, wst, B.uin, D.fn, base, cs, x, P.ils + 1)
+                                  : 0.0;
+#pragma unroll
+    for (int q = 0; q < MF_MAX_COMP; ++q)
+      if (q >= P.ils && q < P.nc) u[q] = fmax(u[q], (q == P.ils) ? f0 : f1);
+  }
+
+  if (FLAGS & kStageAverage) {  // AVERAGESTATE (src/PatchMHDAMF.ChF:289-316), every state
+#pragma unroll
+    for (int q = 0; q < MF_MAX_COMP; ++q)
+      if (q < P.nc) u[q] = u[q] + 0.5 * (B.uold[base + q * cs] - B.uin[base + q * cs]);
+  }
+  bool finite = true;
+#pragma unroll
+  for (int q = 0; q < MF_MAX_COMP; ++q)
+    if (q < P.nc) {
+      finite = finite && isfinite(u[q]);
+      B.uout[base + q * cs] = u[q];
+    }
+  if (!finite) atomicOr(&ss->flags, kFlagNonFinite);
+  if (FLAGS & kStageDt) {
+    dtc = RP.dx / max_wave_speed<IRHON, R>(P, u);
+    myidx = g;
+    if (B.divb && P.use8) B.divb[loc(B.divb_lo, B.divb_n, i, j, k)] = divB;
+  }
+}
+
 template <typename R, int GLM, int FLAGS, typename CE = double>
 __global__ void __launch_bounds__(kMaxBlock, sizeof(R) == 4 ? 2 : 1)
     k_update(const DevParams P, const StageBuffers B, const StageDesc* __restrict__ descs,
              int ndesc, int total, const RunParams* __restrict__ runs,
              StepState* __restrict__ states, const double dt_scale,
              DtPartial* __restrict__ partials) {
-  constexpr int IRHON = 8 + GLM;
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
   double dtc = DBL_MAX;
   int myidx = INT_MAX;
@@ -203,16 +283,6 @@ __global__ void __launch_bounds__(kMaxBlock, sizeof(R) == 4 ? 2 : 1)
       for (int q = 0; q < MF_MAX_COMP; ++q)
         if (q < P.ils) u[q] = u[q] - dtinv * (double)fsum[q];
     }
-
-    // addExplicitSources (srcIdeal/PatchMHDMF.cpp:1149-1389) with the
-    // stage-start primitive state
-    double w[MF_MAX_COMP];
-    const bool need_w = P.use8 || (P.ce && P.nf >= 2);
-    if (need_w) {
-#pragma unroll
-      for (int q = 0; q < MF_MAX_COMP; ++q)
-        if (q < P.ils) w[q] = B.w[base + q * cs];
-    }
     double divB = 0.0;
     if (P.use8) {
 #pragma unroll
@@ -229,59 +299,9 @@ __global__ void __launch_bounds__(kMaxBlock, sizeof(R) == 4 ? 2 : 1)
             divB = divB + (double)Bd[sf] - (double)Bd[0];  // COMPUTEDIVB
         }
       }
-      // SOURCE8WAVES (srcIdeal/PatchIdealMHDF.ChF:681-722) + ADDSOURCES
-      const double dtbydx = dt / RP.dx;
-      const double dB = -divB * dtbydx;
-      const double Ux = w[1], Uy = w[2], Uz = w[3];
-      const double Bx = kInv4Pi * w[5], By = kInv4Pi * w[6], Bz = kInv4Pi * w[7];
-      u[1] = u[1] + dB * Bx;
-      u[2] = u[2] + dB * By;
-      u[3] = u[3] + dB * Bz;
-      u[4] = u[4] + dB * (Bx * Ux + By * Uy + Bz * Uz);
-      u[5] = u[5] + dB * Ux;
-      u[6] = u[6] + dB * Uy;
-      u[7] = u[7] + dB * Uz;
     }
-    if (GLM) u[8] = psi_damp * u[8];  // PSIPARABOLIC (src/DednerF.ChF:65-87)
-    if (P.ce && P.nf >= 2) {
-      const double regtr = P.reg_tracer ? B.w[base + (P.nc - 1) * cs] : 0.0;
-      const int reg = region_cell(P, RP.dx, i, j, k, w, regtr);
-      charge_exchange_add<IRHON, CE>(P, w, reg, dt, u);
-    }
-    // problem post-processing and positivity (src/PatchMHDAM.cpp:705-707); with
-    // constrained transport they follow the recalculation of B (k_recalc_b)
-    if (!P.ct) {
-      if (P.reinit) reinit_cell(P, RP.dx, i, j, k, stage_time(*ss, dt), u);
-      positivity_cell<IRHON>(P, u);
-    }
-    if (P.nls) {  // POSTPROCESSING_LS (srcIdeal/PatchMHDMF.cpp:1414-1424)
-      const int x[3] = {i, j, k};
-      const double f0 = ls_floor(P, RP, wst, B.uin, D.fn, base, cs, x, P.ils);
-      const double f1 = (P.nls > 1) ? ls_floor(P, RP, wst, B.uin, D.fn, base, cs, x, P.ils + 1)
-                                    : 0.0;
-#pragma unroll
-      for (int q = 0; q < MF_MAX_COMP; ++q)
-        if (q >= P.ils && q < P.nc) u[q] = fmax(u[q], (q == P.ils) ? f0 : f1);
-    }
-
-    if (FLAGS & kStageAverage) {  // AVERAGESTATE (src/PatchMHDAMF.ChF:289-316), every state
-#pragma unroll
-      for (int q = 0; q < MF_MAX_COMP; ++q)
-        if (q < P.nc) u[q] = u[q] + 0.5 * (B.uold[base + q * cs] - B.uin[base + q * cs]);
-    }
-    bool finite = true;
-#pragma unroll
-    for (int q = 0; q < MF_MAX_COMP; ++q)
-      if (q < P.nc) {
-        finite = finite && isfinite(u[q]);
-        B.uout[base + q * cs] = u[q];
-      }
-    if (!finite) atomicOr(&ss->flags, kFlagNonFinite);
-    if (FLAGS & kStageDt) {
-      dtc = RP.dx / max_wave_speed<IRHON, R>(P, u);
-      myidx = g;
-      if (B.divb && P.use8) B.divb[loc(B.divb_lo, B.divb_n, i, j, k)] = divB;
-    }
+    update_tail<R, GLM, FLAGS, CE>(P, B, D, RP, ss, i, j, k, base, cs, dt, psi_damp, divB, u, g,
+                                   dtc, myidx);
   }
   if (FLAGS & kStageDt) block_dt_min(dtc, myidx, descs, ndesc, partials);
 }

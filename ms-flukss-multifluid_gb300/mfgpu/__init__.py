@@ -197,6 +197,8 @@ _SIGS = {
     "mf_level_set_time": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double]),
     "mf_level_time": (ctypes.c_int, [ctypes.c_void_p, _P(ctypes.c_double)]),
     "mf_level_launches_per_step": (ctypes.c_int, [ctypes.c_void_p]),
+    "mf_level_set_schedule": (ctypes.c_int, [ctypes.c_void_p, c_int3]),
+    "mf_level_schedule": (ctypes.c_int, [ctypes.c_void_p, c_int3]),
     "mf_level_profile_step": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double,
                                              _P(ctypes.c_float), _P(ctypes.c_int),
                                              _P(ctypes.c_int), ctypes.c_int]),
@@ -730,8 +732,18 @@ class Level:
     def launches_per_step(self):
         return self.lib.mf_level_launches_per_step(self.h)
 
+    def set_schedule(self, tile=(0, 0, 0)):
+        """mf_level_set_schedule: (0,0,0) split kernels, else the fused
+        kernel's tile shape."""
+        check(self.lib.mf_level_set_schedule(self.h, c_int3(*tile)), "mf_level_set_schedule")
+
+    def schedule(self):
+        t = c_int3()
+        check(self.lib.mf_level_schedule(self.h, t), "mf_level_schedule")
+        return tuple(t)
+
     KIND_NAMES = {0: "exchange", 1: "prim", 2: "flux", 3: "update", 4: "finalize", 5: "coupling",
-                  6: "postprocess", 7: "constrained transport"}
+                  6: "postprocess", 7: "constrained transport", 8: "fused"}
 
     def profile_step(self, dt):
         """One step launch by launch with CUDA events between the launches;
