@@ -207,7 +207,7 @@ __device__ double edge_gs2(const FaceView<R>& F, const WAt& w, const int* lo, co
 // stage's field and the step average written on the same edges.
 template <typename R>
 __global__ void __launch_bounds__(kMaxBlock)
-    k_efield(const DevParams P, const void* f0, const void* f1, const void* f2,
+    k_efield(const __grid_constant__ DevParams P, const void* f0, const void* f1, const void* f2,
              const double* __restrict__ W, double* __restrict__ E, const double* __restrict__ E1,
              double* __restrict__ Eavg, const StageDesc* __restrict__ descs, int ndesc,
              int total) {
@@ -293,7 +293,7 @@ __device__ __forceinline__ void recalc_cell(int sd, double HX, const UAt& u, con
 // the neutral fluids start at component 8.
 template <int POST>
 __global__ void __launch_bounds__(kMaxBlock)
-    k_recalc_b(const DevParams P, double* __restrict__ U, const double* __restrict__ Bold,
+    k_recalc_b(const __grid_constant__ DevParams P, double* __restrict__ U, const double* __restrict__ Bold,
                const double* __restrict__ E, const double* __restrict__ U0,
                const double* __restrict__ U1, const StepState* __restrict__ states,
                double dt_scale, const StageDesc* __restrict__ descs, int ndesc, int total,

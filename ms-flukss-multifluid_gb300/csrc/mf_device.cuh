@@ -6,6 +6,7 @@
 // which changes no result (x + 0*y == x for finite y).
 #pragma once
 
+#include <cmath>
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -116,6 +117,44 @@ struct StageDesc {
 };
 
 // Plasma state and current-sheet surface value of the inner-sphere reset.
+// The parameters of the inner-sphere reset, copied out of DevParams so that
+// the out-of-line reset takes them by value (a kernel parameter passed by
+// reference to a function that is not inlined would be copied into every
+// thread's local memory).
+struct ReinitIn {
+  double rint, sun_rho, sun_v, sun_p, gamma, hgamma, dir_br, sun_b, sun_beta;
+  double sin_tilt, cos_tilt;
+  int monopolar;
+};
+
+__device__ __host__ __forceinline__ ReinitIn reinit_in(const DevParams& P) {
+  ReinitIn r;
+  r.rint = P.rint;
+  r.sun_rho = P.sun_rho;
+  r.sun_v = P.sun_v;
+  r.sun_p = P.sun_p;
+  r.gamma = P.gamma;
+  r.hgamma = P.hgamma;
+  r.dir_br = P.dir_br;
+  r.sun_b = P.sun_b;
+  r.sun_beta = P.sun_beta;
+  r.sin_tilt = P.sin_tilt;
+  r.cos_tilt = P.cos_tilt;
+  r.monopolar = P.monopolar;
+  return r;
+}
+
+// sin and cos of a phase through sincospi(phase / pi) on the device (exact
+// argument reduction, no out-of-line slow path); sin / cos on the host.
+__device__ __host__ __forceinline__ void reinit_sincos(double ph, double& sn, double& cs) {
+#ifdef __CUDA_ARCH__
+  sincospi(ph / kPi, &sn, &cs);
+#else
+  sn = std::sin(ph);
+  cs = std::cos(ph);
+#endif
+}
+
 struct ReinitState {
   double u[8];
   double hcs;

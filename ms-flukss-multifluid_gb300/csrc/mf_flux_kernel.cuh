@@ -208,20 +208,21 @@ __device__ void helio_plasma(const DevParams& P, const RunParams& RP, int side, 
     bn = Bx;
     return;
   }
-  const double* Win = side ? wl : wr;
-  const double* Wout = side ? wr : wl;
-  const double sg = side ? 1.0 : -1.0;
+  // element-wise selects at fixed indices keep both face states in registers
+  // (a pointer chosen at run time between two arrays would put them in local memory)
+  const bool hi = side != 0;
+  const double sg = hi ? 1.0 : -1.0;
   double L[8], Rt[8], F[8], Bv;
-  L[0] = Win[0];
-  Rt[0] = Wout[0];
-  L[4] = Win[4];
-  Rt[4] = Wout[4];
+  L[0] = hi ? wl[0] : wr[0];
+  Rt[0] = hi ? wr[0] : wl[0];
+  L[4] = hi ? wl[4] : wr[4];
+  Rt[4] = hi ? wr[4] : wl[4];
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
-    L[1 + a] = sg * Win[iv[a]];
-    Rt[1 + a] = sg * Wout[iv[a]];
-    L[5 + a] = sg * Win[ib[a]];
-    Rt[5 + a] = sg * Wout[ib[a]];
+    L[1 + a] = sg * (hi ? wl[iv[a]] : wr[iv[a]]);
+    Rt[1 + a] = sg * (hi ? wr[iv[a]] : wl[iv[a]]);
+    L[5 + a] = sg * (hi ? wl[ib[a]] : wr[ib[a]]);
+    Rt[5 + a] = sg * (hi ? wr[ib[a]] : wl[ib[a]]);
   }
   Rt[0] = fmax(P.smallr, Rt[0]);
   Rt[4] = fmax(P.smallp, Rt[4]);
@@ -246,8 +247,13 @@ __device__ void helio_neutral(const DevParams& P, int side, int fl, const double
                               const double* nr, double* gn) {
   constexpr int t1 = (DIR + 1) % 3, t2 = (DIR + 2) % 3;
   const int nv[3] = {1 + DIR, 1 + t1, 1 + t2};
-  const double* Win = side ? nl : nr;
-  const double* Wout = side ? nr : nl;
+  const bool hi = side != 0;
+  double Win[5], Wout[5];
+#pragma unroll
+  for (int c = 0; c < 5; ++c) {
+    Win[c] = hi ? nl[c] : nr[c];
+    Wout[c] = hi ? nr[c] : nl[c];
+  }
   auto outflow = [&](const double* st, double vn) {
     const double rho = st[0], vt1 = st[2], vt2 = st[3], p = st[4];
     const double ke = rho * (vn * vn + vt1 * vt1 + vt2 * vt2);
@@ -308,7 +314,7 @@ __device__ __forceinline__ int helio_side(const DevParams& P, const RunParams& R
 // wrote (R = float), instead of converting W value by value here.
 template <typename R, int DIR, int WF>
 __global__ void __launch_bounds__(kMaxBlock, WF ? 2 : 1)
-    k_flux(const DevParams P, const double* __restrict__ W, const float* __restrict__ Wf,
+    k_flux(const __grid_constant__ DevParams P, const double* __restrict__ W, const float* __restrict__ Wf,
            R* __restrict__ F, R* __restrict__ Bn, const StageDesc* __restrict__ descs, int ndesc,
            int total, const RunParams* __restrict__ runs, const StepState* __restrict__ states) {
   const int gi = blockIdx.x * blockDim.x + threadIdx.x;
@@ -488,7 +494,7 @@ __global__ void __launch_bounds__(kMaxBlock, WF ? 2 : 1)
 // + v)*cells(slope) + cell], side 0 = low face, 1 = high face.
 template <typename R, int DIR>
 __global__ void __launch_bounds__(kMaxBlock)
-    k_hflux(const DevParams P, const double* __restrict__ W, const double* __restrict__ FV,
+    k_hflux(const __grid_constant__ DevParams P, const double* __restrict__ W, const double* __restrict__ FV,
             R* __restrict__ F, R* __restrict__ Bn, const StageDesc* __restrict__ descs, int ndesc,
             int total, const RunParams* __restrict__ runs, const StepState* __restrict__ states) {
   const int gi = blockIdx.x * blockDim.x + threadIdx.x;
@@ -613,7 +619,7 @@ cudaError_t launch_hflux_t(const DevParams& P, int dir, const double* w, const d
 // (fluxes out as FP64).
 template <typename R, int DIR>
 __global__ void __launch_bounds__(128)
-    k_face_flux(const DevParams P, const double* __restrict__ wl, const double* __restrict__ wr,
+    k_face_flux(const __grid_constant__ DevParams P, const double* __restrict__ wl, const double* __restrict__ wr,
                 double* __restrict__ f, int n, double ch) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n) return;

@@ -197,7 +197,8 @@ __device__ __forceinline__ void group_faces(const DevParams& P, const RunParams&
                                             const float* __restrict__ sw,
                                             float* __restrict__ sf,
                                             unsigned char* __restrict__ sneg) {
-  for (int f = threadIdx.x; f < TF.off[P.sd]; f += blockDim.x) {
+  const int nf = (P.sd == 3) ? TF.off[3] : TF.off[2];  // (static indices)
+  for (int f = threadIdx.x; f < nf; f += blockDim.x) {
     if (f < TF.off[1])
       face_group<0, GLM>(P, RP, SS, S, T, grp, TF.fn[0], f, f, sw, sf, sneg);
     else if (f < TF.off[2])
@@ -243,7 +244,7 @@ __device__ __forceinline__ void group_accumulate(const DevParams& P, const Fused
 
 template <int GLM, int FLAGS, typename CE>
 __global__ void __launch_bounds__(kFusedThreads, 2)
-    k_fused(const DevParams P, const StageBuffers B, const StageDesc* __restrict__ descs,
+    k_fused(const __grid_constant__ DevParams P, const __grid_constant__ StageBuffers B, const StageDesc* __restrict__ descs,
             int ndesc, const FusedTile* __restrict__ tiles, const FusedShape S,
             const RunParams* __restrict__ runs, StepState* __restrict__ states,
             const double dt_scale, DtPartial* __restrict__ partials) {

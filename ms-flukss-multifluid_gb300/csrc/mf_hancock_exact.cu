@@ -29,7 +29,7 @@ __device__ __forceinline__ long long dstride(const int* n, int d) {
 }
 
 __global__ void __launch_bounds__(kMaxBlock)
-    k_hfaces(const DevParams P, const double* __restrict__ W, HancockBuffers H,
+    k_hfaces(const __grid_constant__ DevParams P, const double* __restrict__ W, HancockBuffers H,
              const StageDesc* __restrict__ descs, int ndesc, int total) {
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= total) return;
@@ -194,7 +194,7 @@ __device__ __forceinline__ void hpredict_dir(const DevParams& P, const RunParams
 
 template <int GLM>
 __global__ void __launch_bounds__(kMaxBlock)
-    k_hpredict(const DevParams P, const double* __restrict__ U, const double* __restrict__ W,
+    k_hpredict(const __grid_constant__ DevParams P, const double* __restrict__ U, const double* __restrict__ W,
                HancockBuffers H, const StageDesc* __restrict__ descs, int ndesc, int total,
                const RunParams* __restrict__ runs, const StepState* __restrict__ states) {
   constexpr int IRHON = 8 + GLM;
@@ -265,7 +265,7 @@ __global__ void __launch_bounds__(kMaxBlock)
 }
 
 __global__ void __launch_bounds__(kMaxBlock)
-    k_hshift(const DevParams P, const double* __restrict__ W, HancockBuffers H,
+    k_hshift(const __grid_constant__ DevParams P, const double* __restrict__ W, HancockBuffers H,
              const StageDesc* __restrict__ descs, int ndesc, int total,
              const RunParams* __restrict__ runs) {
   const int g = blockIdx.x * blockDim.x + threadIdx.x;

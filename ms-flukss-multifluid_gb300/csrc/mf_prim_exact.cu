@@ -11,7 +11,7 @@ namespace mf {
 namespace {
 template <int GLM>
 __global__ void __launch_bounds__(kMaxBlock)
-    k_prim(const DevParams P, const double* __restrict__ U, double* __restrict__ W,
+    k_prim(const __grid_constant__ DevParams P, const double* __restrict__ U, double* __restrict__ W,
            float* __restrict__ Wf, const StageDesc* __restrict__ descs, int ndesc, int total,
            const RunParams* __restrict__ runs) {
   constexpr int IRHON = 8 + GLM;
@@ -93,7 +93,7 @@ __global__ void __launch_bounds__(kMaxBlock)
 // corner) its conserved state never changes and is converted here.
 template <int GLM>
 __global__ void __launch_bounds__(256)
-    k_farfield(const DevParams P, const double* __restrict__ U, double* __restrict__ W,
+    k_farfield(const __grid_constant__ DevParams P, const double* __restrict__ U, double* __restrict__ W,
                float* __restrict__ Wf, const FarReg* __restrict__ regs,
                const RunParams* __restrict__ runs, int have_w) {
   constexpr int IRHON = 8 + GLM;

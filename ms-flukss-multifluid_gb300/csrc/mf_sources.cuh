@@ -231,9 +231,9 @@ __device__ __forceinline__ void charge_exchange_add(const DevParams& P, const do
 // plasma in r <= Rinit becomes the radial wind at time t (the stage's start
 // time plus its dt); bipolar field: B flips where the colatitude is not
 // below the current sheet's, and the current-sheet surface takes +1 / -1.
-// The wind state of a cell inside the sphere, out of line: only the few
-// cells of the sphere execute it.
-static __device__ __host__ __noinline__ void reinit_state(const DevParams& P, double x,
+// The wind state of a cell inside the sphere.  Inlined: a call out of line
+// would cost the whole calling kernel local-memory traffic.
+static __device__ __host__ __forceinline__ void reinit_state(const ReinitIn P, double x,
                                                           double y, double z, double r2,
                                                           double t, ReinitState& o) {
   o.hcs = 0.0;
@@ -258,8 +258,8 @@ static __device__ __host__ __noinline__ void reinit_state(const DevParams& P, do
   const double e0 = pr / P.hgamma + 0.5 * (rho * P.sun_v * P.sun_v + kInv4Pi * b);
   if (!P.monopolar) {
     const double theta = acos(cosT);
-    const double ph = P.sun_beta * (r - P.sun_v * t);
-    const double cosBr = cos(ph), sinBr = sin(ph);
+    double sinBr, cosBr;
+    reinit_sincos(P.sun_beta * (r - P.sun_v * t), sinBr, cosBr);
     const double sinB = sinF * cosBr + cosF * sinBr;
     const double cosB = cosF * cosBr - sinF * sinBr;
     const double ct = P.cos_tilt * cosB;
@@ -302,14 +302,15 @@ __device__ __host__ __forceinline__ void reinit_cell(const DevParams& P, double 
   if (!(r2 <= P.r0 * P.r0)) return;
 #endif
   ReinitState o;
-  reinit_state(P, x, y, z, r2, t, o);
+  reinit_state(reinit_in(P), x, y, z, r2, t, o);
 #pragma unroll
   for (int q = 0; q < 8; ++q) u[q] = o.u[q];
   if (!P.monopolar) {
-    // static indices keep u in registers (ihcs is -1 or a surface component)
+    // a select per component keeps u in registers (ihcs is -1 or a surface
+    // component; conditional stores would be merged into one indexed store,
+    // which puts u in local memory)
 #pragma unroll
-    for (int q = 8; q < MF_MAX_COMP; ++q)
-      if (q == P.ihcs) u[q] = o.hcs;
+    for (int q = 8; q < MF_MAX_COMP; ++q) u[q] = (q == P.ihcs) ? o.hcs : u[q];
   }
 }
 

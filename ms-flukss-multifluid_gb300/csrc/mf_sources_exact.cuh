@@ -205,9 +205,9 @@ __device__ __forceinline__ void charge_exchange_add(const DevParams& P, const do
 // (the stage's start time plus its dt), in the routine's order of
 // operations; sunBmonopolar != 1: the bipolar field (sign by theta < thetaS)
 // and the current-sheet surface iHCS (:1537-1564).
-// The wind state of a cell inside the sphere, out of line: only the few
-// cells of the sphere execute it.
-static __device__ __host__ __noinline__ void reinit_state(const DevParams& P, double x,
+// The wind state of a cell inside the sphere.  Inlined: a call out of line
+// would cost the whole calling kernel local-memory traffic.
+static __device__ __host__ __forceinline__ void reinit_state(const ReinitIn P, double x,
                                                           double y, double z, double r2,
                                                           double t, ReinitState& o) {
   o.hcs = 0.0;
@@ -232,8 +232,11 @@ static __device__ __host__ __noinline__ void reinit_state(const DevParams& P, do
   double e0 = pr / P.hgamma + 0.5 * (rho * P.sun_v * P.sun_v + kInv4Pi * b);
   if (!P.monopolar) {
     double theta = acos(cosT);
-    double cosBr = cos(P.sun_beta * (r - P.sun_v * t));
-    double sinBr = sin(P.sun_beta * (r - P.sun_v * t));
+    // cos / sin of the spiral phase sunBeta (r - sunV t), through the phase
+    // in units of pi (an exact argument reduction: no slow path for large
+    // phases); the phase only places the current sheet
+    double sinBr, cosBr;
+    reinit_sincos(P.sun_beta * (r - P.sun_v * t), sinBr, cosBr);
     double sinB = sinF * cosBr + cosF * sinBr;
     double cosB = cosF * cosBr - sinF * sinBr;
     double thetaS = P.sin_tilt * sinB / sqrt((P.cos_tilt * cosB) * (P.cos_tilt * cosB) + sinB * sinB);
@@ -265,14 +268,15 @@ __device__ __host__ __forceinline__ void reinit_cell(const DevParams& P, double 
   double r2 = (P.sd == 3) ? (x * x + y * y + z * z) : (x * x + y * y);
   if (!(r2 <= P.r0 * P.r0)) return;
   ReinitState o;
-  reinit_state(P, x, y, z, r2, t, o);
+  reinit_state(reinit_in(P), x, y, z, r2, t, o);
 #pragma unroll
   for (int q = 0; q < 8; ++q) u[q] = o.u[q];
   if (!P.monopolar) {
-    // static indices keep u in registers (ihcs is -1 or a surface component)
+    // a select per component keeps u in registers (ihcs is -1 or a surface
+    // component; conditional stores would be merged into one indexed store,
+    // which puts u in local memory)
 #pragma unroll
-    for (int q = 8; q < MF_MAX_COMP; ++q)
-      if (q == P.ihcs) u[q] = o.hcs;
+    for (int q = 8; q < MF_MAX_COMP; ++q) u[q] = (q == P.ihcs) ? o.hcs : u[q];
   }
 }
 

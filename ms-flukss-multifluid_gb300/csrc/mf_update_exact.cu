@@ -14,7 +14,7 @@ using namespace MF_PHYS;
 
 template <int GLM>
 __global__ void __launch_bounds__(kMaxBlock)
-    k_dt(const DevParams P, const double* __restrict__ U, const StageDesc* __restrict__ descs,
+    k_dt(const __grid_constant__ DevParams P, const double* __restrict__ U, const StageDesc* __restrict__ descs,
          int ndesc, int total, const RunParams* __restrict__ runs,
          DtPartial* __restrict__ partials) {
   constexpr int IRHON = 8 + GLM;
@@ -55,7 +55,7 @@ __device__ __forceinline__ bool part_less(const DtPartial& a, const DtPartial& b
 // time after the step, then (advance) its next dt and GLM speeds
 // (AMRLevelIdealMHD::advance, srcIdeal/AMRLevelIdealMHD.cpp:1531-1548, 1588).
 __global__ void __launch_bounds__(256)
-    k_finalize(const DevParams P, const DtPartial* __restrict__ parts,
+    k_finalize(const __grid_constant__ DevParams P, const DtPartial* __restrict__ parts,
                const RunParams* __restrict__ runs, int nt, StepState* __restrict__ states,
                int advance, int nparts) {
   const RunParams& R = runs[blockIdx.x];

@@ -207,7 +207,7 @@ __device__ __forceinline__ void update_tail(const DevParams& P, const StageBuffe
 
 template <typename R, int GLM, int FLAGS, typename CE = double>
 __global__ void __launch_bounds__(kMaxBlock, sizeof(R) == 4 ? 2 : 1)
-    k_update(const DevParams P, const StageBuffers B, const StageDesc* __restrict__ descs,
+    k_update(const __grid_constant__ DevParams P, const __grid_constant__ StageBuffers B, const StageDesc* __restrict__ descs,
              int ndesc, int total, const RunParams* __restrict__ runs,
              StepState* __restrict__ states, const double dt_scale,
              DtPartial* __restrict__ partials) {
