@@ -8,6 +8,7 @@
 #pragma once
 
 #include "mf_device.cuh"
+#include "mf_fp64.cuh"
 
 namespace mf {
 namespace fast {
@@ -19,8 +20,9 @@ constexpr double kInvPi = 0.318309886183790671537767526745028724;
 // are the routine's literals.  Its x > 650 test reads the x of the last
 // solar-wind cell the routine visited (x is assigned in that branch only);
 // here the cell's own x, the same on every domain within x <= 650.
+template <typename WA>
 __device__ __forceinline__ int region_tracer_cell(const DevParams& P, double dx, int i, int j,
-                                                  int k, const double* w, double regtr) {
+                                                  int k, const WA& w, double regtr) {
   const double x = __dadd_rn(__dmul_rn(i + 0.5, dx), -P.sun_c[0]);
   const double ux = w[1], uy = w[2], uz = w[3];
   int reg;
@@ -67,8 +69,9 @@ __device__ __forceinline__ int region_tracer_cell(const DevParams& P, double dx,
 // DEFINE_REGIONS_2F (swlism/SWLISMF.ChF:654-742), Cartesian branch, or the
 // tracer variant above (HeliosphericProblem::defineRegions,
 // swlism/HeliosphericProblem.cpp:2538-2575).
+template <typename WA>
 __device__ __forceinline__ int region_cell(const DevParams& P, double dx, int i, int j, int k,
-                                           const double* w, double regtr) {
+                                           const WA& w, double regtr) {
   if (P.reg_tracer) return region_tracer_cell(P, dx, i, j, k, w, regtr);
   const double x = __dadd_rn(__dmul_rn(i + 0.5, dx), -P.sun_c[0]);
   const double y = __dadd_rn(__dmul_rn(j + 0.5, dx), -P.sun_c[1]);
@@ -109,14 +112,17 @@ __device__ __forceinline__ int ce_recipient(int nN, int reg) {
   return (reg >= 1 && reg <= nN) ? reg : 0;
 }
 
-// Arithmetic type of the charge-exchange rates: FP64, or FP32 in the mixed
-// precision mode (the rates scale a source that is a small fraction of the
-// state per step; their FP32 rounding stays far below the FP32 error the
-// fluxes carry).  The state update itself is FP64 either way.
+// Arithmetic type of the charge-exchange rates: FP64, or FP32 in the opt-in
+// MF_PREC_MIXED_CE32 mode (the rates scale a source that is a small fraction
+// of the state per step).  The FP64 forms take the reciprocal and logarithm
+// of mf_fp64.cuh (within a few units of 2^-53 of the library's).  The state
+// update itself is FP64 either way.
 __device__ __forceinline__ double ce_rsqrt(double x) { return rsqrt(x); }
 __device__ __forceinline__ float ce_rsqrt(float x) { return rsqrtf(x); }
-__device__ __forceinline__ double ce_log(double x) { return log(x); }
+__device__ __forceinline__ double ce_log(double x) { return fp64::log64(x); }
 __device__ __forceinline__ float ce_log(float x) { return logf(x); }
+__device__ __forceinline__ double ce_rcp(double x) { return fp64::rcp64(x); }
+__device__ __forceinline__ float ce_rcp(float x) { return 1.0f / x; }
 __device__ __forceinline__ double ce_exp(double x) { return exp(x); }
 __device__ __forceinline__ float ce_exp(float x) { return expf(x); }
 __device__ __forceinline__ double ce_pow(double x, double y) { return pow(x, y); }
@@ -125,105 +131,101 @@ __device__ __forceinline__ float ce_pow(float x, float y) { return powf(x, y); }
 // Pauls & Zank charge-exchange rates of one cell; adds S = -dt*H to u
 // (HeliosphericProblem::explicitSource, swlism/HeliosphericProblem.cpp:1394-1539,
 // CHARGE_EXCHANGE_4F swlism/ChargeExchange2F.ChF:673-993 and _MF :995-1149).
-// T is the arithmetic type of the rates (double, or float in mixed precision).
-template <int IRHON, typename T = double>
-__device__ __forceinline__ void charge_exchange_add(const DevParams& P, const double* w, int reg,
+// T is the arithmetic type of the rates (double, or float in the opt-in
+// FP32-rate mode).  The plasma's thermal-speed terms that every neutral
+// population shares are formed once per cell.
+// w: the stage-start primitive state (an array, or a column view that
+// loads each component where it is used).
+template <int IRHON, typename T = double, typename WA = const double*>
+__device__ __forceinline__ void charge_exchange_add(const DevParams& P, const WA& w, int reg,
                                                     double dt, double* u) {
   const int nN = P.nf - 1;
   constexpr T c4p = T(4.0 * kInvPi), c16p = T(16.0 * kInvPi), c94pi = T(2.25 * kPi);
-  constexpr T cip = T(kInvPi), c649 = T(64.0 / 9.0);
+  constexpr T c4ip = T(4.0 * kInvPi), c649ip = T(64.0 / 9.0 * kInvPi);
   const T rho = T(w[0]), ux = T(w[1]), uy = T(w[2]), uz = T(w[3]);
-  const T U2 = ux * ux + uy * uy + uz * uz;
-  const T VVTP = T(w[4]) / rho;
+  const T U2 = ux * ux + uy * uy + uz * uz, hU2 = T(0.5) * U2;
+  const T VVTP = T(w[4]) * ce_rcp(rho);
+  // plasma thermal-speed terms of the five speed arguments
+  const T aUDp = c4p * VVTP, aUPMp = c16p * VVTP, aUHMp = c94pi * VVTP;
+  const T aPEp = c4ip * VVTP, aHEp = c649ip * VVTP, q75VP = T(0.75) * VVTP;
   const T scale_vel = T(P.ce_scale_vel), ce_a = T(P.ce_a), ce_b = T(P.ce_b);
-  const T damp_c = T(P.ce_damp_c), damp_pow = T(P.ce_damp_pow), sig_scale = T(P.ce_sigma_scale);
-  T h2 = 0, h3 = 0, h4 = 0, h5 = 0, PPLUX = 0, PPLUY = 0, PPLUZ = 0, ENPLU = 0;
-  T DENPLU[MF_MAX_FLUIDS], PMIX[MF_MAX_FLUIDS], PMIY[MF_MAX_FLUIDS], PMIZ[MF_MAX_FLUIDS],
-      ENMI[MF_MAX_FLUIDS];
+  const T damp_c = T(P.ce_damp_c), damp_pow = T(P.ce_damp_pow);
+  const T srho = T(P.ce_sigma_scale) * rho;
+  // Each population's own loss / gain is applied inside the loop; the
+  // recipient of the newly created neutrals (region-dependent) then also
+  // receives the plasma's totals.  The products ARR*UD, ARR*VVTHU and
+  // ARR*VP_UHM that several terms share are formed once, and the plasma's
+  // terms that carry a cell factor (ux, U2/2, 3 VVTP/4) are summed without it
+  // and scaled after the loop: the reference's H, summed in another order.
+  // G: the sum of ARR (VPHP VP_UHM + 3 VVTP UHE / 4), which both the energy
+  // source and the recipient's energy gain hold; H5: the rest of h5.
+  T h2 = 0, h3 = 0, h4 = 0, DSUM = 0, S1x = 0, S1y = 0, S1z = 0, G = 0, H5 = 0;
 #pragma unroll
   for (int f = 1; f < MF_MAX_FLUIDS; ++f) {
     if (f > nN) break;
-    const double* wn = w + IRHON + (f - 1) * 5;
-    const T rhoN = T(wn[0]), uxN = T(wn[1]), uyN = T(wn[2]), uzN = T(wn[3]);
+    const int o = IRHON + (f - 1) * 5;
+    const T rhoN = T(w[o]), uxN = T(w[o + 1]), uyN = T(w[o + 2]), uzN = T(w[o + 3]);
     const T dx_ = ux - uxN, dy_ = uy - uyN, dz_ = uz - uzN;
     const T UH2 = uxN * uxN + uyN * uyN + uzN * uzN;
-    const T DU2 = dx_ * dx_ + dy_ * dy_ + dz_ * dz_;
+    const T DU2 = dx_ * dx_ + dy_ * dy_ + dz_ * dz_, DU2x4 = T(4) * DU2;
     const T VPHH = dx_ * uxN + dy_ * uyN + dz_ * uzN;
     const T VPHP = dx_ * ux + dy_ * uy + dz_ * uz;
-    const T VVTH = T(2) * T(wn[4]) / rhoN;
+    const T VVTH = T(2) * (T(w[o + 4]) * ce_rcp(rhoN));
     // thermal + relative speeds; every argument is > 0, so sqrt(a) = a*rsqrt(a)
-    const T aUD = c4p * (VVTP + VVTH) + DU2;
+    const T aUD = (aUDp + c4p * VVTH) + DU2;
     const T UD = aUD * ce_rsqrt(aUD);
-    const T iUPM = ce_rsqrt(c16p * VVTP + c94pi * VVTH + T(4) * DU2);
-    const T iUHM = ce_rsqrt(c94pi * VVTP + c16p * VVTH + T(4) * DU2);
-    const T aPE = cip * (T(4) * VVTP + c649 * VVTH) + DU2;
+    const T iUPM = ce_rsqrt((aUPMp + c94pi * VVTH) + DU2x4);
+    const T iUHM = ce_rsqrt((aUHMp + c16p * VVTH) + DU2x4);
+    const T aPE = (aPEp + c649ip * VVTH) + DU2;
     const T UPE = aPE * ce_rsqrt(aPE);
-    const T aHE = cip * (c649 * VVTP + T(4) * VVTH) + DU2;
+    const T aHE = (aHEp + c4ip * VVTH) + DU2;
     const T UHE = aHE * ce_rsqrt(aHE);
     const T UDS = scale_vel * UD;
     const T t = ce_a - ce_b * ce_log(UDS);
     T SIG = t * t;
     if (damp_c > T(0)) SIG = SIG * ce_pow(T(1) - ce_exp(-damp_c / UDS), damp_pow);
-    const T ARR = sig_scale * SIG * rhoN * rho;
-    const T VVTHU = VVTH * iUPM;
-    const T VP_UHM = VVTP * iUHM;
-    const T hv = ARR * (UD + VVTHU + VP_UHM);
+    const T ARR = SIG * (rhoN * srho);
+    const T aU = ARR * UD;                  // -DENPLU
+    const T aT = ARR * (VVTH * iUPM);       // ARR*VVTHU
+    const T aV = ARR * (VVTP * iUHM);       // ARR*VP_UHM
+    const T Y = (ARR * UPE) * VVTH;
+    const T hv = aU + aT + aV;
     h2 = h2 + hv * dx_;
     h3 = h3 + hv * dy_;
     h4 = h4 + hv * dz_;
-    h5 = h5 + T(0.5) * ARR *
-                  (T(1.5) * (UHE * VVTP - UPE * VVTH) + UD * (U2 - UH2) +
-                   T(2) * (VVTHU * VPHH + VPHP * VP_UHM));
-    DENPLU[f] = -ARR * UD;
-    PPLUX = PPLUX - ARR * (ux * UD + dx_ * VP_UHM);
-    PPLUY = PPLUY - ARR * (uy * UD + dy_ * VP_UHM);
-    PPLUZ = PPLUZ - ARR * (uz * UD + dz_ * VP_UHM);
-    ENPLU = ENPLU - ARR * (T(0.5) * U2 * UD + VPHP * VP_UHM + T(0.75) * VVTP * UHE);
-    PMIX[f] = ARR * (uxN * UD - dx_ * VVTHU);
-    PMIY[f] = ARR * (uyN * UD - dy_ * VVTHU);
-    PMIZ[f] = ARR * (uzN * UD - dz_ * VVTHU);
-    ENMI[f] = ARR * (T(0.5) * UH2 * UD - VPHH * VVTHU + T(0.75) * VVTH * UPE);
+    S1x = S1x + aV * dx_;
+    S1y = S1y + aV * dy_;
+    S1z = S1z + aV * dz_;
+    DSUM = DSUM - aU;
+    G = G + aV * VPHP + q75VP * (ARR * UHE);
+    H5 = H5 + aT * VPHH + aU * (hU2 - T(0.5) * UH2) - T(0.75) * Y;
+    double* un = u + IRHON + (f - 1) * 5;
+    un[0] = un[0] - dt * double(aU);
+    un[1] = un[1] - dt * double(uxN * aU - dx_ * aT);
+    un[2] = un[2] - dt * double(uyN * aU - dy_ * aT);
+    un[3] = un[3] - dt * double(uzN * aU - dz_ * aT);
+    un[4] = un[4] - dt * double((T(0.5) * UH2) * aU - VPHH * aT + T(0.75) * Y);
   }
+  const T h5 = G + H5;
+  const T PPLUX = ux * DSUM - S1x, PPLUY = uy * DSUM - S1y, PPLUZ = uz * DSUM - S1z;
+  const T ENPLU = hU2 * DSUM - G;
   u[1] = u[1] - dt * double(h2);
   u[2] = u[2] - dt * double(h3);
   u[3] = u[3] - dt * double(h4);
   u[4] = u[4] - dt * double(h5);
-  // S of the magnetic field (and of psi) is zero
+  // S of the magnetic field (and of psi) is zero; the recipient gets the
+  // other populations' lost density (DSUM less its own, already applied)
   const int rk = ce_recipient(nN, reg);
 #pragma unroll
   for (int f = 1; f < MF_MAX_FLUIDS; ++f) {
     if (f > nN) break;
-    T H1, H2, H3, H4, H5;
-    if (f == rk) {
-      if (nN <= 3) {
-        H1 = 0;
-#pragma unroll
-        for (int q = 1; q < MF_MAX_FLUIDS; ++q)
-          if (q <= nN && q != f) H1 = H1 + DENPLU[q];
-      } else {
-        T sum = DENPLU[1];
-#pragma unroll
-        for (int q = 2; q < MF_MAX_FLUIDS; ++q)
-          if (q <= nN) sum = sum + DENPLU[q];
-        H1 = sum - DENPLU[f];
-      }
-      H2 = PPLUX + PMIX[f];
-      H3 = PPLUY + PMIY[f];
-      H4 = PPLUZ + PMIZ[f];
-      H5 = ENPLU + ENMI[f];
-    } else {
-      H1 = -DENPLU[f];
-      H2 = PMIX[f];
-      H3 = PMIY[f];
-      H4 = PMIZ[f];
-      H5 = ENMI[f];
-    }
+    const bool rec = (f == rk);
     double* un = u + IRHON + (f - 1) * 5;
-    un[0] = un[0] - dt * double(H1);
-    un[1] = un[1] - dt * double(H2);
-    un[2] = un[2] - dt * double(H3);
-    un[3] = un[3] - dt * double(H4);
-    un[4] = un[4] - dt * double(H5);
+    un[0] = rec ? un[0] - dt * double(DSUM) : un[0];
+    un[1] = rec ? un[1] - dt * double(PPLUX) : un[1];
+    un[2] = rec ? un[2] - dt * double(PPLUY) : un[2];
+    un[3] = rec ? un[3] - dt * double(PPLUZ) : un[3];
+    un[4] = rec ? un[4] - dt * double(ENPLU) : un[4];
   }
 }
 
@@ -380,46 +382,47 @@ __device__ __forceinline__ void positivity_cell(const DevParams& P, double* u) {
 }
 
 // MAXWAVESPEED (srcIdeal/PatchIdealMHDF.ChF:5-63) + MAXWAVESPEED_E
-// (srcIdeal/PatchEulerF.ChF:5-50) of one cell, in T (FP64, or FP32 in the
-// mixed precision mode, whose time step then carries FP32 rounding).
+// (srcIdeal/PatchEulerF.ChF:5-50) of one cell.  The pressure is recovered
+// from the total energy in FP64 (E minus kinetic minus magnetic cancels in
+// cold, low-beta flow); the speeds are formed in T (FP64, or FP32 in the
+// mixed precision modes, whose time step then carries FP32 rounding).
 __device__ __forceinline__ double ws_sqrt(double x) { return sqrt(x); }
 __device__ __forceinline__ float ws_sqrt(float x) { return sqrtf(x); }
 
 template <int IRHON, typename T = double>
 __device__ __forceinline__ double max_wave_speed(const DevParams& P, const double* u) {
-  const T i4pi = T(kInv4Pi), hg = T(P.hgamma), gam = T(P.gamma), sp = T(P.smallp);
+  const T i4pi = T(kInv4Pi), gam = T(P.gamma);
   T cmax = 0;
   {
-    const T invrho = T(1) / T(u[0]);
-    const T m1 = T(u[1]), m2 = T(u[2]), m3 = T(u[3]);
-    const T uu = m1 * invrho, vv = m2 * invrho, ww = m3 * invrho;
-    const T ke = m1 * uu + m2 * vv + m3 * ww;
-    const T bx = T(u[5]), by = T(u[6]), bz = T(u[7]);
-    const T b = i4pi * (bx * bx + by * by + bz * bz);
-    T p = hg * (T(u[4]) - T(0.5) * (ke + b));
-    p = fmax(p, sp);
-    const T a2 = gam * p * invrho;
+    const double rinv = fp64::rcp64(u[0]);
+    const double m1 = u[1], m2 = u[2], m3 = u[3], bx = u[5], by = u[6], bz = u[7];
+    const double ke = (m1 * m1 + m2 * m2 + m3 * m3) * rinv;
+    const double bb = kInv4Pi * (bx * bx + by * by + bz * bz);
+    const double p = fmax(P.hgamma * (u[4] - 0.5 * (ke + bb)), P.smallp);
+    const T invrho = T(rinv), b = T(bb);
+    const T uu = T(m1) * invrho, vv = T(m2) * invrho, ww = T(m3) * invrho;
+    const T bxt = T(bx), byt = T(by), bzt = T(bz);
+    const T a2 = gam * T(p) * invrho;
     const T as2 = T(0.5) * (a2 + invrho * b);
     const T as4 = as2 * as2;
     const T k4 = i4pi * invrho * a2;
     // as4 - k4 b^2 >= 0 exactly; contracted rounding can push it below 0
-    T umax = fabs(uu) + ws_sqrt(as2 + ws_sqrt(fmax(T(0), as4 - k4 * bx * bx)));
-    umax = fmax(fabs(vv) + ws_sqrt(as2 + ws_sqrt(fmax(T(0), as4 - k4 * by * by))), umax);
-    umax = fmax(fabs(ww) + ws_sqrt(as2 + ws_sqrt(fmax(T(0), as4 - k4 * bz * bz))), umax);
+    T umax = fabs(uu) + ws_sqrt(as2 + ws_sqrt(fmax(T(0), as4 - k4 * bxt * bxt)));
+    umax = fmax(fabs(vv) + ws_sqrt(as2 + ws_sqrt(fmax(T(0), as4 - k4 * byt * byt))), umax);
+    umax = fmax(fabs(ww) + ws_sqrt(as2 + ws_sqrt(fmax(T(0), as4 - k4 * bzt * bzt))), umax);
     cmax = fmax(umax, cmax);
   }
 #pragma unroll
   for (int f = 1; f < MF_MAX_FLUIDS; ++f) {
     if (f >= P.nf) break;
     const double* un = u + IRHON + (f - 1) * 5;
-    const T rho = fmax(T(un[0]), T(P.smallr));
-    const T invrho = T(1) / rho;
-    const T m1 = T(un[1]), m2 = T(un[2]), m3 = T(un[3]);
-    const T uu = m1 * invrho, vv = m2 * invrho, ww = m3 * invrho;
-    const T ke = m1 * uu + m2 * vv + m3 * ww;
-    T p = hg * (T(un[4]) - T(0.5) * ke);
-    p = fmax(p, sp);
-    const T a = ws_sqrt(gam * p * invrho);
+    const double rinv = fp64::rcp64(fmax(un[0], P.smallr));
+    const double m1 = un[1], m2 = un[2], m3 = un[3];
+    const double ke = (m1 * m1 + m2 * m2 + m3 * m3) * rinv;
+    const double p = fmax(P.hgamma * (un[4] - 0.5 * ke), P.smallp);
+    const T invrho = T(rinv);
+    const T uu = T(m1) * invrho, vv = T(m2) * invrho, ww = T(m3) * invrho;
+    const T a = ws_sqrt(gam * T(p) * invrho);
     const T umax = fmax(fmax(fabs(uu), fabs(vv)), fabs(ww)) + a;
     cmax = fmax(umax, cmax);
   }

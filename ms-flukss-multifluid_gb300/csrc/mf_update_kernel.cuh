@@ -4,6 +4,8 @@
 // namespace of the including unit.
 #pragma once
 
+#include <type_traits>
+
 #include "mf_kernels.cuh"
 
 namespace mf {
@@ -122,6 +124,19 @@ __device__ __forceinline__ double warp_psi_damping(const StageDesc* Dp,
   return __shfl_sync(0xffffffffu, v, src);
 }
 
+// The stage-start primitive state of a cell as the update tail reads it:
+// all components in registers, or a column of the W array read where used.
+struct WArray {
+  double v[MF_MAX_COMP];
+};
+struct WColumn {
+  const double* __restrict__ p;
+  long long cs;
+  __device__ __forceinline__ double operator[](int q) const { return __ldg(p + q * cs); }
+};
+__device__ __forceinline__ const double* w_arg(const WArray& w) { return w.v; }
+__device__ __forceinline__ const WColumn& w_arg(const WColumn& w) { return w; }
+
 // The update of one cell after its flux divergence: u holds the stage-start
 // state minus dt/dx times the flux differences (UPDATECONS); divB is the
 // cell's face-normal B divergence (8-wave source).  Sources with the
@@ -142,13 +157,19 @@ __device__ __forceinline__ void update_tail(const DevParams& P, const StageBuffe
   const double* __restrict__ wst = B.wls ? B.wls : B.w;
   // addExplicitSources (srcIdeal/PatchMHDMF.cpp:1149-1389) with the
   // stage-start primitive state
-  double w[MF_MAX_COMP];
-  const bool need_w = P.use8 || (P.ce && P.nf >= 2);
-  if (need_w) {
+  // FP64 fluxes: the primitive state in registers.  FP32 fluxes (mixed
+  // precision, 2 blocks per SM): a column view that loads each component
+  // where it is used, which keeps the register count within the bound.
+  typename std::conditional<sizeof(R) == 4, WColumn, WArray>::type ws;
+  if constexpr (sizeof(R) == 4) {
+    ws.p = B.w + base;
+    ws.cs = cs;
+  } else if (P.use8 || (P.ce && P.nf >= 2)) {
 #pragma unroll
     for (int q = 0; q < MF_MAX_COMP; ++q)
-      if (q < P.ils) w[q] = B.w[base + q * cs];
+      if (q < P.ils) ws.v[q] = B.w[base + q * cs];
   }
+  const auto& w = w_arg(ws);
   if (P.use8) {
     // SOURCE8WAVES (srcIdeal/PatchIdealMHDF.ChF:681-722) + ADDSOURCES
     const double dtbydx = dt / RP.dx;
