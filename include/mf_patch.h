@@ -382,8 +382,9 @@ int mf_level_launches_per_step(const mf_level* lev);
    order, without constrained transport, characteristic reconstruction,
    tracking surfaces or central Bn (else MF_ERR_UNSUPPORTED); while a
    hierarchy's flux registers are attached the level uses the split kernels.
-   Mixed-precision levels start fused with 8x8x4 tiles (16x16 in 2D) when
-   supported.  mf_level_schedule returns the current tile ({0,0,0}: split). */
+   Levels start with the split kernels; mf_level_autotune picks the
+   schedule by timing.  mf_level_schedule returns the current tile
+   ({0,0,0}: split). */
 mf_status mf_level_set_schedule(mf_level* lev, const int tile[3]);
 mf_status mf_level_schedule(const mf_level* lev, int tile[3]);
 /* Diagnostic (no reference counterpart): one step enqueued launch by launch
@@ -410,9 +411,15 @@ mf_status mf_face_fluxes(mf_ctx* ctx, int dir, int n, const double* wl, const do
    per patch).  Times the prim, flux and update kernels of the level's batch
    at 64, 128 and 256 threads per block (reps launches each, stage-1 form, so
    the level's state is not changed) and keeps the fastest shape of each
-   kind for later steps; previously captured step graphs are rebuilt.
-   threads (nullable) receives the chosen {prim, flux, update} shapes.
-   Results of a step do not depend on the shapes. */
+   kind for later steps.  Where the fused kernel covers the level's options
+   (see mf_level_set_schedule) and no flux registers are attached, it then
+   times stage 1 with the split kernels against the fused kernel at the tile
+   shapes 8x8x4, 8x4x4, 16x8x2, 8x8x2 and 4x4x4 (16x16, 32x8, 16x8, 8x8 in
+   2D) that fit, and keeps the fastest schedule (mf_level_schedule reads
+   it).  Previously captured step graphs are rebuilt.  threads (nullable)
+   receives the chosen {prim, flux, update} shapes.  Results of a step do not
+   depend on the shapes; the schedule changes them at most by FP32 rounding
+   of the charge-exchange rates in MF_PREC_MIXED_CE32. */
 mf_status mf_level_autotune(mf_level* lev, int reps, int threads[3]);
 
 /* ---- Hierarchy: levels coupled across refinement (Berger-Oliger) ----

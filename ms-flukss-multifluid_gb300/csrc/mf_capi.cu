@@ -1706,16 +1706,9 @@ mf_status mf_level_create(mf_ctx* c, int npatch, const mf_box* valid, mf_level**
                            ? 1
                            : 0;
   }
-  if (mf::fused_supported(c->dp, p.precision, p.time_approximation)) {
-    const int t3[3] = {8, 8, 4}, t2[3] = {16, 16, 1};
-    bool ok = false;
-    cudaError_t te = level_set_tiles(L, sd == 3 ? t3 : t2, &ok);
-    if (te != cudaSuccess) {
-      mf_level_destroy(L);
-      return te == cudaErrorMemoryAllocation ? MF_ERR_OOM : MF_ERR_CUDA;
-    }
-    L->fused = ok;
-  }
+  // the split flux and update kernels until mf_level_set_schedule or the
+  // autotuner picks the fused kernel
+  L->fused = false;
   const int per_stage = mf::stage_launches(sd);
   L->launches = (p.time_approximation == MF_TA_RK2) ? (2 * per_stage + 2 + 1)
                 : (p.time_approximation == MF_TA_HANCOCK) ? (mf::hancock_launches(sd) + 1 + 1)
@@ -2008,6 +2001,20 @@ mf_status mf_level_time(mf_level* L, double* time) {
 
 int mf_level_launches_per_step(const mf_level* L) { return L ? L->launches : -1; }
 
+// Make the level step with the fused kernel (its work lists already built)
+// or the split kernels; the captured graphs are rebuilt on next use.
+static void apply_schedule(mf_level* L, bool fused) {
+  const mf_params& p = L->ctx->p;
+  const int per = (p.time_approximation == MF_TA_RK2) ? 2 : 1;
+  L->fused = fused;
+  L->fused_saving = fused ? per * p.space_dim : 0;
+  L->launches = L->base_launches + per * (int)L->gathers.size() -
+                (L->gathers.empty() ? L->fused_saving : 0);
+  if (L->gsync) cudaGraphExecDestroy(L->gsync);
+  if (L->gasync) cudaGraphExecDestroy(L->gasync);
+  L->gsync = L->gasync = nullptr;
+}
+
 mf_status mf_level_set_schedule(mf_level* L, const int tile[3]) {
   if (!L || !tile) return MF_ERR_BAD_ARG;
   const mf_params& p = L->ctx->p;
@@ -2025,14 +2032,7 @@ mf_status mf_level_set_schedule(mf_level* L, const int tile[3]) {
     if (!ok) return MF_ERR_BAD_ARG;
     fused = true;
   }
-  const int per = (p.time_approximation == MF_TA_RK2) ? 2 : 1;
-  L->fused = fused;
-  L->fused_saving = fused ? per * sd : 0;
-  L->launches = L->base_launches + per * (int)L->gathers.size() -
-                (L->gathers.empty() ? L->fused_saving : 0);
-  if (L->gsync) cudaGraphExecDestroy(L->gsync);
-  if (L->gasync) cudaGraphExecDestroy(L->gasync);
-  L->gsync = L->gasync = nullptr;
+  apply_schedule(L, fused);
   return MF_OK;
 }
 
@@ -2080,8 +2080,9 @@ mf_status mf_level_profile_step(mf_level* L, double dt, float* ms, int* kinds, i
   return st;
 }
 
-// Time `reps` launches of one kernel kind of stage 1 (prim, fluxes of every
-// direction, update without averaging) with the level's current threads.
+// Time `reps` launches of one kernel kind of stage 1 (0 prim, 1 fluxes of
+// every direction, 2 update without averaging, 3 the fused flux + update
+// kernel on the work list in fp1) with the level's current threads.
 // Stage 1 reads U and writes only W, F, Bn and U1, so the level's state is
 // left as it was; the step state used is a private copy with dt = 0.
 static mf_status time_kind(mf_level* L, int kind, int reps, cudaEvent_t e0, cudaEvent_t e1,
@@ -2116,6 +2117,9 @@ static mf_status time_kind(mf_level* L, int kind, int reps, cudaEvent_t e0, cuda
         else
           e = mf::launch_flux_exact(c->dp, d, B.w, B.f[d], B.bn[d], b, ds, L->s);
       }
+    } else if (kind == 3) {  // the fused kernel on stage 1's work list
+      e = mf::launch_fused(c->dp, B, b, L->fp1.tiles, L->fp1.ntiles, L->fp1.tile, 0, 1.0, ds,
+                           parts, L->s);
     } else {
       int nb = 0;
       if (p.precision == MF_PREC_MIXED)
@@ -2167,6 +2171,46 @@ mf_status mf_level_autotune(mf_level* L, int reps, int threads[3]) {
       }
     }
     L->b1.nt[kind] = L->b2.nt[kind] = L->bp.nt[kind] = bnt;
+  }
+  // schedule: the split flux + update kernels against the fused kernel at
+  // each tile shape that fits the options, by the time of stage 1 (a level
+  // feeding flux registers keeps the split kernels, which store the fluxes)
+  const mf_params& p = c->p;
+  const int sd = p.space_dim;
+  if (st == MF_OK && mf::fused_supported(c->dp, p.precision, p.time_approximation) &&
+      L->gathers.empty()) {
+    float split = 0.f, tf = 0.f, tu = 0.f;
+    st = time_kind(L, 1, reps, e0, e1, &tf);
+    if (st == MF_OK) st = time_kind(L, 2, reps, e0, e1, &tu);
+    split = tf + tu;
+    static const int c3[][3] = {{8, 8, 4}, {8, 4, 4}, {16, 8, 2}, {8, 8, 2}, {4, 4, 4}};
+    static const int c2[][3] = {{16, 16, 1}, {32, 8, 1}, {16, 8, 1}, {8, 8, 1}};
+    const int ncand = (sd == 3) ? 5 : 4;
+    float best = split;
+    int bt[3] = {0, 0, 0};
+    for (int q = 0; q < ncand && st == MF_OK; ++q) {
+      const int* t = (sd == 3) ? c3[q] : c2[q];
+      bool ok = false;
+      if (level_set_tiles(L, t, &ok) != cudaSuccess) {
+        st = MF_ERR_CUDA;
+        break;
+      }
+      if (!ok) continue;
+      float ms = 0.f;
+      st = time_kind(L, 3, 1, e0, e1, &ms);  // warm-up
+      if (st == MF_OK) st = time_kind(L, 3, reps, e0, e1, &ms);
+      if (st == MF_OK && ms < best) {
+        best = ms;
+        for (int d = 0; d < 3; ++d) bt[d] = t[d];
+      }
+    }
+    bool fused = false;
+    if (st == MF_OK && bt[0] != 0) {
+      bool ok = false;
+      if (level_set_tiles(L, bt, &ok) != cudaSuccess) st = MF_ERR_CUDA;
+      fused = ok;
+    }
+    apply_schedule(L, st == MF_OK && fused);
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);

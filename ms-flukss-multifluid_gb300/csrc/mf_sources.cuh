@@ -325,7 +325,7 @@ __device__ __forceinline__ void positivity_cell(const DevParams& P, double* u) {
     double Rho = u[0];
     bool was = false;
     if (Rho < smallR) { Rho = smallR; was = true; }
-    const double invRho = 1.0 / Rho;
+    const double invRho = fp64::rcp64(Rho);
     const double Ux = u[1] * invRho, Uy = u[2] * invRho, Uz = u[3] * invRho;
     const double BxB = kInv8Pi * (u[5] * u[5] + u[6] * u[6] + u[7] * u[7]);
     const double UxU = 0.5 * (Ux * Ux + Uy * Uy + Uz * Uz);
@@ -339,7 +339,7 @@ __device__ __forceinline__ void positivity_cell(const DevParams& P, double* u) {
   }
   {
     const double Rho0 = u[0];
-    const double invRho = 1.0 / Rho0;
+    const double invRho = fp64::rcp64(Rho0);
     const double Ux = u[1] * invRho, Uy = u[2] * invRho, Uz = u[3] * invRho;
     const double BxB = kInv8Pi * (u[5] * u[5] + u[6] * u[6] + u[7] * u[7]);
     const double UxU = 0.5 * (Ux * Ux + Uy * Uy + Uz * Uz);
@@ -363,7 +363,7 @@ __device__ __forceinline__ void positivity_cell(const DevParams& P, double* u) {
     const double fp = (f == 1) ? smallP : (f == 3) ? kNet3Pres : kNet2Pres;
     double* un = u + IRHON + (f - 1) * 5;
     const double Rho0 = un[0];
-    const double invRho = 1.0 / Rho0;
+    const double invRho = fp64::rcp64(Rho0);
     const double Ux = un[1] * invRho, Uy = un[2] * invRho, Uz = un[3] * invRho;
     const double UxU = 0.5 * (Ux * Ux + Uy * Uy + Uz * Uz);
     double Pr = hg * (un[4] - Rho0 * UxU);

@@ -215,7 +215,8 @@ __device__ __forceinline__ void update_tail(const DevParams& P, const StageBuffe
 #pragma unroll
   for (int q = 0; q < MF_MAX_COMP; ++q)
     if (q < P.nc) {
-      finite = finite && isfinite(u[q]);
+      // exponent field not all ones: an integer test, off the FP64 pipe
+      finite = finite && ((__double2hiint(u[q]) & 0x7ff00000) != 0x7ff00000);
       B.uout[base + q * cs] = u[q];
     }
   if (!finite) atomicOr(&ss->flags, kFlagNonFinite);

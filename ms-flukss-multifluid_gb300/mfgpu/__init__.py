@@ -758,7 +758,9 @@ class Level:
 
     def autotune(self, reps=3):
         """mf_level_autotune: threads per block of the prim, flux and update
-        kernels picked by timing; returns the chosen (prim, flux, update)."""
+        kernels, and the schedule (split kernels or a fused tile shape, read
+        by schedule()), picked by timing; returns the chosen (prim, flux,
+        update) threads."""
         t = c_int3()
         check(self.lib.mf_level_autotune(self.h, reps, t), "mf_level_autotune")
         return tuple(t)

@@ -71,7 +71,7 @@ def test_fused_matches_split(gpulib, name):
     differences over later steps, as between any two FP32 evaluations)."""
     p, n, patch, sd, init = _params(name)
     ctx, lev, boxes, flat = _level(p, n, patch, sd, init)
-    assert lev.schedule() != (0, 0, 0)  # mixed levels start fused
+    assert lev.schedule() == (0, 0, 0)  # levels start with the split kernels
     dt0 = 0.4 * lev.compute_dt()[0]
     ce32 = name.endswith("ce32")
     nsteps = 1 if ce32 else 3
@@ -126,5 +126,27 @@ def test_schedule_arguments(gpulib):
         with pytest.raises(mfgpu.MfError) as ei:
             lev.set_schedule(bad)
         assert ei.value.code == mfgpu.MF_ERR_BAD_ARG
+    lev.close()
+    ctx.close()
+
+
+@pytest.mark.parametrize("prec", [mfgpu.PREC_MIXED, mfgpu.PREC_FP64])
+def test_autotune_picks_a_schedule(gpulib, prec):
+    """The autotuner leaves the level on a schedule it can run (split, or a
+    tile shape for mixed precision; split for FP64), and the level's steps
+    give the split kernels' results bitwise."""
+    p = mfgpu.helio_params(32, precision=prec)
+    ctx, lev, boxes, flat = _level(p, 32, 16, 3)
+    dt0 = 0.4 * lev.compute_dt()[0]
+    a, da = _steps(lev, flat, (0, 0, 0), 2, dt0)
+    lev.upload(flat.ctypes.data)
+    shapes = lev.autotune(2)
+    assert all(s in (64, 128, 256) for s in shapes)
+    sch = lev.schedule()
+    if prec == mfgpu.PREC_FP64:
+        assert sch == (0, 0, 0)
+    b, db = _steps(lev, flat, sch, 2, dt0)
+    assert lev.schedule() == sch
+    assert np.array_equal(a, b) and da == db
     lev.close()
     ctx.close()
