@@ -203,12 +203,17 @@ def _progress(what):
 
 
 def _time_steps(lev, torch, stream, steps):
+    """K asynchronous level steps between CUDA events on the launching
+    stream, inside an NVTX range "timed" (ncu --nvtx-include "timed/" then
+    captures the timed launches only)."""
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.nvtx.range_push("timed")
     ev0.record(stream)
     for _ in range(steps):
         lev.step_async(stream.cuda_stream)
     ev1.record(stream)
+    torch.cuda.nvtx.range_pop()
     torch.cuda.synchronize()
     return ev0.elapsed_time(ev1)
 

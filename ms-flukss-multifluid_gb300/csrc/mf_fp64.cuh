@@ -10,6 +10,8 @@
 // y <- y (1 + e + e^2), e = 1 - x y, whose truncation error is e^3 (< 2^-58):
 // 3 FP64 instructions, within one ulp of the correctly rounded 1/x.
 //
+// f2d: the exact FP32 -> FP64 conversion done with integer instructions.
+//
 // log64: Tang's table-driven method (P. T. P. Tang, "Table-driven
 // implementation of the logarithm function in IEEE floating-point
 // arithmetic", ACM TOMS 16(4), 1990): x = 2^k m with m in [1, 2), a table
@@ -92,6 +94,32 @@ __device__ __forceinline__ double log64(double x) {
   p = fma(p, r, -0.5);
   const double l1p = fma(p, r * r, r);
   return fma(kd, kLn2, t.y) + l1p;
+}
+
+// Exact FP32 -> FP64 conversion in integer arithmetic (the same value as
+// the conversion instruction, which issues on the FP64 pipe): sign and
+// fraction move into place, the exponent is rebiased by 1023 - 127; a
+// subnormal input is normalised by its leading-zero count; zero stays a
+// signed zero and inf / NaN keep their fraction.
+__device__ __forceinline__ double f2d(float f) {
+  const unsigned b = __float_as_uint(f);
+  const unsigned sign = b & 0x80000000u;
+  const unsigned e = (b >> 23) & 0xffu;
+  unsigned m = b & 0x007fffffu;
+  unsigned ed;
+  if (e == 0xffu) {
+    ed = 0x7ffu;
+  } else if (e != 0u) {
+    ed = e + 896u;
+  } else if (m == 0u) {
+    ed = 0u;
+  } else {  // subnormal: m * 2^-149, shift the leading one to bit 23
+    const int sh = __clz(m) - 8;
+    m = (m << sh) & 0x007fffffu;
+    ed = 897u - static_cast<unsigned>(sh);
+  }
+  return __hiloint2double(static_cast<int>(sign | (ed << 20) | (m >> 3)),
+                          static_cast<int>(m << 29));
 }
 
 }  // namespace fp64

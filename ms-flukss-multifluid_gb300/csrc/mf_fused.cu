@@ -238,7 +238,7 @@ __device__ __forceinline__ void group_accumulate(const DevParams& P, const Fused
     const float* bn = sf + kGroupMax * S.nfmax;
 #pragma unroll
     for (int d = 0; d < 3; ++d)
-      if (d < P.sd) divB = divB + (double)(bn[flo[d] + fs[d]] - bn[flo[d]]);
+      if (d < P.sd) divB = divB + fp64::f2d(bn[flo[d] + fs[d]] - bn[flo[d]]);
   }
 }
 
@@ -306,7 +306,7 @@ __global__ void __launch_bounds__(kFusedThreads, 2)
     const double dtinv = dt * RP.invdx;
 #pragma unroll
     for (int q = 0; q < MF_MAX_COMP; ++q)
-      if (q < P.ils) u[q] = u[q] - dtinv * (double)acc[q * kFusedThreads + t];
+      if (q < P.ils) u[q] = u[q] - dtinv * fp64::f2d(acc[q * kFusedThreads + t]);
     update_tail<float, GLM, FLAGS, CE>(P, B, D, RP, ss, i, j, k, base, cs, dt, psi_damp, divB, u,
                                        D.g0[kRegV] + lin, dtc, myidx);
   }

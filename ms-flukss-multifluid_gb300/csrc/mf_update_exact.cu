@@ -104,6 +104,13 @@ __global__ void __launch_bounds__(256)
   }
 }
 
+// One block per copy region, flat over its (component, cell) elements so
+// that small regions (edges, corners) still occupy the block; 32-bit index
+// arithmetic (a region is part of one patch's ghost layers: 2^31 elements
+// would take a patch whose fab alone exceeds HBM) and four loads
+// in flight per thread before their stores.  Sources are valid cells and
+// destinations ghost cells, never the same, so the sources are read through
+// the read-only path.
 template <typename T>
 __global__ void __launch_bounds__(256)
     k_exchange(T* __restrict__ U, const CopyReg* __restrict__ regs, int nc) {
@@ -111,19 +118,31 @@ __global__ void __launch_bounds__(256)
   const int n = R.ext[0] * R.ext[1] * R.ext[2];
   const long long scs = (long long)R.sfn[0] * R.sfn[1] * R.sfn[2];
   const long long dcs = (long long)R.dfn[0] * R.dfn[1] * R.dfn[2];
-  const long long tot = (long long)n * nc;
-  for (long long t = threadIdx.x; t < tot; t += blockDim.x) {
-    const int q = (int)(t / n);
-    const int c = (int)(t - (long long)q * n);
-    const int a = c % R.ext[0];
-    const int r = c / R.ext[0];
-    const int b = r % R.ext[1];
-    const int e = r / R.ext[1];
-    const long long so = R.src_off + q * scs + (R.s0[0] + a) +
-                         (long long)R.sfn[0] * ((R.s0[1] + b) + (long long)R.sfn[1] * (R.s0[2] + e));
-    const long long dof = R.dst_off + q * dcs + (R.d0[0] + a) +
-                          (long long)R.dfn[0] * ((R.d0[1] + b) + (long long)R.dfn[1] * (R.d0[2] + e));
-    U[dof] = U[so];
+  const int tot = n * nc;
+  const int step = blockDim.x;
+  for (int t0 = threadIdx.x; t0 < tot; t0 += 4 * step) {
+    T v[4];
+    long long dof[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int t = t0 + j * step;
+      if (t < tot) {
+        const int q = t / n;
+        const int c = t - q * n;
+        const int a = c % R.ext[0];
+        const int r = c / R.ext[0];
+        const int b = r % R.ext[1];
+        const int e = r / R.ext[1];
+        const long long so = R.src_off + q * scs + (R.s0[0] + a) +
+                             (long long)R.sfn[0] * ((R.s0[1] + b) + (long long)R.sfn[1] * (R.s0[2] + e));
+        dof[j] = R.dst_off + q * dcs + (R.d0[0] + a) +
+                 (long long)R.dfn[0] * ((R.d0[1] + b) + (long long)R.dfn[1] * (R.d0[2] + e));
+        v[j] = __ldg(U + so);
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+      if (t0 + j * step < tot) U[dof[j]] = v[j];
   }
 }
 

@@ -6,6 +6,7 @@
 
 #include <type_traits>
 
+#include "mf_fp64.cuh"
 #include "mf_kernels.cuh"
 
 namespace mf {
@@ -14,10 +15,10 @@ using namespace MF_PHYS;
 
 // Difference of the fluxes on the two faces of a cell.  FP64 fluxes: in
 // FP64.  FP32 fluxes (mixed precision): in FP32, whose rounding is below the
-// FP32 error the fluxes already carry; the accumulation into the state stays
-// FP64.
+// FP32 error the fluxes already carry, converted exactly with integer
+// instructions (fp64::f2d); the accumulation into the state stays FP64.
 __device__ __forceinline__ double flux_diff(double hi, double lo) { return hi - lo; }
-__device__ __forceinline__ double flux_diff(float hi, float lo) { return (double)(hi - lo); }
+__device__ __forceinline__ double flux_diff(float hi, float lo) { return fp64::f2d(hi - lo); }
 
 // Floor of POSTPROCESSING_LS (src/LevelSetF.ChF:426-465) for surface q of
 // the cell at x (offset base): the minimum of the stage-start values of the
@@ -303,7 +304,7 @@ __global__ void __launch_bounds__(kMaxBlock, sizeof(R) == 4 ? 2 : 1)
     if constexpr (sizeof(R) == 4) {
 #pragma unroll
       for (int q = 0; q < MF_MAX_COMP; ++q)
-        if (q < P.ils) u[q] = u[q] - dtinv * (double)fsum[q];
+        if (q < P.ils) u[q] = u[q] - dtinv * fp64::f2d(fsum[q]);
     }
     double divB = 0.0;
     if (P.use8) {
@@ -316,7 +317,7 @@ __global__ void __launch_bounds__(kMaxBlock, sizeof(R) == 4 ? 2 : 1)
                                                        : (long long)fnb[0] * fnb[1];
           const R* __restrict__ Bd = (const R*)B.bn[d] + D.bn_off[d] + loc(D.vlo, fnb, i, j, k);
           if constexpr (sizeof(R) == 4)
-            divB = divB + (double)(Bd[sf] - Bd[0]);  // COMPUTEDIVB, FP32 difference
+            divB = divB + fp64::f2d(Bd[sf] - Bd[0]);  // COMPUTEDIVB, FP32 difference
           else
             divB = divB + (double)Bd[sf] - (double)Bd[0];  // COMPUTEDIVB
         }

@@ -40,6 +40,22 @@ __global__ void k_check(int n, unsigned long long* worst) {
   }
 }
 
+// f2d against the conversion instruction, bit for bit, on every exponent
+// (subnormals, zeros, inf and NaN included) with hashed fractions and signs
+__global__ void k_f2d(int n, unsigned* mismatches) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  uint32_t h = (uint32_t)i * 2654435761u;
+  h ^= h >> 16;
+  h *= 2246822519u;
+  h ^= h >> 13;
+  const unsigned bits = (h & 0x807fffffu) | ((unsigned)(i & 0xff) << 23);
+  const float f = __uint_as_float(bits);
+  const double a = mf::fp64::f2d(f), b = (double)f;
+  const bool same = (__double_as_longlong(a) == __double_as_longlong(b)) || (isnan(a) && isnan(b));
+  if (!same) atomicAdd(mismatches, 1u);
+}
+
 __global__ void k_special(int* bad) {
   const double xs[8] = {0.0, -0.0, -1.0, 4.9406564584124654e-324, 1e-310, INFINITY, -INFINITY, NAN};
   int b = 0;
@@ -62,12 +78,18 @@ int main() {
   cudaMemset(w, 0, 2 * sizeof(unsigned long long));
   k_check<<<(n + 255) / 256, 256>>>(n, w);
   k_special<<<1, 1>>>(bad);
+  unsigned* mm;
+  if (cudaMalloc(&mm, sizeof(unsigned)) != cudaSuccess) return 2;
+  cudaMemset(mm, 0, sizeof(unsigned));
+  k_f2d<<<(n + 255) / 256, 256>>>(n, mm);
+  unsigned hm = 1;
+  cudaMemcpy(&hm, mm, sizeof(unsigned), cudaMemcpyDeviceToHost);
   unsigned long long hw[2];
   int hb = -1;
   cudaMemcpy(hw, w, sizeof(hw), cudaMemcpyDeviceToHost);
   cudaMemcpy(&hb, bad, sizeof(int), cudaMemcpyDeviceToHost);
   const cudaError_t e = cudaDeviceSynchronize();
-  printf("rcp64_ulp %.4f\nlog64_ulp %.4f\nspecial_mismatch %d\nstatus %s\n", hw[0] / 1024.0,
-         hw[1] / 1024.0, hb, cudaGetErrorString(e));
+  printf("rcp64_ulp %.4f\nlog64_ulp %.4f\nspecial_mismatch %d\nf2d_mismatch %u\nstatus %s\n",
+         hw[0] / 1024.0, hw[1] / 1024.0, hb, hm, cudaGetErrorString(e));
   return e == cudaSuccess ? 0 : 1;
 }
