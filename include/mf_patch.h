@@ -387,6 +387,23 @@ int mf_level_launches_per_step(const mf_level* lev);
    ({0,0,0}: split). */
 mf_status mf_level_set_schedule(mf_level* lev, const int tile[3]);
 mf_status mf_level_schedule(const mf_level* lev, int tile[3]);
+
+/* Overlap of the split flux and update kernels (no reference counterpart;
+   results unchanged, bit for bit).  chunks = 1: one flux launch per direction
+   and one update launch per stage.  chunks = 2..MF_MAX_OVERLAP_CHUNKS: the
+   level's patches are cut into about that many chunks of consecutive patches
+   (each starting on a multiple of 256 cells; fewer where the patches do not
+   allow more) and each stage runs the FP32 flux kernels of the chunks on a
+   second stream while the update of the previous chunk runs, so the
+   FP64-bound update and the FP32 fluxes share the SMs; streams are ordered
+   by events only.  MF_PREC_MIXED and MF_PREC_MIXED_CE32 with RK2 or first
+   order and without constrained transport (else MF_ERR_UNSUPPORTED); the
+   fused schedule, attached flux registers and mf_level_profile_step use
+   unchunked launches.  mf_level_overlap returns the current chunk count;
+   mf_level_autotune picks it by timing. */
+#define MF_MAX_OVERLAP_CHUNKS 8
+mf_status mf_level_set_overlap(mf_level* lev, int chunks);
+mf_status mf_level_overlap(const mf_level* lev, int* chunks);
 /* Diagnostic (no reference counterpart): one step enqueued launch by launch
    (no graph) with a CUDA event after every launch on the launching stream;
    ms[i] is the device time of launch i, kinds[i] its kernel kind (0 ghost

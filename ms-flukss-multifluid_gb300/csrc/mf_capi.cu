@@ -383,7 +383,29 @@ struct mf_level {
   int fused_saving = 0;  // launches the fused kernel saves per step
   DevBuf tiles;
   mf::FusedPlan fp1, fp2;
+  // chunked, overlapped flux + update launches of the split mixed-precision
+  // stages (mf_level_set_overlap): a chunk plan per stage batch, the flux
+  // stream and its events (created on first use)
+  int nchunks = 1;
+  std::vector<mf::Chunk> ch1, ch2;
+  mf::OverlapPlan op1{}, op2{};
+  cudaStream_t s2 = nullptr;
+  cudaEvent_t ov_ev[MF_MAX_OVERLAP_CHUNKS + 1] = {};
 };
+
+// Kernel launches of one step: the plain count, plus the flux-register
+// gathers, less the flux launches the fused kernel replaces, plus the extra
+// flux and update launches of the chunked overlap.
+static void count_launches(mf_level* L) {
+  const mf_params& p = L->ctx->p;
+  const int per = (p.time_approximation == MF_TA_RK2) ? 2 : 1;
+  const int sd = p.space_dim;
+  const bool fused = L->fused && L->gathers.empty();
+  const bool overlap = L->nchunks > 1 && !L->fused && L->gathers.empty() && !L->ctx->dp.ct;
+  L->fused_saving = L->fused ? per * sd : 0;
+  L->launches = L->base_launches + per * (int)L->gathers.size() - (fused ? per * sd : 0) +
+                (overlap ? per * (L->nchunks - 1) * (sd + 1) : 0);
+}
 
 // Work list of the fused kernel: each desc's valueBox cut into tiles of the
 // given shape (the last tile of a row may be shorter).
@@ -1384,6 +1406,9 @@ static mf_status enqueue_level_step(mf_level* L, int advance, cudaEvent_t* ev = 
   const int np0 = mf::prim_launches(lean, mixed);
   // the fused flux + update kernel, unless flux registers need the face fluxes
   const bool fused = L->fused && L->gathers.empty();
+  // chunked flux / update overlap of the split mixed-precision stages (not
+  // while profiling launch by launch: the events would straddle two streams)
+  const bool overlap = L->nchunks > 1 && !L->fused && L->gathers.empty() && !c->dp.ct && !ev;
   auto stage_marks = [&](int n0) {
     if (!ev) return;
     kinds[n0] = 1;
@@ -1443,6 +1468,7 @@ static mf_status enqueue_level_step(mf_level* L, int advance, cudaEvent_t* ev = 
     B.uout = (double*)L->U1.p;
     B.ev = ev ? ev + ne : nullptr;
     B.fused = fused ? &L->fp1 : nullptr;
+    B.overlap = overlap ? &L->op1 : nullptr;
     MF_CHECK_CUDA(mf::launch_stage(c->dp, p.precision, B, L->b1, 0, 1.0, ds, parts, &nb, s));
     stage_marks(ne);
     if (ct && (gst = ct_stage(L->b1, B.w, e1, nullptr, nullptr, (double*)L->U1.p, nullptr,
@@ -1459,6 +1485,7 @@ static mf_status enqueue_level_step(mf_level* L, int advance, cudaEvent_t* ev = 
     B.uold = (const double*)L->U.p;
     B.ev = ev ? ev + ne : nullptr;
     B.fused = fused ? &L->fp2 : nullptr;
+    B.overlap = overlap ? &L->op2 : nullptr;
     MF_CHECK_CUDA(mf::launch_stage(c->dp, p.precision, B, L->b2,
                                    ct ? 0 : (mf::kStageAverage | mf::kStageDt), 0.5, ds, parts,
                                    &nb, s));
@@ -1498,6 +1525,7 @@ static mf_status enqueue_level_step(mf_level* L, int advance, cudaEvent_t* ev = 
     B.uout = (double*)L->U.p;
     B.ev = ev ? ev + ne : nullptr;
     B.fused = fused ? &L->fp2 : nullptr;
+    B.overlap = overlap ? &L->op2 : nullptr;
     MF_CHECK_CUDA(mf::launch_stage(c->dp, p.precision, B, L->b2, ct ? 0 : mf::kStageDt, 1.0, ds,
                                    parts, &nb, s));
     stage_marks(ne);
@@ -1599,6 +1627,9 @@ mf_status mf_level_create(mf_ctx* c, int npatch, const mf_box* valid, mf_level**
     delete L;
     return MF_ERR_UNSUPPORTED;  // more than 2^31 cells or faces in one launch
   }
+  // the host copies with their flat offsets (the overlap's chunk plans read them)
+  L->hd1.assign(hd.begin(), hd.begin() + npatch);
+  L->hd2.assign(hd.begin() + npatch, hd.begin() + 2 * npatch);
   mf::batch_default_threads(L->b1);
   mf::batch_default_threads(L->b2);
   mf::batch_default_threads(L->bp);
@@ -1738,6 +1769,9 @@ void mf_level_destroy(mf_level* L) {
   if (L->gsync) cudaGraphExecDestroy(L->gsync);
   if (L->gasync) cudaGraphExecDestroy(L->gasync);
   if (L->s) cudaStreamDestroy(L->s);
+  if (L->s2) cudaStreamDestroy(L->s2);
+  for (cudaEvent_t& e : L->ov_ev)
+    if (e) cudaEventDestroy(e);
   L->U.release();
   L->U1.release();
   L->W.release();
@@ -2004,12 +2038,8 @@ int mf_level_launches_per_step(const mf_level* L) { return L ? L->launches : -1;
 // Make the level step with the fused kernel (its work lists already built)
 // or the split kernels; the captured graphs are rebuilt on next use.
 static void apply_schedule(mf_level* L, bool fused) {
-  const mf_params& p = L->ctx->p;
-  const int per = (p.time_approximation == MF_TA_RK2) ? 2 : 1;
   L->fused = fused;
-  L->fused_saving = fused ? per * p.space_dim : 0;
-  L->launches = L->base_launches + per * (int)L->gathers.size() -
-                (L->gathers.empty() ? L->fused_saving : 0);
+  count_launches(L);
   if (L->gsync) cudaGraphExecDestroy(L->gsync);
   if (L->gasync) cudaGraphExecDestroy(L->gasync);
   L->gsync = L->gasync = nullptr;
@@ -2033,6 +2063,57 @@ mf_status mf_level_set_schedule(mf_level* L, const int tile[3]) {
     fused = true;
   }
   apply_schedule(L, fused);
+  return MF_OK;
+}
+
+// Cut the split flux and update launches of each stage into chunks of
+// consecutive patches whose fluxes and updates overlap (MF_PREC_MIXED and
+// MF_PREC_MIXED_CE32, RK2 or first order, no constrained transport); 1 = one
+// launch each.  The plans and the flux stream are built here, outside any
+// capture.
+static mf_status level_set_chunks(mf_level* L, int chunks) {
+  const mf_params& p = L->ctx->p;
+  if (chunks < 1 || chunks > MF_MAX_OVERLAP_CHUNKS) return MF_ERR_BAD_ARG;
+  if (chunks > 1 && (p.precision != MF_PREC_MIXED ||
+                     (p.time_approximation != MF_TA_RK2 &&
+                      p.time_approximation != MF_TA_FIRST_ORDER) ||
+                     L->ctx->dp.ct))
+    return MF_ERR_UNSUPPORTED;
+  mf_status st = wait_stream(L->s, L->ctx->timeout);  // the old plans may be in use
+  if (st != MF_OK) return st;
+  int n = 1;
+  if (chunks > 1) {
+    if (!L->s2) MF_CHECK_CUDA(cudaStreamCreateWithFlags(&L->s2, cudaStreamNonBlocking));
+    for (int q = 0; q <= chunks; ++q)
+      if (!L->ov_ev[q])
+        MF_CHECK_CUDA(cudaEventCreateWithFlags(&L->ov_ev[q], cudaEventDisableTiming));
+    L->ch1 = mf::make_chunks(L->hd1.data(), (int)L->hd1.size(), L->b1, chunks);
+    L->ch2 = mf::make_chunks(L->hd2.data(), (int)L->hd2.size(), L->b2, chunks);
+    n = (int)std::min(L->ch1.size(), L->ch2.size());
+    if (L->ch1.size() != L->ch2.size()) {  // keep the two stages alike
+      L->ch1 = mf::make_chunks(L->hd1.data(), (int)L->hd1.size(), L->b1, n);
+      L->ch2 = mf::make_chunks(L->hd2.data(), (int)L->hd2.size(), L->b2, n);
+      n = (int)std::min(L->ch1.size(), L->ch2.size());
+    }
+  }
+  L->nchunks = std::max(1, n);
+  L->op1 = {L->ch1.data(), (int)L->ch1.size(), L->s2, L->ov_ev};
+  L->op2 = {L->ch2.data(), (int)L->ch2.size(), L->s2, L->ov_ev};
+  count_launches(L);
+  if (L->gsync) cudaGraphExecDestroy(L->gsync);
+  if (L->gasync) cudaGraphExecDestroy(L->gasync);
+  L->gsync = L->gasync = nullptr;
+  return MF_OK;
+}
+
+mf_status mf_level_set_overlap(mf_level* L, int chunks) {
+  if (!L) return MF_ERR_BAD_ARG;
+  return level_set_chunks(L, chunks);
+}
+
+mf_status mf_level_overlap(const mf_level* L, int* chunks) {
+  if (!L || !chunks) return MF_ERR_BAD_ARG;
+  *chunks = L->nchunks;
   return MF_OK;
 }
 
@@ -2082,7 +2163,8 @@ mf_status mf_level_profile_step(mf_level* L, double dt, float* ms, int* kinds, i
 
 // Time `reps` launches of one kernel kind of stage 1 (0 prim, 1 fluxes of
 // every direction, 2 update without averaging, 3 the fused flux + update
-// kernel on the work list in fp1) with the level's current threads.
+// kernel on the work list in fp1, 4 the fluxes and update in the level's
+// overlap chunks) with the level's current threads.
 // Stage 1 reads U and writes only W, F, Bn and U1, so the level's state is
 // left as it was; the step state used is a private copy with dt = 0.
 static mf_status time_kind(mf_level* L, int kind, int reps, cudaEvent_t e0, cudaEvent_t e1,
@@ -2117,6 +2199,11 @@ static mf_status time_kind(mf_level* L, int kind, int reps, cudaEvent_t e0, cuda
         else
           e = mf::launch_flux_exact(c->dp, d, B.w, B.f[d], B.bn[d], b, ds, L->s);
       }
+    } else if (kind == 4) {  // fluxes + update of stage 1 in the level's chunks, overlapped
+      StageBuffers Bo = B;
+      Bo.overlap = (p.time_approximation == MF_TA_RK2) ? &L->op1 : &L->op2;
+      int nb = 0;
+      e = mf::launch_flux_update_overlap(c->dp, Bo, b, 0, 1.0, ds, parts, &nb, L->s);
     } else if (kind == 3) {  // the fused kernel on stage 1's work list
       e = mf::launch_fused(c->dp, B, b, L->fp1.tiles, L->fp1.ntiles, L->fp1.tile, 0, 1.0, ds,
                            parts, L->s);
@@ -2172,36 +2259,54 @@ mf_status mf_level_autotune(mf_level* L, int reps, int threads[3]) {
     }
     L->b1.nt[kind] = L->b2.nt[kind] = L->bp.nt[kind] = bnt;
   }
-  // schedule: the split flux + update kernels against the fused kernel at
-  // each tile shape that fits the options, by the time of stage 1 (a level
-  // feeding flux registers keeps the split kernels, which store the fluxes)
+  // schedule, by the time of stage 1's fluxes + update: the split kernels,
+  // unchunked or in 2, 4, 8 overlapped chunks (mixed precision), against the
+  // fused kernel at each tile shape that fits the options.  A level feeding
+  // flux registers keeps the split, unchunked kernels, which store the fluxes.
   const mf_params& p = c->p;
   const int sd = p.space_dim;
-  if (st == MF_OK && mf::fused_supported(c->dp, p.precision, p.time_approximation) &&
-      L->gathers.empty()) {
-    float split = 0.f, tf = 0.f, tu = 0.f;
-    st = time_kind(L, 1, reps, e0, e1, &tf);
+  if (st == MF_OK && L->gathers.empty()) {
+    float tf = 0.f, tu = 0.f;
+    if (p.precision == MF_PREC_MIXED) st = level_set_chunks(L, 1);
+    if (st == MF_OK) st = time_kind(L, 1, reps, e0, e1, &tf);
     if (st == MF_OK) st = time_kind(L, 2, reps, e0, e1, &tu);
-    split = tf + tu;
-    static const int c3[][3] = {{8, 8, 4}, {8, 4, 4}, {16, 8, 2}, {8, 8, 2}, {4, 4, 4}};
-    static const int c2[][3] = {{16, 16, 1}, {32, 8, 1}, {16, 8, 1}, {8, 8, 1}};
-    const int ncand = (sd == 3) ? 5 : 4;
-    float best = split;
-    int bt[3] = {0, 0, 0};
-    for (int q = 0; q < ncand && st == MF_OK; ++q) {
-      const int* t = (sd == 3) ? c3[q] : c2[q];
-      bool ok = false;
-      if (level_set_tiles(L, t, &ok) != cudaSuccess) {
-        st = MF_ERR_CUDA;
-        break;
+    float best = tf + tu;
+    int bk = 1;
+    if (p.precision == MF_PREC_MIXED && !c->dp.ct &&
+        (p.time_approximation == MF_TA_RK2 || p.time_approximation == MF_TA_FIRST_ORDER)) {
+      static const int ck[3] = {2, 4, 8};
+      for (int q = 0; q < 3 && st == MF_OK; ++q) {
+        st = level_set_chunks(L, ck[q]);
+        if (st != MF_OK || L->nchunks < 2) continue;
+        float ms = 0.f;
+        st = time_kind(L, 4, 1, e0, e1, &ms);  // warm-up
+        if (st == MF_OK) st = time_kind(L, 4, reps, e0, e1, &ms);
+        if (st == MF_OK && ms < best) {
+          best = ms;
+          bk = L->nchunks;
+        }
       }
-      if (!ok) continue;
-      float ms = 0.f;
-      st = time_kind(L, 3, 1, e0, e1, &ms);  // warm-up
-      if (st == MF_OK) st = time_kind(L, 3, reps, e0, e1, &ms);
-      if (st == MF_OK && ms < best) {
-        best = ms;
-        for (int d = 0; d < 3; ++d) bt[d] = t[d];
+    }
+    int bt[3] = {0, 0, 0};
+    if (st == MF_OK && mf::fused_supported(c->dp, p.precision, p.time_approximation)) {
+      static const int c3[][3] = {{8, 8, 4}, {8, 4, 4}, {16, 8, 2}, {8, 8, 2}, {4, 4, 4}};
+      static const int c2[][3] = {{16, 16, 1}, {32, 8, 1}, {16, 8, 1}, {8, 8, 1}};
+      const int ncand = (sd == 3) ? 5 : 4;
+      for (int q = 0; q < ncand && st == MF_OK; ++q) {
+        const int* t = (sd == 3) ? c3[q] : c2[q];
+        bool ok = false;
+        if (level_set_tiles(L, t, &ok) != cudaSuccess) {
+          st = MF_ERR_CUDA;
+          break;
+        }
+        if (!ok) continue;
+        float ms = 0.f;
+        st = time_kind(L, 3, 1, e0, e1, &ms);  // warm-up
+        if (st == MF_OK) st = time_kind(L, 3, reps, e0, e1, &ms);
+        if (st == MF_OK && ms < best) {
+          best = ms;
+          for (int d = 0; d < 3; ++d) bt[d] = t[d];
+        }
       }
     }
     bool fused = false;
@@ -2210,6 +2315,7 @@ mf_status mf_level_autotune(mf_level* L, int reps, int threads[3]) {
       if (level_set_tiles(L, bt, &ok) != cudaSuccess) st = MF_ERR_CUDA;
       fused = ok;
     }
+    if (p.precision == MF_PREC_MIXED && st == MF_OK) st = level_set_chunks(L, fused ? 1 : bk);
     apply_schedule(L, st == MF_OK && fused);
   }
   cudaEventDestroy(e0);
@@ -2374,10 +2480,9 @@ void level_set_gathers(mf_level* L, const std::vector<FaceGather>& g) {
   if (L->gsync) cudaGraphExecDestroy(L->gsync);
   if (L->gasync) cudaGraphExecDestroy(L->gasync);
   L->gsync = L->gasync = nullptr;
-  const int per = (L->ctx->p.time_approximation == MF_TA_RK2) ? 2 : 1;
   // the fused kernel keeps no face fluxes to gather: with gathers the level
-  // steps through the split flux and update kernels
-  L->launches = L->base_launches + per * (int)g.size() - (g.empty() ? L->fused_saving : 0);
+  // steps through the split flux and update kernels, unchunked
+  count_launches(L);
 }
 
 mf_status status_of_flags(unsigned flags) { return flags_status(flags); }

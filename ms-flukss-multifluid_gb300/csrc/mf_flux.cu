@@ -10,32 +10,35 @@ namespace mf {
 template <typename R, int WF>
 static void flux_dirs(const DevParams& P, int dir, const double* w, const float* wf, R* F,
                       R* Bn, const Batch& b, const StepState* state, unsigned gf, int nt,
-                      int tot, cudaStream_t s) {
+                      int first, int end, cudaStream_t s) {
   if (dir == 0)
-    k_flux<R, 0, WF><<<gf, nt, 0, s>>>(P, w, wf, F, Bn, b.desc, b.ndesc, tot, b.runs, state);
+    k_flux<R, 0, WF><<<gf, nt, 0, s>>>(P, w, wf, F, Bn, b.desc, b.ndesc, first, end, b.runs,
+                                       state);
   if (dir == 1)
-    k_flux<R, 1, WF><<<gf, nt, 0, s>>>(P, w, wf, F, Bn, b.desc, b.ndesc, tot, b.runs, state);
+    k_flux<R, 1, WF><<<gf, nt, 0, s>>>(P, w, wf, F, Bn, b.desc, b.ndesc, first, end, b.runs,
+                                       state);
   if (dir == 2)
-    k_flux<R, 2, WF><<<gf, nt, 0, s>>>(P, w, wf, F, Bn, b.desc, b.ndesc, tot, b.runs, state);
+    k_flux<R, 2, WF><<<gf, nt, 0, s>>>(P, w, wf, F, Bn, b.desc, b.ndesc, first, end, b.runs,
+                                       state);
 }
 
 template <typename R>
 cudaError_t launch_flux_fast(const DevParams& P, int dir, const double* w, void* f, void* bn,
                              const Batch& b, const StepState* state, cudaStream_t s,
-                             const float* wf) {
-  const int tot = b.tot_f[dir];
-  if (tot <= 0) return cudaSuccess;
+                             const float* wf, int first, int end) {
+  if (end < 0) end = b.tot_f[dir];
+  if (end - first <= 0) return cudaSuccess;
   const int nt = b.nt[1];
-  const unsigned gf = flat_blocks(tot, nt);
+  const unsigned gf = flat_blocks(end - first, nt);
   R* F = (R*)f;
   R* Bn = (R*)bn;
   if constexpr (sizeof(R) == 4) {
     if (wf) {
-      flux_dirs<R, 1>(P, dir, w, wf, F, Bn, b, state, gf, nt, tot, s);
+      flux_dirs<R, 1>(P, dir, w, wf, F, Bn, b, state, gf, nt, first, end, s);
       return cudaGetLastError();
     }
   }
-  flux_dirs<R, 0>(P, dir, w, nullptr, F, Bn, b, state, gf, nt, tot, s);
+  flux_dirs<R, 0>(P, dir, w, nullptr, F, Bn, b, state, gf, nt, first, end, s);
   return cudaGetLastError();
 }
 
@@ -68,9 +71,9 @@ template cudaError_t launch_face_flux_fast<float>(const DevParams&, int, const d
 
 template cudaError_t launch_flux_fast<double>(const DevParams&, int, const double*, void*, void*,
                                               const Batch&, const StepState*, cudaStream_t,
-                                              const float*);
+                                              const float*, int, int);
 template cudaError_t launch_flux_fast<float>(const DevParams&, int, const double*, void*, void*,
                                              const Batch&, const StepState*, cudaStream_t,
-                                             const float*);
+                                             const float*, int, int);
 
 }  // namespace mf

@@ -15,13 +15,13 @@ cudaError_t launch_flux_exact(const DevParams& P, int dir, const double* w, void
   double* F = (double*)f;
   double* Bn = (double*)bn;
   if (dir == 0)
-    k_flux<double, 0, 0><<<gf, nt, 0, s>>>(P, w, nullptr, F, Bn, b.desc, b.ndesc, tot, b.runs,
+    k_flux<double, 0, 0><<<gf, nt, 0, s>>>(P, w, nullptr, F, Bn, b.desc, b.ndesc, 0, tot, b.runs,
                                             state);
   if (dir == 1)
-    k_flux<double, 1, 0><<<gf, nt, 0, s>>>(P, w, nullptr, F, Bn, b.desc, b.ndesc, tot, b.runs,
+    k_flux<double, 1, 0><<<gf, nt, 0, s>>>(P, w, nullptr, F, Bn, b.desc, b.ndesc, 0, tot, b.runs,
                                             state);
   if (dir == 2)
-    k_flux<double, 2, 0><<<gf, nt, 0, s>>>(P, w, nullptr, F, Bn, b.desc, b.ndesc, tot, b.runs,
+    k_flux<double, 2, 0><<<gf, nt, 0, s>>>(P, w, nullptr, F, Bn, b.desc, b.ndesc, 0, tot, b.runs,
                                             state);
   return cudaGetLastError();
 }

@@ -316,8 +316,11 @@ template <typename R, int DIR, int WF>
 __global__ void __launch_bounds__(kMaxBlock, WF ? 2 : 1)
     k_flux(const __grid_constant__ DevParams P, const double* __restrict__ W, const float* __restrict__ Wf,
            R* __restrict__ F, R* __restrict__ Bn, const StageDesc* __restrict__ descs, int ndesc,
-           int total, const RunParams* __restrict__ runs, const StepState* __restrict__ states) {
-  const int gi = blockIdx.x * blockDim.x + threadIdx.x;
+           int first, int total, const RunParams* __restrict__ runs,
+           const StepState* __restrict__ states) {
+  // faces [first, total) of the batch's flat face index (first > 0: a chunk
+  // of the batch's patches)
+  const int gi = first + blockIdx.x * blockDim.x + threadIdx.x;
   if (gi >= total) return;
   const StageDesc& D = descs[find_desc(descs, ndesc, kRegF + DIR, gi)];
   const int lin = gi - D.g0[kRegF + DIR];

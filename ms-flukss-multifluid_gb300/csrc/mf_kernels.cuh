@@ -15,6 +15,7 @@
 #include <cfloat>
 #include <climits>
 #include <cstring>
+#include <vector>
 
 #include "mf_device.cuh"
 
@@ -187,6 +188,8 @@ struct FusedPlan {
   int tile[3];             // tile shape (cells)
 };
 
+struct OverlapPlan;
+
 struct StageBuffers {
   const double* uin;   // state the stage starts from
   double* uout;        // state the stage writes (valueBox cells only)
@@ -206,9 +209,35 @@ struct StageBuffers {
   cudaEvent_t* ev;     // optional: an event recorded after each launch (profiling)
   const LeanPrim* lean;  // optional: primitive state on valid cells + ghost copies
   const FusedPlan* fused;  // optional (mixed precision): fluxes + update in one kernel
+  const OverlapPlan* overlap;  // optional (mixed precision): chunked, overlapped flux + update
 };
 
 enum StageFlags : int { kStageAverage = 1, kStageDt = 2 };
+
+// The flux and update launches of a mixed-precision stage cut into chunks of
+// consecutive patches: the FP32 flux kernels of chunk c + 1 run on a second
+// stream while the FP64-bound update of chunk c runs on the stage's stream,
+// so the two kernels share the SMs (no kernel waits on another; the streams
+// are ordered by events).  A chunk's cells start on a multiple of 256.
+struct Chunk {
+  int v0, v1;        // cells [v0, v1) of the batch's flat cell index
+  int f0[3], f1[3];  // faces [f0, f1) per direction
+};
+struct OverlapPlan {
+  const Chunk* c;    // host array
+  int n;             // chunks (>= 2)
+  cudaStream_t s2;   // the flux stream
+  cudaEvent_t* ev;   // n + 1 events: ev[0] the primitive part, ev[1 + c] chunk c's fluxes
+};
+// Chunks of a batch (host descs hd, n of them): about equal cell counts,
+// each starting at a patch whose first cell is a multiple of 256; fewer than
+// nchunks where the patches do not allow more.
+std::vector<Chunk> make_chunks(const StageDesc* hd, int n, const Batch& b, int nchunks);
+// the flux and update launches of a mixed-precision stage in B.overlap's chunks
+cudaError_t launch_flux_update_overlap(const DevParams& P, const StageBuffers& B,
+                                       const Batch& b, int flags, double dt_scale,
+                                       StepState* state, DtPartial* partials, int* nblocks_v,
+                                       cudaStream_t s);
 
 // wf (nullable): also the FP32 copy of w (round to nearest, as the FP32 flux
 // kernels would convert each value)
@@ -223,14 +252,17 @@ cudaError_t launch_update_exact(const DevParams& P, const StageBuffers& B, const
                                 DtPartial* partials, int* nblocks_v, cudaStream_t s);
 // fast physics: R = float (mixed precision) or double (fast FP64)
 // wf (R = float only, nullable): the FP32 copy of w the prim kernel wrote
+// [first, end): a range of the batch's flat face / cell index (end < 0: to
+// the batch's total); an update range starts on a multiple of the block size
 template <typename R>
 cudaError_t launch_flux_fast(const DevParams& P, int dir, const double* w, void* f, void* bn,
                              const Batch& b, const StepState* state, cudaStream_t s,
-                             const float* wf = nullptr);
+                             const float* wf = nullptr, int first = 0, int end = -1);
 template <typename R>
 cudaError_t launch_update_fast(const DevParams& P, const StageBuffers& B, const Batch& b,
                                int flags, double dt_scale, StepState* state,
-                               DtPartial* partials, int* nblocks_v, cudaStream_t s);
+                               DtPartial* partials, int* nblocks_v, cudaStream_t s,
+                               int first = 0, int end = -1);
 
 // Riemann fluxes of n given face-state pairs (primitive, nc values each) in
 // the exact or the fast physics (R = float: mixed precision).

@@ -37,6 +37,8 @@ cudaError_t launch_stage(const DevParams& P, int precision, const StageBuffers& 
     if (e != cudaSuccess) return e;
     if (B.ev) cudaEventRecord(B.ev[ne++], s);
   }
+  if (B.overlap && precision == MF_PREC_MIXED && !B.ev)
+    return launch_flux_update_overlap(P, B, b, flags, dt_scale, state, partials, nblocks_v, s);
   if (B.fused && precision == MF_PREC_MIXED) {
     e = launch_fused(P, B, b, B.fused->tiles, B.fused->ntiles, B.fused->tile, flags, dt_scale,
                      state, partials, s);
@@ -64,6 +66,62 @@ cudaError_t launch_stage(const DevParams& P, int precision, const StageBuffers& 
   if (e != cudaSuccess) return e;
   if (B.ev) cudaEventRecord(B.ev[ne++], s);
   return cudaSuccess;
+}
+
+cudaError_t launch_flux_update_overlap(const DevParams& P, const StageBuffers& B,
+                                       const Batch& b, int flags, double dt_scale,
+                                       StepState* state, DtPartial* partials, int* nblocks_v,
+                                       cudaStream_t s) {
+  // fluxes of chunk c + 1 on the second stream while chunk c updates: the
+  // second stream starts after the work already on s (the primitive part),
+  // each update waits for its chunk's fluxes, and the last wait joins the
+  // streams again
+  const OverlapPlan& O = *B.overlap;
+  cudaError_t e = cudaEventRecord(O.ev[0], s);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(O.s2, O.ev[0], 0);
+  for (int c = 0; c < O.n && e == cudaSuccess; ++c) {
+    const Chunk& C = O.c[c];
+    for (int d = 0; d < P.sd && e == cudaSuccess; ++d)
+      e = launch_flux_fast<float>(P, d, B.w, B.f[d], B.bn[d], b, state, O.s2, B.wf, C.f0[d],
+                                  C.f1[d]);
+    if (e == cudaSuccess) e = cudaEventRecord(O.ev[1 + c], O.s2);
+  }
+  for (int c = 0; c < O.n && e == cudaSuccess; ++c) {
+    const Chunk& C = O.c[c];
+    e = cudaStreamWaitEvent(s, O.ev[1 + c], 0);
+    if (e == cudaSuccess)
+      e = launch_update_fast<float>(P, B, b, flags, dt_scale, state, partials, nblocks_v, s,
+                                    C.v0, C.v1);
+  }
+  return e;
+}
+
+std::vector<Chunk> make_chunks(const StageDesc* hd, int n, const Batch& b, int nchunks) {
+  std::vector<Chunk> out;
+  if (n <= 0 || nchunks < 1) return out;
+  const long long tot = b.tot_v;
+  int d0 = 0;
+  for (int c = 0; c < nchunks && d0 < n; ++c) {
+    int d1 = n;
+    if (c < nchunks - 1) {
+      const long long target = tot * (c + 1) / nchunks;
+      for (int d = d0 + 1; d < n; ++d)
+        if (hd[d].g0[kRegV] >= target && hd[d].g0[kRegV] % 256 == 0) {
+          d1 = d;
+          break;
+        }
+    }
+    Chunk C;
+    C.v0 = hd[d0].g0[kRegV];
+    C.v1 = (d1 < n) ? hd[d1].g0[kRegV] : b.tot_v;
+    for (int d = 0; d < 3; ++d) {
+      C.f0[d] = hd[d0].g0[kRegF + d];
+      C.f1[d] = (d1 < n) ? hd[d1].g0[kRegF + d] : b.tot_f[d];
+    }
+    out.push_back(C);
+    d0 = d1;
+  }
+  return out;
 }
 
 }  // namespace mf

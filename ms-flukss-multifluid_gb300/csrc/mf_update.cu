@@ -9,13 +9,17 @@ namespace mf {
 template <typename R>
 cudaError_t launch_update_fast(const DevParams& P, const StageBuffers& B, const Batch& b,
                                int flags, double dt_scale, StepState* state,
-                               DtPartial* partials, int* nblocks_v, cudaStream_t s) {
+                               DtPartial* partials, int* nblocks_v, cudaStream_t s, int first,
+                               int end) {
   const int nt = b.nt[2];
-  const unsigned gv = flat_blocks(b.tot_v, nt);
-  if (nblocks_v) *nblocks_v = (int)gv;
+  if (end < 0) end = b.tot_v;
+  if (nblocks_v) *nblocks_v = (int)flat_blocks(b.tot_v, nt);
+  if (first % nt != 0) return cudaErrorInvalidValue;
+  if (end - first <= 0) return cudaSuccess;
+  const unsigned gv = flat_blocks(end - first, nt);
   // charge-exchange rates: FP64, or FP32 in the opt-in MF_PREC_MIXED_CE32 form
 #define MF_UPD(G, FL, CE)                                                                    \
-  k_update<R, G, FL, CE><<<gv, nt, 0, s>>>(P, B, b.desc, b.ndesc, b.tot_v, b.runs, state, \
+  k_update<R, G, FL, CE><<<gv, nt, 0, s>>>(P, B, b.desc, b.ndesc, first, end, b.runs, state, \
                                            dt_scale, partials)
 #define MF_UPD_CE(G, FL)                      \
   do {                                        \
@@ -43,9 +47,9 @@ cudaError_t launch_update_fast(const DevParams& P, const StageBuffers& B, const 
 
 template cudaError_t launch_update_fast<double>(const DevParams&, const StageBuffers&,
                                                 const Batch&, int, double, StepState*,
-                                                DtPartial*, int*, cudaStream_t);
+                                                DtPartial*, int*, cudaStream_t, int, int);
 template cudaError_t launch_update_fast<float>(const DevParams&, const StageBuffers&,
                                                const Batch&, int, double, StepState*,
-                                               DtPartial*, int*, cudaStream_t);
+                                               DtPartial*, int*, cudaStream_t, int, int);
 
 }  // namespace mf

@@ -183,7 +183,7 @@ cudaError_t launch_update_exact(const DevParams& P, const StageBuffers& B, const
   const unsigned gv = flat_blocks(b.tot_v, nt);
   if (nblocks_v) *nblocks_v = (int)gv;
 #define MF_UPD(G, FL)                                                                         \
-  k_update<double, G, FL><<<gv, nt, 0, s>>>(P, B, b.desc, b.ndesc, b.tot_v, b.runs, state, \
+  k_update<double, G, FL><<<gv, nt, 0, s>>>(P, B, b.desc, b.ndesc, 0, b.tot_v, b.runs, state, \
                                             dt_scale, partials)
   if (P.glm) {
     if (flags == 0) MF_UPD(1, 0);

@@ -59,13 +59,13 @@ __device__ __forceinline__ bool dt_less(double a, int ia, double b, int ib) {
   return (a < b) || (a == b && ia < ib);
 }
 
-// Block minimum of (dt, flattened index) into partials[blockIdx.x]: warp
+// Block minimum of (dt, flattened index) into partials[pbase + blockIdx.x]: warp
 // shuffles, then one thread over the warps.  The flattened index orders cells
 // by (patch, Fortran-order index), so the minimum is the reference's
 // lexicographic one; it is turned back into (patch, index) once per block.
 __device__ __forceinline__ void block_dt_min(double dtc, int myidx,
                                              const StageDesc* __restrict__ descs, int ndesc,
-                                             DtPartial* __restrict__ partials) {
+                                             DtPartial* __restrict__ partials, int pbase = 0) {
 #pragma unroll
   for (int off = 16; off > 0; off >>= 1) {
     double od = __shfl_down_sync(0xffffffffu, dtc, off);
@@ -101,7 +101,7 @@ __device__ __forceinline__ void block_dt_min(double dtc, int myidx,
       pr.desc = di;
       pr.idx = bi - descs[di].g0[kRegV];
     }
-    partials[blockIdx.x] = pr;
+    partials[pbase + blockIdx.x] = pr;
   }
 }
 
@@ -231,10 +231,13 @@ __device__ __forceinline__ void update_tail(const DevParams& P, const StageBuffe
 template <typename R, int GLM, int FLAGS, typename CE = double>
 __global__ void __launch_bounds__(kMaxBlock, sizeof(R) == 4 ? 2 : 1)
     k_update(const __grid_constant__ DevParams P, const __grid_constant__ StageBuffers B, const StageDesc* __restrict__ descs,
-             int ndesc, int total, const RunParams* __restrict__ runs,
+             int ndesc, int first, int total, const RunParams* __restrict__ runs,
              StepState* __restrict__ states, const double dt_scale,
              DtPartial* __restrict__ partials) {
-  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  // cells [first, total) of the batch's flat cell index; first is a multiple
+  // of the block size, so block b writes the dt partial first/blockDim + b of
+  // the launch over the whole batch
+  const int g = first + blockIdx.x * blockDim.x + threadIdx.x;
   double dtc = DBL_MAX;
   int myidx = INT_MAX;
   const StageDesc* Dp = nullptr;
@@ -326,7 +329,7 @@ __global__ void __launch_bounds__(kMaxBlock, sizeof(R) == 4 ? 2 : 1)
     update_tail<R, GLM, FLAGS, CE>(P, B, D, RP, ss, i, j, k, base, cs, dt, psi_damp, divB, u, g,
                                    dtc, myidx);
   }
-  if (FLAGS & kStageDt) block_dt_min(dtc, myidx, descs, ndesc, partials);
+  if (FLAGS & kStageDt) block_dt_min(dtc, myidx, descs, ndesc, partials, first / blockDim.x);
 }
 
 }  // namespace

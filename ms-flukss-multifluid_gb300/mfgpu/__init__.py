@@ -199,6 +199,8 @@ _SIGS = {
     "mf_level_launches_per_step": (ctypes.c_int, [ctypes.c_void_p]),
     "mf_level_set_schedule": (ctypes.c_int, [ctypes.c_void_p, c_int3]),
     "mf_level_schedule": (ctypes.c_int, [ctypes.c_void_p, c_int3]),
+    "mf_level_set_overlap": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "mf_level_overlap": (ctypes.c_int, [ctypes.c_void_p, _P(ctypes.c_int)]),
     "mf_level_profile_step": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double,
                                              _P(ctypes.c_float), _P(ctypes.c_int),
                                              _P(ctypes.c_int), ctypes.c_int]),
@@ -742,6 +744,17 @@ class Level:
         check(self.lib.mf_level_schedule(self.h, t), "mf_level_schedule")
         return tuple(t)
 
+    def set_overlap(self, chunks=1):
+        """mf_level_set_overlap: 1 = one flux launch per direction and one
+        update launch per stage; 2..8 = that many chunks of patches whose FP32
+        fluxes and update overlap on two streams (mixed precision)."""
+        check(self.lib.mf_level_set_overlap(self.h, chunks), "mf_level_set_overlap")
+
+    def overlap(self):
+        n = ctypes.c_int()
+        check(self.lib.mf_level_overlap(self.h, ctypes.byref(n)), "mf_level_overlap")
+        return n.value
+
     KIND_NAMES = {0: "exchange", 1: "prim", 2: "flux", 3: "update", 4: "finalize", 5: "coupling",
                   6: "postprocess", 7: "constrained transport", 8: "fused"}
 
@@ -759,8 +772,9 @@ class Level:
     def autotune(self, reps=3):
         """mf_level_autotune: threads per block of the prim, flux and update
         kernels, and the schedule (split kernels or a fused tile shape, read
-        by schedule()), picked by timing; returns the chosen (prim, flux,
-        update) threads."""
+        by schedule(); for split mixed precision the overlap chunks, read by
+        overlap()), picked by timing; returns the chosen (prim, flux, update)
+        threads."""
         t = c_int3()
         check(self.lib.mf_level_autotune(self.h, reps, t), "mf_level_autotune")
         return tuple(t)

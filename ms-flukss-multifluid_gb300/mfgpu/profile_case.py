@@ -5,8 +5,9 @@ committed ncu summaries capture.
     python -m mfgpu.profile_case --n 64 --patch 16 --precision mixed --schedule 0,0,0 --steps 2
 
 --schedule: "auto" runs the autotuner; "0,0,0" the split kernels; x,y,z a
-fused tile shape.  Prints the status, the schedule and the step times (CUDA
-events), and exits non-zero when a step reports an error."""
+fused tile shape.  --overlap K: the split kernels in K overlapped chunks.
+Prints the status, the schedule and the step times (CUDA events), and exits
+non-zero when a step reports an error."""
 import argparse
 import sys
 
@@ -24,6 +25,8 @@ def main(argv=None):
     ap.add_argument("--patch", type=int, default=16)
     ap.add_argument("--precision", choices=sorted(PRECISIONS), default="mixed")
     ap.add_argument("--schedule", default="0,0,0")
+    ap.add_argument("--overlap", type=int, default=1,
+                    help="chunks of overlapped fluxes and update (mixed precision, split)")
     ap.add_argument("--steps", type=int, default=2)
     a = ap.parse_args(argv)
     import torch
@@ -41,6 +44,8 @@ def main(argv=None):
         lev.autotune(3)
     else:
         lev.set_schedule(tuple(int(v) for v in a.schedule.split(",")))
+        if a.overlap > 1:
+            lev.set_overlap(a.overlap)
     stream = torch.cuda.Stream()
     dt0 = lev.compute_dt()[0]
     lev.seed_dt(0.4 * dt0, 0.4, stream.cuda_stream)
@@ -54,7 +59,7 @@ def main(argv=None):
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / max(1, a.steps)
     print(f"status {st} cells {lev.ncells} patches {len(boxes)} precision {a.precision} "
-          f"schedule {lev.schedule()} launches/step {lev.launches_per_step()} ms/step {ms:.3f}")
+          f"schedule {lev.schedule()} overlap {lev.overlap()} launches/step {lev.launches_per_step()} ms/step {ms:.3f}")
     lev.close()
     ctx.close()
     return 0 if st == 0 else 1
