@@ -388,6 +388,19 @@ int mf_level_launches_per_step(const mf_level* lev);
 mf_status mf_level_set_schedule(mf_level* lev, const int tile[3]);
 mf_status mf_level_schedule(const mf_level* lev, int tile[3]);
 
+/* Face-flux form of the FP64 paths (MF_PREC_FP64 and MF_PREC_FP64_FAST; no
+   reference counterpart; results unchanged, bit for bit).  MF_FLUX_FACES: one
+   thread per face, which evaluates the limited face values of both cells
+   beside it.  MF_FLUX_LINES: a block takes whole lines of faces along the
+   direction and computes each cell's limited face values once, in shared
+   memory, before the Riemann fluxes.  RK2 and first order (Hancock keeps
+   its own face-value arrays); MF_ERR_UNSUPPORTED for mixed precision, for
+   Hancock, and for a patch longer than 254 cells along a direction.  Levels
+   start with MF_FLUX_FACES; mf_level_autotune picks the form by timing. */
+enum { MF_FLUX_FACES = 0, MF_FLUX_LINES = 1 };
+mf_status mf_level_set_flux_form(mf_level* lev, int form);
+mf_status mf_level_flux_form(const mf_level* lev, int* form);
+
 /* Overlap of the split flux and update kernels (no reference counterpart;
    results unchanged, bit for bit).  chunks = 1: one flux launch per direction
    and one update launch per stage.  chunks = 2..MF_MAX_OVERLAP_CHUNKS: the

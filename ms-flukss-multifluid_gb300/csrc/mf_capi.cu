@@ -391,6 +391,11 @@ struct mf_level {
   mf::OverlapPlan op1{}, op2{};
   cudaStream_t s2 = nullptr;
   cudaEvent_t ov_ev[MF_MAX_OVERLAP_CHUNKS + 1] = {};
+  // face fluxes by lines (FP64 paths, mf_level_set_flux_form): the work lists
+  // of both stage batches, built on first use
+  int flux_form = MF_FLUX_FACES;
+  DevBuf lines;
+  mf::LinePlan lp1{}, lp2{};
 };
 
 // Kernel launches of one step: the plain count, plus the flux-register
@@ -1409,6 +1414,7 @@ static mf_status enqueue_level_step(mf_level* L, int advance, cudaEvent_t* ev = 
   // chunked flux / update overlap of the split mixed-precision stages (not
   // while profiling launch by launch: the events would straddle two streams)
   const bool overlap = L->nchunks > 1 && !L->fused && L->gathers.empty() && !c->dp.ct && !ev;
+  const bool lines = L->flux_form == MF_FLUX_LINES;
   auto stage_marks = [&](int n0) {
     if (!ev) return;
     kinds[n0] = 1;
@@ -1469,6 +1475,7 @@ static mf_status enqueue_level_step(mf_level* L, int advance, cudaEvent_t* ev = 
     B.ev = ev ? ev + ne : nullptr;
     B.fused = fused ? &L->fp1 : nullptr;
     B.overlap = overlap ? &L->op1 : nullptr;
+    B.lines = lines ? &L->lp1 : nullptr;
     MF_CHECK_CUDA(mf::launch_stage(c->dp, p.precision, B, L->b1, 0, 1.0, ds, parts, &nb, s));
     stage_marks(ne);
     if (ct && (gst = ct_stage(L->b1, B.w, e1, nullptr, nullptr, (double*)L->U1.p, nullptr,
@@ -1486,6 +1493,7 @@ static mf_status enqueue_level_step(mf_level* L, int advance, cudaEvent_t* ev = 
     B.ev = ev ? ev + ne : nullptr;
     B.fused = fused ? &L->fp2 : nullptr;
     B.overlap = overlap ? &L->op2 : nullptr;
+    B.lines = lines ? &L->lp2 : nullptr;
     MF_CHECK_CUDA(mf::launch_stage(c->dp, p.precision, B, L->b2,
                                    ct ? 0 : (mf::kStageAverage | mf::kStageDt), 0.5, ds, parts,
                                    &nb, s));
@@ -1526,6 +1534,7 @@ static mf_status enqueue_level_step(mf_level* L, int advance, cudaEvent_t* ev = 
     B.ev = ev ? ev + ne : nullptr;
     B.fused = fused ? &L->fp2 : nullptr;
     B.overlap = overlap ? &L->op2 : nullptr;
+    B.lines = lines ? &L->lp2 : nullptr;
     MF_CHECK_CUDA(mf::launch_stage(c->dp, p.precision, B, L->b2, ct ? 0 : mf::kStageDt, 1.0, ds,
                                    parts, &nb, s));
     stage_marks(ne);
@@ -1772,6 +1781,7 @@ void mf_level_destroy(mf_level* L) {
   if (L->s2) cudaStreamDestroy(L->s2);
   for (cudaEvent_t& e : L->ov_ev)
     if (e) cudaEventDestroy(e);
+  L->lines.release();
   L->U.release();
   L->U1.release();
   L->W.release();
@@ -2106,6 +2116,65 @@ static mf_status level_set_chunks(mf_level* L, int chunks) {
   return MF_OK;
 }
 
+// Face fluxes of the FP64 paths per face (k_flux) or by lines (k_lflux);
+// the line work lists of both stage batches are built on first use.
+static mf_status level_set_flux_form(mf_level* L, int form) {
+  const mf_params& p = L->ctx->p;
+  if (form != MF_FLUX_FACES && form != MF_FLUX_LINES) return MF_ERR_BAD_ARG;
+  if (form == MF_FLUX_LINES &&
+      (p.precision == MF_PREC_MIXED || p.time_approximation == MF_TA_HANCOCK))
+    return MF_ERR_UNSUPPORTED;
+  mf_status st = wait_stream(L->s, L->ctx->timeout);  // the old lists may be in use
+  if (st != MF_OK) return st;
+  if (form == MF_FLUX_LINES && L->lp1.w[0] == nullptr) {
+    const int sd = p.space_dim;
+    std::vector<mf::LineWork> w1[3], w2[3];
+    int m1[3], m2[3];
+    if (!mf::make_lines(L->hd1.data(), (int)L->hd1.size(), sd, w1, m1) ||
+        !mf::make_lines(L->hd2.data(), (int)L->hd2.size(), sd, w2, m2))
+      return MF_ERR_UNSUPPORTED;  // a patch too long along a direction
+    std::vector<mf::LineWork> all;
+    size_t o1[3], o2[3];
+    for (int d = 0; d < 3; ++d) {
+      o1[d] = all.size();
+      all.insert(all.end(), w1[d].begin(), w1[d].end());
+    }
+    for (int d = 0; d < 3; ++d) {
+      o2[d] = all.size();
+      all.insert(all.end(), w2[d].begin(), w2[d].end());
+    }
+    MF_CHECK_CUDA(mf::lines_prepare());
+    MF_CHECK_CUDA(L->lines.ensure(sizeof(mf::LineWork) * std::max<size_t>(1, all.size())));
+    MF_CHECK_CUDA(cudaMemcpy(L->lines.p, all.data(), sizeof(mf::LineWork) * all.size(),
+                             cudaMemcpyHostToDevice));
+    const mf::LineWork* base = (const mf::LineWork*)L->lines.p;
+    for (int d = 0; d < 3; ++d) {
+      L->lp1.w[d] = base + o1[d];
+      L->lp1.n[d] = (int)w1[d].size();
+      L->lp1.maxcells[d] = m1[d];
+      L->lp2.w[d] = base + o2[d];
+      L->lp2.n[d] = (int)w2[d].size();
+      L->lp2.maxcells[d] = m2[d];
+    }
+  }
+  L->flux_form = form;
+  if (L->gsync) cudaGraphExecDestroy(L->gsync);
+  if (L->gasync) cudaGraphExecDestroy(L->gasync);
+  L->gsync = L->gasync = nullptr;
+  return MF_OK;
+}
+
+mf_status mf_level_set_flux_form(mf_level* L, int form) {
+  if (!L) return MF_ERR_BAD_ARG;
+  return level_set_flux_form(L, form);
+}
+
+mf_status mf_level_flux_form(const mf_level* L, int* form) {
+  if (!L || !form) return MF_ERR_BAD_ARG;
+  *form = L->flux_form;
+  return MF_OK;
+}
+
 mf_status mf_level_set_overlap(mf_level* L, int chunks) {
   if (!L) return MF_ERR_BAD_ARG;
   return level_set_chunks(L, chunks);
@@ -2191,13 +2260,17 @@ static mf_status time_kind(mf_level* L, int kind, int reps, cudaEvent_t e0, cuda
     if (kind == 0) {
       e = mf::launch_prim(c->dp, B.uin, B.w, L->lean ? L->bp : b, L->s, B.wf);
     } else if (kind == 1) {
+      const mf::LinePlan& lp = (p.time_approximation == MF_TA_RK2) ? L->lp1 : L->lp2;
+      const bool lines = L->flux_form == MF_FLUX_LINES;
       for (int d = 0; d < sd && e == cudaSuccess; ++d) {
         if (p.precision == MF_PREC_MIXED)
           e = mf::launch_flux_fast<float>(c->dp, d, B.w, B.f[d], B.bn[d], b, ds, L->s, B.wf);
         else if (p.precision == MF_PREC_FP64_FAST)
-          e = mf::launch_flux_fast<double>(c->dp, d, B.w, B.f[d], B.bn[d], b, ds, L->s);
+          e = lines ? mf::launch_flux_lines_fast(c->dp, d, B.w, B.f[d], B.bn[d], b, lp, ds, L->s)
+                    : mf::launch_flux_fast<double>(c->dp, d, B.w, B.f[d], B.bn[d], b, ds, L->s);
         else
-          e = mf::launch_flux_exact(c->dp, d, B.w, B.f[d], B.bn[d], b, ds, L->s);
+          e = lines ? mf::launch_flux_lines_exact(c->dp, d, B.w, B.f[d], B.bn[d], b, lp, ds, L->s)
+                    : mf::launch_flux_exact(c->dp, d, B.w, B.f[d], B.bn[d], b, ds, L->s);
       }
     } else if (kind == 4) {  // fluxes + update of stage 1 in the level's chunks, overlapped
       StageBuffers Bo = B;
@@ -2265,6 +2338,19 @@ mf_status mf_level_autotune(mf_level* L, int reps, int threads[3]) {
   // flux registers keeps the split, unchunked kernels, which store the fluxes.
   const mf_params& p = c->p;
   const int sd = p.space_dim;
+  // FP64 paths: the face fluxes per face against by lines
+  if (st == MF_OK && p.precision != MF_PREC_MIXED && p.time_approximation != MF_TA_HANCOCK) {
+    float tfa = 0.f, tli = 0.f;
+    st = level_set_flux_form(L, MF_FLUX_FACES);
+    if (st == MF_OK) st = time_kind(L, 1, reps, e0, e1, &tfa);
+    int form = MF_FLUX_FACES;
+    if (st == MF_OK && level_set_flux_form(L, MF_FLUX_LINES) == MF_OK) {
+      st = time_kind(L, 1, 1, e0, e1, &tli);  // warm-up
+      if (st == MF_OK) st = time_kind(L, 1, reps, e0, e1, &tli);
+      if (st == MF_OK && tli < tfa) form = MF_FLUX_LINES;
+    }
+    if (st == MF_OK) st = level_set_flux_form(L, form);
+  }
   if (st == MF_OK && L->gathers.empty()) {
     float tf = 0.f, tu = 0.f;
     if (p.precision == MF_PREC_MIXED) st = level_set_chunks(L, 1);

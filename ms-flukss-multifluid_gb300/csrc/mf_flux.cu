@@ -1,6 +1,8 @@
 // mf_flux.cu - face-flux kernel with the fast physics (contraction allowed,
 // reciprocals reused): FP32 for the mixed-precision path, FP64 for the fast
 // FP64 path.
+#include <algorithm>
+
 #define MF_PHYS fast
 #include "mf_riemann.cuh"
 #include "mf_flux_kernel.cuh"
@@ -40,6 +42,54 @@ cudaError_t launch_flux_fast(const DevParams& P, int dir, const double* w, void*
   }
   flux_dirs<R, 0>(P, dir, w, nullptr, F, Bn, b, state, gf, nt, first, end, s);
   return cudaGetLastError();
+}
+
+cudaError_t launch_flux_lines_fast(const DevParams& P, int dir, const double* w, void* f,
+                                   void* bn, const Batch& b, const LinePlan& lp,
+                                   const StepState* state, cudaStream_t s) {
+  return launch_lflux_t<double>(P, dir, w, f, bn, b, lp, state, s);
+}
+
+cudaError_t lines_prepare_exact();
+
+cudaError_t lines_prepare() {
+  static bool done[64] = {};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev >= 0 && dev < 64 && done[dev]) return cudaSuccess;
+  e = lflux_allow_t<double>();
+  if (e == cudaSuccess) e = lines_prepare_exact();
+  if (e == cudaSuccess && dev >= 0 && dev < 64) done[dev] = true;
+  return e;
+}
+
+bool make_lines(const StageDesc* hd, int n, int sd, std::vector<LineWork> out[3],
+                int maxcells[3]) {
+  for (int d = 0; d < 3; ++d) {
+    out[d].clear();
+    maxcells[d] = 0;
+  }
+  for (int d = 0; d < sd; ++d) {
+    const int t1 = (d == 0) ? 1 : 0, t2 = (d == 2) ? 1 : 2;
+    for (int i = 0; i < n; ++i) {
+      const StageDesc& D = hd[i];
+      const int nd = D.vn[d];
+      const int lines = D.vn[t1] * D.vn[t2];
+      if (nd <= 0 || lines <= 0) continue;
+      if (nd + 2 > kLineMaxCells) return false;
+      const int per = std::max(1, kLineThreads / (nd + 1));
+      for (int l0 = 0; l0 < lines; l0 += per) {
+        LineWork Wk;
+        Wk.desc = i;
+        Wk.line0 = l0;
+        Wk.nlines = std::min(per, lines - l0);
+        maxcells[d] = std::max(maxcells[d], Wk.nlines * (nd + 2));
+        out[d].push_back(Wk);
+      }
+    }
+  }
+  return true;
 }
 
 template <typename R>

@@ -26,6 +26,14 @@ cudaError_t launch_flux_exact(const DevParams& P, int dir, const double* w, void
   return cudaGetLastError();
 }
 
+cudaError_t launch_flux_lines_exact(const DevParams& P, int dir, const double* w, void* f,
+                                    void* bn, const Batch& b, const LinePlan& lp,
+                                    const StepState* state, cudaStream_t s) {
+  return launch_lflux_t<double>(P, dir, w, f, bn, b, lp, state, s);
+}
+
+cudaError_t lines_prepare_exact() { return lflux_allow_t<double>(); }
+
 cudaError_t launch_face_flux_exact(const DevParams& P, int dir, const double* wl,
                                    const double* wr, double* f, int n, double ch,
                                    cudaStream_t s) {

@@ -489,40 +489,29 @@ __global__ void __launch_bounds__(kMaxBlock, WF ? 2 : 1)
   }
 }
 
-// Corrector fluxes of the Hancock step (correctorHancock, src/PatchMHDAM.cpp:
-// 1002-1189): the Riemann problem of each face of the valueBox between the
-// high-face value of the low cell and the low-face value of the high cell,
-// both shifted by W(t+dt/2) - W(t); Bn from the same states (recomputed
-// after the shift in predictorHancock, :981-985).  Face values: fv[(side*nc
-// + v)*cells(slope) + cell], side 0 = low face, 1 = high face.
-template <typename R, int DIR>
-__global__ void __launch_bounds__(kMaxBlock)
-    k_hflux(const __grid_constant__ DevParams P, const double* __restrict__ W, const double* __restrict__ FV,
-            R* __restrict__ F, R* __restrict__ Bn, const StageDesc* __restrict__ descs, int ndesc,
-            int total, const RunParams* __restrict__ runs, const StepState* __restrict__ states) {
-  const int gi = blockIdx.x * blockDim.x + threadIdx.x;
-  if (gi >= total) return;
-  const StageDesc& D = descs[find_desc(descs, ndesc, kRegF + DIR, gi)];
-  const int lin = gi - D.g0[kRegF + DIR];
-  const RunParams& RP = runs[D.run];
+// Fluxes of face (i,j,k) (normal DIR) from given face states: the plasma
+// solver, the GLM (Bn, psi) system, Bn (PatchMHDMF::computeBn), HELIOBC on
+// the domain boundary, the neutral van Leer fluxes and LEVELSETFLUX.  fs(side,
+// v): component v of the left (side 0: the high-face value of the low cell)
+// or the right (side 1: the low-face value of the high cell) state.  Written
+// to F / Bn at the face's offsets; W: the cell-centred primitive state (Bn of
+// divb_method 2).
+template <typename R, int DIR, typename FS>
+__device__ __forceinline__ void riemann_face(const DevParams& P, const RunParams& RP,
+                                             const StageDesc& D, int i, int j, int k,
+                                             const double* __restrict__ W, R* __restrict__ F,
+                                             R* __restrict__ Bn, const StepState* states,
+                                             const FS& fs) {
   int fnb[3] = {D.vn[0], D.vn[1], D.vn[2]};
   fnb[DIR] += 1;
-  int i, j, k;
-  decode(lin, D.vlo, fnb, i, j, k);
-  const long long scs = (long long)D.sn[0] * D.sn[1] * D.sn[2];
-  const double* __restrict__ fv = FV + D.fv_off[DIR];
-  const long long cr = loc(D.slo, D.sn, i, j, k);
-  const long long cl = cr - ((DIR == 0) ? 1 : (DIR == 1) ? (long long)D.sn[0]
-                                                         : (long long)D.sn[0] * D.sn[1]);
-  const int nc = P.nc;
   const long long fcs = (long long)fnb[0] * fnb[1] * fnb[2];
   R* __restrict__ Fo = F + D.f_off[DIR] + loc(D.vlo, fnb, i, j, k);
   R wl[9], wr[9];
 #pragma unroll
   for (int v = 0; v < 9; ++v) {
     const bool on = (v < 8) || P.glm;
-    wl[v] = on ? R(fv[(nc + v) * scs + cl]) : R(0);
-    wr[v] = on ? R(fv[v * scs + cr]) : R(0);
+    wl[v] = on ? R(fs(0, v)) : R(0);
+    wr[v] = on ? R(fs(1, v)) : R(0);
   }
   R g[9];
   plasma_flux<R, DIR>(P, wl, wr, g);
@@ -547,7 +536,7 @@ __global__ void __launch_bounds__(kMaxBlock)
     const double* wv = W + D.u_off + loc(D.flo, D.fn, i, j, k) + (5 + DIR) * cs;
     bn = R(0.5 * (wv[-st] + wv[0]));
   }
-  // fluxBC of correctorHancock (src/PatchMHDAM.cpp:1105-1106)
+  // HELIOBC on the domain boundary (after the Riemann fluxes and Bn)
   const int hside = helio_side<DIR>(P, RP, i, j, k);
   if (hside >= 0) {
     double dl[8], dr[8], dg[8], dbn = double(bn);
@@ -570,8 +559,8 @@ __global__ void __launch_bounds__(kMaxBlock)
     R nl[5], nr[5], gn[5];
 #pragma unroll
     for (int m = 0; m < 5; ++m) {
-      nl[m] = R(fv[(nc + s0 + m) * scs + cl]);
-      nr[m] = R(fv[(s0 + m) * scs + cr]);
+      nl[m] = R(fs(0, s0 + m));
+      nr[m] = R(fs(1, s0 + m));
     }
     if (hside >= 0) {
       double dl[5], dr[5], dg[5];
@@ -589,15 +578,193 @@ __global__ void __launch_bounds__(kMaxBlock)
 #pragma unroll
     for (int m = 0; m < 5; ++m) Fo[(s0 + m) * fcs] = gn[m];
   }
-  // tracking surfaces (LEVELSETFLUX of the shifted face values,
-  // src/PatchMHDAM.cpp:1111-1115)
+  // tracking surfaces: LEVELSETFLUX (src/LevelSetF.ChF:37-105), the upwind
+  // face value by the sign of sqrt(rho_L) u_L + sqrt(rho_R) u_R
   if (P.nls) {
     const R uavg = sqrt(wl[0]) * wl[1 + DIR] + sqrt(wr[0]) * wr[1 + DIR];
     for (int q = P.ils; q < P.nc; ++q) {
-      const R l = R(fv[(nc + q) * scs + cl]), r = R(fv[q * scs + cr]);
+      const R l = R(fs(0, q)), r = R(fs(1, q));
       Fo[q * fcs] = (uavg > R(0)) ? l : r;
     }
   }
+}
+
+// Corrector fluxes of the Hancock step (correctorHancock, src/PatchMHDAM.cpp:
+// 1002-1189): the Riemann problem of each face of the valueBox between the
+// high-face value of the low cell and the low-face value of the high cell,
+// both shifted by W(t+dt/2) - W(t); Bn from the same states (recomputed
+// after the shift in predictorHancock, :981-985); fluxBC of correctorHancock
+// (:1105-1106) and LEVELSETFLUX of the shifted face values (:1111-1115).
+// Face values: fv[(side*nc + v)*cells(slope) + cell], side 0 = low face,
+// 1 = high face.
+template <typename R, int DIR>
+__global__ void __launch_bounds__(kMaxBlock)
+    k_hflux(const __grid_constant__ DevParams P, const double* __restrict__ W, const double* __restrict__ FV,
+            R* __restrict__ F, R* __restrict__ Bn, const StageDesc* __restrict__ descs, int ndesc,
+            int total, const RunParams* __restrict__ runs, const StepState* __restrict__ states) {
+  const int gi = blockIdx.x * blockDim.x + threadIdx.x;
+  if (gi >= total) return;
+  const StageDesc& D = descs[find_desc(descs, ndesc, kRegF + DIR, gi)];
+  const int lin = gi - D.g0[kRegF + DIR];
+  const RunParams& RP = runs[D.run];
+  int fnb[3] = {D.vn[0], D.vn[1], D.vn[2]};
+  fnb[DIR] += 1;
+  int i, j, k;
+  decode(lin, D.vlo, fnb, i, j, k);
+  const long long scs = (long long)D.sn[0] * D.sn[1] * D.sn[2];
+  const double* __restrict__ fv = FV + D.fv_off[DIR];
+  const long long cr = loc(D.slo, D.sn, i, j, k);
+  const long long cl = cr - ((DIR == 0) ? 1 : (DIR == 1) ? (long long)D.sn[0]
+                                                         : (long long)D.sn[0] * D.sn[1]);
+  const int nc = P.nc;
+  riemann_face<R, DIR>(P, RP, D, i, j, k, W, F, Bn, states, [&](int side, int v) -> double {
+    return side ? fv[v * scs + cr] : fv[(nc + v) * scs + cl];
+  });
+}
+
+// Face fluxes of one direction by lines (FP64 paths): a block takes whole
+// lines of faces along DIR of one patch (LineWork); it first computes the
+// limited face values of every cell of its lines once (the cells from one
+// below to one above the valueBox along DIR, with the positivity fallback
+// and characteristic limiting as k_flux applies them) into shared memory,
+// then the Riemann fluxes of the lines' faces from them.  k_flux evaluates
+// the limiters of both cells beside each face, i.e. twice per cell; the
+// results are the same values (the same face_values calls on the same
+// inputs).  Shared memory: sv[(2 v + side) ncell + c], side 0 = low face,
+// c = the thread index of the cell in phase 1 (x-fastest order).
+template <typename R, int DIR>
+__global__ void __launch_bounds__(kLineThreads, 2)
+    k_lflux(const __grid_constant__ DevParams P, const double* __restrict__ W, R* __restrict__ F,
+            R* __restrict__ Bn, const StageDesc* __restrict__ descs,
+            const LineWork* __restrict__ work, const RunParams* __restrict__ runs,
+            const StepState* __restrict__ states) {
+  extern __shared__ double sv[];
+  const LineWork Wk = work[blockIdx.x];
+  const StageDesc& D = descs[Wk.desc];
+  const RunParams& RP = runs[D.run];
+  constexpr int T1 = (DIR == 0) ? 1 : 0, T2 = (DIR == 2) ? 1 : 2;  // transverse dims
+  const int nd = D.vn[DIR], nt1 = D.vn[T1];
+  const int nl = Wk.nlines, ncl = nd + 2, ncell = nl * ncl;
+  const long long cs = (long long)D.fn[0] * D.fn[1] * D.fn[2];
+  const long long st = (DIR == 0) ? 1 : (DIR == 1) ? (long long)D.fn[0]
+                                                   : (long long)D.fn[0] * D.fn[1];
+  const int nc = P.nc;
+  // phase 1: DIR 0 takes a line's cells consecutively, DIR 1 and 2 the lines
+  // (consecutive x) consecutively, so that loads follow the x-fastest layout
+  for (int t = threadIdx.x; t < ncell; t += blockDim.x) {
+    int line, pos;
+    if (DIR == 0) {
+      line = t / ncl;
+      pos = t - line * ncl;
+    } else {
+      pos = t / nl;
+      line = t - pos * nl;
+    }
+    const int L = Wk.line0 + line;
+    int x[3];
+    x[DIR] = D.vlo[DIR] - 1 + pos;
+    x[T1] = D.vlo[T1] + L % nt1;
+    x[T2] = D.vlo[T2] + L / nt1;
+    const double* __restrict__ w0 = W + D.u_off + loc(D.flo, D.fn, x[0], x[1], x[2]);
+    bool neg = false;
+    double clo[8], chi[8];
+    if (P.char_rec) {
+      double a8[8], b8[8], c8[8];
+#pragma unroll
+      for (int v = 0; v < 8; ++v) {
+        const double* wv = w0 + v * cs;
+        a8[v] = wv[-st];
+        b8[v] = wv[0];
+        c8[v] = wv[st];
+      }
+      char_face_values<DIR>(P, a8, b8, c8, clo, chi);
+      if (P.check_pos) neg = clo[0] <= 0.0 || chi[0] <= 0.0 || clo[4] <= 0.0 || chi[4] <= 0.0;
+    } else if (P.check_pos) {
+#pragma unroll
+      for (int q = 0; q < 2; ++q) {
+        const int v = q ? 4 : 0;
+        const double* wv = w0 + v * cs;
+        R lo, hi;
+        face_values<R>(P.lim[v], R(wv[-st]), R(wv[0]), R(wv[st]), lo, hi);
+        if (lo <= R(0) || hi <= R(0)) neg = true;
+      }
+    }
+    for (int v = 0; v < nc; ++v) {
+      const double* wv = w0 + v * cs;
+      R lo, hi;
+      if (neg) {
+        lo = R(wv[0]);
+        hi = lo;
+      } else if (P.char_rec && v < 8) {
+        lo = R(clo[v]);
+        hi = R(chi[v]);
+      } else if (v >= P.ils) {
+        ls_face_values<R>(P, R(wv[-st]), R(wv[0]), R(wv[st]), lo, hi);
+      } else {
+        const int lim = (v < 8) ? P.lim[v] : (int)MF_LIM_MINMOD;
+        face_values<R>(lim, R(wv[-st]), R(wv[0]), R(wv[st]), lo, hi);
+      }
+      sv[(2 * v) * ncell + t] = double(lo);
+      sv[(2 * v + 1) * ncell + t] = double(hi);
+    }
+  }
+  __syncthreads();
+  // phase 2: the faces of the lines, x-fastest as in phase 1
+  const int nfl = nd + 1, nface = nl * nfl;
+  for (int t = threadIdx.x; t < nface; t += blockDim.x) {
+    int line, f, cl, cr;
+    if (DIR == 0) {
+      line = t / nfl;
+      f = t - line * nfl;
+      cl = line * ncl + f;
+      cr = cl + 1;
+    } else {
+      f = t / nl;
+      line = t - f * nl;
+      cl = f * nl + line;
+      cr = cl + nl;
+    }
+    const int L = Wk.line0 + line;
+    int x[3];
+    x[DIR] = D.vlo[DIR] + f;
+    x[T1] = D.vlo[T1] + L % nt1;
+    x[T2] = D.vlo[T2] + L / nt1;
+    riemann_face<R, DIR>(P, RP, D, x[0], x[1], x[2], W, F, Bn, states,
+                         [&](int side, int v) -> double {
+                           return side ? sv[(2 * v) * ncell + cr] : sv[(2 * v + 1) * ncell + cl];
+                         });
+  }
+}
+
+// Launch the line kernel for direction dir on a batch's line work list.
+template <typename R>
+cudaError_t launch_lflux_t(const DevParams& P, int dir, const double* w, void* f, void* bn,
+                           const Batch& b, const LinePlan& lp, const StepState* state,
+                           cudaStream_t s) {
+  const int n = lp.n[dir];
+  if (n <= 0) return cudaSuccess;
+  const size_t smem = line_smem_bytes(P.nc, lp.maxcells[dir]);
+  R* F = (R*)f;
+  R* Bn = (R*)bn;
+  if (dir == 0)
+    k_lflux<R, 0><<<n, kLineThreads, smem, s>>>(P, w, F, Bn, b.desc, lp.w[0], b.runs, state);
+  if (dir == 1)
+    k_lflux<R, 1><<<n, kLineThreads, smem, s>>>(P, w, F, Bn, b.desc, lp.w[1], b.runs, state);
+  if (dir == 2)
+    k_lflux<R, 2><<<n, kLineThreads, smem, s>>>(P, w, F, Bn, b.desc, lp.w[2], b.runs, state);
+  return cudaGetLastError();
+}
+
+// Allow the line kernels' shared memory (once per device, outside any capture).
+template <typename R>
+cudaError_t lflux_allow_t() {
+  const int most = (int)line_smem_bytes(MF_MAX_COMP, kLineMaxCells);
+  cudaError_t e = cudaFuncSetAttribute(k_lflux<R, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, most);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_lflux<R, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, most);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_lflux<R, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, most);
+  return e;
 }
 
 template <typename R>

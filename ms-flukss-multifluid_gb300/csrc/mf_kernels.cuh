@@ -190,6 +190,29 @@ struct FusedPlan {
 
 struct OverlapPlan;
 
+// Face fluxes by lines (FP64 paths): each block takes whole lines of faces
+// along one direction of one patch and shares the cells' face values.
+constexpr int kLineThreads = 128;
+constexpr int kLineMaxCells = 256;  // cells of one block's lines (2 beyond each line's faces)
+struct LineWork {
+  int desc;    // desc index in the batch
+  int line0;   // first line: index over the transverse cells, the lower dimension fastest
+  int nlines;  // lines of the block
+};
+struct LinePlan {
+  const LineWork* w[3];  // device work lists per direction
+  int n[3];              // blocks per direction
+  int maxcells[3];       // most cells of one block per direction
+};
+inline size_t line_smem_bytes(int nc, int cells) {
+  return sizeof(double) * 2 * (size_t)nc * (size_t)cells;
+}
+// Work lists of a batch's descs (host) per direction: lines of up to
+// kLineThreads faces per block; false when a patch is too long along a
+// direction for one block's shared memory (kLineMaxCells).
+bool make_lines(const StageDesc* hd, int n, int sd, std::vector<LineWork> out[3],
+                int maxcells[3]);
+
 struct StageBuffers {
   const double* uin;   // state the stage starts from
   double* uout;        // state the stage writes (valueBox cells only)
@@ -210,6 +233,7 @@ struct StageBuffers {
   const LeanPrim* lean;  // optional: primitive state on valid cells + ghost copies
   const FusedPlan* fused;  // optional (mixed precision): fluxes + update in one kernel
   const OverlapPlan* overlap;  // optional (mixed precision): chunked, overlapped flux + update
+  const LinePlan* lines;       // optional (FP64 paths): face fluxes by lines
 };
 
 enum StageFlags : int { kStageAverage = 1, kStageDt = 2 };
@@ -252,6 +276,15 @@ cudaError_t launch_update_exact(const DevParams& P, const StageBuffers& B, const
                                 DtPartial* partials, int* nblocks_v, cudaStream_t s);
 // fast physics: R = float (mixed precision) or double (fast FP64)
 // wf (R = float only, nullable): the FP32 copy of w the prim kernel wrote
+// face fluxes by lines (k_lflux), FP64 paths; *_prepare once per device
+// before the first launch (outside any capture)
+cudaError_t launch_flux_lines_exact(const DevParams& P, int dir, const double* w, void* f,
+                                    void* bn, const Batch& b, const LinePlan& lp,
+                                    const StepState* state, cudaStream_t s);
+cudaError_t launch_flux_lines_fast(const DevParams& P, int dir, const double* w, void* f,
+                                   void* bn, const Batch& b, const LinePlan& lp,
+                                   const StepState* state, cudaStream_t s);
+cudaError_t lines_prepare();
 // [first, end): a range of the batch's flat face / cell index (end < 0: to
 // the batch's total); an update range starts on a multiple of the block size
 template <typename R>

@@ -51,9 +51,11 @@ cudaError_t launch_stage(const DevParams& P, int precision, const StageBuffers& 
     if (precision == MF_PREC_MIXED)
       e = launch_flux_fast<float>(P, d, B.w, B.f[d], B.bn[d], b, state, s, B.wf);
     else if (precision == MF_PREC_FP64_FAST)
-      e = launch_flux_fast<double>(P, d, B.w, B.f[d], B.bn[d], b, state, s);
+      e = B.lines ? launch_flux_lines_fast(P, d, B.w, B.f[d], B.bn[d], b, *B.lines, state, s)
+                  : launch_flux_fast<double>(P, d, B.w, B.f[d], B.bn[d], b, state, s);
     else
-      e = launch_flux_exact(P, d, B.w, B.f[d], B.bn[d], b, state, s);
+      e = B.lines ? launch_flux_lines_exact(P, d, B.w, B.f[d], B.bn[d], b, *B.lines, state, s)
+                  : launch_flux_exact(P, d, B.w, B.f[d], B.bn[d], b, state, s);
     if (e != cudaSuccess) return e;
     if (B.ev) cudaEventRecord(B.ev[ne++], s);
   }

@@ -33,6 +33,7 @@ NOALLOC_SCRATCH_BYTES = 16 << 20
 
 TA_FIRST_ORDER, TA_HANCOCK, TA_RK2 = 0, 1, 2
 PREC_FP64, PREC_MIXED, PREC_FP64_FAST, PREC_MIXED_CE32 = 0, 1, 2, 3
+FLUX_FACES, FLUX_LINES = 0, 1
 BC_NONE, BC_FARFIELD = 0, 1
 LIM_CD, LIM_MINMOD, LIM_SUPERBEE, LIM_VANALBADA, LIM_MC, LIM_HARMONIC, LIM_VANLEER = (
     0, 1, 2, 3, 4, 5, 9)
@@ -201,6 +202,8 @@ _SIGS = {
     "mf_level_schedule": (ctypes.c_int, [ctypes.c_void_p, c_int3]),
     "mf_level_set_overlap": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "mf_level_overlap": (ctypes.c_int, [ctypes.c_void_p, _P(ctypes.c_int)]),
+    "mf_level_set_flux_form": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "mf_level_flux_form": (ctypes.c_int, [ctypes.c_void_p, _P(ctypes.c_int)]),
     "mf_level_profile_step": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double,
                                              _P(ctypes.c_float), _P(ctypes.c_int),
                                              _P(ctypes.c_int), ctypes.c_int]),
@@ -750,6 +753,17 @@ class Level:
         fluxes and update overlap on two streams (mixed precision)."""
         check(self.lib.mf_level_set_overlap(self.h, chunks), "mf_level_set_overlap")
 
+    def set_flux_form(self, form):
+        """mf_level_set_flux_form: FLUX_FACES (one thread per face) or
+        FLUX_LINES (blocks over whole lines of faces, each cell's face values
+        computed once); FP64 paths, results unchanged."""
+        check(self.lib.mf_level_set_flux_form(self.h, form), "mf_level_set_flux_form")
+
+    def flux_form(self):
+        n = ctypes.c_int()
+        check(self.lib.mf_level_flux_form(self.h, ctypes.byref(n)), "mf_level_flux_form")
+        return n.value
+
     def overlap(self):
         n = ctypes.c_int()
         check(self.lib.mf_level_overlap(self.h, ctypes.byref(n)), "mf_level_overlap")
@@ -773,8 +787,9 @@ class Level:
         """mf_level_autotune: threads per block of the prim, flux and update
         kernels, and the schedule (split kernels or a fused tile shape, read
         by schedule(); for split mixed precision the overlap chunks, read by
-        overlap()), picked by timing; returns the chosen (prim, flux, update)
-        threads."""
+        overlap(); for the FP64 paths the face-flux form, read by
+        flux_form()), picked by timing; returns the chosen (prim, flux,
+        update) threads."""
         t = c_int3()
         check(self.lib.mf_level_autotune(self.h, reps, t), "mf_level_autotune")
         return tuple(t)

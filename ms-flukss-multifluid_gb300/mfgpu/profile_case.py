@@ -5,7 +5,8 @@ committed ncu summaries capture.
     python -m mfgpu.profile_case --n 64 --patch 16 --precision mixed --schedule 0,0,0 --steps 2
 
 --schedule: "auto" runs the autotuner; "0,0,0" the split kernels; x,y,z a
-fused tile shape.  --overlap K: the split kernels in K overlapped chunks.
+fused tile shape.  --overlap K: the split kernels in K overlapped chunks;
+--flux-form lines: the FP64 face fluxes by lines.
 Prints the status, the schedule and the step times (CUDA events), and exits
 non-zero when a step reports an error."""
 import argparse
@@ -27,6 +28,8 @@ def main(argv=None):
     ap.add_argument("--schedule", default="0,0,0")
     ap.add_argument("--overlap", type=int, default=1,
                     help="chunks of overlapped fluxes and update (mixed precision, split)")
+    ap.add_argument("--flux-form", choices=["faces", "lines"], default="faces",
+                    help="face fluxes of the FP64 paths per face or by lines")
     ap.add_argument("--steps", type=int, default=2)
     a = ap.parse_args(argv)
     import torch
@@ -46,6 +49,8 @@ def main(argv=None):
         lev.set_schedule(tuple(int(v) for v in a.schedule.split(",")))
         if a.overlap > 1:
             lev.set_overlap(a.overlap)
+        if a.flux_form == "lines":
+            lev.set_flux_form(mfgpu.FLUX_LINES)
     stream = torch.cuda.Stream()
     dt0 = lev.compute_dt()[0]
     lev.seed_dt(0.4 * dt0, 0.4, stream.cuda_stream)
