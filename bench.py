@@ -246,7 +246,8 @@ def run_ours(a):
     ctx, lev, host, dt0 = _build_level(mfgpu, p64, boxes, torch)
     # the project's autotuner: threads per block of each kernel kind and the
     # stage schedule (split kernels or a fused tile shape), picked by timing
-    tuned = {"threads": list(lev.autotune(3)), "schedule": list(lev.schedule())}
+    tuned = {"threads": list(lev.autotune(3)), "schedule": list(lev.schedule()),
+             "flux_form": "lines" if lev.flux_form() == mfgpu.FLUX_LINES else "faces"}
     lev.seed_dt(CFL * dt0, CFL, stream.cuda_stream)
     for _ in range(a.warmup):
         lev.step_async(stream.cuda_stream)
@@ -317,7 +318,8 @@ def run_ours(a):
     if not a.no_mixed:
         pf = mfgpu.helio_params(n, precision=mfgpu.PREC_FP64_FAST)
         ctxf, levf, hostf, dtf = _build_level(mfgpu, pf, boxes, torch)
-        tunedf = {"threads": list(levf.autotune(3)), "schedule": list(levf.schedule())}
+        tunedf = {"threads": list(levf.autotune(3)), "schedule": list(levf.schedule()),
+                  "flux_form": "lines" if levf.flux_form() == mfgpu.FLUX_LINES else "faces"}
         levf.seed_dt(CFL * dtf, CFL, stream.cuda_stream)
         for _ in range(a.warmup):
             levf.step_async(stream.cuda_stream)
@@ -354,7 +356,8 @@ def run_ours(a):
         for name, prec, dtype in forms:
             pm = mfgpu.helio_params(n, precision=prec)
             ctxm, levm, hostm, dtm = _build_level(mfgpu, pm, boxes, torch)
-            tunedm = {"threads": list(levm.autotune(3)), "schedule": list(levm.schedule())}
+            tunedm = {"threads": list(levm.autotune(3)), "schedule": list(levm.schedule()),
+                      "overlap_chunks": levm.overlap()}
             levm.seed_dt(CFL * dtm, CFL, stream.cuda_stream)
             for _ in range(a.warmup):
                 levm.step_async(stream.cuda_stream)
