@@ -10,7 +10,8 @@
 // y <- y (1 + e + e^2), e = 1 - x y, whose truncation error is e^3 (< 2^-58):
 // 3 FP64 instructions, within one ulp of the correctly rounded 1/x.
 //
-// f2d: the exact FP32 -> FP64 conversion done with integer instructions.
+// f2d: the exact FP32 -> FP64 conversion done with integer instructions;
+// d2f: the rounded FP64 -> FP32 conversion likewise (normal results).
 //
 // log64: Tang's table-driven method (P. T. P. Tang, "Table-driven
 // implementation of the logarithm function in IEEE floating-point
@@ -120,6 +121,29 @@ __device__ __forceinline__ double f2d(float f) {
   }
   return __hiloint2double(static_cast<int>(sign | (ed << 20) | (m >> 3)),
                           static_cast<int>(m << 29));
+}
+
+// FP64 -> FP32 conversion, round to nearest even, in integer arithmetic (the
+// conversion instruction's result, bit for bit) for results in the normal
+// FP32 range: the 52-bit fraction keeps its leading 23 bits, the 29 dropped
+// bits decide the rounding (above half, or exactly half with an odd last
+// bit), and a carry out of the fraction moves into the exponent (up to inf).
+// Zero stays a signed zero; results below the normal range, inf and NaN
+// take the conversion instruction.
+__device__ __forceinline__ float d2f(double x) {
+  const unsigned hi = static_cast<unsigned>(__double2hiint(x));
+  const unsigned lo = static_cast<unsigned>(__double2loint(x));
+  const unsigned sign = hi & 0x80000000u;
+  const unsigned e = (hi >> 20) & 0x7ffu;
+  if (e - 897u < 254u) {  // FP32 exponent e - 896 in [1, 254]
+    const unsigned m = ((hi & 0x000fffffu) << 3) | (lo >> 29);
+    const unsigned rem = lo & 0x1fffffffu;
+    unsigned bits = ((e - 896u) << 23) | m;
+    bits += (rem > 0x10000000u || (rem == 0x10000000u && (m & 1u))) ? 1u : 0u;
+    return __uint_as_float(sign | bits);
+  }
+  if ((hi & 0x7fffffffu) == 0u && lo == 0u) return __uint_as_float(sign);
+  return static_cast<float>(x);
 }
 
 }  // namespace fp64

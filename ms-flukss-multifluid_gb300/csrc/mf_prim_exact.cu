@@ -3,8 +3,12 @@
 //
 // Built with -fmad=false: the primitive state feeds the limiter sign tests
 // and the region thresholds, so it is rounded exactly as in the CPU
-// restatement of the reference (EqSysMHDMF::stateToPrim).
+// restatement of the reference (EqSysMHDMF::stateToPrim).  The FP32 copy of
+// W (mixed precision) is rounded to nearest by fp64::d2f, which gives the
+// conversion instruction's bits with integer instructions (the kernel is
+// bound by the FP64 pipe, where the conversion instruction issues).
 #include "mf_internal.h"
+#include "mf_fp64.cuh"
 #include "mf_kernels.cuh"
 
 namespace mf {
@@ -77,8 +81,8 @@ __global__ void __launch_bounds__(kMaxBlock)
   if (Wf) {  // the FP32 copy the mixed-precision flux kernels read
 #pragma unroll
     for (int q = 0; q < MF_MAX_COMP; ++q)
-      if (q < P.ils) Wf[base + q * cs] = (float)w[q];
-    for (int q = P.ils; q < P.nc; ++q) Wf[base + q * cs] = (float)W[base + q * cs];
+      if (q < P.ils) Wf[base + q * cs] = fp64::d2f(w[q]);
+    for (int q = P.ils; q < P.nc; ++q) Wf[base + q * cs] = fp64::d2f(W[base + q * cs]);
   }
 }
 
@@ -120,7 +124,7 @@ __global__ void __launch_bounds__(256)
       for (int q = 0; q < 5; ++q) w[IRHON + q] = R.bc_n1[q];
     }
 #pragma unroll
-    for (int q = 0; q < MF_MAX_COMP; ++q) wf[q] = (float)w[q];
+    for (int q = 0; q < MF_MAX_COMP; ++q) wf[q] = fp64::d2f(w[q]);
     x[od] = (x[od] < R.dlo[od]) ? R.dlo[od] : R.dhi[od];
     bool inside = true;
     for (int d = 0; d < P.sd; ++d)
@@ -136,12 +140,12 @@ __global__ void __launch_bounds__(256)
           for (int q = 0; q < 5; ++q) u5[q] = U[eb + (s0 + q) * cs];
           cons_to_prim_euler(P, u5, w + s0);
 #pragma unroll
-          for (int q = 0; q < 5; ++q) wf[s0 + q] = (float)w[s0 + q];
+          for (int q = 0; q < 5; ++q) wf[s0 + q] = fp64::d2f(w[s0 + q]);
         } else if (have_w) {
 #pragma unroll
           for (int q = 0; q < 5; ++q) {
             w[s0 + q] = W[eb + (s0 + q) * cs];
-            wf[s0 + q] = (float)w[s0 + q];
+            wf[s0 + q] = fp64::d2f(w[s0 + q]);
           }
         } else {
 #pragma unroll
@@ -161,7 +165,7 @@ __global__ void __launch_bounds__(256)
     for (int q = P.ils; q < P.nc; ++q) {
       const double v = (P.reg_tracer && q == P.nc - 1) ? 1.0 : U[base + q * cs];
       W[base + q * cs] = v;
-      if (Wf) Wf[base + q * cs] = (float)v;
+      if (Wf) Wf[base + q * cs] = fp64::d2f(v);
     }
   }
 }

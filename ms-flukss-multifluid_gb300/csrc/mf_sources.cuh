@@ -127,6 +127,16 @@ __device__ __forceinline__ double ce_exp(double x) { return exp(x); }
 __device__ __forceinline__ float ce_exp(float x) { return expf(x); }
 __device__ __forceinline__ double ce_pow(double x, double y) { return pow(x, y); }
 __device__ __forceinline__ float ce_pow(float x, float y) { return powf(x, y); }
+// conversions between the FP64 state and the rates' type T (identities for
+// T = double).  The conversion instructions: their integer forms
+// (fp64::d2f / f2d) made the FP32-rate update 10% slower (more registers
+// and branches in a kernel bounded at 128 registers), measured.
+template <typename T>
+__device__ __forceinline__ T to_t(double x) {
+  return static_cast<T>(x);
+}
+__device__ __forceinline__ double to_d(float x) { return static_cast<double>(x); }
+__device__ __forceinline__ double to_d(double x) { return x; }
 
 // Pauls & Zank charge-exchange rates of one cell; adds S = -dt*H to u
 // (HeliosphericProblem::explicitSource, swlism/HeliosphericProblem.cpp:1394-1539,
@@ -142,15 +152,15 @@ __device__ __forceinline__ void charge_exchange_add(const DevParams& P, const WA
   const int nN = P.nf - 1;
   constexpr T c4p = T(4.0 * kInvPi), c16p = T(16.0 * kInvPi), c94pi = T(2.25 * kPi);
   constexpr T c4ip = T(4.0 * kInvPi), c649ip = T(64.0 / 9.0 * kInvPi);
-  const T rho = T(w[0]), ux = T(w[1]), uy = T(w[2]), uz = T(w[3]);
+  const T rho = to_t<T>(w[0]), ux = to_t<T>(w[1]), uy = to_t<T>(w[2]), uz = to_t<T>(w[3]);
   const T U2 = ux * ux + uy * uy + uz * uz, hU2 = T(0.5) * U2;
-  const T VVTP = T(w[4]) * ce_rcp(rho);
+  const T VVTP = to_t<T>(w[4]) * ce_rcp(rho);
   // plasma thermal-speed terms of the five speed arguments
   const T aUDp = c4p * VVTP, aUPMp = c16p * VVTP, aUHMp = c94pi * VVTP;
   const T aPEp = c4ip * VVTP, aHEp = c649ip * VVTP, q75VP = T(0.75) * VVTP;
-  const T scale_vel = T(P.ce_scale_vel), ce_a = T(P.ce_a), ce_b = T(P.ce_b);
-  const T damp_c = T(P.ce_damp_c), damp_pow = T(P.ce_damp_pow);
-  const T srho = T(P.ce_sigma_scale) * rho;
+  const T scale_vel = to_t<T>(P.ce_scale_vel), ce_a = to_t<T>(P.ce_a), ce_b = to_t<T>(P.ce_b);
+  const T damp_c = to_t<T>(P.ce_damp_c), damp_pow = to_t<T>(P.ce_damp_pow);
+  const T srho = to_t<T>(P.ce_sigma_scale) * rho;
   // Each population's own loss / gain is applied inside the loop; the
   // recipient of the newly created neutrals (region-dependent) then also
   // receives the plasma's totals.  The products ARR*UD, ARR*VVTHU and
@@ -164,13 +174,13 @@ __device__ __forceinline__ void charge_exchange_add(const DevParams& P, const WA
   for (int f = 1; f < MF_MAX_FLUIDS; ++f) {
     if (f > nN) break;
     const int o = IRHON + (f - 1) * 5;
-    const T rhoN = T(w[o]), uxN = T(w[o + 1]), uyN = T(w[o + 2]), uzN = T(w[o + 3]);
+    const T rhoN = to_t<T>(w[o]), uxN = to_t<T>(w[o + 1]), uyN = to_t<T>(w[o + 2]), uzN = to_t<T>(w[o + 3]);
     const T dx_ = ux - uxN, dy_ = uy - uyN, dz_ = uz - uzN;
     const T UH2 = uxN * uxN + uyN * uyN + uzN * uzN;
     const T DU2 = dx_ * dx_ + dy_ * dy_ + dz_ * dz_, DU2x4 = T(4) * DU2;
     const T VPHH = dx_ * uxN + dy_ * uyN + dz_ * uzN;
     const T VPHP = dx_ * ux + dy_ * uy + dz_ * uz;
-    const T VVTH = T(2) * (T(w[o + 4]) * ce_rcp(rhoN));
+    const T VVTH = T(2) * (to_t<T>(w[o + 4]) * ce_rcp(rhoN));
     // thermal + relative speeds; every argument is > 0, so sqrt(a) = a*rsqrt(a)
     const T aUD = (aUDp + c4p * VVTH) + DU2;
     const T UD = aUD * ce_rsqrt(aUD);
@@ -200,19 +210,19 @@ __device__ __forceinline__ void charge_exchange_add(const DevParams& P, const WA
     G = G + aV * VPHP + q75VP * (ARR * UHE);
     H5 = H5 + aT * VPHH + aU * (hU2 - T(0.5) * UH2) - T(0.75) * Y;
     double* un = u + IRHON + (f - 1) * 5;
-    un[0] = un[0] - dt * double(aU);
-    un[1] = un[1] - dt * double(uxN * aU - dx_ * aT);
-    un[2] = un[2] - dt * double(uyN * aU - dy_ * aT);
-    un[3] = un[3] - dt * double(uzN * aU - dz_ * aT);
-    un[4] = un[4] - dt * double((T(0.5) * UH2) * aU - VPHH * aT + T(0.75) * Y);
+    un[0] = un[0] - dt * to_d(aU);
+    un[1] = un[1] - dt * to_d(uxN * aU - dx_ * aT);
+    un[2] = un[2] - dt * to_d(uyN * aU - dy_ * aT);
+    un[3] = un[3] - dt * to_d(uzN * aU - dz_ * aT);
+    un[4] = un[4] - dt * to_d((T(0.5) * UH2) * aU - VPHH * aT + T(0.75) * Y);
   }
   const T h5 = G + H5;
   const T PPLUX = ux * DSUM - S1x, PPLUY = uy * DSUM - S1y, PPLUZ = uz * DSUM - S1z;
   const T ENPLU = hU2 * DSUM - G;
-  u[1] = u[1] - dt * double(h2);
-  u[2] = u[2] - dt * double(h3);
-  u[3] = u[3] - dt * double(h4);
-  u[4] = u[4] - dt * double(h5);
+  u[1] = u[1] - dt * to_d(h2);
+  u[2] = u[2] - dt * to_d(h3);
+  u[3] = u[3] - dt * to_d(h4);
+  u[4] = u[4] - dt * to_d(h5);
   // S of the magnetic field (and of psi) is zero; the recipient gets the
   // other populations' lost density (DSUM less its own, already applied)
   const int rk = ce_recipient(nN, reg);
@@ -221,11 +231,11 @@ __device__ __forceinline__ void charge_exchange_add(const DevParams& P, const WA
     if (f > nN) break;
     const bool rec = (f == rk);
     double* un = u + IRHON + (f - 1) * 5;
-    un[0] = rec ? un[0] - dt * double(DSUM) : un[0];
-    un[1] = rec ? un[1] - dt * double(PPLUX) : un[1];
-    un[2] = rec ? un[2] - dt * double(PPLUY) : un[2];
-    un[3] = rec ? un[3] - dt * double(PPLUZ) : un[3];
-    un[4] = rec ? un[4] - dt * double(ENPLU) : un[4];
+    un[0] = rec ? un[0] - dt * to_d(DSUM) : un[0];
+    un[1] = rec ? un[1] - dt * to_d(PPLUX) : un[1];
+    un[2] = rec ? un[2] - dt * to_d(PPLUY) : un[2];
+    un[3] = rec ? un[3] - dt * to_d(PPLUZ) : un[3];
+    un[4] = rec ? un[4] - dt * to_d(ENPLU) : un[4];
   }
 }
 
@@ -391,7 +401,7 @@ __device__ __forceinline__ float ws_sqrt(float x) { return sqrtf(x); }
 
 template <int IRHON, typename T = double>
 __device__ __forceinline__ double max_wave_speed(const DevParams& P, const double* u) {
-  const T i4pi = T(kInv4Pi), gam = T(P.gamma);
+  const T i4pi = T(kInv4Pi), gam = to_t<T>(P.gamma);
   T cmax = 0;
   {
     const double rinv = fp64::rcp64(u[0]);
@@ -399,10 +409,10 @@ __device__ __forceinline__ double max_wave_speed(const DevParams& P, const doubl
     const double ke = (m1 * m1 + m2 * m2 + m3 * m3) * rinv;
     const double bb = kInv4Pi * (bx * bx + by * by + bz * bz);
     const double p = fmax(P.hgamma * (u[4] - 0.5 * (ke + bb)), P.smallp);
-    const T invrho = T(rinv), b = T(bb);
-    const T uu = T(m1) * invrho, vv = T(m2) * invrho, ww = T(m3) * invrho;
-    const T bxt = T(bx), byt = T(by), bzt = T(bz);
-    const T a2 = gam * T(p) * invrho;
+    const T invrho = to_t<T>(rinv), b = to_t<T>(bb);
+    const T uu = to_t<T>(m1) * invrho, vv = to_t<T>(m2) * invrho, ww = to_t<T>(m3) * invrho;
+    const T bxt = to_t<T>(bx), byt = to_t<T>(by), bzt = to_t<T>(bz);
+    const T a2 = gam * to_t<T>(p) * invrho;
     const T as2 = T(0.5) * (a2 + invrho * b);
     const T as4 = as2 * as2;
     const T k4 = i4pi * invrho * a2;
@@ -420,13 +430,13 @@ __device__ __forceinline__ double max_wave_speed(const DevParams& P, const doubl
     const double m1 = un[1], m2 = un[2], m3 = un[3];
     const double ke = (m1 * m1 + m2 * m2 + m3 * m3) * rinv;
     const double p = fmax(P.hgamma * (un[4] - 0.5 * ke), P.smallp);
-    const T invrho = T(rinv);
-    const T uu = T(m1) * invrho, vv = T(m2) * invrho, ww = T(m3) * invrho;
-    const T a = ws_sqrt(gam * T(p) * invrho);
+    const T invrho = to_t<T>(rinv);
+    const T uu = to_t<T>(m1) * invrho, vv = to_t<T>(m2) * invrho, ww = to_t<T>(m3) * invrho;
+    const T a = ws_sqrt(gam * to_t<T>(p) * invrho);
     const T umax = fmax(fmax(fabs(uu), fabs(vv)), fabs(ww)) + a;
     cmax = fmax(umax, cmax);
   }
-  return double(cmax);
+  return to_d(cmax);
 }
 
 }  // namespace fast

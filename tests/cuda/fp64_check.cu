@@ -56,6 +56,27 @@ __global__ void k_f2d(int n, unsigned* mismatches) {
   if (!same) atomicAdd(mismatches, 1u);
 }
 
+// d2f against the conversion instruction, bit for bit: doubles over the
+// whole exponent range with hashed fractions, and fractions whose 29 dropped
+// bits are exactly half, just below and just above half (rounding ties)
+__global__ void k_d2f(int n, unsigned* mismatches) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  uint64_t h = (uint64_t)i * 0x9E3779B97F4A7C15ull;
+  h ^= h >> 31;
+  h *= 0xBF58476D1CE4E5B9ull;
+  h ^= h >> 29;
+  const uint64_t expo = (uint64_t)((i >> 2) % 2048) << 52;
+  uint64_t frac = h & 0x000fffffffffffffull;
+  const int tie = i & 3;  // 0: hashed; 1: exactly half; 2: half - 1; 3: half + 1
+  if (tie) frac = (frac & ~0x1fffffffull) | (0x10000000ull + (tie == 2 ? -1ll : tie == 3 ? 1 : 0));
+  const uint64_t bits = (h & 0x8000000000000000ull) | expo | frac;
+  const double x = __longlong_as_double((long long)bits);
+  const float a = mf::fp64::d2f(x), b = (float)x;
+  const bool same = (__float_as_uint(a) == __float_as_uint(b)) || (isnan(a) && isnan(b));
+  if (!same) atomicAdd(mismatches, 1u);
+}
+
 __global__ void k_special(int* bad) {
   const double xs[8] = {0.0, -0.0, -1.0, 4.9406564584124654e-324, 1e-310, INFINITY, -INFINITY, NAN};
   int b = 0;
@@ -84,12 +105,17 @@ int main() {
   k_f2d<<<(n + 255) / 256, 256>>>(n, mm);
   unsigned hm = 1;
   cudaMemcpy(&hm, mm, sizeof(unsigned), cudaMemcpyDeviceToHost);
+  cudaMemset(mm, 0, sizeof(unsigned));
+  k_d2f<<<(n + 255) / 256, 256>>>(n, mm);
+  unsigned hd = 1;
+  cudaMemcpy(&hd, mm, sizeof(unsigned), cudaMemcpyDeviceToHost);
   unsigned long long hw[2];
   int hb = -1;
   cudaMemcpy(hw, w, sizeof(hw), cudaMemcpyDeviceToHost);
   cudaMemcpy(&hb, bad, sizeof(int), cudaMemcpyDeviceToHost);
   const cudaError_t e = cudaDeviceSynchronize();
-  printf("rcp64_ulp %.4f\nlog64_ulp %.4f\nspecial_mismatch %d\nf2d_mismatch %u\nstatus %s\n",
-         hw[0] / 1024.0, hw[1] / 1024.0, hb, hm, cudaGetErrorString(e));
+  printf("rcp64_ulp %.4f\nlog64_ulp %.4f\nspecial_mismatch %d\nf2d_mismatch %u\nd2f_mismatch %u\n"
+         "status %s\n",
+         hw[0] / 1024.0, hw[1] / 1024.0, hb, hm, hd, cudaGetErrorString(e));
   return e == cudaSuccess ? 0 : 1;
 }

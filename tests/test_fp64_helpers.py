@@ -1,8 +1,8 @@
 """The FP64 helpers of csrc/mf_fp64.cuh on the GPU: the reciprocal and
 logarithm (used by the FP64 charge-exchange rates of the mixed-precision and
 FP64-fast paths) against the CUDA library's correctly rounded 1/x and its
-log, and the integer FP32 -> FP64 conversion against the conversion
-instruction, bit for bit."""
+log, and the integer FP32 <-> FP64 conversions against the conversion
+instructions, bit for bit."""
 import os
 import shutil
 import subprocess
@@ -49,5 +49,7 @@ def test_fp64_helpers_accuracy(tmp_path):
     assert float(vals["log64_ulp"]) <= 4.0
     # zero, negatives, subnormals, inf and NaN fall back to the library
     assert int(vals["special_mismatch"]) == 0
-    # the integer FP32 -> FP64 conversion equals the conversion instruction
+    # the integer FP32 -> FP64 and FP64 -> FP32 conversions equal the
+    # conversion instructions bit for bit (ties included)
     assert int(vals["f2d_mismatch"]) == 0
+    assert int(vals["d2f_mismatch"]) == 0
