@@ -146,10 +146,13 @@ __device__ __forceinline__ double to_d(double x) { return x; }
 // population shares are formed once per cell.
 // w: the stage-start primitive state (an array, or a column view that
 // loads each component where it is used).
-template <int IRHON, typename T = double, typename WA = const double*>
+// NN > 0: the number of neutral populations fixed at compile time (the
+// loops run a known count, so the populations' independent chains can be
+// scheduled together); 0: P.nf - 1 at run time.
+template <int IRHON, typename T = double, typename WA = const double*, int NN = 0>
 __device__ __forceinline__ void charge_exchange_add(const DevParams& P, const WA& w, int reg,
                                                     double dt, double* u) {
-  const int nN = P.nf - 1;
+  const int nN = NN > 0 ? NN : P.nf - 1;
   constexpr T c4p = T(4.0 * kInvPi), c16p = T(16.0 * kInvPi), c94pi = T(2.25 * kPi);
   constexpr T c4ip = T(4.0 * kInvPi), c649ip = T(64.0 / 9.0 * kInvPi);
   const T rho = to_t<T>(w[0]), ux = to_t<T>(w[1]), uy = to_t<T>(w[2]), uz = to_t<T>(w[3]);
