@@ -104,11 +104,14 @@ __device__ __forceinline__ int ce_recipient(int nN, int reg) {
 // (HeliosphericProblem::explicitSource, swlism/HeliosphericProblem.cpp:1394-1539).
 // T names the arithmetic type for interface symmetry with the fast physics;
 // the parity physics is FP64 only.
-template <int IRHON, typename T = double>
-__device__ __forceinline__ void charge_exchange_add(const DevParams& P, const double* w, int reg,
+// NN > 0: the number of neutral populations fixed at compile time (the same
+// operations in the same order; the loops run a known count, so the
+// populations' independent chains can be scheduled together); 0: P.nf - 1.
+template <int IRHON, typename T = double, typename WA = const double*, int NN = 0>
+__device__ __forceinline__ void charge_exchange_add(const DevParams& P, const WA& w, int reg,
                                                     double dt, double* u) {
   static_assert(sizeof(T) == sizeof(double), "FP64 physics");
-  const int nN = P.nf - 1;
+  const int nN = NN > 0 ? NN : P.nf - 1;
   double rho = w[0], ux = w[1], uy = w[2], uz = w[3], pp = w[4];
   double U2 = ux * ux + uy * uy + uz * uz;
   double VVTP = pp / rho;

@@ -189,17 +189,12 @@ __device__ __forceinline__ void update_tail(const DevParams& P, const StageBuffe
   if (P.ce && P.nf >= 2) {
     const double regtr = P.reg_tracer ? B.w[base + (P.nc - 1) * cs] : 0.0;
     const int reg = region_cell(P, RP.dx, i, j, k, w, regtr);
-    if constexpr (sizeof(R) == 4) {
-      // mixed precision: three neutral populations (the multi-fluid model's
-      // usual 4 fluids) with a compile-time count
-      if (P.nf == 4)
-        charge_exchange_add<IRHON, CE, typename std::decay<decltype(w)>::type, 3>(P, w, reg, dt,
-                                                                                  u);
-      else
-        charge_exchange_add<IRHON, CE>(P, w, reg, dt, u);
-    } else {
+    // three neutral populations (the multi-fluid model's usual 4 fluids)
+    // with a compile-time count, others with the run-time one
+    if (P.nf == 4)
+      charge_exchange_add<IRHON, CE, typename std::decay<decltype(w)>::type, 3>(P, w, reg, dt, u);
+    else
       charge_exchange_add<IRHON, CE>(P, w, reg, dt, u);
-    }
   }
   // problem post-processing and positivity (src/PatchMHDAM.cpp:705-707); with
   // constrained transport they follow the recalculation of B (k_recalc_b)
