@@ -406,13 +406,12 @@ mf_status mf_level_flux_form(const mf_level* lev, int* form);
    and one update launch per stage.  chunks = 2..MF_MAX_OVERLAP_CHUNKS: the
    level's patches are cut into about that many chunks of consecutive patches
    (each starting on a multiple of 256 cells; fewer where the patches do not
-   allow more) and each stage runs the FP32 flux kernels of the chunks on a
-   second stream while the update of the previous chunk runs, so the
-   FP64-bound update and the FP32 fluxes share the SMs; streams are ordered
-   by events only.  MF_PREC_MIXED and MF_PREC_MIXED_CE32 with RK2 or first
+   allow more) and each stage runs chunks + 1 launches, launch k computing
+   the FP32 fluxes of chunk k and the update of chunk k - 1 in one grid of
+   alternating blocks, so that the FP64-bound update and the FP32 fluxes
+   share the SMs.  MF_PREC_MIXED and MF_PREC_MIXED_CE32 with RK2 or first
    order and without constrained transport (else MF_ERR_UNSUPPORTED); the
-   fused schedule, attached flux registers and mf_level_profile_step use
-   unchunked launches.  mf_level_overlap returns the current chunk count;
+   fused schedule and attached flux registers use unchunked launches.  mf_level_overlap returns the current chunk count;
    mf_level_autotune picks it by timing. */
 #define MF_MAX_OVERLAP_CHUNKS 8
 mf_status mf_level_set_overlap(mf_level* lev, int chunks);
@@ -422,7 +421,8 @@ mf_status mf_level_overlap(const mf_level* lev, int* chunks);
    ms[i] is the device time of launch i, kinds[i] its kernel kind (0 ghost
    exchange, 1 primitive variables, 2 face fluxes, 3 update + sources,
    4 dt reduction, 5 hierarchy coupling, 6 problem post-processing,
-   7 constrained transport, 8 fused fluxes + update).  The state advances by
+   7 constrained transport, 8 fused fluxes + update, 9 the fluxes of one
+   overlap chunk with the update of the previous one).  The state advances by
    one step with time step dt. */
 mf_status mf_level_profile_step(mf_level* lev, double dt, float* ms, int* kinds, int* nlaunch,
                                 int max_launch);

@@ -384,13 +384,10 @@ struct mf_level {
   DevBuf tiles;
   mf::FusedPlan fp1, fp2;
   // chunked, overlapped flux + update launches of the split mixed-precision
-  // stages (mf_level_set_overlap): a chunk plan per stage batch, the flux
-  // stream and its events (created on first use)
+  // stages (mf_level_set_overlap): a chunk plan per stage batch
   int nchunks = 1;
   std::vector<mf::Chunk> ch1, ch2;
   mf::OverlapPlan op1{}, op2{};
-  cudaStream_t s2 = nullptr;
-  cudaEvent_t ov_ev[MF_MAX_OVERLAP_CHUNKS + 1] = {};
   // face fluxes by lines (FP64 paths, mf_level_set_flux_form): the work lists
   // of both stage batches, built on first use
   int flux_form = MF_FLUX_FACES;
@@ -399,8 +396,8 @@ struct mf_level {
 };
 
 // Kernel launches of one step: the plain count, plus the flux-register
-// gathers, less the flux launches the fused kernel replaces, plus the extra
-// flux and update launches of the chunked overlap.
+// gathers, less the flux launches the fused kernel replaces, and with the
+// chunked overlap n + 1 flux-and-update launches per stage instead of sd + 1.
 static void count_launches(mf_level* L) {
   const mf_params& p = L->ctx->p;
   const int per = (p.time_approximation == MF_TA_RK2) ? 2 : 1;
@@ -409,7 +406,7 @@ static void count_launches(mf_level* L) {
   const bool overlap = L->nchunks > 1 && !L->fused && L->gathers.empty() && !L->ctx->dp.ct;
   L->fused_saving = L->fused ? per * sd : 0;
   L->launches = L->base_launches + per * (int)L->gathers.size() - (fused ? per * sd : 0) +
-                (overlap ? per * (L->nchunks - 1) * (sd + 1) : 0);
+                (overlap ? per * (L->nchunks - sd) : 0);
 }
 
 // Work list of the fused kernel: each desc's valueBox cut into tiles of the
@@ -1411,9 +1408,8 @@ static mf_status enqueue_level_step(mf_level* L, int advance, cudaEvent_t* ev = 
   const int np0 = mf::prim_launches(lean, mixed);
   // the fused flux + update kernel, unless flux registers need the face fluxes
   const bool fused = L->fused && L->gathers.empty();
-  // chunked flux / update overlap of the split mixed-precision stages (not
-  // while profiling launch by launch: the events would straddle two streams)
-  const bool overlap = L->nchunks > 1 && !L->fused && L->gathers.empty() && !c->dp.ct && !ev;
+  // chunked flux / update overlap of the split mixed-precision stages
+  const bool overlap = L->nchunks > 1 && !L->fused && L->gathers.empty() && !c->dp.ct;
   const bool lines = L->flux_form == MF_FLUX_LINES;
   auto stage_marks = [&](int n0) {
     if (!ev) return;
@@ -1422,6 +1418,11 @@ static mf_status enqueue_level_step(mf_level* L, int advance, cudaEvent_t* ev = 
     if (fused) {
       kinds[n0 + np0] = 8;
       ne = n0 + np0 + 1;
+      return;
+    }
+    if (overlap) {  // chunks + 1 launches of fluxes and updates
+      for (int q = 0; q <= L->nchunks; ++q) kinds[n0 + np0 + q] = 9;
+      ne = n0 + np0 + L->nchunks + 1;
       return;
     }
     for (int d = 0; d < sd; ++d) kinds[n0 + np0 + d] = 2;
@@ -1778,9 +1779,6 @@ void mf_level_destroy(mf_level* L) {
   if (L->gsync) cudaGraphExecDestroy(L->gsync);
   if (L->gasync) cudaGraphExecDestroy(L->gasync);
   if (L->s) cudaStreamDestroy(L->s);
-  if (L->s2) cudaStreamDestroy(L->s2);
-  for (cudaEvent_t& e : L->ov_ev)
-    if (e) cudaEventDestroy(e);
   L->lines.release();
   L->U.release();
   L->U1.release();
@@ -2079,8 +2077,7 @@ mf_status mf_level_set_schedule(mf_level* L, const int tile[3]) {
 // Cut the split flux and update launches of each stage into chunks of
 // consecutive patches whose fluxes and updates overlap (MF_PREC_MIXED and
 // MF_PREC_MIXED_CE32, RK2 or first order, no constrained transport); 1 = one
-// launch each.  The plans and the flux stream are built here, outside any
-// capture.
+// launch each.
 static mf_status level_set_chunks(mf_level* L, int chunks) {
   const mf_params& p = L->ctx->p;
   if (chunks < 1 || chunks > MF_MAX_OVERLAP_CHUNKS) return MF_ERR_BAD_ARG;
@@ -2093,10 +2090,6 @@ static mf_status level_set_chunks(mf_level* L, int chunks) {
   if (st != MF_OK) return st;
   int n = 1;
   if (chunks > 1) {
-    if (!L->s2) MF_CHECK_CUDA(cudaStreamCreateWithFlags(&L->s2, cudaStreamNonBlocking));
-    for (int q = 0; q <= chunks; ++q)
-      if (!L->ov_ev[q])
-        MF_CHECK_CUDA(cudaEventCreateWithFlags(&L->ov_ev[q], cudaEventDisableTiming));
     L->ch1 = mf::make_chunks(L->hd1.data(), (int)L->hd1.size(), L->b1, chunks);
     L->ch2 = mf::make_chunks(L->hd2.data(), (int)L->hd2.size(), L->b2, chunks);
     n = (int)std::min(L->ch1.size(), L->ch2.size());
@@ -2107,8 +2100,8 @@ static mf_status level_set_chunks(mf_level* L, int chunks) {
     }
   }
   L->nchunks = std::max(1, n);
-  L->op1 = {L->ch1.data(), (int)L->ch1.size(), L->s2, L->ov_ev};
-  L->op2 = {L->ch2.data(), (int)L->ch2.size(), L->s2, L->ov_ev};
+  L->op1 = {L->ch1.data(), (int)L->ch1.size()};
+  L->op2 = {L->ch2.data(), (int)L->ch2.size()};
   count_launches(L);
   if (L->gsync) cudaGraphExecDestroy(L->gsync);
   if (L->gasync) cudaGraphExecDestroy(L->gasync);

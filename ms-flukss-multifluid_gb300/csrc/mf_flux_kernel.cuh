@@ -310,17 +310,18 @@ __device__ __forceinline__ int helio_side(const DevParams& P, const RunParams& R
   return (f == RP.dlo[DIR]) ? 0 : (f == RP.dhi[DIR] + 1) ? 1 : -1;
 }
 
-// WF: read the limiter inputs from Wf, the FP32 copy of W the prim kernel
-// wrote (R = float), instead of converting W value by value here.
+// The fluxes of face gi of the batch's flat face index of direction DIR
+// (gi >= total: none).  WF: read the limiter inputs from Wf, the FP32 copy of
+// W the prim kernel wrote (R = float), instead of converting W value by
+// value here.
 template <typename R, int DIR, int WF>
-__global__ void __launch_bounds__(kMaxBlock, WF ? 2 : 1)
-    k_flux(const __grid_constant__ DevParams P, const double* __restrict__ W, const float* __restrict__ Wf,
-           R* __restrict__ F, R* __restrict__ Bn, const StageDesc* __restrict__ descs, int ndesc,
-           int first, int total, const RunParams* __restrict__ runs,
-           const StepState* __restrict__ states) {
-  // faces [first, total) of the batch's flat face index (first > 0: a chunk
-  // of the batch's patches)
-  const int gi = first + blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void flux_face(const DevParams& P, const double* __restrict__ W,
+                                          const float* __restrict__ Wf, R* __restrict__ F,
+                                          R* __restrict__ Bn,
+                                          const StageDesc* __restrict__ descs, int ndesc,
+                                          int gi, int total,
+                                          const RunParams* __restrict__ runs,
+                                          const StepState* __restrict__ states) {
   if (gi >= total) return;
   const StageDesc& D = descs[find_desc(descs, ndesc, kRegF + DIR, gi)];
   const int lin = gi - D.g0[kRegF + DIR];
@@ -487,6 +488,18 @@ __global__ void __launch_bounds__(kMaxBlock, WF ? 2 : 1)
       Fo[q * fcs] = (uavg > R(0)) ? l : r;
     }
   }
+}
+
+template <typename R, int DIR, int WF>
+__global__ void __launch_bounds__(kMaxBlock, WF ? 2 : 1)
+    k_flux(const __grid_constant__ DevParams P, const double* __restrict__ W, const float* __restrict__ Wf,
+           R* __restrict__ F, R* __restrict__ Bn, const StageDesc* __restrict__ descs, int ndesc,
+           int first, int total, const RunParams* __restrict__ runs,
+           const StepState* __restrict__ states) {
+  // faces [first, total) of the batch's flat face index (first > 0: a chunk
+  // of the batch's patches)
+  flux_face<R, DIR, WF>(P, W, Wf, F, Bn, descs, ndesc, first + blockIdx.x * blockDim.x + threadIdx.x,
+                        total, runs, states);
 }
 
 // Fluxes of face (i,j,k) (normal DIR) from given face states: the plasma

@@ -310,7 +310,7 @@ __global__ void __launch_bounds__(kFusedThreads, 2)
     update_tail<float, GLM, FLAGS, CE>(P, B, D, RP, ss, i, j, k, base, cs, dt, psi_damp, divB, u,
                                        D.g0[kRegV] + lin, dtc, myidx);
   }
-  if (FLAGS & kStageDt) block_dt_min(dtc, myidx, descs, ndesc, partials);
+  if (FLAGS & kStageDt) block_dt_min(dtc, myidx, descs, ndesc, partials, blockIdx.x);
 }
 
 FusedShape fused_shape(const int tile[3], int sd) {

@@ -239,25 +239,22 @@ struct StageBuffers {
 enum StageFlags : int { kStageAverage = 1, kStageDt = 2 };
 
 // The flux and update launches of a mixed-precision stage cut into chunks of
-// consecutive patches: the FP32 flux kernels of chunk c + 1 run on a second
-// stream while the FP64-bound update of chunk c runs on the stage's stream,
-// so the two kernels share the SMs (no kernel waits on another; the streams
-// are ordered by events).  A chunk's cells start on a multiple of 256.
+// consecutive patches: launch k computes the FP32 fluxes of chunk k and the
+// FP64-bound update of chunk k - 1 in one grid of alternating blocks, so the
+// two share the SMs (mf_fu.cu).  A chunk's cells start on a multiple of 256.
 struct Chunk {
   int v0, v1;        // cells [v0, v1) of the batch's flat cell index
   int f0[3], f1[3];  // faces [f0, f1) per direction
 };
 struct OverlapPlan {
-  const Chunk* c;    // host array
-  int n;             // chunks (>= 2)
-  cudaStream_t s2;   // the flux stream
-  cudaEvent_t* ev;   // n + 1 events: ev[0] the primitive part, ev[1 + c] chunk c's fluxes
+  const Chunk* c;  // host array
+  int n;           // chunks (>= 2): n + 1 launches per stage
 };
 // Chunks of a batch (host descs hd, n of them): about equal cell counts,
 // each starting at a patch whose first cell is a multiple of 256; fewer than
 // nchunks where the patches do not allow more.
 std::vector<Chunk> make_chunks(const StageDesc* hd, int n, const Batch& b, int nchunks);
-// the flux and update launches of a mixed-precision stage in B.overlap's chunks
+// the flux and update launches of a mixed-precision stage in B.overlap's chunks (mf_fu.cu)
 cudaError_t launch_flux_update_overlap(const DevParams& P, const StageBuffers& B,
                                        const Batch& b, int flags, double dt_scale,
                                        StepState* state, DtPartial* partials, int* nblocks_v,

@@ -37,8 +37,11 @@ cudaError_t launch_stage(const DevParams& P, int precision, const StageBuffers& 
     if (e != cudaSuccess) return e;
     if (B.ev) cudaEventRecord(B.ev[ne++], s);
   }
-  if (B.overlap && precision == MF_PREC_MIXED && !B.ev)
-    return launch_flux_update_overlap(P, B, b, flags, dt_scale, state, partials, nblocks_v, s);
+  if (B.overlap && precision == MF_PREC_MIXED) {
+    StageBuffers Bo = B;  // its events continue after the primitive part's
+    Bo.ev = B.ev ? B.ev + ne : nullptr;
+    return launch_flux_update_overlap(P, Bo, b, flags, dt_scale, state, partials, nblocks_v, s);
+  }
   if (B.fused && precision == MF_PREC_MIXED) {
     e = launch_fused(P, B, b, B.fused->tiles, B.fused->ntiles, B.fused->tile, flags, dt_scale,
                      state, partials, s);
@@ -68,34 +71,6 @@ cudaError_t launch_stage(const DevParams& P, int precision, const StageBuffers& 
   if (e != cudaSuccess) return e;
   if (B.ev) cudaEventRecord(B.ev[ne++], s);
   return cudaSuccess;
-}
-
-cudaError_t launch_flux_update_overlap(const DevParams& P, const StageBuffers& B,
-                                       const Batch& b, int flags, double dt_scale,
-                                       StepState* state, DtPartial* partials, int* nblocks_v,
-                                       cudaStream_t s) {
-  // fluxes of chunk c + 1 on the second stream while chunk c updates: the
-  // second stream starts after the work already on s (the primitive part),
-  // each update waits for its chunk's fluxes, and the last wait joins the
-  // streams again
-  const OverlapPlan& O = *B.overlap;
-  cudaError_t e = cudaEventRecord(O.ev[0], s);
-  if (e == cudaSuccess) e = cudaStreamWaitEvent(O.s2, O.ev[0], 0);
-  for (int c = 0; c < O.n && e == cudaSuccess; ++c) {
-    const Chunk& C = O.c[c];
-    for (int d = 0; d < P.sd && e == cudaSuccess; ++d)
-      e = launch_flux_fast<float>(P, d, B.w, B.f[d], B.bn[d], b, state, O.s2, B.wf, C.f0[d],
-                                  C.f1[d]);
-    if (e == cudaSuccess) e = cudaEventRecord(O.ev[1 + c], O.s2);
-  }
-  for (int c = 0; c < O.n && e == cudaSuccess; ++c) {
-    const Chunk& C = O.c[c];
-    e = cudaStreamWaitEvent(s, O.ev[1 + c], 0);
-    if (e == cudaSuccess)
-      e = launch_update_fast<float>(P, B, b, flags, dt_scale, state, partials, nblocks_v, s,
-                                    C.v0, C.v1);
-  }
-  return e;
 }
 
 std::vector<Chunk> make_chunks(const StageDesc* hd, int n, const Batch& b, int nchunks) {

@@ -41,7 +41,7 @@ __global__ void __launch_bounds__(kMaxBlock)
     dtc = runs[D.run].dx / max_wave_speed<IRHON>(P, u);
     myidx = g;
   }
-  block_dt_min(dtc, myidx, descs, ndesc, partials);
+  block_dt_min(dtc, myidx, descs, ndesc, partials, blockIdx.x);
 }
 
 __device__ __forceinline__ bool part_less(const DtPartial& a, const DtPartial& b) {

@@ -59,13 +59,13 @@ __device__ __forceinline__ bool dt_less(double a, int ia, double b, int ib) {
   return (a < b) || (a == b && ia < ib);
 }
 
-// Block minimum of (dt, flattened index) into partials[pbase + blockIdx.x]: warp
+// Block minimum of (dt, flattened index) into partials[slot]: warp
 // shuffles, then one thread over the warps.  The flattened index orders cells
 // by (patch, Fortran-order index), so the minimum is the reference's
 // lexicographic one; it is turned back into (patch, index) once per block.
 __device__ __forceinline__ void block_dt_min(double dtc, int myidx,
                                              const StageDesc* __restrict__ descs, int ndesc,
-                                             DtPartial* __restrict__ partials, int pbase = 0) {
+                                             DtPartial* __restrict__ partials, int slot) {
 #pragma unroll
   for (int off = 16; off > 0; off >>= 1) {
     double od = __shfl_down_sync(0xffffffffu, dtc, off);
@@ -101,7 +101,7 @@ __device__ __forceinline__ void block_dt_min(double dtc, int myidx,
       pr.desc = di;
       pr.idx = bi - descs[di].g0[kRegV];
     }
-    partials[pbase + blockIdx.x] = pr;
+    partials[slot] = pr;
   }
 }
 
@@ -233,16 +233,15 @@ __device__ __forceinline__ void update_tail(const DevParams& P, const StageBuffe
   }
 }
 
-template <typename R, int GLM, int FLAGS, typename CE = double>
-__global__ void __launch_bounds__(kMaxBlock, sizeof(R) == 4 ? 2 : 1)
-    k_update(const __grid_constant__ DevParams P, const __grid_constant__ StageBuffers B, const StageDesc* __restrict__ descs,
-             int ndesc, int first, int total, const RunParams* __restrict__ runs,
-             StepState* __restrict__ states, const double dt_scale,
-             DtPartial* __restrict__ partials) {
-  // cells [first, total) of the batch's flat cell index; first is a multiple
-  // of the block size, so block b writes the dt partial first/blockDim + b of
-  // the launch over the whole batch
-  const int g = first + blockIdx.x * blockDim.x + threadIdx.x;
+// The update of cell g of the batch's flat cell index (g >= total: no cell)
+// by every thread of a block; the block's dt minimum goes to partials[slot].
+template <typename R, int GLM, int FLAGS, typename CE>
+__device__ __forceinline__ void update_cells(const DevParams& P, const StageBuffers& B,
+                                             const StageDesc* __restrict__ descs, int ndesc,
+                                             int g, int total, const RunParams* __restrict__ runs,
+                                             StepState* __restrict__ states,
+                                             const double dt_scale,
+                                             DtPartial* __restrict__ partials, int slot) {
   double dtc = DBL_MAX;
   int myidx = INT_MAX;
   const StageDesc* Dp = nullptr;
@@ -334,7 +333,21 @@ __global__ void __launch_bounds__(kMaxBlock, sizeof(R) == 4 ? 2 : 1)
     update_tail<R, GLM, FLAGS, CE>(P, B, D, RP, ss, i, j, k, base, cs, dt, psi_damp, divB, u, g,
                                    dtc, myidx);
   }
-  if (FLAGS & kStageDt) block_dt_min(dtc, myidx, descs, ndesc, partials, first / blockDim.x);
+  if (FLAGS & kStageDt) block_dt_min(dtc, myidx, descs, ndesc, partials, slot);
+}
+
+template <typename R, int GLM, int FLAGS, typename CE = double>
+__global__ void __launch_bounds__(kMaxBlock, sizeof(R) == 4 ? 2 : 1)
+    k_update(const __grid_constant__ DevParams P, const __grid_constant__ StageBuffers B, const StageDesc* __restrict__ descs,
+             int ndesc, int first, int total, const RunParams* __restrict__ runs,
+             StepState* __restrict__ states, const double dt_scale,
+             DtPartial* __restrict__ partials) {
+  // cells [first, total) of the batch's flat cell index; first is a multiple
+  // of the block size, so block b writes the dt partial first/blockDim + b of
+  // the launch over the whole batch
+  update_cells<R, GLM, FLAGS, CE>(P, B, descs, ndesc, first + blockIdx.x * blockDim.x + threadIdx.x,
+                                  total, runs, states, dt_scale, partials,
+                                  first / (int)blockDim.x + (int)blockIdx.x);
 }
 
 }  // namespace

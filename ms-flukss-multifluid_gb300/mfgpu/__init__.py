@@ -770,7 +770,8 @@ class Level:
         return n.value
 
     KIND_NAMES = {0: "exchange", 1: "prim", 2: "flux", 3: "update", 4: "finalize", 5: "coupling",
-                  6: "postprocess", 7: "constrained transport", 8: "fused"}
+                  6: "postprocess", 7: "constrained transport", 8: "fused",
+                  9: "flux+update"}
 
     def profile_step(self, dt):
         """One step launch by launch with CUDA events between the launches;

@@ -1,8 +1,9 @@
 """Chunked overlap of the split flux and update kernels of mixed-precision
-stages (mf_level_set_overlap): the FP32 flux launches of a chunk of patches
-run on a second stream while the update of the previous chunk runs.  The
-same kernels on the same data in a different launch order: the states, dts
-and argmin cells equal the unchunked ones bit for bit."""
+stages (mf_level_set_overlap): launch k of a stage computes the FP32 fluxes
+of chunk k and the update of chunk k - 1 in one grid of alternating blocks.
+The same per-face and per-cell code on the same data in a different launch
+order: the states, dts and argmin cells equal the unchunked ones bit for
+bit."""
 import numpy as np
 import pytest
 
@@ -70,7 +71,7 @@ def test_overlap_equals_unchunked(gpulib, name, prec, use_async):
         k = lev.overlap()
         assert 2 <= k <= chunks
         per = 1 if "first_order" in name else 2
-        assert lev.launches_per_step() == base_launches + per * (k - 1) * (sd + 1)
+        assert lev.launches_per_step() == base_launches + per * (k - sd)
         assert np.array_equal(ref, got), chunks
         assert rdt == gdt, chunks
     lev.close()
@@ -97,16 +98,21 @@ def test_overlap_arguments(gpulib):
     ctx.close()
 
 
-def test_overlap_profile_step_unchunked(gpulib):
-    """mf_level_profile_step times launch by launch on one stream, so it runs
-    the unchunked launches; the step it takes is the same."""
-    p = mfgpu.helio_params(32, precision=mfgpu.PREC_MIXED)
-    ctx, lev, flat = _level(p, 32, 16, 3, "helio")
+@pytest.mark.parametrize("chunks", [2, 4, 8])
+def test_overlap_profile_step(gpulib, chunks):
+    """mf_level_profile_step times the overlapped launches one by one: chunks
+    + 1 flux-and-update launches per RK2 stage, no separate flux or update
+    launch, as many launches as mf_level_launches_per_step counts."""
+    p = mfgpu.helio_params(48, precision=mfgpu.PREC_MIXED)
+    ctx, lev, flat = _level(p, 48, 16, 3, "helio")
     lev.upload(flat.ctypes.data)
-    lev.set_overlap(4)
+    lev.set_overlap(chunks)
+    k = lev.overlap()
     dt0 = 0.4 * lev.compute_dt()[0]
     prof = lev.profile_step(dt0)
-    kinds = [k for k, _ in prof]
-    assert kinds.count("update") == 2 and kinds.count("flux") == 6
+    kinds = [kd for kd, _ in prof]
+    assert kinds.count("flux+update") == 2 * (k + 1)
+    assert kinds.count("flux") == 0 and kinds.count("update") == 0
+    assert len(prof) == lev.launches_per_step()
     lev.close()
     ctx.close()
