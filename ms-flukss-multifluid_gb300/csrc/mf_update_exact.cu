@@ -104,24 +104,29 @@ __global__ void __launch_bounds__(256)
   }
 }
 
-// One block per copy region, flat over its (component, cell) elements so
-// that small regions (edges, corners) still occupy the block; 32-bit index
-// arithmetic (a region is part of one patch's ghost layers: 2^31 elements
-// would take a patch whose fab alone exceeds HBM) and four loads
-// in flight per thread before their stores.  Sources are valid cells and
-// destinations ghost cells, never the same, so the sources are read through
-// the read-only path.
-template <typename T>
-__global__ void __launch_bounds__(256)
-    k_exchange(T* __restrict__ U, const CopyReg* __restrict__ regs, int nc) {
-  const CopyReg R = regs[blockIdx.x];
-  const int n = R.ext[0] * R.ext[1] * R.ext[2];
-  const long long scs = (long long)R.sfn[0] * R.sfn[1] * R.sfn[2];
-  const long long dcs = (long long)R.dfn[0] * R.dfn[1] * R.dfn[2];
+// 16-byte vector of V elements of T
+template <typename T, int V>
+struct Vec;
+template <> struct Vec<float, 4> { using type = float4; };
+template <> struct Vec<double, 2> { using type = double2; };
+template <typename T> struct Vec<T, 1> { using type = T; };
+
+// The copy of one region's components in vectors of V elements along x (V
+// divides the region's x extent, and every row starts on a multiple of V).
+// Flat over the (component, vector) items so that small regions still occupy
+// the block; 32-bit index arithmetic (a region is part of one patch's ghost
+// layers: 2^31 elements would take a patch whose fab alone exceeds HBM); four
+// loads in flight per thread before their stores.
+template <typename T, int V>
+__device__ __forceinline__ void copy_region(T* __restrict__ U, const CopyReg& R, int nc,
+                                            long long scs, long long dcs) {
+  using VT = typename Vec<T, V>::type;
+  const int rowv = R.ext[0] / V;
+  const int n = rowv * R.ext[1] * R.ext[2];
   const int tot = n * nc;
   const int step = blockDim.x;
   for (int t0 = threadIdx.x; t0 < tot; t0 += 4 * step) {
-    T v[4];
+    VT v[4];
     long long dof[4];
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
@@ -129,21 +134,42 @@ __global__ void __launch_bounds__(256)
       if (t < tot) {
         const int q = t / n;
         const int c = t - q * n;
-        const int a = c % R.ext[0];
-        const int r = c / R.ext[0];
+        const int a = c % rowv;
+        const int r = c / rowv;
         const int b = r % R.ext[1];
         const int e = r / R.ext[1];
-        const long long so = R.src_off + q * scs + (R.s0[0] + a) +
+        const long long so = R.src_off + q * scs + (R.s0[0] + a * V) +
                              (long long)R.sfn[0] * ((R.s0[1] + b) + (long long)R.sfn[1] * (R.s0[2] + e));
-        dof[j] = R.dst_off + q * dcs + (R.d0[0] + a) +
+        dof[j] = R.dst_off + q * dcs + (R.d0[0] + a * V) +
                  (long long)R.dfn[0] * ((R.d0[1] + b) + (long long)R.dfn[1] * (R.d0[2] + e));
-        v[j] = __ldg(U + so);
+        v[j] = __ldg(reinterpret_cast<const VT*>(U + so));
       }
     }
 #pragma unroll
     for (int j = 0; j < 4; ++j)
-      if (t0 + j * step < tot) U[dof[j]] = v[j];
+      if (t0 + j * step < tot) *reinterpret_cast<VT*>(U + dof[j]) = v[j];
   }
+}
+
+// One block per copy region.  Sources are valid cells and destinations ghost
+// cells, never the same, so the sources are read through the read-only path.
+// Rows are copied in 16-byte vectors where the region's x extent, its rows'
+// starts and the fabs' strides are multiples of the vector (the fabs start on
+// 256-byte boundaries), else element by element.
+template <typename T>
+__global__ void __launch_bounds__(256)
+    k_exchange(T* __restrict__ U, const CopyReg* __restrict__ regs, int nc) {
+  constexpr int V = 16 / sizeof(T);
+  const CopyReg R = regs[blockIdx.x];
+  const long long scs = (long long)R.sfn[0] * R.sfn[1] * R.sfn[2];
+  const long long dcs = (long long)R.dfn[0] * R.dfn[1] * R.dfn[2];
+  const bool vec = R.ext[0] % V == 0 && (R.src_off + R.s0[0]) % V == 0 &&
+                   (R.dst_off + R.d0[0]) % V == 0 && R.sfn[0] % V == 0 && R.dfn[0] % V == 0 &&
+                   scs % V == 0 && dcs % V == 0;
+  if (vec)
+    copy_region<T, V>(U, R, nc, scs, dcs);
+  else
+    copy_region<T, 1>(U, R, nc, scs, dcs);
 }
 
 template <typename R>
