@@ -53,6 +53,8 @@ def _args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-mixed", action="store_true")
     ap.add_argument("--no-amr", action="store_true")
+    ap.add_argument("--no-config1", action="store_true")
+    ap.add_argument("--config1-steps", type=int, default=200)
     ap.add_argument("--amr-n0", type=int, default=48)
     ap.add_argument("--amr-steps", type=int, default=3)
     ap.add_argument("--l1-steps", type=int, default=500)
@@ -439,6 +441,8 @@ def run_ours(a):
             levm.close()
             ctxm.close()
 
+    _progress("config 1")
+    c1_res = None if a.no_config1 else run_config1(mfgpu, torch, stream, a)
     _progress("amr")
     amr_res = None if a.no_amr else run_amr(mfgpu, torch, stream, a)
     _progress("serving")
@@ -481,6 +485,8 @@ def run_ours(a):
         line["fp64_fast"] = fast
     for name, res in mixed_forms.items():
         line[name] = res
+    if c1_res is not None:
+        line["config1"] = c1_res
     if amr_res is not None:
         line["amr"] = amr_res
     if serve_res is not None:
@@ -499,6 +505,67 @@ def run_ours(a):
 AMR_TAG_STEPS = 60      # base-grid steps before tagging (t ~ 0.19: shocks have formed)
 AMR_THRESHOLD = 0.3     # undivided relative density gradient
 AMR_SEED = 20240601
+
+
+def run_config1(mfgpu, torch, stream, a):
+    """Config 1: 2D single-fluid ideal MHD on one 256^2 periodic patch over
+    [0,1]^2 with 4 ghost layers (Orszag-Tang, problems/OrszagF.ChF), Roe
+    8-wave, minmod, 8-wave source, RK2, CFL 0.4: the patch as a one-patch
+    level (its periodic images through the level's exchange), autotuned,
+    K steps between CUDA events after 3 warm-up steps, FP64 and mixed.  Beside
+    it the oracle on the same patch for a bounded sample of steps (one patch:
+    one host thread does the work)."""
+    import numpy as np
+    n, steps = 256, max(1, a.config1_steps)
+    boxes = [((0, 0, 0), (n - 1, n - 1, 0))]
+    res = {"config": "Orszag-Tang 256^2 periodic, 1 patch + 4 ghosts, single-fluid ideal MHD, "
+                     "Roe 8-wave, minmod, 8-wave source, RK2, CFL 0.4",
+           "zones_per_step": n * n, "steps": steps}
+    p64 = None
+    for name, prec in (("fp64", mfgpu.PREC_FP64), ("mixed", mfgpu.PREC_MIXED)):
+        p = mfgpu.orszag_params(n, mfgpu.TA_RK2, prec)
+        if prec == mfgpu.PREC_FP64:
+            p64 = p
+        ctx = mfgpu.Context(p)
+        lev = mfgpu.Level(ctx, boxes)
+        flat = np.zeros(lev.ndoubles)
+        flo, fhi = lev.fab_box(0)
+        lev.patch_view(flat, 0)[:] = mfgpu.init_host_fab(p, flo, fhi, "orszag")
+        lev.upload(flat.ctypes.data)
+        lev.autotune(3)
+        lev.upload(flat.ctypes.data)
+        dt0 = lev.compute_dt()[0]
+        lev.seed_dt(CFL * dt0, CFL, stream.cuda_stream)
+        for _ in range(3):
+            lev.step_async(stream.cuda_stream)
+        torch.cuda.synchronize()
+        ms = _time_steps(lev, torch, stream, steps)
+        st = lev.result(stream.cuda_stream)[0]
+        mfgpu.check(st, f"config 1 {name} steps")
+        res[name] = {"value": n * n * steps / (ms * 1e-3), "ms_per_step": ms / steps,
+                     "launches_per_step": lev.launches_per_step()}
+        lev.close()
+        ctx.close()
+    res["mixed"]["speedup_vs_fp64"] = res["mixed"]["value"] / res["fp64"]["value"]
+    res["value"] = res["fp64"]["value"]
+    # the oracle on the same patch: a bounded sample of level steps
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+    ng = pyoracle.num_ghost(p64)
+    flo, fhi = pyoracle.grow(boxes[0][0], boxes[0][1], ng, 2)
+    U = np.zeros(pyoracle.fab_shape(flo, fhi, pyoracle.num_cons(p64)))
+    pyoracle.init_orszag(p64, U, flo, fhi, boxes[0][0], boxes[0][1])
+    dt = CFL * pyoracle.compute_dt(p64, U, flo, fhi, boxes[0][0], boxes[0][1])[1]
+    nst = 20
+    t0 = time.perf_counter()
+    for _ in range(nst):
+        st, ndt, _, _ = pyoracle.level_step(p64, [U], [(flo, fhi)], boxes, dt, 1)
+        assert st == 0, st
+        dt = CFL * ndt
+    el = time.perf_counter() - t0
+    res["cpu_oracle"] = {"value": n * n * nst / el, "unit": UNIT, "cores": 1, "kind": "port",
+                         "sample": f"{nst} steps of the patch, {el:.1f} s"}
+    return res
 
 
 def run_amr(mfgpu, torch, stream, a):
