@@ -143,3 +143,19 @@ def test_flux_form_arguments(gpulib):
     assert all(s in (64, 128, 256) for s in shapes)
     lev.close()
     ctx.close()
+
+
+def test_flux_lines_refuse_long_patches(gpulib):
+    """A patch longer than 254 cells along a direction does not fit one
+    block's shared memory in the line form: MF_ERR_UNSUPPORTED, and the level
+    keeps stepping per face."""
+    p = mfgpu.orszag_params(512, mfgpu.TA_RK2, mfgpu.PREC_FP64)
+    ctx = mfgpu.Context(p)
+    lev = mfgpu.Level(ctx, [((0, 0, 0), (511, 63, 0))] + [((0, y, 0), (511, y + 63, 0))
+                                                         for y in range(64, 512, 64)])
+    with pytest.raises(mfgpu.MfError) as ei:
+        lev.set_flux_form(mfgpu.FLUX_LINES)
+    assert ei.value.code == mfgpu.MF_ERR_UNSUPPORTED
+    assert lev.flux_form() == mfgpu.FLUX_FACES
+    lev.close()
+    ctx.close()
